@@ -1,0 +1,321 @@
+"""Benchmark: node-fixpoints/s of linear-constraint bound propagation on one GB300.
+
+Workload (the batched branch-and-bound node case): one shared matrix of 200,000 rows x 400,000 columns
+(row lengths U{5..40}, |a| log-uniform in [1e-2, 1e2], 60 % integer columns), 4,096 node subproblems that fix
+1..64 integer columns each to random values inside the root fixpoint bounds, every node propagated to its
+own fixpoint.  One step = one batch of 4,096 nodes.
+
+  value      node-fixpoints/s of the batched path, inputs resident in HBM (gbp_propagate_nodes_device)
+  e2e        the same through the host-pointer C ABI (gbp_propagate_nodes): node changes and base bounds
+             copied host->device and results device->host inside the timed region
+  plain      the plain one-node-per-launch-sequence path (gbp_propagate with seeds), on a sample of nodes
+  cpu_baseline / --impl reference   the C restatement of SCIP's propagation (oracle) on the host cores
+
+Timing: CUDA events on the library's stream around each step, W untimed warm-up steps, L2 flushed
+(256 MiB write) between timed steps, nvidia-smi clocks sampled during the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+NNODES = 4096
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(rows, nnz, changes, avg_col_len):
+    """Bytes one propagation must move: per processed nonzero 8 (value) + 4 (column) + 16 (lb, ub gather),
+    per processed row 40 (row pointer, lhs, rhs, activity outputs), per accepted change 16 (bound write)
+    plus 8 per entry of the changed column's CSC list (frontier expansion)."""
+    return 28.0 * nnz + 40.0 * rows + 16.0 * changes + 8.0 * changes * avg_col_len
+
+
+def build_workload(seed=2, nnodes=NNODES, m=200_000, n=400_000):
+    from scip_gb300 import instances
+
+    inst = instances.node_mip(seed=seed, m=m, n=n)
+    return inst
+
+
+def cpu_arm(inst, rlb, rub, nodes, par, nthreads, budget_s=15.0):
+    """Oracle over a bounded sample of nodes; returns (node-fixpoints/s, sample description)."""
+    import oracle as orc
+    from scip_gb300.instances import NodeBatch
+
+    o = orc.Oracle(inst)
+    take = 256
+    while True:
+        k = min(take, nodes.nnodes)
+        sub = NodeBatch(nodes.ptr[:k + 1].copy(), nodes.col[:nodes.ptr[k]], nodes.lb[:nodes.ptr[k]],
+                        nodes.ub[:nodes.ptr[k]])
+        t0 = time.perf_counter()
+        o.propagate_nodes(rlb, rub, sub, par, cap=1, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or k == nodes.nnodes:
+            return k / dt, f"{k} of {nodes.nnodes} nodes, {nthreads} threads, {dt:.2f} s"
+        take *= 4
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nodes", type=int, default=NNODES)
+    ap.add_argument("--maxeasy", type=float, default=0.0)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from scip_gb300 import instances
+
+    config = {"workload": "batched B&B nodes: 200,000 x 400,000 rows/cols, ~4.5M nnz, 4,096 nodes fixing 1-64 "
+                          "integer columns each, every node to fixpoint",
+              "rows": 200000, "cols": 400000, "nodes_per_step": args.nodes, "rule": "residual (maxeasyactivitydelta="
+              f"{args.maxeasy:g})", "l2": "flushed between timed steps (256 MiB write)",
+              "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle as orc
+
+        orc.build()
+        inst = build_workload()
+        o = orc.Oracle(inst)
+        par = orc.params(args.maxeasy)
+        rlb, rub, _ = o.propagate(inst.lb, inst.ub, par)
+        nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3)
+        threads = os.cpu_count() or 1
+        for _ in range(args.warmup):
+            cpu_arm(inst, rlb, rub, nodes, par, threads, budget_s=4.0)
+        rates = []
+        sample = ""
+        for _ in range(args.steps):
+            r, sample = cpu_arm(inst, rlb, rub, nodes, par, threads, budget_s=8.0)
+            rates.append(r)
+        v = float(np.mean(rates))
+        print(json.dumps({"impl": "reference", "metric": "node-fixpoints/sec", "value": v, "unit": "node-fixpoints/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * args.nodes / v, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                          "config": config,
+                          "cpu_baseline": {"value": v, "unit": "node-fixpoints/s", "cores": threads, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": v, "unit": "node-fixpoints/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    from scip_gb300 import gbp
+    from scip_gb300.build import build_libgbp
+
+    build_libgbp()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+
+    inst = build_workload()
+    prop = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy))
+    prop.upload(inst)
+    rlb, rub, rcut, rres = prop.propagate(inst.lb, inst.ub)
+    nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3 + rank)
+    N = nodes.nnodes
+    avg_col_len = inst.nnz / inst.n
+
+    stream = torch.cuda.ExternalStream(prop.stream())
+    d = torch.device("cuda", dev)
+    t_lb = torch.from_numpy(rlb).to(d)
+    t_ub = torch.from_numpy(rub).to(d)
+    t_ptr = torch.from_numpy(nodes.ptr).to(d)
+    t_col = torch.from_numpy(nodes.col).to(d)
+    t_nlb = torch.from_numpy(nodes.lb).to(d)
+    t_nub = torch.from_numpy(nodes.ub).to(d)
+    out_cap = 256 * N
+    out = {"cutoff": torch.zeros(N, dtype=torch.int8, device=d), "rounds": torch.zeros(N, dtype=torch.int32, device=d),
+           "off": torch.zeros(N, dtype=torch.int64, device=d), "n": torch.zeros(N, dtype=torch.int32, device=d),
+           "col": torch.zeros(out_cap, dtype=torch.int32, device=d), "lb": torch.zeros(out_cap, dtype=torch.float64, device=d),
+           "ub": torch.zeros(out_cap, dtype=torch.float64, device=d)}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=d)
+    torch.cuda.synchronize()
+
+    def step():
+        return prop.propagate_nodes_device(t_lb, t_ub, N, t_ptr, t_col, t_nlb, t_nub, out, out_cap)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    evs = []
+    stats = []
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        res = step()
+        e1.record(stream)
+        evs.append((e0, e1))
+        stats.append(res.asdict())
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=d)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    clk = clocks.stop()
+    value = world * N / (ms / 1e3)
+    kern_ms = float(np.mean([s["kernel_ms"] for s in stats]))
+    rows = stats[-1]["rows"]
+    nnz = stats[-1]["nnz"]
+    changes = stats[-1]["changes"]
+    algo = algorithmic_bytes(rows, nnz, changes, avg_col_len)
+    peak, peak_kind = measured_peak()
+    achieved = algo / (ms / 1e3) / 1e9
+    cutoffs = stats[-1]["cutoff"]
+
+    # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
+    h_lb, h_ub = pin(rlb), pin(rub)
+    hn = instances.NodeBatch(pin(nodes.ptr), pin(nodes.col), pin(nodes.lb), pin(nodes.ub))
+    e2e_ms = []
+    r_host = None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r_host = prop.propagate_nodes(h_lb, h_ub, hn, out_cap=out_cap)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append(1e3 * (t1 - t0))
+    e2e_v = world * N / (np.mean(e2e_ms) / 1e3)
+    h2d = 16 * inst.n + 8 * (N + 1) + 20 * len(nodes.col)
+    used = int(r_host.n[r_host.n > 0].sum())
+    d2h = N * (1 + 4 + 8 + 4) + 20 * used
+
+    # plain path: the same nodes one at a time through the seeded single-problem call
+    plain_nodes = min(128, N)
+    t0 = time.perf_counter()
+    for k in range(plain_nodes):
+        lb, ub = rlb.copy(), rub.copy()
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        cols = nodes.col[sl]
+        olb, oub = lb[cols].copy(), ub[cols].copy()
+        lb[cols] = np.maximum(lb[cols], nodes.lb[sl])
+        ub[cols] = np.minimum(ub[cols], nodes.ub[sl])
+        prop.propagate(lb, ub, seed=(cols, olb, oub))
+    plain_v = plain_nodes / (time.perf_counter() - t0)
+
+    line = {"metric": "node-fixpoints/sec", "value": value, "unit": "node-fixpoints/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": config,
+            "e2e": {"value": e2e_v, "unit": "node-fixpoints/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_step": algo, "kernel": "k_nodes"},
+            "clocks": clk,
+            "nnz_per_s": nnz / (ms / 1e3), "kernel_ms": kern_ms, "wall_s": wall,
+            "nodes_cut_off": int(cutoffs), "max_rounds": int(stats[-1]["rounds"]),
+            "plain": {"value": plain_v, "unit": "node-fixpoints/s", "sample_nodes": plain_nodes,
+                      "root_ms": rres.kernel_ms, "root_rounds": rres.rounds},
+            }
+    if rank == 0:
+        import oracle as orc
+
+        orc.build()
+        par = orc.params(args.maxeasy)
+        cpu_v, sample = cpu_arm(inst, rlb, rub, nodes, par, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": sample}
+        print(json.dumps(line))
+    prop.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+/* gbp.h -- C ABI of the GB300 linear-constraint bound propagator (libgbp.so).
+ *
+ * The library replaces the propagation work of SCIP's linear constraint handler
+ *   consPropLinear -> propagateCons -> tightenBounds -> tightenVarBounds / tightenVarBoundsEasy
+ *   (src/scip/cons_linear.c:16126-16195, 7621-7758, 6980-7154, 6700-6974, 5380-5653)
+ * for a propagator plugin registered through SCIPincludePropBasic (src/scip/scip_prop.c:118-140) whose
+ * SCIP_DECL_PROPEXEC callback (src/scip/type_prop.h:217) hands the transformed problem's rows and local
+ * bounds to these entry points and writes the returned bounds back with SCIPinferVarLbProp/UbProp
+ * (src/scip/scip_var.c:7589/7705) or reports SCIP_CUTOFF.  scip_gb300/plugin/prop_gpulinear.c is that plugin.
+ *
+ * Conventions: plain C types only; sizes are int64_t; every function returns GBP_OK (0) or a negative
+ * GBP_ERR_* code (no exceptions cross the boundary; gbp_error_string() names the code and
+ * gbp_last_error() gives the context's last message).  Host pointers are ordinary CPU memory unless the
+ * function name ends in _device, in which case every array argument is a device pointer on the context's
+ * GPU.  Infinite sides and bounds are +-params.infinity (1e20 by default), as in SCIP.
+ *
+ * Rows are stored once on the device in CSR and CSC form; bound vectors, node bound changes and results
+ * are the only per-call traffic.  One context = one GPU = one CUDA stream; calls on a context must not
+ * overlap from several host threads.
+ */
+#ifndef GBP_H
+#define GBP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBP_OK              0
+#define GBP_ERR_INVALID    -1   /* bad argument (sizes, indices, null pointers, problem not uploaded) */
+#define GBP_ERR_CUDA       -2   /* a CUDA runtime call failed (message in gbp_last_error) */
+#define GBP_ERR_NOMEM      -3   /* device or host allocation failed */
+#define GBP_ERR_NODEVICE   -4   /* no CUDA device, or the device is not an sm_103 GPU */
+#define GBP_ERR_LIMIT      -5   /* the round limit was reached before the fixpoint (results are valid bounds) */
+#define GBP_ERR_OVERFLOW   -6   /* an output list was too small (out_n reports -1 for that node) */
+#define GBP_ERR_STATE      -7   /* the device reported an inconsistent state (a bounded loop gave up) */
+
+typedef struct gbp_ctx gbp_ctx;
+
+/* numerics of SCIP's set.c / def.h and the two parameters of cons_linear propagation that matter here */
+typedef struct
+{
+   double infinity;             /* numerics/infinity (1e20) */
+   double epsilon;              /* numerics/epsilon (1e-9) */
+   double sumepsilon;           /* numerics/sumepsilon (1e-6) */
+   double feastol;              /* numerics/feastol (1e-6) */
+   double hugeval;              /* numerics/hugeval (1e15) */
+   double boundstreps;          /* numerics/boundstreps (0.05), minimal relative bound improvement */
+   double recompfac;            /* numerics/recompfac (1e6) */
+   double maxeasyactivitydelta; /* constraints/linear/maxeasyactivitydelta; SCIP's default is 1e6, 0 selects the
+                                 * residual rule (cons_linear.c:6700) for every row */
+   int32_t maxrounds;           /* propagation round cap per problem or node; <= 0 means 1,000,000 */
+   int32_t flags;               /* reserved, 0 */
+} gbp_params;
+
+typedef struct
+{
+   int32_t cutoff;      /* number of problems/nodes found infeasible */
+   int32_t rounds;      /* largest number of rounds any problem/node took */
+   int32_t status;      /* 0 fixpoint, 1 cutoff (single problem), 2 round limit */
+   int32_t launches;    /* kernels launched by the call */
+   int64_t rows;        /* frontier rows processed, summed over rounds and nodes */
+   int64_t nnz;         /* nonzeros of those rows */
+   int64_t candidates;  /* candidate bounds emitted */
+   int64_t changes;     /* accepted bound changes (lower and upper counted separately) */
+   double kernel_ms;    /* device time of the propagation kernels (CUDA events on the context's stream) */
+} gbp_result;
+
+/* ---------------------------------------------------------------- context */
+int gbp_version(void);
+const char* gbp_error_string(int code);
+const char* gbp_last_error(const gbp_ctx* ctx);
+
+/* device: CUDA ordinal; stream: a cudaStream_t to run on, or NULL for a stream the context creates */
+int gbp_create(gbp_ctx** ctx, int device, void* stream);
+int gbp_destroy(gbp_ctx* ctx);
+void gbp_default_params(gbp_params* params);
+int gbp_set_params(gbp_ctx* ctx, const gbp_params* params);
+int gbp_get_stream(const gbp_ctx* ctx, void** stream);
+
+/* ---------------------------------------------------------------- problem (SCIP_ConsData of all linear rows)
+ * Replaces the per-row vars/vals/lhs/rhs that cons_linear keeps in struct SCIP_ConsData (cons_linear.c:187-266)
+ * and the column-major view of SCIPmatrixCreate (src/scip/matrix.c:703); the CSC copy is built here.
+ * rowptr[m+1] (int64), colidx[nnz] (0..n-1, no repeats inside a row), vals[nnz] (nonzero), lhs/rhs[m],
+ * isint[n] (nonzero = integral column, SCIPvarIsIntegral).  m must be below 2^30. */
+int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+   const double* vals, const double* lhs, const double* rhs, const int8_t* isint);
+
+/* ---------------------------------------------------------------- plain path: one problem per call
+ * Propagates lb/ub (length n, in place) to the fixpoint.  The first frontier is every row (nseed < 0), or
+ * the rows that the listed column changes make relevant: seedcols[k] moved from [oldlb[k], oldub[k]] to its
+ * current bounds (SCIP marks exactly those rows through its bound-change events, cons_linear.c:17162-17255).
+ * *cutoff is set to 1 if the problem is infeasible (SCIP_CUTOFF). */
+int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols,
+   const double* oldlb, const double* oldub, int32_t* cutoff, gbp_result* res);
+int gbp_propagate_device(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols,
+   const double* oldlb, const double* oldub, int32_t* cutoff, gbp_result* res);
+
+/* row activities from scratch (min/max activity as double-double plus the eight infinity/huge counters of
+ * struct SCIP_ConsData): act[4*i] = minhi, minlo, maxhi, maxlo; cnt[8*i] = minposinf, minneginf,
+ * minposhuge, minneghuge, maxposinf, maxneginf, maxposhuge, maxneghuge; for all m rows. */
+int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double* act, int32_t* cnt);
+
+/* ---------------------------------------------------------------- batched path: branch-and-bound nodes
+ * nnodes nodes share the uploaded rows and the base bounds baselb/baseub (length n); node k applies the
+ * bound changes chg_col/chg_lb/chg_ub[ptr[k] .. ptr[k+1]) (tightenings, as SCIPchgVarLb/UbProbing; a column
+ * appears at most once per node) and propagates to its own fixpoint -- the per-node work SCIP does in
+ * SCIPpropagateProbing (src/scip/scip_probing.c:581) or at each branch-and-bound node.  All nodes run in one
+ * persistent launch.  Per node: out_cutoff[k], out_rounds[k] and the columns whose final bounds differ from
+ * the base: out_n[k] entries at out_col/out_lb/out_ub[out_off[k] ..].  Node results are packed in completion
+ * order into arrays of out_cap entries; a node that does not fit gets out_n[k] = -1 and the call returns
+ * GBP_ERR_OVERFLOW. */
+int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
+   const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+   int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int64_t out_cap, gbp_result* res);
+int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
+   const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+   int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int64_t out_cap, gbp_result* res);
+
+/* launch shape of the batched kernel: CTAs per SM (0 = occupancy maximum) -- what the autotuner sets */
+int gbp_set_batch_shape(gbp_ctx* ctx, int32_t ctas_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

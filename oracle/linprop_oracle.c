@@ -1,0 +1,1107 @@
+/* Test infrastructure only: CPU restatement of SCIP 11's cons_linear activity-based bound propagation.
+ * The tests, smoke() and the CPU-baseline leg of bench.py use it as the checker of the CUDA path; the
+ * product library never links it.  Round semantics are described in linprop_oracle.h.
+ *
+ * Every rule below restates the SCIP function cited beside it (paths relative to the SCIP source tree).
+ */
+#define _POSIX_C_SOURCE 200809L
+#include "linprop_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ numerics (src/scip/def.h:192-204,
+ * set.c:6824-6845, 7025-7050, 7425-7460, 7705-7753, 8032-8046, misc.c:11162-11176) */
+typedef struct
+{
+   double inf, eps, sumeps, feastol, huge, bstreps, recomp, maxeasy;
+} Num;
+
+static int isInf(const Num* s, double x) { return x >= s->inf; }                    /* SCIPsetIsInfinity */
+static int isHuge(const Num* s, double x) { return x >= s->huge; }                  /* SCIPsetIsHugeValue */
+static int lt(const Num* s, double a, double b) { return a - b < -s->eps; }         /* EPSLT */
+static int le(const Num* s, double a, double b) { return a - b <= s->eps; }         /* EPSLE */
+static int gt(const Num* s, double a, double b) { return a - b > s->eps; }          /* EPSGT */
+static int ge(const Num* s, double a, double b) { return a - b >= -s->eps; }        /* EPSGE */
+static int eq(const Num* s, double a, double b) { return fabs(a - b) <= s->eps; }   /* EPSEQ */
+static int sumGt(const Num* s, double a, double b) { return a - b > s->sumeps; }    /* SCIPsetIsSumGT */
+static int positive(const Num* s, double a) { return a > s->eps; }                  /* SCIPsetIsPositive */
+static int feasZero(const Num* s, double a) { return fabs(a) <= s->feastol; }       /* SCIPsetIsFeasZero */
+
+static double relDiff(double a, double b)                                           /* SCIPrelDiff */
+{
+   double q = fabs(a);
+   if( fabs(b) > q )
+      q = fabs(b);
+   if( 1.0 > q )
+      q = 1.0;
+   return (a - b) / q;
+}
+static int feasLt(const Num* s, double a, double b) { return relDiff(a, b) < -s->feastol; }
+static int feasGt(const Num* s, double a, double b) { return relDiff(a, b) > s->feastol; }
+static double feasFloor(const Num* s, double x) { return floor(x + s->feastol); }  /* EPSFLOOR */
+static double feasCeil(const Num* s, double x) { return ceil(x - s->feastol); }    /* EPSCEIL */
+
+static double dmax(double a, double b) { return a > b ? a : b; }
+static double dmin(double a, double b) { return a < b ? a : b; }
+
+/* SCIPsetIsLbBetter / SCIPsetIsUbBetter, set.c:7711-7753 */
+static int lbBetter(const Num* s, double newlb, double oldlb, double oldub)
+{
+   if( oldlb < 0.0 && newlb >= 0.0 )
+      return 1;
+   return newlb - oldlb > s->bstreps * dmax(dmin(oldub - oldlb, fabs(oldlb)), 1e-3);
+}
+static int ubBetter(const Num* s, double newub, double oldlb, double oldub)
+{
+   if( oldub > 0.0 && newub <= 0.0 )
+      return 1;
+   return newub - oldub < -(s->bstreps * dmax(dmin(oldub - oldlb, fabs(oldub)), 1e-3));
+}
+
+/* SCIPsetIsUpdateUnreliable, set.c:8032-8046 */
+static int updateUnreliable(const Num* s, double newvalue, double oldvalue)
+{
+   double quot = fabs(oldvalue) / dmax(fabs(newvalue), s->eps);
+   return quot >= s->recomp;
+}
+
+/* adjustedLb / adjustedUb, var.c:1957-2020 */
+static double adjLb(const Num* s, int isint, double lb)
+{
+   if( lb < 0.0 && isInf(s, -lb) )
+      return -s->inf;
+   if( lb > 0.0 && isInf(s, lb) )
+      return s->inf;
+   if( isint )
+      return feasCeil(s, lb);
+   if( lb > 0.0 && lb < s->eps )
+      return 0.0;
+   return lb;
+}
+static double adjUb(const Num* s, int isint, double ub)
+{
+   if( ub > 0.0 && isInf(s, ub) )
+      return s->inf;
+   if( ub < 0.0 && isInf(s, -ub) )
+      return -s->inf;
+   if( isint )
+      return feasFloor(s, ub);
+   if( ub < 0.0 && ub > -s->eps )
+      return 0.0;
+   return ub;
+}
+
+/* SCIPdbldblSum21 (dbldblarith.h:154-190): (hi,lo) + b, TwoSum on the high part, low parts added */
+static void sum21(double* hi, double* lo, double b)
+{
+   double s = *hi + b;
+   double bb = s - *hi;
+   double err = (*hi - (s - bb)) + (b - bb);
+   *lo = err + *lo;
+   *hi = s;
+}
+
+static void numFrom(const lpo_params* p, Num* s)
+{
+   s->inf = p->infinity;
+   s->eps = p->epsilon;
+   s->sumeps = p->sumepsilon;
+   s->feastol = p->feastol;
+   s->huge = p->hugeval;
+   s->bstreps = p->boundstreps;
+   s->recomp = p->recompfac;
+   s->maxeasy = p->maxeasyactivitydelta;
+}
+
+void lpo_default_params(lpo_params* p)
+{
+   p->infinity = 1e20;
+   p->epsilon = 1e-9;
+   p->sumepsilon = 1e-6;
+   p->feastol = 1e-6;
+   p->hugeval = 1e15;
+   p->boundstreps = 0.05;
+   p->recompfac = 1e6;
+   p->maxeasyactivitydelta = 0.0;
+   p->maxrounds = 0;
+   p->reserved = 0;
+}
+
+/* ------------------------------------------------------------------ row activity */
+typedef struct
+{
+   double minhi, minlo, maxhi, maxlo;
+   int minposinf, minneginf, minposhuge, minneghuge;
+   int maxposinf, maxneginf, maxposhuge, maxneghuge;
+} Act;
+
+/* one contribution val*bound to an activity: infinite bounds and huge products are counted, the rest
+ * summed (consdataUpdateActivities with oldbound 0, cons_linear.c:1772-1945, as used by
+ * consdataCalcActivities/consdataUpdateAddCoef, cons_linear.c:2092-2339) */
+static void addContribution(const Num* s, double val, double bound, double* hi, double* lo, int* posinf,
+   int* neginf, int* poshuge, int* neghuge)
+{
+   if( isInf(s, fabs(bound)) )
+   {
+      if( (val > 0.0) == (bound > 0.0) )
+         ++(*posinf);
+      else
+         ++(*neginf);
+   }
+   else
+   {
+      double c = val * bound;
+      if( isHuge(s, fabs(c)) )
+      {
+         if( c > 0.0 )
+            ++(*poshuge);
+         else
+            ++(*neghuge);
+      }
+      else if( c != 0.0 )
+         sum21(hi, lo, c);
+   }
+}
+
+static void addTerm(const Num* s, Act* a, double v, double l, double u)
+{
+   addContribution(s, v, v > 0.0 ? l : u, &a->minhi, &a->minlo, &a->minposinf, &a->minneginf, &a->minposhuge,
+      &a->minneghuge);
+   addContribution(s, v, v > 0.0 ? u : l, &a->maxhi, &a->maxlo, &a->maxposinf, &a->maxneginf, &a->maxposhuge,
+      &a->maxneghuge);
+}
+
+/* partial activity b merged into a: b's high word through the compensated sum, low words added */
+static void actMerge(Act* a, const Act* b)
+{
+   sum21(&a->minhi, &a->minlo, b->minhi);
+   a->minlo = a->minlo + b->minlo;
+   sum21(&a->maxhi, &a->maxlo, b->maxhi);
+   a->maxlo = a->maxlo + b->maxlo;
+   a->minposinf += b->minposinf; a->minneginf += b->minneginf;
+   a->minposhuge += b->minposhuge; a->minneghuge += b->minneghuge;
+   a->maxposinf += b->maxposinf; a->maxneginf += b->maxneginf;
+   a->maxposhuge += b->maxposhuge; a->maxneghuge += b->maxneghuge;
+}
+
+/* Activities are summed in a fixed order that does not depend on how the GPU schedules the row: rows of
+ * up to LONGROW entries in row order (consdataCalcActivities order), longer rows as 32 interleaved partial
+ * sums (entry p goes to partial (p - rowstart) mod 32, each summed in row order) merged pairwise
+ * (partial k absorbs partial k + 16, then k + 8, 4, 2, 1). */
+#define LONGROW 64
+static void rowActivity(const Num* s, const lpo_problem* P, const double* lb, const double* ub, int64_t i, Act* a)
+{
+   int64_t p;
+   int64_t p0 = P->rowptr[i];
+   int64_t p1 = P->rowptr[i + 1];
+   memset(a, 0, sizeof(*a));
+   if( p1 - p0 <= LONGROW )
+   {
+      for( p = p0; p < p1; ++p )
+      {
+         int32_t j = P->colidx[p];
+         addTerm(s, a, P->vals[p], lb[j], ub[j]);
+      }
+   }
+   else
+   {
+      Act part[32];
+      int k;
+      int off;
+      memset(part, 0, sizeof(part));
+      for( k = 0; k < 32; ++k )
+      {
+         for( p = p0 + k; p < p1; p += 32 )
+         {
+            int32_t j = P->colidx[p];
+            addTerm(s, &part[k], P->vals[p], lb[j], ub[j]);
+         }
+      }
+      for( off = 16; off >= 1; off /= 2 )
+         for( k = 0; k < off; ++k )
+            actMerge(&part[k], &part[k + off]);
+      *a = part[0];
+   }
+}
+
+/* getMinActivity, cons_linear.c:2345-2436 */
+static void getMinAct(const Num* s, const Act* a, int posinf, int neginf, int poshuge, int neghuge, double delta,
+   int goodrelax, double* val, int* tight, int* settoinf)
+{
+   if( neginf > 0 )
+   {
+      *val = -s->inf; *settoinf = 1; *tight = (posinf == 0);
+   }
+   else if( posinf > 0 )
+   {
+      *val = s->inf; *settoinf = 1; *tight = 1;
+   }
+   else if( neghuge > 0 || (poshuge > 0 && !goodrelax) )
+   {
+      *val = -s->inf; *settoinf = 1; *tight = 0;
+   }
+   else
+   {
+      double hi = a->minhi;
+      double lo = a->minlo;
+      sum21(&hi, &lo, -delta);
+      if( poshuge > 0 )
+      {
+         sum21(&hi, &lo, poshuge * s->huge);
+         *tight = 0;
+      }
+      else
+         *tight = 1;
+      *val = hi + lo;
+      *settoinf = 0;
+   }
+}
+
+/* getMaxActivity, cons_linear.c:2441-2529 */
+static void getMaxAct(const Num* s, const Act* a, int posinf, int neginf, int poshuge, int neghuge, double delta,
+   int goodrelax, double* val, int* tight, int* settoinf)
+{
+   if( posinf > 0 )
+   {
+      *val = s->inf; *settoinf = 1; *tight = (neginf == 0);
+   }
+   else if( neginf > 0 )
+   {
+      *val = -s->inf; *settoinf = 1; *tight = 1;
+   }
+   else if( poshuge > 0 || (neghuge > 0 && !goodrelax) )
+   {
+      *val = s->inf; *settoinf = 1; *tight = 0;
+   }
+   else
+   {
+      double hi = a->maxhi;
+      double lo = a->maxlo;
+      sum21(&hi, &lo, -delta);
+      if( neghuge > 0 )
+      {
+         sum21(&hi, &lo, -neghuge * s->huge);
+         *tight = 0;
+      }
+      else
+         *tight = 1;
+      *val = hi + lo;
+      *settoinf = 0;
+   }
+}
+
+/* consdataGetActivityResiduals, cons_linear.c:2661-2806 (goodrelax FALSE as in tightenVarBounds) */
+static void residuals(const Num* s, const Act* a, double val, double lb, double ub, double* minres, double* maxres,
+   int* mintight, int* maxtight, int* mininf, int* maxinf)
+{
+   double minb, maxb, absval;
+   if( val > 0.0 )
+   {
+      minb = lb; maxb = ub; absval = val;
+   }
+   else
+   {
+      minb = -ub; maxb = -lb; absval = -val;
+   }
+   if( isInf(s, minb) )
+      getMinAct(s, a, a->minposinf - 1, a->minneginf, a->minposhuge, a->minneghuge, 0.0, 0, minres, mintight, mininf);
+   else if( isInf(s, -minb) )
+      getMinAct(s, a, a->minposinf, a->minneginf - 1, a->minposhuge, a->minneghuge, 0.0, 0, minres, mintight, mininf);
+   else if( isHuge(s, minb * absval) )
+      getMinAct(s, a, a->minposinf, a->minneginf, a->minposhuge - 1, a->minneghuge, 0.0, 0, minres, mintight, mininf);
+   else if( isHuge(s, -minb * absval) )
+      getMinAct(s, a, a->minposinf, a->minneginf, a->minposhuge, a->minneghuge - 1, 0.0, 0, minres, mintight, mininf);
+   else
+      getMinAct(s, a, a->minposinf, a->minneginf, a->minposhuge, a->minneghuge, absval * minb, 0, minres, mintight, mininf);
+
+   if( isInf(s, -maxb) )
+      getMaxAct(s, a, a->maxposinf, a->maxneginf - 1, a->maxposhuge, a->maxneghuge, 0.0, 0, maxres, maxtight, maxinf);
+   else if( isInf(s, maxb) )
+      getMaxAct(s, a, a->maxposinf - 1, a->maxneginf, a->maxposhuge, a->maxneghuge, 0.0, 0, maxres, maxtight, maxinf);
+   else if( isHuge(s, absval * maxb) )
+      getMaxAct(s, a, a->maxposinf, a->maxneginf, a->maxposhuge - 1, a->maxneghuge, 0.0, 0, maxres, maxtight, maxinf);
+   else if( isHuge(s, -absval * maxb) )
+      getMaxAct(s, a, a->maxposinf, a->maxneginf, a->maxposhuge, a->maxneghuge - 1, 0.0, 0, maxres, maxtight, maxinf);
+   else
+      getMaxAct(s, a, a->maxposinf, a->maxneginf, a->maxposhuge, a->maxneghuge, absval * maxb, 0, maxres, maxtight, maxinf);
+}
+
+/* consdataGetReliableResidualActivity, cons_linear.c:2580-2657: plain double sum in row order */
+static double reliableResidual(const lpo_problem* P, const double* lb, const double* ub, int64_t i, int64_t skip,
+   int ismin)
+{
+   double r = 0.0;
+   int64_t p;
+   for( p = P->rowptr[i]; p < P->rowptr[i + 1]; ++p )
+   {
+      double v = P->vals[p];
+      int32_t j = P->colidx[p];
+      if( p == skip )
+         continue;
+      if( v > 0.0 )
+         r += ismin ? v * lb[j] : v * ub[j];
+      else
+         r += ismin ? v * ub[j] : v * lb[j];
+   }
+   return r;
+}
+
+void lpo_row_activities(const lpo_problem* prob, const lpo_params* par, const double* lb, const double* ub,
+   const int32_t* rows, int64_t nrows, double* act, int32_t* cnt)
+{
+   Num s;
+   int64_t k;
+   numFrom(par, &s);
+   if( rows == NULL )
+      nrows = prob->m;
+   for( k = 0; k < nrows; ++k )
+   {
+      Act a;
+      rowActivity(&s, prob, lb, ub, rows == NULL ? k : rows[k], &a);
+      act[4 * k + 0] = a.minhi;
+      act[4 * k + 1] = a.minlo;
+      act[4 * k + 2] = a.maxhi;
+      act[4 * k + 3] = a.maxlo;
+      cnt[8 * k + 0] = a.minposinf;
+      cnt[8 * k + 1] = a.minneginf;
+      cnt[8 * k + 2] = a.minposhuge;
+      cnt[8 * k + 3] = a.minneghuge;
+      cnt[8 * k + 4] = a.maxposinf;
+      cnt[8 * k + 5] = a.maxneginf;
+      cnt[8 * k + 6] = a.maxposhuge;
+      cnt[8 * k + 7] = a.maxneghuge;
+   }
+}
+
+/* ------------------------------------------------------------------ propagation work space */
+typedef struct
+{
+   const lpo_problem* P;
+   Num s;
+   int32_t maxrounds;
+   /* candidates per column: best non-forced / forced upper and lower bound */
+   double* cub;
+   double* clb;
+   double* cubf;
+   double* clbf;
+   uint8_t* cflag;      /* bit0 ub, bit1 ubf, bit2 lb, bit3 lbf */
+   int32_t* touched;
+   int64_t ntouched;
+   int32_t* front;      /* current frontier */
+   int32_t* next;       /* next frontier */
+   int64_t nfront;
+   int64_t nnext;
+   int32_t* rowstamp;
+   int32_t stamp;
+   double* oldlb;       /* per changed column: bounds at round start */
+   double* oldub;
+   int32_t* chg;
+   int64_t nchg;
+   /* node bookkeeping: columns modified since the base bounds */
+   uint8_t* dirty;
+   int32_t* dirtylist;
+   int64_t ndirty;
+   double* savelb;
+   double* saveub;
+} Work;
+
+static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
+{
+   int64_t n = P->n;
+   int64_t m = P->m;
+   memset(w, 0, sizeof(*w));
+   w->P = P;
+   numFrom(par, &w->s);
+   w->maxrounds = par->maxrounds > 0 ? par->maxrounds : 1000000;
+   w->cub = malloc(sizeof(double) * (size_t)(n + 1));
+   w->clb = malloc(sizeof(double) * (size_t)(n + 1));
+   w->cubf = malloc(sizeof(double) * (size_t)(n + 1));
+   w->clbf = malloc(sizeof(double) * (size_t)(n + 1));
+   w->cflag = calloc((size_t)(n + 1), 1);
+   w->touched = malloc(sizeof(int32_t) * (size_t)(n + 1));
+   w->front = malloc(sizeof(int32_t) * (size_t)(m + 1));
+   w->next = malloc(sizeof(int32_t) * (size_t)(m + 1));
+   w->rowstamp = calloc((size_t)(m + 1), sizeof(int32_t));
+   w->oldlb = malloc(sizeof(double) * (size_t)(n + 1));
+   w->oldub = malloc(sizeof(double) * (size_t)(n + 1));
+   w->chg = malloc(sizeof(int32_t) * (size_t)(n + 1));
+   w->dirty = calloc((size_t)(n + 1), 1);
+   w->dirtylist = malloc(sizeof(int32_t) * (size_t)(n + 1));
+   w->savelb = malloc(sizeof(double) * (size_t)(n + 1));
+   w->saveub = malloc(sizeof(double) * (size_t)(n + 1));
+   return (w->cub && w->clb && w->cubf && w->clbf && w->cflag && w->touched && w->front && w->next && w->rowstamp
+      && w->oldlb && w->oldub && w->chg && w->dirty && w->dirtylist && w->savelb && w->saveub) ? 0 : -1;
+}
+
+static void workFree(Work* w)
+{
+   free(w->cub); free(w->clb); free(w->cubf); free(w->clbf); free(w->cflag); free(w->touched);
+   free(w->front); free(w->next); free(w->rowstamp); free(w->oldlb); free(w->oldub); free(w->chg);
+   free(w->dirty); free(w->dirtylist); free(w->savelb); free(w->saveub);
+}
+
+static void newStamp(Work* w)
+{
+   if( ++w->stamp == INT32_MAX )
+   {
+      memset(w->rowstamp, 0, sizeof(int32_t) * (size_t)(w->P->m + 1));
+      w->stamp = 1;
+   }
+}
+
+static void pushNext(Work* w, int32_t row)
+{
+   if( w->rowstamp[row] != w->stamp )
+   {
+      w->rowstamp[row] = w->stamp;
+      w->next[w->nnext++] = row;
+   }
+}
+
+/* rows that a bound move of column j makes worth re-tightening: the boundstightened reset of
+ * eventExecLinear, cons_linear.c:17239-17255 (lower bound up with a > 0 needs a finite rhs, with a < 0 a
+ * finite lhs; upper bound down with a > 0 needs a finite lhs, with a < 0 a finite rhs) */
+static void expandColumn(Work* w, int32_t j, int lbup, int ubdown)
+{
+   const lpo_problem* P = w->P;
+   int64_t p;
+   for( p = P->colptr[j]; p < P->colptr[j + 1]; ++p )
+   {
+      int32_t i = P->rowidx[p];
+      double a = P->cvals[p];
+      int rhsfin = !isInf(&w->s, P->rhs[i]);
+      int lhsfin = !isInf(&w->s, -P->lhs[i]);
+      int rel = 0;
+      if( lbup )
+         rel |= a > 0.0 ? rhsfin : lhsfin;
+      if( ubdown )
+         rel |= a > 0.0 ? lhsfin : rhsfin;
+      if( rel )
+         pushNext(w, i);
+   }
+}
+
+static void candUb(Work* w, int32_t j, double v, int force)
+{
+   uint8_t bit = force ? 2 : 1;
+   double* arr = force ? w->cubf : w->cub;
+   if( w->cflag[j] == 0 )
+      w->touched[w->ntouched++] = j;
+   if( !(w->cflag[j] & bit) || v < arr[j] )
+      arr[j] = v;
+   w->cflag[j] |= bit;
+}
+
+static void candLb(Work* w, int32_t j, double v, int force)
+{
+   uint8_t bit = force ? 8 : 4;
+   double* arr = force ? w->clbf : w->clb;
+   if( w->cflag[j] == 0 )
+      w->touched[w->ntouched++] = j;
+   if( !(w->cflag[j] & bit) || v > arr[j] )
+      arr[j] = v;
+   w->cflag[j] |= bit;
+}
+
+/* one frontier row: cutoff check of propagateCons (cons_linear.c:7718-7753), skip tests of tightenBounds
+ * (cons_linear.c:7017-7083, canTightenBounds :5214-5238) and candidate bounds of tightenVarBounds
+ * (:6700-6974, residual rule) or tightenVarBoundsEasy (:5380-5653, slack rule).  Returns 1 on cutoff. */
+static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lpo_result* res)
+{
+   const lpo_problem* P = w->P;
+   const Num* s = &w->s;
+   Act a;
+   double lhs = P->lhs[i];
+   double rhs = P->rhs[i];
+   int64_t p0 = P->rowptr[i];
+   int64_t p1 = P->rowptr[i + 1];
+   int64_t p;
+   int force;
+   double maxactdelta;
+   int easy;
+
+   rowActivity(s, P, lb, ub, i, &a);
+   res->rows++;
+   res->nnz += p1 - p0;
+
+   /* infeasibility with relaxed huge contributions (goodrelax TRUE), cons_linear.c:7718-7740 */
+   {
+      double minact, maxact;
+      int t1, t2, f1, f2;
+      getMinAct(s, &a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, 1, &minact, &t1, &f1);
+      getMaxAct(s, &a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, 1, &maxact, &t2, &f2);
+      if( feasGt(s, minact, rhs) || feasLt(s, maxact, lhs) )
+         return 1;
+   }
+
+   /* canTightenBounds */
+   if( a.minneginf + a.minposinf + a.minneghuge + a.minposhuge > 1
+      && a.maxneginf + a.maxposinf + a.maxneghuge + a.maxposhuge > 1 )
+      return 0;
+
+   /* consdataRecomputeMaxActivityDelta, cons_linear.c:1542-1599 */
+   maxactdelta = 0.0;
+   for( p = p0; p < p1; ++p )
+   {
+      int32_t j = P->colidx[p];
+      double d;
+      if( isInf(s, -lb[j]) || isInf(s, ub[j]) )
+      {
+         maxactdelta = s->inf;
+         break;
+      }
+      d = fabs(P->vals[p]) * (ub[j] - lb[j]);
+      if( d > maxactdelta )
+         maxactdelta = d;
+   }
+   if( feasZero(s, maxactdelta) )
+      return 0;
+   if( !isInf(s, maxactdelta) )
+   {
+      double minact, maxact, slack, surplus;
+      int t1, t2, f1, f2;
+      getMinAct(s, &a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, 0, &minact, &t1, &f1);
+      getMaxAct(s, &a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, 0, &maxact, &t2, &f2);
+      slack = (isInf(s, rhs) || f1) ? s->inf : rhs - minact;
+      surplus = (isInf(s, -lhs) || f2) ? s->inf : maxact - lhs;
+      if( le(s, maxactdelta, dmin(slack, surplus)) )
+         return 0;
+   }
+   easy = lt(s, maxactdelta, s->maxeasy);
+   force = (p1 - p0 == 1);
+
+   for( p = p0; p < p1; ++p )
+   {
+      int32_t j = P->colidx[p];
+      double val = P->vals[p];
+      double l = lb[j];
+      double u = ub[j];
+      int isint = P->isint[j] != 0;
+
+      if( easy )
+      {
+         /* tightenVarBoundsEasy; the finite part of the activity is QUAD_TO_DBL(minactivity) */
+         double minact = a.minhi + a.minlo;
+         double maxact = a.maxhi + a.maxlo;
+         if( !isInf(s, rhs) )
+         {
+            double slack, alpha;
+            if( feasLt(s, rhs, minact) )
+               return 1;
+            slack = rhs - minact;
+            if( !positive(s, slack) )
+               slack = 0.0;
+            alpha = val > 0.0 ? val * (u - l) : val * (l - u);
+            if( sumGt(s, alpha, slack) || (force && gt(s, alpha, slack)) )
+            {
+               if( val > 0.0 )
+               {
+                  /* tightenVarUb, cons_linear.c:5242-5304 */
+                  double nb = adjUb(s, isint, l + slack / val);
+                  if( force || ubBetter(s, nb, l, u) )
+                  {
+                     candUb(w, j, nb, force);
+                     res->candidates++;
+                  }
+               }
+               else
+               {
+                  /* tightenVarLb, cons_linear.c:5307-5376 */
+                  double nb = adjLb(s, isint, u + slack / val);
+                  if( force || lbBetter(s, nb, l, u) )
+                  {
+                     candLb(w, j, nb, force);
+                     res->candidates++;
+                  }
+               }
+            }
+         }
+         if( !isInf(s, -lhs) )
+         {
+            double slack, alpha;
+            if( feasLt(s, maxact, lhs) )
+               return 1;
+            slack = maxact - lhs;
+            if( !positive(s, slack) )
+               slack = 0.0;
+            alpha = val > 0.0 ? val * (u - l) : val * (l - u);
+            if( sumGt(s, alpha, slack) || (force && gt(s, alpha, slack)) )
+            {
+               if( val > 0.0 )
+               {
+                  double nb = adjLb(s, isint, u - slack / val);
+                  if( force || lbBetter(s, nb, l, u) )
+                  {
+                     candLb(w, j, nb, force);
+                     res->candidates++;
+                  }
+               }
+               else
+               {
+                  double nb = adjUb(s, isint, l - slack / val);
+                  if( force || ubBetter(s, nb, l, u) )
+                  {
+                     candUb(w, j, nb, force);
+                     res->candidates++;
+                  }
+               }
+            }
+         }
+         continue;
+      }
+
+      {
+         /* tightenVarBounds, residual rule */
+         double minres, maxres;
+         int mintight, maxtight, mininf, maxinf;
+         residuals(s, &a, val, l, u, &minres, &maxres, &mintight, &maxtight, &mininf, &maxinf);
+
+         if( val > 0.0 )
+         {
+            if( !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !eq(s, minres / rhs, 1.0)) )
+            {
+               double newub = (rhs - minres) / val;
+               if( !isInf(s, newub)
+                  && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u)) )
+               {
+                  int unreliable = updateUnreliable(s, minres, a.minhi + a.minlo);
+                  if( unreliable )
+                  {
+                     minres = reliableResidual(P, lb, ub, i, p, 1);
+                     newub = (rhs - minres) / val;
+                     unreliable = isInf(s, -minres) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint)
+                        && (!force || !lt(s, newub, u)));
+                  }
+                  if( !unreliable )
+                  {
+                     candUb(w, j, newub, force);
+                     res->candidates++;
+                  }
+               }
+            }
+            if( !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !eq(s, maxres / lhs, 1.0)) )
+            {
+               double newlb = (lhs - maxres) / val;
+               if( !isInf(s, -newlb)
+                  && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u)) )
+               {
+                  int skip = 0;
+                  if( updateUnreliable(s, maxres, a.maxhi + a.maxlo) )
+                  {
+                     maxres = reliableResidual(P, lb, ub, i, p, 0);
+                     newlb = (lhs - maxres) / val;
+                     skip = isInf(s, maxres) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint)
+                        && (!force || !gt(s, newlb, l)));
+                  }
+                  if( !skip )
+                  {
+                     candLb(w, j, newlb, force);
+                     res->candidates++;
+                  }
+               }
+            }
+         }
+         else
+         {
+            if( !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !eq(s, minres / rhs, 1.0)) )
+            {
+               double newlb = (rhs - minres) / val;
+               if( !isInf(s, -newlb)
+                  && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u)) )
+               {
+                  int unreliable = updateUnreliable(s, minres, a.minhi + a.minlo);
+                  if( unreliable )
+                  {
+                     minres = reliableResidual(P, lb, ub, i, p, 1);
+                     newlb = (rhs - minres) / val;
+                     unreliable = isInf(s, -minres) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint)
+                        && (!force || !gt(s, newlb, l)));
+                  }
+                  if( !unreliable )
+                  {
+                     candLb(w, j, newlb, force);
+                     res->candidates++;
+                  }
+               }
+            }
+            if( !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !eq(s, maxres / lhs, 1.0)) )
+            {
+               double newub = (lhs - maxres) / val;
+               if( !isInf(s, newub)
+                  && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u)) )
+               {
+                  int skip = 0;
+                  if( updateUnreliable(s, maxres, a.maxhi + a.maxlo) )
+                  {
+                     maxres = reliableResidual(P, lb, ub, i, p, 0);
+                     newub = (lhs - maxres) / val;
+                     /* the upper-bound branch for a < 0 combines its conditions with && (cons_linear.c:6936-6938) */
+                     skip = isInf(s, maxres) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) && !isint)
+                        && (!force || !lt(s, newub, u)));
+                  }
+                  if( !skip )
+                  {
+                     candUb(w, j, newub, force);
+                     res->candidates++;
+                  }
+               }
+            }
+         }
+      }
+   }
+   return 0;
+}
+
+/* acceptance of the best candidates of one column: SCIPinferVarUbCons / SCIPinferVarLbCons
+ * (scip_var.c:7071-7112 / 6965-7006) against the round-start bounds, upper bound first and the lower
+ * bound against the new upper bound.  Returns 1 on cutoff. */
+static int applyColumn(Work* w, int32_t j, double* lb, double* ub, int* lbup, int* ubdown)
+{
+   const Num* s = &w->s;
+   const lpo_problem* P = w->P;
+   int isint = P->isint[j] != 0;
+   double l = lb[j];
+   double u = ub[j];
+   double nu = u;
+   double nl = l;
+   uint8_t f = w->cflag[j];
+   int k;
+
+   for( k = 0; k < 2; ++k )
+   {
+      int force = (k == 1);
+      double c;
+      if( !(f & (force ? 2 : 1)) )
+         continue;
+      c = adjUb(s, isint, force ? w->cubf[j] : w->cub[j]);
+      if( isInf(s, -c) || feasLt(s, c, l) )
+         return 1;
+      c = dmax(c, l);
+      if( force ? !ge(s, c, u) : ubBetter(s, c, l, u) )
+         nu = dmin(nu, c);
+   }
+   for( k = 0; k < 2; ++k )
+   {
+      int force = (k == 1);
+      double c;
+      if( !(f & (force ? 8 : 4)) )
+         continue;
+      c = adjLb(s, isint, force ? w->clbf[j] : w->clb[j]);
+      if( isInf(s, c) || feasGt(s, c, nu) )
+         return 1;
+      c = dmin(c, nu);
+      if( force ? !le(s, c, l) : lbBetter(s, c, l, nu) )
+         nl = dmax(nl, c);
+   }
+   *lbup = nl > l;
+   *ubdown = nu < u;
+   lb[j] = nl;
+   ub[j] = nu;
+   return 0;
+}
+
+static void markDirty(Work* w, int32_t j, double l, double u)
+{
+   if( !w->dirty[j] )
+   {
+      w->dirty[j] = 1;
+      w->dirtylist[w->ndirty++] = j;
+      w->savelb[j] = l;
+      w->saveub[j] = u;
+   }
+}
+
+/* the fixpoint loop over the frontier in w->next (already stamped) */
+static int fixpoint(Work* w, double* lb, double* ub, lpo_result* res, int track)
+{
+   int32_t round;
+   res->cutoff = 0;
+   res->status = 0;
+   res->rounds = 0;
+   for( round = 0; w->nnext > 0; ++round )
+   {
+      int64_t k;
+      int32_t* t;
+      if( round >= w->maxrounds )
+      {
+         res->status = 2;
+         return 0;
+      }
+      t = w->front; w->front = w->next; w->next = t;
+      w->nfront = w->nnext;
+      w->nnext = 0;
+      res->rounds = round + 1;
+
+      w->ntouched = 0;
+      for( k = 0; k < w->nfront; ++k )
+      {
+         if( processRow(w, lb, ub, w->front[k], res) )
+         {
+            int64_t q;
+            for( q = 0; q < w->ntouched; ++q )
+               w->cflag[w->touched[q]] = 0;
+            res->cutoff = 1;
+            res->status = 1;
+            return 1;
+         }
+      }
+
+      newStamp(w);
+      for( k = 0; k < w->ntouched; ++k )
+      {
+         int32_t j = w->touched[k];
+         int lbup = 0, ubdown = 0;
+         double l0 = lb[j], u0 = ub[j];
+         if( applyColumn(w, j, lb, ub, &lbup, &ubdown) )
+         {
+            int64_t q;
+            for( q = 0; q < w->ntouched; ++q )
+               w->cflag[w->touched[q]] = 0;
+            res->cutoff = 1;
+            res->status = 1;
+            return 1;
+         }
+         w->cflag[j] = 0;
+         if( lbup || ubdown )
+         {
+            if( track )
+               markDirty(w, j, l0, u0);
+            res->changes += lbup + ubdown;
+            expandColumn(w, j, lbup, ubdown);
+         }
+      }
+   }
+   return 0;
+}
+
+int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, lpo_result* res)
+{
+   Work w;
+   int64_t k;
+   memset(res, 0, sizeof(*res));
+   if( workInit(&w, prob, par) != 0 )
+   {
+      workFree(&w);
+      return -1;
+   }
+   newStamp(&w);
+   w.nnext = 0;
+   if( seedcols == NULL )
+   {
+      for( k = 0; k < prob->m; ++k )
+         pushNext(&w, (int32_t)k);
+   }
+   else
+   {
+      for( k = 0; k < nseed; ++k )
+      {
+         int32_t j = seedcols[k];
+         expandColumn(&w, j, lb[j] > oldlb[k], ub[j] < oldub[k]);
+      }
+   }
+   fixpoint(&w, lb, ub, res, 0);
+   workFree(&w);
+   return 0;
+}
+
+typedef struct
+{
+   const lpo_problem* P;
+   const lpo_params* par;
+   const double* baselb;
+   const double* baseub;
+   int64_t k0, k1;
+   const int64_t* ptr;
+   const int32_t* chg_col;
+   const double* chg_lb;
+   const double* chg_ub;
+   int8_t* out_cutoff;
+   int32_t* out_rounds;
+   int32_t* out_n;
+   int32_t* out_col;
+   double* out_lb;
+   double* out_ub;
+   int32_t cap;
+   lpo_result tot;
+   int err;
+} NodeJob;
+
+static void* nodeWorker(void* arg)
+{
+   NodeJob* J = arg;
+   const lpo_problem* P = J->P;
+   Work w;
+   double* lb;
+   double* ub;
+   int64_t k;
+
+   memset(&J->tot, 0, sizeof(J->tot));
+   lb = malloc(sizeof(double) * (size_t)P->n);
+   ub = malloc(sizeof(double) * (size_t)P->n);
+   if( lb == NULL || ub == NULL || workInit(&w, P, J->par) != 0 )
+   {
+      J->err = -1;
+      free(lb);
+      free(ub);
+      return NULL;
+   }
+   memcpy(lb, J->baselb, sizeof(double) * (size_t)P->n);
+   memcpy(ub, J->baseub, sizeof(double) * (size_t)P->n);
+
+   for( k = J->k0; k < J->k1; ++k )
+   {
+      lpo_result r;
+      int64_t q;
+      int cut = 0;
+      memset(&r, 0, sizeof(r));
+      newStamp(&w);
+      w.nnext = 0;
+      w.ndirty = 0;
+      for( q = J->ptr[k]; q < J->ptr[k + 1]; ++q )
+      {
+         int32_t j = J->chg_col[q];
+         double nl = J->chg_lb[q];
+         double nu = J->chg_ub[q];
+         double l0 = lb[j], u0 = ub[j];
+         if( nl > u0 || nu < l0 )
+            cut = 1;
+         else
+         {
+            /* branching bound changes tighten only (SCIPchgVarLb/UbProbing semantics) */
+            if( nl > l0 || nu < u0 )
+            {
+               markDirty(&w, j, l0, u0);
+               if( nl > l0 )
+                  lb[j] = nl;
+               if( nu < u0 )
+                  ub[j] = nu;
+            }
+         }
+      }
+      if( !cut )
+      {
+         for( q = J->ptr[k]; q < J->ptr[k + 1]; ++q )
+         {
+            int32_t j = J->chg_col[q];
+            if( w.dirty[j] )
+               expandColumn(&w, j, lb[j] > w.savelb[j], ub[j] < w.saveub[j]);
+         }
+         cut = fixpoint(&w, lb, ub, &r, 1);
+      }
+      else
+      {
+         r.cutoff = 1;
+         r.status = 1;
+      }
+      J->out_cutoff[k] = (int8_t)cut;
+      J->out_rounds[k] = r.rounds;
+      {
+         int32_t cnt = 0;
+         if( !cut )
+         {
+            for( q = 0; q < w.ndirty; ++q )
+            {
+               int32_t j = w.dirtylist[q];
+               if( lb[j] != J->baselb[j] || ub[j] != J->baseub[j] )
+               {
+                  if( cnt < J->cap )
+                  {
+                     int64_t o = k * (int64_t)J->cap + cnt;
+                     J->out_col[o] = j;
+                     J->out_lb[o] = lb[j];
+                     J->out_ub[o] = ub[j];
+                  }
+                  ++cnt;
+               }
+            }
+         }
+         J->out_n[k] = cnt > J->cap ? -1 : cnt;
+      }
+      /* restore the base bounds */
+      for( q = 0; q < w.ndirty; ++q )
+      {
+         int32_t j = w.dirtylist[q];
+         lb[j] = J->baselb[j];
+         ub[j] = J->baseub[j];
+         w.dirty[j] = 0;
+      }
+      w.ndirty = 0;
+      J->tot.rows += r.rows;
+      J->tot.nnz += r.nnz;
+      J->tot.candidates += r.candidates;
+      J->tot.changes += r.changes;
+      J->tot.cutoff += cut;
+      if( r.rounds > J->tot.rounds )
+         J->tot.rounds = r.rounds;
+   }
+   workFree(&w);
+   free(lb);
+   free(ub);
+   return NULL;
+}
+
+int lpo_propagate_nodes(const lpo_problem* prob, const lpo_params* par, const double* baselb, const double* baseub,
+   int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+   int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb, double* out_ub,
+   int32_t cap, int32_t nthreads, lpo_result* total)
+{
+   NodeJob* jobs;
+   pthread_t* th;
+   int t;
+   int err = 0;
+   if( nthreads <= 0 )
+      nthreads = 1;
+   if( nthreads > nnodes && nnodes > 0 )
+      nthreads = (int32_t)nnodes;
+   jobs = calloc((size_t)nthreads, sizeof(NodeJob));
+   th = calloc((size_t)nthreads, sizeof(pthread_t));
+   if( jobs == NULL || th == NULL )
+   {
+      free(jobs);
+      free(th);
+      return -1;
+   }
+   for( t = 0; t < nthreads; ++t )
+   {
+      NodeJob* J = &jobs[t];
+      J->P = prob; J->par = par; J->baselb = baselb; J->baseub = baseub;
+      J->k0 = nnodes * t / nthreads;
+      J->k1 = nnodes * (t + 1) / nthreads;
+      J->ptr = ptr; J->chg_col = chg_col; J->chg_lb = chg_lb; J->chg_ub = chg_ub;
+      J->out_cutoff = out_cutoff; J->out_rounds = out_rounds; J->out_n = out_n;
+      J->out_col = out_col; J->out_lb = out_lb; J->out_ub = out_ub; J->cap = cap;
+   }
+   if( nthreads == 1 )
+      nodeWorker(&jobs[0]);
+   else
+   {
+      for( t = 0; t < nthreads; ++t )
+         pthread_create(&th[t], NULL, nodeWorker, &jobs[t]);
+      for( t = 0; t < nthreads; ++t )
+         pthread_join(th[t], NULL);
+   }
+   if( total != NULL )
+      memset(total, 0, sizeof(*total));
+   for( t = 0; t < nthreads; ++t )
+   {
+      if( jobs[t].err )
+         err = jobs[t].err;
+      if( total != NULL )
+      {
+         total->rows += jobs[t].tot.rows;
+         total->nnz += jobs[t].tot.nnz;
+         total->candidates += jobs[t].tot.candidates;
+         total->changes += jobs[t].tot.changes;
+         total->cutoff += jobs[t].tot.cutoff;
+         if( jobs[t].tot.rounds > total->rounds )
+            total->rounds = jobs[t].tot.rounds;
+      }
+   }
+   free(jobs);
+   free(th);
+   return err;
+}

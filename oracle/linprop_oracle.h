@@ -1,0 +1,91 @@
+/* Test infrastructure only: CPU restatement of SCIP's cons_linear activity-based bound propagation,
+ * used by tests/, smoke() and the CPU-baseline leg of bench.py as the checker of the CUDA path.
+ * It is never linked into the product library (scip_gb300/_lib/libgbp.so).
+ *
+ * Round semantics (shared with the CUDA path, so that both produce bit-identical integer bounds):
+ *   a round takes the current frontier of rows and the bounds B_r at the start of the round;
+ *   every frontier row computes its activities from B_r and emits candidate bounds with SCIP's rules;
+ *   per column the best candidates (min upper / max lower) are accepted with SCIP's acceptance rules
+ *   against B_r (upper bound first, then lower bound against the new upper bound); the next frontier
+ *   is every row holding a column whose bound moved in a direction that row's finite sides can use.
+ * SCIP itself (cons_linear.c consPropLinear) walks marked rows one at a time and applies each
+ * tightening at once; because of the minimal-improvement test (set.c:7711-7753) the two orders can stop
+ * at different, equally valid fixpoints.  tests/golden holds SCIP's own results to measure that.
+ */
+#ifndef LINPROP_ORACLE_H
+#define LINPROP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct
+{
+   double infinity;             /* numerics/infinity, def.h:172 */
+   double epsilon;              /* numerics/epsilon */
+   double sumepsilon;           /* numerics/sumepsilon */
+   double feastol;              /* numerics/feastol */
+   double hugeval;              /* numerics/hugeval */
+   double boundstreps;          /* numerics/boundstreps */
+   double recompfac;            /* numerics/recompfac */
+   double maxeasyactivitydelta; /* constraints/linear/maxeasyactivitydelta (0 = residual rule everywhere) */
+   int32_t maxrounds;           /* round cap; <= 0 means 1,000,000 */
+   int32_t reserved;
+} lpo_params;
+
+typedef struct
+{
+   int64_t m;
+   int64_t n;
+   const int64_t* rowptr;
+   const int32_t* colidx;
+   const double* vals;
+   const double* lhs;
+   const double* rhs;
+   const int8_t* isint;
+   const int64_t* colptr;
+   const int32_t* rowidx;
+   const double* cvals;
+} lpo_problem;
+
+typedef struct
+{
+   int32_t cutoff;
+   int32_t rounds;
+   int32_t status;      /* 0 fixpoint, 1 cutoff, 2 round limit */
+   int32_t reserved;
+   int64_t rows;        /* frontier rows processed over all rounds */
+   int64_t nnz;         /* nonzeros of those rows */
+   int64_t candidates;  /* candidate bounds emitted */
+   int64_t changes;     /* accepted bound changes (lower and upper counted separately) */
+} lpo_result;
+
+void lpo_default_params(lpo_params* p);
+
+/* activities of rows[0..nrows) (all rows if rows == NULL) from scratch under [lb,ub]:
+ * act[4*k..] = minhi, minlo, maxhi, maxlo (double-double), cnt[8*k..] = minposinf, minneginf, minposhuge,
+ * minneghuge, maxposinf, maxneginf, maxposhuge, maxneghuge. */
+void lpo_row_activities(const lpo_problem* prob, const lpo_params* par, const double* lb, const double* ub,
+   const int32_t* rows, int64_t nrows, double* act, int32_t* cnt);
+
+/* propagate to fixpoint in place; the first frontier is every row (seedcols == NULL) or the rows that the
+ * listed column changes make relevant (seedcols[k] moved from [oldlb[k],oldub[k]] to the bounds in lb/ub) */
+int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, lpo_result* res);
+
+/* batch of nodes sharing base bounds: node k applies bound changes chg_col/chg_lb/chg_ub[ptr[k]..ptr[k+1])
+ * and propagates; outputs per node the cutoff flag, rounds, and up to cap changed columns
+ * (out_col/out_lb/out_ub[k*cap..]) whose final bounds differ from the base; out_n[k] = count (or -1 if
+ * more than cap).  nthreads <= 0 uses one thread. Returns 0. */
+int lpo_propagate_nodes(const lpo_problem* prob, const lpo_params* par, const double* baselb, const double* baseub,
+   int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+   int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb, double* out_ub,
+   int32_t cap, int32_t nthreads, lpo_result* total);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,168 @@
+"""Test infrastructure only: ctypes binding of the C restatement (oracle/linprop_oracle.c) and runner of the
+SCIP oracle driver (oracle/_ref/scip_oracle, present only where the SCIP sources were available to build it).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module, as the checker of
+the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liblinprop_oracle.so")
+SCIP_ORACLE = os.path.join(HERE, "_ref", "scip_oracle")
+
+_P = ctypes.c_void_p
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("infinity", ctypes.c_double), ("epsilon", ctypes.c_double), ("sumepsilon", ctypes.c_double),
+                ("feastol", ctypes.c_double), ("hugeval", ctypes.c_double), ("boundstreps", ctypes.c_double),
+                ("recompfac", ctypes.c_double), ("maxeasyactivitydelta", ctypes.c_double),
+                ("maxrounds", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int64), ("n", ctypes.c_int64), ("rowptr", _P), ("colidx", _P), ("vals", _P),
+                ("lhs", _P), ("rhs", _P), ("isint", _P), ("colptr", _P), ("rowidx", _P), ("cvals", _P)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("cutoff", ctypes.c_int32), ("rounds", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("rows", ctypes.c_int64), ("nnz", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64)]
+
+
+def build() -> str:
+    """Compile the C restatement (gcc, a few seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        L.lpo_default_params.argtypes = [ctypes.POINTER(Params)]
+        L.lpo_row_activities.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P,
+                                         ctypes.c_int64, _P, _P]
+        L.lpo_propagate.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
+                                    _P, _P, ctypes.POINTER(Result)]
+        L.lpo_propagate_nodes.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64,
+                                          _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.POINTER(Result)]
+        _lib = L
+    return _lib
+
+
+def params(maxeasy: float = 0.0, maxrounds: int = 0) -> Params:
+    p = Params()
+    lib().lpo_default_params(ctypes.byref(p))
+    p.maxeasyactivitydelta = maxeasy
+    p.maxrounds = maxrounds
+    return p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class Oracle:
+    """Keeps an instance (and its CSC copy) alive for repeated oracle calls."""
+
+    def __init__(self, inst):
+        self.inst = inst
+        self.rowptr = np.ascontiguousarray(inst.rowptr, dtype=np.int64)
+        self.colidx = np.ascontiguousarray(inst.colidx, dtype=np.int32)
+        self.vals = np.ascontiguousarray(inst.vals, dtype=np.float64)
+        self.lhs = np.ascontiguousarray(inst.lhs, dtype=np.float64)
+        self.rhs = np.ascontiguousarray(inst.rhs, dtype=np.float64)
+        self.isint = np.ascontiguousarray(inst.isint, dtype=np.int8)
+        cp, ri, cv = inst.csc()
+        self.colptr, self.rowidx, self.cvals = cp, ri, cv
+        self.prob = Problem(inst.m, inst.n, _ptr(self.rowptr), _ptr(self.colidx), _ptr(self.vals), _ptr(self.lhs),
+                            _ptr(self.rhs), _ptr(self.isint), _ptr(self.colptr), _ptr(self.rowidx), _ptr(self.cvals))
+
+    def activities(self, lb, ub, rows=None, par=None):
+        par = par or params()
+        lb = np.ascontiguousarray(lb, dtype=np.float64)
+        ub = np.ascontiguousarray(ub, dtype=np.float64)
+        nr = self.inst.m if rows is None else len(rows)
+        r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+        act = np.zeros((nr, 4))
+        cnt = np.zeros((nr, 8), dtype=np.int32)
+        lib().lpo_row_activities(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), _ptr(r), nr,
+                                 _ptr(act), _ptr(cnt))
+        return act, cnt
+
+    def propagate(self, lb, ub, par=None, seed=None):
+        """Root-style fixpoint from all rows (seed None) or from (cols, oldlb, oldub) changes; returns
+        (lb, ub, Result)."""
+        par = par or params()
+        lb = np.array(lb, dtype=np.float64)
+        ub = np.array(ub, dtype=np.float64)
+        res = Result()
+        if seed is None:
+            lib().lpo_propagate(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), 0, None, None, None,
+                                ctypes.byref(res))
+        else:
+            cols, olb, oub = (np.ascontiguousarray(x) for x in seed)
+            cols = cols.astype(np.int32)
+            olb = olb.astype(np.float64)
+            oub = oub.astype(np.float64)
+            lib().lpo_propagate(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), len(cols), _ptr(cols),
+                                _ptr(olb), _ptr(oub), ctypes.byref(res))
+        return lb, ub, res
+
+    def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1):
+        """Node batch; returns dict with cutoff [N], rounds [N], n [N], col/lb/ub [N, cap] and totals."""
+        par = par or params()
+        N = nodes.nnodes
+        baselb = np.ascontiguousarray(baselb, dtype=np.float64)
+        baseub = np.ascontiguousarray(baseub, dtype=np.float64)
+        ptr = np.ascontiguousarray(nodes.ptr, dtype=np.int64)
+        col = np.ascontiguousarray(nodes.col, dtype=np.int32)
+        nlb = np.ascontiguousarray(nodes.lb, dtype=np.float64)
+        nub = np.ascontiguousarray(nodes.ub, dtype=np.float64)
+        out = dict(cutoff=np.zeros(N, dtype=np.int8), rounds=np.zeros(N, dtype=np.int32),
+                   n=np.zeros(N, dtype=np.int32), col=np.zeros((N, cap), dtype=np.int32),
+                   lb=np.zeros((N, cap)), ub=np.zeros((N, cap)))
+        tot = Result()
+        rc = lib().lpo_propagate_nodes(ctypes.byref(self.prob), ctypes.byref(par), _ptr(baselb), _ptr(baseub), N,
+                                       _ptr(ptr), _ptr(col), _ptr(nlb), _ptr(nub), _ptr(out["cutoff"]),
+                                       _ptr(out["rounds"]), _ptr(out["n"]), _ptr(out["col"]), _ptr(out["lb"]),
+                                       _ptr(out["ub"]), cap, nthreads, ctypes.byref(tot))
+        if rc != 0:
+            raise MemoryError("oracle node batch failed")
+        out["total"] = tot
+        return out
+
+
+def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None):
+    """Run SCIP itself (oracle/_ref/scip_oracle) on the instance; returns the parsed output of
+    scip_gb300.instances.read_oracle_output."""
+    from scip_gb300.instances import read_oracle_output
+
+    if not os.path.exists(SCIP_ORACLE):
+        raise FileNotFoundError("SCIP oracle driver not built (make -C oracle ref needs the SCIP sources)")
+    with tempfile.TemporaryDirectory(dir=workdir) as d:
+        ip = os.path.join(d, "inst.bin")
+        op = os.path.join(d, "out.bin")
+        inst.write(ip)
+        npth = "-"
+        if nodes is not None:
+            npth = os.path.join(d, "nodes.bin")
+            nodes.write(npth)
+        cmd = [SCIP_ORACLE, ip, npth, op] + (["--easy"] if easy else []) + ["--repeat", str(repeat)]
+        subprocess.run(cmd, check=True, capture_output=True)
+        return read_oracle_output(op)

@@ -1,0 +1,768 @@
+// C ABI of libgbp (declarations and contract: include/gbp.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gbp.h"
+#include "gbp_internal.h"
+
+using namespace gbp;
+
+namespace {
+constexpr int GBP_ABI_VERSION = 1;
+}
+
+struct gbp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sms = 0;
+  gbp_params par{};
+  Num num{};
+  std::string err;
+
+  // problem
+  bool has_problem = false;
+  int64_t m = 0, n = 0, nnz = 0;
+  int64_t* d_rowptr = nullptr;
+  int32_t* d_colidx = nullptr;
+  double* d_vals = nullptr;
+  double* d_lhs = nullptr;
+  double* d_rhs = nullptr;
+  int8_t* d_isint = nullptr;
+  int64_t* d_colptr = nullptr;
+  uint32_t* d_cscrow = nullptr;
+
+  // plain path
+  double* d_lb = nullptr;
+  double* d_ub = nullptr;
+  long long* d_cand = nullptr;  // 4*n keys: cub, clb, cubf, clbf
+  int* d_cflag = nullptr;
+  int* d_touched = nullptr;
+  int* d_list[2] = {nullptr, nullptr};
+  int* d_rowstamp = nullptr;
+  int* d_allrows = nullptr;
+  int nshort_all = 0, nlong_all = 0;
+  int* d_ctr = nullptr;  // nshort[2], nlong[2], ntouched, cutoff
+  unsigned long long* d_stats = nullptr;  // rows, nnz, cands, changes, cutoffs, maxrounds
+  int stamp = 0;
+  int32_t* d_seedcols = nullptr;
+  double* d_seedold = nullptr;  // 2*cap: oldlb, oldub
+  int64_t seedcap = 0;
+  int* h_ctr = nullptr;  // pinned
+
+  // batched path
+  int ctas_per_sm = 0;
+  int nslots = 0;
+  SlotArrays slots{};
+  void* slot_mem = nullptr;
+  int64_t slot_stamp_budget = 0;
+  double2* d_base = nullptr;
+  int* d_next_item = nullptr;
+  int* d_status = nullptr;
+  unsigned long long* d_out_used = nullptr;
+  // staging for the host-pointer node API
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
+      return e_ == cudaErrorMemoryAllocation ? GBP_ERR_NOMEM : GBP_ERR_CUDA;             \
+    }                                                                                    \
+  } while (0)
+
+static int fail(gbp_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+static void freeProblem(gbp_ctx* ctx) {
+  void* ptrs[] = {ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint, ctx->d_colptr,
+                  ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
+                  ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
+  ctx->d_rhs = nullptr; ctx->d_isint = nullptr; ctx->d_colptr = nullptr; ctx->d_cscrow = nullptr;
+  ctx->d_lb = nullptr; ctx->d_ub = nullptr; ctx->d_cand = nullptr; ctx->d_cflag = nullptr;
+  ctx->d_touched = nullptr; ctx->d_list[0] = ctx->d_list[1] = nullptr; ctx->d_rowstamp = nullptr;
+  ctx->d_allrows = nullptr; ctx->d_base = nullptr; ctx->slot_mem = nullptr; ctx->stage = nullptr;
+  ctx->stage_bytes = 0;
+  ctx->nslots = 0;
+  ctx->has_problem = false;
+}
+
+static Prob devProb(const gbp_ctx* ctx) {
+  return Prob{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
+              ctx->d_colptr, ctx->d_cscrow};
+}
+
+static int gridFor(const gbp_ctx* ctx, int64_t work, int per_block = 256, int cap_per_sm = 16) {
+  int64_t g = (work + per_block - 1) / per_block;
+  int64_t cap = (int64_t)ctx->sms * cap_per_sm;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+extern "C" {
+
+int gbp_version(void) { return GBP_ABI_VERSION; }
+
+const char* gbp_error_string(int code) {
+  switch (code) {
+    case GBP_OK: return "ok";
+    case GBP_ERR_INVALID: return "invalid argument";
+    case GBP_ERR_CUDA: return "CUDA error";
+    case GBP_ERR_NOMEM: return "out of memory";
+    case GBP_ERR_NODEVICE: return "no suitable CUDA device";
+    case GBP_ERR_LIMIT: return "round limit reached";
+    case GBP_ERR_OVERFLOW: return "output list too small";
+    case GBP_ERR_STATE: return "inconsistent device state";
+    default: return "unknown error";
+  }
+}
+
+const char* gbp_last_error(const gbp_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void gbp_default_params(gbp_params* p) {
+  if (!p) return;
+  p->infinity = 1e20;
+  p->epsilon = 1e-9;
+  p->sumepsilon = 1e-6;
+  p->feastol = 1e-6;
+  p->hugeval = 1e15;
+  p->boundstreps = 0.05;
+  p->recompfac = 1e6;
+  p->maxeasyactivitydelta = 1e6;
+  p->maxrounds = 0;
+  p->flags = 0;
+}
+
+int gbp_set_params(gbp_ctx* ctx, const gbp_params* p) {
+  if (!ctx || !p) return GBP_ERR_INVALID;
+  if (!(p->infinity > 0) || !(p->epsilon >= 0) || !(p->feastol >= 0) || !(p->hugeval > 0) || !(p->boundstreps >= 0))
+    return fail(ctx, GBP_ERR_INVALID, "invalid numerics");
+  ctx->par = *p;
+  ctx->num = Num{p->infinity, p->epsilon, p->sumepsilon, p->feastol, p->hugeval, p->boundstreps, p->recompfac,
+                 p->maxeasyactivitydelta};
+  return GBP_OK;
+}
+
+int gbp_create(gbp_ctx** out, int device, void* stream) {
+  if (!out) return GBP_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+    cudaGetLastError();
+    return GBP_ERR_NODEVICE;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return GBP_ERR_NODEVICE;
+  if (prop.major != 10 || prop.minor != 3) return GBP_ERR_NODEVICE;  // built for sm_103a only
+  gbp_ctx* ctx = new (std::nothrow) gbp_ctx();
+  if (!ctx) return GBP_ERR_NOMEM;
+  ctx->device = device;
+  ctx->sms = prop.multiProcessorCount;
+  gbp_params p;
+  gbp_default_params(&p);
+  gbp_set_params(ctx, &p);
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete ctx;
+    return GBP_ERR_NODEVICE;
+  }
+  if (stream) {
+    ctx->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return GBP_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+  }
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+      cudaMalloc(&ctx->d_ctr, 8 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_stats, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_next_item, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_status, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_out_used, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&ctx->h_ctr, 16 * sizeof(int)) != cudaSuccess) {
+    gbp_destroy(ctx);
+    return GBP_ERR_CUDA;
+  }
+  *out = ctx;
+  return GBP_OK;
+}
+
+int gbp_destroy(gbp_ctx* ctx) {
+  if (!ctx) return GBP_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  freeProblem(ctx);
+  if (ctx->d_seedcols) cudaFree(ctx->d_seedcols);
+  if (ctx->d_seedold) cudaFree(ctx->d_seedold);
+  if (ctx->d_ctr) cudaFree(ctx->d_ctr);
+  if (ctx->d_stats) cudaFree(ctx->d_stats);
+  if (ctx->d_next_item) cudaFree(ctx->d_next_item);
+  if (ctx->d_status) cudaFree(ctx->d_status);
+  if (ctx->d_out_used) cudaFree(ctx->d_out_used);
+  if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GBP_OK;
+}
+
+int gbp_get_stream(const gbp_ctx* ctx, void** stream) {
+  if (!ctx || !stream) return GBP_ERR_INVALID;
+  *stream = (void*)ctx->stream;
+  return GBP_OK;
+}
+
+int gbp_set_batch_shape(gbp_ctx* ctx, int32_t ctas_per_sm) {
+  if (!ctx || ctas_per_sm < 0 || ctas_per_sm > 32) return GBP_ERR_INVALID;
+  if (ctas_per_sm != ctx->ctas_per_sm) {
+    ctx->ctas_per_sm = ctas_per_sm;
+    if (ctx->slot_mem) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->slot_mem);
+      ctx->slot_mem = nullptr;
+      ctx->nslots = 0;
+    }
+  }
+  return GBP_OK;
+}
+
+int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                       const double* vals, const double* lhs, const double* rhs, const int8_t* isint) {
+  if (!ctx || m < 0 || n < 0 || !rowptr || (m > 0 && (!lhs || !rhs)) || (n > 0 && !isint))
+    return fail(ctx, GBP_ERR_INVALID, "null argument or negative size");
+  if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1)
+    return fail(ctx, GBP_ERR_INVALID, "problem too large (m < 2^30, n < 2^31 required)");
+  if (rowptr[0] != 0) return fail(ctx, GBP_ERR_INVALID, "rowptr[0] must be 0");
+  for (int64_t i = 0; i < m; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
+  const int64_t nnz = rowptr[m];
+  if (nnz > 0 && (!colidx || !vals)) return fail(ctx, GBP_ERR_INVALID, "null colidx/vals");
+  for (int64_t p = 0; p < nnz; ++p)
+    if (colidx[p] < 0 || colidx[p] >= n) return fail(ctx, GBP_ERR_INVALID, "column index out of range");
+
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  freeProblem(ctx);
+
+  // column-major copy with relevance flags (which bound moves each row can use)
+  std::vector<int64_t> colptr(n + 1, 0);
+  for (int64_t p = 0; p < nnz; ++p) colptr[colidx[p] + 1]++;
+  for (int64_t j = 0; j < n; ++j) colptr[j + 1] += colptr[j];
+  std::vector<int32_t> rowidx(nnz);
+  std::vector<double> cvals(nnz);
+  {
+    std::vector<int64_t> fill(colptr.begin(), colptr.end() - 1);
+    for (int64_t i = 0; i < m; ++i)
+      for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+        int64_t q = fill[colidx[p]]++;
+        rowidx[q] = (int32_t)i;
+        cvals[q] = vals[p];
+      }
+  }
+  // all-rows frontier: short rows from the front, long rows from the back
+  std::vector<int> allrows(std::max<int64_t>(m, 1));
+  int ns = 0, nl = 0;
+  for (int64_t i = 0; i < m; ++i) {
+    if (rowptr[i + 1] - rowptr[i] <= LONGROW) allrows[ns++] = (int)i;
+    else allrows[m - 1 - nl++] = (int)i;
+  }
+
+  const size_t mm = (size_t)std::max<int64_t>(m, 1), nn = (size_t)std::max<int64_t>(n, 1),
+               zz = (size_t)std::max<int64_t>(nnz, 1);
+  CK(cudaMalloc(&ctx->d_rowptr, (mm + 1) * sizeof(int64_t)));
+  CK(cudaMalloc(&ctx->d_colidx, zz * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->d_vals, zz * sizeof(double)));
+  CK(cudaMalloc(&ctx->d_lhs, mm * sizeof(double)));
+  CK(cudaMalloc(&ctx->d_rhs, mm * sizeof(double)));
+  CK(cudaMalloc(&ctx->d_isint, nn));
+  CK(cudaMalloc(&ctx->d_colptr, (nn + 1) * sizeof(int64_t)));
+  CK(cudaMalloc(&ctx->d_cscrow, zz * sizeof(uint32_t)));
+  CK(cudaMalloc(&ctx->d_lb, nn * sizeof(double)));
+  CK(cudaMalloc(&ctx->d_ub, nn * sizeof(double)));
+  CK(cudaMalloc(&ctx->d_cand, 4 * nn * sizeof(long long)));
+  CK(cudaMalloc(&ctx->d_cflag, nn * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_touched, nn * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_list[0], mm * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_list[1], mm * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_rowstamp, mm * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_allrows, mm * sizeof(int)));
+  CK(cudaMalloc(&ctx->d_base, nn * sizeof(double2)));
+
+  CK(cudaMemcpyAsync(ctx->d_rowptr, rowptr, (m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  if (nnz) {
+    CK(cudaMemcpyAsync(ctx->d_colidx, colidx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_vals, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (m) {
+    CK(cudaMemcpyAsync(ctx->d_lhs, lhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_rhs, rhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_allrows, allrows.data(), m * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (n) CK(cudaMemcpyAsync(ctx->d_isint, isint, n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_colptr, colptr.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  if (nnz) {
+    int32_t* d_rowidx = nullptr;
+    double* d_cvals = nullptr;
+    CK(cudaMalloc(&d_rowidx, nnz * sizeof(int32_t)));
+    CK(cudaMalloc(&d_cvals, nnz * sizeof(double)));
+    CK(cudaMemcpyAsync(d_rowidx, rowidx.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_cvals, cvals.data(), nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(launchCscFlags(ctx->stream, gridFor(ctx, nnz), nnz, d_cvals, d_rowidx, ctx->d_lhs, ctx->d_rhs,
+                      ctx->par.infinity, ctx->d_cscrow));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_rowidx);
+    cudaFree(d_cvals);
+  }
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand, nn, KEY_NONE_UB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + nn, nn, KEY_NONE_LB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 2 * nn, nn, KEY_NONE_UB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 3 * nn, nn, KEY_NONE_LB));
+  CK(cudaMemsetAsync(ctx->d_cflag, 0, nn * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_rowstamp, 0, mm * sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->m = m;
+  ctx->n = n;
+  ctx->nnz = nnz;
+  ctx->nshort_all = ns;
+  ctx->nlong_all = nl;
+  ctx->stamp = 0;
+  ctx->has_problem = true;
+  return GBP_OK;
+}
+
+// ------------------------------------------------------------------------------------------ plain path
+static Cands plainCands(gbp_ctx* ctx) {
+  const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+  return Cands{ctx->d_cand, ctx->d_cand + n, ctx->d_cand + 2 * n, ctx->d_cand + 3 * n, ctx->d_cflag,
+               ctx->d_touched, ctx->d_ctr + 4};
+}
+
+static int nextStamp(gbp_ctx* ctx) {
+  if (ctx->stamp >= 0x7ffffff0) {
+    cudaMemsetAsync(ctx->d_rowstamp, 0, (size_t)std::max<int64_t>(ctx->m, 1) * sizeof(int), ctx->stream);
+    ctx->stamp = 0;
+  }
+  return ++ctx->stamp;
+}
+
+static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
+                         const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
+  const Prob P = devProb(ctx);
+  const Num s = ctx->num;
+  Cands C = plainCands(ctx);
+  const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
+  int launches = 0;
+  CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_ctr, 0, 8 * sizeof(int), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+
+  int* cur = nullptr;
+  int curidx = 0;
+  int ns = 0, nl = 0;
+  if (nseed < 0) {
+    cur = ctx->d_allrows;
+    ns = ctx->nshort_all;
+    nl = ctx->nlong_all;
+    ctx->h_ctr[0] = ns;
+    ctx->h_ctr[1] = 0;
+    ctx->h_ctr[2] = nl;
+    ctx->h_ctr[3] = 0;
+    CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, 4 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    cur = ctx->d_list[0];
+    if (nseed > 0) {
+      Front F{cur, ctx->d_ctr + 0, ctx->d_ctr + 2, ctx->d_rowstamp, (int)ctx->m};
+      CK(launchSeed(ctx->stream, gridFor(ctx, nseed), P, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, F,
+                    nextStamp(ctx)));
+      ++launches;
+    }
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ns = ctx->h_ctr[0];
+    nl = ctx->h_ctr[2];
+  }
+
+  int rounds = 0, status = 0;
+  bool cut = false;
+  while (ns + nl > 0) {
+    if (rounds >= maxrounds) {
+      status = 2;
+      break;
+    }
+    const int nxt = curidx ^ 1;
+    int* nextlist = ctx->d_list[nxt];  // the current list is d_list[curidx] or the all-rows list
+    // reset next counters and the touched count
+    CK(cudaMemsetAsync(ctx->d_ctr + nxt, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_ctr + 2 + nxt, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_ctr + 4, 0, sizeof(int), ctx->stream));
+    if (ns > 0) {
+      CK(launchRowsShort(ctx->stream, gridFor(ctx, ns), s, P, lb, ub, cur, ctx->d_ctr + curidx, C, ctx->d_ctr + 5,
+                         ctx->d_stats));
+      ++launches;
+    }
+    if (nl > 0) {
+      CK(launchRowsLong(ctx->stream, gridFor(ctx, (int64_t)nl * 32), s, P, lb, ub, cur, ctx->d_ctr + 2 + curidx,
+                        (int)ctx->m, C, ctx->d_ctr + 5, ctx->d_stats));
+      ++launches;
+    }
+    Front F{nextlist, ctx->d_ctr + nxt, ctx->d_ctr + 2 + nxt, ctx->d_rowstamp, (int)ctx->m};
+    CK(launchApply(ctx->stream, gridFor(ctx, ctx->n, 256, 8), s, P, lb, ub, C, F, nextStamp(ctx), ctx->d_ctr + 5,
+                   ctx->d_stats));
+    ++launches;
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ++rounds;
+    if (ctx->h_ctr[5]) {
+      cut = true;
+      status = 1;
+      break;
+    }
+    cur = nextlist;
+    curidx = nxt;
+    ns = ctx->h_ctr[nxt];
+    nl = ctx->h_ctr[2 + nxt];
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  unsigned long long st[8];
+  CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (cutoff) *cutoff = cut ? 1 : 0;
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->cutoff = cut ? 1 : 0;
+    res->rounds = rounds;
+    res->status = status;
+    res->launches = launches;
+    res->rows = (int64_t)st[0];
+    res->nnz = (int64_t)st[1];
+    res->candidates = (int64_t)st[2];
+    res->changes = (int64_t)st[3];
+    res->kernel_ms = ms;
+  }
+  return status == 2 ? GBP_ERR_LIMIT : GBP_OK;
+}
+
+static int ensureSeedBuf(gbp_ctx* ctx, int64_t nseed) {
+  if (nseed <= ctx->seedcap) return GBP_OK;
+  if (ctx->d_seedcols) cudaFree(ctx->d_seedcols);
+  if (ctx->d_seedold) cudaFree(ctx->d_seedold);
+  ctx->d_seedcols = nullptr;
+  ctx->d_seedold = nullptr;
+  ctx->seedcap = 0;
+  CK(cudaMalloc(&ctx->d_seedcols, nseed * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->d_seedold, 2 * nseed * sizeof(double)));
+  ctx->seedcap = nseed;
+  return GBP_OK;
+}
+
+static int checkSeeds(gbp_ctx* ctx, int64_t nseed, const int32_t* cols, const double* oldlb, const double* oldub) {
+  if (nseed > 0 && (!cols || !oldlb || !oldub)) return fail(ctx, GBP_ERR_INVALID, "null seed arrays");
+  return GBP_OK;
+}
+
+int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols, const double* oldlb,
+                  const double* oldub, int32_t* cutoff, gbp_result* res) {
+  if (!ctx || !ctx->has_problem || !lb || !ub) return fail(ctx, GBP_ERR_INVALID, "no problem or null bounds");
+  int rc = checkSeeds(ctx, nseed, seedcols, oldlb, oldub);
+  if (rc) return rc;
+  for (int64_t k = 0; k < nseed; ++k)
+    if (seedcols[k] < 0 || seedcols[k] >= ctx->n) return fail(ctx, GBP_ERR_INVALID, "seed column out of range");
+  CK(cudaSetDevice(ctx->device));
+  const size_t nb = (size_t)ctx->n * sizeof(double);
+  if (nb) {
+    CK(cudaMemcpyAsync(ctx->d_lb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_ub, ub, nb, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (nseed > 0) {
+    rc = ensureSeedBuf(ctx, nseed);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_seedcols, seedcols, nseed * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_seedold, oldlb, nseed * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_seedold + nseed, oldub, nseed * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  rc = propagateCore(ctx, ctx->d_lb, ctx->d_ub, nseed, ctx->d_seedcols, ctx->d_seedold,
+                     ctx->d_seedold + (nseed > 0 ? nseed : 0), cutoff, res);
+  if (rc != GBP_OK && rc != GBP_ERR_LIMIT) return rc;
+  if (nb) {
+    CK(cudaMemcpyAsync(lb, ctx->d_lb, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ub, ctx->d_ub, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return rc;
+}
+
+int gbp_propagate_device(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols,
+                         const double* oldlb, const double* oldub, int32_t* cutoff, gbp_result* res) {
+  if (!ctx || !ctx->has_problem || (ctx->n > 0 && (!lb || !ub)))
+    return fail(ctx, GBP_ERR_INVALID, "no problem or null bounds");
+  int rc = checkSeeds(ctx, nseed, seedcols, oldlb, oldub);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device));
+  return propagateCore(ctx, lb, ub, nseed, seedcols, oldlb, oldub, cutoff, res);
+}
+
+int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double* act, int32_t* cnt) {
+  if (!ctx || !ctx->has_problem || !lb || !ub || !act || !cnt) return fail(ctx, GBP_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  const size_t nb = (size_t)ctx->n * sizeof(double);
+  const size_t m = (size_t)ctx->m;
+  double* d_act = nullptr;
+  int32_t* d_cnt = nullptr;
+  CK(cudaMalloc(&d_act, std::max<size_t>(m, 1) * 4 * sizeof(double)));
+  CK(cudaMalloc(&d_cnt, std::max<size_t>(m, 1) * 8 * sizeof(int32_t)));
+  if (nb) {
+    CK(cudaMemcpyAsync(ctx->d_lb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_ub, ub, nb, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(launchActivities(ctx->stream, gridFor(ctx, (int64_t)m, 256, 8), ctx->num, devProb(ctx), ctx->d_lb, ctx->d_ub,
+                      d_act, d_cnt));
+  if (m) {
+    CK(cudaMemcpyAsync(act, d_act, m * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(cnt, d_cnt, m * 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d_act);
+  cudaFree(d_cnt);
+  return GBP_OK;
+}
+
+// ------------------------------------------------------------------------------------------ batched path
+static int ensureSlots(gbp_ctx* ctx) {
+  if (ctx->slot_mem) return GBP_OK;
+  int occ = 0;
+  CK(nodesOccupancy(&occ));
+  int per_sm = ctx->ctas_per_sm > 0 ? std::min(ctx->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+  const int64_t ns = std::max<int64_t>(ctx->n, 1), ms = std::max<int64_t>(ctx->m, 1);
+  const size_t per_slot = (size_t)ns * (sizeof(double2) + sizeof(int) + 4 * sizeof(long long) + 3 * sizeof(int)) +
+                          (size_t)ms * 3 * sizeof(int) + 64 * 16;
+  size_t freeb = 0, totalb = 0;
+  CK(cudaMemGetInfo(&freeb, &totalb));
+  int64_t nslots = (int64_t)ctx->sms * per_sm;
+  const size_t budget = freeb / 3;
+  while (nslots > 1 && (size_t)nslots * per_slot > budget) nslots -= 1;
+  if ((size_t)nslots * per_slot > budget) return fail(ctx, GBP_ERR_NOMEM, "not enough device memory for one slot");
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  const size_t S = (size_t)nslots;
+  size_t o_ovl = off; off = align(off + S * ns * sizeof(double2));
+  size_t o_ost = off; off = align(off + S * ns * sizeof(int));
+  size_t o_cand = off; off = align(off + 4 * S * ns * sizeof(long long));
+  size_t o_cflag = off; off = align(off + S * ns * sizeof(int));
+  size_t o_touch = off; off = align(off + S * ns * sizeof(int));
+  size_t o_dirty = off; off = align(off + S * ns * sizeof(int));
+  size_t o_rst = off; off = align(off + S * ms * sizeof(int));
+  size_t o_la = off; off = align(off + S * ms * sizeof(int));
+  size_t o_lb = off; off = align(off + S * ms * sizeof(int));
+  size_t o_ctr = off; off = align(off + S * sizeof(int));
+  char* base = nullptr;
+  CK(cudaMalloc(&base, off));
+  ctx->slot_mem = base;
+  SlotArrays& A = ctx->slots;
+  A.nstride = ns;
+  A.mstride = ms;
+  A.ovl = (double2*)(base + o_ovl);
+  A.ostamp = (int*)(base + o_ost);
+  A.cub = (long long*)(base + o_cand);
+  A.clb = A.cub + S * ns;
+  A.cubf = A.clb + S * ns;
+  A.clbf = A.cubf + S * ns;
+  A.cflag = (int*)(base + o_cflag);
+  A.touched = (int*)(base + o_touch);
+  A.dirty = (int*)(base + o_dirty);
+  A.rowstamp = (int*)(base + o_rst);
+  A.listA = (int*)(base + o_la);
+  A.listB = (int*)(base + o_lb);
+  A.counter = (int*)(base + o_ctr);
+  CK(cudaMemsetAsync(A.ostamp, 0, S * ns * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(A.cflag, 0, S * ns * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(A.rowstamp, 0, S * ms * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(A.counter, 0, S * sizeof(int), ctx->stream));
+  CK(launchFill64(ctx->stream, ctx->sms * 8, A.cub, (int64_t)(S * ns), KEY_NONE_UB));
+  CK(launchFill64(ctx->stream, ctx->sms * 8, A.clb, (int64_t)(S * ns), KEY_NONE_LB));
+  CK(launchFill64(ctx->stream, ctx->sms * 8, A.cubf, (int64_t)(S * ns), KEY_NONE_UB));
+  CK(launchFill64(ctx->stream, ctx->sms * 8, A.clbf, (int64_t)(S * ns), KEY_NONE_LB));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->nslots = (int)nslots;
+  ctx->slot_stamp_budget = 0;
+  return GBP_OK;
+}
+
+int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
+                               const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+                               int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n,
+                               int32_t* out_col, double* out_lb, double* out_ub, int64_t out_cap, gbp_result* res) {
+  if (!ctx || !ctx->has_problem) return fail(ctx, GBP_ERR_INVALID, "no problem uploaded");
+  if (nnodes < 0 || nnodes >= (int64_t(1) << 31) - 1 || out_cap < 0) return fail(ctx, GBP_ERR_INVALID, "bad sizes");
+  if (nnodes == 0) {
+    if (res) std::memset(res, 0, sizeof(*res));
+    return GBP_OK;
+  }
+  if (!baselb || !baseub || !ptr || !out_cutoff || !out_rounds || !out_off || !out_n ||
+      (out_cap > 0 && (!out_col || !out_lb || !out_ub)))
+    return fail(ctx, GBP_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensureSlots(ctx);
+  if (rc) return rc;
+  const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
+  // stamp counters grow by (rounds + 1) per node and slot; re-zero the stamps long before they wrap
+  if (ctx->slot_stamp_budget > (int64_t(1) << 30)) {
+    const size_t S = (size_t)ctx->nslots;
+    CK(cudaMemsetAsync(ctx->slots.ostamp, 0, S * ctx->slots.nstride * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->slots.rowstamp, 0, S * ctx->slots.mstride * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->slots.counter, 0, S * sizeof(int), ctx->stream));
+    ctx->slot_stamp_budget = 0;
+  }
+  CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_next_item, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_out_used, 0, sizeof(unsigned long long), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launchPack(ctx->stream, gridFor(ctx, ctx->n), baselb, baseub, ctx->d_base, ctx->n));
+  NodesArgs A;
+  A.s = ctx->num;
+  A.P = devProb(ctx);
+  A.base = ctx->d_base;
+  A.nnodes = nnodes;
+  A.ptr = ptr;
+  A.chg_col = chg_col;
+  A.chg_lb = chg_lb;
+  A.chg_ub = chg_ub;
+  A.out_cutoff = out_cutoff;
+  A.out_rounds = out_rounds;
+  A.out_off = out_off;
+  A.out_n = out_n;
+  A.out_col = out_col;
+  A.out_lb = out_lb;
+  A.out_ub = out_ub;
+  A.out_cap = out_cap;
+  A.out_used = ctx->d_out_used;
+  A.maxrounds = maxrounds;
+  A.next_item = ctx->d_next_item;
+  A.S = ctx->slots;
+  A.stats = ctx->d_stats;
+  A.status = ctx->d_status;
+  const int grid = (int)std::min<int64_t>(ctx->nslots, nnodes);
+  CK(launchNodes(ctx->stream, grid, A));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  unsigned long long st[8];
+  int status = 0;
+  CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->slot_stamp_budget += (nnodes / std::max(grid, 1) + 1) * ((int64_t)st[5] + 2);
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->cutoff = (int32_t)st[4];
+    res->rounds = (int32_t)st[5];
+    res->status = (status & 1) ? 2 : 0;
+    res->launches = 2;
+    res->rows = (int64_t)st[0];
+    res->nnz = (int64_t)st[1];
+    res->candidates = (int64_t)st[2];
+    res->changes = (int64_t)st[3];
+    res->kernel_ms = ms;
+  }
+  if (status & 2) return fail(ctx, GBP_ERR_OVERFLOW, "node output arrays too small");
+  if (status & 1) return GBP_ERR_LIMIT;
+  return GBP_OK;
+}
+
+int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes, const int64_t* ptr,
+                        const int32_t* chg_col, const double* chg_lb, const double* chg_ub, int8_t* out_cutoff,
+                        int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
+                        double* out_ub, int64_t out_cap, gbp_result* res) {
+  if (!ctx || !ctx->has_problem) return fail(ctx, GBP_ERR_INVALID, "no problem uploaded");
+  if (nnodes < 0 || out_cap < 0) return fail(ctx, GBP_ERR_INVALID, "bad sizes");
+  if (nnodes == 0) {
+    if (res) std::memset(res, 0, sizeof(*res));
+    return GBP_OK;
+  }
+  if (!baselb || !baseub || !ptr || !out_cutoff || !out_rounds || !out_off || !out_n ||
+      (out_cap > 0 && (!out_col || !out_lb || !out_ub)))
+    return fail(ctx, GBP_ERR_INVALID, "null argument");
+  if (ptr[0] != 0) return fail(ctx, GBP_ERR_INVALID, "ptr[0] must be 0");
+  for (int64_t k = 0; k < nnodes; ++k)
+    if (ptr[k + 1] < ptr[k]) return fail(ctx, GBP_ERR_INVALID, "ptr not monotone");
+  const int64_t nchg = ptr[nnodes];
+  if (nchg > 0 && (!chg_col || !chg_lb || !chg_ub)) return fail(ctx, GBP_ERR_INVALID, "null change arrays");
+  for (int64_t q = 0; q < nchg; ++q)
+    if (chg_col[q] < 0 || chg_col[q] >= ctx->n) return fail(ctx, GBP_ERR_INVALID, "change column out of range");
+  CK(cudaSetDevice(ctx->device));
+  // one staging allocation for inputs and outputs
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t n = (size_t)ctx->n;
+  size_t off = 0;
+  const size_t o_blb = off; off = al(off + n * 8);
+  const size_t o_bub = off; off = al(off + n * 8);
+  const size_t o_ptr = off; off = al(off + (nnodes + 1) * 8);
+  const size_t o_col = off; off = al(off + nchg * 4);
+  const size_t o_clb = off; off = al(off + nchg * 8);
+  const size_t o_cub = off; off = al(off + nchg * 8);
+  const size_t o_cut = off; off = al(off + nnodes);
+  const size_t o_rnd = off; off = al(off + nnodes * 4);
+  const size_t o_off = off; off = al(off + nnodes * 8);
+  const size_t o_n = off; off = al(off + nnodes * 4);
+  const size_t o_ocol = off; off = al(off + out_cap * 4);
+  const size_t o_olb = off; off = al(off + out_cap * 8);
+  const size_t o_oub = off; off = al(off + out_cap * 8);
+  if (off > ctx->stage_bytes) {
+    if (ctx->stage) cudaFree(ctx->stage);
+    ctx->stage = nullptr;
+    ctx->stage_bytes = 0;
+    CK(cudaMalloc(&ctx->stage, off));
+    ctx->stage_bytes = off;
+  }
+  char* b = (char*)ctx->stage;
+  CK(cudaMemcpyAsync(b + o_blb, baselb, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(b + o_bub, baseub, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(b + o_ptr, ptr, (nnodes + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+  if (nchg) {
+    CK(cudaMemcpyAsync(b + o_col, chg_col, nchg * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(b + o_clb, chg_lb, nchg * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(b + o_cub, chg_ub, nchg * 8, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  int rc = gbp_propagate_nodes_device(ctx, (double*)(b + o_blb), (double*)(b + o_bub), nnodes, (int64_t*)(b + o_ptr),
+                                      (int32_t*)(b + o_col), (double*)(b + o_clb), (double*)(b + o_cub),
+                                      (int8_t*)(b + o_cut), (int32_t*)(b + o_rnd), (int64_t*)(b + o_off),
+                                      (int32_t*)(b + o_n), (int32_t*)(b + o_ocol), (double*)(b + o_olb),
+                                      (double*)(b + o_oub), out_cap, res);
+  if (rc != GBP_OK && rc != GBP_ERR_LIMIT && rc != GBP_ERR_OVERFLOW) return rc;
+  unsigned long long used = 0;
+  CK(cudaMemcpyAsync(&used, ctx->d_out_used, sizeof(used), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out_cutoff, b + o_cut, nnodes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out_rounds, b + o_rnd, nnodes * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out_off, b + o_off, nnodes * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out_n, b + o_n, nnodes * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t cnt = (size_t)std::min<unsigned long long>(used, (unsigned long long)out_cap);
+  if (cnt) {
+    CK(cudaMemcpyAsync(out_col, b + o_ocol, cnt * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_lb, b + o_olb, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_ub, b + o_oub, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return rc;
+}
+
+}  // extern "C"

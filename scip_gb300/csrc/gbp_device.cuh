@@ -1,0 +1,406 @@
+// Device procedures shared by the plain (one problem per launch sequence) and the batched (persistent,
+// one CTA per node) propagation paths.
+//
+// One propagation round, for the rows of the current frontier and the bounds B_r at its start:
+//   rowThread / rowWarp   activity + cutoff test + candidate bounds of every frontier row
+//                         (propagateCons -> tightenBounds -> tightenVarBounds[Easy], cons_linear.c)
+//   applyColumn           per touched column, SCIP's acceptance of the best candidates against B_r
+//                         (SCIPinferVarUbCons / SCIPinferVarLbCons, scip_var.c:7071 / 6965)
+//   expandColumn          rows that the accepted change makes worth re-tightening
+//                         (eventExecLinear, cons_linear.c:17226-17255)
+// Candidate bounds meet in per-column slots through atomicMin / atomicMax on order-preserving int64 keys,
+// so the result does not depend on the order in which rows run.
+#pragma once
+
+#include "gbp_rules.cuh"
+
+namespace gbp {
+
+constexpr int LONGROW = 64;  // rows longer than this are summed as 32 interleaved partials (warp per row)
+constexpr long long KEY_NONE_UB = 0x7fffffffffffffffLL;       // empty upper-bound candidate slot
+constexpr long long KEY_NONE_LB = (long long)0x8000000000000000ULL;  // empty lower-bound candidate slot
+constexpr uint32_t CSC_LBUP = 1u << 30;    // row uses a raised lower bound of this column
+constexpr uint32_t CSC_UBDOWN = 1u << 31;  // row uses a lowered upper bound of this column
+constexpr uint32_t CSC_ROW = (1u << 30) - 1u;
+
+struct Prob {
+  int64_t m, n;
+  const int64_t* rowptr;
+  const int32_t* colidx;
+  const double* vals;
+  const double* lhs;
+  const double* rhs;
+  const int8_t* isint;
+  const int64_t* colptr;
+  const uint32_t* cscrow;  // row index | CSC_LBUP | CSC_UBDOWN
+};
+
+struct Cands {
+  long long* cub;   // best non-forced upper bound candidate (key), KEY_NONE_UB when empty
+  long long* clb;   // best non-forced lower bound candidate (key), KEY_NONE_LB when empty
+  long long* cubf;  // forced (single-entry row) candidates
+  long long* clbf;
+  int* cflag;       // bit0 ub, bit1 ubf, bit2 lb, bit3 lbf; 0 when the column is untouched this round
+  int* touched;     // list of touched columns
+  int* ntouched;    // its length (global or shared counter)
+};
+
+struct Stats {
+  long long rows, nnz, cands;
+};
+
+// frontier lists: short rows from the front of `list`, long rows from the back
+struct Front {
+  int* list;
+  int* nshort;
+  int* nlong;
+  int* rowstamp;
+  int cap;  // = m
+};
+
+__device__ __forceinline__ void emitUb(Cands& C, int j, double v, bool force) {
+  atomicMin(force ? &C.cubf[j] : &C.cub[j], dkey(v));
+  int old = atomicOr(&C.cflag[j], force ? 2 : 1);
+  if (old == 0) C.touched[atomicAdd(C.ntouched, 1)] = j;
+}
+__device__ __forceinline__ void emitLb(Cands& C, int j, double v, bool force) {
+  atomicMax(force ? &C.clbf[j] : &C.clb[j], dkey(v));
+  int old = atomicOr(&C.cflag[j], force ? 8 : 4);
+  if (old == 0) C.touched[atomicAdd(C.ntouched, 1)] = j;
+}
+
+__device__ __forceinline__ void pushRow(const Prob& P, Front& F, int row, int stamp) {
+  if (atomicExch(&F.rowstamp[row], stamp) != stamp) {
+    int64_t len = P.rowptr[row + 1] - P.rowptr[row];
+    if (len <= LONGROW) F.list[atomicAdd(F.nshort, 1)] = row;
+    else F.list[F.cap - 1 - atomicAdd(F.nlong, 1)] = row;
+  }
+}
+
+// rows of column j made relevant by a raised lower bound (lbup) and/or a lowered upper bound (ubdown)
+__device__ __forceinline__ void expandColumn(const Prob& P, Front& F, int j, bool lbup, bool ubdown, int stamp) {
+  uint32_t need = (lbup ? CSC_LBUP : 0u) | (ubdown ? CSC_UBDOWN : 0u);
+  for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+    uint32_t e = P.cscrow[q];
+    if (e & need) pushRow(P, F, (int)(e & CSC_ROW), stamp);
+  }
+}
+
+// Candidate bounds of column j (entry val) in a row with activity a, under bounds [l,u]:
+// tightenVarBoundsEasy (cons_linear.c:5380-5653) when `easy`, else tightenVarBounds (:6700-6974).
+// `relres` recomputes a residual in plain double (consdataGetReliableResidualActivity, :2580-2657).
+// Returns true if the row proves infeasibility (easy rule only).
+template <class RELRES>
+__device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, double lhs, double rhs, bool easy,
+                                                 bool force, int j, double val, double l, double u, bool isint,
+                                                 Cands& C, long long& ncand, const RELRES& relres) {
+  if (easy) {
+    double minact = a.minhi + a.minlo;
+    double maxact = a.maxhi + a.maxlo;
+    if (!isInf(s, rhs)) {
+      if (feasLt(s, rhs, minact)) return true;
+      double slack = rhs - minact;
+      if (!positive(s, slack)) slack = 0.0;
+      double alpha = val > 0.0 ? val * (u - l) : val * (l - u);
+      if (sumGt(s, alpha, slack) || (force && gt(s, alpha, slack))) {
+        if (val > 0.0) {
+          double nb = adjUb(s, isint, l + slack / val);  // tightenVarUb, cons_linear.c:5242
+          if (force || ubBetter(s, nb, l, u)) { emitUb(C, j, nb, force); ++ncand; }
+        } else {
+          double nb = adjLb(s, isint, u + slack / val);  // tightenVarLb, cons_linear.c:5307
+          if (force || lbBetter(s, nb, l, u)) { emitLb(C, j, nb, force); ++ncand; }
+        }
+      }
+    }
+    if (!isInf(s, -lhs)) {
+      if (feasLt(s, maxact, lhs)) return true;
+      double slack = maxact - lhs;
+      if (!positive(s, slack)) slack = 0.0;
+      double alpha = val > 0.0 ? val * (u - l) : val * (l - u);
+      if (sumGt(s, alpha, slack) || (force && gt(s, alpha, slack))) {
+        if (val > 0.0) {
+          double nb = adjLb(s, isint, u - slack / val);
+          if (force || lbBetter(s, nb, l, u)) { emitLb(C, j, nb, force); ++ncand; }
+        } else {
+          double nb = adjUb(s, isint, l - slack / val);
+          if (force || ubBetter(s, nb, l, u)) { emitUb(C, j, nb, force); ++ncand; }
+        }
+      }
+    }
+    return false;
+  }
+
+  double minres, maxres;
+  bool mintight, maxtight, mininf, maxinf;
+  residuals(s, a, val, l, u, minres, maxres, mintight, maxtight, mininf, maxinf);
+  bool rhsok = !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !eq(s, minres / rhs, 1.0));
+  bool lhsok = !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !eq(s, maxres / lhs, 1.0));
+  if (val > 0.0) {
+    if (rhsok) {
+      double newub = (rhs - minres) / val;
+      if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
+        bool unrel = updateUnreliable(s, minres, a.minhi + a.minlo);
+        if (unrel) {
+          minres = relres(true);
+          newub = (rhs - minres) / val;
+          unrel = isInf(s, -minres) ||
+                  (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
+        }
+        if (!unrel) { emitUb(C, j, newub, force); ++ncand; }
+      }
+    }
+    if (lhsok) {
+      double newlb = (lhs - maxres) / val;
+      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+        bool skip = false;
+        if (updateUnreliable(s, maxres, a.maxhi + a.maxlo)) {
+          maxres = relres(false);
+          newlb = (lhs - maxres) / val;
+          skip = isInf(s, maxres) ||
+                 (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
+        }
+        if (!skip) { emitLb(C, j, newlb, force); ++ncand; }
+      }
+    }
+  } else {
+    if (rhsok) {
+      double newlb = (rhs - minres) / val;
+      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+        bool unrel = updateUnreliable(s, minres, a.minhi + a.minlo);
+        if (unrel) {
+          minres = relres(true);
+          newlb = (rhs - minres) / val;
+          unrel = isInf(s, -minres) ||
+                  (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
+        }
+        if (!unrel) { emitLb(C, j, newlb, force); ++ncand; }
+      }
+    }
+    if (lhsok) {
+      double newub = (lhs - maxres) / val;
+      if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
+        bool skip = false;
+        if (updateUnreliable(s, maxres, a.maxhi + a.maxlo)) {
+          maxres = relres(false);
+          newub = (lhs - maxres) / val;
+          // this branch of SCIP joins its conditions with && (cons_linear.c:6936-6938)
+          skip = isInf(s, maxres) ||
+                 (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) && !isint) && (!force || !lt(s, newub, u)));
+        }
+        if (!skip) { emitUb(C, j, newub, force); ++ncand; }
+      }
+    }
+  }
+  return false;
+}
+
+// Row-level tests before candidates: infeasibility with relaxed huge contributions (propagateCons,
+// cons_linear.c:7718-7740), canTightenBounds (:5214-5238), all-fixed and maximal-activity-delta skips
+// (tightenBounds, :7050-7083).  Returns 1 = cutoff, 0 = skip row, 2 = generate candidates.
+__device__ __forceinline__ int rowTests(const Num& s, const Act& a, double lhs, double rhs, double maxactdelta,
+                                        bool& easy) {
+  double minact, maxact;
+  bool t1, t2, f1, f2;
+  getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, true, minact, t1, f1);
+  getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, true, maxact, t2, f2);
+  if (feasGt(s, minact, rhs) || feasLt(s, maxact, lhs)) return 1;
+  if (a.minneginf + a.minposinf + a.minneghuge + a.minposhuge > 1 &&
+      a.maxneginf + a.maxposinf + a.maxneghuge + a.maxposhuge > 1)
+    return 0;
+  if (feasZero(s, maxactdelta)) return 0;
+  if (!isInf(s, maxactdelta)) {
+    getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, false, minact, t1, f1);
+    getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, false, maxact, t2, f2);
+    double slack = (isInf(s, rhs) || f1) ? s.inf : rhs - minact;
+    double surplus = (isInf(s, -lhs) || f2) ? s.inf : maxact - lhs;
+    if (le(s, maxactdelta, dmin(slack, surplus))) return 0;
+  }
+  easy = lt(s, maxactdelta, s.maxeasy);
+  return 2;
+}
+
+// maximal activity contribution of one entry (consdataRecomputeMaxActivityDelta, cons_linear.c:1542-1599);
+// returns -1 for an infinite bound
+__device__ __forceinline__ double entryDelta(const Num& s, double val, double l, double u) {
+  if (isInf(s, -l) || isInf(s, u)) return -1.0;
+  return fabs(val) * (u - l);
+}
+
+// One frontier row of at most LONGROW entries, processed by a single thread.  Returns true on cutoff.
+template <class BND>
+__device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+  const double lhs = P.lhs[i], rhs = P.rhs[i];
+  Act a;
+  actZero(a);
+  double mad = 0.0;
+  bool madinf = false;
+  for (int64_t p = p0; p < p1; ++p) {
+    int j = P.colidx[p];
+    double v = P.vals[p];
+    double l, u;
+    B.get(j, l, u);
+    addTerm(s, a, v, l, u);
+    double d = entryDelta(s, v, l, u);
+    if (d < 0.0) madinf = true;
+    else if (d > mad) mad = d;
+  }
+  st.rows += 1;
+  st.nnz += p1 - p0;
+  bool easy = false;
+  int t = rowTests(s, a, lhs, rhs, madinf ? s.inf : mad, easy);
+  if (t == 1) return true;
+  if (t == 0) return false;
+  const bool force = (p1 - p0 == 1);
+  for (int64_t p = p0; p < p1; ++p) {
+    int j = P.colidx[p];
+    double v = P.vals[p];
+    double l, u;
+    B.get(j, l, u);
+    auto relres = [&](bool ismin) {
+      double r = 0.0;
+      for (int64_t q = p0; q < p1; ++q) {
+        if (q == p) continue;
+        int jj = P.colidx[q];
+        double vv = P.vals[q], ll, uu;
+        B.get(jj, ll, uu);
+        if (vv > 0.0) r += ismin ? vv * ll : vv * uu;
+        else r += ismin ? vv * uu : vv * ll;
+      }
+      return r;
+    };
+    if (columnCandidates(s, a, lhs, rhs, easy, force, j, v, l, u, P.isint[j] != 0, C, st.cands, relres))
+      return true;
+  }
+  return false;
+}
+
+// One frontier row longer than LONGROW, processed by a whole warp: lane k sums entries k, k+32, ... and the
+// 32 partials are merged pairwise (k absorbs k+16, k+8, ..., k+1) -- the same order the oracle uses.
+// Returns true (on every lane) on cutoff.
+template <class BND>
+__device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+  const int lane = threadIdx.x & 31;
+  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+  const double lhs = P.lhs[i], rhs = P.rhs[i];
+  Act a;
+  actZero(a);
+  double mad = 0.0;
+  bool madinf = false;
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    int j = P.colidx[p];
+    double v = P.vals[p];
+    double l, u;
+    B.get(j, l, u);
+    addTerm(s, a, v, l, u);
+    double d = entryDelta(s, v, l, u);
+    if (d < 0.0) madinf = true;
+    else if (d > mad) mad = d;
+  }
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    Act b;
+    b.minhi = __shfl_down_sync(0xffffffffu, a.minhi, off);
+    b.minlo = __shfl_down_sync(0xffffffffu, a.minlo, off);
+    b.maxhi = __shfl_down_sync(0xffffffffu, a.maxhi, off);
+    b.maxlo = __shfl_down_sync(0xffffffffu, a.maxlo, off);
+    b.minposinf = __shfl_down_sync(0xffffffffu, a.minposinf, off);
+    b.minneginf = __shfl_down_sync(0xffffffffu, a.minneginf, off);
+    b.minposhuge = __shfl_down_sync(0xffffffffu, a.minposhuge, off);
+    b.minneghuge = __shfl_down_sync(0xffffffffu, a.minneghuge, off);
+    b.maxposinf = __shfl_down_sync(0xffffffffu, a.maxposinf, off);
+    b.maxneginf = __shfl_down_sync(0xffffffffu, a.maxneginf, off);
+    b.maxposhuge = __shfl_down_sync(0xffffffffu, a.maxposhuge, off);
+    b.maxneghuge = __shfl_down_sync(0xffffffffu, a.maxneghuge, off);
+    double dm = __shfl_down_sync(0xffffffffu, mad, off);
+    if (lane < off) {
+      actMerge(a, b);
+      if (dm > mad) mad = dm;
+    }
+  }
+  a.minhi = __shfl_sync(0xffffffffu, a.minhi, 0);
+  a.minlo = __shfl_sync(0xffffffffu, a.minlo, 0);
+  a.maxhi = __shfl_sync(0xffffffffu, a.maxhi, 0);
+  a.maxlo = __shfl_sync(0xffffffffu, a.maxlo, 0);
+  a.minposinf = __shfl_sync(0xffffffffu, a.minposinf, 0);
+  a.minneginf = __shfl_sync(0xffffffffu, a.minneginf, 0);
+  a.minposhuge = __shfl_sync(0xffffffffu, a.minposhuge, 0);
+  a.minneghuge = __shfl_sync(0xffffffffu, a.minneghuge, 0);
+  a.maxposinf = __shfl_sync(0xffffffffu, a.maxposinf, 0);
+  a.maxneginf = __shfl_sync(0xffffffffu, a.maxneginf, 0);
+  a.maxposhuge = __shfl_sync(0xffffffffu, a.maxposhuge, 0);
+  a.maxneghuge = __shfl_sync(0xffffffffu, a.maxneghuge, 0);
+  mad = __shfl_sync(0xffffffffu, mad, 0);
+  madinf = __any_sync(0xffffffffu, madinf);
+  if (lane == 0) {
+    st.rows += 1;
+    st.nnz += p1 - p0;
+  }
+  bool easy = false;
+  int t = rowTests(s, a, lhs, rhs, madinf ? s.inf : mad, easy);
+  if (t == 1) return true;
+  if (t == 0) return false;
+  bool cut = false;
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    int j = P.colidx[p];
+    double v = P.vals[p];
+    double l, u;
+    B.get(j, l, u);
+    auto relres = [&](bool ismin) {
+      double r = 0.0;
+      for (int64_t q = p0; q < p1; ++q) {
+        if (q == p) continue;
+        int jj = P.colidx[q];
+        double vv = P.vals[q], ll, uu;
+        B.get(jj, ll, uu);
+        if (vv > 0.0) r += ismin ? vv * ll : vv * uu;
+        else r += ismin ? vv * uu : vv * ll;
+      }
+      return r;
+    };
+    if (columnCandidates(s, a, lhs, rhs, easy, false, j, v, l, u, P.isint[j] != 0, C, st.cands, relres)) {
+      cut = true;
+      break;
+    }
+  }
+  return __any_sync(0xffffffffu, cut);
+}
+
+// Acceptance of column j's best candidates against its round-start bounds [l,u]: upper bound first
+// (SCIPinferVarUbCons: adjust, infeasible if FeasLT(new, lb), clamp, accept if UbBetter or forced), then the
+// lower bound against the new upper bound (SCIPinferVarLbCons).  Resets the candidate slots.
+// Returns true on cutoff; nl/nu receive the new bounds.
+__device__ __forceinline__ bool applyColumn(const Num& s, bool isint, double l, double u, Cands& C, int j,
+                                            double& nl, double& nu) {
+  const int f = C.cflag[j];
+  const long long kub = C.cub[j], kubf = C.cubf[j], klb = C.clb[j], klbf = C.clbf[j];
+  C.cflag[j] = 0;
+  C.cub[j] = KEY_NONE_UB;
+  C.cubf[j] = KEY_NONE_UB;
+  C.clb[j] = KEY_NONE_LB;
+  C.clbf[j] = KEY_NONE_LB;
+  nu = u;
+  nl = l;
+  bool cut = false;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const bool force = (k == 1);
+    if (!(f & (force ? 2 : 1))) continue;
+    double c = adjUb(s, isint, keyd(force ? kubf : kub));
+    if (isInf(s, -c) || feasLt(s, c, l)) { cut = true; continue; }
+    c = dmax(c, l);
+    if (force ? !ge(s, c, u) : ubBetter(s, c, l, u)) nu = dmin(nu, c);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const bool force = (k == 1);
+    if (!(f & (force ? 8 : 4))) continue;
+    double c = adjLb(s, isint, keyd(force ? klbf : klb));
+    if (isInf(s, c) || feasGt(s, c, nu)) { cut = true; continue; }
+    c = dmin(c, nu);
+    if (force ? !le(s, c, l) : lbBetter(s, c, l, nu)) nl = dmax(nl, c);
+  }
+  return cut;
+}
+
+}  // namespace gbp

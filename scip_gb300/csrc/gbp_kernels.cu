@@ -1,0 +1,420 @@
+// Propagation kernels for sm_103a (FP64, sparse, no tensor cores).
+//
+// Plain path (one problem, one launch sequence per round):
+//   k_rows_short  one thread per frontier row of <= LONGROW entries
+//   k_rows_long   one warp per longer frontier row
+//   k_apply       one thread per touched column: acceptance, bound write, frontier expansion
+// Batched path:
+//   k_nodes       persistent; each CTA takes branch-and-bound nodes off a queue and runs a node's whole
+//                 fixpoint with CTA-wide barriers between the phases of a round.  A node's bounds are the
+//                 shared base vector plus a per-CTA overlay (ovl/ostamp), so nodes cost what they touch.
+#include "gbp_internal.h"
+
+namespace gbp {
+
+struct PlainBnd {
+  const double* lb;
+  const double* ub;
+  __device__ __forceinline__ void get(int j, double& l, double& u) const {
+    l = lb[j];
+    u = ub[j];
+  }
+};
+
+struct OvlBnd {
+  const double2* base;
+  double2* ovl;
+  int* ostamp;
+  int epoch;
+  __device__ __forceinline__ void get(int j, double& l, double& u) const {
+    double2 b = (ostamp[j] == epoch) ? ovl[j] : base[j];
+    l = b.x;
+    u = b.y;
+  }
+};
+
+__device__ __forceinline__ void flushStats(unsigned long long* stats, const Stats& st) {
+  if (st.rows) atomicAdd(&stats[0], (unsigned long long)st.rows);
+  if (st.nnz) atomicAdd(&stats[1], (unsigned long long)st.nnz);
+  if (st.cands) atomicAdd(&stats[2], (unsigned long long)st.cands);
+}
+
+// ------------------------------------------------------------------------------------------ plain path
+__global__ void __launch_bounds__(256) k_rows_short(Num s, Prob P, PlainBnd B, const int* list, const int* nshort,
+                                                    Cands C, int* cutoff, unsigned long long* stats) {
+  Stats st{0, 0, 0};
+  const int n = *nshort;
+  bool cut = false;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    cut |= rowThread(s, P, B, list[t], C, st);
+  if (cut) atomicExch(cutoff, 1);
+  flushStats(stats, st);
+}
+
+__global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
+                                                   int cap, Cands C, int* cutoff, unsigned long long* stats) {
+  Stats st{0, 0, 0};
+  const int n = *nlong;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  bool cut = false;
+  for (int w = warp; w < n; w += nwarps) cut |= rowWarp(s, P, B, list[cap - 1 - w], C, st);
+  if (cut && lane == 0) atomicExch(cutoff, 1);
+  flushStats(stats, st);
+}
+
+__global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double* ub, Cands C, Front F, int stamp,
+                                               int* cutoff, unsigned long long* stats) {
+  const int n = *C.ntouched;
+  unsigned long long changes = 0;
+  bool cut = false;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int j = C.touched[t];
+    double l = lb[j], u = ub[j], nl, nu;
+    if (applyColumn(s, P.isint[j] != 0, l, u, C, j, nl, nu)) {
+      cut = true;
+      continue;
+    }
+    bool lbup = nl > l, ubdown = nu < u;
+    if (lbup || ubdown) {
+      lb[j] = nl;
+      ub[j] = nu;
+      changes += (unsigned long long)lbup + (unsigned long long)ubdown;
+      expandColumn(P, F, j, lbup, ubdown, stamp);
+    }
+  }
+  if (cut) atomicExch(cutoff, 1);
+  if (changes) atomicAdd(&stats[3], changes);
+}
+
+__global__ void k_seed(Prob P, const double* lb, const double* ub, int64_t nseed, const int32_t* cols,
+                       const double* oldlb, const double* oldub, Front F, int stamp) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nseed; k += (int64_t)gridDim.x * blockDim.x) {
+    int j = cols[k];
+    expandColumn(P, F, j, lb[j] > oldlb[k], ub[j] < oldub[k], stamp);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_activities(Num s, Prob P, PlainBnd B, double* act, int32_t* cnt) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  // warp per 32 rows for short rows (one lane each), warp per row for long rows -- the summation orders
+  // of rowThread / rowWarp
+  for (int64_t base = (int64_t)warp * 32; base < P.m; base += (int64_t)nwarps * 32) {
+    int64_t i = base + lane;
+    bool mine = i < P.m && (P.rowptr[i + 1] - P.rowptr[i]) <= LONGROW;
+    Act a;
+    actZero(a);
+    if (mine) {
+      for (int64_t p = P.rowptr[i]; p < P.rowptr[i + 1]; ++p) {
+        int j = P.colidx[p];
+        double l, u;
+        B.get(j, l, u);
+        addTerm(s, a, P.vals[p], l, u);
+      }
+    }
+    unsigned longmask = __ballot_sync(0xffffffffu, i < P.m && !mine);
+    while (longmask) {
+      int src = __ffs(longmask) - 1;
+      longmask &= longmask - 1;
+      int64_t r = base + src;
+      Act b;
+      actZero(b);
+      for (int64_t p = P.rowptr[r] + lane; p < P.rowptr[r + 1]; p += 32) {
+        int j = P.colidx[p];
+        double l, u;
+        B.get(j, l, u);
+        addTerm(s, b, P.vals[p], l, u);
+      }
+#pragma unroll
+      for (int off = 16; off >= 1; off >>= 1) {
+        Act c;
+        c.minhi = __shfl_down_sync(0xffffffffu, b.minhi, off);
+        c.minlo = __shfl_down_sync(0xffffffffu, b.minlo, off);
+        c.maxhi = __shfl_down_sync(0xffffffffu, b.maxhi, off);
+        c.maxlo = __shfl_down_sync(0xffffffffu, b.maxlo, off);
+        c.minposinf = __shfl_down_sync(0xffffffffu, b.minposinf, off);
+        c.minneginf = __shfl_down_sync(0xffffffffu, b.minneginf, off);
+        c.minposhuge = __shfl_down_sync(0xffffffffu, b.minposhuge, off);
+        c.minneghuge = __shfl_down_sync(0xffffffffu, b.minneghuge, off);
+        c.maxposinf = __shfl_down_sync(0xffffffffu, b.maxposinf, off);
+        c.maxneginf = __shfl_down_sync(0xffffffffu, b.maxneginf, off);
+        c.maxposhuge = __shfl_down_sync(0xffffffffu, b.maxposhuge, off);
+        c.maxneghuge = __shfl_down_sync(0xffffffffu, b.maxneghuge, off);
+        if (lane < off) actMerge(b, c);
+      }
+      if (lane == 0) {
+        act[4 * r + 0] = b.minhi; act[4 * r + 1] = b.minlo; act[4 * r + 2] = b.maxhi; act[4 * r + 3] = b.maxlo;
+        cnt[8 * r + 0] = b.minposinf; cnt[8 * r + 1] = b.minneginf; cnt[8 * r + 2] = b.minposhuge;
+        cnt[8 * r + 3] = b.minneghuge; cnt[8 * r + 4] = b.maxposinf; cnt[8 * r + 5] = b.maxneginf;
+        cnt[8 * r + 6] = b.maxposhuge; cnt[8 * r + 7] = b.maxneghuge;
+      }
+    }
+    if (mine) {
+      act[4 * i + 0] = a.minhi; act[4 * i + 1] = a.minlo; act[4 * i + 2] = a.maxhi; act[4 * i + 3] = a.maxlo;
+      cnt[8 * i + 0] = a.minposinf; cnt[8 * i + 1] = a.minneginf; cnt[8 * i + 2] = a.minposhuge;
+      cnt[8 * i + 3] = a.minneghuge; cnt[8 * i + 4] = a.maxposinf; cnt[8 * i + 5] = a.maxneginf;
+      cnt[8 * i + 6] = a.maxposhuge; cnt[8 * i + 7] = a.maxneghuge;
+    }
+  }
+}
+
+__global__ void k_pack(const double* lb, const double* ub, double2* out, int64_t n) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = make_double2(lb[j], ub[j]);
+}
+
+__global__ void k_fill64(long long* p, int64_t n, long long v) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+    p[j] = v;
+}
+
+// relevance flags of each CSC entry (which bound moves of the column the row can use)
+__global__ void k_csc_flags(int64_t nnz, const double* cvals, const int32_t* rowidx, const double* lhs,
+                            const double* rhs, double inf, uint32_t* out) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+    int i = rowidx[q];
+    double a = cvals[q];
+    bool rhsfin = !(rhs[i] >= inf);
+    bool lhsfin = !(-lhs[i] >= inf);
+    uint32_t e = (uint32_t)i;
+    if (a > 0.0 ? rhsfin : lhsfin) e |= CSC_LBUP;
+    if (a > 0.0 ? lhsfin : rhsfin) e |= CSC_UBDOWN;
+    out[q] = e;
+  }
+}
+
+// ------------------------------------------------------------------------------------------ batched path
+__device__ __forceinline__ void ovlSet(const OvlBnd& B, int* dirty, int* ndirty, int j, double l, double u) {
+  if (B.ostamp[j] != B.epoch) {
+    B.ostamp[j] = B.epoch;
+    dirty[atomicAdd(ndirty, 1)] = j;
+  }
+  B.ovl[j] = make_double2(l, u);
+}
+
+__global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
+  __shared__ int s_item, s_cut, s_ns[2], s_nl[2], s_ntouched, s_ndirty, s_nout, s_rounds, s_epoch, s_rstamp;
+  __shared__ long long s_off;
+  __shared__ unsigned long long s_changes;
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  constexpr int NW = NODE_THREADS / 32;
+  const SlotArrays& S = A.S;
+  const int64_t ns = S.nstride, ms = S.mstride;
+  const size_t slot = blockIdx.x;
+  double2* ovl = S.ovl + slot * ns;
+  int* ostamp = S.ostamp + slot * ns;
+  int* touched = S.touched + slot * ns;
+  int* dirty = S.dirty + slot * ns;
+  int* lists[2] = {S.listA + slot * ms, S.listB + slot * ms};
+  int* rowstamp = S.rowstamp + slot * ms;
+  Cands C;
+  C.cub = S.cub + slot * ns;
+  C.clb = S.clb + slot * ns;
+  C.cubf = S.cubf + slot * ns;
+  C.clbf = S.clbf + slot * ns;
+  C.cflag = S.cflag + slot * ns;
+  C.touched = touched;
+  C.ntouched = &s_ntouched;
+  const int m = (int)A.P.m;
+
+  int counter = 0;
+  if (tid == 0) counter = S.counter[slot];
+  Stats st{0, 0, 0};
+  unsigned long long mycut = 0, mymaxr = 0;
+
+  for (;;) {
+    if (tid == 0) {
+      s_item = atomicAdd(A.next_item, 1);
+      s_epoch = ++counter;
+      s_cut = 0;
+      s_ns[0] = s_nl[0] = s_ns[1] = s_nl[1] = 0;
+      s_ndirty = 0;
+      s_nout = 0;
+      s_rounds = 0;
+      s_changes = 0;
+    }
+    __syncthreads();
+    const int item = s_item;
+    if (item >= A.nnodes) break;
+    OvlBnd B{A.base, ovl, ostamp, s_epoch};
+
+    // branching bound changes of the node, then the rows they make relevant
+    {
+      Front F{lists[0], &s_ns[0], &s_nl[0], rowstamp, m};
+      for (int64_t q = A.ptr[item] + tid; q < A.ptr[item + 1]; q += NODE_THREADS) {
+        int j = A.chg_col[q];
+        double nl = A.chg_lb[q], nu = A.chg_ub[q];
+        double l0, u0;
+        B.get(j, l0, u0);
+        if (nl > u0 || nu < l0) {
+          s_cut = 1;
+        } else if (nl > l0 || nu < u0) {
+          ovlSet(B, dirty, &s_ndirty, j, nl > l0 ? nl : l0, nu < u0 ? nu : u0);
+          expandColumn(A.P, F, j, nl > l0, nu < u0, B.epoch);
+        }
+      }
+    }
+    __syncthreads();
+
+    int r = 0;
+    while (!s_cut) {
+      const int cur = r & 1, nxt = cur ^ 1;
+      const int nsh = s_ns[cur], nlo = s_nl[cur];
+      if (nsh + nlo == 0) break;
+      if (r >= A.maxrounds) {
+        if (tid == 0) atomicOr(A.status, 1);
+        break;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        s_ns[nxt] = 0;
+        s_nl[nxt] = 0;
+        s_ntouched = 0;
+        s_rstamp = ++counter;
+        s_rounds = r + 1;
+      }
+      __syncthreads();
+      const int* list = lists[cur];
+      bool cut = false;
+      for (int t = tid; t < nsh; t += NODE_THREADS) cut |= rowThread(A.s, A.P, B, list[t], C, st);
+      for (int w = warp; w < nlo; w += NW) cut |= rowWarp(A.s, A.P, B, list[m - 1 - w], C, st);
+      if (cut) s_cut = 1;
+      __syncthreads();
+      // acceptance; runs even after a cutoff so that every candidate slot is reset
+      Front F{lists[nxt], &s_ns[nxt], &s_nl[nxt], rowstamp, m};
+      const int nt = s_ntouched;
+      const bool alive = !s_cut;
+      unsigned long long ch = 0;
+      for (int t = tid; t < nt; t += NODE_THREADS) {
+        int j = touched[t];
+        double l, u, nl, nu;
+        B.get(j, l, u);
+        if (applyColumn(A.s, A.P.isint[j] != 0, l, u, C, j, nl, nu)) {
+          s_cut = 1;
+          continue;
+        }
+        bool lbup = nl > l, ubdown = nu < u;
+        if (alive && (lbup || ubdown)) {
+          ovlSet(B, dirty, &s_ndirty, j, nl, nu);
+          ch += (unsigned long long)lbup + (unsigned long long)ubdown;
+          expandColumn(A.P, F, j, lbup, ubdown, s_rstamp);
+        }
+      }
+      if (ch) atomicAdd(&s_changes, ch);
+      __syncthreads();
+      ++r;
+    }
+    __syncthreads();
+
+    // results: columns whose final bounds differ from the base, packed at a reserved offset
+    const bool cutoff = s_cut != 0;
+    const int nd = s_ndirty;
+    int mine = 0;
+    if (!cutoff) {
+      for (int t = tid; t < nd; t += NODE_THREADS) {
+        int j = dirty[t];
+        double2 o = ovl[j], b = A.base[j];
+        if (o.x != b.x || o.y != b.y) ++mine;
+      }
+      if (mine) atomicAdd(&s_nout, mine);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      long long off = 0;
+      int cnt = s_nout;
+      if (cnt > 0) {
+        off = (long long)atomicAdd(A.out_used, (unsigned long long)cnt);
+        if (off + cnt > A.out_cap) {
+          atomicOr(A.status, 2);
+          cnt = -1;
+        }
+      }
+      s_off = cnt < 0 ? -1 : off;
+      A.out_off[item] = cnt < 0 ? 0 : off;
+      A.out_n[item] = cnt;
+      A.out_cutoff[item] = cutoff ? 1 : 0;
+      A.out_rounds[item] = s_rounds;
+      s_nout = 0;
+      mycut += cutoff ? 1 : 0;
+      if ((unsigned long long)s_rounds > mymaxr) mymaxr = s_rounds;
+      if (s_changes) atomicAdd(&A.stats[3], s_changes);
+    }
+    __syncthreads();
+    if (!cutoff && s_off >= 0) {
+      for (int t = tid; t < nd; t += NODE_THREADS) {
+        int j = dirty[t];
+        double2 o = ovl[j], b = A.base[j];
+        if (o.x != b.x || o.y != b.y) {
+          long long pos = s_off + atomicAdd(&s_nout, 1);
+          A.out_col[pos] = j;
+          A.out_lb[pos] = o.x;
+          A.out_ub[pos] = o.y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    S.counter[slot] = counter;
+    if (mycut) atomicAdd(&A.stats[4], mycut);
+    atomicMax(&A.stats[5], mymaxr);
+  }
+  flushStats(A.stats, st);
+}
+
+// ------------------------------------------------------------------------------------------ launchers
+cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
+                            const double* ub, const int* list, const int* nshort, Cands C, int* cutoff,
+                            unsigned long long* stats) {
+  k_rows_short<<<grid, 256, 0, st>>>(s, P, PlainBnd{lb, ub}, list, nshort, C, cutoff, stats);
+  return cudaGetLastError();
+}
+cudaError_t launchRowsLong(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
+                           const double* ub, const int* list, const int* nlong, int cap, Cands C, int* cutoff,
+                           unsigned long long* stats) {
+  k_rows_long<<<grid, 256, 0, st>>>(s, P, PlainBnd{lb, ub}, list, nlong, cap, C, cutoff, stats);
+  return cudaGetLastError();
+}
+cudaError_t launchApply(cudaStream_t st, int grid, const Num& s, const Prob& P, double* lb, double* ub, Cands C,
+                        Front F, int stamp, int* cutoff, unsigned long long* stats) {
+  k_apply<<<grid, 256, 0, st>>>(s, P, lb, ub, C, F, stamp, cutoff, stats);
+  return cudaGetLastError();
+}
+cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* lb, const double* ub, int64_t nseed,
+                       const int32_t* cols, const double* oldlb, const double* oldub, Front F, int stamp) {
+  k_seed<<<grid, 256, 0, st>>>(P, lb, ub, nseed, cols, oldlb, oldub, F, stamp);
+  return cudaGetLastError();
+}
+cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
+                             const double* ub, double* act, int32_t* cnt) {
+  k_activities<<<grid, 256, 0, st>>>(s, P, PlainBnd{lb, ub}, act, cnt);
+  return cudaGetLastError();
+}
+cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n) {
+  k_pack<<<grid, 256, 0, st>>>(lb, ub, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v) {
+  k_fill64<<<grid, 256, 0, st>>>(p, n, v);
+  return cudaGetLastError();
+}
+cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double* cvals, const int32_t* rowidx,
+                           const double* lhs, const double* rhs, double inf, uint32_t* out) {
+  k_csc_flags<<<grid, 256, 0, st>>>(nnz, cvals, rowidx, lhs, rhs, inf, out);
+  return cudaGetLastError();
+}
+cudaError_t launchNodes(cudaStream_t st, int grid, const NodesArgs& A) {
+  k_nodes<<<grid, NODE_THREADS, 0, st>>>(A);
+  return cudaGetLastError();
+}
+cudaError_t nodesOccupancy(int* blocksPerSm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes, NODE_THREADS, 0);
+}
+
+}  // namespace gbp

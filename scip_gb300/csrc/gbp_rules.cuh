@@ -1,0 +1,203 @@
+// Device-side numerics and tightening rules of SCIP's linear-constraint propagation.
+//
+// Everything here is FP64 and is compiled with --fmad=false, so each expression rounds exactly like the
+// plain C restatement used as the test oracle; integer bounds, cutoff verdicts and (for rows summed in
+// the same order) activities are bit-identical.  The rule each function restates is cited beside it
+// (paths relative to the SCIP source tree).
+#pragma once
+
+#include <cstdint>
+
+namespace gbp {
+
+struct Num {
+  double inf, eps, sumeps, feastol, huge, bstreps, recomp, maxeasy;
+};
+
+__host__ __device__ __forceinline__ bool isInf(const Num& s, double x) { return x >= s.inf; }   // set.c:6824
+__host__ __device__ __forceinline__ bool isHuge(const Num& s, double x) { return x >= s.huge; }  // set.c:6835
+__host__ __device__ __forceinline__ bool lt(const Num& s, double a, double b) { return a - b < -s.eps; }  // def.h:193
+__host__ __device__ __forceinline__ bool le(const Num& s, double a, double b) { return a - b <= s.eps; }
+__host__ __device__ __forceinline__ bool gt(const Num& s, double a, double b) { return a - b > s.eps; }
+__host__ __device__ __forceinline__ bool ge(const Num& s, double a, double b) { return a - b >= -s.eps; }
+__host__ __device__ __forceinline__ bool eq(const Num& s, double a, double b) { return fabs(a - b) <= s.eps; }
+__host__ __device__ __forceinline__ bool sumGt(const Num& s, double a, double b) { return a - b > s.sumeps; }
+__host__ __device__ __forceinline__ bool positive(const Num& s, double a) { return a > s.eps; }
+__host__ __device__ __forceinline__ bool feasZero(const Num& s, double a) { return fabs(a) <= s.feastol; }
+
+// SCIPrelDiff, misc.c:11162-11176
+__host__ __device__ __forceinline__ double relDiff(double a, double b) {
+  double q = fabs(a);
+  if (fabs(b) > q) q = fabs(b);
+  if (1.0 > q) q = 1.0;
+  return (a - b) / q;
+}
+__host__ __device__ __forceinline__ bool feasLt(const Num& s, double a, double b) { return relDiff(a, b) < -s.feastol; }
+__host__ __device__ __forceinline__ bool feasGt(const Num& s, double a, double b) { return relDiff(a, b) > s.feastol; }
+__host__ __device__ __forceinline__ double feasFloor(const Num& s, double x) { return floor(x + s.feastol); }
+__host__ __device__ __forceinline__ double feasCeil(const Num& s, double x) { return ceil(x - s.feastol); }
+__host__ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__host__ __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+
+// SCIPsetIsLbBetter / SCIPsetIsUbBetter, set.c:7711-7753 (minimal improvement "boundstreps")
+__host__ __device__ __forceinline__ bool lbBetter(const Num& s, double nl, double ol, double ou) {
+  if (ol < 0.0 && nl >= 0.0) return true;
+  return nl - ol > s.bstreps * dmax(dmin(ou - ol, fabs(ol)), 1e-3);
+}
+__host__ __device__ __forceinline__ bool ubBetter(const Num& s, double nu, double ol, double ou) {
+  if (ou > 0.0 && nu <= 0.0) return true;
+  return nu - ou < -(s.bstreps * dmax(dmin(ou - ol, fabs(ou)), 1e-3));
+}
+
+// SCIPsetIsUpdateUnreliable, set.c:8032-8046
+__host__ __device__ __forceinline__ bool updateUnreliable(const Num& s, double nv, double ov) {
+  return fabs(ov) / dmax(fabs(nv), s.eps) >= s.recomp;
+}
+
+// adjustedLb / adjustedUb, var.c:1957-2020 (integral columns are rounded within feastol)
+__host__ __device__ __forceinline__ double adjLb(const Num& s, bool isint, double lb) {
+  if (lb < 0.0 && isInf(s, -lb)) return -s.inf;
+  if (lb > 0.0 && isInf(s, lb)) return s.inf;
+  if (isint) return feasCeil(s, lb);
+  if (lb > 0.0 && lb < s.eps) return 0.0;
+  return lb;
+}
+__host__ __device__ __forceinline__ double adjUb(const Num& s, bool isint, double ub) {
+  if (ub > 0.0 && isInf(s, ub)) return s.inf;
+  if (ub < 0.0 && isInf(s, -ub)) return -s.inf;
+  if (isint) return feasFloor(s, ub);
+  if (ub < 0.0 && ub > -s.eps) return 0.0;
+  return ub;
+}
+
+// Compensated accumulation (hi, lo) += b: Knuth's TwoSum on the high word, low words added without
+// renormalisation -- the accumulation SCIP applies to activities (dbldblarith.h SCIPdbldblSum21).
+__host__ __device__ __forceinline__ void sum21(double& hi, double& lo, double b) {
+  double s = hi + b;
+  double bb = s - hi;
+  double err = (hi - (s - bb)) + (b - bb);
+  lo = err + lo;
+  hi = s;
+}
+
+// Order-preserving int64 key of a double, for atomicMin / atomicMax on candidate bounds.
+__device__ __forceinline__ long long dkey(double x) {
+  long long i = __double_as_longlong(x);
+  return i >= 0 ? i : (i ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double keyd(long long k) {
+  return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffLL));
+}
+
+// Activity of one row: double-double finite parts plus infinity/huge counters
+// (struct SCIP_ConsData minactivity/maxactivity and the eight counters, cons_linear.c:187-266).
+struct Act {
+  double minhi, minlo, maxhi, maxlo;
+  int minposinf, minneginf, minposhuge, minneghuge;
+  int maxposinf, maxneginf, maxposhuge, maxneghuge;
+};
+
+__device__ __forceinline__ void actZero(Act& a) {
+  a.minhi = a.minlo = a.maxhi = a.maxlo = 0.0;
+  a.minposinf = a.minneginf = a.minposhuge = a.minneghuge = 0;
+  a.maxposinf = a.maxneginf = a.maxposhuge = a.maxneghuge = 0;
+}
+
+// One contribution val*bound (consdataUpdateActivities with old bound 0, cons_linear.c:1772-1945).
+__device__ __forceinline__ void addContribution(const Num& s, double val, double bound, double& hi, double& lo,
+                                                int& posinf, int& neginf, int& poshuge, int& neghuge) {
+  if (isInf(s, fabs(bound))) {
+    if ((val > 0.0) == (bound > 0.0)) ++posinf; else ++neginf;
+  } else {
+    double c = val * bound;
+    if (isHuge(s, fabs(c))) {
+      if (c > 0.0) ++poshuge; else ++neghuge;
+    } else if (c != 0.0) {
+      sum21(hi, lo, c);
+    }
+  }
+}
+
+__device__ __forceinline__ void addTerm(const Num& s, Act& a, double val, double lb, double ub) {
+  addContribution(s, val, val > 0.0 ? lb : ub, a.minhi, a.minlo, a.minposinf, a.minneginf, a.minposhuge,
+                  a.minneghuge);
+  addContribution(s, val, val > 0.0 ? ub : lb, a.maxhi, a.maxlo, a.maxposinf, a.maxneginf, a.maxposhuge,
+                  a.maxneghuge);
+}
+
+// Combination of two partial activities (lane partials of long rows): b's high word enters through the
+// compensated sum, its low word is added to the low word.
+__device__ __forceinline__ void actMerge(Act& a, const Act& b) {
+  sum21(a.minhi, a.minlo, b.minhi);
+  a.minlo = a.minlo + b.minlo;
+  sum21(a.maxhi, a.maxlo, b.maxhi);
+  a.maxlo = a.maxlo + b.maxlo;
+  a.minposinf += b.minposinf; a.minneginf += b.minneginf; a.minposhuge += b.minposhuge; a.minneghuge += b.minneghuge;
+  a.maxposinf += b.maxposinf; a.maxneginf += b.maxneginf; a.maxposhuge += b.maxposhuge; a.maxneghuge += b.maxneghuge;
+}
+
+// getMinActivity / getMaxActivity, cons_linear.c:2345-2529
+__device__ __forceinline__ void getMinAct(const Num& s, const Act& a, int posinf, int neginf, int poshuge,
+                                          int neghuge, double delta, bool goodrelax, double& val, bool& tight,
+                                          bool& settoinf) {
+  if (neginf > 0) { val = -s.inf; settoinf = true; tight = (posinf == 0); }
+  else if (posinf > 0) { val = s.inf; settoinf = true; tight = true; }
+  else if (neghuge > 0 || (poshuge > 0 && !goodrelax)) { val = -s.inf; settoinf = true; tight = false; }
+  else {
+    double hi = a.minhi, lo = a.minlo;
+    sum21(hi, lo, -delta);
+    if (poshuge > 0) { sum21(hi, lo, poshuge * s.huge); tight = false; }
+    else tight = true;
+    val = hi + lo;
+    settoinf = false;
+  }
+}
+__device__ __forceinline__ void getMaxAct(const Num& s, const Act& a, int posinf, int neginf, int poshuge,
+                                          int neghuge, double delta, bool goodrelax, double& val, bool& tight,
+                                          bool& settoinf) {
+  if (posinf > 0) { val = s.inf; settoinf = true; tight = (neginf == 0); }
+  else if (neginf > 0) { val = -s.inf; settoinf = true; tight = true; }
+  else if (poshuge > 0 || (neghuge > 0 && !goodrelax)) { val = s.inf; settoinf = true; tight = false; }
+  else {
+    double hi = a.maxhi, lo = a.maxlo;
+    sum21(hi, lo, -delta);
+    if (neghuge > 0) { sum21(hi, lo, -neghuge * s.huge); tight = false; }
+    else tight = true;
+    val = hi + lo;
+    settoinf = false;
+  }
+}
+
+// consdataGetActivityResiduals, cons_linear.c:2661-2806 (goodrelax FALSE, as tightenVarBounds asks)
+__device__ __forceinline__ void residuals(const Num& s, const Act& a, double val, double lb, double ub,
+                                          double& minres, double& maxres, bool& mintight, bool& maxtight,
+                                          bool& mininf, bool& maxinf) {
+  double minb, maxb, absval;
+  if (val > 0.0) { minb = lb; maxb = ub; absval = val; }
+  else { minb = -ub; maxb = -lb; absval = -val; }
+  if (isInf(s, minb))
+    getMinAct(s, a, a.minposinf - 1, a.minneginf, a.minposhuge, a.minneghuge, 0.0, false, minres, mintight, mininf);
+  else if (isInf(s, -minb))
+    getMinAct(s, a, a.minposinf, a.minneginf - 1, a.minposhuge, a.minneghuge, 0.0, false, minres, mintight, mininf);
+  else if (isHuge(s, minb * absval))
+    getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge - 1, a.minneghuge, 0.0, false, minres, mintight, mininf);
+  else if (isHuge(s, -minb * absval))
+    getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge - 1, 0.0, false, minres, mintight, mininf);
+  else
+    getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, absval * minb, false, minres, mintight,
+              mininf);
+
+  if (isInf(s, -maxb))
+    getMaxAct(s, a, a.maxposinf, a.maxneginf - 1, a.maxposhuge, a.maxneghuge, 0.0, false, maxres, maxtight, maxinf);
+  else if (isInf(s, maxb))
+    getMaxAct(s, a, a.maxposinf - 1, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, false, maxres, maxtight, maxinf);
+  else if (isHuge(s, absval * maxb))
+    getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge - 1, a.maxneghuge, 0.0, false, maxres, maxtight, maxinf);
+  else if (isHuge(s, -absval * maxb))
+    getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge - 1, 0.0, false, maxres, maxtight, maxinf);
+  else
+    getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, absval * maxb, false, maxres, maxtight,
+              maxinf);
+}
+
+}  // namespace gbp

@@ -1,0 +1,245 @@
+"""Python binding of libgbp's C ABI (include/gbp.h) through ctypes.
+
+This is the host-side mirror of the propagator interface for Python callers (tests, bench, the serving
+loop).  Every call goes to the CUDA library; there is no CPU fallback: if libgbp.so is missing or no
+sm_103 GPU is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from .build import LIBGBP
+
+_P = ctypes.c_void_p
+
+GBP_OK = 0
+GBP_ERR_INVALID = -1
+GBP_ERR_CUDA = -2
+GBP_ERR_NOMEM = -3
+GBP_ERR_NODEVICE = -4
+GBP_ERR_LIMIT = -5
+GBP_ERR_OVERFLOW = -6
+GBP_ERR_STATE = -7
+
+# every symbol include/gbp.h declares (checked by the CPU test suite)
+EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
+           "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
+           "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape"]
+
+
+class GbpParams(ctypes.Structure):
+    _fields_ = [("infinity", ctypes.c_double), ("epsilon", ctypes.c_double), ("sumepsilon", ctypes.c_double),
+                ("feastol", ctypes.c_double), ("hugeval", ctypes.c_double), ("boundstreps", ctypes.c_double),
+                ("recompfac", ctypes.c_double), ("maxeasyactivitydelta", ctypes.c_double),
+                ("maxrounds", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+class GbpResult(ctypes.Structure):
+    _fields_ = [("cutoff", ctypes.c_int32), ("rounds", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("launches", ctypes.c_int32), ("rows", ctypes.c_int64), ("nnz", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64), ("kernel_ms", ctypes.c_double)]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GbpError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbp error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    """Load libgbp.so (raises FileNotFoundError if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIBGBP
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} missing: build it with scip_gb300.build.build_libgbp()")
+    L = ctypes.CDLL(p)
+    L.gbp_version.restype = ctypes.c_int
+    L.gbp_error_string.restype = ctypes.c_char_p
+    L.gbp_error_string.argtypes = [ctypes.c_int]
+    L.gbp_last_error.restype = ctypes.c_char_p
+    L.gbp_last_error.argtypes = [_P]
+    L.gbp_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, _P]
+    L.gbp_destroy.argtypes = [_P]
+    L.gbp_default_params.argtypes = [ctypes.POINTER(GbpParams)]
+    L.gbp_default_params.restype = None
+    L.gbp_set_params.argtypes = [_P, ctypes.POINTER(GbpParams)]
+    L.gbp_get_stream.argtypes = [_P, ctypes.POINTER(_P)]
+    L.gbp_upload_problem.argtypes = [_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P, _P]
+    L.gbp_propagate.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(GbpResult)]
+    L.gbp_propagate_device.argtypes = L.gbp_propagate.argtypes
+    L.gbp_row_activities.argtypes = [_P, _P, _P, _P, _P]
+    L.gbp_propagate_nodes.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                      ctypes.c_int64, ctypes.POINTER(GbpResult)]
+    L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
+    L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32]
+    if path is None:
+        _lib = L
+    return L
+
+
+def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0) -> GbpParams:
+    p = GbpParams()
+    load_library().gbp_default_params(ctypes.byref(p))
+    if maxeasy is not None:
+        p.maxeasyactivitydelta = maxeasy
+    p.maxrounds = maxrounds
+    return p
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    if hasattr(a, "data_ptr"):  # torch tensor on the device
+        return ctypes.c_void_p(a.data_ptr())
+    return a
+
+
+@dataclass
+class NodeResults:
+    cutoff: np.ndarray
+    rounds: np.ndarray
+    off: np.ndarray
+    n: np.ndarray
+    col: np.ndarray
+    lb: np.ndarray
+    ub: np.ndarray
+    result: GbpResult
+
+    def node(self, k):
+        o, c = int(self.off[k]), int(self.n[k])
+        return self.col[o:o + c], self.lb[o:o + c], self.ub[o:o + c]
+
+
+class Propagator:
+    """One GPU context with one uploaded set of rows (the state a SCIP propagator keeps between calls)."""
+
+    def __init__(self, device: int = 0, stream=None, params: Optional[GbpParams] = None):
+        self.L = load_library()
+        h = _P()
+        rc = self.L.gbp_create(ctypes.byref(h), device, _ptr(stream) if stream is not None else None)
+        if rc != GBP_OK:
+            raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        self.h = h
+        self.n = 0
+        self.m = 0
+        if params is not None:
+            self.set_params(params)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gbp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, allow=()):
+        if rc != GBP_OK and rc not in allow:
+            raise GbpError(rc, f"{self.L.gbp_error_string(rc).decode()}: {self.L.gbp_last_error(self.h).decode()}")
+        return rc
+
+    def set_params(self, p: GbpParams):
+        self._check(self.L.gbp_set_params(self.h, ctypes.byref(p)))
+
+    def set_batch_shape(self, ctas_per_sm: int):
+        self._check(self.L.gbp_set_batch_shape(self.h, ctas_per_sm))
+
+    def stream(self):
+        s = _P()
+        self._check(self.L.gbp_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def upload(self, inst):
+        self._keep = [np.ascontiguousarray(inst.rowptr, dtype=np.int64),
+                      np.ascontiguousarray(inst.colidx, dtype=np.int32),
+                      np.ascontiguousarray(inst.vals, dtype=np.float64),
+                      np.ascontiguousarray(inst.lhs, dtype=np.float64),
+                      np.ascontiguousarray(inst.rhs, dtype=np.float64),
+                      np.ascontiguousarray(inst.isint, dtype=np.int8)]
+        rp, ci, va, lh, rh, ii = self._keep
+        self._check(self.L.gbp_upload_problem(self.h, inst.m, inst.n, _ptr(rp), _ptr(ci), _ptr(va), _ptr(lh),
+                                              _ptr(rh), _ptr(ii)))
+        self._keep = None
+        self.m, self.n = inst.m, inst.n
+
+    def propagate(self, lb, ub, seed=None):
+        """Host arrays; returns (lb, ub, cutoff, GbpResult).  seed = (cols, oldlb, oldub) or None (all rows)."""
+        lb = np.array(lb, dtype=np.float64)
+        ub = np.array(ub, dtype=np.float64)
+        cut = ctypes.c_int32(0)
+        res = GbpResult()
+        if seed is None:
+            rc = self.L.gbp_propagate(self.h, _ptr(lb), _ptr(ub), -1, None, None, None, ctypes.byref(cut),
+                                      ctypes.byref(res))
+        else:
+            cols = np.ascontiguousarray(seed[0], dtype=np.int32)
+            olb = np.ascontiguousarray(seed[1], dtype=np.float64)
+            oub = np.ascontiguousarray(seed[2], dtype=np.float64)
+            rc = self.L.gbp_propagate(self.h, _ptr(lb), _ptr(ub), len(cols), _ptr(cols), _ptr(olb), _ptr(oub),
+                                      ctypes.byref(cut), ctypes.byref(res))
+        self._check(rc, allow=(GBP_ERR_LIMIT,))
+        return lb, ub, bool(cut.value), res
+
+    def propagate_device(self, lb, ub):
+        """Device bound vectors (torch float64 tensors), all rows seeded; returns (cutoff, GbpResult)."""
+        cut = ctypes.c_int32(0)
+        res = GbpResult()
+        rc = self.L.gbp_propagate_device(self.h, _ptr(lb), _ptr(ub), -1, None, None, None, ctypes.byref(cut),
+                                         ctypes.byref(res))
+        self._check(rc, allow=(GBP_ERR_LIMIT,))
+        return bool(cut.value), res
+
+    def activities(self, lb, ub):
+        lb = np.ascontiguousarray(lb, dtype=np.float64)
+        ub = np.ascontiguousarray(ub, dtype=np.float64)
+        act = np.zeros((self.m, 4))
+        cnt = np.zeros((self.m, 8), dtype=np.int32)
+        self._check(self.L.gbp_row_activities(self.h, _ptr(lb), _ptr(ub), _ptr(act), _ptr(cnt)))
+        return act, cnt
+
+    def propagate_nodes(self, baselb, baseub, nodes, out_cap: Optional[int] = None) -> NodeResults:
+        """Host arrays: nodes is an instances.NodeBatch.  Returns packed per-node results."""
+        N = nodes.nnodes
+        if out_cap is None:
+            out_cap = max(1024, 64 * N)
+        baselb = np.ascontiguousarray(baselb, dtype=np.float64)
+        baseub = np.ascontiguousarray(baseub, dtype=np.float64)
+        ptr = np.ascontiguousarray(nodes.ptr, dtype=np.int64)
+        col = np.ascontiguousarray(nodes.col, dtype=np.int32)
+        nlb = np.ascontiguousarray(nodes.lb, dtype=np.float64)
+        nub = np.ascontiguousarray(nodes.ub, dtype=np.float64)
+        r = NodeResults(np.zeros(N, np.int8), np.zeros(N, np.int32), np.zeros(N, np.int64), np.zeros(N, np.int32),
+                        np.zeros(out_cap, np.int32), np.zeros(out_cap), np.zeros(out_cap), GbpResult())
+        rc = self.L.gbp_propagate_nodes(self.h, _ptr(baselb), _ptr(baseub), N, _ptr(ptr), _ptr(col), _ptr(nlb),
+                                        _ptr(nub), _ptr(r.cutoff), _ptr(r.rounds), _ptr(r.off), _ptr(r.n),
+                                        _ptr(r.col), _ptr(r.lb), _ptr(r.ub), out_cap, ctypes.byref(r.result))
+        self._check(rc, allow=(GBP_ERR_LIMIT,))
+        return r
+
+    def propagate_nodes_device(self, baselb, baseub, nnodes, ptr, col, nlb, nub, out, out_cap):
+        """All arguments device tensors; out = dict(cutoff, rounds, off, n, col, lb, ub).  Returns GbpResult."""
+        res = GbpResult()
+        rc = self.L.gbp_propagate_nodes_device(self.h, _ptr(baselb), _ptr(baseub), nnodes, _ptr(ptr), _ptr(col),
+                                               _ptr(nlb), _ptr(nub), _ptr(out["cutoff"]), _ptr(out["rounds"]),
+                                               _ptr(out["off"]), _ptr(out["n"]), _ptr(out["col"]), _ptr(out["lb"]),
+                                               _ptr(out["ub"]), out_cap, ctypes.byref(res))
+        self._check(rc, allow=(GBP_ERR_LIMIT,))
+        return res

@@ -1,0 +1,341 @@
+"""Seeded synthetic propagation workloads (linear rows + column bounds + node bound changes).
+
+Every instance is a set of linear rows  lhs_i <= sum_j a_ij x_j <= rhs_i  (CSR, infinite sides = +-1e20)
+over columns with bounds [lb_j, ub_j] and an integrality flag, the data that SCIP's cons_linear
+propagation reads from its transformed problem (struct SCIP_ConsData, cons_linear.c:187-266).
+
+Generators (all driven by numpy's PCG64 so that this container and an aarch64 host produce the same
+arrays for the same seed):
+
+* ``root_mip``  -- 2,000 x 5,000, row length U{5..15}, integer coefficients U{-10..10}\\{0}, 70 % integer
+  columns in [0,10], 30 % continuous in [0,100]; 80 % ``<=`` rows with rhs = a.x0 + U[0,5], 10 % ranged
+  rows a.x0 -+ U[0,5], 10 % equalities at a.x0 for a feasible point x0.
+* ``zipf_mip``  -- 1,000,000 x 2,000,000, row lengths Zipf(1.5) truncated to [2,5000] by rejection,
+  |a| log-uniform in [1e-2,1e2] with random sign, 60 % integer in [0,20], 30 % continuous in [0,1e3],
+  10 % continuous with one infinite bound; senses from x0 with 85 % ``<=``, 10 % ranged, 5 % equalities.
+* ``node_mip``  -- 200,000 x 400,000 built like ``zipf_mip`` but with row lengths U{5..40}.
+* ``node_batch`` -- branch-and-bound node bound changes: 1..64 integer columns per node (count
+  log-uniform) fixed to random integer values inside the given (root) bounds.
+* ``uneven_batch`` -- distinct instances of three families (set covering, multi-knapsack, network flow
+  with arc-open indicators) with log-uniform row counts and columns = 2 x rows.
+
+Sizes are parameters, so tests use the same generators at small scale.
+"""
+from __future__ import annotations
+
+import dataclasses
+import struct
+from typing import List, Optional
+
+import numpy as np
+
+INF = 1e20
+
+
+@dataclasses.dataclass
+class Instance:
+    """Rows in CSR form plus column data; the layout the C-ABI uploads (include/gbp.h)."""
+
+    rowptr: np.ndarray  # int64 [m+1]
+    colidx: np.ndarray  # int32 [nnz]
+    vals: np.ndarray  # float64 [nnz]
+    lhs: np.ndarray  # float64 [m]
+    rhs: np.ndarray  # float64 [m]
+    lb: np.ndarray  # float64 [n]
+    ub: np.ndarray  # float64 [n]
+    isint: np.ndarray  # int8 [n]
+    name: str = ""
+
+    @property
+    def m(self) -> int:
+        return int(self.rowptr.shape[0] - 1)
+
+    @property
+    def n(self) -> int:
+        return int(self.lb.shape[0])
+
+    @property
+    def nnz(self) -> int:
+        return int(self.colidx.shape[0])
+
+    def csc(self):
+        """Column-major copy (colptr int64 [n+1], rowidx int32 [nnz], vals float64 [nnz])."""
+        m, n = self.m, self.n
+        rows = np.repeat(np.arange(m, dtype=np.int32), np.diff(self.rowptr))
+        order = np.lexsort((rows, self.colidx))
+        colptr = np.zeros(n + 1, dtype=np.int64)
+        np.cumsum(np.bincount(self.colidx, minlength=n), out=colptr[1:])
+        return colptr, rows[order].astype(np.int32), self.vals[order].copy()
+
+    def write(self, path: str) -> None:
+        """Instance file read by the SCIP oracle driver (oracle/scip_driver.c)."""
+        with open(path, "wb") as f:
+            f.write(b"LPINST01")
+            f.write(struct.pack("<4q", self.m, self.n, self.nnz, 0))
+            for arr, dt in ((self.rowptr, "<i8"), (self.colidx, "<i4"), (self.vals, "<f8"),
+                            (self.lhs, "<f8"), (self.rhs, "<f8"), (self.lb, "<f8"), (self.ub, "<f8"),
+                            (self.isint, "i1")):
+                f.write(np.ascontiguousarray(arr, dtype=dt).tobytes())
+
+
+@dataclasses.dataclass
+class NodeBatch:
+    """Bound changes per node: node k changes columns col[ptr[k]:ptr[k+1]] to [lb, ub]."""
+
+    ptr: np.ndarray  # int64 [nnodes+1]
+    col: np.ndarray  # int32
+    lb: np.ndarray  # float64
+    ub: np.ndarray  # float64
+
+    @property
+    def nnodes(self) -> int:
+        return int(self.ptr.shape[0] - 1)
+
+    def write(self, path: str) -> None:
+        with open(path, "wb") as f:
+            f.write(b"LPNODE01")
+            f.write(struct.pack("<2q", self.nnodes, int(self.col.shape[0])))
+            for arr, dt in ((self.ptr, "<i8"), (self.col, "<i4"), (self.lb, "<f8"), (self.ub, "<f8")):
+                f.write(np.ascontiguousarray(arr, dtype=dt).tobytes())
+
+
+# ----------------------------------------------------------------------------------------------
+def _distinct_columns(rng: np.random.Generator, lengths: np.ndarray, n: int) -> np.ndarray:
+    """Uniform columns per row without repeats inside a row (rows keep their sampling order)."""
+    m = lengths.shape[0]
+    rowptr = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(lengths, out=rowptr[1:])
+    nnz = int(rowptr[-1])
+    rows = np.repeat(np.arange(m, dtype=np.int64), lengths)
+    cols = rng.integers(0, n, size=nnz, dtype=np.int64)
+    for _ in range(100):
+        key = rows * n + cols
+        order = np.argsort(key, kind="stable")
+        sk = key[order]
+        dup = np.zeros(nnz, dtype=bool)
+        dup[order[1:][sk[1:] == sk[:-1]]] = True
+        nd = int(dup.sum())
+        if nd == 0:
+            break
+        cols[dup] = rng.integers(0, n, size=nd, dtype=np.int64)
+    else:  # pragma: no cover - probability ~0 for the sizes used
+        raise RuntimeError("could not draw distinct columns")
+    return rowptr, cols.astype(np.int32)
+
+
+def _sides_from_point(rng, rowptr, colidx, vals, x0, frac_le, frac_ranged, slack_hi):
+    """Row senses from a feasible point: '<=' with slack, ranged +-slack, or equality."""
+    m = rowptr.shape[0] - 1
+    rows = np.repeat(np.arange(m), np.diff(rowptr))
+    act = np.bincount(rows, weights=vals * x0[colidx], minlength=m)
+    u = rng.random(m)
+    s1 = rng.uniform(0.0, slack_hi, size=m)
+    s2 = rng.uniform(0.0, slack_hi, size=m)
+    lhs = np.full(m, -INF)
+    rhs = act + s1
+    ranged = (u >= frac_le) & (u < frac_le + frac_ranged)
+    eq = u >= frac_le + frac_ranged
+    lhs[ranged] = act[ranged] - s2[ranged]
+    lhs[eq] = act[eq]
+    rhs[eq] = act[eq]
+    return lhs, rhs
+
+
+def root_mip(seed: int = 0, m: int = 2000, n: int = 5000) -> Instance:
+    """Plain single-problem root propagation workload (2,000 x 5,000 at default size)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    lengths = rng.integers(5, 16, size=m)
+    rowptr, colidx = _distinct_columns(rng, lengths, n)
+    mag = rng.integers(1, 11, size=colidx.shape[0]).astype(np.float64)
+    vals = np.where(rng.random(colidx.shape[0]) < 0.5, -mag, mag)
+    isint = (rng.random(n) < 0.7).astype(np.int8)
+    lb = np.zeros(n)
+    ub = np.where(isint == 1, 10.0, 100.0)
+    x0 = np.where(isint == 1, rng.integers(0, 11, size=n).astype(np.float64), rng.uniform(0.0, 100.0, size=n))
+    lhs, rhs = _sides_from_point(rng, rowptr, colidx, vals, x0, 0.8, 0.1, 5.0)
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"root_mip(seed={seed},{m}x{n})")
+
+
+def _general_columns(rng, n):
+    """60 % integer [0,20], 30 % continuous [0,1e3], 10 % continuous with one infinite bound."""
+    u = rng.random(n)
+    isint = (u < 0.6).astype(np.int8)
+    lb = np.zeros(n)
+    ub = np.where(u < 0.6, 20.0, 1e3)
+    oneinf = u >= 0.9
+    lowinf = oneinf & (rng.random(n) < 0.5)
+    upinf = oneinf & ~lowinf
+    lb[lowinf] = -INF
+    ub[upinf] = INF
+    x0 = np.where(isint == 1, rng.integers(0, 21, size=n).astype(np.float64), rng.uniform(0.0, 1e3, size=n))
+    return isint, lb, ub, x0
+
+
+def _general_mip(rng, lengths, n, name):
+    rowptr, colidx = _distinct_columns(rng, lengths, n)
+    nnz = colidx.shape[0]
+    mag = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), size=nnz))
+    vals = np.where(rng.random(nnz) < 0.5, -mag, mag)
+    isint, lb, ub, x0 = _general_columns(rng, n)
+    lhs, rhs = _sides_from_point(rng, rowptr, colidx, vals, x0, 0.85, 0.10, 5.0)
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=name)
+
+
+def zipf_lengths(rng: np.random.Generator, m: int, a: float = 1.5, lo: int = 2, hi: int = 5000) -> np.ndarray:
+    """Zipf(a) row lengths truncated to [lo, hi] by rejection."""
+    out = np.empty(0, dtype=np.int64)
+    while out.shape[0] < m:
+        x = rng.zipf(a, size=2 * (m - out.shape[0]) + 64)
+        out = np.concatenate([out, x[(x >= lo) & (x <= hi)]])
+    return out[:m]
+
+
+def zipf_mip(seed: int = 1, m: int = 1_000_000, n: int = 2_000_000, hi: int = 5000) -> Instance:
+    """Large single instance with Zipf row lengths (load-balance stress)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    lengths = zipf_lengths(rng, m, 1.5, 2, min(hi, n))
+    return _general_mip(rng, lengths, n, f"zipf_mip(seed={seed},{m}x{n})")
+
+
+def node_mip(seed: int = 2, m: int = 200_000, n: int = 400_000) -> Instance:
+    """Shared matrix of the batched branch-and-bound node workload (row lengths U{5..40})."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    lengths = rng.integers(5, 41, size=m)
+    return _general_mip(rng, lengths, n, f"node_mip(seed={seed},{m}x{n})")
+
+
+def node_batch(inst: Instance, lb: np.ndarray, ub: np.ndarray, nnodes: int, seed: int = 3,
+               kmax: int = 64) -> NodeBatch:
+    """Nodes fixing 1..kmax integer columns (count log-uniform) to random values inside [lb, ub]."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    intcols = np.flatnonzero((inst.isint == 1) & (ub > lb) & (ub < INF) & (lb > -INF))
+    if intcols.shape[0] == 0:
+        raise ValueError("no unfixed finite integer columns")
+    kmax = min(kmax, intcols.shape[0])
+    ks = np.floor(np.exp(rng.uniform(0.0, np.log(kmax + 1), size=nnodes))).astype(np.int64)
+    ks = np.clip(ks, 1, kmax)
+    ptr = np.zeros(nnodes + 1, dtype=np.int64)
+    np.cumsum(ks, out=ptr[1:])
+    cols = np.empty(int(ptr[-1]), dtype=np.int32)
+    for k in range(nnodes):
+        cols[ptr[k]:ptr[k + 1]] = np.sort(rng.choice(intcols, size=int(ks[k]), replace=False))
+    lo = lb[cols]
+    hi = ub[cols]
+    v = np.floor(lo + rng.random(cols.shape[0]) * (hi - lo + 1.0))
+    v = np.minimum(v, hi)
+    return NodeBatch(ptr, cols, v.copy(), v.copy())
+
+
+# ---------------------------------------------------------------- uneven instance families
+def set_cover(rng: np.random.Generator, m: int, n: int) -> Instance:
+    """Set covering: binary columns, rows sum_{j in S_i} x_j >= 1 with |S_i| in 3..30."""
+    lengths = rng.integers(3, 31, size=m)
+    lengths = np.minimum(lengths, n)
+    rowptr, colidx = _distinct_columns(rng, lengths, n)
+    vals = np.ones(colidx.shape[0])
+    lhs = np.ones(m)
+    rhs = np.full(m, INF)
+    return Instance(rowptr, colidx, vals, lhs, rhs, np.zeros(n), np.ones(n), np.ones(n, dtype=np.int8),
+                    name=f"set_cover({m}x{n})")
+
+
+def multi_knapsack(rng: np.random.Generator, m: int, n: int) -> Instance:
+    """Multi-knapsack: integer columns in [0,5], weights U{1..100}, capacity 40 % of the row's max activity."""
+    lengths = np.minimum(rng.integers(5, 41, size=m), n)
+    rowptr, colidx = _distinct_columns(rng, lengths, n)
+    vals = rng.integers(1, 101, size=colidx.shape[0]).astype(np.float64)
+    rows = np.repeat(np.arange(m), lengths)
+    maxact = np.bincount(rows, weights=vals * 5.0, minlength=m)
+    rhs = np.floor(0.4 * maxact)
+    lhs = np.full(m, -INF)
+    return Instance(rowptr, colidx, vals, lhs, rhs, np.zeros(n), np.full(n, 5.0), np.ones(n, dtype=np.int8),
+                    name=f"multi_knapsack({m}x{n})")
+
+
+def network_flow(rng: np.random.Generator, m: int) -> Instance:
+    """Fixed-charge network flow: conservation equalities over continuous arc flows in [0, cap] plus
+    linking rows flow_a - cap_a * open_a <= 0 with integer open_a in [0,1].
+
+    With V graph nodes and A arcs there are V + A rows and 2A columns; A = 2V/... is chosen so that
+    rows ~ m and the arc count matches the column budget as closely as the family allows."""
+    nv = max(2, m // 3)
+    na = max(1, m - nv)
+    tail = rng.integers(0, nv, size=na)
+    head = (tail + rng.integers(1, nv, size=na)) % nv
+    cap = rng.uniform(1.0, 50.0, size=na)
+    x0 = rng.uniform(0.0, 1.0, size=na) * cap * (rng.random(na) < 0.7)
+    supply = np.bincount(tail, weights=x0, minlength=nv) - np.bincount(head, weights=x0, minlength=nv)
+    # conservation rows: out - in = supply
+    crow = np.concatenate([tail, head])
+    ccol = np.concatenate([np.arange(na), np.arange(na)])
+    cval = np.concatenate([np.ones(na), -np.ones(na)])
+    order = np.lexsort((ccol, crow))
+    crow, ccol, cval = crow[order], ccol[order], cval[order]
+    cnt = np.bincount(crow, minlength=nv)
+    # linking rows
+    lrow = np.repeat(np.arange(na), 2) + nv
+    lcol = np.stack([np.arange(na), na + np.arange(na)], axis=1).reshape(-1)
+    lval = np.stack([np.ones(na), -cap], axis=1).reshape(-1)
+    mm = nv + na
+    rowlen = np.concatenate([cnt, np.full(na, 2)])
+    rowptr = np.zeros(mm + 1, dtype=np.int64)
+    np.cumsum(rowlen, out=rowptr[1:])
+    colidx = np.concatenate([ccol, lcol]).astype(np.int32)
+    vals = np.concatenate([cval, lval])
+    lhs = np.concatenate([supply, np.full(na, -INF)])
+    rhs = np.concatenate([supply, np.zeros(na)])
+    n = 2 * na
+    lb = np.zeros(n)
+    ub = np.concatenate([cap, np.ones(na)])
+    isint = np.concatenate([np.zeros(na, dtype=np.int8), np.ones(na, dtype=np.int8)])
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"network_flow({mm}x{n})")
+
+
+def uneven_batch(seed: int = 4, count: int = 512, rmin: int = 1000, rmax: int = 200_000) -> List[Instance]:
+    """Distinct instances with log-uniform row counts; families cycle set cover / knapsack / network."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    rows = np.floor(np.exp(rng.uniform(np.log(rmin), np.log(rmax), size=count))).astype(np.int64)
+    out = []
+    for k in range(count):
+        m = int(rows[k])
+        fam = k % 3
+        if fam == 0:
+            out.append(set_cover(rng, m, 2 * m))
+        elif fam == 1:
+            out.append(multi_knapsack(rng, m, 2 * m))
+        else:
+            out.append(network_flow(rng, m))
+    return out
+
+
+# ---------------------------------------------------------------- result files of the SCIP oracle
+def read_oracle_output(path: str):
+    """Parse the oracle driver's output: (rootcutoff, rootlb, rootub, nodes) where nodes is a list of
+    (cutoff, seconds, cols, lb, ub) with the columns whose bounds differ from the root fixpoint."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] != b"LPOUT001":
+        raise ValueError("bad oracle output")
+    n, nnodes = struct.unpack_from("<2q", data, 8)
+    off = 24
+    rootcut = data[off]
+    off += 1
+    (roottime,) = struct.unpack_from("<d", data, off)
+    off += 8
+    rootlb = np.frombuffer(data, dtype="<f8", count=n, offset=off).copy()
+    off += 8 * n
+    rootub = np.frombuffer(data, dtype="<f8", count=n, offset=off).copy()
+    off += 8 * n
+    nodes = []
+    rec = np.dtype([("col", "<i4"), ("lb", "<f8"), ("ub", "<f8")])
+    for _ in range(nnodes):
+        cut = data[off]
+        off += 1
+        (secs,) = struct.unpack_from("<d", data, off)
+        off += 8
+        (nch,) = struct.unpack_from("<i", data, off)
+        off += 4
+        r = np.frombuffer(data, dtype=rec, count=nch, offset=off)
+        off += rec.itemsize * nch
+        nodes.append((bool(cut), secs, r["col"].copy(), r["lb"].copy(), r["ub"].copy()))
+    return bool(rootcut), rootlb, rootub, nodes

@@ -1,0 +1,114 @@
+"""CUDA path vs the oracle (C restatement) on the same seeded inputs, through the C ABI.
+
+Bit-exact comparison: both sides evaluate the same rules in the same order of floating-point operations
+(libgbp is compiled with --fmad=false; activities are summed in a fixed canonical order), so bounds,
+cutoff verdicts, activities and infinity counts must be identical, not merely close.
+"""
+import numpy as np
+import pytest
+
+from scip_gb300 import gbp, instances
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(maxeasy):
+    return gbp.default_params(maxeasy=maxeasy)
+
+
+def _nodes_equal(r, o, nnodes):
+    assert np.array_equal(r.cutoff, o["cutoff"]), "cutoff verdicts differ"
+    assert np.array_equal(r.rounds[r.cutoff == 0], o["rounds"][o["cutoff"] == 0]), "round counts differ"
+    for k in range(nnodes):
+        if r.cutoff[k]:
+            continue
+        c, l, u = r.node(k)
+        n = o["n"][k]
+        assert n >= 0
+        oc = o["col"][k, :n]
+        a, b = np.argsort(c), np.argsort(oc)
+        assert np.array_equal(c[a], oc[b]), f"node {k}: changed columns differ"
+        assert np.array_equal(l[a], o["lb"][k, :n][b]), f"node {k}: lower bounds differ"
+        assert np.array_equal(u[a], o["ub"][k, :n][b]), f"node {k}: upper bounds differ"
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_root_fixpoint_matches_oracle(gpu_prop, oracle_mod, seed, maxeasy):
+    inst = instances.root_mip(seed)
+    gpu_prop.set_params(_params(maxeasy))
+    gpu_prop.upload(inst)
+    lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
+    olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(maxeasy))
+    assert cut == bool(ores.cutoff)
+    assert res.rounds == ores.rounds
+    assert res.rows == ores.rows and res.nnz == ores.nnz and res.candidates == ores.candidates
+    assert np.array_equal(lb, olb) and np.array_equal(ub, oub)
+
+
+def test_activities_and_counts_bit_exact(gpu_prop, oracle_mod):
+    # Zipf rows (long rows take the warp path) with infinite and huge bounds
+    inst = instances.zipf_mip(seed=11, m=3000, n=6000, hi=600)
+    lb = inst.lb.copy()
+    ub = inst.ub.copy()
+    rng = np.random.default_rng(5)
+    huge = rng.random(inst.n) < 0.02
+    ub[huge] = 3e16
+    gpu_prop.upload(inst)
+    act, cnt = gpu_prop.activities(lb, ub)
+    oact, ocnt = oracle_mod.Oracle(inst).activities(lb, ub)
+    assert np.array_equal(cnt, ocnt)
+    assert np.array_equal(act, oact)
+    assert (np.diff(inst.rowptr) > 64).any()
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_zipf_root_matches_oracle(gpu_prop, oracle_mod, maxeasy):
+    inst = instances.zipf_mip(seed=3, m=20000, n=40000, hi=2000)
+    gpu_prop.set_params(_params(maxeasy))
+    gpu_prop.upload(inst)
+    lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
+    olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(maxeasy))
+    assert cut == bool(ores.cutoff)
+    if not cut:
+        assert np.array_equal(lb, olb) and np.array_equal(ub, oub)
+        assert res.rounds == ores.rounds
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_nodes_match_oracle(gpu_prop, oracle_mod, maxeasy):
+    inst = instances.node_mip(seed=2, m=20000, n=40000)
+    orc = oracle_mod.Oracle(inst)
+    par = oracle_mod.params(maxeasy)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    nodes = instances.node_batch(inst, rlb, rub, 512, seed=9)
+    gpu_prop.set_params(_params(maxeasy))
+    gpu_prop.upload(inst)
+    r = gpu_prop.propagate_nodes(rlb, rub, nodes)
+    o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+    _nodes_equal(r, o, nodes.nnodes)
+
+
+def test_nodes_seeded_plain_path_equals_batched(gpu_prop, oracle_mod):
+    """Each node alone through the plain path (seeded propagate) equals its result inside the batch."""
+    inst = instances.root_mip(4)
+    gpu_prop.set_params(_params(0.0))
+    gpu_prop.upload(inst)
+    rlb, rub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
+    nodes = instances.node_batch(inst, rlb, rub, 40, seed=2)
+    r = gpu_prop.propagate_nodes(rlb, rub, nodes)
+    for k in range(nodes.nnodes):
+        lb, ub = rlb.copy(), rub.copy()
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        cols = nodes.col[sl]
+        olb, oub = lb[cols].copy(), ub[cols].copy()
+        lb[cols] = np.maximum(lb[cols], nodes.lb[sl])
+        ub[cols] = np.minimum(ub[cols], nodes.ub[sl])
+        plb, pub, cut, _ = gpu_prop.propagate(lb, ub, seed=(cols, olb, oub))
+        assert cut == bool(r.cutoff[k])
+        if not cut:
+            c, l, u = r.node(k)
+            elb, eub = rlb.copy(), rub.copy()
+            elb[c] = l
+            eub[c] = u
+            assert np.array_equal(plb, elb) and np.array_equal(pub, eub)
