@@ -64,6 +64,7 @@ typedef struct
    int64_t nnz;         /* nonzeros of those rows */
    int64_t candidates;  /* candidate bounds emitted */
    int64_t changes;     /* accepted bound changes (lower and upper counted separately) */
+   int64_t live_rows;   /* frontier rows that passed the skip tests and produced candidate work */
    double kernel_ms;    /* device time of the propagation kernels (CUDA events on the context's stream) */
 } gbp_result;
 
@@ -120,8 +121,9 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
    int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
    double* out_ub, int64_t out_cap, gbp_result* res);
 
-/* launch shape of the batched kernel: CTAs per SM (0 = occupancy maximum) -- what the autotuner sets */
-int gbp_set_batch_shape(gbp_ctx* ctx, int32_t ctas_per_sm);
+/* launch shape of the batched kernel -- what the autotuner sets: threads that work on one node (32, 64, 128 or
+ * 256; one CTA per node at a time) and resident CTAs per SM (0 = occupancy maximum) */
+int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per_sm);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,7 @@ struct gbp_ctx {
 
   // batched path
   int ctas_per_sm = 0;
+  int node_threads = 32;
   int nslots = 0;
   SlotArrays slots{};
   void* slot_mem = nullptr;
@@ -231,10 +232,13 @@ int gbp_get_stream(const gbp_ctx* ctx, void** stream) {
   return GBP_OK;
 }
 
-int gbp_set_batch_shape(gbp_ctx* ctx, int32_t ctas_per_sm) {
+int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per_sm) {
   if (!ctx || ctas_per_sm < 0 || ctas_per_sm > 32) return GBP_ERR_INVALID;
-  if (ctas_per_sm != ctx->ctas_per_sm) {
+  if (threads_per_node != 32 && threads_per_node != 64 && threads_per_node != 128 && threads_per_node != 256)
+    return fail(ctx, GBP_ERR_INVALID, "threads per node must be 32, 64, 128 or 256");
+  if (ctas_per_sm != ctx->ctas_per_sm || threads_per_node != ctx->node_threads) {
     ctx->ctas_per_sm = ctas_per_sm;
+    ctx->node_threads = threads_per_node;
     if (ctx->slot_mem) {
       cudaStreamSynchronize(ctx->stream);
       cudaFree(ctx->slot_mem);
@@ -415,7 +419,7 @@ static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, co
     CK(cudaMemsetAsync(ctx->d_ctr + 2 + nxt, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->d_ctr + 4, 0, sizeof(int), ctx->stream));
     if (ns > 0) {
-      CK(launchRowsShort(ctx->stream, gridFor(ctx, ns), s, P, lb, ub, cur, ctx->d_ctr + curidx, C, ctx->d_ctr + 5,
+      CK(launchRowsShort(ctx->stream, gridFor(ctx, ns, 128), s, P, lb, ub, cur, ctx->d_ctr + curidx, C, ctx->d_ctr + 5,
                          ctx->d_stats));
       ++launches;
     }
@@ -457,6 +461,7 @@ static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, co
     res->nnz = (int64_t)st[1];
     res->candidates = (int64_t)st[2];
     res->changes = (int64_t)st[3];
+    res->live_rows = (int64_t)st[6];
     res->kernel_ms = ms;
   }
   return status == 2 ? GBP_ERR_LIMIT : GBP_OK;
@@ -550,7 +555,7 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
 static int ensureSlots(gbp_ctx* ctx) {
   if (ctx->slot_mem) return GBP_OK;
   int occ = 0;
-  CK(nodesOccupancy(&occ));
+  CK(nodesOccupancy(ctx->node_threads, &occ));
   int per_sm = ctx->ctas_per_sm > 0 ? std::min(ctx->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
   const int64_t ns = std::max<int64_t>(ctx->n, 1), ms = std::max<int64_t>(ctx->m, 1);
   const size_t per_slot = (size_t)ns * (sizeof(double2) + sizeof(int) + 4 * sizeof(long long) + 3 * sizeof(int)) +
@@ -662,7 +667,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   A.stats = ctx->d_stats;
   A.status = ctx->d_status;
   const int grid = (int)std::min<int64_t>(ctx->nslots, nnodes);
-  CK(launchNodes(ctx->stream, grid, A));
+  CK(launchNodes(ctx->stream, grid, ctx->node_threads, A));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   unsigned long long st[8];
   int status = 0;
@@ -681,6 +686,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
     res->nnz = (int64_t)st[1];
     res->candidates = (int64_t)st[2];
     res->changes = (int64_t)st[3];
+    res->live_rows = (int64_t)st[6];
     res->kernel_ms = ms;
   }
   if (status & 2) return fail(ctx, GBP_ERR_OVERFLOW, "node output arrays too small");

@@ -46,7 +46,7 @@ struct Cands {
 };
 
 struct Stats {
-  long long rows, nnz, cands;
+  long long rows, nnz, cands, live;  // live: rows that passed the skip tests
 };
 
 // frontier lists: short rows from the front of `list`, long rows from the back
@@ -226,24 +226,55 @@ __device__ __forceinline__ double entryDelta(const Num& s, double val, double l,
   return fabs(val) * (u - l);
 }
 
-// One frontier row of at most LONGROW entries, processed by a single thread.  Returns true on cutoff.
+// Per-thread staging of one chunk of a row's entries (shared memory), so that the candidate pass can loop
+// over a chunk whose gathers were issued back to back.
+constexpr int CHUNK = 4;
+struct Stage {
+  int j[CHUNK];
+  double v[CHUNK];
+  double l[CHUNK];
+  double u[CHUNK];
+};
+
+// Load entries [pb, min(pb+CHUNK, p1)) of a row: column indices and values first, then all bound gathers,
+// so a chunk costs two memory round trips instead of two per entry.
 template <class BND>
-__device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+__device__ __forceinline__ void loadChunk(const Prob& P, const BND& B, int64_t pb, int64_t p1, int (&jj)[CHUNK],
+                                          double (&vv)[CHUNK], double (&ll)[CHUNK], double (&uu)[CHUNK]) {
+#pragma unroll
+  for (int k = 0; k < CHUNK; ++k) {
+    const bool ok = pb + k < p1;
+    jj[k] = ok ? P.colidx[pb + k] : 0;
+    vv[k] = ok ? P.vals[pb + k] : 0.0;
+  }
+#pragma unroll
+  for (int k = 0; k < CHUNK; ++k)
+    if (pb + k < p1) B.get(jj[k], ll[k], uu[k]);
+}
+
+// One frontier row of at most LONGROW entries, processed by a single thread; entries are summed in row
+// order.  Returns true on cutoff.
+template <class BND>
+__device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st, Stage& stg) {
   const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
   const double lhs = P.lhs[i], rhs = P.rhs[i];
   Act a;
   actZero(a);
   double mad = 0.0;
   bool madinf = false;
-  for (int64_t p = p0; p < p1; ++p) {
-    int j = P.colidx[p];
-    double v = P.vals[p];
-    double l, u;
-    B.get(j, l, u);
-    addTerm(s, a, v, l, u);
-    double d = entryDelta(s, v, l, u);
-    if (d < 0.0) madinf = true;
-    else if (d > mad) mad = d;
+  for (int64_t pb = p0; pb < p1; pb += CHUNK) {
+    int jj[CHUNK];
+    double vv[CHUNK], ll[CHUNK], uu[CHUNK];
+    loadChunk(P, B, pb, p1, jj, vv, ll, uu);
+#pragma unroll
+    for (int k = 0; k < CHUNK; ++k) {
+      if (pb + k < p1) {
+        addTerm(s, a, vv[k], ll[k], uu[k]);
+        double d = entryDelta(s, vv[k], ll[k], uu[k]);
+        if (d < 0.0) madinf = true;
+        else if (d > mad) mad = d;
+      }
+    }
   }
   st.rows += 1;
   st.nnz += p1 - p0;
@@ -251,26 +282,41 @@ __device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cand
   int t = rowTests(s, a, lhs, rhs, madinf ? s.inf : mad, easy);
   if (t == 1) return true;
   if (t == 0) return false;
+  st.live += 1;
   const bool force = (p1 - p0 == 1);
-  for (int64_t p = p0; p < p1; ++p) {
-    int j = P.colidx[p];
-    double v = P.vals[p];
-    double l, u;
-    B.get(j, l, u);
-    auto relres = [&](bool ismin) {
-      double r = 0.0;
-      for (int64_t q = p0; q < p1; ++q) {
-        if (q == p) continue;
-        int jj = P.colidx[q];
-        double vv = P.vals[q], ll, uu;
-        B.get(jj, ll, uu);
-        if (vv > 0.0) r += ismin ? vv * ll : vv * uu;
-        else r += ismin ? vv * uu : vv * ll;
+  for (int64_t pb = p0; pb < p1; pb += CHUNK) {
+    {
+      int jj[CHUNK];
+      double vv[CHUNK], ll[CHUNK], uu[CHUNK];
+      loadChunk(P, B, pb, p1, jj, vv, ll, uu);
+#pragma unroll
+      for (int k = 0; k < CHUNK; ++k) {
+        stg.j[k] = jj[k];
+        stg.v[k] = vv[k];
+        stg.l[k] = ll[k];
+        stg.u[k] = uu[k];
       }
-      return r;
-    };
-    if (columnCandidates(s, a, lhs, rhs, easy, force, j, v, l, u, P.isint[j] != 0, C, st.cands, relres))
-      return true;
+    }
+    const int cnt = (int)((p1 - pb) < CHUNK ? (p1 - pb) : CHUNK);
+    for (int k = 0; k < cnt; ++k) {
+      const int64_t p = pb + k;
+      const int j = stg.j[k];
+      auto relres = [&](bool ismin) {
+        double r = 0.0;
+        for (int64_t q = p0; q < p1; ++q) {
+          if (q == p) continue;
+          int jj2 = P.colidx[q];
+          double vv2 = P.vals[q], l2, u2;
+          B.get(jj2, l2, u2);
+          if (vv2 > 0.0) r += ismin ? vv2 * l2 : vv2 * u2;
+          else r += ismin ? vv2 * u2 : vv2 * l2;
+        }
+        return r;
+      };
+      if (columnCandidates(s, a, lhs, rhs, easy, force, j, stg.v[k], stg.l[k], stg.u[k], P.isint[j] != 0, C,
+                           st.cands, relres))
+        return true;
+    }
   }
   return false;
 }
@@ -340,6 +386,7 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
   int t = rowTests(s, a, lhs, rhs, madinf ? s.inf : mad, easy);
   if (t == 1) return true;
   if (t == 0) return false;
+  if (lane == 0) st.live += 1;
   bool cut = false;
   for (int64_t p = p0 + lane; p < p1; p += 32) {
     int j = P.colidx[p];

@@ -53,7 +53,6 @@ struct NodesArgs {
   int* status;                   // bit0 round limit, bit1 output overflow
 };
 
-constexpr int NODE_THREADS = 256;
 
 // launchers (return the cudaError_t of the launch)
 cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
@@ -69,8 +68,8 @@ cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* l
 cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
                              const double* ub, double* act, int32_t* cnt);
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n);
-cudaError_t launchNodes(cudaStream_t st, int grid, const NodesArgs& A);
-cudaError_t nodesOccupancy(int* blocksPerSm);
+cudaError_t launchNodes(cudaStream_t st, int grid, int threads, const NodesArgs& A);
+cudaError_t nodesOccupancy(int threads, int* blocksPerSm);
 cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double* cvals, const int32_t* rowidx,
                            const double* lhs, const double* rhs, double inf, uint32_t* out);
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v);

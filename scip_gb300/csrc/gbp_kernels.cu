@@ -37,23 +37,28 @@ __device__ __forceinline__ void flushStats(unsigned long long* stats, const Stat
   if (st.rows) atomicAdd(&stats[0], (unsigned long long)st.rows);
   if (st.nnz) atomicAdd(&stats[1], (unsigned long long)st.nnz);
   if (st.cands) atomicAdd(&stats[2], (unsigned long long)st.cands);
+  if (st.live) atomicAdd(&stats[6], (unsigned long long)st.live);
 }
 
 // ------------------------------------------------------------------------------------------ plain path
-__global__ void __launch_bounds__(256) k_rows_short(Num s, Prob P, PlainBnd B, const int* list, const int* nshort,
-                                                    Cands C, int* cutoff, unsigned long long* stats) {
-  Stats st{0, 0, 0};
+constexpr int ROW_THREADS = 128;
+
+__global__ void __launch_bounds__(ROW_THREADS) k_rows_short(Num s, Prob P, PlainBnd B, const int* list,
+                                                           const int* nshort, Cands C, int* cutoff,
+                                                           unsigned long long* stats) {
+  __shared__ Stage stage[ROW_THREADS];
+  Stats st{0, 0, 0, 0};
   const int n = *nshort;
   bool cut = false;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-    cut |= rowThread(s, P, B, list[t], C, st);
+    cut |= rowThread(s, P, B, list[t], C, st, stage[threadIdx.x]);
   if (cut) atomicExch(cutoff, 1);
   flushStats(stats, st);
 }
 
 __global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
                                                    int cap, Cands C, int* cutoff, unsigned long long* stats) {
-  Stats st{0, 0, 0};
+  Stats st{0, 0, 0, 0};
   const int n = *nlong;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -195,7 +200,9 @@ __device__ __forceinline__ void ovlSet(const OvlBnd& B, int* dirty, int* ndirty,
   B.ovl[j] = make_double2(l, u);
 }
 
-__global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
+  __shared__ Stage stage[NT];
   __shared__ int s_item, s_cut, s_ns[2], s_nl[2], s_ntouched, s_ndirty, s_nout, s_rounds, s_epoch, s_rstamp;
   __shared__ long long s_off;
   __shared__ unsigned long long s_changes;
@@ -203,7 +210,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  constexpr int NW = NODE_THREADS / 32;
+  constexpr int NW = NT / 32;
   const SlotArrays& S = A.S;
   const int64_t ns = S.nstride, ms = S.mstride;
   const size_t slot = blockIdx.x;
@@ -225,7 +232,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
 
   int counter = 0;
   if (tid == 0) counter = S.counter[slot];
-  Stats st{0, 0, 0};
+  Stats st{0, 0, 0, 0};
   unsigned long long mycut = 0, mymaxr = 0;
 
   for (;;) {
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
     // branching bound changes of the node, then the rows they make relevant
     {
       Front F{lists[0], &s_ns[0], &s_nl[0], rowstamp, m};
-      for (int64_t q = A.ptr[item] + tid; q < A.ptr[item + 1]; q += NODE_THREADS) {
+      for (int64_t q = A.ptr[item] + tid; q < A.ptr[item + 1]; q += NT) {
         int j = A.chg_col[q];
         double nl = A.chg_lb[q], nu = A.chg_ub[q];
         double l0, u0;
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
       __syncthreads();
       const int* list = lists[cur];
       bool cut = false;
-      for (int t = tid; t < nsh; t += NODE_THREADS) cut |= rowThread(A.s, A.P, B, list[t], C, st);
+      for (int t = tid; t < nsh; t += NT) cut |= rowThread(A.s, A.P, B, list[t], C, st, stage[tid]);
       for (int w = warp; w < nlo; w += NW) cut |= rowWarp(A.s, A.P, B, list[m - 1 - w], C, st);
       if (cut) s_cut = 1;
       __syncthreads();
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
       const int nt = s_ntouched;
       const bool alive = !s_cut;
       unsigned long long ch = 0;
-      for (int t = tid; t < nt; t += NODE_THREADS) {
+      for (int t = tid; t < nt; t += NT) {
         int j = touched[t];
         double l, u, nl, nu;
         B.get(j, l, u);
@@ -317,7 +324,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
     const int nd = s_ndirty;
     int mine = 0;
     if (!cutoff) {
-      for (int t = tid; t < nd; t += NODE_THREADS) {
+      for (int t = tid; t < nd; t += NT) {
         int j = dirty[t];
         double2 o = ovl[j], b = A.base[j];
         if (o.x != b.x || o.y != b.y) ++mine;
@@ -347,7 +354,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
     }
     __syncthreads();
     if (!cutoff && s_off >= 0) {
-      for (int t = tid; t < nd; t += NODE_THREADS) {
+      for (int t = tid; t < nd; t += NT) {
         int j = dirty[t];
         double2 o = ovl[j], b = A.base[j];
         if (o.x != b.x || o.y != b.y) {
@@ -372,7 +379,7 @@ __global__ void __launch_bounds__(NODE_THREADS) k_nodes(NodesArgs A) {
 cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
                             const double* ub, const int* list, const int* nshort, Cands C, int* cutoff,
                             unsigned long long* stats) {
-  k_rows_short<<<grid, 256, 0, st>>>(s, P, PlainBnd{lb, ub}, list, nshort, C, cutoff, stats);
+  k_rows_short<<<grid, ROW_THREADS, 0, st>>>(s, P, PlainBnd{lb, ub}, list, nshort, C, cutoff, stats);
   return cudaGetLastError();
 }
 cudaError_t launchRowsLong(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
@@ -409,12 +416,24 @@ cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double*
   k_csc_flags<<<grid, 256, 0, st>>>(nnz, cvals, rowidx, lhs, rhs, inf, out);
   return cudaGetLastError();
 }
-cudaError_t launchNodes(cudaStream_t st, int grid, const NodesArgs& A) {
-  k_nodes<<<grid, NODE_THREADS, 0, st>>>(A);
+cudaError_t launchNodes(cudaStream_t st, int grid, int nt, const NodesArgs& A) {
+  switch (nt) {
+    case 32: k_nodes<32><<<grid, 32, 0, st>>>(A); break;
+    case 64: k_nodes<64><<<grid, 64, 0, st>>>(A); break;
+    case 128: k_nodes<128><<<grid, 128, 0, st>>>(A); break;
+    case 256: k_nodes<256><<<grid, 256, 0, st>>>(A); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
-cudaError_t nodesOccupancy(int* blocksPerSm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes, NODE_THREADS, 0);
+cudaError_t nodesOccupancy(int nt, int* blocksPerSm) {
+  switch (nt) {
+    case 32: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<32>, 32, 0);
+    case 64: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<64>, 64, 0);
+    case 128: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<128>, 128, 0);
+    case 256: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<256>, 256, 0);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace gbp

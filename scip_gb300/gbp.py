@@ -42,7 +42,8 @@ class GbpParams(ctypes.Structure):
 class GbpResult(ctypes.Structure):
     _fields_ = [("cutoff", ctypes.c_int32), ("rounds", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("rows", ctypes.c_int64), ("nnz", ctypes.c_int64),
-                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64), ("kernel_ms", ctypes.c_double)]
+                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64), ("live_rows", ctypes.c_int64),
+                ("kernel_ms", ctypes.c_double)]
 
     def asdict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -84,7 +85,7 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_nodes.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
-    L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32]
+    L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32, ctypes.c_int32]
     if path is None:
         _lib = L
     return L
@@ -159,8 +160,8 @@ class Propagator:
     def set_params(self, p: GbpParams):
         self._check(self.L.gbp_set_params(self.h, ctypes.byref(p)))
 
-    def set_batch_shape(self, ctas_per_sm: int):
-        self._check(self.L.gbp_set_batch_shape(self.h, ctas_per_sm))
+    def set_batch_shape(self, threads_per_node: int = 32, ctas_per_sm: int = 0):
+        self._check(self.L.gbp_set_batch_shape(self.h, threads_per_node, ctas_per_sm))
 
     def stream(self):
         s = _P()
