@@ -552,17 +552,25 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
 }
 
 // ------------------------------------------------------------------------------------------ batched path
-static int ensureSlots(gbp_ctx* ctx) {
-  if (ctx->slot_mem) return GBP_OK;
+// per-CTA scratch for min(resident CTAs, nnodes) slots; grown when a later call has more nodes
+static int ensureSlots(gbp_ctx* ctx, int64_t nnodes) {
   int occ = 0;
   CK(nodesOccupancy(ctx->node_threads, &occ));
   int per_sm = ctx->ctas_per_sm > 0 ? std::min(ctx->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+  const int64_t want = std::min<int64_t>((int64_t)ctx->sms * per_sm, std::max<int64_t>(nnodes, 1));
+  if (ctx->slot_mem && ctx->nslots >= want) return GBP_OK;
+  if (ctx->slot_mem) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->slot_mem);
+    ctx->slot_mem = nullptr;
+    ctx->nslots = 0;
+  }
   const int64_t ns = std::max<int64_t>(ctx->n, 1), ms = std::max<int64_t>(ctx->m, 1);
   const size_t per_slot = (size_t)ns * (sizeof(double2) + sizeof(int) + 4 * sizeof(long long) + 3 * sizeof(int)) +
                           (size_t)ms * 3 * sizeof(int) + 64 * 16;
   size_t freeb = 0, totalb = 0;
   CK(cudaMemGetInfo(&freeb, &totalb));
-  int64_t nslots = (int64_t)ctx->sms * per_sm;
+  int64_t nslots = want;
   const size_t budget = freeb / 3;
   while (nslots > 1 && (size_t)nslots * per_slot > budget) nslots -= 1;
   if ((size_t)nslots * per_slot > budget) return fail(ctx, GBP_ERR_NOMEM, "not enough device memory for one slot");
@@ -626,7 +634,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
       (out_cap > 0 && (!out_col || !out_lb || !out_ub)))
     return fail(ctx, GBP_ERR_INVALID, "null argument");
   CK(cudaSetDevice(ctx->device));
-  int rc = ensureSlots(ctx);
+  int rc = ensureSlots(ctx, nnodes);
   if (rc) return rc;
   const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
   // stamp counters grow by (rounds + 1) per node and slot; re-zero the stamps long before they wrap

@@ -226,14 +226,33 @@ __device__ __forceinline__ double entryDelta(const Num& s, double val, double l,
   return fabs(val) * (u - l);
 }
 
-// Per-thread staging of one chunk of a row's entries (shared memory), so that the candidate pass can loop
-// over a chunk whose gathers were issued back to back.
+// ------------------------------------------------------------------------------------------------------
+// Short rows (<= LONGROW entries) are processed by a CTA in batches of NT rows:
+//   1. the batch is sorted by row length (so a warp's lanes run loops of similar length),
+//   2. one thread per row sums the activity in row order (the oracle's order) and runs the row tests,
+//   3. each live row selects the few entries that can possibly yield a candidate bound (see selectEntries),
+//   4. the CTA evaluates the selected (row, entry) pairs with all lanes busy -- SCIP's full rule, so the
+//      result is exactly the oracle's.
+// FP64 instructions on GB300 cost the same with 1 or 32 active lanes, so keeping lanes converged is what
+// sets the speed of this phase.
 constexpr int CHUNK = 4;
-struct Stage {
-  int j[CHUNK];
-  double v[CHUNK];
-  double l[CHUNK];
-  double u[CHUNK];
+constexpr int TOPK = 4;          // largest entry deltas remembered per row
+constexpr int MAXSEL = TOPK + 2;  // + the single infinite/huge contributor of each activity
+
+template <int NT>
+struct RowBatch {
+  Act act[NT];
+  double lhs[NT];
+  double rhs[NT];
+  long long p0[NT];
+  int len[NT];
+  int nsel[NT];          // entries to evaluate (len when the whole row is selected)
+  int full[NT];
+  unsigned char sel[NT][MAXSEL];
+  unsigned char easy[NT];
+  int prefix[NT + 1];
+  int order[NT];         // batch position -> row, sorted by length
+  int hist[LONGROW + 2];
 };
 
 // Load entries [pb, min(pb+CHUNK, p1)) of a row: column indices and values first, then all bound gathers,
@@ -252,16 +271,116 @@ __device__ __forceinline__ void loadChunk(const Prob& P, const BND& B, int64_t p
     if (pb + k < p1) B.get(jj[k], ll[k], uu[k]);
 }
 
-// One frontier row of at most LONGROW entries, processed by a single thread; entries are summed in row
-// order.  Returns true on cutoff.
+// bit pattern of a non-negative double (order-preserving as a signed integer); +inf for an entry with an
+// infinite bound
+__device__ __forceinline__ long long deltaBits(const Num& s, double val, double l, double u) {
+  if (isInf(s, -l) || isInf(s, u)) return 0x7ff0000000000000LL;
+  return __double_as_longlong(fabs(val) * (u - l));
+}
+__device__ __forceinline__ long long absBits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+
+// Which entries of a live row can produce a candidate (necessary conditions, never sufficient):
+// * residual rule, rhs side: the residual minimal activity of entry j is finite only if the row's minimal
+//   activity has no infinite/huge contribution (then newub < ub needs delta_j > slack, up to rounding, where
+//   delta_j = |a_j|(ub_j - lb_j) and slack = rhs - minact), or exactly one (then only that entry); lhs side
+//   likewise with the maximal activity and the surplus maxact - lhs;
+// * easy rule: a candidate needs alpha_j = delta_j > max(slack, 0) (tightenVarBoundsEasy), exactly;
+// * a row of one entry is always evaluated (forced tightening).
+// `margin` covers every rounding difference between this estimate and the exact rule: the exact residual
+// path differs from slack - delta_j by a few units in the last place of the row's largest magnitudes, and
+// the plain-double recomputation of consdataGetReliableResidualActivity by at most len such units.
+struct ScanOut {
+  long long topd[TOPK];
+  int topp[TOPK];
+  int minspec, maxspec;  // entry holding an infinite or huge contribution (last one seen)
+  long long maxabs;      // largest |contribution| and |a_j|*|bound| seen, as bits
+};
+
+__device__ __forceinline__ int selectEntries(const Num& s, const Act& a, const ScanOut& so, double lhs, double rhs,
+                                             int len, bool easy, unsigned char (&sel)[MAXSEL], bool& full) {
+  full = false;
+  if (len == 1) {
+    full = true;
+    return 1;
+  }
+  const bool rhsfin = !isInf(s, rhs), lhsfin = !isInf(s, -lhs);
+  const int mintot = a.minposinf + a.minneginf + a.minposhuge + a.minneghuge;
+  const int maxtot = a.maxposinf + a.maxneginf + a.maxposhuge + a.maxneghuge;
+  double thrR = s.inf, thrL = s.inf;  // entries with delta > thr qualify
+  bool useR = false, useL = false;
+  int n = 0;
+  if (easy) {
+    if (rhsfin) {
+      double slack = rhs - (a.minhi + a.minlo);
+      if (!positive(s, slack)) slack = 0.0;
+      thrR = slack;
+      useR = true;
+    }
+    if (lhsfin) {
+      double surplus = (a.maxhi + a.maxlo) - lhs;
+      if (!positive(s, surplus)) surplus = 0.0;
+      thrL = surplus;
+      useL = true;
+    }
+  } else {
+    const double big = __longlong_as_double(so.maxabs);
+    const double margin = 1e-9 * ((rhsfin ? fabs(rhs) : 0.0) + (lhsfin ? fabs(lhs) : 0.0) + (double)(len + 2) * big) +
+                          1e-300;
+    if (rhsfin) {
+      if (mintot == 0) {
+        thrR = (rhs - (a.minhi + a.minlo)) - margin;
+        useR = true;
+      } else if (mintot == 1) {
+        sel[n++] = (unsigned char)so.minspec;
+      }
+    }
+    if (lhsfin) {
+      if (maxtot == 0) {
+        thrL = ((a.maxhi + a.maxlo) - lhs) - margin;
+        useL = true;
+      } else if (maxtot == 1) {
+        if (n == 0 || sel[0] != (unsigned char)so.maxspec) sel[n++] = (unsigned char)so.maxspec;
+      }
+    }
+  }
+  if (useR || useL) {
+    const double thr = dmin(useR ? thrR : s.inf, useL ? thrL : s.inf);
+    int k = 0;
+    for (; k < TOPK; ++k) {
+      if (so.topp[k] < 0) break;
+      const double d = __longlong_as_double(so.topd[k]);
+      if (!(d > thr)) break;
+      bool dup = false;
+      for (int q = 0; q < n; ++q) dup |= (sel[q] == (unsigned char)so.topp[k]);
+      if (!dup) sel[n++] = (unsigned char)so.topp[k];
+    }
+    if (k == TOPK) {  // the TOPK largest all qualify: more may, so evaluate the whole row
+      full = true;
+      return len;
+    }
+  }
+  return n;
+}
+
+// Pass 1 of a short row by one thread: activity in row order, maximal activity delta, row tests, entry
+// selection.  Returns 1 on cutoff, else 0; *nsel/full describe the selected entries of a live row.
 template <class BND>
-__device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st, Stage& stg) {
+__device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B, int i, Act& a, bool& easy,
+                                       unsigned char (&sel)[MAXSEL], int& nsel, bool& full, Stats& st) {
   const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+  const int len = (int)(p1 - p0);
   const double lhs = P.lhs[i], rhs = P.rhs[i];
-  Act a;
   actZero(a);
-  double mad = 0.0;
-  bool madinf = false;
+  ScanOut so;
+#pragma unroll
+  for (int k = 0; k < TOPK; ++k) {
+    so.topd[k] = -1;
+    so.topp[k] = -1;
+  }
+  so.minspec = so.maxspec = 0;
+  so.maxabs = 0;
+  long long mad = 0;  // max delta as bits (non-negative doubles order as integers)
+  const long long infb = __double_as_longlong(s.inf), hugeb = __double_as_longlong(s.huge);
   for (int64_t pb = p0; pb < p1; pb += CHUNK) {
     int jj[CHUNK];
     double vv[CHUNK], ll[CHUNK], uu[CHUNK];
@@ -269,38 +388,169 @@ __device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cand
 #pragma unroll
     for (int k = 0; k < CHUNK; ++k) {
       if (pb + k < p1) {
-        addTerm(s, a, vv[k], ll[k], uu[k]);
-        double d = entryDelta(s, vv[k], ll[k], uu[k]);
-        if (d < 0.0) madinf = true;
-        else if (d > mad) mad = d;
+        const double v = vv[k], l = ll[k], u = uu[k];
+        const int pos = (int)(pb + k - p0);
+        // the two contributions of the entry (addContribution semantics; classification on bit patterns so
+        // that only the products and sums occupy the FP64 pipe)
+        const bool vpos = __double_as_longlong(v) >= 0;
+        const double bmin = vpos ? l : u, bmax = vpos ? u : l;
+        const long long ibmin = __double_as_longlong(bmin), ibmax = __double_as_longlong(bmax);
+        if ((ibmin & 0x7fffffffffffffffLL) >= infb) {
+          if (vpos == (ibmin >= 0)) ++a.minposinf; else ++a.minneginf;
+          so.minspec = pos;
+        } else {
+          const double c = v * bmin;
+          const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
+          if (ca >= hugeb) {
+            if (cb >= 0) ++a.minposhuge; else ++a.minneghuge;
+            so.minspec = pos;
+          } else if (ca != 0) {
+            sum21(a.minhi, a.minlo, c);
+          }
+          if (ca > so.maxabs) so.maxabs = ca;
+        }
+        if ((ibmax & 0x7fffffffffffffffLL) >= infb) {
+          if (vpos == (ibmax >= 0)) ++a.maxposinf; else ++a.maxneginf;
+          so.maxspec = pos;
+        } else {
+          const double c = v * bmax;
+          const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
+          if (ca >= hugeb) {
+            if (cb >= 0) ++a.maxposhuge; else ++a.maxneghuge;
+            so.maxspec = pos;
+          } else if (ca != 0) {
+            sum21(a.maxhi, a.maxlo, c);
+          }
+          if (ca > so.maxabs) so.maxabs = ca;
+        }
+        // maximal activity delta of the entry (consdataRecomputeMaxActivityDelta): infinite if a bound is
+        const long long il = __double_as_longlong(l), iu = __double_as_longlong(u);
+        const bool linf = il < 0 && (il & 0x7fffffffffffffffLL) >= infb;   // -l >= inf
+        const bool uinf = iu >= 0 && iu >= infb;                            // u >= inf
+        const long long d = (linf || uinf) ? 0x7ff0000000000000LL : __double_as_longlong(fabs(v) * (u - l));
+        if (d > mad) mad = d;
+        // keep the TOPK largest deltas (ties keep the earlier entry)
+        if (d > so.topd[TOPK - 1]) {
+          long long cd = d;
+          int cp = pos;
+#pragma unroll
+          for (int q = 0; q < TOPK; ++q) {
+            if (cd > so.topd[q]) {
+              long long td = so.topd[q];
+              int tp = so.topp[q];
+              so.topd[q] = cd;
+              so.topp[q] = cp;
+              cd = td;
+              cp = tp;
+            }
+          }
+        }
       }
     }
   }
   st.rows += 1;
-  st.nnz += p1 - p0;
-  bool easy = false;
-  int t = rowTests(s, a, lhs, rhs, madinf ? s.inf : mad, easy);
-  if (t == 1) return true;
-  if (t == 0) return false;
+  st.nnz += len;
+  const double maxactdelta = (mad == 0x7ff0000000000000LL) ? s.inf : __longlong_as_double(mad);
+  int t = rowTests(s, a, lhs, rhs, maxactdelta, easy);
+  nsel = 0;
+  full = false;
+  if (t == 1) return 1;
+  if (t == 0) return 0;
   st.live += 1;
-  const bool force = (p1 - p0 == 1);
-  for (int64_t pb = p0; pb < p1; pb += CHUNK) {
-    {
-      int jj[CHUNK];
-      double vv[CHUNK], ll[CHUNK], uu[CHUNK];
-      loadChunk(P, B, pb, p1, jj, vv, ll, uu);
-#pragma unroll
-      for (int k = 0; k < CHUNK; ++k) {
-        stg.j[k] = jj[k];
-        stg.v[k] = vv[k];
-        stg.l[k] = ll[k];
-        stg.u[k] = uu[k];
+  if (easy) {
+    // the slack rule's own infeasibility test (tightenVarBoundsEasy), independent of the entry
+    if ((!isInf(s, rhs) && feasLt(s, rhs, a.minhi + a.minlo)) || (!isInf(s, -lhs) && feasLt(s, a.maxhi + a.maxlo, lhs)))
+      return 1;
+  }
+  nsel = selectEntries(s, a, so, lhs, rhs, len, easy, sel, full);
+  return 0;
+}
+
+// The CTA processes rows[0..nrows) (all <= LONGROW entries).  All threads of the CTA must call it with the
+// same arguments.  Sets *cut on infeasibility.
+template <int NT, class BND>
+__device__ void processShortRows(const Num& s, const Prob& P, const BND& B, const int* rows, int nrows, Cands& C,
+                                 Stats& st, RowBatch<NT>& rb, int* cut) {
+  const int tid = threadIdx.x;
+  for (int base = 0; base < nrows; base += NT) {
+    const int cnt = (nrows - base) < NT ? (nrows - base) : NT;
+    // counting sort of the batch by row length (descending)
+    for (int b = tid; b < LONGROW + 2; b += NT) rb.hist[b] = 0;
+    __syncthreads();
+    int myrow = -1, mylen = 0;
+    if (tid < cnt) {
+      myrow = rows[base + tid];
+      mylen = (int)(P.rowptr[myrow + 1] - P.rowptr[myrow]);
+      atomicAdd(&rb.hist[LONGROW - mylen], 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int acc = 0;
+      for (int b = 0; b <= LONGROW; ++b) {
+        int h = rb.hist[b];
+        rb.hist[b] = acc;
+        acc += h;
       }
     }
-    const int cnt = (int)((p1 - pb) < CHUNK ? (p1 - pb) : CHUNK);
-    for (int k = 0; k < cnt; ++k) {
-      const int64_t p = pb + k;
-      const int j = stg.j[k];
+    __syncthreads();
+    if (tid < cnt) rb.order[atomicAdd(&rb.hist[LONGROW - mylen], 1)] = myrow;
+    __syncthreads();
+
+    int nsel = 0;
+    bool full = false;
+    if (tid < cnt) {
+      const int i = rb.order[tid];
+      Act a;
+      bool easy = false;
+      unsigned char sel[MAXSEL];
+      if (scanRow(s, P, B, i, a, easy, sel, nsel, full, st)) *cut = 1;
+      rb.act[tid] = a;
+      rb.lhs[tid] = P.lhs[i];
+      rb.rhs[tid] = P.rhs[i];
+      rb.p0[tid] = P.rowptr[i];
+      rb.len[tid] = (int)(P.rowptr[i + 1] - P.rowptr[i]);
+      rb.easy[tid] = easy ? 1 : 0;
+      rb.full[tid] = full ? 1 : 0;
+#pragma unroll
+      for (int q = 0; q < MAXSEL; ++q) rb.sel[tid][q] = sel[q];
+    }
+    rb.nsel[tid] = nsel;
+    __syncthreads();
+    // exclusive prefix of the selection counts
+    if (tid < 32) {
+      int carry = 0;
+      for (int c0 = 0; c0 < NT; c0 += 32) {
+        int v = rb.nsel[c0 + tid];
+        int x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          int y = __shfl_up_sync(0xffffffffu, x, off);
+          if (tid >= off) x += y;
+        }
+        rb.prefix[c0 + tid] = carry + x - v;
+        carry += __shfl_sync(0xffffffffu, x, 31);
+      }
+      if (tid == 0) rb.prefix[NT] = carry;
+    }
+    __syncthreads();
+    const int total = rb.prefix[NT];
+    for (int w = tid; w < total; w += NT) {
+      int lo = 0, hi = NT - 1;  // owner: last o with prefix[o] <= w
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rb.prefix[mid] <= w) lo = mid;
+        else hi = mid - 1;
+      }
+      const int o = lo;
+      const int k = w - rb.prefix[o];
+      const int64_t p0 = rb.p0[o];
+      const int64_t p1 = p0 + rb.len[o];
+      const int64_t p = p0 + (rb.full[o] ? k : (int)rb.sel[o][k]);
+      const int j = P.colidx[p];
+      const double v = P.vals[p];
+      double l, u;
+      B.get(j, l, u);
+      const Act a = rb.act[o];
       auto relres = [&](bool ismin) {
         double r = 0.0;
         for (int64_t q = p0; q < p1; ++q) {
@@ -313,12 +563,12 @@ __device__ bool rowThread(const Num& s, const Prob& P, const BND& B, int i, Cand
         }
         return r;
       };
-      if (columnCandidates(s, a, lhs, rhs, easy, force, j, stg.v[k], stg.l[k], stg.u[k], P.isint[j] != 0, C,
+      if (columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, p1 - p0 == 1, j, v, l, u, P.isint[j] != 0, C,
                            st.cands, relres))
-        return true;
+        *cut = 1;
     }
+    __syncthreads();
   }
-  return false;
 }
 
 // One frontier row longer than LONGROW, processed by a whole warp: lane k sums entries k, k+32, ... and the

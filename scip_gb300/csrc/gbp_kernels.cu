@@ -46,13 +46,18 @@ constexpr int ROW_THREADS = 128;
 __global__ void __launch_bounds__(ROW_THREADS) k_rows_short(Num s, Prob P, PlainBnd B, const int* list,
                                                            const int* nshort, Cands C, int* cutoff,
                                                            unsigned long long* stats) {
-  __shared__ Stage stage[ROW_THREADS];
+  __shared__ RowBatch<ROW_THREADS> rb;
+  __shared__ int s_cut;
+  if (threadIdx.x == 0) s_cut = 0;
+  __syncthreads();
   Stats st{0, 0, 0, 0};
   const int n = *nshort;
-  bool cut = false;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-    cut |= rowThread(s, P, B, list[t], C, st, stage[threadIdx.x]);
-  if (cut) atomicExch(cutoff, 1);
+  for (int base = blockIdx.x * ROW_THREADS; base < n; base += gridDim.x * ROW_THREADS) {
+    const int cnt = (n - base) < ROW_THREADS ? (n - base) : ROW_THREADS;
+    processShortRows<ROW_THREADS>(s, P, B, list + base, cnt, C, st, rb, &s_cut);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_cut) atomicExch(cutoff, 1);
   flushStats(stats, st);
 }
 
@@ -202,7 +207,7 @@ __device__ __forceinline__ void ovlSet(const OvlBnd& B, int* dirty, int* ndirty,
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
-  __shared__ Stage stage[NT];
+  __shared__ RowBatch<NT> rb;
   __shared__ int s_item, s_cut, s_ns[2], s_nl[2], s_ntouched, s_ndirty, s_nout, s_rounds, s_epoch, s_rstamp;
   __shared__ long long s_off;
   __shared__ unsigned long long s_changes;
@@ -288,8 +293,8 @@ __global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
       }
       __syncthreads();
       const int* list = lists[cur];
+      processShortRows<NT>(A.s, A.P, B, list, nsh, C, st, rb, &s_cut);
       bool cut = false;
-      for (int t = tid; t < nsh; t += NT) cut |= rowThread(A.s, A.P, B, list[t], C, st, stage[tid]);
       for (int w = warp; w < nlo; w += NW) cut |= rowWarp(A.s, A.P, B, list[m - 1 - w], C, st);
       if (cut) s_cut = 1;
       __syncthreads();
