@@ -35,6 +35,7 @@ extern "C" {
 #define GBP_ERR_LIMIT      -5   /* the round limit was reached before the fixpoint (results are valid bounds) */
 #define GBP_ERR_OVERFLOW   -6   /* an output list was too small (out_n reports -1 for that node) */
 #define GBP_ERR_STATE      -7   /* the device reported an inconsistent state (a bounded loop gave up) */
+#define GBP_ERR_TOO_LARGE  -8   /* the problem does not fit the fixed scratch of gbp_propagate_nodes_noalloc */
 
 typedef struct gbp_ctx gbp_ctx;
 
@@ -124,6 +125,32 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
 /* launch shape of the batched kernel -- what the autotuner sets: threads that work on one node (32, 64, 128 or
  * 256; one CTA per node at a time) and resident CTAs per SM (0 = occupancy maximum) */
 int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per_sm);
+
+/* ---------------------------------------------------------------- batched path without allocation
+ * No counterpart in the reference: an addition for callers that cannot let a library allocate device memory
+ * -- applications that give all device memory to their own pool allocator at start-up, and callers that must
+ * not trigger the implicit device-wide synchronisation of cudaMalloc/cudaFree (for example a propagation
+ * callback running while other streams of the host application are busy).  It computes exactly what
+ * gbp_propagate_nodes_device computes, without a context: every array argument is a device pointer supplied
+ * by the caller (the rows in CSR and plain CSC form: colptr[n+1], rowidx[nnz], cvals[nnz]), and the scratch
+ * is one fixed __device__ array of GBP_NOALLOC_SCRATCH_BYTES inside libgbp that every GPU loading the library
+ * holds until exit.  The call allocates nothing (no cudaMalloc, cudaFree or allocating library routine).
+ * Limits: one node slot needs about 64*n + 12*m bytes; the call uses as many slots as fit (at most one per
+ * resident CTA) and returns GBP_ERR_TOO_LARGE when not even one fits (about n <= 900,000 for m = n/2), so
+ * only problems far below that limit run with useful parallelism.
+ * The first call on a device (with that device current) looks up the array's address; make it before any
+ * stream capture.  All calls on a device share the array, so calls that overlap on the GPU race and must be
+ * serialised by the caller.  stream: a cudaStream_t or NULL.  With res == NULL the call only enqueues work
+ * (an overfull output shows as out_n[k] = -1); with res != NULL it waits for the stream, fills res and
+ * returns GBP_ERR_LIMIT / GBP_ERR_OVERFLOW like gbp_propagate_nodes_device.  params == NULL uses the defaults
+ * of gbp_default_params. */
+#define GBP_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+   const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const int64_t* colptr,
+   const int32_t* rowidx, const double* cvals, const double* baselb, const double* baseub, int64_t nnodes,
+   const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub, int8_t* out_cutoff,
+   int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb, double* out_ub,
+   int64_t out_cap, const gbp_params* params, void* stream, gbp_result* res);
 
 #ifdef __cplusplus
 }

@@ -106,7 +106,7 @@ static void freeProblem(gbp_ctx* ctx) {
 
 static Prob devProb(const gbp_ctx* ctx) {
   return Prob{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
-              ctx->d_colptr, ctx->d_cscrow};
+              ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity};
 }
 
 static int gridFor(const gbp_ctx* ctx, int64_t work, int per_block = 256, int cap_per_sm = 16) {
@@ -131,6 +131,7 @@ const char* gbp_error_string(int code) {
     case GBP_ERR_LIMIT: return "round limit reached";
     case GBP_ERR_OVERFLOW: return "output list too small";
     case GBP_ERR_STATE: return "inconsistent device state";
+    case GBP_ERR_TOO_LARGE: return "problem too large for the no-alloc scratch";
     default: return "unknown error";
   }
 }
@@ -566,46 +567,20 @@ static int ensureSlots(gbp_ctx* ctx, int64_t nnodes) {
     ctx->nslots = 0;
   }
   const int64_t ns = std::max<int64_t>(ctx->n, 1), ms = std::max<int64_t>(ctx->m, 1);
-  const size_t per_slot = (size_t)ns * (sizeof(double2) + sizeof(int) + 4 * sizeof(long long) + 3 * sizeof(int)) +
-                          (size_t)ms * 3 * sizeof(int) + 64 * 16;
+  const size_t per_slot = slotLayout(ns, ms, 1, nullptr, nullptr);
   size_t freeb = 0, totalb = 0;
   CK(cudaMemGetInfo(&freeb, &totalb));
   int64_t nslots = want;
   const size_t budget = freeb / 3;
   while (nslots > 1 && (size_t)nslots * per_slot > budget) nslots -= 1;
   if ((size_t)nslots * per_slot > budget) return fail(ctx, GBP_ERR_NOMEM, "not enough device memory for one slot");
-  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
-  size_t off = 0;
-  const size_t S = (size_t)nslots;
-  size_t o_ovl = off; off = align(off + S * ns * sizeof(double2));
-  size_t o_ost = off; off = align(off + S * ns * sizeof(int));
-  size_t o_cand = off; off = align(off + 4 * S * ns * sizeof(long long));
-  size_t o_cflag = off; off = align(off + S * ns * sizeof(int));
-  size_t o_touch = off; off = align(off + S * ns * sizeof(int));
-  size_t o_dirty = off; off = align(off + S * ns * sizeof(int));
-  size_t o_rst = off; off = align(off + S * ms * sizeof(int));
-  size_t o_la = off; off = align(off + S * ms * sizeof(int));
-  size_t o_lb = off; off = align(off + S * ms * sizeof(int));
-  size_t o_ctr = off; off = align(off + S * sizeof(int));
+  const size_t bytes = slotLayout(ns, ms, nslots, nullptr, nullptr);
   char* base = nullptr;
-  CK(cudaMalloc(&base, off));
+  CK(cudaMalloc(&base, bytes));
   ctx->slot_mem = base;
   SlotArrays& A = ctx->slots;
-  A.nstride = ns;
-  A.mstride = ms;
-  A.ovl = (double2*)(base + o_ovl);
-  A.ostamp = (int*)(base + o_ost);
-  A.cub = (long long*)(base + o_cand);
-  A.clb = A.cub + S * ns;
-  A.cubf = A.clb + S * ns;
-  A.clbf = A.cubf + S * ns;
-  A.cflag = (int*)(base + o_cflag);
-  A.touched = (int*)(base + o_touch);
-  A.dirty = (int*)(base + o_dirty);
-  A.rowstamp = (int*)(base + o_rst);
-  A.listA = (int*)(base + o_la);
-  A.listB = (int*)(base + o_lb);
-  A.counter = (int*)(base + o_ctr);
+  slotLayout(ns, ms, nslots, base, &A);
+  const size_t S = (size_t)nslots;
   CK(cudaMemsetAsync(A.ostamp, 0, S * ns * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(A.cflag, 0, S * ns * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(A.rowstamp, 0, S * ms * sizeof(int), ctx->stream));
@@ -655,6 +630,8 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   A.s = ctx->num;
   A.P = devProb(ctx);
   A.base = ctx->d_base;
+  A.baselb = nullptr;
+  A.baseub = nullptr;
   A.nnodes = nnodes;
   A.ptr = ptr;
   A.chg_col = chg_col;

@@ -32,7 +32,10 @@ struct Prob {
   const double* rhs;
   const int8_t* isint;
   const int64_t* colptr;
-  const uint32_t* cscrow;  // row index | CSC_LBUP | CSC_UBDOWN
+  const uint32_t* cscrow;  // row index | CSC_LBUP | CSC_UBDOWN; null: use rowidx/cvals below
+  const int32_t* rowidx;   // plain CSC (only read when cscrow is null)
+  const double* cvals;
+  double inf;              // infinity threshold for the relevance test on plain CSC
 };
 
 struct Cands {
@@ -79,10 +82,20 @@ __device__ __forceinline__ void pushRow(const Prob& P, Front& F, int row, int st
 
 // rows of column j made relevant by a raised lower bound (lbup) and/or a lowered upper bound (ubdown)
 __device__ __forceinline__ void expandColumn(const Prob& P, Front& F, int j, bool lbup, bool ubdown, int stamp) {
-  uint32_t need = (lbup ? CSC_LBUP : 0u) | (ubdown ? CSC_UBDOWN : 0u);
-  for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
-    uint32_t e = P.cscrow[q];
-    if (e & need) pushRow(P, F, (int)(e & CSC_ROW), stamp);
+  if (P.cscrow != nullptr) {
+    uint32_t need = (lbup ? CSC_LBUP : 0u) | (ubdown ? CSC_UBDOWN : 0u);
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      uint32_t e = P.cscrow[q];
+      if (e & need) pushRow(P, F, (int)(e & CSC_ROW), stamp);
+    }
+  } else {
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      const int i = P.rowidx[q];
+      const double a = P.cvals[q];
+      const bool rhsfin = !(P.rhs[i] >= P.inf), lhsfin = !(-P.lhs[i] >= P.inf);
+      const bool rel = (lbup && (a > 0.0 ? rhsfin : lhsfin)) || (ubdown && (a > 0.0 ? lhsfin : rhsfin));
+      if (rel) pushRow(P, F, i, stamp);
+    }
   }
 }
 

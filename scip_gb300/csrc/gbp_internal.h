@@ -28,10 +28,48 @@ struct SlotArrays {
   int* counter;        // [slots] stamp counter of each slot (persists across launches)
 };
 
+// Carves the per-CTA scratch of `nslots` slots out of one block starting at `base` (null: only measure).
+// Returns the bytes needed.
+inline size_t slotLayout(int64_t ns, int64_t ms, int64_t nslots, char* base, SlotArrays* out) {
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t S = (size_t)nslots, N = (size_t)ns, M = (size_t)ms;
+  size_t off = 0;
+  const size_t o_ovl = off; off = align(off + S * N * sizeof(double2));
+  const size_t o_ost = off; off = align(off + S * N * sizeof(int));
+  const size_t o_cand = off; off = align(off + 4 * S * N * sizeof(long long));
+  const size_t o_cflag = off; off = align(off + S * N * sizeof(int));
+  const size_t o_touch = off; off = align(off + S * N * sizeof(int));
+  const size_t o_dirty = off; off = align(off + S * N * sizeof(int));
+  const size_t o_rst = off; off = align(off + S * M * sizeof(int));
+  const size_t o_la = off; off = align(off + S * M * sizeof(int));
+  const size_t o_lb = off; off = align(off + S * M * sizeof(int));
+  const size_t o_ctr = off; off = align(off + S * sizeof(int));
+  if (base != nullptr && out != nullptr) {
+    out->nstride = ns;
+    out->mstride = ms;
+    out->ovl = (double2*)(base + o_ovl);
+    out->ostamp = (int*)(base + o_ost);
+    out->cub = (long long*)(base + o_cand);
+    out->clb = out->cub + S * N;
+    out->cubf = out->clb + S * N;
+    out->clbf = out->cubf + S * N;
+    out->cflag = (int*)(base + o_cflag);
+    out->touched = (int*)(base + o_touch);
+    out->dirty = (int*)(base + o_dirty);
+    out->rowstamp = (int*)(base + o_rst);
+    out->listA = (int*)(base + o_la);
+    out->listB = (int*)(base + o_lb);
+    out->counter = (int*)(base + o_ctr);
+  }
+  return off;
+}
+
 struct NodesArgs {
   Num s;
   Prob P;
-  const double2* base;
+  const double2* base;     // packed base bounds, or null to read baselb/baseub
+  const double* baselb;
+  const double* baseub;
   int64_t nnodes;
   const int64_t* ptr;
   const int32_t* chg_col;

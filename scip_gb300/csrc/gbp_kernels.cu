@@ -21,13 +21,20 @@ struct PlainBnd {
   }
 };
 
+// node bounds: the per-CTA overlay where this node changed a column, else the shared base (packed pairs,
+// or two separate arrays when `base` is null)
 struct OvlBnd {
   const double2* base;
+  const double* baselb;
+  const double* baseub;
   double2* ovl;
   int* ostamp;
   int epoch;
+  __device__ __forceinline__ double2 getBase(int j) const {
+    return base != nullptr ? base[j] : make_double2(baselb[j], baseub[j]);
+  }
   __device__ __forceinline__ void get(int j, double& l, double& u) const {
-    double2 b = (ostamp[j] == epoch) ? ovl[j] : base[j];
+    double2 b = (ostamp[j] == epoch) ? ovl[j] : getBase(j);
     l = b.x;
     u = b.y;
   }
@@ -254,7 +261,7 @@ __global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
     __syncthreads();
     const int item = s_item;
     if (item >= A.nnodes) break;
-    OvlBnd B{A.base, ovl, ostamp, s_epoch};
+    OvlBnd B{A.base, A.baselb, A.baseub, ovl, ostamp, s_epoch};
 
     // branching bound changes of the node, then the rows they make relevant
     {
@@ -331,7 +338,7 @@ __global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
     if (!cutoff) {
       for (int t = tid; t < nd; t += NT) {
         int j = dirty[t];
-        double2 o = ovl[j], b = A.base[j];
+        double2 o = ovl[j], b = B.getBase(j);
         if (o.x != b.x || o.y != b.y) ++mine;
       }
       if (mine) atomicAdd(&s_nout, mine);
@@ -361,7 +368,7 @@ __global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
     if (!cutoff && s_off >= 0) {
       for (int t = tid; t < nd; t += NT) {
         int j = dirty[t];
-        double2 o = ovl[j], b = A.base[j];
+        double2 o = ovl[j], b = B.getBase(j);
         if (o.x != b.x || o.y != b.y) {
           long long pos = s_off + atomicAdd(&s_nout, 1);
           A.out_col[pos] = j;

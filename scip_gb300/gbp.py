@@ -25,11 +25,13 @@ GBP_ERR_NODEVICE = -4
 GBP_ERR_LIMIT = -5
 GBP_ERR_OVERFLOW = -6
 GBP_ERR_STATE = -7
+GBP_ERR_TOO_LARGE = -8
 
 # every symbol include/gbp.h declares (checked by the CPU test suite)
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
            "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
-           "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape"]
+           "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
+           "gbp_propagate_nodes_noalloc"]
 
 
 class GbpParams(ctypes.Structure):
@@ -86,6 +88,9 @@ def load_library(path: Optional[str] = None):
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
     L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32, ctypes.c_int32]
+    L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
+                                              + [_P] * 11 + [ctypes.c_int64, ctypes.POINTER(GbpParams), _P,
+                                                              ctypes.POINTER(GbpResult)])
     if path is None:
         _lib = L
     return L
