@@ -45,6 +45,7 @@ class Instance:
     ub: np.ndarray  # float64 [n]
     isint: np.ndarray  # int8 [n]
     name: str = ""
+    x0: Optional[np.ndarray] = None  # a feasible point the generator built the sides from (if any)
 
     @property
     def m(self) -> int:
@@ -153,7 +154,7 @@ def root_mip(seed: int = 0, m: int = 2000, n: int = 5000) -> Instance:
     ub = np.where(isint == 1, 10.0, 100.0)
     x0 = np.where(isint == 1, rng.integers(0, 11, size=n).astype(np.float64), rng.uniform(0.0, 100.0, size=n))
     lhs, rhs = _sides_from_point(rng, rowptr, colidx, vals, x0, 0.8, 0.1, 5.0)
-    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"root_mip(seed={seed},{m}x{n})")
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"root_mip(seed={seed},{m}x{n})", x0=x0)
 
 
 def _general_columns(rng, n):
@@ -168,7 +169,7 @@ def _general_columns(rng, n):
     lb[lowinf] = -INF
     ub[upinf] = INF
     x0 = np.where(isint == 1, rng.integers(0, 21, size=n).astype(np.float64), rng.uniform(0.0, 1e3, size=n))
-    return isint, lb, ub, x0
+    return isint, lb, ub, x0  # x0 lies in [0, 1e3] for every column, inside all bounds
 
 
 def _general_mip(rng, lengths, n, name):
@@ -178,7 +179,7 @@ def _general_mip(rng, lengths, n, name):
     vals = np.where(rng.random(nnz) < 0.5, -mag, mag)
     isint, lb, ub, x0 = _general_columns(rng, n)
     lhs, rhs = _sides_from_point(rng, rowptr, colidx, vals, x0, 0.85, 0.10, 5.0)
-    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=name)
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=name, x0=x0)
 
 
 def zipf_lengths(rng: np.random.Generator, m: int, a: float = 1.5, lo: int = 2, hi: int = 5000) -> np.ndarray:
@@ -236,7 +237,7 @@ def set_cover(rng: np.random.Generator, m: int, n: int) -> Instance:
     lhs = np.ones(m)
     rhs = np.full(m, INF)
     return Instance(rowptr, colidx, vals, lhs, rhs, np.zeros(n), np.ones(n), np.ones(n, dtype=np.int8),
-                    name=f"set_cover({m}x{n})")
+                    name=f"set_cover({m}x{n})", x0=np.ones(n))
 
 
 def multi_knapsack(rng: np.random.Generator, m: int, n: int) -> Instance:
@@ -249,7 +250,7 @@ def multi_knapsack(rng: np.random.Generator, m: int, n: int) -> Instance:
     rhs = np.floor(0.4 * maxact)
     lhs = np.full(m, -INF)
     return Instance(rowptr, colidx, vals, lhs, rhs, np.zeros(n), np.full(n, 5.0), np.ones(n, dtype=np.int8),
-                    name=f"multi_knapsack({m}x{n})")
+                    name=f"multi_knapsack({m}x{n})", x0=np.zeros(n))
 
 
 def network_flow(rng: np.random.Generator, m: int) -> Instance:
@@ -288,7 +289,8 @@ def network_flow(rng: np.random.Generator, m: int) -> Instance:
     lb = np.zeros(n)
     ub = np.concatenate([cap, np.ones(na)])
     isint = np.concatenate([np.zeros(na, dtype=np.int8), np.ones(na, dtype=np.int8)])
-    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"network_flow({mm}x{n})")
+    x0full = np.concatenate([x0, (x0 > 0).astype(np.float64)])
+    return Instance(rowptr, colidx, vals, lhs, rhs, lb, ub, isint, name=f"network_flow({mm}x{n})", x0=x0full)
 
 
 def uneven_batch(seed: int = 4, count: int = 512, rmin: int = 1000, rmax: int = 200_000) -> List[Instance]:

@@ -1,0 +1,83 @@
+"""Generate the golden fixtures: SCIP 11's own cons_linear propagation results on seeded instances.
+
+Runs oracle/_ref/scip_oracle (SCIP built from the reference sources by `make -C oracle ref`) in the
+probing-in-heuristic pattern described in oracle/scip_driver.c and stores, per case, the instance arrays
+(so that the fixtures do not depend on numpy's generator streams), SCIP's root fixpoint, and for node cases
+SCIP's per-node cutoff verdicts and changed bounds.  Cases:
+
+  root_mip_s{0,1,2}          2,000 x 5,000 root fixpoint, residual rule (maxeasyactivitydelta 0) and easy rule
+  root_mip_s0_nodes          200 branch-and-bound nodes on top of SCIP's root fixpoint
+  node_mip_small             1,500 x 3,000 general rows (log-uniform coefficients, infinite bounds) + 200 nodes
+  zipf_small                 1,500 x 3,000 Zipf row lengths up to 400 (rows longer than 64 entries)
+  set_cover / knapsack / network   one small instance of each uneven-batch family + 100 nodes
+
+Usage: python tests/golden/make_golden.py   (needs the SCIP sources; writes tests/golden/*.npz)
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from scip_gb300 import instances  # noqa: E402
+import oracle  # noqa: E402
+
+
+def node_arrays(nodes_out):
+    cut = np.array([x[0] for x in nodes_out], dtype=np.int8)
+    cnt = np.array([len(x[2]) for x in nodes_out], dtype=np.int64)
+    ptr = np.zeros(len(nodes_out) + 1, dtype=np.int64)
+    np.cumsum(cnt, out=ptr[1:])
+    col = np.concatenate([x[2] for x in nodes_out] + [np.zeros(0, np.int32)]).astype(np.int32)
+    lb = np.concatenate([x[3] for x in nodes_out] + [np.zeros(0)])
+    ub = np.concatenate([x[4] for x in nodes_out] + [np.zeros(0)])
+    return cut, ptr, col, lb, ub
+
+
+def save_case(name, inst, nnodes=0, node_seed=11):
+    out = {"rowptr": inst.rowptr, "colidx": inst.colidx, "vals": inst.vals, "lhs": inst.lhs, "rhs": inst.rhs,
+           "lb": inst.lb, "ub": inst.ub, "isint": inst.isint}
+    for easy in (False, True):
+        tag = "easy" if easy else "res"
+        rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy)
+        out[f"{tag}_rootcut"] = np.int8(rcut)
+        out[f"{tag}_rootlb"] = rlb
+        out[f"{tag}_rootub"] = rub
+    if nnodes:
+        # nodes start from SCIP's own root fixpoint (residual rule) so that node results compare node work only
+        rlb, rub = out["res_rootlb"], out["res_rootub"]
+        nodes = instances.node_batch(inst, rlb, rub, nnodes, seed=node_seed)
+        out["node_ptr"], out["node_col"], out["node_lb"], out["node_ub"] = nodes.ptr, nodes.col, nodes.lb, nodes.ub
+        for easy in (False, True):
+            tag = "easy" if easy else "res"
+            _, rlb2, rub2, res = oracle.run_scip(inst, nodes, easy=easy)
+            assert np.array_equal(rlb2, out[f"{tag}_rootlb"]) and np.array_equal(rub2, out[f"{tag}_rootub"])
+            cut, ptr, col, lb, ub = node_arrays(res)
+            out[f"{tag}_ncut"], out[f"{tag}_nptr"], out[f"{tag}_ncol"] = cut, ptr, col
+            out[f"{tag}_nlb"], out[f"{tag}_nub"] = lb, ub
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {nnodes} nodes, {os.path.getsize(path) // 1024} KiB")
+
+
+def main():
+    if not os.path.exists(oracle.SCIP_ORACLE):
+        raise SystemExit("oracle/_ref/scip_oracle missing: run `make -C oracle ref` where the SCIP sources are")
+    for s in (0, 1, 2):
+        save_case(f"root_mip_s{s}", instances.root_mip(s), nnodes=200 if s == 0 else 0)
+    save_case("node_mip_small", instances.node_mip(seed=21, m=1500, n=3000), nnodes=200)
+    save_case("zipf_small", instances.zipf_mip(seed=22, m=1500, n=3000, hi=400), nnodes=100)
+    rng = np.random.default_rng(np.random.PCG64(23))
+    save_case("set_cover", instances.set_cover(rng, 1200, 2400), nnodes=100)
+    save_case("knapsack", instances.multi_knapsack(rng, 1000, 2000), nnodes=100)
+    save_case("network", instances.network_flow(rng, 1500), nnodes=100)
+
+
+if __name__ == "__main__":
+    main()

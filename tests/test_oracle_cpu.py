@@ -1,0 +1,83 @@
+"""Known-answer tests of the oracle's arithmetic and rules on hand-checkable rows."""
+import numpy as np
+import pytest
+
+from scip_gb300.instances import INF, Instance, NodeBatch
+
+
+def single_rows(rows, lb, ub, isint):
+    """rows: list of (cols, vals, lhs, rhs)."""
+    rowptr = np.zeros(len(rows) + 1, dtype=np.int64)
+    cols, vals, lhs, rhs = [], [], [], []
+    for i, (c, v, l, r) in enumerate(rows):
+        rowptr[i + 1] = rowptr[i] + len(c)
+        cols += list(c)
+        vals += list(v)
+        lhs.append(l)
+        rhs.append(r)
+    return Instance(rowptr, np.array(cols, np.int32), np.array(vals, float), np.array(lhs, float),
+                    np.array(rhs, float), np.array(lb, float), np.array(ub, float), np.array(isint, np.int8))
+
+
+def test_compensated_activity(oracle_mod):
+    # 2^49 + 1/16 - 2^49: a plain double sum loses the 1/16 (half an ulp of 2^49), the compensated (TwoSum)
+    # sum keeps it; 2^49 stays below the huge-value threshold 1e15
+    big = 2.0 ** 49
+    inst = single_rows([([0, 1, 2], [1.0, 1.0, -1.0], -INF, INF)], [big, 0.0625, big], [big, 0.0625, big], [0, 0, 0])
+    act, cnt = oracle_mod.Oracle(inst).activities(inst.lb, inst.ub)
+    assert act[0, 0] + act[0, 1] == 0.0625
+    assert ((big + 0.0625) - big) == 0.0
+    assert not cnt.any()
+
+
+def test_infinity_and_huge_counters(oracle_mod):
+    # x0 in (-inf, 1], x1 in [0, inf), x2 in [2e15, 3e15] (huge contributions), x3 in [1, 2]
+    inst = single_rows([([0, 1, 2, 3], [2.0, -3.0, 1.0, 1.0], -INF, INF)],
+                       [-INF, 0.0, 2e15, 1.0], [1.0, INF, 3e15, 2.0], [0, 0, 0, 0])
+    act, cnt = oracle_mod.Oracle(inst).activities(inst.lb, inst.ub)
+    # min activity: 2*(-inf) -> neg inf; -3*(+inf) -> neg inf; 1*2e15 -> pos huge; 1*1 finite
+    # max activity: 2*1 finite; -3*0 = 0; 1*3e15 -> pos huge; 1*2 finite
+    assert list(cnt[0]) == [0, 2, 1, 0, 0, 0, 1, 0]
+    assert act[0, 0] + act[0, 1] == 1.0 and act[0, 2] + act[0, 3] == 4.0
+
+
+@pytest.mark.parametrize("rhs,expect_ub", [(19.0, 20.0), (18.0, 18.0)])
+def test_minimal_improvement_rule(oracle_mod, rhs, expect_ub):
+    # x + y <= rhs with integer x, y in [0, 20]: the upper bound 20 -> 19 improves by exactly 1.0, which SCIP's
+    # bound strengthening test (0.05 * min(ub - lb, |ub|) = 1.0, strict) rejects; 20 -> 18 is accepted
+    inst = single_rows([([0, 1], [1.0, 1.0], -INF, rhs)], [0.0, 0.0], [20.0, 20.0], [1, 1])
+    lb, ub, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0))
+    assert not r.cutoff
+    assert list(ub) == [expect_ub, expect_ub]
+
+
+def test_integer_rounding_and_chain(oracle_mod):
+    # 3x + 2y <= 7, x - z >= 1, z >= 0: x <= floor(7/3) = 2, y <= 3; x >= 1 + z >= 1 -> y <= 2
+    inst = single_rows([([0, 1], [3.0, 2.0], -INF, 7.0), ([0, 2], [1.0, -1.0], 1.0, INF)],
+                       [0.0, 0.0, 0.0], [10.0, 10.0, 10.0], [1, 1, 1])
+    lb, ub, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0))
+    assert not r.cutoff
+    assert list(lb) == [1.0, 0.0, 0.0] and list(ub) == [2.0, 2.0, 1.0]
+
+
+def test_cutoff_detected(oracle_mod):
+    # x + y >= 5 with x, y in [0, 2] is infeasible
+    inst = single_rows([([0, 1], [1.0, 1.0], 5.0, INF)], [0.0, 0.0], [2.0, 2.0], [1, 1])
+    _, _, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0))
+    assert r.cutoff == 1
+
+
+def test_single_entry_row_forces(oracle_mod):
+    # 4x <= 3.99 with continuous x in [0, 1]: the forced single-entry tightening accepts any improvement
+    inst = single_rows([([0], [4.0], -INF, 3.99)], [0.0], [1.0], [0])
+    lb, ub, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0))
+    assert ub[0] == pytest.approx(3.99 / 4.0, rel=1e-15)
+
+
+def test_node_outside_domain_is_cut_off(oracle_mod):
+    inst = single_rows([([0, 1], [1.0, 1.0], -INF, 10.0)], [0.0, 0.0], [5.0, 5.0], [1, 1])
+    nodes = NodeBatch(np.array([0, 1, 2], np.int64), np.array([0, 1], np.int32), np.array([7.0, 3.0]),
+                      np.array([7.0, 3.0]))
+    out = oracle_mod.Oracle(inst).propagate_nodes(inst.lb, inst.ub, nodes, oracle_mod.params(0.0), cap=4)
+    assert list(out["cutoff"]) == [1, 0]
+    assert out["n"][1] == 1 and out["col"][1, 0] == 1 and out["lb"][1, 0] == 3.0
