@@ -57,7 +57,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -129,11 +129,13 @@ def cpu_arm(inst, rlb, rub, nodes, par, nthreads, budget_s=15.0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nodes", type=int, default=NNODES)
     ap.add_argument("--maxeasy", type=float, default=0.0)
+    ap.add_argument("--quick", action="store_true", help="skip the plain-path and CPU arms (profiling runs)")
+    ap.add_argument("--shape", default="", help="threads_per_node,ctas_per_sm instead of autotuning (e.g. 128,0)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -215,6 +217,16 @@ def main():
     def step():
         return prop.propagate_nodes_device(t_lb, t_ub, N, t_ptr, t_col, t_nlb, t_nub, out, out_cap)
 
+    from scip_gb300 import autotune
+
+    tune_log = []
+    if args.shape:
+        shape = tuple(int(x) for x in args.shape.split(","))
+        prop.set_batch_shape(*shape)
+    else:
+        shape = autotune.tune_nodes(prop, step, ("nodes", inst.m, inst.n, inst.nnz, N), log=tune_log)
+    config["launch_shape"] = {"threads_per_node": shape[0], "ctas_per_sm": shape[1], "tuned_over": tune_log}
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -275,7 +287,7 @@ def main():
     d2h = N * (1 + 4 + 8 + 4) + 20 * used
 
     # plain path: the same nodes one at a time through the seeded single-problem call
-    plain_nodes = min(128, N)
+    plain_nodes = min(8 if args.quick else 128, N)
     t0 = time.perf_counter()
     for k in range(plain_nodes):
         lb, ub = rlb.copy(), rub.copy()
@@ -304,13 +316,14 @@ def main():
                       "root_ms": rres.kernel_ms, "root_rounds": rres.rounds},
             }
     if rank == 0:
-        import oracle as orc
+        if not args.quick:
+            import oracle as orc
 
-        orc.build()
-        par = orc.params(args.maxeasy)
-        cpu_v, sample = cpu_arm(inst, rlb, rub, nodes, par, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
-                                "kind": "port", "sample": sample}
+            orc.build()
+            par = orc.params(args.maxeasy)
+            cpu_v, sample = cpu_arm(inst, rlb, rub, nodes, par, os.cpu_count() or 1)
+            line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
+                                    "kind": "port", "sample": sample}
         print(json.dumps(line))
     prop.close()
     if world > 1:
