@@ -1,0 +1,401 @@
+/* prop_gpulinear.c -- SCIP propagator plugin over libgbp (see prop_gpulinear.h).
+ *
+ * Call path: SCIPpropExec (src/scip/prop.c:646) -> propExecGpulinear -> gbp_propagate (C ABI, one device
+ * round trip per call: local bounds and changed columns in, tightened bounds and the cutoff flag out) ->
+ * SCIPtightenVarLb/Ub for every moved bound.
+ */
+#include <float.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "prop_gpulinear.h"
+#include "scip/cons_linear.h"
+#include "gbp.h"
+
+#define PROP_NAME     "gpulinear"
+#define PROP_DESC     "linear-constraint bound propagation on a GB300 GPU (cons_linear rules, libgbp)"
+#define PROP_PRIORITY 1000 /* >= 0: runs before the constraint handlers' propagation (solve.c:481-591) */
+#define PROP_FREQ     1
+#define PROP_DELAY    FALSE
+#define PROP_TIMING   SCIP_PROPTIMING_BEFORELP
+
+struct SCIP_PropData
+{
+   gbp_ctx*              ctx;                /**< libgbp context (NULL while inactive) */
+   int                   device;             /**< CUDA device ordinal */
+   SCIP_Bool             replacelinear;      /**< switch cons_linear's propagation off at include time */
+   SCIP_Bool             failed;             /**< the GPU path failed or is unavailable: do not run */
+   int                   nconss;             /**< number of linear constraints the matrix was built from */
+   int                   nrows;              /**< rows in the matrix */
+   int                   ncols;              /**< columns = transformed variables */
+   SCIP_VAR**            vars;               /**< column -> variable */
+   int64_t*              rowptr;
+   int32_t*              colidx;
+   double*               vals;
+   double*               lhs;
+   double*               rhs;
+   int8_t*               isint;
+   double*               lb;                 /**< bounds handed to the device / returned from it */
+   double*               ub;
+   double*               snaplb;             /**< local bounds after the previous call */
+   double*               snapub;
+   SCIP_Bool             havesnap;
+   int32_t*              seeds;
+   double*               seedlo;
+   double*               seedhi;
+   SCIP_Longint          ncalls;
+   SCIP_Longint          nchgbds;
+   SCIP_Longint          ncutoffs;
+};
+
+static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   SCIPfreeMemoryArrayNull(scip, &pd->vars);
+   SCIPfreeMemoryArrayNull(scip, &pd->rowptr);
+   SCIPfreeMemoryArrayNull(scip, &pd->colidx);
+   SCIPfreeMemoryArrayNull(scip, &pd->vals);
+   SCIPfreeMemoryArrayNull(scip, &pd->lhs);
+   SCIPfreeMemoryArrayNull(scip, &pd->rhs);
+   SCIPfreeMemoryArrayNull(scip, &pd->isint);
+   SCIPfreeMemoryArrayNull(scip, &pd->lb);
+   SCIPfreeMemoryArrayNull(scip, &pd->ub);
+   SCIPfreeMemoryArrayNull(scip, &pd->snaplb);
+   SCIPfreeMemoryArrayNull(scip, &pd->snapub);
+   SCIPfreeMemoryArrayNull(scip, &pd->seeds);
+   SCIPfreeMemoryArrayNull(scip, &pd->seedlo);
+   SCIPfreeMemoryArrayNull(scip, &pd->seedhi);
+   pd->nrows = 0;
+   pd->ncols = 0;
+   pd->havesnap = FALSE;
+}
+
+/** copies the linear constraints into CSR form: active variables become columns (SCIPvarGetProbindex),
+ *  fixed variables move into the sides, constraints with other variables are left to cons_linear */
+static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   SCIP_CONSHDLR* conshdlr = SCIPfindConshdlr(scip, "linear");
+   SCIP_CONS** conss;
+   int nconss;
+   int nvars = SCIPgetNVars(scip);
+   SCIP_VAR** vars = SCIPgetVars(scip);
+   int64_t nnz = 0;
+   int64_t cap;
+   int c;
+   int j;
+
+   freeMatrix(scip, pd);
+   nconss = conshdlr == NULL ? 0 : SCIPconshdlrGetNConss(conshdlr);
+   conss = conshdlr == NULL ? NULL : SCIPconshdlrGetConss(conshdlr);
+   pd->nconss = nconss;
+   pd->ncols = nvars;
+
+   SCIP_CALL( SCIPduplicateMemoryArray(scip, &pd->vars, vars, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->isint, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->lb, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->ub, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snaplb, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snapub, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seeds, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seedlo, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seedhi, nvars > 0 ? nvars : 1) );
+   for( j = 0; j < nvars; ++j )
+      pd->isint[j] = SCIPvarIsIntegral(vars[j]) ? 1 : 0;
+
+   for( c = 0; c < nconss; ++c )
+      nnz += SCIPgetNVarsLinear(scip, conss[c]);
+   cap = nnz > 0 ? nnz : 1;
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowptr, nconss + 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->lhs, nconss > 0 ? nconss : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rhs, nconss > 0 ? nconss : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->vals, cap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->colidx, cap) );
+
+   pd->rowptr[0] = 0;
+   pd->nrows = 0;
+   for( c = 0; c < nconss; ++c )
+   {
+      SCIP_CONS* cons = conss[c];
+      SCIP_VAR** cvars = SCIPgetVarsLinear(scip, cons);
+      SCIP_Real* cvals = SCIPgetValsLinear(scip, cons);
+      int cn = SCIPgetNVarsLinear(scip, cons);
+      SCIP_Real l = SCIPgetLhsLinear(scip, cons);
+      SCIP_Real r = SCIPgetRhsLinear(scip, cons);
+      int64_t start = pd->rowptr[pd->nrows];
+      int64_t p = start;
+      SCIP_Bool ok = !SCIPconsIsModifiable(cons);
+      int q;
+
+      for( q = 0; q < cn && ok; ++q )
+      {
+         SCIP_VAR* v = cvars[q];
+         if( SCIPvarIsActive(v) )
+         {
+            pd->colidx[p] = (int32_t)SCIPvarGetProbindex(v);
+            pd->vals[p] = cvals[q];
+            ++p;
+         }
+         else if( SCIPvarGetStatus(v) == SCIP_VARSTATUS_FIXED )
+         {
+            SCIP_Real shift = cvals[q] * SCIPvarGetLbGlobal(v);
+            if( !SCIPisInfinity(scip, -l) )
+               l -= shift;
+            if( !SCIPisInfinity(scip, r) )
+               r -= shift;
+         }
+         else
+            ok = FALSE;
+      }
+      if( !ok || p == start )
+         continue;
+      pd->lhs[pd->nrows] = SCIPisInfinity(scip, -l) ? -SCIPinfinity(scip) : l;
+      pd->rhs[pd->nrows] = SCIPisInfinity(scip, r) ? SCIPinfinity(scip) : r;
+      pd->nrows++;
+      pd->rowptr[pd->nrows] = p;
+   }
+   return SCIP_OKAY;
+}
+
+static void disable(SCIP* scip, SCIP_PROPDATA* pd, const char* why, int rc)
+{
+   SCIPwarningMessage(scip, "propagator <%s> disabled: %s (%s%s%s); cons_linear keeps propagating\n", PROP_NAME, why,
+      gbp_error_string(rc), pd->ctx != NULL ? ": " : "", pd->ctx != NULL ? gbp_last_error(pd->ctx) : "");
+   pd->failed = TRUE;
+}
+
+/** numerics of the running SCIP (set.c / def.h) for the device rules */
+static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   gbp_params p;
+   SCIP_Real v;
+   gbp_default_params(&p);
+   p.infinity = SCIPinfinity(scip);
+   p.epsilon = SCIPepsilon(scip);
+   p.sumepsilon = SCIPsumepsilon(scip);
+   p.feastol = SCIPfeastol(scip);
+   p.hugeval = SCIPgetHugeValue(scip);
+   SCIP_CALL( SCIPgetRealParam(scip, "numerics/boundstreps", &v) );
+   p.boundstreps = v;
+   SCIP_CALL( SCIPgetRealParam(scip, "numerics/recompfac", &v) );
+   p.recompfac = v;
+   if( SCIPgetRealParam(scip, "constraints/linear/maxeasyactivitydelta", &v) == SCIP_OKAY )
+      p.maxeasyactivitydelta = v;
+   if( gbp_set_params(pd->ctx, &p) != GBP_OK )
+      return SCIP_INVALIDDATA;
+   return SCIP_OKAY;
+}
+
+static SCIP_RETCODE upload(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   int rc;
+   SCIP_CALL( buildMatrix(scip, pd) );
+   SCIP_CALL( setDeviceParams(scip, pd) );
+   rc = gbp_upload_problem(pd->ctx, pd->nrows, pd->ncols, pd->rowptr, pd->colidx, pd->vals, pd->lhs, pd->rhs, pd->isint);
+   if( rc != GBP_OK )
+      disable(scip, pd, "uploading the rows failed", rc);
+   pd->havesnap = FALSE;
+   return SCIP_OKAY;
+}
+
+/** replacelinear = TRUE switches cons_linear's propagation off (constraints/linear/propfreq, cons.c:2247) */
+static SCIP_DECL_PARAMCHGD(paramChgdReplacelinear)
+{
+   if( SCIPparamGetBool(param) )
+   {
+      SCIP_CALL( SCIPsetIntParam(scip, "constraints/linear/propfreq", -1) );
+   }
+   return SCIP_OKAY;
+}
+
+static SCIP_DECL_PROPFREE(propFreeGpulinear)
+{
+   SCIP_PROPDATA* pd = SCIPpropGetData(prop);
+   freeMatrix(scip, pd);
+   if( pd->ctx != NULL )
+      (void)gbp_destroy(pd->ctx);
+   SCIPfreeMemory(scip, &pd);
+   SCIPpropSetData(prop, NULL);
+   return SCIP_OKAY;
+}
+
+static SCIP_DECL_PROPINITSOL(propInitsolGpulinear)
+{
+   SCIP_PROPDATA* pd = SCIPpropGetData(prop);
+   int rc;
+   pd->failed = FALSE;
+   if( pd->ctx == NULL )
+   {
+      rc = gbp_create(&pd->ctx, pd->device, NULL);
+      if( rc != GBP_OK )
+      {
+         pd->ctx = NULL;
+         disable(scip, pd, "no usable GB300 device", rc);
+         SCIP_CALL( buildMatrix(scip, pd) );
+         return SCIP_OKAY;
+      }
+   }
+   SCIP_CALL( upload(scip, pd) );
+   return SCIP_OKAY;
+}
+
+static SCIP_DECL_PROPEXITSOL(propExitsolGpulinear)
+{
+   SCIP_PROPDATA* pd = SCIPpropGetData(prop);
+   freeMatrix(scip, pd);
+   return SCIP_OKAY;
+}
+
+static SCIP_DECL_PROPEXEC(propExecGpulinear)
+{
+   SCIP_PROPDATA* pd = SCIPpropGetData(prop);
+   SCIP_CONSHDLR* conshdlr;
+   int64_t nseed = -1;
+   int32_t cutoff = 0;
+   gbp_result res;
+   int rc;
+   int j;
+   SCIP_Bool reduced = FALSE;
+
+   *result = SCIP_DIDNOTRUN;
+   if( pd->failed || pd->ctx == NULL )
+      return SCIP_OKAY;
+
+   /* constraints added or removed since the upload: rebuild */
+   conshdlr = SCIPfindConshdlr(scip, "linear");
+   if( (conshdlr == NULL ? 0 : SCIPconshdlrGetNConss(conshdlr)) != pd->nconss || SCIPgetNVars(scip) != pd->ncols )
+   {
+      SCIP_CALL( upload(scip, pd) );
+      if( pd->failed )
+         return SCIP_OKAY;
+   }
+
+   for( j = 0; j < pd->ncols; ++j )
+   {
+      pd->lb[j] = SCIPvarGetLbLocal(pd->vars[j]);
+      pd->ub[j] = SCIPvarGetUbLocal(pd->vars[j]);
+   }
+   if( pd->havesnap )
+   {
+      /* columns that moved in either direction since the last call: their rows are re-propagated (a relaxed
+       * column can be re-tightened by its own rows after SCIP switched to another node) */
+      nseed = 0;
+      for( j = 0; j < pd->ncols; ++j )
+      {
+         if( pd->lb[j] != pd->snaplb[j] || pd->ub[j] != pd->snapub[j] )
+         {
+            pd->seeds[nseed] = j;
+            pd->seedlo[nseed] = -DBL_MAX;
+            pd->seedhi[nseed] = DBL_MAX;
+            ++nseed;
+         }
+      }
+      if( nseed == 0 )
+      {
+         *result = SCIP_DIDNOTFIND;
+         return SCIP_OKAY;
+      }
+   }
+
+   rc = gbp_propagate(pd->ctx, pd->lb, pd->ub, nseed, nseed > 0 ? pd->seeds : NULL, nseed > 0 ? pd->seedlo : NULL,
+      nseed > 0 ? pd->seedhi : NULL, &cutoff, &res);
+   pd->ncalls++;
+   if( rc != GBP_OK && rc != GBP_ERR_LIMIT )
+   {
+      disable(scip, pd, "propagation call failed", rc);
+      return SCIP_OKAY;
+   }
+   if( cutoff )
+   {
+      pd->ncutoffs++;
+      pd->havesnap = FALSE;
+      *result = SCIP_CUTOFF;
+      return SCIP_OKAY;
+   }
+
+   /* the device applied cons_linear's acceptance rules already: force the moves through */
+   for( j = 0; j < pd->ncols; ++j )
+   {
+      SCIP_VAR* var = pd->vars[j];
+      SCIP_Bool infeasible = FALSE;
+      SCIP_Bool tightened = FALSE;
+      if( pd->lb[j] > SCIPvarGetLbLocal(var) )
+      {
+         SCIP_CALL( SCIPtightenVarLb(scip, var, pd->lb[j], TRUE, &infeasible, &tightened) );
+         if( infeasible )
+         {
+            pd->havesnap = FALSE;
+            *result = SCIP_CUTOFF;
+            return SCIP_OKAY;
+         }
+         reduced = reduced || tightened;
+         pd->nchgbds += tightened ? 1 : 0;
+      }
+      if( pd->ub[j] < SCIPvarGetUbLocal(var) )
+      {
+         SCIP_CALL( SCIPtightenVarUb(scip, var, pd->ub[j], TRUE, &infeasible, &tightened) );
+         if( infeasible )
+         {
+            pd->havesnap = FALSE;
+            *result = SCIP_CUTOFF;
+            return SCIP_OKAY;
+         }
+         reduced = reduced || tightened;
+         pd->nchgbds += tightened ? 1 : 0;
+      }
+   }
+   for( j = 0; j < pd->ncols; ++j )
+   {
+      pd->snaplb[j] = SCIPvarGetLbLocal(pd->vars[j]);
+      pd->snapub[j] = SCIPvarGetUbLocal(pd->vars[j]);
+   }
+   pd->havesnap = TRUE;
+   *result = reduced ? SCIP_REDUCEDDOM : SCIP_DIDNOTFIND;
+   return SCIP_OKAY;
+}
+
+SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
+{
+   SCIP_PROPDATA* pd;
+   SCIP_PROP* prop = NULL;
+
+   SCIP_CALL( SCIPallocMemory(scip, &pd) );
+   memset(pd, 0, sizeof(*pd));
+   SCIP_CALL( SCIPincludePropBasic(scip, &prop, PROP_NAME, PROP_DESC, PROP_PRIORITY, PROP_FREQ, PROP_DELAY,
+         PROP_TIMING, propExecGpulinear, pd) );
+   SCIP_CALL( SCIPsetPropFree(scip, prop, propFreeGpulinear) );
+   SCIP_CALL( SCIPsetPropInitsol(scip, prop, propInitsolGpulinear) );
+   SCIP_CALL( SCIPsetPropExitsol(scip, prop, propExitsolGpulinear) );
+   SCIP_CALL( SCIPaddIntParam(scip, "propagating/" PROP_NAME "/device", "CUDA device ordinal of the GPU",
+         &pd->device, FALSE, 0, 0, 1024, NULL, NULL) );
+   SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacelinear",
+         "switch off cons_linear's own propagation (constraints/linear/propfreq = -1) when included",
+         &pd->replacelinear, FALSE, FALSE, paramChgdReplacelinear, NULL) );
+   return SCIP_OKAY;
+}
+
+SCIP_RETCODE SCIPgetGpulinearMatrix(SCIP* scip, int* nrows, int* ncols, const int64_t** rowptr, const int32_t** colidx,
+   const double** vals, const double** lhs, const double** rhs)
+{
+   SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
+   SCIP_PROPDATA* pd;
+   if( prop == NULL )
+      return SCIP_PLUGINNOTFOUND;
+   pd = SCIPpropGetData(prop);
+   *nrows = pd->nrows;
+   *ncols = pd->ncols;
+   *rowptr = pd->rowptr;
+   *colidx = pd->colidx;
+   *vals = pd->vals;
+   *lhs = pd->lhs;
+   *rhs = pd->rhs;
+   return SCIP_OKAY;
+}
+
+SCIP_Bool SCIPgpulinearIsActive(SCIP* scip)
+{
+   SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
+   SCIP_PROPDATA* pd;
+   if( prop == NULL )
+      return FALSE;
+   pd = SCIPpropGetData(prop);
+   return pd->ctx != NULL && !pd->failed;
+}

@@ -1,0 +1,41 @@
+/* prop_gpulinear.h -- SCIP propagator that runs linear-constraint bound propagation on a GB300 GPU.
+ *
+ * Registered through SCIPincludePropBasic (src/scip/scip_prop.c:118-140) with a SCIP_DECL_PROPEXEC callback
+ * (src/scip/type_prop.h:217).  At PROPINITSOL it copies every linear constraint of the transformed problem
+ * (SCIPgetVarsLinear/SCIPgetValsLinear/SCIPgetLhsLinear/SCIPgetRhsLinear, src/scip/cons_linear.h:263-307) into
+ * libgbp's device-resident CSR/CSC; each PROPEXEC hands the current local bounds and the columns that changed
+ * since its last call to gbp_propagate (include/gbp.h), then writes the tightened bounds back with
+ * SCIPtightenVarLb/SCIPtightenVarUb (src/scip/scip_var.c:6402/6652) or reports SCIP_CUTOFF.  The device runs
+ * the propagation rules of cons_linear (tightenVarBounds / tightenVarBoundsEasy) to a fixpoint.
+ *
+ * Parameters (propagating/gpulinear/...): device (CUDA ordinal, default 0) and replacelinear (default FALSE:
+ * if TRUE, SCIPincludePropGpulinear sets constraints/linear/propfreq = -1 so that the GPU replaces
+ * cons_linear's own propagation; cons_linear keeps checking, enforcing and presolving).
+ * Without a usable GPU the propagator disables itself with a warning and SCIP continues with cons_linear.
+ */
+#ifndef PROP_GPULINEAR_H
+#define PROP_GPULINEAR_H
+
+#include "scip/scip.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/** includes the GPU linear propagator in SCIP */
+SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip);
+
+/** the rows the propagator uploads (valid after PROPINITSOL, i.e. once solving has started): CSR arrays owned
+ *  by the propagator; column j is SCIPgetVars(scip)[j].  Rows with a variable that is neither active nor
+ *  fixed (aggregated, multi-aggregated) are left to cons_linear and are not part of the matrix. */
+SCIP_RETCODE SCIPgetGpulinearMatrix(SCIP* scip, int* nrows, int* ncols, const int64_t** rowptr, const int32_t** colidx,
+   const double** vals, const double** lhs, const double** rhs);
+
+/** whether the propagator runs on a GPU (FALSE before PROPINITSOL or after it disabled itself) */
+SCIP_Bool SCIPgpulinearIsActive(SCIP* scip);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

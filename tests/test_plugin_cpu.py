@@ -1,0 +1,71 @@
+"""The SCIP propagator plugin, built and run inside SCIP itself (compiled from the reference sources into
+oracle/_ref).  On a machine without an sm_103 GPU the plugin must register, extract exactly the problem's rows,
+disable itself with a warning and leave SCIP's own propagation to produce the root fixpoint.  Skipped where the
+SCIP build is absent."""
+import os
+import subprocess
+
+import pytest
+
+from scip_gb300 import instances
+from scip_gb300.build import LIBDIR, build_libgbp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.path.join(ROOT, "oracle", "_ref")
+LIBSCIP = os.path.join(REF, "libscip.a")
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    if not os.path.exists(LIBSCIP):
+        pytest.skip("SCIP build (oracle/_ref) not present")
+    build_libgbp()
+    out = tmp_path_factory.mktemp("plugin")
+    exe = str(out / "plugin_driver")
+    src = [os.path.join(ROOT, "tests", "plugin", "plugin_driver.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c")]
+    inc = ["-I" + os.path.join(REF, "include"), "-I/root/reference/src", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(ROOT, "scip_gb300", "plugin")]
+    cmd = ["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", *inc, "-o", exe, *src, LIBSCIP,
+           "-L" + LIBDIR, "-lgbp", "-Wl,-rpath," + LIBDIR, "-lstdc++", "-lm", "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def run(driver, inst, tmp_path, *args):
+    p = str(tmp_path / "inst.bin")
+    inst.write(p)
+    r = subprocess.run([driver, p, *args], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = dict(l.split(" ", 1) for l in r.stdout.strip().splitlines())
+    return lines, r.stdout + r.stderr
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the behaviour without a GPU")
+def test_plugin_without_gpu_extracts_rows_and_steps_aside(driver, oracle_mod, tmp_path):
+    inst = instances.root_mip(0)
+    lines, text = run(driver, inst, tmp_path)
+    assert lines["active"] == "0"
+    assert "propagator <gpulinear> disabled" in text
+    m, n, nnz, ok = lines["matrix"].split()
+    assert (int(m), int(n), int(nnz), ok) == (inst.m, inst.n, inst.nnz, "1")
+    # cons_linear still propagates: the root equals SCIP's own root fixpoint
+    _, slb, sub, _ = oracle_mod.run_scip(inst)
+    cut, s_lb, s_ub = lines["root"].split()
+    assert cut == "0"
+    assert float(s_lb) == pytest.approx(float(slb.sum()), rel=1e-12)
+    assert float(s_ub) == pytest.approx(float(sub.sum()), rel=1e-12)
+
+
+def test_replacelinear_switches_cons_linear_propagation_off(driver, tmp_path):
+    inst = instances.root_mip(1, m=200, n=500)
+    lines, _ = run(driver, inst, tmp_path, "--replace")
+    assert lines["propfreq"] == "-1"
