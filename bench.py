@@ -126,6 +126,97 @@ def cpu_arm(inst, rlb, rub, nodes, par, nthreads, budget_s=15.0):
         take *= 4
 
 
+def other_workload(args):
+    """Root fixpoints of the uneven-instance batch (all instances in one block-diagonal problem) or of the large
+    Zipf instance (plain path); prints one JSON line."""
+    import torch
+    from scip_gb300 import gbp, instances
+    from scip_gb300.build import build_libgbp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    build_libgbp()
+    t0 = time.perf_counter()
+    if args.workload == "uneven":
+        insts = instances.uneven_batch(seed=4, count=args.instances)
+        big, row_off, col_off = instances.concat_instances(insts)
+        units = len(insts)
+        cfg = {"workload": f"{units} distinct instances (set cover / multi-knapsack / network flow), rows log-uniform "
+                           "in [1e3, 2e5], all in one block-diagonal problem, every instance to its root fixpoint",
+               "rows": big.m, "cols": big.n, "nnz": big.nnz}
+    else:
+        big = instances.zipf_mip(seed=1)
+        units = 1
+        cfg = {"workload": "one 1,000,000 x 2,000,000 instance, Zipf(1.5) row lengths in [2, 5000], root fixpoint "
+                           "through the plain path", "rows": big.m, "cols": big.n, "nnz": big.nnz}
+    gen_s = time.perf_counter() - t0
+    prop = gbp.Propagator(0, params=gbp.default_params(maxeasy=args.maxeasy))
+    t0 = time.perf_counter()
+    if args.workload == "uneven":
+        prop.upload_instances(insts)
+    else:
+        prop.upload(big)
+    up_s = time.perf_counter() - t0
+    d = torch.device("cuda", 0)
+    lb0 = torch.from_numpy(big.lb).to(d)
+    ub0 = torch.from_numpy(big.ub).to(d)
+    lb, ub = lb0.clone(), ub0.clone()
+    cut = torch.zeros(max(units, 1), dtype=torch.int8, device=d)
+    stream = torch.cuda.ExternalStream(prop.stream())
+
+    def step():
+        if args.workload == "uneven":
+            return prop.propagate_instances_device(lb, ub, cut)
+        return prop.propagate_device(lb, ub)[1]
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            lb.copy_(lb0)
+            ub.copy_(ub0)
+        step()
+    times, res = [], None
+    clocks = ClockSampler()
+    clocks.start()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            lb.copy_(lb0)
+            ub.copy_(ub0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        res = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    ms = float(np.mean(times))
+    algo = algorithmic_bytes(res.rows, res.nnz, res.changes, big.nnz / max(big.n, 1))
+    peak, peak_kind = measured_peak()
+    line = {"metric": "node-fixpoints/sec", "value": units / (ms / 1e3), "unit": "instance-fixpoints/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": cfg, "rounds": res.rounds, "cutoffs": res.cutoff, "rows_processed": res.rows,
+            "nnz_per_s": res.nnz / (ms / 1e3), "launches": res.launches, "generate_s": gen_s, "upload_s": up_s,
+            "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind},
+            "clocks": clk}
+    if args.workload == "uneven" and not args.quick:
+        import oracle as orc
+        from concurrent.futures import ThreadPoolExecutor
+
+        orc.build()
+        par = orc.params(args.maxeasy)
+        take = insts[: max(8, len(insts) // 8)]
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+            list(ex.map(lambda i: orc.Oracle(i).propagate(i.lb, i.ub, par), take))
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(take) / dt, "unit": "instance-fixpoints/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": f"{len(take)} of {len(insts)} instances, {dt:.2f} s "
+                                                          "(includes the oracle's CSC build per instance)"}
+    print(json.dumps(line))
+    prop.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -136,7 +227,13 @@ def main():
     ap.add_argument("--maxeasy", type=float, default=0.0)
     ap.add_argument("--quick", action="store_true", help="skip the plain-path and CPU arms (profiling runs)")
     ap.add_argument("--shape", default="", help="threads_per_node,ctas_per_sm instead of autotuning (e.g. 128,0)")
+    ap.add_argument("--workload", default="nodes", choices=["nodes", "uneven", "zipf"],
+                    help="nodes: batched B&B nodes (headline); uneven: 512 distinct instances in one problem; "
+                         "zipf: one 1M x 2M instance through the plain path")
+    ap.add_argument("--instances", type=int, default=512)
     args = ap.parse_args()
+    if args.workload != "nodes":
+        return other_workload(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -104,6 +104,19 @@ int gbp_propagate_device(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, co
  * minposhuge, minneghuge, maxposinf, maxneginf, maxposhuge, maxneghuge; for all m rows. */
 int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double* act, int32_t* cnt);
 
+/* ---------------------------------------------------------------- batched path: distinct instances
+ * Uneven independent instances (each a set of linear rows with its own columns) propagated together: instance k
+ * owns rows [row_off[k], row_off[k+1]) and columns [col_off[k], col_off[k+1]) of one block-diagonal problem whose
+ * rows reference only their own instance's columns (global column indices).  gbp_propagate_instances runs every
+ * instance's root fixpoint from the given bounds -- what SCIP's root propagation does per instance -- with the
+ * frontier rows of all instances in the same launches; inst_cutoff[k] = 1 marks an infeasible instance (its
+ * bounds are then meaningless).  The upload replaces any problem uploaded before. */
+int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, const int64_t* col_off,
+   const int64_t* rowptr, const int32_t* colidx, const double* vals, const double* lhs, const double* rhs,
+   const int8_t* isint);
+int gbp_propagate_instances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
+int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
+
 /* ---------------------------------------------------------------- batched path: branch-and-bound nodes
  * nnodes nodes share the uploaded rows and the base bounds baselb/baseub (length n); node k applies the
  * bound changes chg_col/chg_lb/chg_ub[ptr[k] .. ptr[k+1]) (tightenings, as SCIPchgVarLb/UbProbing; a column

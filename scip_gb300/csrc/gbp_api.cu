@@ -56,6 +56,13 @@ struct gbp_ctx {
   int64_t seedcap = 0;
   int* h_ctr = nullptr;  // pinned
 
+  // several instances uploaded as one block-diagonal problem
+  int64_t ninst = 0;
+  int32_t* d_rowinst = nullptr;
+  int32_t* d_colinst = nullptr;
+  int* d_instcut = nullptr;
+  bool instmode = false;  // propagateCore works per instance
+
   // batched path
   int ctas_per_sm = 0;
   int node_threads = 32;
@@ -91,7 +98,8 @@ static int fail(gbp_ctx* ctx, int code, const std::string& msg) {
 static void freeProblem(gbp_ctx* ctx) {
   void* ptrs[] = {ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint, ctx->d_colptr,
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
-                  ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage};
+                  ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
+                  ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -99,14 +107,17 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_lb = nullptr; ctx->d_ub = nullptr; ctx->d_cand = nullptr; ctx->d_cflag = nullptr;
   ctx->d_touched = nullptr; ctx->d_list[0] = ctx->d_list[1] = nullptr; ctx->d_rowstamp = nullptr;
   ctx->d_allrows = nullptr; ctx->d_base = nullptr; ctx->slot_mem = nullptr; ctx->stage = nullptr;
+  ctx->d_rowinst = nullptr; ctx->d_colinst = nullptr; ctx->d_instcut = nullptr; ctx->ninst = 0;
   ctx->stage_bytes = 0;
   ctx->nslots = 0;
   ctx->has_problem = false;
 }
 
-static Prob devProb(const gbp_ctx* ctx) {
+static Prob devProb(const gbp_ctx* ctx, bool instances = false) {
   return Prob{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
-              ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity};
+              ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity,
+              instances ? ctx->d_rowinst : nullptr, instances ? ctx->d_colinst : nullptr,
+              instances ? ctx->d_instcut : nullptr};
 }
 
 static int gridFor(const gbp_ctx* ctx, int64_t work, int per_block = 256, int cap_per_sm = 16) {
@@ -371,7 +382,7 @@ static int nextStamp(gbp_ctx* ctx) {
 
 static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
                          const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
-  const Prob P = devProb(ctx);
+  const Prob P = devProb(ctx, ctx->instmode);
   const Num s = ctx->num;
   Cands C = plainCands(ctx);
   const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
@@ -550,6 +561,92 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
   cudaFree(d_act);
   cudaFree(d_cnt);
   return GBP_OK;
+}
+
+// ------------------------------------------------------------------------------------------ instances
+int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, const int64_t* col_off,
+                         const int64_t* rowptr, const int32_t* colidx, const double* vals, const double* lhs,
+                         const double* rhs, const int8_t* isint) {
+  if (!ctx || ninst < 1 || !row_off || !col_off || !rowptr) return fail(ctx, GBP_ERR_INVALID, "null argument");
+  if (ninst >= (int64_t(1) << 31) - 1) return fail(ctx, GBP_ERR_INVALID, "too many instances");
+  if (row_off[0] != 0 || col_off[0] != 0) return fail(ctx, GBP_ERR_INVALID, "offsets must start at 0");
+  for (int64_t k = 0; k < ninst; ++k)
+    if (row_off[k + 1] < row_off[k] || col_off[k + 1] < col_off[k])
+      return fail(ctx, GBP_ERR_INVALID, "instance offsets not monotone");
+  const int64_t m = row_off[ninst], n = col_off[ninst];
+  std::vector<int32_t> rowinst(std::max<int64_t>(m, 1)), colinst(std::max<int64_t>(n, 1));
+  for (int64_t k = 0; k < ninst; ++k) {
+    for (int64_t i = row_off[k]; i < row_off[k + 1]; ++i) rowinst[i] = (int32_t)k;
+    for (int64_t j = col_off[k]; j < col_off[k + 1]; ++j) colinst[j] = (int32_t)k;
+  }
+  if (m > 0 && rowptr[0] == 0) {
+    for (int64_t i = 0; i < m; ++i) {
+      if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
+      for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p)
+        if (colidx[p] < 0 || colidx[p] >= n || colinst[colidx[p]] != rowinst[i])
+          return fail(ctx, GBP_ERR_INVALID, "a row references a column of another instance");
+    }
+  }
+  int rc = gbp_upload_problem(ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
+  if (rc != GBP_OK) return rc;
+  CK(cudaMalloc(&ctx->d_rowinst, rowinst.size() * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->d_colinst, colinst.size() * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->d_instcut, ninst * sizeof(int)));
+  CK(cudaMemcpyAsync(ctx->d_rowinst, rowinst.data(), rowinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_colinst, colinst.data(), colinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->ninst = ninst;
+  return GBP_OK;
+}
+
+static int propagateInstances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, bool host, gbp_result* res) {
+  if (!ctx || !ctx->has_problem || ctx->ninst < 1 || !lb || !ub || !inst_cutoff)
+    return fail(ctx, GBP_ERR_INVALID, "no instances uploaded or null argument");
+  CK(cudaSetDevice(ctx->device));
+  const size_t nb = (size_t)ctx->n * sizeof(double);
+  double* dlb = lb;
+  double* dub = ub;
+  if (host) {
+    dlb = ctx->d_lb;
+    dub = ctx->d_ub;
+    if (nb) {
+      CK(cudaMemcpyAsync(dlb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(dub, ub, nb, cudaMemcpyHostToDevice, ctx->stream));
+    }
+  }
+  CK(cudaMemsetAsync(ctx->d_instcut, 0, ctx->ninst * sizeof(int), ctx->stream));
+  ctx->instmode = true;
+  int32_t anycut = 0;
+  int rc = propagateCore(ctx, dlb, dub, -1, nullptr, nullptr, nullptr, &anycut, res);
+  ctx->instmode = false;
+  if (rc != GBP_OK && rc != GBP_ERR_LIMIT) return rc;
+  std::vector<int> cut(ctx->ninst);
+  CK(cudaMemcpyAsync(cut.data(), ctx->d_instcut, ctx->ninst * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (host && nb) {
+    CK(cudaMemcpyAsync(lb, dlb, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ub, dub, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  int ncut = 0;
+  for (int64_t k = 0; k < ctx->ninst; ++k) {
+    inst_cutoff[k] = cut[k] ? 1 : 0;
+    ncut += cut[k] ? 1 : 0;
+  }
+  if (res) {
+    res->cutoff = ncut;
+    res->status = rc == GBP_ERR_LIMIT ? 2 : 0;
+  }
+  return rc;
+}
+
+int gbp_propagate_instances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res) {
+  return propagateInstances(ctx, lb, ub, inst_cutoff, true, res);
+}
+
+int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res) {
+  return propagateInstances(ctx, lb, ub, inst_cutoff, false, res);
 }
 
 // ------------------------------------------------------------------------------------------ batched path

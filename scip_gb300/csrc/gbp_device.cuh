@@ -36,7 +36,21 @@ struct Prob {
   const int32_t* rowidx;   // plain CSC (only read when cscrow is null)
   const double* cvals;
   double inf;              // infinity threshold for the relevance test on plain CSC
+  // several independent instances in one block-diagonal problem (all null for a single problem)
+  const int32_t* rowinst;  // instance of each row
+  const int32_t* colinst;  // instance of each column
+  int* instcut;            // per-instance cutoff flags
 };
+
+// rows of an instance that is already infeasible are skipped
+__device__ __forceinline__ bool rowDead(const Prob& P, int i) {
+  return P.instcut != nullptr && P.instcut[P.rowinst[i]] != 0;
+}
+// infeasibility found by row i: the row's instance (instances) or the whole problem (*cut)
+__device__ __forceinline__ void cutRow(const Prob& P, int i, int* cut) {
+  if (P.instcut != nullptr) atomicExch(&P.instcut[P.rowinst[i]], 1);
+  else *cut = 1;
+}
 
 struct Cands {
   long long* cub;   // best non-forced upper bound candidate (key), KEY_NONE_UB when empty
@@ -511,12 +525,12 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
 
     int nsel = 0;
     bool full = false;
-    if (tid < cnt) {
+    if (tid < cnt && !rowDead(P, rb.order[tid])) {
       const int i = rb.order[tid];
       Act a;
       bool easy = false;
       unsigned char sel[MAXSEL];
-      if (scanRow(s, P, B, i, a, easy, sel, nsel, full, st)) *cut = 1;
+      if (scanRow(s, P, B, i, a, easy, sel, nsel, full, st)) cutRow(P, i, cut);
       rb.act[tid] = a;
       rb.lhs[tid] = P.lhs[i];
       rb.rhs[tid] = P.rhs[i];
@@ -578,7 +592,7 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
       };
       if (columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, p1 - p0 == 1, j, v, l, u, P.isint[j] != 0, C,
                            st.cands, relres))
-        *cut = 1;
+        cutRow(P, rb.order[o], cut);
     }
     __syncthreads();
   }

@@ -75,9 +75,14 @@ __global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, co
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  bool cut = false;
-  for (int w = warp; w < n; w += nwarps) cut |= rowWarp(s, P, B, list[cap - 1 - w], C, st);
-  if (cut && lane == 0) atomicExch(cutoff, 1);
+  for (int w = warp; w < n; w += nwarps) {
+    const int row = list[cap - 1 - w];
+    if (rowDead(P, row)) continue;
+    if (rowWarp(s, P, B, row, C, st) && lane == 0) {
+      if (P.instcut != nullptr) atomicExch(&P.instcut[P.rowinst[row]], 1);
+      else atomicExch(cutoff, 1);
+    }
+  }
   flushStats(stats, st);
 }
 
@@ -89,7 +94,12 @@ __global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     int j = C.touched[t];
     double l = lb[j], u = ub[j], nl, nu;
-    if (applyColumn(s, P.isint[j] != 0, l, u, C, j, nl, nu)) {
+    const bool c = applyColumn(s, P.isint[j] != 0, l, u, C, j, nl, nu);
+    if (P.instcut != nullptr) {
+      int* flag = &P.instcut[P.colinst[j]];
+      if (c) atomicExch(flag, 1);
+      if (c || *flag) continue;
+    } else if (c) {
       cut = true;
       continue;
     }

@@ -31,7 +31,8 @@ GBP_ERR_TOO_LARGE = -8
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
            "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
-           "gbp_propagate_nodes_noalloc"]
+           "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
+           "gbp_propagate_instances_device"]
 
 
 class GbpParams(ctypes.Structure):
@@ -88,6 +89,9 @@ def load_library(path: Optional[str] = None):
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
     L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32, ctypes.c_int32]
+    L.gbp_upload_instances.argtypes = [_P, ctypes.c_int64] + [_P] * 8
+    L.gbp_propagate_instances.argtypes = [_P, _P, _P, _P, ctypes.POINTER(GbpResult)]
+    L.gbp_propagate_instances_device.argtypes = L.gbp_propagate_instances.argtypes
     L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
                                               + [_P] * 11 + [ctypes.c_int64, ctypes.POINTER(GbpParams), _P,
                                                               ctypes.POINTER(GbpResult)])
@@ -203,6 +207,35 @@ class Propagator:
                                       ctypes.byref(cut), ctypes.byref(res))
         self._check(rc, allow=(GBP_ERR_LIMIT,))
         return lb, ub, bool(cut.value), res
+
+    def upload_instances(self, insts):
+        """Upload several independent instances as one block-diagonal problem; returns (row_off, col_off)."""
+        from .instances import concat_instances
+
+        big, row_off, col_off = concat_instances(insts)
+        self._inst_off = (row_off, col_off)
+        keep = [np.ascontiguousarray(a) for a in (row_off, col_off, big.rowptr, big.colidx, big.vals, big.lhs,
+                                                   big.rhs, big.isint)]
+        self._check(self.L.gbp_upload_instances(self.h, len(insts), *[_ptr(a) for a in keep]))
+        self.m, self.n = big.m, big.n
+        return row_off, col_off
+
+    def propagate_instances(self, lb, ub):
+        """Host bound vectors of the block-diagonal problem; returns (lb, ub, cutoff per instance, GbpResult)."""
+        lb = np.array(lb, dtype=np.float64)
+        ub = np.array(ub, dtype=np.float64)
+        cut = np.zeros(len(self._inst_off[0]) - 1, dtype=np.int8)
+        res = GbpResult()
+        self._check(self.L.gbp_propagate_instances(self.h, _ptr(lb), _ptr(ub), _ptr(cut), ctypes.byref(res)),
+                    allow=(GBP_ERR_LIMIT,))
+        return lb, ub, cut, res
+
+    def propagate_instances_device(self, lb, ub, cut):
+        """Device tensors (float64 bounds, int8 cutoff per instance); returns GbpResult."""
+        res = GbpResult()
+        self._check(self.L.gbp_propagate_instances_device(self.h, _ptr(lb), _ptr(ub), _ptr(cut), ctypes.byref(res)),
+                    allow=(GBP_ERR_LIMIT,))
+        return res
 
     def propagate_device(self, lb, ub):
         """Device bound vectors (torch float64 tensors), all rows seeded; returns (cutoff, GbpResult)."""

@@ -310,6 +310,28 @@ def uneven_batch(seed: int = 4, count: int = 512, rmin: int = 1000, rmax: int = 
     return out
 
 
+def concat_instances(insts: List[Instance]):
+    """Block-diagonal union of independent instances: (instance, row_off, col_off) with instance k owning rows
+    row_off[k]:row_off[k+1] and columns col_off[k]:col_off[k+1]."""
+    row_off = np.zeros(len(insts) + 1, dtype=np.int64)
+    col_off = np.zeros(len(insts) + 1, dtype=np.int64)
+    nnz_off = np.zeros(len(insts) + 1, dtype=np.int64)
+    for k, inst in enumerate(insts):
+        row_off[k + 1] = row_off[k] + inst.m
+        col_off[k + 1] = col_off[k] + inst.n
+        nnz_off[k + 1] = nnz_off[k] + inst.nnz
+    rowptr = np.zeros(int(row_off[-1]) + 1, dtype=np.int64)
+    colidx = np.empty(int(nnz_off[-1]), dtype=np.int32)
+    for k, inst in enumerate(insts):
+        rowptr[row_off[k] + 1:row_off[k + 1] + 1] = inst.rowptr[1:] + nnz_off[k]
+        colidx[nnz_off[k]:nnz_off[k + 1]] = inst.colidx + col_off[k]
+    cat = lambda f: np.concatenate([getattr(i, f) for i in insts])
+    x0 = np.concatenate([i.x0 for i in insts]) if all(i.x0 is not None for i in insts) else None
+    big = Instance(rowptr, colidx, cat("vals"), cat("lhs"), cat("rhs"), cat("lb"), cat("ub"), cat("isint"),
+                   name=f"{len(insts)} instances", x0=x0)
+    return big, row_off, col_off
+
+
 # ---------------------------------------------------------------- result files of the SCIP oracle
 def read_oracle_output(path: str):
     """Parse the oracle driver's output: (rootcutoff, rootlb, rootub, nodes) where nodes is a list of

@@ -121,3 +121,27 @@ def test_nodes_seeded_plain_path_equals_batched(gpu_prop, oracle_mod):
             elb[c] = l
             eub[c] = u
             assert np.array_equal(plb, elb) and np.array_equal(pub, eub)
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_uneven_instances_in_one_problem_match_oracle_per_instance(gpu_prop, oracle_mod, maxeasy):
+    """Independent instances uploaded as one block-diagonal problem: each instance's result equals the oracle
+    run on that instance alone (also covering an instance that becomes infeasible)."""
+    insts = instances.uneven_batch(seed=8, count=12, rmin=300, rmax=6000)
+    # one infeasible instance: x + y >= 5 with x, y in [0, 2]
+    from scip_gb300.instances import Instance
+    bad = Instance(np.array([0, 2], np.int64), np.array([0, 1], np.int32), np.array([1.0, 1.0]), np.array([5.0]),
+                   np.array([1e20]), np.zeros(2), np.full(2, 2.0), np.ones(2, np.int8), x0=np.zeros(2))
+    insts.insert(5, bad)
+    gpu_prop.set_params(_params(maxeasy))
+    row_off, col_off = gpu_prop.upload_instances(insts)
+    lb = np.concatenate([i.lb for i in insts])
+    ub = np.concatenate([i.ub for i in insts])
+    glb, gub, cut, res = gpu_prop.propagate_instances(lb, ub)
+    assert cut[5] == 1
+    for k, inst in enumerate(insts):
+        olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(maxeasy))
+        assert bool(cut[k]) == bool(ores.cutoff), f"instance {k}"
+        if not cut[k]:
+            sl = slice(col_off[k], col_off[k + 1])
+            assert np.array_equal(glb[sl], olb) and np.array_equal(gub[sl], oub), f"instance {k}"
