@@ -12,7 +12,7 @@
  * GBP_ERR_* code (no exceptions cross the boundary; gbp_error_string() names the code and
  * gbp_last_error() gives the context's last message).  Host pointers are ordinary CPU memory unless the
  * function name ends in _device, in which case every array argument is a device pointer on the context's
- * GPU.  Infinite sides and bounds are +-params.infinity (1e20 by default), as in SCIP.
+ * GPU; scalar out-parameters (cutoff, res) are always host pointers.  Infinite sides and bounds are +-params.infinity (1e20 by default), as in SCIP.
  *
  * Rows are stored once on the device in CSR and CSC form; bound vectors, node bound changes and results
  * are the only per-call traffic.  One context = one GPU = one CUDA stream; calls on a context must not

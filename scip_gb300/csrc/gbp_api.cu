@@ -628,10 +628,12 @@ static int propagateInstances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst
     CK(cudaMemcpyAsync(lb, dlb, nb, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ub, dub, nb, cudaMemcpyDeviceToHost, ctx->stream));
   }
+  if (!host)  // inst_cutoff is a device array: convert the flags on the device
+    CK(launchFlags8(ctx->stream, gridFor(ctx, ctx->ninst), ctx->d_instcut, inst_cutoff, ctx->ninst));
   CK(cudaStreamSynchronize(ctx->stream));
   int ncut = 0;
   for (int64_t k = 0; k < ctx->ninst; ++k) {
-    inst_cutoff[k] = cut[k] ? 1 : 0;
+    if (host) inst_cutoff[k] = cut[k] ? 1 : 0;
     ncut += cut[k] ? 1 : 0;
   }
   if (res) {

@@ -111,5 +111,6 @@ cudaError_t nodesOccupancy(int threads, int* blocksPerSm);
 cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double* cvals, const int32_t* rowidx,
                            const double* lhs, const double* rhs, double inf, uint32_t* out);
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v);
+cudaError_t launchFlags8(cudaStream_t st, int grid, const int* in, int8_t* out, int64_t n);
 
 }  // namespace gbp

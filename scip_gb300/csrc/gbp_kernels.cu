@@ -193,6 +193,11 @@ __global__ void k_pack(const double* lb, const double* ub, double2* out, int64_t
     out[j] = make_double2(lb[j], ub[j]);
 }
 
+__global__ void k_flags8(const int* in, int8_t* out, int64_t n) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = in[j] != 0 ? 1 : 0;
+}
+
 __global__ void k_fill64(long long* p, int64_t n, long long v) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
     p[j] = v;
@@ -427,6 +432,10 @@ cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob
 }
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n) {
   k_pack<<<grid, 256, 0, st>>>(lb, ub, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launchFlags8(cudaStream_t st, int grid, const int* in, int8_t* out, int64_t n) {
+  k_flags8<<<grid, 256, 0, st>>>(in, out, n);
   return cudaGetLastError();
 }
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v) {

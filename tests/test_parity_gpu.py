@@ -145,3 +145,23 @@ def test_uneven_instances_in_one_problem_match_oracle_per_instance(gpu_prop, ora
         if not cut[k]:
             sl = slice(col_off[k], col_off[k + 1])
             assert np.array_equal(glb[sl], olb) and np.array_equal(gub[sl], oub), f"instance {k}"
+
+
+def test_uneven_instances_device_variant(gpu_prop, oracle_mod):
+    """gbp_propagate_instances_device: bounds and per-instance cutoff flags in device memory."""
+    torch = pytest.importorskip("torch")
+    insts = instances.uneven_batch(seed=9, count=9, rmin=300, rmax=3000)
+    gpu_prop.set_params(_params(0.0))
+    row_off, col_off = gpu_prop.upload_instances(insts)
+    d = torch.device("cuda", 0)
+    lb = torch.from_numpy(np.concatenate([i.lb for i in insts])).to(d)
+    ub = torch.from_numpy(np.concatenate([i.ub for i in insts])).to(d)
+    cut = torch.full((len(insts),), 7, dtype=torch.int8, device=d)
+    gpu_prop.propagate_instances_device(lb, ub, cut)
+    hlb, hub, hcut = lb.cpu().numpy(), ub.cpu().numpy(), cut.cpu().numpy()
+    for k, inst in enumerate(insts):
+        olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0))
+        assert hcut[k] == int(bool(ores.cutoff))
+        sl = slice(col_off[k], col_off[k + 1])
+        if not hcut[k]:
+            assert np.array_equal(hlb[sl], olb) and np.array_equal(hub[sl], oub)
