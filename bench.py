@@ -217,6 +217,61 @@ def other_workload(args):
     prop.close()
 
 
+def serving_workload(args):
+    """Poisson request streams (80 % node requests against the resident 200,000 x 400,000 matrix, 20 % new
+    instances from the uneven-instance generator) at each rate: p50/p99 latency and throughput of the served
+    (continuously batched) and of the plain one-request-per-call path, with identical replies checked."""
+    from scip_gb300 import gbp, instances, serving
+    from scip_gb300.build import build_libgbp
+
+    build_libgbp()
+    sys.setswitchinterval(1e-4)
+    matrix = build_workload()
+    params = gbp.default_params(maxeasy=args.maxeasy)
+    p = gbp.Propagator(0, params=params)
+    p.upload(matrix)
+    rlb, rub, _, _ = p.propagate(matrix.lb, matrix.ub)
+    p.close()
+    pool = instances.uneven_batch(seed=41, count=24)  # the uneven-instance generator: rows log-uniform in [1e3, 2e5]
+    srv = serving.PropagationServer(matrix, rlb, rub, node_workers=2, inst_workers=4, params=params,
+                                    hbm_cap=150e9)
+    plain = serving.PlainServer(matrix, rlb, rub, params=params)
+    # warm-up: both paths once over a short stream
+    warm = serving.make_stream(matrix, rlb, rub, pool, rate=2000.0, duration=0.2, seed=99)
+    serving.replay(srv, warm, served=True)
+    for req in warm.reqs[:20]:
+        plain.answer(req)
+    rows = []
+    for k, rate in enumerate(float(r) for r in args.rates.split(",")):
+        st = serving.make_stream(matrix, rlb, rub, pool, rate=rate, duration=args.duration, seed=k)
+        replies, lat, wall = serving.replay(srv, st, served=True)
+        nb = len(srv.batches)
+        row = {"rate": rate, "requests": len(st.reqs), "served": {
+            "throughput": len(st.reqs) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "wall_s": wall}}
+        # the plain path on the first requests of the same stream (it saturates early)
+        take = min(len(st.reqs), int(400 * args.duration) + 1)
+        sub = serving.Stream(st.times[:take], st.reqs[:take])
+        p_replies, p_lat, p_wall = serving.replay(plain, sub, served=False)
+        same = all(serving.same_reply(replies[q], p_replies[q]) for q in range(take))
+        row["plain"] = {"requests": take, "throughput": take / p_wall, "p50_ms": 1e3 * float(np.percentile(p_lat, 50)),
+                        "p99_ms": 1e3 * float(np.percentile(p_lat, 99)), "identical_replies": same}
+        rows.append(row)
+    batches = srv.batches
+    srv.close()
+    plain.close()
+    best = max(r["served"]["throughput"] for r in rows)
+    print(json.dumps({"metric": "node-fixpoints/sec", "value": best, "unit": "requests/s", "n_gpus": 1,
+                      "steps": len(rows), "warmup": 1, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                      "config": {"workload": "served propagation: Poisson request streams, 80 % node requests "
+                                             "against the resident 200,000 x 400,000 matrix, 20 % new instances "
+                                             "from the uneven-instance generator", "workers": "2 node + 4 instance",
+                                 "hbm_cap_gb": 150, "duration_s": args.duration},
+                      "sweep": rows, "batches": len(batches),
+                      "mean_batch": float(np.mean([b[1] for b in batches])) if batches else 0.0}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,11 +282,15 @@ def main():
     ap.add_argument("--maxeasy", type=float, default=0.0)
     ap.add_argument("--quick", action="store_true", help="skip the plain-path and CPU arms (profiling runs)")
     ap.add_argument("--shape", default="", help="threads_per_node,ctas_per_sm instead of autotuning (e.g. 128,0)")
-    ap.add_argument("--workload", default="nodes", choices=["nodes", "uneven", "zipf"],
+    ap.add_argument("--workload", default="nodes", choices=["nodes", "uneven", "zipf", "serving"],
                     help="nodes: batched B&B nodes (headline); uneven: 512 distinct instances in one problem; "
                          "zipf: one 1M x 2M instance through the plain path")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serving: arrival rates (req/s)")
+    ap.add_argument("--duration", type=float, default=1.0, help="serving: seconds of arrivals per rate")
     args = ap.parse_args()
+    if args.workload == "serving":
+        return serving_workload(args)
     if args.workload != "nodes":
         return other_workload(args)
 
