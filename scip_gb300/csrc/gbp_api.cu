@@ -26,9 +26,10 @@ struct gbp_ctx {
   Num num{};
   std::string err;
 
-  // problem
+  // problem (device arrays are kept and reused by later uploads that fit their capacities)
   bool has_problem = false;
   int64_t m = 0, n = 0, nnz = 0;
+  int64_t cap_m = 0, cap_n = 0, cap_nnz = 0, cap_inst = 0;
   int64_t* d_rowptr = nullptr;
   int32_t* d_colidx = nullptr;
   double* d_vals = nullptr;
@@ -108,6 +109,7 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_touched = nullptr; ctx->d_list[0] = ctx->d_list[1] = nullptr; ctx->d_rowstamp = nullptr;
   ctx->d_allrows = nullptr; ctx->d_base = nullptr; ctx->slot_mem = nullptr; ctx->stage = nullptr;
   ctx->d_rowinst = nullptr; ctx->d_colinst = nullptr; ctx->d_instcut = nullptr; ctx->ninst = 0;
+  ctx->cap_m = ctx->cap_n = ctx->cap_nnz = ctx->cap_inst = 0;
   ctx->stage_bytes = 0;
   ctx->nslots = 0;
   ctx->has_problem = false;
@@ -272,28 +274,12 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
     if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
   const int64_t nnz = rowptr[m];
   if (nnz > 0 && (!colidx || !vals)) return fail(ctx, GBP_ERR_INVALID, "null colidx/vals");
-  for (int64_t p = 0; p < nnz; ++p)
-    if (colidx[p] < 0 || colidx[p] >= n) return fail(ctx, GBP_ERR_INVALID, "column index out of range");
 
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  freeProblem(ctx);
+  ctx->has_problem = false;
+  ctx->ninst = 0;
 
-  // column-major copy with relevance flags (which bound moves each row can use)
-  std::vector<int64_t> colptr(n + 1, 0);
-  for (int64_t p = 0; p < nnz; ++p) colptr[colidx[p] + 1]++;
-  for (int64_t j = 0; j < n; ++j) colptr[j + 1] += colptr[j];
-  std::vector<int32_t> rowidx(nnz);
-  std::vector<double> cvals(nnz);
-  {
-    std::vector<int64_t> fill(colptr.begin(), colptr.end() - 1);
-    for (int64_t i = 0; i < m; ++i)
-      for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) {
-        int64_t q = fill[colidx[p]]++;
-        rowidx[q] = (int32_t)i;
-        cvals[q] = vals[p];
-      }
-  }
   // all-rows frontier: short rows from the front, long rows from the back
   std::vector<int> allrows(std::max<int64_t>(m, 1));
   int ns = 0, nl = 0;
@@ -304,24 +290,39 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
 
   const size_t mm = (size_t)std::max<int64_t>(m, 1), nn = (size_t)std::max<int64_t>(n, 1),
                zz = (size_t)std::max<int64_t>(nnz, 1);
-  CK(cudaMalloc(&ctx->d_rowptr, (mm + 1) * sizeof(int64_t)));
-  CK(cudaMalloc(&ctx->d_colidx, zz * sizeof(int32_t)));
-  CK(cudaMalloc(&ctx->d_vals, zz * sizeof(double)));
-  CK(cudaMalloc(&ctx->d_lhs, mm * sizeof(double)));
-  CK(cudaMalloc(&ctx->d_rhs, mm * sizeof(double)));
-  CK(cudaMalloc(&ctx->d_isint, nn));
-  CK(cudaMalloc(&ctx->d_colptr, (nn + 1) * sizeof(int64_t)));
-  CK(cudaMalloc(&ctx->d_cscrow, zz * sizeof(uint32_t)));
-  CK(cudaMalloc(&ctx->d_lb, nn * sizeof(double)));
-  CK(cudaMalloc(&ctx->d_ub, nn * sizeof(double)));
-  CK(cudaMalloc(&ctx->d_cand, 4 * nn * sizeof(long long)));
-  CK(cudaMalloc(&ctx->d_cflag, nn * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_touched, nn * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_list[0], mm * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_list[1], mm * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_rowstamp, mm * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_allrows, mm * sizeof(int)));
-  CK(cudaMalloc(&ctx->d_base, nn * sizeof(double2)));
+  if ((int64_t)mm > ctx->cap_m || (int64_t)nn > ctx->cap_n || (int64_t)zz > ctx->cap_nnz) {
+    // grow (a quarter of headroom, so that a stream of similar uploads reuses the arrays; freeing and
+    // allocating synchronise the device, reuse does not)
+    const int64_t cm = std::max<int64_t>(mm, ctx->cap_m + ctx->cap_m / 4);
+    const int64_t cn = std::max<int64_t>(nn, ctx->cap_n + ctx->cap_n / 4);
+    const int64_t cz = std::max<int64_t>(zz, ctx->cap_nnz + ctx->cap_nnz / 4);
+    freeProblem(ctx);
+    CK(cudaMalloc(&ctx->d_rowptr, (cm + 1) * sizeof(int64_t)));
+    CK(cudaMalloc(&ctx->d_colidx, cz * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_vals, cz * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_lhs, cm * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_rhs, cm * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_isint, cn));
+    CK(cudaMalloc(&ctx->d_colptr, (cn + 1) * sizeof(int64_t)));
+    CK(cudaMalloc(&ctx->d_cscrow, cz * sizeof(uint32_t)));
+    CK(cudaMalloc(&ctx->d_lb, cn * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_ub, cn * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_cand, 4 * cn * sizeof(long long)));
+    CK(cudaMalloc(&ctx->d_cflag, cn * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_touched, cn * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_list[0], cm * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_list[1], cm * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_rowstamp, cm * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_allrows, cm * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_base, cn * sizeof(double2)));
+    ctx->cap_m = cm;
+    ctx->cap_n = cn;
+    ctx->cap_nnz = cz;
+  } else if (ctx->slot_mem && (ctx->slots.nstride < (int64_t)nn || ctx->slots.mstride < (int64_t)mm)) {
+    CK(cudaFree(ctx->slot_mem));
+    ctx->slot_mem = nullptr;
+    ctx->nslots = 0;
+  }
 
   CK(cudaMemcpyAsync(ctx->d_rowptr, rowptr, (m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
   if (nnz) {
@@ -334,24 +335,38 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
     CK(cudaMemcpyAsync(ctx->d_allrows, allrows.data(), m * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   }
   if (n) CK(cudaMemcpyAsync(ctx->d_isint, isint, n, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_colptr, colptr.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-  if (nnz) {
-    int32_t* d_rowidx = nullptr;
-    double* d_cvals = nullptr;
-    CK(cudaMalloc(&d_rowidx, nnz * sizeof(int32_t)));
-    CK(cudaMalloc(&d_cvals, nnz * sizeof(double)));
-    CK(cudaMemcpyAsync(d_rowidx, rowidx.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_cvals, cvals.data(), nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(launchCscFlags(ctx->stream, gridFor(ctx, nnz), nnz, d_cvals, d_rowidx, ctx->d_lhs, ctx->d_rhs,
-                      ctx->par.infinity, ctx->d_cscrow));
+
+  // CSC with relevance flags, built on the device: count per column, prefix sum, scatter
+  {
+    unsigned long long* count = nullptr;
+    unsigned long long* cursor = nullptr;
+    CK(cudaMallocAsync((void**)&count, (nn + 1) * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMallocAsync((void**)&cursor, (nn + 1) * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(count, 0, (nn + 1) * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_ctr, 0, 8 * sizeof(int), ctx->stream));
+    if (nnz) CK(launchCscCount(ctx->stream, gridFor(ctx, nnz), nnz, ctx->d_colidx, n, count, ctx->d_ctr + 7));
+    CK(columnPointers(ctx->stream, count, (unsigned long long*)ctx->d_colptr, n));
+    CK(cudaMemcpyAsync(cursor, ctx->d_colptr, (nn + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, ctx->d_ctr + 7, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_rowidx);
-    cudaFree(d_cvals);
+    if (bad) {
+      cudaFreeAsync(count, ctx->stream);
+      cudaFreeAsync(cursor, ctx->stream);
+      freeProblem(ctx);
+      return fail(ctx, GBP_ERR_INVALID, "column index out of range");
+    }
+    if (m) CK(launchCscScatter(ctx->stream, gridFor(ctx, m), m, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs,
+                               ctx->d_rhs, ctx->par.infinity, cursor, ctx->d_cscrow));
+    CK(cudaFreeAsync(count, ctx->stream));
+    CK(cudaFreeAsync(cursor, ctx->stream));
   }
+  const size_t cn = (size_t)ctx->cap_n;
   CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand, nn, KEY_NONE_UB));
-  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + nn, nn, KEY_NONE_LB));
-  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 2 * nn, nn, KEY_NONE_UB));
-  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 3 * nn, nn, KEY_NONE_LB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + cn, nn, KEY_NONE_LB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 2 * cn, nn, KEY_NONE_UB));
+  CK(launchFill64(ctx->stream, gridFor(ctx, nn), ctx->d_cand + 3 * cn, nn, KEY_NONE_LB));
   CK(cudaMemsetAsync(ctx->d_cflag, 0, nn * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_rowstamp, 0, mm * sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -367,7 +382,7 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
 
 // ------------------------------------------------------------------------------------------ plain path
 static Cands plainCands(gbp_ctx* ctx) {
-  const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+  const size_t n = (size_t)ctx->cap_n;
   return Cands{ctx->d_cand, ctx->d_cand + n, ctx->d_cand + 2 * n, ctx->d_cand + 3 * n, ctx->d_cflag,
                ctx->d_touched, ctx->d_ctr + 4};
 }
@@ -579,24 +594,35 @@ int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, co
     for (int64_t i = row_off[k]; i < row_off[k + 1]; ++i) rowinst[i] = (int32_t)k;
     for (int64_t j = col_off[k]; j < col_off[k + 1]; ++j) colinst[j] = (int32_t)k;
   }
-  if (m > 0 && rowptr[0] == 0) {
-    for (int64_t i = 0; i < m; ++i) {
-      if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
-      for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p)
-        if (colidx[p] < 0 || colidx[p] >= n || colinst[colidx[p]] != rowinst[i])
-          return fail(ctx, GBP_ERR_INVALID, "a row references a column of another instance");
-    }
-  }
   int rc = gbp_upload_problem(ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
   if (rc != GBP_OK) return rc;
-  CK(cudaMalloc(&ctx->d_rowinst, rowinst.size() * sizeof(int32_t)));
-  CK(cudaMalloc(&ctx->d_colinst, colinst.size() * sizeof(int32_t)));
-  CK(cudaMalloc(&ctx->d_instcut, ninst * sizeof(int)));
+  if (!ctx->d_rowinst || ninst > ctx->cap_inst) {
+    if (ctx->d_rowinst) cudaFree(ctx->d_rowinst);
+    if (ctx->d_colinst) cudaFree(ctx->d_colinst);
+    if (ctx->d_instcut) cudaFree(ctx->d_instcut);
+    ctx->d_rowinst = ctx->d_colinst = nullptr;
+    ctx->d_instcut = nullptr;
+    CK(cudaMalloc(&ctx->d_rowinst, ctx->cap_m * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_colinst, ctx->cap_n * sizeof(int32_t)));
+    const int64_t ci = std::max<int64_t>(ninst, ctx->cap_inst + ctx->cap_inst / 4);
+    CK(cudaMalloc(&ctx->d_instcut, ci * sizeof(int)));
+    ctx->cap_inst = ci;
+  }
   CK(cudaMemcpyAsync(ctx->d_rowinst, rowinst.data(), rowinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_colinst, colinst.data(), colinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                      ctx->stream));
+  // rows may only reference columns of their own instance (checked on the device)
+  CK(cudaMemsetAsync(ctx->d_ctr + 7, 0, sizeof(int), ctx->stream));
+  if (m) CK(launchCheckBlocks(ctx->stream, gridFor(ctx, m), m, ctx->d_rowptr, ctx->d_colidx, ctx->d_rowinst,
+                              ctx->d_colinst, ctx->d_ctr + 7));
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, ctx->d_ctr + 7, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (bad) {
+    freeProblem(ctx);
+    return fail(ctx, GBP_ERR_INVALID, "a row references a column of another instance");
+  }
   ctx->ninst = ninst;
   return GBP_OK;
 }

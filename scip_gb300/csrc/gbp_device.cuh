@@ -610,12 +610,21 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
   actZero(a);
   double mad = 0.0;
   bool madinf = false;
+  long long maxabs = 0;  // largest |contribution| of the lane's entries, as bits
   for (int64_t p = p0 + lane; p < p1; p += 32) {
     int j = P.colidx[p];
     double v = P.vals[p];
     double l, u;
     B.get(j, l, u);
     addTerm(s, a, v, l, u);
+    if (!isInf(s, fabs(l))) {
+      long long b = absBits(v * l);
+      if (b > maxabs) maxabs = b;
+    }
+    if (!isInf(s, fabs(u))) {
+      long long b = absBits(v * u);
+      if (b > maxabs) maxabs = b;
+    }
     double d = entryDelta(s, v, l, u);
     if (d < 0.0) madinf = true;
     else if (d > mad) mad = d;
@@ -641,6 +650,11 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
       if (dm > mad) mad = dm;
     }
   }
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    long long o = __shfl_xor_sync(0xffffffffu, maxabs, off);
+    if (o > maxabs) maxabs = o;
+  }
   a.minhi = __shfl_sync(0xffffffffu, a.minhi, 0);
   a.minlo = __shfl_sync(0xffffffffu, a.minlo, 0);
   a.maxhi = __shfl_sync(0xffffffffu, a.maxhi, 0);
@@ -664,12 +678,55 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
   if (t == 1) return true;
   if (t == 0) return false;
   if (lane == 0) st.live += 1;
+  const bool rhsfin = !isInf(s, rhs), lhsfin = !isInf(s, -lhs);
+  if (easy && ((rhsfin && feasLt(s, rhs, a.minhi + a.minlo)) || (lhsfin && feasLt(s, a.maxhi + a.maxlo, lhs))))
+    return true;  // the slack rule's own infeasibility test (tightenVarBoundsEasy)
+
+  // which entries can produce a candidate (the necessary conditions of selectEntries, per entry)
+  const int mintot = a.minposinf + a.minneginf + a.minposhuge + a.minneghuge;
+  const int maxtot = a.maxposinf + a.maxneginf + a.maxposhuge + a.maxneghuge;
+  bool useR = false, useL = false;
+  double thrR = 0.0, thrL = 0.0;
+  const bool specMin = !easy && rhsfin && mintot == 1, specMax = !easy && lhsfin && maxtot == 1;
+  if (easy) {
+    if (rhsfin) {
+      double slack = rhs - (a.minhi + a.minlo);
+      thrR = positive(s, slack) ? slack : 0.0;
+      useR = true;
+    }
+    if (lhsfin) {
+      double surplus = (a.maxhi + a.maxlo) - lhs;
+      thrL = positive(s, surplus) ? surplus : 0.0;
+      useL = true;
+    }
+  } else {
+    const double margin = 1e-9 * ((rhsfin ? fabs(rhs) : 0.0) + (lhsfin ? fabs(lhs) : 0.0) +
+                                  (double)(p1 - p0 + 2) * __longlong_as_double(maxabs)) + 1e-300;
+    if (rhsfin && mintot == 0) {
+      thrR = (rhs - (a.minhi + a.minlo)) - margin;
+      useR = true;
+    }
+    if (lhsfin && maxtot == 0) {
+      thrL = ((a.maxhi + a.maxlo) - lhs) - margin;
+      useL = true;
+    }
+  }
+  const long long infb = __double_as_longlong(s.inf), hugeb = __double_as_longlong(s.huge);
   bool cut = false;
   for (int64_t p = p0 + lane; p < p1; p += 32) {
     int j = P.colidx[p];
     double v = P.vals[p];
     double l, u;
     B.get(j, l, u);
+    const double d = __longlong_as_double(deltaBits(s, v, l, u));  // +inf for an infinite bound
+    bool go = (useR && d > thrR) || (useL && d > thrL);
+    if (!go && (specMin || specMax)) {
+      const bool vpos = __double_as_longlong(v) >= 0;
+      const double bmin = vpos ? l : u, bmax = vpos ? u : l;
+      if (specMin) go |= (absBits(bmin) >= infb) || (absBits(v * bmin) >= hugeb);
+      if (specMax) go |= (absBits(bmax) >= infb) || (absBits(v * bmax) >= hugeb);
+    }
+    if (!go) continue;
     auto relres = [&](bool ismin) {
       double r = 0.0;
       for (int64_t q = p0; q < p1; ++q) {

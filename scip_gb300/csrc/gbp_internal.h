@@ -112,5 +112,13 @@ cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double*
                            const double* lhs, const double* rhs, double inf, uint32_t* out);
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v);
 cudaError_t launchFlags8(cudaStream_t st, int grid, const int* in, int8_t* out, int64_t n);
+cudaError_t launchCscCount(cudaStream_t st, int grid, int64_t nnz, const int32_t* colidx, int64_t n,
+                           unsigned long long* count, int* bad);
+cudaError_t launchCscScatter(cudaStream_t st, int grid, int64_t m, const int64_t* rowptr, const int32_t* colidx,
+                             const double* vals, const double* lhs, const double* rhs, double inf,
+                             unsigned long long* cursor, uint32_t* cscrow);
+cudaError_t launchCheckBlocks(cudaStream_t st, int grid, int64_t m, const int64_t* rowptr, const int32_t* colidx,
+                              const int32_t* rowinst, const int32_t* colinst, int* bad);
+cudaError_t columnPointers(cudaStream_t st, const unsigned long long* count, unsigned long long* colptr, int64_t n);
 
 }  // namespace gbp

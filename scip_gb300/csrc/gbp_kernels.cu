@@ -203,6 +203,43 @@ __global__ void k_fill64(long long* p, int64_t n, long long v) {
     p[j] = v;
 }
 
+// column-major copy built on the device: count entries per column, then scatter each row's entries to its
+// columns' next free slots (the order inside a column does not matter to any result)
+__global__ void k_csc_count(int64_t nnz, const int32_t* colidx, int64_t n, unsigned long long* count, int* bad) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x) {
+    const int j = colidx[p];
+    if (j < 0 || j >= n) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    atomicAdd(&count[j], 1ull);
+  }
+}
+
+__global__ void k_csc_scatter(int64_t m, const int64_t* rowptr, const int32_t* colidx, const double* vals,
+                              const double* lhs, const double* rhs, double inf, unsigned long long* cursor,
+                              uint32_t* cscrow) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool rhsfin = !(rhs[i] >= inf), lhsfin = !(-lhs[i] >= inf);
+    for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+      const double a = vals[p];
+      uint32_t e = (uint32_t)i;
+      if (a > 0.0 ? rhsfin : lhsfin) e |= CSC_LBUP;
+      if (a > 0.0 ? lhsfin : rhsfin) e |= CSC_UBDOWN;
+      const unsigned long long q = atomicAdd(&cursor[colidx[p]], 1ull);
+      cscrow[q] = e;
+    }
+  }
+}
+
+// rows of instance k may only reference columns of instance k
+__global__ void k_check_blocks(int64_t m, const int64_t* rowptr, const int32_t* colidx, const int32_t* rowinst,
+                               const int32_t* colinst, int* bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p)
+      if (colinst[colidx[p]] != rowinst[i]) atomicExch(bad, 1);
+}
+
 // relevance flags of each CSC entry (which bound moves of the column the row can use)
 __global__ void k_csc_flags(int64_t nnz, const double* cvals, const int32_t* rowidx, const double* lhs,
                             const double* rhs, double inf, uint32_t* out) {
@@ -434,6 +471,22 @@ cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double
   k_pack<<<grid, 256, 0, st>>>(lb, ub, out, n);
   return cudaGetLastError();
 }
+cudaError_t launchCscCount(cudaStream_t st, int grid, int64_t nnz, const int32_t* colidx, int64_t n,
+                           unsigned long long* count, int* bad) {
+  k_csc_count<<<grid, 256, 0, st>>>(nnz, colidx, n, count, bad);
+  return cudaGetLastError();
+}
+cudaError_t launchCscScatter(cudaStream_t st, int grid, int64_t m, const int64_t* rowptr, const int32_t* colidx,
+                             const double* vals, const double* lhs, const double* rhs, double inf,
+                             unsigned long long* cursor, uint32_t* cscrow) {
+  k_csc_scatter<<<grid, 256, 0, st>>>(m, rowptr, colidx, vals, lhs, rhs, inf, cursor, cscrow);
+  return cudaGetLastError();
+}
+cudaError_t launchCheckBlocks(cudaStream_t st, int grid, int64_t m, const int64_t* rowptr, const int32_t* colidx,
+                              const int32_t* rowinst, const int32_t* colinst, int* bad) {
+  k_check_blocks<<<grid, 256, 0, st>>>(m, rowptr, colidx, rowinst, colinst, bad);
+  return cudaGetLastError();
+}
 cudaError_t launchFlags8(cudaStream_t st, int grid, const int* in, int8_t* out, int64_t n) {
   k_flags8<<<grid, 256, 0, st>>>(in, out, n);
   return cudaGetLastError();
@@ -467,4 +520,20 @@ cudaError_t nodesOccupancy(int nt, int* blocksPerSm) {
   }
 }
 
+}  // namespace gbp
+
+// exclusive prefix sum of the per-column counts (n + 1 entries, count[n] = 0): the CSC column pointers
+#include <cub/device/device_scan.cuh>
+namespace gbp {
+cudaError_t columnPointers(cudaStream_t st, const unsigned long long* count, unsigned long long* colptr, int64_t n) {
+  size_t tmp = 0;
+  cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, tmp, count, colptr, n + 1, st);
+  if (e != cudaSuccess) return e;
+  void* buf = nullptr;
+  e = cudaMallocAsync(&buf, tmp, st);
+  if (e != cudaSuccess) return e;
+  e = cub::DeviceScan::ExclusiveSum(buf, tmp, count, colptr, n + 1, st);
+  cudaError_t f = cudaFreeAsync(buf, st);
+  return e != cudaSuccess ? e : f;
+}
 }  // namespace gbp

@@ -43,12 +43,14 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
 
 
 def test_hbm_cap_defers_admission():
-    """With a cap smaller than two instance batches, instance requests wait for memory to free up instead of
-    being admitted together; every request is still answered."""
+    """With a cap that holds one instance request but never two, instance requests wait for memory to free up
+    instead of being admitted together; every request is still answered."""
     matrix = instances.node_mip(seed=33, m=5000, n=10000)
     params = gbp.default_params(maxeasy=0.0)
     pool = instances.uneven_batch(seed=34, count=4, rmin=2000, rmax=3000)
-    cap = 1.5 * max(serving._inst_bytes(i) for i in pool)
+    sizes = [serving._inst_bytes(i) for i in pool]
+    cap = max(sizes)
+    assert 2 * min(sizes) > cap
     srv = serving.PropagationServer(matrix, matrix.lb, matrix.ub, node_workers=1, inst_workers=2, params=params,
                                     hbm_cap=cap)
     try:
