@@ -52,8 +52,12 @@ typedef struct
    double maxeasyactivitydelta; /* constraints/linear/maxeasyactivitydelta; SCIP's default is 1e6, 0 selects the
                                  * residual rule (cons_linear.c:6700) for every row */
    int32_t maxrounds;           /* propagation round cap per problem or node; <= 0 means 1,000,000 */
-   int32_t flags;               /* reserved, 0 */
+   int32_t flags;               /* GBP_FLAG_* bits, 0 by default */
 } gbp_params;
+
+/* plain path: drive the rounds from the host (one synchronisation per round) instead of the device-side loop
+ * (a CUDA graph whose conditional while-node repeats the round until the frontier is empty) */
+#define GBP_FLAG_HOSTLOOP 1
 
 typedef struct
 {
@@ -135,8 +139,10 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
    int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
    double* out_ub, int64_t out_cap, gbp_result* res);
 
-/* launch shape of the batched kernel -- what the autotuner sets: threads that work on one node (32, 64, 128 or
- * 256; one CTA per node at a time) and resident CTAs per SM (0 = occupancy maximum) */
+/* launch shape of the batched kernel -- what the autotuner sets: threads that work on one node (one CTA per node
+ * at a time) and the register budget the kernel variant was compiled for, given as resident CTAs per SM.
+ * Compiled shapes: (32,16) (32,24) (64,8) (64,12) (128,4) (128,6) (256,2); ctas_per_sm = 0 picks the first
+ * listed budget for that width.  Results never depend on the shape. */
 int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per_sm);
 
 /* ---------------------------------------------------------------- batched path without allocation

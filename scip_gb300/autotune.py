@@ -1,17 +1,17 @@
 """Autotuner for the batched propagation kernel's launch shape.
 
-The shape is (threads working on one node, resident CTAs per SM).  Row-to-thread mapping inside a CTA is
+The shape is (threads working on one node, register budget of the compiled kernel variant given as resident
+CTAs per SM).  Row-to-thread mapping inside a CTA is
 fixed by the summation order (one thread per row of up to 64 entries, one warp per longer row), so the tuner
 only changes how many nodes run at once and how wide each node's CTA is -- choices that never change results.
 Results are cached per problem shape for the process.
 """
 from __future__ import annotations
 
-import itertools
 import time
 from typing import Dict, Tuple
 
-SHAPES = [(t, c) for t, c in itertools.product((32, 64, 128, 256), (0, 4))]
+SHAPES = [(32, 16), (32, 24), (64, 8), (64, 12), (128, 4), (128, 6), (256, 2)]
 
 _cache: Dict[Tuple, Tuple[int, int]] = {}
 

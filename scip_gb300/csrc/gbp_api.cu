@@ -65,8 +65,8 @@ struct gbp_ctx {
   bool instmode = false;  // propagateCore works per instance
 
   // batched path
-  int ctas_per_sm = 0;
-  int node_threads = 32;
+  int ctas_per_sm = 4;     // register budget / residency of the node kernel variant
+  int node_threads = 128;
   int nslots = 0;
   SlotArrays slots{};
   void* slot_mem = nullptr;
@@ -79,8 +79,25 @@ struct gbp_ctx {
   void* stage = nullptr;
   size_t stage_bytes = 0;
 
+  // device-driven fixpoint loop: one CUDA graph per mode (0 single problem, 1 instances) whose conditional
+  // while-node repeats rows -> apply -> advance until the frontier is empty, cut off or at the round cap
+  LoopState* d_state = nullptr;
+  LoopState* h_state = nullptr;  // pinned
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  bool graph_failed = false;
+
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
+
+static void destroyGraphs(gbp_ctx* ctx) {
+  for (int k = 0; k < 2; ++k) {
+    if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
+    if (ctx->graph[k]) cudaGraphDestroy(ctx->graph[k]);
+    ctx->gexec[k] = nullptr;
+    ctx->graph[k] = nullptr;
+  }
+}
 
 #define CK(call)                                                                         \
   do {                                                                                   \
@@ -97,6 +114,7 @@ static int fail(gbp_ctx* ctx, int code, const std::string& msg) {
 }
 
 static void freeProblem(gbp_ctx* ctx) {
+  destroyGraphs(ctx);
   void* ptrs[] = {ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint, ctx->d_colptr,
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
@@ -172,6 +190,7 @@ int gbp_set_params(gbp_ctx* ctx, const gbp_params* p) {
   ctx->par = *p;
   ctx->num = Num{p->infinity, p->epsilon, p->sumepsilon, p->feastol, p->hugeval, p->boundstreps, p->recompfac,
                  p->maxeasyactivitydelta};
+  destroyGraphs(ctx);  // the numerics are baked into the graphs' kernel arguments
   return GBP_OK;
 }
 
@@ -212,7 +231,9 @@ int gbp_create(gbp_ctx** out, int device, void* stream) {
       cudaMalloc(&ctx->d_next_item, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->d_status, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->d_out_used, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMallocHost(&ctx->h_ctr, 16 * sizeof(int)) != cudaSuccess) {
+      cudaMallocHost(&ctx->h_ctr, 16 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_state, sizeof(LoopState)) != cudaSuccess ||
+      cudaMallocHost(&ctx->h_state, sizeof(LoopState)) != cudaSuccess) {
     gbp_destroy(ctx);
     return GBP_ERR_CUDA;
   }
@@ -233,6 +254,8 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_out_used) cudaFree(ctx->d_out_used);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  if (ctx->d_state) cudaFree(ctx->d_state);
+  if (ctx->h_state) cudaFreeHost(ctx->h_state);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -246,10 +269,22 @@ int gbp_get_stream(const gbp_ctx* ctx, void** stream) {
   return GBP_OK;
 }
 
+// compiled register budgets of the node kernel: (threads per node, resident CTAs per SM)
+static bool shapeCompiled(int t, int b) {
+  static const int shapes[][2] = {{32, 16}, {64, 8}, {128, 4}, {256, 2}, {128, 6}, {64, 12}, {32, 24}};
+  for (const auto& sh : shapes)
+    if (sh[0] == t && sh[1] == b) return true;
+  return false;
+}
+static int defaultBudget(int t) { return t == 32 ? 16 : t == 64 ? 8 : t == 128 ? 4 : 2; }
+
 int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per_sm) {
-  if (!ctx || ctas_per_sm < 0 || ctas_per_sm > 32) return GBP_ERR_INVALID;
+  if (!ctx) return GBP_ERR_INVALID;
   if (threads_per_node != 32 && threads_per_node != 64 && threads_per_node != 128 && threads_per_node != 256)
     return fail(ctx, GBP_ERR_INVALID, "threads per node must be 32, 64, 128 or 256");
+  if (ctas_per_sm == 0) ctas_per_sm = defaultBudget(threads_per_node);
+  if (!shapeCompiled(threads_per_node, ctas_per_sm))
+    return fail(ctx, GBP_ERR_INVALID, "no compiled variant for this (threads per node, CTAs per SM) shape");
   if (ctas_per_sm != ctx->ctas_per_sm || threads_per_node != ctx->node_threads) {
     ctx->ctas_per_sm = ctas_per_sm;
     ctx->node_threads = threads_per_node;
@@ -279,6 +314,7 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->has_problem = false;
   ctx->ninst = 0;
+  destroyGraphs(ctx);
 
   // all-rows frontier: short rows from the front, long rows from the back
   std::vector<int> allrows(std::max<int64_t>(m, 1));
@@ -395,8 +431,135 @@ static int nextStamp(gbp_ctx* ctx) {
   return ++ctx->stamp;
 }
 
+static int buildGraph(gbp_ctx* ctx, int mode) {
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  ctx->graph[mode] = g;
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cn;
+  CK(cudaGraphAddNode(&cn, g, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+
+  Num s = ctx->num;
+  Prob P = devProb(ctx, mode == 1);
+  Cands C = plainCands(ctx);
+  C.ntouched = &ctx->d_state->ntouched;
+  ListSet L{{ctx->d_list[0], ctx->d_list[1], ctx->d_allrows}, ctx->d_rowstamp, (int)ctx->m};
+  LoopState* S = ctx->d_state;
+  unsigned long long* stats = ctx->d_stats;
+  void* args[] = {&s, &P, &C, &L, &S, &stats};
+  void* advargs[] = {&S, &h};
+  const dim3 grids[4] = {dim3(ctx->sms * 16), dim3(ctx->sms * 8), dim3(ctx->sms * 8), dim3(1)};
+  const dim3 blocks[4] = {dim3(ROW_THREADS_G), dim3(256), dim3(256), dim3(1)};
+  cudaGraphNode_t prev = nullptr;
+  for (int k = 0; k < 4; ++k) {
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)graphKernel(k);
+    kp.gridDim = grids[k];
+    kp.blockDim = blocks[k];
+    kp.kernelParams = k == 3 ? advargs : args;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddKernelNode(&node, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
+    prev = node;
+  }
+  CK(cudaGraphInstantiate(&ctx->gexec[mode], g, 0));
+  return GBP_OK;
+}
+
+// one fixpoint through the graph: seeds (if any) on the stream, then one graph launch for all rounds
+static int propagateGraph(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
+                          const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
+  const int mode = ctx->instmode ? 1 : 0;
+  if (!ctx->gexec[mode]) {
+    int rc = buildGraph(ctx, mode);
+    if (rc != GBP_OK) {
+      destroyGraphs(ctx);
+      return rc;
+    }
+  }
+  const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
+  if ((int64_t)ctx->stamp > (int64_t)0x7fffffff - maxrounds - 16) {
+    CK(cudaMemsetAsync(ctx->d_rowstamp, 0, (size_t)std::max<int64_t>(ctx->m, 1) * sizeof(int), ctx->stream));
+    ctx->stamp = 0;
+  }
+  LoopState& hs = *ctx->h_state;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.maxrounds = maxrounds;
+  hs.lb = lb;
+  hs.ub = ub;
+  int seedstamp = 0;
+  if (nseed < 0) {
+    hs.cur = 2;
+    hs.nshort[2] = ctx->nshort_all;
+    hs.nlong[2] = ctx->nlong_all;
+  } else {
+    hs.cur = 0;
+    seedstamp = ++ctx->stamp;
+  }
+  hs.stamp = ++ctx->stamp;
+  CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_state, &hs, sizeof(LoopState), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  int launches = 0;
+  if (nseed > 0) {
+    const Prob P = devProb(ctx, ctx->instmode);
+    Front F{ctx->d_list[0], &ctx->d_state->nshort[0], &ctx->d_state->nlong[0], ctx->d_rowstamp, (int)ctx->m};
+    CK(launchSeed(ctx->stream, gridFor(ctx, nseed), P, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, F, seedstamp));
+    ++launches;
+  }
+  if (nseed != 0) {
+    CK(cudaGraphLaunch(ctx->gexec[mode], ctx->stream));
+    ++launches;
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  unsigned long long st[8];
+  CK(cudaMemcpyAsync(&hs, ctx->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (nseed != 0) ctx->stamp = std::max(ctx->stamp, hs.stamp);
+  const bool cut = !ctx->instmode && hs.cutoff != 0;
+  const int status = cut ? 1 : (hs.status == 2 ? 2 : 0);
+  if (cutoff) *cutoff = cut ? 1 : 0;
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->cutoff = cut ? 1 : 0;
+    res->rounds = hs.worked;
+    res->status = status;
+    res->launches = launches;
+    res->rows = (int64_t)st[0];
+    res->nnz = (int64_t)st[1];
+    res->candidates = (int64_t)st[2];
+    res->changes = (int64_t)st[3];
+    res->live_rows = (int64_t)st[6];
+    res->kernel_ms = ms;
+  }
+  return status == 2 ? GBP_ERR_LIMIT : GBP_OK;
+}
+
+static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
+                             const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res);
+
 static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
                          const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
+  if (!(ctx->par.flags & GBP_FLAG_HOSTLOOP) && !ctx->graph_failed) {
+    int rc = propagateGraph(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
+    if (rc != GBP_ERR_CUDA || ctx->gexec[ctx->instmode ? 1 : 0] != nullptr) return rc;
+    // graphs unavailable: fall back to the host-driven rounds for the rest of the context's life
+    ctx->graph_failed = true;
+    cudaGetLastError();
+  }
+  return propagateHostLoop(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
+}
+
+static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
+                             const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
   const Prob P = devProb(ctx, ctx->instmode);
   const Num s = ctx->num;
   Cands C = plainCands(ctx);
@@ -681,8 +844,8 @@ int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t*
 // per-CTA scratch for min(resident CTAs, nnodes) slots; grown when a later call has more nodes
 static int ensureSlots(gbp_ctx* ctx, int64_t nnodes) {
   int occ = 0;
-  CK(nodesOccupancy(ctx->node_threads, &occ));
-  int per_sm = ctx->ctas_per_sm > 0 ? std::min(ctx->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+  CK(nodesOccupancy(ctx->node_threads, ctx->ctas_per_sm, &occ));
+  int per_sm = std::max(occ, 1);
   const int64_t want = std::min<int64_t>((int64_t)ctx->sms * per_sm, std::max<int64_t>(nnodes, 1));
   if (ctx->slot_mem && ctx->nslots >= want) return GBP_OK;
   if (ctx->slot_mem) {
@@ -776,6 +939,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   A.S = ctx->slots;
   A.stats = ctx->d_stats;
   A.status = ctx->d_status;
+  A.minblocks = ctx->ctas_per_sm;
   const int grid = (int)std::min<int64_t>(ctx->nslots, nnodes);
   CK(launchNodes(ctx->stream, grid, ctx->node_threads, A));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -66,6 +66,28 @@ struct Stats {
   long long rows, nnz, cands, live;  // live: rows that passed the skip tests
 };
 
+// state of the graph-driven fixpoint loop (device memory): which list holds the frontier (0, 1, or 2 = the
+// all-rows list), the lists' sizes, stamps, flags and the bound vectors being propagated
+struct LoopState {
+  int cur;
+  int nshort[3];
+  int nlong[3];
+  int ntouched;
+  int cutoff;
+  int round;
+  int worked;     // rounds that processed a non-empty frontier
+  int maxrounds;
+  int stamp;      // row stamp of the list being filled
+  int status;     // 2: round limit reached
+  double* lb;
+  double* ub;
+};
+struct ListSet {
+  int* list[3];
+  int* rowstamp;
+  int cap;        // m: long rows are stored from the back of each list
+};
+
 // frontier lists: short rows from the front of `list`, long rows from the back
 struct Front {
   int* list;

@@ -89,6 +89,7 @@ struct NodesArgs {
   SlotArrays S;
   unsigned long long* stats;     // rows, nnz, candidates, changes, cutoffs, max rounds
   int* status;                   // bit0 round limit, bit1 output overflow
+  int minblocks;                 // register-budget variant of the kernel (1 = unconstrained)
 };
 
 
@@ -107,7 +108,7 @@ cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob
                              const double* ub, double* act, int32_t* cnt);
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n);
 cudaError_t launchNodes(cudaStream_t st, int grid, int threads, const NodesArgs& A);
-cudaError_t nodesOccupancy(int threads, int* blocksPerSm);
+cudaError_t nodesOccupancy(int threads, int minblocks, int* blocksPerSm);
 cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double* cvals, const int32_t* rowidx,
                            const double* lhs, const double* rhs, double inf, uint32_t* out);
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v);
@@ -119,6 +120,9 @@ cudaError_t launchCscScatter(cudaStream_t st, int grid, int64_t m, const int64_t
                              unsigned long long* cursor, uint32_t* cscrow);
 cudaError_t launchCheckBlocks(cudaStream_t st, int grid, int64_t m, const int64_t* rowptr, const int32_t* colidx,
                               const int32_t* rowinst, const int32_t* colinst, int* bad);
+// kernels of the graph-driven loop: 0 rows (short), 1 rows (long), 2 apply, 3 advance
+const void* graphKernel(int which);
+constexpr int ROW_THREADS_G = 128;
 cudaError_t columnPointers(cudaStream_t st, const unsigned long long* count, unsigned long long* colptr, int64_t n);
 
 }  // namespace gbp

@@ -50,28 +50,25 @@ __device__ __forceinline__ void flushStats(unsigned long long* stats, const Stat
 // ------------------------------------------------------------------------------------------ plain path
 constexpr int ROW_THREADS = 128;
 
-__global__ void __launch_bounds__(ROW_THREADS) k_rows_short(Num s, Prob P, PlainBnd B, const int* list,
-                                                           const int* nshort, Cands C, int* cutoff,
-                                                           unsigned long long* stats) {
-  __shared__ RowBatch<ROW_THREADS> rb;
-  __shared__ int s_cut;
-  if (threadIdx.x == 0) s_cut = 0;
+// ---- bodies shared by the host-driven kernels and the graph-driven loop
+__device__ __forceinline__ void rowsShortBody(const Num& s, const Prob& P, const PlainBnd& B, const int* list, int n,
+                                              Cands& C, int* cutoff, unsigned long long* stats,
+                                              RowBatch<ROW_THREADS>& rb, int* s_cut) {
+  if (threadIdx.x == 0) *s_cut = 0;
   __syncthreads();
   Stats st{0, 0, 0, 0};
-  const int n = *nshort;
   for (int base = blockIdx.x * ROW_THREADS; base < n; base += gridDim.x * ROW_THREADS) {
     const int cnt = (n - base) < ROW_THREADS ? (n - base) : ROW_THREADS;
-    processShortRows<ROW_THREADS>(s, P, B, list + base, cnt, C, st, rb, &s_cut);
+    processShortRows<ROW_THREADS>(s, P, B, list + base, cnt, C, st, rb, s_cut);
   }
   __syncthreads();
-  if (threadIdx.x == 0 && s_cut) atomicExch(cutoff, 1);
+  if (threadIdx.x == 0 && *s_cut) atomicExch(cutoff, 1);
   flushStats(stats, st);
 }
 
-__global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
-                                                   int cap, Cands C, int* cutoff, unsigned long long* stats) {
+__device__ __forceinline__ void rowsLongBody(const Num& s, const Prob& P, const PlainBnd& B, const int* list, int n,
+                                             int cap, Cands& C, int* cutoff, unsigned long long* stats) {
   Stats st{0, 0, 0, 0};
-  const int n = *nlong;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -86,8 +83,8 @@ __global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, co
   flushStats(stats, st);
 }
 
-__global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double* ub, Cands C, Front F, int stamp,
-                                               int* cutoff, unsigned long long* stats) {
+__device__ __forceinline__ void applyBody(const Num& s, const Prob& P, double* lb, double* ub, Cands& C, Front& F,
+                                          int stamp, int* cutoff, unsigned long long* stats) {
   const int n = *C.ntouched;
   unsigned long long changes = 0;
   bool cut = false;
@@ -113,6 +110,67 @@ __global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double
   }
   if (cut) atomicExch(cutoff, 1);
   if (changes) atomicAdd(&stats[3], changes);
+}
+
+// ---- host-driven round (the host reads the frontier sizes after each round)
+__global__ void __launch_bounds__(ROW_THREADS) k_rows_short(Num s, Prob P, PlainBnd B, const int* list,
+                                                           const int* nshort, Cands C, int* cutoff,
+                                                           unsigned long long* stats) {
+  __shared__ RowBatch<ROW_THREADS> rb;
+  __shared__ int s_cut;
+  rowsShortBody(s, P, B, list, *nshort, C, cutoff, stats, rb, &s_cut);
+}
+
+__global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
+                                                   int cap, Cands C, int* cutoff, unsigned long long* stats) {
+  rowsLongBody(s, P, B, list, *nlong, cap, C, cutoff, stats);
+}
+
+__global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double* ub, Cands C, Front F, int stamp,
+                                               int* cutoff, unsigned long long* stats) {
+  applyBody(s, P, lb, ub, C, F, stamp, cutoff, stats);
+}
+
+// ---- graph-driven rounds: the frontier sizes, list parity, stamps and bound pointers live in LoopState
+__global__ void __launch_bounds__(ROW_THREADS) k_rows_short_g(Num s, Prob P, Cands C, ListSet L, LoopState* S,
+                                                             unsigned long long* stats) {
+  __shared__ RowBatch<ROW_THREADS> rb;
+  __shared__ int s_cut;
+  const int cur = S->cur;
+  rowsShortBody(s, P, PlainBnd{S->lb, S->ub}, L.list[cur], S->nshort[cur], C, &S->cutoff, stats, rb, &s_cut);
+}
+
+__global__ void __launch_bounds__(256) k_rows_long_g(Num s, Prob P, Cands C, ListSet L, LoopState* S,
+                                                     unsigned long long* stats) {
+  const int cur = S->cur;
+  rowsLongBody(s, P, PlainBnd{S->lb, S->ub}, L.list[cur], S->nlong[cur], L.cap, C, &S->cutoff, stats);
+}
+
+__global__ void __launch_bounds__(256) k_apply_g(Num s, Prob P, Cands C, ListSet L, LoopState* S,
+                                                 unsigned long long* stats) {
+  const int nxt = S->cur == 1 ? 0 : 1;
+  Front F{L.list[nxt], &S->nshort[nxt], &S->nlong[nxt], L.rowstamp, L.cap};
+  applyBody(s, P, S->lb, S->ub, C, F, S->stamp, &S->cutoff, stats);
+}
+
+// end of a round: switch to the list just filled, clear the other one, and tell the graph whether to go on
+__global__ void k_advance_g(LoopState* S, cudaGraphConditionalHandle h) {
+  const int ran = S->nshort[S->cur] + S->nlong[S->cur];
+  if (ran > 0) S->worked += 1;
+  S->round += 1;
+  const int nxt = S->cur == 1 ? 0 : 1;
+  S->cur = nxt;
+  const int other = nxt ^ 1;
+  S->nshort[other] = 0;
+  S->nlong[other] = 0;
+  S->ntouched = 0;
+  S->stamp += 1;
+  int more = (S->nshort[nxt] + S->nlong[nxt] > 0) && !S->cutoff;
+  if (more && S->worked >= S->maxrounds) {
+    S->status = 2;
+    more = 0;
+  }
+  cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 __global__ void k_seed(Prob P, const double* lb, const double* ub, int64_t nseed, const int32_t* cols,
@@ -264,8 +322,8 @@ __device__ __forceinline__ void ovlSet(const OvlBnd& B, int* dirty, int* ndirty,
   B.ovl[j] = make_double2(l, u);
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT) k_nodes(NodesArgs A) {
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
   __shared__ RowBatch<NT> rb;
   __shared__ int s_item, s_cut, s_ns[2], s_nl[2], s_ntouched, s_ndirty, s_nout, s_rounds, s_epoch, s_rstamp;
   __shared__ long long s_off;
@@ -457,6 +515,15 @@ cudaError_t launchApply(cudaStream_t st, int grid, const Num& s, const Prob& P, 
   k_apply<<<grid, 256, 0, st>>>(s, P, lb, ub, C, F, stamp, cutoff, stats);
   return cudaGetLastError();
 }
+const void* graphKernel(int which) {
+  switch (which) {
+    case 0: return (const void*)k_rows_short_g;
+    case 1: return (const void*)k_rows_long_g;
+    case 2: return (const void*)k_apply_g;
+    case 3: return (const void*)k_advance_g;
+    default: return nullptr;
+  }
+}
 cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* lb, const double* ub, int64_t nseed,
                        const int32_t* cols, const double* oldlb, const double* oldub, Front F, int stamp) {
   k_seed<<<grid, 256, 0, st>>>(P, lb, ub, nseed, cols, oldlb, oldub, F, stamp);
@@ -500,26 +567,27 @@ cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double*
   k_csc_flags<<<grid, 256, 0, st>>>(nnz, cvals, rowidx, lhs, rhs, inf, out);
   return cudaGetLastError();
 }
-cudaError_t launchNodes(cudaStream_t st, int grid, int nt, const NodesArgs& A) {
-  switch (nt) {
-    case 32: k_nodes<32><<<grid, 32, 0, st>>>(A); break;
-    case 64: k_nodes<64><<<grid, 64, 0, st>>>(A); break;
-    case 128: k_nodes<128><<<grid, 128, 0, st>>>(A); break;
-    case 256: k_nodes<256><<<grid, 256, 0, st>>>(A); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-cudaError_t nodesOccupancy(int nt, int* blocksPerSm) {
-  switch (nt) {
-    case 32: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<32>, 32, 0);
-    case 64: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<64>, 64, 0);
-    case 128: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<128>, 128, 0);
-    case 256: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<256>, 256, 0);
-    default: return cudaErrorInvalidValue;
-  }
-}
+// launch shapes: threads per node CTA x register budget (MINB resident CTAs per SM requested from ptxas)
+#define GBP_NODE_SHAPES(X) X(32, 16) X(64, 8) X(128, 4) X(256, 2) X(128, 6) X(64, 12) X(32, 24)
 
+cudaError_t launchNodes(cudaStream_t st, int grid, int nt, const NodesArgs& A) {
+  const int minb = A.minblocks;
+#define GBP_LAUNCH(T, B)                             \
+  if (nt == T && minb == B) {                        \
+    k_nodes<T, B><<<grid, T, 0, st>>>(A);            \
+    return cudaGetLastError();                       \
+  }
+  GBP_NODE_SHAPES(GBP_LAUNCH)
+#undef GBP_LAUNCH
+  return cudaErrorInvalidValue;
+}
+cudaError_t nodesOccupancy(int nt, int minb, int* blocksPerSm) {
+#define GBP_OCC(T, B) \
+  if (nt == T && minb == B) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_nodes<T, B>, T, 0);
+  GBP_NODE_SHAPES(GBP_OCC)
+#undef GBP_OCC
+  return cudaErrorInvalidValue;
+}
 }  // namespace gbp
 
 // exclusive prefix sum of the per-column counts (n + 1 entries, count[n] = 0): the CSC column pointers

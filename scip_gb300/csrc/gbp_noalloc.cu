@@ -44,6 +44,7 @@ struct Header {
 constexpr size_t kHeaderBytes = 256;
 static_assert(sizeof(Header) <= kHeaderBytes, "header too large");
 constexpr int kThreads = 128;
+constexpr int kBudget = 4;  // compiled variant: 128 threads per node, 4 resident CTAs per SM
 
 int scratchAddress(int device, void** out) {
   if (device < 0 || device >= kMaxDevices) return GBP_ERR_NODEVICE;
@@ -97,7 +98,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
 
   int sms = 0, occ = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return GBP_ERR_CUDA;
-  if (nodesOccupancy(kThreads, &occ) != cudaSuccess) return GBP_ERR_CUDA;
+  if (nodesOccupancy(kThreads, kBudget, &occ) != cudaSuccess) return GBP_ERR_CUDA;
   int64_t nslots = std::min<int64_t>((int64_t)sms * std::max(occ, 1), nnodes);
   while (nslots > 1 && kHeaderBytes + slotLayout(ns, ms, nslots, nullptr, nullptr) > GBP_NOALLOC_SCRATCH_BYTES)
     --nslots;
@@ -151,6 +152,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   A.S = S;
   A.stats = hdr->stats;
   A.status = &hdr->status;
+  A.minblocks = kBudget;
   if (launchNodes(st, (int)nslots, kThreads, A) != cudaSuccess) return GBP_ERR_CUDA;
   if (res == nullptr) return GBP_OK;
 

@@ -26,6 +26,7 @@ GBP_ERR_LIMIT = -5
 GBP_ERR_OVERFLOW = -6
 GBP_ERR_STATE = -7
 GBP_ERR_TOO_LARGE = -8
+GBP_FLAG_HOSTLOOP = 1
 
 # every symbol include/gbp.h declares (checked by the CPU test suite)
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
@@ -169,7 +170,7 @@ class Propagator:
     def set_params(self, p: GbpParams):
         self._check(self.L.gbp_set_params(self.h, ctypes.byref(p)))
 
-    def set_batch_shape(self, threads_per_node: int = 32, ctas_per_sm: int = 0):
+    def set_batch_shape(self, threads_per_node: int = 128, ctas_per_sm: int = 0):
         self._check(self.L.gbp_set_batch_shape(self.h, threads_per_node, ctas_per_sm))
 
     def stream(self):

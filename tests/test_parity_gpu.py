@@ -62,10 +62,14 @@ def test_activities_and_counts_bit_exact(gpu_prop, oracle_mod):
     assert (np.diff(inst.rowptr) > 64).any()
 
 
+@pytest.mark.parametrize("hostloop", [False, True])
 @pytest.mark.parametrize("maxeasy", [0.0, 1e6])
-def test_zipf_root_matches_oracle(gpu_prop, oracle_mod, maxeasy):
+def test_zipf_root_matches_oracle(gpu_prop, oracle_mod, maxeasy, hostloop):
+    """Both drivers of the plain path: the device-side graph loop and host-driven rounds."""
     inst = instances.zipf_mip(seed=3, m=20000, n=40000, hi=2000)
-    gpu_prop.set_params(_params(maxeasy))
+    p = _params(maxeasy)
+    p.flags = gbp.GBP_FLAG_HOSTLOOP if hostloop else 0
+    gpu_prop.set_params(p)
     gpu_prop.upload(inst)
     lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
     olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(maxeasy))
@@ -73,6 +77,8 @@ def test_zipf_root_matches_oracle(gpu_prop, oracle_mod, maxeasy):
     if not cut:
         assert np.array_equal(lb, olb) and np.array_equal(ub, oub)
         assert res.rounds == ores.rounds
+    assert res.launches <= (3 * res.rounds + 1 if hostloop else 2)
+    gpu_prop.set_params(_params(maxeasy))
 
 
 @pytest.mark.parametrize("maxeasy", [0.0, 1e6])

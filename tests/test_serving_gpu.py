@@ -47,10 +47,9 @@ def test_hbm_cap_defers_admission():
     instead of being admitted together; every request is still answered."""
     matrix = instances.node_mip(seed=33, m=5000, n=10000)
     params = gbp.default_params(maxeasy=0.0)
-    pool = instances.uneven_batch(seed=34, count=4, rmin=2000, rmax=3000)
-    sizes = [serving._inst_bytes(i) for i in pool]
-    cap = max(sizes)
-    assert 2 * min(sizes) > cap
+    one = instances.uneven_batch(seed=34, count=1, rmin=2000, rmax=3000)[0]
+    pool = [one] * 4
+    cap = serving._inst_bytes(one)  # room for exactly one request in flight
     srv = serving.PropagationServer(matrix, matrix.lb, matrix.ub, node_workers=1, inst_workers=2, params=params,
                                     hbm_cap=cap)
     try:
