@@ -444,6 +444,7 @@ def main():
 
     # plain path: the same nodes one at a time through the seeded single-problem call
     plain_nodes = min(8 if args.quick else 128, N)
+    prop.set_global_bounds(rlb, rub)  # a node's global domain: the root fixpoint
     t0 = time.perf_counter()
     for k in range(plain_nodes):
         lb, ub = rlb.copy(), rub.copy()
@@ -454,6 +455,7 @@ def main():
         ub[cols] = np.minimum(ub[cols], nodes.ub[sl])
         prop.propagate(lb, ub, seed=(cols, olb, oub))
     plain_v = plain_nodes / (time.perf_counter() - t0)
+    prop.set_global_bounds(None)
 
     line = {"metric": "node-fixpoints/sec", "value": value, "unit": "node-fixpoints/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,

@@ -58,6 +58,11 @@ typedef struct
 /* plain path: drive the rounds from the host (one synchronisation per round) instead of the device-side loop
  * (a CUDA graph whose conditional while-node repeats the round until the frontier is empty) */
 #define GBP_FLAG_HOSTLOOP 1
+/* constraints/linear/sortvars = FALSE: every entry of a row is tried.  By default (SCIP's default, TRUE) the
+ * binary columns of a row are tried in decreasing |a| (ties: lower column index first) and the first unfixed
+ * binary that yields no tightening ends the visit of the binaries, as tightenBounds does
+ * (cons_linear.c:7110-7138; order of consdataCompVarProp, cons_linear.c:3229-3254). */
+#define GBP_FLAG_NOSORTVARS 2
 
 typedef struct
 {
@@ -107,6 +112,13 @@ int gbp_propagate_device(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, co
  * struct SCIP_ConsData): act[4*i] = minhi, minlo, maxhi, maxlo; cnt[8*i] = minposinf, minneginf,
  * minposhuge, minneghuge, maxposinf, maxneginf, maxposhuge, maxneghuge; for all m rows. */
 int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double* act, int32_t* cnt);
+
+/* global domain of the plain path, for the binary test of GBP_FLAG_NOSORTVARS (a column is binary when it is
+ * integral and its global bounds lie inside [0,1], SCIPvarIsBinary, var.c:23801-23810).  glb/gub (host arrays
+ * of length n) are copied and used by later gbp_propagate calls until cleared with NULL or until the next upload;
+ * without them a call treats the bounds it propagates as global, as SCIP does at the root (depth 0).  The
+ * plugin passes SCIPvarGetLbGlobal/SCIPvarGetUbGlobal.  Batched nodes use their base bounds. */
+int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub);
 
 /* ---------------------------------------------------------------- batched path: distinct instances
  * Uneven independent instances (each a set of linear rows with its own columns) propagated together: instance k

@@ -127,7 +127,7 @@ void lpo_default_params(lpo_params* p)
    p->recompfac = 1e6;
    p->maxeasyactivitydelta = 0.0;
    p->maxrounds = 0;
-   p->reserved = 0;
+   p->flags = 0;
 }
 
 /* ------------------------------------------------------------------ row activity */
@@ -406,13 +406,30 @@ typedef struct
    int64_t ndirty;
    double* savelb;
    double* saveub;
+   /* binary skip: global domain for the binary test (NULL = current bounds) and the candidates of the
+    * row being processed, per entry position */
+   int binskip;
+   const double* glb;
+   const double* gub;
+   double* rub;
+   double* rlb;
+   uint8_t* rflag;      /* bit0 ub, bit1 forced ub, bit2 lb, bit3 forced lb */
 } Work;
 
 static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
 {
    int64_t n = P->n;
    int64_t m = P->m;
+   int64_t maxlen = 1;
+   int64_t i;
    memset(w, 0, sizeof(*w));
+   for( i = 0; i < m; ++i )
+      if( P->rowptr[i + 1] - P->rowptr[i] > maxlen )
+         maxlen = P->rowptr[i + 1] - P->rowptr[i];
+   w->binskip = !(par->flags & LPO_FLAG_NOSORTVARS);
+   w->rub = malloc(sizeof(double) * (size_t)maxlen);
+   w->rlb = malloc(sizeof(double) * (size_t)maxlen);
+   w->rflag = calloc((size_t)maxlen, 1);
    w->P = P;
    numFrom(par, &w->s);
    w->maxrounds = par->maxrounds > 0 ? par->maxrounds : 1000000;
@@ -433,7 +450,8 @@ static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
    w->savelb = malloc(sizeof(double) * (size_t)(n + 1));
    w->saveub = malloc(sizeof(double) * (size_t)(n + 1));
    return (w->cub && w->clb && w->cubf && w->clbf && w->cflag && w->touched && w->front && w->next && w->rowstamp
-      && w->oldlb && w->oldub && w->chg && w->dirty && w->dirtylist && w->savelb && w->saveub) ? 0 : -1;
+      && w->oldlb && w->oldub && w->chg && w->dirty && w->dirtylist && w->savelb && w->saveub && w->rub && w->rlb
+      && w->rflag) ? 0 : -1;
 }
 
 static void workFree(Work* w)
@@ -441,6 +459,7 @@ static void workFree(Work* w)
    free(w->cub); free(w->clb); free(w->cubf); free(w->clbf); free(w->cflag); free(w->touched);
    free(w->front); free(w->next); free(w->rowstamp); free(w->oldlb); free(w->oldub); free(w->chg);
    free(w->dirty); free(w->dirtylist); free(w->savelb); free(w->saveub);
+   free(w->rub); free(w->rlb); free(w->rflag);
 }
 
 static void newStamp(Work* w)
@@ -504,6 +523,86 @@ static void candLb(Work* w, int32_t j, double v, int force)
    if( !(w->cflag[j] & bit) || v > arr[j] )
       arr[j] = v;
    w->cflag[j] |= bit;
+}
+
+/* candidate of the row being processed for its entry at position k */
+static void rowUb(Work* w, int64_t k, double v, int force)
+{
+   uint8_t bit = force ? 2 : 1;
+   if( !(w->rflag[k] & 3) || v < w->rub[k] )
+      w->rub[k] = v;
+   w->rflag[k] |= bit;
+}
+
+static void rowLb(Work* w, int64_t k, double v, int force)
+{
+   uint8_t bit = force ? 8 : 4;
+   if( !(w->rflag[k] & 12) || v > w->rlb[k] )
+      w->rlb[k] = v;
+   w->rflag[k] |= bit;
+}
+
+/* SCIPvarIsBinary (var.c:23801-23810): integral with a global domain inside [0,1] */
+static int isBinary(const Work* w, int32_t j, const double* lb, const double* ub)
+{
+   const double* gl = w->glb != NULL ? w->glb : lb;
+   const double* gu = w->gub != NULL ? w->gub : ub;
+   return w->P->isint[j] != 0 && gl[j] >= 0.0 && gu[j] <= 1.0;
+}
+
+/* order of a row's binaries during solving, consdataCompVarProp (cons_linear.c:3229-3254): larger |a| first, ties
+ * by problem index (the column index).  SCIP counts |a| values within 1e-9 of each other as a tie; here |a| is
+ * compared exactly, which orders the same whenever a row's distinct binary coefficients differ by more than
+ * 1e-9 (a tolerance-based tie is not transitive, so it cannot define the order of a parallel reduction). */
+static int binBefore(const lpo_problem* P, int64_t p, int64_t q)
+{
+   double a1 = fabs(P->vals[p]);
+   double a2 = fabs(P->vals[q]);
+   if( a1 != a2 )
+      return a1 > a2;
+   return P->colidx[p] < P->colidx[q];
+}
+
+/* the candidates of one row reach the columns as tightenBounds would apply them (cons_linear.c:7110-7138):
+ * with the row's binaries visited in the order above, the first unfixed binary that gets no candidate ends
+ * the visit of the binaries, so candidates of the binaries after it are dropped; other columns keep theirs */
+static void commitRow(Work* w, const double* lb, const double* ub, int64_t p0, int64_t p1, lpo_result* res)
+{
+   const lpo_problem* P = w->P;
+   int64_t blocker = -1;
+   int64_t p;
+   if( w->binskip )
+   {
+      for( p = p0; p < p1; ++p )
+      {
+         int32_t j = P->colidx[p];
+         if( w->rflag[p - p0] != 0 || !isBinary(w, j, lb, ub) )
+            continue;
+         if( fabs(relDiff(ub[j], lb[j])) <= w->s.feastol )   /* SCIPisFeasEQ: fixed binaries never end it */
+            continue;
+         if( blocker < 0 || binBefore(P, p, blocker) )
+            blocker = p;
+      }
+   }
+   for( p = p0; p < p1; ++p )
+   {
+      uint8_t f = w->rflag[p - p0];
+      int32_t j = P->colidx[p];
+      if( f == 0 )
+         continue;
+      if( blocker >= 0 && binBefore(P, blocker, p) && isBinary(w, j, lb, ub) )
+         continue;
+      if( f & 3 )
+      {
+         candUb(w, j, w->rub[p - p0], (f & 2) != 0);
+         res->candidates++;
+      }
+      if( f & 12 )
+      {
+         candLb(w, j, w->rlb[p - p0], (f & 8) != 0);
+         res->candidates++;
+      }
+   }
 }
 
 /* one frontier row: cutoff check of propagateCons (cons_linear.c:7718-7753), skip tests of tightenBounds
@@ -572,6 +671,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
    }
    easy = lt(s, maxactdelta, s->maxeasy);
    force = (p1 - p0 == 1);
+   memset(w->rflag, 0, (size_t)(p1 - p0));
 
    for( p = p0; p < p1; ++p )
    {
@@ -603,8 +703,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   double nb = adjUb(s, isint, l + slack / val);
                   if( force || ubBetter(s, nb, l, u) )
                   {
-                     candUb(w, j, nb, force);
-                     res->candidates++;
+                     rowUb(w, p - p0, nb, force);
                   }
                }
                else
@@ -613,8 +712,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   double nb = adjLb(s, isint, u + slack / val);
                   if( force || lbBetter(s, nb, l, u) )
                   {
-                     candLb(w, j, nb, force);
-                     res->candidates++;
+                     rowLb(w, p - p0, nb, force);
                   }
                }
             }
@@ -635,8 +733,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   double nb = adjLb(s, isint, u - slack / val);
                   if( force || lbBetter(s, nb, l, u) )
                   {
-                     candLb(w, j, nb, force);
-                     res->candidates++;
+                     rowLb(w, p - p0, nb, force);
                   }
                }
                else
@@ -644,8 +741,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   double nb = adjUb(s, isint, l - slack / val);
                   if( force || ubBetter(s, nb, l, u) )
                   {
-                     candUb(w, j, nb, force);
-                     res->candidates++;
+                     rowUb(w, p - p0, nb, force);
                   }
                }
             }
@@ -677,8 +773,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   }
                   if( !unreliable )
                   {
-                     candUb(w, j, newub, force);
-                     res->candidates++;
+                     rowUb(w, p - p0, newub, force);
                   }
                }
             }
@@ -698,8 +793,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   }
                   if( !skip )
                   {
-                     candLb(w, j, newlb, force);
-                     res->candidates++;
+                     rowLb(w, p - p0, newlb, force);
                   }
                }
             }
@@ -722,8 +816,7 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   }
                   if( !unreliable )
                   {
-                     candLb(w, j, newlb, force);
-                     res->candidates++;
+                     rowLb(w, p - p0, newlb, force);
                   }
                }
             }
@@ -744,14 +837,14 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
                   }
                   if( !skip )
                   {
-                     candUb(w, j, newub, force);
-                     res->candidates++;
+                     rowUb(w, p - p0, newub, force);
                   }
                }
             }
          }
       }
    }
+   commitRow(w, lb, ub, p0, p1, res);
    return 0;
 }
 
@@ -878,7 +971,8 @@ static int fixpoint(Work* w, double* lb, double* ub, lpo_result* res, int track)
 }
 
 int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
-   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, lpo_result* res)
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
+   const double* gub, lpo_result* res)
 {
    Work w;
    int64_t k;
@@ -888,6 +982,8 @@ int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, do
       workFree(&w);
       return -1;
    }
+   w.glb = glb;
+   w.gub = gub;
    newStamp(&w);
    w.nnext = 0;
    if( seedcols == NULL )
@@ -951,6 +1047,8 @@ static void* nodeWorker(void* arg)
    }
    memcpy(lb, J->baselb, sizeof(double) * (size_t)P->n);
    memcpy(ub, J->baseub, sizeof(double) * (size_t)P->n);
+   w.glb = J->baselb;
+   w.gub = J->baseub;
 
    for( k = J->k0; k < J->k1; ++k )
    {

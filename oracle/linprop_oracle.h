@@ -32,8 +32,12 @@ typedef struct
    double recompfac;            /* numerics/recompfac */
    double maxeasyactivitydelta; /* constraints/linear/maxeasyactivitydelta (0 = residual rule everywhere) */
    int32_t maxrounds;           /* round cap; <= 0 means 1,000,000 */
-   int32_t reserved;
+   int32_t flags;               /* LPO_FLAG_* */
 } lpo_params;
+
+/* constraints/linear/sortvars = FALSE: every entry of a row is tried (no skipping of the binaries that
+ * follow one that cannot be tightened, cons_linear.c:7131-7136) */
+#define LPO_FLAG_NOSORTVARS 1
 
 typedef struct
 {
@@ -71,12 +75,15 @@ void lpo_row_activities(const lpo_problem* prob, const lpo_params* par, const do
    const int32_t* rows, int64_t nrows, double* act, int32_t* cnt);
 
 /* propagate to fixpoint in place; the first frontier is every row (seedcols == NULL) or the rows that the
- * listed column changes make relevant (seedcols[k] moved from [oldlb[k],oldub[k]] to the bounds in lb/ub) */
+ * listed column changes make relevant (seedcols[k] moved from [oldlb[k],oldub[k]] to the bounds in lb/ub).
+ * glb/gub: the global domain that decides which integer columns count as binary (SCIPvarIsBinary); NULL
+ * means the current bounds (propagation at the root, where local and global bounds coincide). */
 int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
-   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, lpo_result* res);
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
+   const double* gub, lpo_result* res);
 
-/* batch of nodes sharing base bounds: node k applies bound changes chg_col/chg_lb/chg_ub[ptr[k]..ptr[k+1])
- * and propagates; outputs per node the cutoff flag, rounds, and up to cap changed columns
+/* batch of nodes sharing base bounds, which are also every node's global domain: node k applies bound
+ * changes chg_col/chg_lb/chg_ub[ptr[k]..ptr[k+1]) and propagates; outputs per node the cutoff flag, rounds, and up to cap changed columns
  * (out_col/out_lb/out_ub[k*cap..]) whose final bounds differ from the base; out_n[k] = count (or -1 if
  * more than cap).  nthreads <= 0 uses one thread. Returns 0. */
 int lpo_propagate_nodes(const lpo_problem* prob, const lpo_params* par, const double* baselb, const double* baseub,

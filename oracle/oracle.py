@@ -16,6 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liblinprop_oracle.so")
 SCIP_ORACLE = os.path.join(HERE, "_ref", "scip_oracle")
+# the SCIP source tree the Makefile's `ref` target compiles (same default as its REFDIR)
+REFDIR = os.environ.get("REFDIR", "/root/reference")
 
 _P = ctypes.c_void_p
 
@@ -24,7 +26,11 @@ class Params(ctypes.Structure):
     _fields_ = [("infinity", ctypes.c_double), ("epsilon", ctypes.c_double), ("sumepsilon", ctypes.c_double),
                 ("feastol", ctypes.c_double), ("hugeval", ctypes.c_double), ("boundstreps", ctypes.c_double),
                 ("recompfac", ctypes.c_double), ("maxeasyactivitydelta", ctypes.c_double),
-                ("maxrounds", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("maxrounds", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+# Params.flags: constraints/linear/sortvars = FALSE (every entry of a row is tried)
+FLAG_NOSORTVARS = 1
 
 
 class Problem(ctypes.Structure):
@@ -57,7 +63,7 @@ def lib():
         L.lpo_row_activities.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P,
                                          ctypes.c_int64, _P, _P]
         L.lpo_propagate.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
-                                    _P, _P, ctypes.POINTER(Result)]
+                                    _P, _P, _P, _P, ctypes.POINTER(Result)]
         L.lpo_propagate_nodes.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64,
                                           _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(Result)]
@@ -65,11 +71,12 @@ def lib():
     return _lib
 
 
-def params(maxeasy: float = 0.0, maxrounds: int = 0) -> Params:
+def params(maxeasy: float = 0.0, maxrounds: int = 0, sortvars: bool = True) -> Params:
     p = Params()
     lib().lpo_default_params(ctypes.byref(p))
     p.maxeasyactivitydelta = maxeasy
     p.maxrounds = maxrounds
+    p.flags = 0 if sortvars else FLAG_NOSORTVARS
     return p
 
 
@@ -105,23 +112,27 @@ class Oracle:
                                  _ptr(act), _ptr(cnt))
         return act, cnt
 
-    def propagate(self, lb, ub, par=None, seed=None):
-        """Root-style fixpoint from all rows (seed None) or from (cols, oldlb, oldub) changes; returns
-        (lb, ub, Result)."""
+    def propagate(self, lb, ub, par=None, seed=None, glob=None):
+        """Fixpoint from all rows (seed None) or from (cols, oldlb, oldub) changes; returns (lb, ub, Result).
+        glob: (glb, gub), the global domain for the binary test; None = the current bounds (root)."""
         par = par or params()
         lb = np.array(lb, dtype=np.float64)
         ub = np.array(ub, dtype=np.float64)
         res = Result()
+        glb = gub = None
+        if glob is not None:
+            glb = np.ascontiguousarray(glob[0], dtype=np.float64)
+            gub = np.ascontiguousarray(glob[1], dtype=np.float64)
         if seed is None:
             lib().lpo_propagate(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), 0, None, None, None,
-                                ctypes.byref(res))
+                                _ptr(glb), _ptr(gub), ctypes.byref(res))
         else:
             cols, olb, oub = (np.ascontiguousarray(x) for x in seed)
             cols = cols.astype(np.int32)
             olb = olb.astype(np.float64)
             oub = oub.astype(np.float64)
             lib().lpo_propagate(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), len(cols), _ptr(cols),
-                                _ptr(olb), _ptr(oub), ctypes.byref(res))
+                                _ptr(olb), _ptr(oub), _ptr(glb), _ptr(gub), ctypes.byref(res))
         return lb, ub, res
 
     def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1):

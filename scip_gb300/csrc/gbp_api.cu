@@ -38,6 +38,11 @@ struct gbp_ctx {
   int8_t* d_isint = nullptr;
   int64_t* d_colptr = nullptr;
   uint32_t* d_cscrow = nullptr;
+  // explicit global bounds of the plain path (gbp_set_global_bounds)
+  bool has_global = false;
+  double* d_glb = nullptr;
+  double* d_gub = nullptr;
+  int64_t cap_glob = 0;
 
   // plain path
   double* d_lb = nullptr;
@@ -118,7 +123,7 @@ static void freeProblem(gbp_ctx* ctx) {
   void* ptrs[] = {ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint, ctx->d_colptr,
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
-                  ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut};
+                  ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -127,6 +132,7 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_touched = nullptr; ctx->d_list[0] = ctx->d_list[1] = nullptr; ctx->d_rowstamp = nullptr;
   ctx->d_allrows = nullptr; ctx->d_base = nullptr; ctx->slot_mem = nullptr; ctx->stage = nullptr;
   ctx->d_rowinst = nullptr; ctx->d_colinst = nullptr; ctx->d_instcut = nullptr; ctx->ninst = 0;
+  ctx->d_glb = nullptr; ctx->d_gub = nullptr; ctx->cap_glob = 0; ctx->has_global = false;
   ctx->cap_m = ctx->cap_n = ctx->cap_nnz = ctx->cap_inst = 0;
   ctx->stage_bytes = 0;
   ctx->nslots = 0;
@@ -137,7 +143,8 @@ static Prob devProb(const gbp_ctx* ctx, bool instances = false) {
   return Prob{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
               ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity,
               instances ? ctx->d_rowinst : nullptr, instances ? ctx->d_colinst : nullptr,
-              instances ? ctx->d_instcut : nullptr};
+              instances ? ctx->d_instcut : nullptr, (!instances && ctx->has_global) ? ctx->d_glb : nullptr,
+              (!instances && ctx->has_global) ? ctx->d_gub : nullptr};
 }
 
 static int gridFor(const gbp_ctx* ctx, int64_t work, int per_block = 256, int cap_per_sm = 16) {
@@ -189,7 +196,7 @@ int gbp_set_params(gbp_ctx* ctx, const gbp_params* p) {
     return fail(ctx, GBP_ERR_INVALID, "invalid numerics");
   ctx->par = *p;
   ctx->num = Num{p->infinity, p->epsilon, p->sumepsilon, p->feastol, p->hugeval, p->boundstreps, p->recompfac,
-                 p->maxeasyactivitydelta};
+                 p->maxeasyactivitydelta, (p->flags & GBP_FLAG_NOSORTVARS) ? 1 : 0};
   destroyGraphs(ctx);  // the numerics are baked into the graphs' kernel arguments
   return GBP_OK;
 }
@@ -313,6 +320,7 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->has_problem = false;
+  ctx->has_global = false;
   ctx->ninst = 0;
   destroyGraphs(ctx);
 
@@ -738,6 +746,35 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
   CK(cudaStreamSynchronize(ctx->stream));
   cudaFree(d_act);
   cudaFree(d_cnt);
+  return GBP_OK;
+}
+
+int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub) {
+  if (!ctx || !ctx->has_problem) return fail(ctx, GBP_ERR_INVALID, "no problem uploaded");
+  if ((glb == nullptr) != (gub == nullptr)) return fail(ctx, GBP_ERR_INVALID, "give both global bound arrays or none");
+  CK(cudaSetDevice(ctx->device));
+  destroyGraphs(ctx);  // the graphs hold the problem's pointers, including these
+  if (glb == nullptr) {
+    ctx->has_global = false;
+    return GBP_OK;
+  }
+  const int64_t nn = std::max<int64_t>(ctx->n, 1);
+  if (nn > ctx->cap_glob) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_glb) cudaFree(ctx->d_glb);
+    if (ctx->d_gub) cudaFree(ctx->d_gub);
+    ctx->d_glb = ctx->d_gub = nullptr;
+    ctx->cap_glob = 0;
+    CK(cudaMalloc(&ctx->d_glb, nn * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_gub, nn * sizeof(double)));
+    ctx->cap_glob = nn;
+  }
+  if (ctx->n) {
+    CK(cudaMemcpyAsync(ctx->d_glb, glb, ctx->n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_gub, gub, ctx->n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));  // the host arrays may go away after the call
+  ctx->has_global = true;
   return GBP_OK;
 }
 

@@ -40,6 +40,9 @@ struct Prob {
   const int32_t* rowinst;  // instance of each row
   const int32_t* colinst;  // instance of each column
   int* instcut;            // per-instance cutoff flags
+  // global domain for the binary test of the plain path (null: the bounds being propagated, as at the root)
+  const double* glb;
+  const double* gub;
 };
 
 // rows of an instance that is already infeasible are skipped
@@ -97,6 +100,8 @@ struct Front {
   int cap;  // = m
 };
 
+__device__ __forceinline__ long long absBitsOf(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+
 __device__ __forceinline__ void emitUb(Cands& C, int j, double v, bool force) {
   atomicMin(force ? &C.cubf[j] : &C.cub[j], dkey(v));
   int old = atomicOr(&C.cflag[j], force ? 2 : 1);
@@ -106,6 +111,41 @@ __device__ __forceinline__ void emitLb(Cands& C, int j, double v, bool force) {
   atomicMax(force ? &C.clbf[j] : &C.clb[j], dkey(v));
   int old = atomicOr(&C.cflag[j], force ? 8 : 4);
   if (old == 0) C.touched[atomicAdd(C.ntouched, 1)] = j;
+}
+
+// candidate sinks for columnCandidates: into the column slots (counted), or only noted
+struct EmitTo {
+  Cands* C;
+  int j;
+  long long* n;
+  __device__ __forceinline__ void operator()(bool isub, double v, bool force) const {
+    if (isub) emitUb(*C, j, v, force);
+    else emitLb(*C, j, v, force);
+    ++*n;
+  }
+};
+struct Probe {
+  bool* hit;
+  __device__ __forceinline__ void operator()(bool, double, bool) const { *hit = true; }
+};
+
+// SCIPvarIsBinary (var.c:23801-23810): integral with a global domain inside [0,1]; the accessor supplies
+// the global domain (base bounds of a node batch, explicit global bounds, or the bounds being propagated)
+template <class BND>
+__device__ __forceinline__ bool isBinaryCol(const Prob& P, const BND& B, int j) {
+  if (P.isint[j] == 0) return false;
+  double gl, gu;
+  B.glob(P, j, gl, gu);
+  return gl >= 0.0 && gu <= 1.0;
+}
+
+// Order of a row's binaries during solving (consdataCompVarProp, cons_linear.c:3229-3254): larger |a| first,
+// ties by column index.  |a| is compared exactly (SCIP's 1e-9 tie tolerance is not transitive); the two
+// orders agree whenever a row's distinct binary coefficients differ by more than 1e-9.
+__device__ __forceinline__ bool binBefore(const Prob& P, int64_t p, int64_t q) {
+  const long long a1 = absBitsOf(P.vals[p]), a2 = absBitsOf(P.vals[q]);
+  if (a1 != a2) return a1 > a2;
+  return P.colidx[p] < P.colidx[q];
 }
 
 __device__ __forceinline__ void pushRow(const Prob& P, Front& F, int row, int stamp) {
@@ -135,14 +175,15 @@ __device__ __forceinline__ void expandColumn(const Prob& P, Front& F, int j, boo
   }
 }
 
-// Candidate bounds of column j (entry val) in a row with activity a, under bounds [l,u]:
+// Candidate bounds of one entry (value val, column bounds [l,u]) in a row with activity a:
 // tightenVarBoundsEasy (cons_linear.c:5380-5653) when `easy`, else tightenVarBounds (:6700-6974).
-// `relres` recomputes a residual in plain double (consdataGetReliableResidualActivity, :2580-2657).
-// Returns true if the row proves infeasibility (easy rule only).
-template <class RELRES>
+// Each candidate goes to emit(isub, value, force).  `relres` recomputes a residual in plain double
+// (consdataGetReliableResidualActivity, :2580-2657).  Returns true if the row proves infeasibility (easy
+// rule only).
+template <class EMIT, class RELRES>
 __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, double lhs, double rhs, bool easy,
-                                                 bool force, int j, double val, double l, double u, bool isint,
-                                                 Cands& C, long long& ncand, const RELRES& relres) {
+                                                 bool force, double val, double l, double u, bool isint,
+                                                 const EMIT& emit, const RELRES& relres) {
   if (easy) {
     double minact = a.minhi + a.minlo;
     double maxact = a.maxhi + a.maxlo;
@@ -154,10 +195,10 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
       if (sumGt(s, alpha, slack) || (force && gt(s, alpha, slack))) {
         if (val > 0.0) {
           double nb = adjUb(s, isint, l + slack / val);  // tightenVarUb, cons_linear.c:5242
-          if (force || ubBetter(s, nb, l, u)) { emitUb(C, j, nb, force); ++ncand; }
+          if (force || ubBetter(s, nb, l, u)) emit(true, nb, force);
         } else {
           double nb = adjLb(s, isint, u + slack / val);  // tightenVarLb, cons_linear.c:5307
-          if (force || lbBetter(s, nb, l, u)) { emitLb(C, j, nb, force); ++ncand; }
+          if (force || lbBetter(s, nb, l, u)) emit(false, nb, force);
         }
       }
     }
@@ -169,10 +210,10 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
       if (sumGt(s, alpha, slack) || (force && gt(s, alpha, slack))) {
         if (val > 0.0) {
           double nb = adjLb(s, isint, u - slack / val);
-          if (force || lbBetter(s, nb, l, u)) { emitLb(C, j, nb, force); ++ncand; }
+          if (force || lbBetter(s, nb, l, u)) emit(false, nb, force);
         } else {
           double nb = adjUb(s, isint, l - slack / val);
-          if (force || ubBetter(s, nb, l, u)) { emitUb(C, j, nb, force); ++ncand; }
+          if (force || ubBetter(s, nb, l, u)) emit(true, nb, force);
         }
       }
     }
@@ -195,7 +236,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
           unrel = isInf(s, -minres) ||
                   (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
         }
-        if (!unrel) { emitUb(C, j, newub, force); ++ncand; }
+        if (!unrel) emit(true, newub, force);
       }
     }
     if (lhsok) {
@@ -208,7 +249,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
           skip = isInf(s, maxres) ||
                  (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
         }
-        if (!skip) { emitLb(C, j, newlb, force); ++ncand; }
+        if (!skip) emit(false, newlb, force);
       }
     }
   } else {
@@ -222,7 +263,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
           unrel = isInf(s, -minres) ||
                   (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
         }
-        if (!unrel) { emitLb(C, j, newlb, force); ++ncand; }
+        if (!unrel) emit(false, newlb, force);
       }
     }
     if (lhsok) {
@@ -236,7 +277,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
           skip = isInf(s, maxres) ||
                  (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) && !isint) && (!force || !lt(s, newub, u)));
         }
-        if (!skip) { emitUb(C, j, newub, force); ++ncand; }
+        if (!skip) emit(true, newub, force);
       }
     }
   }
@@ -302,6 +343,7 @@ struct RowBatch {
   int prefix[NT + 1];
   int order[NT];         // batch position -> row, sorted by length
   int hist[LONGROW + 2];
+  int bpos[NT];          // first binary in propagation order that gets no candidate (entry position, -1: none)
 };
 
 // Load entries [pb, min(pb+CHUNK, p1)) of a row: column indices and values first, then all bound gathers,
@@ -515,6 +557,36 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
   return 0;
 }
 
+// work item w of a batch belongs to the last batch row o with prefix[o] <= w
+template <int NT>
+__device__ __forceinline__ int itemOwner(const RowBatch<NT>& rb, int w) {
+  int lo = 0, hi = NT - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (rb.prefix[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// consdataGetReliableResidualActivity (cons_linear.c:2580-2657): the residual activity of entry p summed
+// again in plain double, in row order
+template <class BND>
+__device__ __forceinline__ double reliableResidual(const Prob& P, const BND& B, int64_t p0, int64_t p1, int64_t p,
+                                                   bool ismin) {
+  double r = 0.0;
+  for (int64_t q = p0; q < p1; ++q) {
+    if (q == p) continue;
+    const int jj = P.colidx[q];
+    const double vv = P.vals[q];
+    double ll, uu;
+    B.get(jj, ll, uu);
+    if (vv > 0.0) r += ismin ? vv * ll : vv * uu;
+    else r += ismin ? vv * uu : vv * ll;
+  }
+  return r;
+}
+
 // The CTA processes rows[0..nrows) (all <= LONGROW entries).  All threads of the CTA must call it with the
 // same arguments.  Sets *cut on infeasibility.
 template <int NT, class BND>
@@ -564,6 +636,7 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
       for (int q = 0; q < MAXSEL; ++q) rb.sel[tid][q] = sel[q];
     }
     rb.nsel[tid] = nsel;
+    rb.bpos[tid] = -1;
     __syncthreads();
     // exclusive prefix of the selection counts
     if (tid < 32) {
@@ -583,14 +656,15 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
     }
     __syncthreads();
     const int total = rb.prefix[NT];
-    for (int w = tid; w < total; w += NT) {
-      int lo = 0, hi = NT - 1;  // owner: last o with prefix[o] <= w
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (rb.prefix[mid] <= w) lo = mid;
-        else hi = mid - 1;
-      }
-      const int o = lo;
+    // Binary columns follow tightenBounds' visit (cons_linear.c:7110-7138): the row's binaries are tried in
+    // the order of binBefore and the first unfixed one without a candidate ends the visit.  So the candidates
+    // of binaries are held back (bit `it` of candm: this thread's it-th work item) until every binary of the
+    // batch has been tried and each row knows its first such binary (rb.bpos); then the ones before it are
+    // evaluated again and emitted.  A thread has at most LONGROW work items (total <= NT * LONGROW).
+    unsigned long long candm = 0ull;
+    int it = 0;
+    for (int w = tid; w < total; w += NT, ++it) {
+      const int o = itemOwner(rb, w);
       const int k = w - rb.prefix[o];
       const int64_t p0 = rb.p0[o];
       const int64_t p1 = p0 + rb.len[o];
@@ -600,21 +674,50 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
       double l, u;
       B.get(j, l, u);
       const Act a = rb.act[o];
-      auto relres = [&](bool ismin) {
-        double r = 0.0;
-        for (int64_t q = p0; q < p1; ++q) {
-          if (q == p) continue;
-          int jj2 = P.colidx[q];
-          double vv2 = P.vals[q], l2, u2;
-          B.get(jj2, l2, u2);
-          if (vv2 > 0.0) r += ismin ? vv2 * l2 : vv2 * u2;
-          else r += ismin ? vv2 * u2 : vv2 * l2;
-        }
-        return r;
-      };
-      if (columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, p1 - p0 == 1, j, v, l, u, P.isint[j] != 0, C,
-                           st.cands, relres))
+      const bool force = p1 - p0 == 1;
+      auto relres = [&](bool ismin) { return reliableResidual(P, B, p0, p1, p, ismin); };
+      if (s.nosort || force || !isBinaryCol(P, B, j)) {
+        if (columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, force, v, l, u, P.isint[j] != 0,
+                             EmitTo{&C, j, &st.cands}, relres))
+          cutRow(P, rb.order[o], cut);
+        continue;
+      }
+      bool hit = false;
+      if (columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, false, v, l, u, true, Probe{&hit}, relres))
         cutRow(P, rb.order[o], cut);
+      if (hit) {
+        candm |= 1ull << it;
+      } else if (!feasEq(s, u, l)) {
+        // keep the earliest such binary of the row
+        const int mine = (int)(p - p0);
+        int cur = rb.bpos[o];
+        while (cur < 0 || binBefore(P, p, p0 + cur)) {
+          const int prev = atomicCAS(&rb.bpos[o], cur, mine);
+          if (prev == cur) break;
+          cur = prev;
+        }
+      }
+    }
+    if (__syncthreads_or(candm != 0ull)) {
+      it = 0;
+      for (int w = tid; w < total; w += NT, ++it) {
+        if (!((candm >> it) & 1ull)) continue;
+        const int o = itemOwner(rb, w);
+        const int k = w - rb.prefix[o];
+        const int64_t p0 = rb.p0[o];
+        const int64_t p1 = p0 + rb.len[o];
+        const int64_t p = p0 + (rb.full[o] ? k : (int)rb.sel[o][k]);
+        const int b = rb.bpos[o];
+        if (b >= 0 && binBefore(P, p0 + b, p)) continue;  // visited after the end of the binaries
+        const int j = P.colidx[p];
+        const double v = P.vals[p];
+        double l, u;
+        B.get(j, l, u);
+        const Act a = rb.act[o];
+        auto relres = [&](bool ismin) { return reliableResidual(P, B, p0, p1, p, ismin); };
+        columnCandidates(s, a, rb.lhs[o], rb.rhs[o], rb.easy[o] != 0, false, v, l, u, true, EmitTo{&C, j, &st.cands},
+                         relres);
+      }
     }
     __syncthreads();
   }
@@ -734,12 +837,8 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
     }
   }
   const long long infb = __double_as_longlong(s.inf), hugeb = __double_as_longlong(s.huge);
-  bool cut = false;
-  for (int64_t p = p0 + lane; p < p1; p += 32) {
-    int j = P.colidx[p];
-    double v = P.vals[p];
-    double l, u;
-    B.get(j, l, u);
+  // entry p can produce a candidate (the necessary conditions above)
+  auto selected = [&](double v, double l, double u) {
     const double d = __longlong_as_double(deltaBits(s, v, l, u));  // +inf for an infinite bound
     bool go = (useR && d > thrR) || (useL && d > thrL);
     if (!go && (specMin || specMax)) {
@@ -748,25 +847,81 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
       if (specMin) go |= (absBits(bmin) >= infb) || (absBits(v * bmin) >= hugeb);
       if (specMax) go |= (absBits(bmax) >= infb) || (absBits(v * bmax) >= hugeb);
     }
-    if (!go) continue;
-    auto relres = [&](bool ismin) {
-      double r = 0.0;
-      for (int64_t q = p0; q < p1; ++q) {
-        if (q == p) continue;
-        int jj = P.colidx[q];
-        double vv = P.vals[q], ll, uu;
-        B.get(jj, ll, uu);
-        if (vv > 0.0) r += ismin ? vv * ll : vv * uu;
-        else r += ismin ? vv * uu : vv * ll;
+    return go;
+  };
+  // Binary columns follow tightenBounds' visit (cons_linear.c:7110-7138), as in processShortRows: their
+  // candidates wait until the warp knows the row's first binary (in binBefore order) that gets none.  Bit it
+  // of candm marks the lane's it-th entry; entries past the 64th of a lane are tried again afterwards.
+  bool cut = false;
+  unsigned long long candm = 0ull;
+  bool later = false;                 // a binary candidate beyond the 64th entry of this lane
+  long long blkA = -1;                // the lane's first candidate-free unfixed binary: |a| bits, column
+  int blkC = 0x7fffffff;
+  int it = 0;
+  for (int64_t p = p0 + lane; p < p1; p += 32, ++it) {
+    int j = P.colidx[p];
+    double v = P.vals[p];
+    double l, u;
+    B.get(j, l, u);
+    if (!selected(v, l, u)) continue;
+    auto relres = [&](bool ismin) { return reliableResidual(P, B, p0, p1, p, ismin); };
+    if (s.nosort || !isBinaryCol(P, B, j)) {
+      if (columnCandidates(s, a, lhs, rhs, easy, false, v, l, u, P.isint[j] != 0, EmitTo{&C, j, &st.cands},
+                           relres)) {
+        cut = true;
+        break;
       }
-      return r;
-    };
-    if (columnCandidates(s, a, lhs, rhs, easy, false, j, v, l, u, P.isint[j] != 0, C, st.cands, relres)) {
+      continue;
+    }
+    bool hit = false;
+    if (columnCandidates(s, a, lhs, rhs, easy, false, v, l, u, true, Probe{&hit}, relres)) {
       cut = true;
       break;
     }
+    if (hit) {
+      if (it < 64) candm |= 1ull << it;
+      else later = true;
+    } else if (!feasEq(s, u, l)) {
+      const long long ab = absBitsOf(v);
+      if (ab > blkA || (ab == blkA && j < blkC)) {
+        blkA = ab;
+        blkC = j;
+      }
+    }
   }
-  return __any_sync(0xffffffffu, cut);
+  if (__any_sync(0xffffffffu, cut)) return true;
+  if (!__any_sync(0xffffffffu, candm != 0ull || later)) return false;
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    const long long oa = __shfl_xor_sync(0xffffffffu, blkA, off);
+    const int oc = __shfl_xor_sync(0xffffffffu, blkC, off);
+    if (oa > blkA || (oa == blkA && oc < blkC)) {
+      blkA = oa;
+      blkC = oc;
+    }
+  }
+  // a binary is visited if it comes before the first candidate-free one
+  auto visited = [&](double v, int j) {
+    const long long ab = absBitsOf(v);
+    return blkA < 0 || ab > blkA || (ab == blkA && j < blkC);
+  };
+  it = 0;
+  for (int64_t p = p0 + lane; p < p1; p += 32, ++it) {
+    if (it < 64) {
+      if (!((candm >> it) & 1ull)) continue;
+    } else if (!later) {
+      break;
+    }
+    const int j = P.colidx[p];
+    const double v = P.vals[p];
+    if (!visited(v, j)) continue;
+    double l, u;
+    B.get(j, l, u);
+    if (it >= 64 && (!selected(v, l, u) || !isBinaryCol(P, B, j))) continue;
+    auto relres = [&](bool ismin) { return reliableResidual(P, B, p0, p1, p, ismin); };
+    columnCandidates(s, a, lhs, rhs, easy, false, v, l, u, true, EmitTo{&C, j, &st.cands}, relres);
+  }
+  return false;
 }
 
 // Acceptance of column j's best candidates against its round-start bounds [l,u]: upper bound first

@@ -19,6 +19,11 @@ struct PlainBnd {
     l = lb[j];
     u = ub[j];
   }
+  // global domain: the problem's explicit global bounds, else the bounds being propagated (root)
+  __device__ __forceinline__ void glob(const Prob& P, int j, double& l, double& u) const {
+    l = P.glb != nullptr ? P.glb[j] : lb[j];
+    u = P.gub != nullptr ? P.gub[j] : ub[j];
+  }
 };
 
 // node bounds: the per-CTA overlay where this node changed a column, else the shared base (packed pairs,
@@ -35,6 +40,12 @@ struct OvlBnd {
   }
   __device__ __forceinline__ void get(int j, double& l, double& u) const {
     double2 b = (ostamp[j] == epoch) ? ovl[j] : getBase(j);
+    l = b.x;
+    u = b.y;
+  }
+  // global domain of every node of the batch: the base bounds
+  __device__ __forceinline__ void glob(const Prob&, int j, double& l, double& u) const {
+    double2 b = getBase(j);
     l = b.x;
     u = b.y;
   }

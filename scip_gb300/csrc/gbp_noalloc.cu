@@ -128,7 +128,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   else gbp_default_params(&p);
   NodesArgs A;
   A.s = Num{p.infinity, p.epsilon, p.sumepsilon, p.feastol, p.hugeval, p.boundstreps, p.recompfac,
-            p.maxeasyactivitydelta};
+            p.maxeasyactivitydelta, (p.flags & GBP_FLAG_NOSORTVARS) ? 1 : 0};
   A.P = Prob{m, n, rowptr, colidx, vals, lhs, rhs, isint, colptr, nullptr, rowidx, cvals, p.infinity};
   A.base = nullptr;
   A.baselb = baselb;

@@ -12,6 +12,7 @@ namespace gbp {
 
 struct Num {
   double inf, eps, sumeps, feastol, huge, bstreps, recomp, maxeasy;
+  int nosort;  // constraints/linear/sortvars = FALSE: every entry of a row is tried (no binary skip)
 };
 
 __host__ __device__ __forceinline__ bool isInf(const Num& s, double x) { return x >= s.inf; }   // set.c:6824
@@ -34,6 +35,7 @@ __host__ __device__ __forceinline__ double relDiff(double a, double b) {
 }
 __host__ __device__ __forceinline__ bool feasLt(const Num& s, double a, double b) { return relDiff(a, b) < -s.feastol; }
 __host__ __device__ __forceinline__ bool feasGt(const Num& s, double a, double b) { return relDiff(a, b) > s.feastol; }
+__host__ __device__ __forceinline__ bool feasEq(const Num& s, double a, double b) { return fabs(relDiff(a, b)) <= s.feastol; }
 __host__ __device__ __forceinline__ double feasFloor(const Num& s, double x) { return floor(x + s.feastol); }
 __host__ __device__ __forceinline__ double feasCeil(const Num& s, double x) { return ceil(x - s.feastol); }
 __host__ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }

@@ -27,13 +27,14 @@ GBP_ERR_OVERFLOW = -6
 GBP_ERR_STATE = -7
 GBP_ERR_TOO_LARGE = -8
 GBP_FLAG_HOSTLOOP = 1
+GBP_FLAG_NOSORTVARS = 2
 
 # every symbol include/gbp.h declares (checked by the CPU test suite)
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
            "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
-           "gbp_propagate_instances_device"]
+           "gbp_propagate_instances_device", "gbp_set_global_bounds"]
 
 
 class GbpParams(ctypes.Structure):
@@ -86,6 +87,7 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_device.argtypes = L.gbp_propagate.argtypes
     L.gbp_row_activities.argtypes = [_P, _P, _P, _P, _P]
+    L.gbp_set_global_bounds.argtypes = [_P, _P, _P]
     L.gbp_propagate_nodes.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
@@ -101,12 +103,14 @@ def load_library(path: Optional[str] = None):
     return L
 
 
-def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0) -> GbpParams:
+def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars: bool = True) -> GbpParams:
     p = GbpParams()
     load_library().gbp_default_params(ctypes.byref(p))
     if maxeasy is not None:
         p.maxeasyactivitydelta = maxeasy
     p.maxrounds = maxrounds
+    if not sortvars:
+        p.flags |= GBP_FLAG_NOSORTVARS
     return p
 
 
@@ -254,6 +258,16 @@ class Propagator:
         cnt = np.zeros((self.m, 8), dtype=np.int32)
         self._check(self.L.gbp_row_activities(self.h, _ptr(lb), _ptr(ub), _ptr(act), _ptr(cnt)))
         return act, cnt
+
+    def set_global_bounds(self, glb=None, gub=None):
+        """Global domain for the binary test of later propagate() calls (None: the propagated bounds, as at the
+        root)."""
+        if glb is None:
+            self._check(self.L.gbp_set_global_bounds(self.h, None, None))
+            return
+        glb = np.ascontiguousarray(glb, dtype=np.float64)
+        gub = np.ascontiguousarray(gub, dtype=np.float64)
+        self._check(self.L.gbp_set_global_bounds(self.h, _ptr(glb), _ptr(gub)))
 
     def propagate_nodes(self, baselb, baseub, nodes, out_cap: Optional[int] = None) -> NodeResults:
         """Host arrays: nodes is an instances.NodeBatch.  Returns packed per-node results."""

@@ -240,6 +240,29 @@ def set_cover(rng: np.random.Generator, m: int, n: int) -> Instance:
                     name=f"set_cover({m}x{n})", x0=np.ones(n))
 
 
+def indicator_packing(rng: np.random.Generator, m: int, n: int, kmin: int = 4, kmax: int = 30,
+                      long_frac: float = 0.0) -> Instance:
+    """Binary packing rows with one indicator: sum_{j in S_i} x_j - y_i <= 1 (|S_i| in kmin..kmax, the rows of
+    a long_frac share have 65..300 entries), all columns binary.  Once two members of a row are fixed to 1 its
+    minimal activity equals the right-hand side; the residual rule then leaves the free members alone
+    (cons_linear.c:6766) and fixes y_i to 1 only if y_i comes before the first free member in the row's
+    propagation order (larger |a| first, ties by column index).  The members carry coefficient 1 and the
+    indicator 1 or 2, so both outcomes occur."""
+    lengths = rng.integers(kmin, kmax + 1, size=m)
+    if long_frac > 0:
+        big = rng.random(m) < long_frac
+        lengths[big] = rng.integers(65, 301, size=int(big.sum()))
+    lengths = np.minimum(lengths, n - 1)
+    rowptr, colidx = _distinct_columns(rng, lengths + 1, n)
+    vals = np.ones(colidx.shape[0])
+    last = rowptr[1:] - 1                      # the indicator: the last entry of each row
+    vals[last] = -rng.choice([1.0, 2.0], size=m, p=[0.8, 0.2])
+    lhs = np.full(m, -INF)
+    rhs = np.ones(m)
+    return Instance(rowptr, colidx, vals, lhs, rhs, np.zeros(n), np.ones(n), np.ones(n, dtype=np.int8),
+                    name=f"indicator_packing({m}x{n})", x0=np.zeros(n))
+
+
 def multi_knapsack(rng: np.random.Generator, m: int, n: int) -> Instance:
     """Multi-knapsack: integer columns in [0,5], weights U{1..100}, capacity 40 % of the row's max activity."""
     lengths = np.minimum(rng.integers(5, 41, size=m), n)

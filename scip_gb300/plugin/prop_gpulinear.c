@@ -40,6 +40,9 @@ struct SCIP_PropData
    double*               snaplb;             /**< local bounds after the previous call */
    double*               snapub;
    SCIP_Bool             havesnap;
+   double*               glb;                /**< global bounds last passed to the device (binary test) */
+   double*               gub;
+   SCIP_Bool             haveglobal;
    int32_t*              seeds;
    double*               seedlo;
    double*               seedhi;
@@ -61,6 +64,9 @@ static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIPfreeMemoryArrayNull(scip, &pd->ub);
    SCIPfreeMemoryArrayNull(scip, &pd->snaplb);
    SCIPfreeMemoryArrayNull(scip, &pd->snapub);
+   SCIPfreeMemoryArrayNull(scip, &pd->glb);
+   SCIPfreeMemoryArrayNull(scip, &pd->gub);
+   pd->haveglobal = FALSE;
    SCIPfreeMemoryArrayNull(scip, &pd->seeds);
    SCIPfreeMemoryArrayNull(scip, &pd->seedlo);
    SCIPfreeMemoryArrayNull(scip, &pd->seedhi);
@@ -95,6 +101,8 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->ub, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snaplb, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snapub, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->glb, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->gub, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seeds, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seedlo, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seedhi, nvars > 0 ? nvars : 1) );
@@ -179,6 +187,11 @@ static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
    p.recompfac = v;
    if( SCIPgetRealParam(scip, "constraints/linear/maxeasyactivitydelta", &v) == SCIP_OKAY )
       p.maxeasyactivitydelta = v;
+   {
+      SCIP_Bool sortvars = TRUE;
+      if( SCIPgetBoolParam(scip, "constraints/linear/sortvars", &sortvars) == SCIP_OKAY && !sortvars )
+         p.flags |= GBP_FLAG_NOSORTVARS;
+   }
    if( gbp_set_params(pd->ctx, &p) != GBP_OK )
       return SCIP_INVALIDDATA;
    return SCIP_OKAY;
@@ -272,6 +285,43 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    {
       pd->lb[j] = SCIPvarGetLbLocal(pd->vars[j]);
       pd->ub[j] = SCIPvarGetUbLocal(pd->vars[j]);
+   }
+   /* the binary test of the device reads the global domain (SCIPvarIsBinary); at the root the local bounds are
+    * the global ones, below it the global bounds go to the device whenever they changed */
+   if( SCIPgetDepth(scip) > 0 )
+   {
+      SCIP_Bool changed = !pd->haveglobal;
+      for( j = 0; j < pd->ncols; ++j )
+      {
+         double gl = SCIPvarGetLbGlobal(pd->vars[j]);
+         double gu = SCIPvarGetUbGlobal(pd->vars[j]);
+         if( changed || gl != pd->glb[j] || gu != pd->gub[j] )
+         {
+            changed = TRUE;
+            pd->glb[j] = gl;
+            pd->gub[j] = gu;
+         }
+      }
+      if( changed )
+      {
+         rc = gbp_set_global_bounds(pd->ctx, pd->glb, pd->gub);
+         if( rc != GBP_OK )
+         {
+            disable(scip, pd, "passing the global bounds failed", rc);
+            return SCIP_OKAY;
+         }
+         pd->haveglobal = TRUE;
+      }
+   }
+   else if( pd->haveglobal )
+   {
+      rc = gbp_set_global_bounds(pd->ctx, NULL, NULL);
+      if( rc != GBP_OK )
+      {
+         disable(scip, pd, "clearing the global bounds failed", rc);
+         return SCIP_OKAY;
+      }
+      pd->haveglobal = FALSE;
    }
    if( pd->havesnap )
    {

@@ -199,6 +199,7 @@ class PlainServer:
         self.params = params or gbp.default_params(maxeasy=0.0)
         self.node_prop = gbp.Propagator(device, params=self.params)
         self.node_prop.upload(matrix)
+        self.node_prop.set_global_bounds(self.root_lb, self.root_ub)  # a node's global domain: the root bounds
         self.inst_prop = gbp.Propagator(device, params=self.params)
 
     def answer(self, req):

@@ -10,8 +10,11 @@ SCIP's per-node cutoff verdicts and changed bounds.  Cases:
   node_mip_small             1,500 x 3,000 general rows (log-uniform coefficients, infinite bounds) + 200 nodes
   zipf_small                 1,500 x 3,000 Zipf row lengths up to 400 (rows longer than 64 entries)
   set_cover / knapsack / network   one small instance of each uneven-batch family + 100 nodes
+  indicator_packing          2,000 x 4,000 binary packing rows with an indicator (3 % of rows 65..300 long)
+                             + 300 nodes: SCIP's binary skip in tightenBounds decides many of them
 
-Usage: python tests/golden/make_golden.py   (needs the SCIP sources; writes tests/golden/*.npz)
+Usage: python tests/golden/make_golden.py [case ...]   (needs the SCIP sources; writes tests/golden/*.npz;
+no argument builds every case)
 """
 from __future__ import annotations
 
@@ -66,18 +69,38 @@ def save_case(name, inst, nnodes=0, node_seed=11):
     print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {nnodes} nodes, {os.path.getsize(path) // 1024} KiB")
 
 
-def main():
+def cases():
+    """name -> (instance builder, nodes); the uneven-family cases share one generator, drawn in this order."""
+    out = {}
+    for s in (0, 1, 2):
+        out[f"root_mip_s{s}"] = (lambda s=s: instances.root_mip(s), 200 if s == 0 else 0)
+    out["node_mip_small"] = (lambda: instances.node_mip(seed=21, m=1500, n=3000), 200)
+    out["zipf_small"] = (lambda: instances.zipf_mip(seed=22, m=1500, n=3000, hi=400), 100)
+    rng = np.random.default_rng(np.random.PCG64(23))
+    fam = {}
+
+    def family(k):
+        if not fam:
+            fam["set_cover"] = instances.set_cover(rng, 1200, 2400)
+            fam["knapsack"] = instances.multi_knapsack(rng, 1000, 2000)
+            fam["network"] = instances.network_flow(rng, 1500)
+        return fam[k]
+
+    for k in ("set_cover", "knapsack", "network"):
+        out[k] = (lambda k=k: family(k), 100)
+    out["indicator_packing"] = (lambda: instances.indicator_packing(np.random.default_rng(np.random.PCG64(24)),
+                                                                    2000, 4000, long_frac=0.03), 300)
+    return out
+
+
+def main(names):
     if not os.path.exists(oracle.SCIP_ORACLE):
         raise SystemExit("oracle/_ref/scip_oracle missing: run `make -C oracle ref` where the SCIP sources are")
-    for s in (0, 1, 2):
-        save_case(f"root_mip_s{s}", instances.root_mip(s), nnodes=200 if s == 0 else 0)
-    save_case("node_mip_small", instances.node_mip(seed=21, m=1500, n=3000), nnodes=200)
-    save_case("zipf_small", instances.zipf_mip(seed=22, m=1500, n=3000, hi=400), nnodes=100)
-    rng = np.random.default_rng(np.random.PCG64(23))
-    save_case("set_cover", instances.set_cover(rng, 1200, 2400), nnodes=100)
-    save_case("knapsack", instances.multi_knapsack(rng, 1000, 2000), nnodes=100)
-    save_case("network", instances.network_flow(rng, 1500), nnodes=100)
+    all_cases = cases()
+    for name in names or list(all_cases):
+        make, nnodes = all_cases[name]
+        save_case(name, make(), nnodes=nnodes)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

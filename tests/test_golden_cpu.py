@@ -22,11 +22,12 @@ RECORDED = {
     ("root_mip_s2", "res"): (0, 17, 0), ("root_mip_s2", "easy"): (0, 17, 0),
     ("set_cover", "res"): (0, 0, 0), ("set_cover", "easy"): (0, 0, 0),
     ("zipf_small", "res"): (0, 427, 30), ("zipf_small", "easy"): (0, 427, 30),
+    ("indicator_packing", "res"): (0, 0, 0), ("indicator_packing", "easy"): (0, 0, 0),
 }
 
 
-def run_oracle(oracle_mod, inst, z, tag):
-    par = oracle_mod.params(0.0 if tag == "res" else 1e6)
+def run_oracle(oracle_mod, inst, z, tag, sortvars=True):
+    par = oracle_mod.params(0.0 if tag == "res" else 1e6, sortvars=sortvars)
     orc = oracle_mod.Oracle(inst)
     root = G.Agreement()
     lb, ub, r = orc.propagate(inst.lb, inst.ub, par)
@@ -74,3 +75,14 @@ def test_scip_fixpoint_is_oracle_fixpoint(oracle_mod, case, tag):
     il = inst.isint == 1
     assert not ((lb != slb) | (ub != sub))[il].any(), "SCIP's root fixpoint admits an integer tightening"
     assert int(((lb != slb) | (ub != sub))[~il].sum()) <= 2
+
+
+def test_indicator_packing_pins_the_binary_skip(oracle_mod):
+    """On the indicator-packing fixture SCIP's result depends on tightenBounds ending the visit of a row's
+    binaries at the first one it cannot tighten (cons_linear.c:7110-7138): trying every entry instead
+    (constraints/linear/sortvars = FALSE) contradicts SCIP's own node results, with it they agree exactly."""
+    inst, z = G.load("indicator_packing")
+    _, with_skip = run_oracle(oracle_mod, inst, z, "res")
+    _, without = run_oracle(oracle_mod, inst, z, "res", sortvars=False)
+    assert with_skip.cutoff_mismatch == 0 and with_skip.int_exact == with_skip.problems
+    assert without.cutoff_mismatch > 0 and without.int_exact < without.problems

@@ -81,3 +81,61 @@ def test_node_outside_domain_is_cut_off(oracle_mod):
     out = oracle_mod.Oracle(inst).propagate_nodes(inst.lb, inst.ub, nodes, oracle_mod.params(0.0), cap=4)
     assert list(out["cutoff"]) == [1, 0]
     assert out["n"][1] == 1 and out["col"][1, 0] == 1 and out["lb"][1, 0] == 3.0
+
+
+def _scip_or_skip(oracle_mod, inst, easy):
+    import os
+    if not os.path.exists(oracle_mod.SCIP_ORACLE):
+        return None
+    cut, lb, ub, _ = oracle_mod.run_scip(inst, easy=easy)
+    return cut, lb, ub
+
+
+@pytest.mark.parametrize("indicator_first,sortvars,expect_lb4", [(False, True, 0.0), (True, True, 1.0),
+                                                                  (False, False, 1.0), (True, False, 1.0)])
+def test_binary_skip_order(oracle_mod, indicator_first, sortvars, expect_lb4):
+    # x0 + x1 + x2 + x3 - y <= 1, all binary, x0 = x1 = 1: the minimal activity equals the right-hand side.
+    # Residual rule: x2 and x3 (lb 0) would drop to 0, but their residual equals rhs, which tightenVarBounds
+    # refuses (cons_linear.c:6766); y would rise to 1.  tightenBounds tries the binaries by |a|, then column
+    # index, and the first unfixed one it cannot tighten ends the visit (cons_linear.c:7131-7136): y is
+    # tightened only if it comes before x2, i.e. if its column index is the lowest.
+    cols = [1, 2, 3, 4, 0] if indicator_first else [0, 1, 2, 3, 4]
+    y = cols[4]
+    lb = np.zeros(5)
+    ub = np.ones(5)
+    lb[cols[0]] = lb[cols[1]] = 1.0
+    inst = single_rows([(cols, [1.0, 1.0, 1.0, 1.0, -1.0], -INF, 1.0)], lb, ub, [1] * 5)
+    plb, pub, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(0.0, sortvars=sortvars))
+    assert not r.cutoff
+    assert plb[y] == expect_lb4 and pub[y] == 1.0
+    assert pub[cols[2]] == 1.0 and pub[cols[3]] == 1.0   # the guard keeps the members free
+    if sortvars:
+        scip = _scip_or_skip(oracle_mod, inst, easy=False)
+        if scip is not None:
+            assert not scip[0] and np.array_equal(scip[1], plb) and np.array_equal(scip[2], pub)
+
+
+def test_binary_skip_leaves_the_easy_rule_alone(oracle_mod):
+    # the slack rule has no residual guard: with slack 0 every free member drops to 0 and y rises to 1,
+    # whatever the order
+    lb = np.array([1.0, 1.0, 0.0, 0.0, 0.0])
+    inst = single_rows([([0, 1, 2, 3, 4], [1.0, 1.0, 1.0, 1.0, -1.0], -INF, 1.0)], lb, np.ones(5), [1] * 5)
+    plb, pub, r = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(1e6))
+    assert list(pub) == [1.0, 1.0, 0.0, 0.0, 1.0] and plb[4] == 1.0
+    scip = _scip_or_skip(oracle_mod, inst, easy=True)
+    if scip is not None:
+        assert np.array_equal(scip[1], plb) and np.array_equal(scip[2], pub)
+
+
+def test_binary_test_uses_the_global_domain(oracle_mod):
+    # x2 is integral with global domain [0, 3] but local [0, 1]: not binary, so it does not end the visit
+    # of the binaries and y (after it in column order) is tightened; with global [0, 1] it does end it
+    lb = np.array([1.0, 1.0, 0.0, 0.0])
+    ub = np.array([1.0, 1.0, 1.0, 1.0])
+    inst = single_rows([([0, 1, 2, 3], [1.0, 1.0, 1.0, -1.0], -INF, 1.0)], lb, ub, [1] * 4)
+    orc = oracle_mod.Oracle(inst)
+    glb = np.zeros(4)
+    wide = np.array([1.0, 1.0, 3.0, 1.0])
+    l1, _, _ = orc.propagate(lb, ub, oracle_mod.params(0.0), glob=(glb, wide))
+    l2, _, _ = orc.propagate(lb, ub, oracle_mod.params(0.0), glob=(glb, ub))
+    assert l1[3] == 1.0 and l2[3] == 0.0

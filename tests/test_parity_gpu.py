@@ -112,6 +112,7 @@ def test_nodes_seeded_plain_path_equals_batched(gpu_prop, oracle_mod):
     rlb, rub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
     nodes = instances.node_batch(inst, rlb, rub, 40, seed=2)
     r = gpu_prop.propagate_nodes(rlb, rub, nodes)
+    gpu_prop.set_global_bounds(rlb, rub)  # the nodes' global domain is the root fixpoint
     for k in range(nodes.nnodes):
         lb, ub = rlb.copy(), rub.copy()
         sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
@@ -127,6 +128,7 @@ def test_nodes_seeded_plain_path_equals_batched(gpu_prop, oracle_mod):
             elb[c] = l
             eub[c] = u
             assert np.array_equal(plb, elb) and np.array_equal(pub, eub)
+    gpu_prop.set_global_bounds(None)
 
 
 @pytest.mark.parametrize("maxeasy", [0.0, 1e6])
@@ -171,3 +173,81 @@ def test_uneven_instances_device_variant(gpu_prop, oracle_mod):
         sl = slice(col_off[k], col_off[k + 1])
         if not hcut[k]:
             assert np.array_equal(hlb[sl], olb) and np.array_equal(hub[sl], oub)
+
+
+# ---------------------------------------------------------------------------------------------------------
+# binary skip of tightenBounds (cons_linear.c:7110-7138): packing rows with an indicator, where it decides
+# many nodes under the residual rule; long_frac adds rows of 65..300 entries (warp path)
+def _indicator(long_frac):
+    return instances.indicator_packing(np.random.default_rng(7), 6000, 12000, long_frac=long_frac)
+
+
+@pytest.mark.parametrize("sortvars", [True, False])
+@pytest.mark.parametrize("long_frac", [0.0, 0.1])
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_indicator_nodes_match_oracle(gpu_prop, oracle_mod, maxeasy, long_frac, sortvars):
+    inst = _indicator(long_frac)
+    orc = oracle_mod.Oracle(inst)
+    par = oracle_mod.params(maxeasy, sortvars=sortvars)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    nodes = instances.node_batch(inst, rlb, rub, 1024, seed=4)
+    gpu_prop.set_params(gbp.default_params(maxeasy=maxeasy, sortvars=sortvars))
+    gpu_prop.upload(inst)
+    for threads in (32, 128, 256):
+        gpu_prop.set_batch_shape(threads, 0)
+        r = gpu_prop.propagate_nodes(rlb, rub, nodes)
+        o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+        _nodes_equal(r, o, nodes.nnodes)
+    gpu_prop.set_batch_shape(128, 0)
+    gpu_prop.set_params(_params(maxeasy))
+
+
+@pytest.mark.parametrize("hostloop", [False, True])
+@pytest.mark.parametrize("long_frac", [0.0, 0.1])
+def test_indicator_plain_path_matches_oracle(gpu_prop, oracle_mod, long_frac, hostloop):
+    """Plain path, residual rule: the root and each node alone (seeded, global domain = root bounds)."""
+    inst = _indicator(long_frac)
+    orc = oracle_mod.Oracle(inst)
+    par = oracle_mod.params(0.0)
+    p = _params(0.0)
+    p.flags = gbp.GBP_FLAG_HOSTLOOP if hostloop else 0
+    gpu_prop.set_params(p)
+    gpu_prop.upload(inst)
+    lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
+    olb, oub, ores = orc.propagate(inst.lb, inst.ub, par)
+    assert cut == bool(ores.cutoff) and np.array_equal(lb, olb) and np.array_equal(ub, oub)
+    nodes = instances.node_batch(inst, olb, oub, 60, seed=6)
+    gpu_prop.set_global_bounds(olb, oub)
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        cols = nodes.col[sl]
+        nlb, nub = olb.copy(), oub.copy()
+        old_l, old_u = nlb[cols].copy(), nub[cols].copy()
+        nlb[cols] = np.maximum(old_l, nodes.lb[sl])
+        nub[cols] = np.minimum(old_u, nodes.ub[sl])
+        glb, gub, gcut, _ = gpu_prop.propagate(nlb, nub, seed=(cols, old_l, old_u))
+        elb, eub, er = orc.propagate(nlb, nub, par, seed=(cols, old_l, old_u), glob=(olb, oub))
+        assert gcut == bool(er.cutoff)
+        if not gcut:
+            assert np.array_equal(glb, elb) and np.array_equal(gub, eub), f"node {k}"
+    gpu_prop.set_global_bounds(None)
+    gpu_prop.set_params(_params(0.0))
+
+
+def test_binary_test_reads_the_global_domain(gpu_prop, oracle_mod):
+    """x0 + x1 + x2 - y <= 1 with x0 = x1 = 1: y rises to 1 unless the unfixed x2 counts as binary (global
+    domain inside [0,1]) and, coming first, ends the visit of the binaries."""
+    rowptr = np.array([0, 4], dtype=np.int64)
+    inst = instances.Instance(rowptr, np.array([0, 1, 2, 3], np.int32), np.array([1.0, 1.0, 1.0, -1.0]),
+                              np.array([-instances.INF]), np.array([1.0]), np.array([1.0, 1.0, 0.0, 0.0]),
+                              np.ones(4), np.ones(4, dtype=np.int8))
+    gpu_prop.set_params(_params(0.0))
+    gpu_prop.upload(inst)
+    lb, ub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
+    assert lb[3] == 0.0
+    gpu_prop.set_global_bounds(np.zeros(4), np.array([1.0, 1.0, 3.0, 1.0]))
+    lb, ub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
+    assert lb[3] == 1.0
+    gpu_prop.set_global_bounds(None)
+    lb, ub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
+    assert lb[3] == 0.0
