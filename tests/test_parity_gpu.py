@@ -193,10 +193,11 @@ def test_indicator_nodes_match_oracle(gpu_prop, oracle_mod, maxeasy, long_frac, 
     nodes = instances.node_batch(inst, rlb, rub, 1024, seed=4)
     gpu_prop.set_params(gbp.default_params(maxeasy=maxeasy, sortvars=sortvars))
     gpu_prop.upload(inst)
+    o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+    cap = int(o["n"].sum()) + 1024  # packed output: every changed column of every node
     for threads in (32, 128, 256):
         gpu_prop.set_batch_shape(threads, 0)
-        r = gpu_prop.propagate_nodes(rlb, rub, nodes)
-        o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+        r = gpu_prop.propagate_nodes(rlb, rub, nodes, out_cap=cap)
         _nodes_equal(r, o, nodes.nnodes)
     gpu_prop.set_batch_shape(128, 0)
     gpu_prop.set_params(_params(maxeasy))
