@@ -489,28 +489,28 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
         if ((ibmin & 0x7fffffffffffffffLL) >= infb) {
           if (vpos == (ibmin >= 0)) ++a.minposinf; else ++a.minneginf;
           so.minspec = pos;
-        } else {
+        } else if ((ibmin & 0x7fffffffffffffffLL) != 0) {  // a zero bound contributes a zero: nothing to add
           const double c = v * bmin;
           const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
           if (ca >= hugeb) {
             if (cb >= 0) ++a.minposhuge; else ++a.minneghuge;
             so.minspec = pos;
           } else if (ca != 0) {
-            sum21(a.minhi, a.minlo, c);
+            sum21f(a.minhi, a.minlo, c);
           }
           if (ca > so.maxabs) so.maxabs = ca;
         }
         if ((ibmax & 0x7fffffffffffffffLL) >= infb) {
           if (vpos == (ibmax >= 0)) ++a.maxposinf; else ++a.maxneginf;
           so.maxspec = pos;
-        } else {
+        } else if ((ibmax & 0x7fffffffffffffffLL) != 0) {
           const double c = v * bmax;
           const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
           if (ca >= hugeb) {
             if (cb >= 0) ++a.maxposhuge; else ++a.maxneghuge;
             so.maxspec = pos;
           } else if (ca != 0) {
-            sum21(a.maxhi, a.maxlo, c);
+            sum21f(a.maxhi, a.maxlo, c);
           }
           if (ca > so.maxabs) so.maxabs = ca;
         }
@@ -518,7 +518,9 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
         const long long il = __double_as_longlong(l), iu = __double_as_longlong(u);
         const bool linf = il < 0 && (il & 0x7fffffffffffffffLL) >= infb;   // -l >= inf
         const bool uinf = iu >= 0 && iu >= infb;                            // u >= inf
-        const long long d = (linf || uinf) ? 0x7ff0000000000000LL : __double_as_longlong(fabs(v) * (u - l));
+        // u - (+0) is u bit for bit, so a lower bound of +0 needs no subtraction
+        const double width = il == 0 ? u : u - l;
+        const long long d = (linf || uinf) ? 0x7ff0000000000000LL : __double_as_longlong(fabs(v) * width);
         if (d > mad) mad = d;
         // keep the TOPK largest deltas (ties keep the earlier entry)
         if (d > so.topd[TOPK - 1]) {

@@ -82,6 +82,21 @@ __host__ __device__ __forceinline__ void sum21(double& hi, double& lo, double b)
   hi = s;
 }
 
+// The same accumulation for a nonzero summand b added to a high word that is not -0 (every per-entry
+// contribution and every partial merge): the rounding error of hi + b is computed with Dekker's Fast2Sum
+// after ordering the operands by magnitude, compared as integer bit patterns off the FP64 pipe.  Fast2Sum
+// and TwoSum both return the exact rounding error (an exact zero as +0 in both), so (hi, lo) is bit for bit
+// what sum21 gives, with 4 FP64 operations instead of 7.
+__device__ __forceinline__ void sum21f(double& hi, double& lo, double b) {
+  const double s = hi + b;
+  const bool hbig = (__double_as_longlong(hi) & 0x7fffffffffffffffLL) >= (__double_as_longlong(b) & 0x7fffffffffffffffLL);
+  const double x = hbig ? hi : b;
+  const double y = hbig ? b : hi;
+  const double err = y - (s - x);
+  lo = err + lo;
+  hi = s;
+}
+
 // Order-preserving int64 key of a double, for atomicMin / atomicMax on candidate bounds.
 __device__ __forceinline__ long long dkey(double x) {
   long long i = __double_as_longlong(x);
@@ -115,7 +130,7 @@ __device__ __forceinline__ void addContribution(const Num& s, double val, double
     if (isHuge(s, fabs(c))) {
       if (c > 0.0) ++poshuge; else ++neghuge;
     } else if (c != 0.0) {
-      sum21(hi, lo, c);
+      sum21f(hi, lo, c);
     }
   }
 }
@@ -130,9 +145,9 @@ __device__ __forceinline__ void addTerm(const Num& s, Act& a, double val, double
 // Combination of two partial activities (lane partials of long rows): b's high word enters through the
 // compensated sum, its low word is added to the low word.
 __device__ __forceinline__ void actMerge(Act& a, const Act& b) {
-  sum21(a.minhi, a.minlo, b.minhi);
+  sum21f(a.minhi, a.minlo, b.minhi);
   a.minlo = a.minlo + b.minlo;
-  sum21(a.maxhi, a.maxlo, b.maxhi);
+  sum21f(a.maxhi, a.maxlo, b.maxhi);
   a.maxlo = a.maxlo + b.maxlo;
   a.minposinf += b.minposinf; a.minneginf += b.minneginf; a.minposhuge += b.minposhuge; a.minneghuge += b.minneghuge;
   a.maxposinf += b.maxposinf; a.maxneginf += b.maxneginf; a.maxposhuge += b.maxposhuge; a.maxneghuge += b.maxneghuge;
