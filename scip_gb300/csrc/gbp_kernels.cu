@@ -26,6 +26,15 @@ struct PlainBnd {
   }
 };
 
+// A node's changed columns are also kept in a small open-addressing table in shared memory, so that the
+// bound lookup of every row entry costs a shared-memory probe plus a read of the (L2-resident) base bounds
+// instead of a read of the per-CTA global stamp array.  A node that changes more than OVL_HASH_MAX columns
+// switches to the global overlay, which is always maintained.
+constexpr int OVL_HASH = 512;
+constexpr int OVL_HASH_MAX = OVL_HASH / 2;
+__device__ __forceinline__ unsigned ovlSlot(int j) { return ((unsigned)j * 2654435761u) >> (32 - 9); }
+static_assert((1 << 9) == OVL_HASH, "ovlSlot hashes to 9 bits");
+
 // node bounds: the per-CTA overlay where this node changed a column, else the shared base (packed pairs,
 // or two separate arrays when `base` is null)
 struct OvlBnd {
@@ -35,11 +44,33 @@ struct OvlBnd {
   double2* ovl;
   int* ostamp;
   int epoch;
+  int* hkey;      // shared table: column or -1
+  double2* hval;  // its bounds
+  int* hstate;    // [0] entries, [1] nonzero once the node uses the global overlay only
   __device__ __forceinline__ double2 getBase(int j) const {
     return base != nullptr ? base[j] : make_double2(baselb[j], baseub[j]);
   }
   __device__ __forceinline__ void get(int j, double& l, double& u) const {
-    double2 b = (ostamp[j] == epoch) ? ovl[j] : getBase(j);
+    double2 b;
+    bool found = false;
+    if (hstate[1] == 0) {
+      unsigned h = ovlSlot(j);
+      for (int t = 0; t < OVL_HASH; ++t) {
+        const int k = hkey[h];
+        if (k == j) {
+          b = hval[h];
+          found = true;
+          break;
+        }
+        if (k < 0) {
+          b = getBase(j);
+          found = true;
+          break;
+        }
+        h = (h + 1) & (OVL_HASH - 1);
+      }
+    }
+    if (!found) b = (ostamp[j] == epoch) ? ovl[j] : getBase(j);
     l = b.x;
     u = b.y;
   }
@@ -325,12 +356,26 @@ __global__ void k_csc_flags(int64_t nnz, const double* cvals, const int32_t* row
 }
 
 // ------------------------------------------------------------------------------------------ batched path
+// Column j of the node gets bounds [l,u].  Only the thread that owns j in the current phase reads or writes
+// j's entry, so the table needs atomics only to claim free slots.
 __device__ __forceinline__ void ovlSet(const OvlBnd& B, int* dirty, int* ndirty, int j, double l, double u) {
   if (B.ostamp[j] != B.epoch) {
     B.ostamp[j] = B.epoch;
     dirty[atomicAdd(ndirty, 1)] = j;
   }
   B.ovl[j] = make_double2(l, u);
+  if (B.hstate[1] != 0) return;
+  unsigned h = ovlSlot(j);
+  for (int t = 0; t < OVL_HASH; ++t) {
+    const int k = atomicCAS(&B.hkey[h], -1, j);
+    if (k == -1 || k == j) {
+      B.hval[h] = make_double2(l, u);
+      if (k == -1 && atomicAdd(&B.hstate[0], 1) + 1 > OVL_HASH_MAX) atomicExch(&B.hstate[1], 1);
+      return;
+    }
+    h = (h + 1) & (OVL_HASH - 1);
+  }
+  atomicExch(&B.hstate[1], 1);
 }
 
 template <int NT, int MINB>
@@ -339,6 +384,9 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
   __shared__ int s_item, s_cut, s_ns[2], s_nl[2], s_ntouched, s_ndirty, s_nout, s_rounds, s_epoch, s_rstamp;
   __shared__ long long s_off;
   __shared__ unsigned long long s_changes;
+  __shared__ int s_hkey[OVL_HASH];
+  __shared__ double2 s_hval[OVL_HASH];
+  __shared__ int s_hstate[2];
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -369,7 +417,10 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
   unsigned long long mycut = 0, mymaxr = 0;
 
   for (;;) {
+    for (int t = tid; t < OVL_HASH; t += NT) s_hkey[t] = -1;
     if (tid == 0) {
+      s_hstate[0] = 0;
+      s_hstate[1] = 0;
       s_item = atomicAdd(A.next_item, 1);
       s_epoch = ++counter;
       s_cut = 0;
@@ -382,7 +433,7 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
     __syncthreads();
     const int item = s_item;
     if (item >= A.nnodes) break;
-    OvlBnd B{A.base, A.baselb, A.baseub, ovl, ostamp, s_epoch};
+    OvlBnd B{A.base, A.baselb, A.baseub, ovl, ostamp, s_epoch, s_hkey, s_hval, s_hstate};
 
     // branching bound changes of the node, then the rows they make relevant
     {
