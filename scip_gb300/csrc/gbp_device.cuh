@@ -223,8 +223,24 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
   double minres, maxres;
   bool mintight, maxtight, mininf, maxinf;
   residuals(s, a, val, l, u, minres, maxres, mintight, maxtight, mininf, maxinf);
-  bool rhsok = !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !eq(s, minres / rhs, 1.0));
-  bool lhsok = !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !eq(s, maxres / lhs, 1.0));
+  bool rhsok = !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !quotNear1(minres, rhs, s.eps));
+  bool lhsok = !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !quotNear1(maxres, lhs, s.eps));
+  // Every acceptance test of a new upper bound (forced LT, integral FeasLT, UbBetter) needs newub < u, and of a
+  // new lower bound newlb > l.  A side whose exact quotient misses that by more than the rounding of the
+  // product bound*val is skipped before its division (the quotient would round to the same side of the
+  // bound); the reliable recomputation is only reached when these tests pass, so nothing else changes.
+  auto beyond = [](double num, double bv) {  // num > bound*val, decided with margin: +1, -1, or 0 if unsure
+    const double m = fabs(bv) * 0x1p-40 + 1e-290;
+    return num > bv + m ? 1 : (num < bv - m ? -1 : 0);
+  };
+  if (rhsok) {
+    const int c = beyond(rhs - minres, (val > 0.0 ? u : l) * val);
+    if (c > 0) rhsok = false;  // a > 0: newub >= u; a < 0: newlb <= l
+  }
+  if (lhsok) {
+    const int c = beyond(lhs - maxres, (val > 0.0 ? l : u) * val);
+    if (c < 0) lhsok = false;  // a > 0: newlb <= l; a < 0: newub >= u
+  }
   if (val > 0.0) {
     if (rhsok) {
       double newub = (rhs - minres) / val;

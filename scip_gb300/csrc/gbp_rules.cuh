@@ -33,9 +33,52 @@ __host__ __device__ __forceinline__ double relDiff(double a, double b) {
   if (1.0 > q) q = 1.0;
   return (a - b) / q;
 }
-__host__ __device__ __forceinline__ bool feasLt(const Num& s, double a, double b) { return relDiff(a, b) < -s.feastol; }
-__host__ __device__ __forceinline__ bool feasGt(const Num& s, double a, double b) { return relDiff(a, b) > s.feastol; }
-__host__ __device__ __forceinline__ bool feasEq(const Num& s, double a, double b) { return fabs(relDiff(a, b)) <= s.feastol; }
+
+// Tests of a rounded quotient against a threshold, decided like the division itself but mostly without it
+// (a double division is a long FP64 instruction sequence on this part).  For q > 0, fl(d/q) < t holds when
+// the exact d/q < t by more than the rounding of fl(d/q), and fails when the exact d/q >= t (rounding is
+// monotone and t is a double).  Comparing d with the rounded product t*q decides both cases whenever d lies
+// outside a band of 2^-40 (relative) around t*q -- far wider than the product's own rounding (2^-53) --
+// and the division decides inside the band.  The 1e-290 floor covers a zero or subnormal product; callers
+// keep d/q away from the subnormal range (q <= 1e30, |d| above 1e-290 outside the band).
+__host__ __device__ __forceinline__ bool quotLt(double d, double q, double t) {
+  const double tq = t * q;
+  const double m = fabs(tq) * 0x1p-40 + 1e-290;
+  if (d < tq - m) return true;
+  if (d > tq + m) return false;
+  return d / q < t;
+}
+__host__ __device__ __forceinline__ bool quotGt(double d, double q, double t) {
+  const double tq = t * q;
+  const double m = fabs(tq) * 0x1p-40 + 1e-290;
+  if (d > tq + m) return true;
+  if (d < tq - m) return false;
+  return d / q > t;
+}
+// the denominator of SCIPrelDiff
+__host__ __device__ __forceinline__ double relDen(double a, double b) {
+  double q = fabs(a);
+  if (fabs(b) > q) q = fabs(b);
+  if (1.0 > q) q = 1.0;
+  return q;
+}
+// SCIPisFeasLT / SCIPisFeasGT / SCIPisFeasEQ (set.c:7025-7050): relDiff(a, b) against -feastol / feastol
+__host__ __device__ __forceinline__ bool feasLt(const Num& s, double a, double b) { return quotLt(a - b, relDen(a, b), -s.feastol); }
+__host__ __device__ __forceinline__ bool feasGt(const Num& s, double a, double b) { return quotGt(a - b, relDen(a, b), s.feastol); }
+__host__ __device__ __forceinline__ bool feasEq(const Num& s, double a, double b) {
+  const double d = a - b, q = relDen(a, b);
+  return !quotGt(d, q, s.feastol) && !quotLt(d, q, -s.feastol);
+}
+// EPSEQ(num / den, 1.0, eps) for |den| >= 1 - eps, the residual guard of tightenVarBounds
+// (cons_linear.c:6766): |fl(num/den) - 1| is within 2^-52 of |num - den| / |den|, so a difference clearly
+// above or below eps * |den| decides it; the division decides the rest.
+__host__ __device__ __forceinline__ bool quotNear1(double num, double den, double eps) {
+  if (eps < 1e-12) return fabs(num / den - 1.0) <= eps;  // the margins below need eps >> 2^-52
+  const double diff = fabs(num - den), scale = eps * fabs(den);
+  if (diff > 2.0 * scale) return false;
+  if (diff < 0.5 * scale) return true;
+  return fabs(num / den - 1.0) <= eps;
+}
 __host__ __device__ __forceinline__ double feasFloor(const Num& s, double x) { return floor(x + s.feastol); }
 __host__ __device__ __forceinline__ double feasCeil(const Num& s, double x) { return ceil(x - s.feastol); }
 __host__ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
@@ -53,7 +96,7 @@ __host__ __device__ __forceinline__ bool ubBetter(const Num& s, double nu, doubl
 
 // SCIPsetIsUpdateUnreliable, set.c:8032-8046
 __host__ __device__ __forceinline__ bool updateUnreliable(const Num& s, double nv, double ov) {
-  return fabs(ov) / dmax(fabs(nv), s.eps) >= s.recomp;
+  return !quotLt(fabs(ov), dmax(fabs(nv), s.eps), s.recomp);  // fabs(ov) / max(|nv|, eps) >= recompfac
 }
 
 // adjustedLb / adjustedUb, var.c:1957-2020 (integral columns are rounded within feastol)
