@@ -463,7 +463,7 @@ def main():
             "config": config,
             "e2e": {"value": e2e_v, "unit": "node-fixpoints/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": int(sum(st["launches"] for st in stats)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_step": algo, "kernel": "k_nodes"},

@@ -77,6 +77,9 @@ struct gbp_ctx {
   void* slot_mem = nullptr;
   int64_t slot_stamp_budget = 0;
   double2* d_base = nullptr;
+  int* d_order = nullptr;     // node order of the queue (capacity order_cap) and its counting-sort buckets
+  int* d_orderhist = nullptr;
+  int64_t order_cap = 0;
   int* d_next_item = nullptr;
   int* d_status = nullptr;
   unsigned long long* d_out_used = nullptr;
@@ -236,6 +239,7 @@ int gbp_create(gbp_ctx** out, int device, void* stream) {
       cudaMalloc(&ctx->d_ctr, 8 * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->d_stats, 8 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&ctx->d_next_item, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_orderhist, 2 * ORDER_BUCKETS * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->d_status, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->d_out_used, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&ctx->h_ctr, 16 * sizeof(int)) != cudaSuccess ||
@@ -258,6 +262,8 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->d_ctr) cudaFree(ctx->d_ctr);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   if (ctx->d_next_item) cudaFree(ctx->d_next_item);
+  if (ctx->d_orderhist) cudaFree(ctx->d_orderhist);
+  if (ctx->d_order) cudaFree(ctx->d_order);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_out_used) cudaFree(ctx->d_out_used);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
@@ -949,7 +955,18 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   CK(cudaMemsetAsync(ctx->d_next_item, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_out_used, 0, sizeof(unsigned long long), ctx->stream));
+  if (nnodes > ctx->order_cap) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_order) cudaFree(ctx->d_order);
+    ctx->d_order = nullptr;
+    ctx->order_cap = 0;
+    const int64_t cap = std::max<int64_t>(nnodes, 4096);
+    CK(cudaMalloc(&ctx->d_order, cap * sizeof(int)));
+    ctx->order_cap = cap;
+  }
+  CK(cudaMemsetAsync(ctx->d_orderhist, 0, 2 * ORDER_BUCKETS * sizeof(int), ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launchNodeOrder(ctx->stream, gridFor(ctx, nnodes, 256, 2), nnodes, ptr, ctx->d_orderhist, ctx->d_order));
   CK(launchPack(ctx->stream, gridFor(ctx, ctx->n), baselb, baseub, ctx->d_base, ctx->n));
   NodesArgs A;
   A.s = ctx->num;
@@ -973,6 +990,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   A.out_used = ctx->d_out_used;
   A.maxrounds = maxrounds;
   A.next_item = ctx->d_next_item;
+  A.order = ctx->d_order;
   A.S = ctx->slots;
   A.stats = ctx->d_stats;
   A.status = ctx->d_status;
@@ -992,7 +1010,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
     res->cutoff = (int32_t)st[4];
     res->rounds = (int32_t)st[5];
     res->status = (status & 1) ? 2 : 0;
-    res->launches = 2;
+    res->launches = 4;  // order (2), pack, nodes
     res->rows = (int64_t)st[0];
     res->nnz = (int64_t)st[1];
     res->candidates = (int64_t)st[2];

@@ -502,41 +502,56 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
         const bool vpos = __double_as_longlong(v) >= 0;
         const double bmin = vpos ? l : u, bmax = vpos ? u : l;
         const long long ibmin = __double_as_longlong(bmin), ibmax = __double_as_longlong(bmax);
-        if ((ibmin & 0x7fffffffffffffffLL) >= infb) {
+        const bool minInf = (ibmin & 0x7fffffffffffffffLL) >= infb, maxInf = (ibmax & 0x7fffffffffffffffLL) >= infb;
+        if (minInf) {
           if (vpos == (ibmin >= 0)) ++a.minposinf; else ++a.minneginf;
           so.minspec = pos;
-        } else if ((ibmin & 0x7fffffffffffffffLL) != 0) {  // a zero bound contributes a zero: nothing to add
-          const double c = v * bmin;
-          const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
-          if (ca >= hugeb) {
-            if (cb >= 0) ++a.minposhuge; else ++a.minneghuge;
-            so.minspec = pos;
-          } else if (ca != 0) {
-            sum21f(a.minhi, a.minlo, c);
-          }
-          if (ca > so.maxabs) so.maxabs = ca;
         }
-        if ((ibmax & 0x7fffffffffffffffLL) >= infb) {
+        if (maxInf) {
           if (vpos == (ibmax >= 0)) ++a.maxposinf; else ++a.maxneginf;
           so.maxspec = pos;
-        } else if ((ibmax & 0x7fffffffffffffffLL) != 0) {
-          const double c = v * bmax;
+        }
+        // a finite contribution v * b enters the side's compensated sum (a zero bound contributes nothing)
+        auto contribute = [&](bool tomax, double c) {
           const long long cb = __double_as_longlong(c), ca = cb & 0x7fffffffffffffffLL;
           if (ca >= hugeb) {
-            if (cb >= 0) ++a.maxposhuge; else ++a.maxneghuge;
-            so.maxspec = pos;
+            if (tomax) {
+              if (cb >= 0) ++a.maxposhuge; else ++a.maxneghuge;
+              so.maxspec = pos;
+            } else {
+              if (cb >= 0) ++a.minposhuge; else ++a.minneghuge;
+              so.minspec = pos;
+            }
           } else if (ca != 0) {
-            sum21f(a.maxhi, a.maxlo, c);
+            double hi = tomax ? a.maxhi : a.minhi, lo = tomax ? a.maxlo : a.minlo;
+            sum21f(hi, lo, c);
+            if (tomax) {
+              a.maxhi = hi;
+              a.maxlo = lo;
+            } else {
+              a.minhi = hi;
+              a.minlo = lo;
+            }
           }
           if (ca > so.maxabs) so.maxabs = ca;
-        }
+        };
+        const bool needMin = !minInf && (ibmin & 0x7fffffffffffffffLL) != 0;
+        const bool needMax = !maxInf && (ibmax & 0x7fffffffffffffffLL) != 0;
+        // Usually one bound is zero or infinite and the entry has a single product; choosing its side per lane
+        // lets the warp issue one multiplication and one compensated sum for all lanes.  Each side still
+        // receives its contributions in row order.
+        if (needMin || needMax) contribute(needMax, v * (needMax ? bmax : bmin));
+        if (needMin && needMax) contribute(false, v * bmin);
         // maximal activity delta of the entry (consdataRecomputeMaxActivityDelta): infinite if a bound is
         const long long il = __double_as_longlong(l), iu = __double_as_longlong(u);
         const bool linf = il < 0 && (il & 0x7fffffffffffffffLL) >= infb;   // -l >= inf
         const bool uinf = iu >= 0 && iu >= infb;                            // u >= inf
-        // u - (+0) is u bit for bit, so a lower bound of +0 needs no subtraction
-        const double width = il == 0 ? u : u - l;
-        const long long d = (linf || uinf) ? 0x7ff0000000000000LL : __double_as_longlong(fabs(v) * width);
+        long long d = 0x7ff0000000000000LL;
+        if (!(linf || uinf)) {
+          double width = u;  // u - (+0) is u bit for bit
+          if (il != 0) width = u - l;
+          d = __double_as_longlong(fabs(v) * width);
+        }
         if (d > mad) mad = d;
         // keep the TOPK largest deltas (ties keep the earlier entry)
         if (d > so.topd[TOPK - 1]) {

@@ -86,12 +86,19 @@ struct NodesArgs {
   unsigned long long* out_used;  // packed result entries allocated so far
   int maxrounds;
   int* next_item;                // work queue head
+  const int* order;              // queue position -> node (longest expected work first), or null: identity
   SlotArrays S;
   unsigned long long* stats;     // rows, nnz, candidates, changes, cutoffs, max rounds
   int* status;                   // bit0 round limit, bit1 output overflow
   int minblocks;                 // register-budget variant of the kernel (1 = unconstrained)
 };
 
+
+// Node order for the queue: more branching changes first (a node's work grows with its changes), so that the
+// longest nodes start early and the batch does not end waiting for one of them.  Counting sort on the change
+// count (clamped to 255) in two launches; hist holds 2 * ORDER_BUCKETS zeroed ints (counts, cursors).
+constexpr int ORDER_BUCKETS = 256;
+cudaError_t launchNodeOrder(cudaStream_t st, int grid, int64_t nnodes, const int64_t* ptr, int* hist, int* order);
 
 // launchers (return the cudaError_t of the launch)
 cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,

@@ -421,7 +421,8 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
     if (tid == 0) {
       s_hstate[0] = 0;
       s_hstate[1] = 0;
-      s_item = atomicAdd(A.next_item, 1);
+      const int q = atomicAdd(A.next_item, 1);
+      s_item = (q < A.nnodes && A.order != nullptr) ? A.order[q] : q;
       s_epoch = ++counter;
       s_cut = 0;
       s_ns[0] = s_nl[0] = s_ns[1] = s_nl[1] = 0;
@@ -559,7 +560,44 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
   flushStats(A.stats, st);
 }
 
+// ------------------------------------------------------------------------------------------ node order
+__device__ __forceinline__ int orderBucket(const int64_t* ptr, int64_t k) {
+  const int64_t c = ptr[k + 1] - ptr[k];
+  return ORDER_BUCKETS - 1 - (int)(c < ORDER_BUCKETS - 1 ? c : ORDER_BUCKETS - 1);  // bucket 0: most changes
+}
+__global__ void __launch_bounds__(256) k_order_hist(int64_t nnodes, const int64_t* ptr, int* hist) {
+  __shared__ int h[ORDER_BUCKETS];
+  for (int b = threadIdx.x; b < ORDER_BUCKETS; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnodes; k += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[orderBucket(ptr, k)], 1);
+  __syncthreads();
+  for (int b = threadIdx.x; b < ORDER_BUCKETS; b += blockDim.x)
+    if (h[b]) atomicAdd(&hist[b], h[b]);
+}
+__global__ void __launch_bounds__(256) k_order_scatter(int64_t nnodes, const int64_t* ptr, const int* hist,
+                                                       int* cursor, int* order) {
+  __shared__ int start[ORDER_BUCKETS];
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < ORDER_BUCKETS; ++b) {
+      start[b] = acc;
+      acc += hist[b];
+    }
+  }
+  __syncthreads();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnodes; k += (int64_t)gridDim.x * blockDim.x) {
+    const int b = orderBucket(ptr, k);
+    order[start[b] + atomicAdd(&cursor[b], 1)] = (int)k;
+  }
+}
+
 // ------------------------------------------------------------------------------------------ launchers
+cudaError_t launchNodeOrder(cudaStream_t st, int grid, int64_t nnodes, const int64_t* ptr, int* hist, int* order) {
+  k_order_hist<<<grid, 256, 0, st>>>(nnodes, ptr, hist);
+  k_order_scatter<<<grid, 256, 0, st>>>(nnodes, ptr, hist, hist + ORDER_BUCKETS, order);
+  return cudaGetLastError();
+}
 cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
                             const double* ub, const int* list, const int* nshort, Cands C, int* cutoff,
                             unsigned long long* stats) {

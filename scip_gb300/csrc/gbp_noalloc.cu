@@ -106,8 +106,12 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   char* base = (char*)scratch;
   Header* hdr = (Header*)base;
   SlotArrays S;
-  slotLayout(ns, ms, nslots, base + kHeaderBytes, &S);
+  const size_t slot_bytes = slotLayout(ns, ms, nslots, base + kHeaderBytes, &S);
   const size_t NS = (size_t)nslots;
+  // the node order of the queue, when it fits behind the slots (else nodes run in index order)
+  const size_t order_off = (kHeaderBytes + slot_bytes + 255) & ~size_t(255);
+  const size_t order_bytes = (2 * ORDER_BUCKETS + (size_t)nnodes) * sizeof(int);
+  int* orderhist = order_off + order_bytes <= GBP_NOALLOC_SCRATCH_BYTES ? (int*)(base + order_off) : nullptr;
 
   // clear what must start at zero (the array keeps the previous call's contents)
   if (cudaMemsetAsync(hdr, 0, sizeof(Header), st) != cudaSuccess ||
@@ -117,6 +121,11 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
       cudaMemsetAsync(S.counter, 0, NS * sizeof(int), st) != cudaSuccess)
     return GBP_ERR_CUDA;
   const int fillgrid = sms * 4;
+  if (orderhist != nullptr) {
+    if (cudaMemsetAsync(orderhist, 0, 2 * ORDER_BUCKETS * sizeof(int), st) != cudaSuccess ||
+        launchNodeOrder(st, sms * 2, nnodes, ptr, orderhist, orderhist + 2 * ORDER_BUCKETS) != cudaSuccess)
+      return GBP_ERR_CUDA;
+  }
   if (launchFill64(st, fillgrid, S.cub, (int64_t)(NS * ns), KEY_NONE_UB) != cudaSuccess ||
       launchFill64(st, fillgrid, S.clb, (int64_t)(NS * ns), KEY_NONE_LB) != cudaSuccess ||
       launchFill64(st, fillgrid, S.cubf, (int64_t)(NS * ns), KEY_NONE_UB) != cudaSuccess ||
@@ -149,6 +158,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   A.out_used = &hdr->out_used;
   A.maxrounds = p.maxrounds > 0 ? p.maxrounds : 1000000;
   A.next_item = &hdr->next_item;
+  A.order = orderhist != nullptr ? orderhist + 2 * ORDER_BUCKETS : nullptr;
   A.S = S;
   A.stats = hdr->stats;
   A.status = &hdr->status;
@@ -164,7 +174,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   res->cutoff = (int32_t)h.stats[4];
   res->rounds = (int32_t)h.stats[5];
   res->status = (h.status & 1) ? 2 : 0;
-  res->launches = 6;
+  res->launches = orderhist != nullptr ? 8 : 6;
   res->rows = (int64_t)h.stats[0];
   res->nnz = (int64_t)h.stats[1];
   res->candidates = (int64_t)h.stats[2];
