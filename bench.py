@@ -43,6 +43,22 @@ def measured_peak():
         return HBM_FALLBACK_GBS, "fallback"
 
 
+def measured_traffic(nnodes, shape):
+    """DRAM bytes (read + write) of one k_nodes launch of the default node workload, from the committed one-pass ncu
+    capture (profiles/k_nodes_traffic.json), when this run is that workload; else None."""
+    p = os.path.join(ROOT, "profiles", "k_nodes_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+    except Exception:
+        return None, None
+    if nnodes != NNODES:
+        return None, None
+    src = {"from": "profiles/k_nodes_traffic.json", "launch_shape": d["launch_shape"], "command": d["command"],
+           "this_run_shape": list(shape)}
+    return int(d["dram_bytes_read"]) + int(d["dram_bytes_write"]), src
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples during the timed region."""
 
@@ -423,6 +439,7 @@ def main():
     peak, peak_kind = measured_peak()
     achieved = algo / (ms / 1e3) / 1e9
     cutoffs = stats[-1]["cutoff"]
+    traffic, traffic_src = measured_traffic(N, shape)
 
     # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
@@ -465,7 +482,7 @@ def main():
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(sum(st["launches"] for st in stats)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "peak_kind": peak_kind,
+                         "traffic": traffic, "traffic_source": traffic_src, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_step": algo, "kernel": "k_nodes"},
             "clocks": clk,
             "nnz_per_s": nnz / (ms / 1e3), "kernel_ms": kern_ms, "wall_s": wall,
