@@ -315,8 +315,11 @@ __device__ __forceinline__ int rowTests(const Num& s, const Act& a, double lhs, 
     return 0;
   if (feasZero(s, maxactdelta)) return 0;
   if (!isInf(s, maxactdelta)) {
-    getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, false, minact, t1, f1);
-    getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, false, maxact, t2, f2);
+    // without huge contributions the relaxed (goodrelax) activities above are already the plain ones
+    if (a.minposhuge + a.minneghuge + a.maxposhuge + a.maxneghuge != 0) {
+      getMinAct(s, a, a.minposinf, a.minneginf, a.minposhuge, a.minneghuge, 0.0, false, minact, t1, f1);
+      getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, false, maxact, t2, f2);
+    }
     double slack = (isInf(s, rhs) || f1) ? s.inf : rhs - minact;
     double surplus = (isInf(s, -lhs) || f2) ? s.inf : maxact - lhs;
     if (le(s, maxactdelta, dmin(slack, surplus))) return 0;

@@ -205,7 +205,8 @@ __device__ __forceinline__ void getMinAct(const Num& s, const Act& a, int posinf
   else if (neghuge > 0 || (poshuge > 0 && !goodrelax)) { val = -s.inf; settoinf = true; tight = false; }
   else {
     double hi = a.minhi, lo = a.minlo;
-    sum21(hi, lo, -delta);
+    // subtracting a zero delta leaves (hi, lo) as they are: hi is never -0 and the sum's error is +0
+    if ((__double_as_longlong(delta) & 0x7fffffffffffffffLL) != 0) sum21(hi, lo, -delta);
     if (poshuge > 0) { sum21(hi, lo, poshuge * s.huge); tight = false; }
     else tight = true;
     val = hi + lo;
@@ -220,7 +221,7 @@ __device__ __forceinline__ void getMaxAct(const Num& s, const Act& a, int posinf
   else if (poshuge > 0 || (neghuge > 0 && !goodrelax)) { val = s.inf; settoinf = true; tight = false; }
   else {
     double hi = a.maxhi, lo = a.maxlo;
-    sum21(hi, lo, -delta);
+    if ((__double_as_longlong(delta) & 0x7fffffffffffffffLL) != 0) sum21(hi, lo, -delta);
     if (neghuge > 0) { sum21(hi, lo, -neghuge * s.huge); tight = false; }
     else tight = true;
     val = hi + lo;
