@@ -188,9 +188,11 @@ static void actMerge(Act* a, const Act* b)
 }
 
 /* Activities are summed in a fixed order that does not depend on how the GPU schedules the row: rows of
- * up to LONGROW entries in row order (consdataCalcActivities order), longer rows as 32 interleaved partial
+ * up to LONGROW entries as two halves (entries [0, ceil(len/2)) and the rest), each in row order
+ * (consdataCalcActivities order), the second merged into the first; longer rows as 32 interleaved partial
  * sums (entry p goes to partial (p - rowstart) mod 32, each summed in row order) merged pairwise
- * (partial k absorbs partial k + 16, then k + 8, 4, 2, 1). */
+ * (partial k absorbs partial k + 16, then k + 8, 4, 2, 1).  A merge adds the other partial's high word through
+ * the compensated sum and its low word to the low word. */
 #define LONGROW 64
 static void rowActivity(const Num* s, const lpo_problem* P, const double* lb, const double* ub, int64_t i, Act* a)
 {
@@ -200,11 +202,21 @@ static void rowActivity(const Num* s, const lpo_problem* P, const double* lb, co
    memset(a, 0, sizeof(*a));
    if( p1 - p0 <= LONGROW )
    {
-      for( p = p0; p < p1; ++p )
+      /* two halves, each in row order, the second merged into the first */
+      Act second;
+      int64_t ph = p0 + (p1 - p0 + 1) / 2;
+      memset(&second, 0, sizeof(second));
+      for( p = p0; p < ph; ++p )
       {
          int32_t j = P->colidx[p];
          addTerm(s, a, P->vals[p], lb[j], ub[j]);
       }
+      for( p = ph; p < p1; ++p )
+      {
+         int32_t j = P->colidx[p];
+         addTerm(s, &second, P->vals[p], lb[j], ub[j]);
+      }
+      actMerge(a, &second);
    }
    else
    {

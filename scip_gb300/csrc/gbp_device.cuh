@@ -338,7 +338,8 @@ __device__ __forceinline__ double entryDelta(const Num& s, double val, double l,
 // ------------------------------------------------------------------------------------------------------
 // Short rows (<= LONGROW entries) are processed by a CTA in batches of NT rows:
 //   1. the batch is sorted by row length (so a warp's lanes run loops of similar length),
-//   2. one thread per row sums the activity in row order (the oracle's order) and runs the row tests,
+//   2. two lanes per row (one when the batch has more than NT/2 rows) sum the activity as two halves in row
+//      order (the oracle's order) and run the row tests,
 //   3. each live row selects the few entries that can possibly yield a candidate bound (see selectEntries),
 //   4. the CTA evaluates the selected (row, entry) pairs with all lanes busy -- SCIP's full rule, so the
 //      result is exactly the oracle's.
@@ -363,6 +364,12 @@ struct RowBatch {
   int order[NT];         // batch position -> row, sorted by length
   int hist[LONGROW + 2];
   int bpos[NT];          // first binary in propagation order that gets no candidate (entry position, -1: none)
+  // second-half scan state handed from the odd to the even lane of a pair (its activity goes to act[NT/2 + pair])
+  long long htopd[NT / 2][TOPK];
+  int htopp[NT / 2][TOPK];
+  int hspec[NT / 2][2];
+  long long hmaxabs[NT / 2];
+  long long hmad[NT / 2];
 };
 
 // Load entries [pb, min(pb+CHUNK, p1)) of a row: column indices and values first, then all bound gathers,
@@ -472,16 +479,11 @@ __device__ __forceinline__ int selectEntries(const Num& s, const Act& a, const S
   return n;
 }
 
-// Pass 1 of a short row by one thread: activity in row order, maximal activity delta, row tests, entry
-// selection.  Returns 1 on cutoff, else 0; *nsel/full describe the selected entries of a live row.
-template <class BND>
-__device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B, int i, Act& a, bool& easy,
-                                       unsigned char (&sel)[MAXSEL], int& nsel, bool& full, Stats& st) {
-  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
-  const int len = (int)(p1 - p0);
-  const double lhs = P.lhs[i], rhs = P.rhs[i];
+// Pass 1 of a short row.  Its activity is summed as two halves, entries [p0, ph) and [ph, p1) with
+// ph = p0 + ceil(len/2), each in row order, the second merged into the first (the oracle's order), so that two
+// lanes can scan a row together; one lane scanning both halves gets the same bits.
+__device__ __forceinline__ void scanInit(Act& a, ScanOut& so, long long& mad) {
   actZero(a);
-  ScanOut so;
 #pragma unroll
   for (int k = 0; k < TOPK; ++k) {
     so.topd[k] = -1;
@@ -489,15 +491,22 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
   }
   so.minspec = so.maxspec = 0;
   so.maxabs = 0;
-  long long mad = 0;  // max delta as bits (non-negative doubles order as integers)
+  mad = 0;  // max delta as bits (non-negative doubles order as integers)
+}
+
+// Entries [pb0, pb1) of the row that starts at p0: contributions into a, the largest deltas, the special
+// (infinite/huge) entries and the largest magnitude into so, the maximal delta into mad.
+template <class BND>
+__device__ __forceinline__ void scanEntries(const Num& s, const Prob& P, const BND& B, int64_t p0, int64_t pb0,
+                                            int64_t pb1, Act& a, ScanOut& so, long long& mad) {
   const long long infb = __double_as_longlong(s.inf), hugeb = __double_as_longlong(s.huge);
-  for (int64_t pb = p0; pb < p1; pb += CHUNK) {
+  for (int64_t pb = pb0; pb < pb1; pb += CHUNK) {
     int jj[CHUNK];
     double vv[CHUNK], ll[CHUNK], uu[CHUNK];
-    loadChunk(P, B, pb, p1, jj, vv, ll, uu);
+    loadChunk(P, B, pb, pb1, jj, vv, ll, uu);
 #pragma unroll
     for (int k = 0; k < CHUNK; ++k) {
-      if (pb + k < p1) {
+      if (pb + k < pb1) {
         const double v = vv[k], l = ll[k], u = uu[k];
         const int pos = (int)(pb + k - p0);
         // the two contributions of the entry (addContribution semantics; classification on bit patterns so
@@ -575,15 +584,55 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
       }
     }
   }
-  st.rows += 1;
-  st.nnz += len;
+}
+
+// The second half's results merged into the first's: its entries all come after the first half's, so the
+// largest-delta list takes them after equal deltas of the first half (the sequential scan's tie rule), and its
+// special entries are the later ones.
+__device__ __forceinline__ void scanMerge(Act& a, ScanOut& so, long long& mad, const Act& b, const ScanOut& sb,
+                                          long long madb) {
+  const bool bmin = b.minposinf + b.minneginf + b.minposhuge + b.minneghuge != 0;
+  const bool bmax = b.maxposinf + b.maxneginf + b.maxposhuge + b.maxneghuge != 0;
+  actMerge(a, b);
+  if (bmin) so.minspec = sb.minspec;
+  if (bmax) so.maxspec = sb.maxspec;
+  if (sb.maxabs > so.maxabs) so.maxabs = sb.maxabs;
+  if (madb > mad) mad = madb;
+#pragma unroll
+  for (int r = 0; r < TOPK; ++r) {
+    long long cd = sb.topd[r];
+    int cp = sb.topp[r];
+    if (cp < 0 || !(cd > so.topd[TOPK - 1])) continue;
+#pragma unroll
+    for (int q = 0; q < TOPK; ++q) {
+      if (cd > so.topd[q]) {
+        long long td = so.topd[q];
+        int tp = so.topp[q];
+        so.topd[q] = cd;
+        so.topp[q] = cp;
+        cd = td;
+        cp = tp;
+      }
+    }
+  }
+}
+
+// End of pass 1 once the row's scan is complete: row tests, the slack rule's infeasibility test, entry
+// selection.  Returns 1 on cutoff, else 0; *nsel/full describe the selected entries of a live row.
+__device__ __forceinline__ int finishRow(const Num& s, int len, double lhs, double rhs, const Act& a,
+                                         const ScanOut& so, long long mad, bool& easy, unsigned char (&sel)[MAXSEL],
+                                         int& nsel, bool& full, Stats& st, bool count) {
+  if (count) {
+    st.rows += 1;
+    st.nnz += len;
+  }
   const double maxactdelta = (mad == 0x7ff0000000000000LL) ? s.inf : __longlong_as_double(mad);
   int t = rowTests(s, a, lhs, rhs, maxactdelta, easy);
   nsel = 0;
   full = false;
   if (t == 1) return 1;
   if (t == 0) return 0;
-  st.live += 1;
+  if (count) st.live += 1;
   if (easy) {
     // the slack rule's own infeasibility test (tightenVarBoundsEasy), independent of the entry
     if ((!isInf(s, rhs) && feasLt(s, rhs, a.minhi + a.minlo)) || (!isInf(s, -lhs) && feasLt(s, a.maxhi + a.maxlo, lhs)))
@@ -591,6 +640,27 @@ __device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B
   }
   nsel = selectEntries(s, a, so, lhs, rhs, len, easy, sel, full);
   return 0;
+}
+
+// Pass 1 of a short row by one thread (both halves in turn); the first half's activity waits in *stash.
+template <class BND>
+__device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B, int i, Act& a, bool& easy,
+                                       unsigned char (&sel)[MAXSEL], int& nsel, bool& full, Stats& st, Act* stash) {
+  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+  const int len = (int)(p1 - p0);
+  const int64_t ph = p0 + (len + 1) / 2;
+  ScanOut so;
+  long long mad;
+  scanInit(a, so, mad);
+  scanEntries(s, P, B, p0, p0, ph, a, so, mad);
+  // the second half continues the same list, specials and maxima; only its activity is a separate partial
+  *stash = a;
+  actZero(a);
+  scanEntries(s, P, B, p0, ph, p1, a, so, mad);
+  Act whole = *stash;
+  actMerge(whole, a);
+  a = whole;
+  return finishRow(s, len, P.lhs[i], P.rhs[i], a, so, mad, easy, sel, nsel, full, st, true);
 }
 
 // work item w of a batch belongs to the last batch row o with prefix[o] <= w
@@ -655,24 +725,86 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
 
     int nsel = 0;
     bool full = false;
-    if (tid < cnt && !rowDead(P, rb.order[tid])) {
-      const int i = rb.order[tid];
+    {
+      // Batches of up to NT/2 rows give each row two adjacent lanes, one half each: the odd lane hands its half
+      // to the even lane through shared memory.  Larger batches give each row one lane that scans both halves
+      // in turn, parking the first half's activity in the row's slot.  Either way the even lane (or the single
+      // lane) merges first-then-second and finishes the row; the scan loop has one call site.
+      const bool pairs = cnt <= NT / 2;
+      const int pos = pairs ? (tid >> 1) : tid;
+      const bool second = pairs && (tid & 1) != 0;
+      const bool live = pos < cnt && !rowDead(P, rb.order[pos]);
       Act a;
-      bool easy = false;
-      unsigned char sel[MAXSEL];
-      if (scanRow(s, P, B, i, a, easy, sel, nsel, full, st)) cutRow(P, i, cut);
-      rb.act[tid] = a;
-      rb.lhs[tid] = P.lhs[i];
-      rb.rhs[tid] = P.rhs[i];
-      rb.p0[tid] = P.rowptr[i];
-      rb.len[tid] = (int)(P.rowptr[i + 1] - P.rowptr[i]);
-      rb.easy[tid] = easy ? 1 : 0;
-      rb.full[tid] = full ? 1 : 0;
+      ScanOut so;
+      long long mad;
+      scanInit(a, so, mad);
+      int64_t p0 = 0;
+      int len = 0;
+      if (live) {
+        const int i = rb.order[pos];
+        p0 = P.rowptr[i];
+        len = (int)(P.rowptr[i + 1] - p0);
+        const int64_t ph = p0 + (len + 1) / 2;
+        const int nr = pairs ? 1 : 2;
+#pragma unroll 1
+        for (int r = 0; r < nr; ++r) {
+          const bool h2 = pairs ? second : (r == 1);
+          if (!pairs && r == 1) {
+            rb.act[pos] = a;  // the first half's activity waits in the row's slot
+            actZero(a);
+          }
+          scanEntries(s, P, B, p0, h2 ? ph : p0, h2 ? p0 + len : ph, a, so, mad);
+        }
+        if (!pairs) {
+          Act whole = rb.act[pos];
+          actMerge(whole, a);
+          a = whole;
+        } else if (second) {
+          rb.act[NT / 2 + pos] = a;
 #pragma unroll
-      for (int q = 0; q < MAXSEL; ++q) rb.sel[tid][q] = sel[q];
+          for (int k = 0; k < TOPK; ++k) {
+            rb.htopd[pos][k] = so.topd[k];
+            rb.htopp[pos][k] = so.topp[k];
+          }
+          rb.hspec[pos][0] = so.minspec;
+          rb.hspec[pos][1] = so.maxspec;
+          rb.hmaxabs[pos] = so.maxabs;
+          rb.hmad[pos] = mad;
+        }
+      }
+      __syncwarp();
+      if (live && !second) {
+        const int i = rb.order[pos];
+        if (pairs) {
+          ScanOut sb;
+#pragma unroll
+          for (int k = 0; k < TOPK; ++k) {
+            sb.topd[k] = rb.htopd[pos][k];
+            sb.topp[k] = rb.htopp[pos][k];
+          }
+          sb.minspec = rb.hspec[pos][0];
+          sb.maxspec = rb.hspec[pos][1];
+          sb.maxabs = rb.hmaxabs[pos];
+          scanMerge(a, so, mad, rb.act[NT / 2 + pos], sb, rb.hmad[pos]);
+        }
+        const double lhs = P.lhs[i], rhs = P.rhs[i];
+        bool easy = false;
+        unsigned char sel[MAXSEL];
+        if (finishRow(s, len, lhs, rhs, a, so, mad, easy, sel, nsel, full, st, true)) cutRow(P, i, cut);
+        rb.act[pos] = a;
+        rb.lhs[pos] = lhs;
+        rb.rhs[pos] = rhs;
+        rb.p0[pos] = p0;
+        rb.len[pos] = len;
+        rb.easy[pos] = easy ? 1 : 0;
+        rb.full[pos] = full ? 1 : 0;
+#pragma unroll
+        for (int q = 0; q < MAXSEL; ++q) rb.sel[pos][q] = sel[q];
+      }
+      const int slot = second ? NT / 2 + pos : pos;  // in pairs the odd lanes clear the upper half of the slots
+      rb.nsel[slot] = (live && !second) ? nsel : 0;
+      rb.bpos[slot] = -1;
     }
-    rb.nsel[tid] = nsel;
-    rb.bpos[tid] = -1;
     __syncthreads();
     // exclusive prefix of the selection counts
     if (tid < 32) {

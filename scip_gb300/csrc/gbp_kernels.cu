@@ -228,19 +228,24 @@ __global__ void __launch_bounds__(256) k_activities(Num s, Prob P, PlainBnd B, d
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   // warp per 32 rows for short rows (one lane each), warp per row for long rows -- the summation orders
-  // of rowThread / rowWarp
+  // of the short-row scan and of rowWarp
   for (int64_t base = (int64_t)warp * 32; base < P.m; base += (int64_t)nwarps * 32) {
     int64_t i = base + lane;
     bool mine = i < P.m && (P.rowptr[i + 1] - P.rowptr[i]) <= LONGROW;
     Act a;
     actZero(a);
     if (mine) {
-      for (int64_t p = P.rowptr[i]; p < P.rowptr[i + 1]; ++p) {
+      // two halves in row order, the second merged into the first (the order of the row scan)
+      const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1], ph = p0 + (p1 - p0 + 1) / 2;
+      Act second;
+      actZero(second);
+      for (int64_t p = p0; p < p1; ++p) {
         int j = P.colidx[p];
         double l, u;
         B.get(j, l, u);
-        addTerm(s, a, P.vals[p], l, u);
+        addTerm(s, p < ph ? a : second, P.vals[p], l, u);
       }
+      actMerge(a, second);
     }
     unsigned longmask = __ballot_sync(0xffffffffu, i < P.m && !mine);
     while (longmask) {
