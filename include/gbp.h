@@ -120,6 +120,18 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
  * plugin passes SCIPvarGetLbGlobal/SCIPvarGetUbGlobal.  Batched nodes use their base bounds. */
 int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub);
 
+/* change log of the plain path, for conflict analysis.  With a capacity > 0, every later gbp_propagate /
+ * gbp_propagate_device / gbp_propagate_instances call records each accepted bound change: the column, the round
+ * that made it, and the column's bounds after it (a column that moves in several rounds appears once per round).
+ * Each change follows from the bounds at the start of its round, so applying the log round by round through
+ * SCIPinferVarLbProp / SCIPinferVarUbProp lets SCIP explain every change from bounds it already holds (the
+ * propagator's resolve callback, type_prop.h:258, as cons_linear's resolvePropagation does, cons_linear.c:5097).
+ * Capacity 0 switches the log off. */
+int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity);
+/* the last call's log sorted by (round, column): up to cap entries into col/round/lb/ub (host arrays), *n = the
+ * number of changes the call made.  GBP_ERR_OVERFLOW if the log capacity or cap was smaller than *n. */
+int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, double* lb, double* ub, int64_t* n);
+
 /* ---------------------------------------------------------------- batched path: distinct instances
  * Uneven independent instances (each a set of linear rows with its own columns) propagated together: instance k
  * owns rows [row_off[k], row_off[k+1]) and columns [col_off[k], col_off[k+1]) of one block-diagonal problem whose

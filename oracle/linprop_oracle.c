@@ -426,6 +426,7 @@ typedef struct
    double* rub;
    double* rlb;
    uint8_t* rflag;      /* bit0 ub, bit1 forced ub, bit2 lb, bit3 forced lb */
+   lpo_log* log;        /* change log, or NULL */
 } Work;
 
 static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
@@ -975,6 +976,18 @@ static int fixpoint(Work* w, double* lb, double* ub, lpo_result* res, int track)
             if( track )
                markDirty(w, j, l0, u0);
             res->changes += lbup + ubdown;
+            if( w->log != NULL )
+            {
+               lpo_log* g = w->log;
+               if( g->n < g->cap )
+               {
+                  g->col[g->n] = j;
+                  g->round[g->n] = round;
+                  g->lb[g->n] = lb[j];
+                  g->ub[g->n] = ub[j];
+               }
+               g->n++;
+            }
             expandColumn(w, j, lbup, ubdown);
          }
       }
@@ -986,6 +999,13 @@ int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, do
    int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
    const double* gub, lpo_result* res)
 {
+   return lpo_propagate_logged(prob, par, lb, ub, nseed, seedcols, oldlb, oldub, glb, gub, res, NULL);
+}
+
+int lpo_propagate_logged(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
+   const double* gub, lpo_result* res, lpo_log* log)
+{
    Work w;
    int64_t k;
    memset(res, 0, sizeof(*res));
@@ -996,6 +1016,9 @@ int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, do
    }
    w.glb = glb;
    w.gub = gub;
+   w.log = log;
+   if( log != NULL )
+      log->n = 0;
    newStamp(&w);
    w.nnext = 0;
    if( seedcols == NULL )

@@ -82,6 +82,23 @@ int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, do
    int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
    const double* gub, lpo_result* res);
 
+/* change log: every accepted bound change with the round that made it and the column's bounds after it,
+ * entries grouped by round in the order they are accepted; n counts all changes, at most cap are stored */
+typedef struct
+{
+   int64_t cap;
+   int64_t n;
+   int32_t* col;
+   int32_t* round;
+   double* lb;
+   double* ub;
+} lpo_log;
+
+/* lpo_propagate that also fills *log (log may be NULL) */
+int lpo_propagate_logged(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int64_t nseed, const int32_t* seedcols, const double* oldlb, const double* oldub, const double* glb,
+   const double* gub, lpo_result* res, lpo_log* log);
+
 /* batch of nodes sharing base bounds, which are also every node's global domain: node k applies bound
  * changes chg_col/chg_lb/chg_ub[ptr[k]..ptr[k+1]) and propagates; outputs per node the cutoff flag, rounds, and up to cap changed columns
  * (out_col/out_lb/out_ub[k*cap..]) whose final bounds differ from the base; out_n[k] = count (or -1 if

@@ -33,6 +33,10 @@ class Params(ctypes.Structure):
 FLAG_NOSORTVARS = 1
 
 
+class Log(ctypes.Structure):
+    _fields_ = [("cap", ctypes.c_int64), ("n", ctypes.c_int64), ("col", _P), ("round", _P), ("lb", _P), ("ub", _P)]
+
+
 class Problem(ctypes.Structure):
     _fields_ = [("m", ctypes.c_int64), ("n", ctypes.c_int64), ("rowptr", _P), ("colidx", _P), ("vals", _P),
                 ("lhs", _P), ("rhs", _P), ("isint", _P), ("colptr", _P), ("rowidx", _P), ("cvals", _P)]
@@ -64,6 +68,8 @@ def lib():
                                          ctypes.c_int64, _P, _P]
         L.lpo_propagate.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
                                     _P, _P, _P, _P, ctypes.POINTER(Result)]
+        L.lpo_propagate_logged.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64,
+                                           _P, _P, _P, _P, _P, ctypes.POINTER(Result), ctypes.POINTER(Log)]
         L.lpo_propagate_nodes.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64,
                                           _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(Result)]
@@ -134,6 +140,34 @@ class Oracle:
             lib().lpo_propagate(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), len(cols), _ptr(cols),
                                 _ptr(olb), _ptr(oub), _ptr(glb), _ptr(gub), ctypes.byref(res))
         return lb, ub, res
+
+    def propagate_logged(self, lb, ub, par=None, seed=None, glob=None, cap=None):
+        """propagate() plus the change log sorted by (round, column): returns (lb, ub, Result, (col, round, lb, ub))."""
+        par = par or params()
+        lb = np.array(lb, dtype=np.float64)
+        ub = np.array(ub, dtype=np.float64)
+        cap = cap or 8 * self.inst.n + 1024
+        col, rnd = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+        llb, lub = np.zeros(cap), np.zeros(cap)
+        log = Log(cap, 0, _ptr(col), _ptr(rnd), _ptr(llb), _ptr(lub))
+        res = Result()
+        glb = gub = None
+        if glob is not None:
+            glb = np.ascontiguousarray(glob[0], dtype=np.float64)
+            gub = np.ascontiguousarray(glob[1], dtype=np.float64)
+        if seed is None:
+            args = (0, None, None, None)
+        else:
+            cols, olb, oub = (np.ascontiguousarray(x) for x in seed)
+            cols, olb, oub = cols.astype(np.int32), olb.astype(np.float64), oub.astype(np.float64)
+            args = (len(cols), _ptr(cols), _ptr(olb), _ptr(oub))
+        lib().lpo_propagate_logged(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), *args, _ptr(glb),
+                                   _ptr(gub), ctypes.byref(res), ctypes.byref(log))
+        if log.n > cap:
+            raise MemoryError("oracle change log capacity exceeded")
+        n = log.n
+        o = np.lexsort((col[:n], rnd[:n]))
+        return lb, ub, res, (col[:n][o], rnd[:n][o], llb[:n][o], lub[:n][o])
 
     def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1):
         """Node batch; returns dict with cutoff [N], rounds [N], n [N], col/lb/ub [N, cap] and totals."""

@@ -38,6 +38,9 @@ struct gbp_ctx {
   int8_t* d_isint = nullptr;
   int64_t* d_colptr = nullptr;
   uint32_t* d_cscrow = nullptr;
+  // change log of the plain path (gbp_set_change_log): device arrays and the entry counter
+  ChangeLog log{};
+  int64_t log_cap = 0;
   // explicit global bounds of the plain path (gbp_set_global_bounds)
   bool has_global = false;
   double* d_glb = nullptr;
@@ -263,6 +266,11 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   if (ctx->d_next_item) cudaFree(ctx->d_next_item);
   if (ctx->d_orderhist) cudaFree(ctx->d_orderhist);
+  {
+    void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub};
+    for (void* p : lp)
+      if (p) cudaFree(p);
+  }
   if (ctx->d_order) cudaFree(ctx->d_order);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_out_used) cudaFree(ctx->d_out_used);
@@ -507,6 +515,8 @@ static int propagateGraph(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, c
   hs.maxrounds = maxrounds;
   hs.lb = lb;
   hs.ub = ub;
+  hs.log = ctx->log;
+  if (ctx->log.n) CK(cudaMemsetAsync(ctx->log.n, 0, sizeof(int), ctx->stream));
   int seedstamp = 0;
   if (nseed < 0) {
     hs.cur = 2;
@@ -581,6 +591,7 @@ static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed
   int launches = 0;
   CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, 8 * sizeof(int), ctx->stream));
+  if (ctx->log.n) CK(cudaMemsetAsync(ctx->log.n, 0, sizeof(int), ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
 
   int* cur = nullptr;
@@ -634,7 +645,7 @@ static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed
     }
     Front F{nextlist, ctx->d_ctr + nxt, ctx->d_ctr + 2 + nxt, ctx->d_rowstamp, (int)ctx->m};
     CK(launchApply(ctx->stream, gridFor(ctx, ctx->n, 256, 8), s, P, lb, ub, C, F, nextStamp(ctx), ctx->d_ctr + 5,
-                   ctx->d_stats));
+                   ctx->d_stats, ctx->log, rounds));
     ++launches;
     CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -781,6 +792,65 @@ int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub) {
   }
   CK(cudaStreamSynchronize(ctx->stream));  // the host arrays may go away after the call
   ctx->has_global = true;
+  return GBP_OK;
+}
+
+int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity) {
+  if (!ctx || capacity < 0 || capacity >= (int64_t(1) << 31)) return fail(ctx, GBP_ERR_INVALID, "bad log capacity");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub};
+  for (void* p : lp)
+    if (p) cudaFree(p);
+  ctx->log = ChangeLog{};
+  ctx->log_cap = 0;
+  if (capacity == 0) return GBP_OK;
+  ChangeLog G{};
+  G.cap = capacity;
+  CK(cudaMalloc(&G.n, sizeof(int)));
+  CK(cudaMalloc(&G.col, capacity * sizeof(int32_t)));
+  CK(cudaMalloc(&G.round, capacity * sizeof(int32_t)));
+  CK(cudaMalloc(&G.lb, capacity * sizeof(double)));
+  CK(cudaMalloc(&G.ub, capacity * sizeof(double)));
+  CK(cudaMemset(G.n, 0, sizeof(int)));
+  ctx->log = G;
+  ctx->log_cap = capacity;
+  return GBP_OK;
+}
+
+int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, double* lb, double* ub, int64_t* n) {
+  if (!ctx || !n || cap < 0 || (cap > 0 && (!col || !round || !lb || !ub)))
+    return fail(ctx, GBP_ERR_INVALID, "null argument");
+  *n = 0;
+  if (!ctx->log.n) return fail(ctx, GBP_ERR_STATE, "no change log (gbp_set_change_log)");
+  CK(cudaSetDevice(ctx->device));
+  int cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, ctx->log.n, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *n = cnt;
+  const int64_t have = std::min<int64_t>(cnt, ctx->log_cap);
+  std::vector<int32_t> c(have), r(have);
+  std::vector<double> l(have), u(have);
+  if (have > 0) {
+    CK(cudaMemcpyAsync(c.data(), ctx->log.col, have * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(r.data(), ctx->log.round, have * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(l.data(), ctx->log.lb, have * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(u.data(), ctx->log.ub, have * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  // device order within a round depends on scheduling: report by (round, column)
+  std::vector<int64_t> ord(have);
+  for (int64_t k = 0; k < have; ++k) ord[k] = k;
+  std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return r[a] != r[b] ? r[a] < r[b] : c[a] < c[b]; });
+  const int64_t out = std::min<int64_t>(have, cap);
+  for (int64_t k = 0; k < out; ++k) {
+    col[k] = c[ord[k]];
+    round[k] = r[ord[k]];
+    lb[k] = l[ord[k]];
+    ub[k] = u[ord[k]];
+  }
+  if (cnt > ctx->log_cap) return fail(ctx, GBP_ERR_OVERFLOW, "change log capacity exceeded");
+  if (cnt > cap) return fail(ctx, GBP_ERR_OVERFLOW, "output arrays too small for the change log");
   return GBP_OK;
 }
 

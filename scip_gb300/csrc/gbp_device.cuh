@@ -69,6 +69,28 @@ struct Stats {
   long long rows, nnz, cands, live;  // live: rows that passed the skip tests
 };
 
+// Change log of the plain path: every accepted bound change with the round that made it (col null: off).
+// SCIP's conflict analysis needs tightenings in an order where each one's reasons already hold; applying the
+// log round by round gives that order.
+struct ChangeLog {
+  int* n;          // entries written (may exceed cap: the log overflowed)
+  int64_t cap;
+  int32_t* col;
+  int32_t* round;
+  double* lb;      // the column's bounds after the change
+  double* ub;
+};
+__device__ __forceinline__ void logChange(const ChangeLog& G, int j, int round, double l, double u) {
+  if (G.col == nullptr) return;
+  const int k = atomicAdd(G.n, 1);
+  if (k < G.cap) {
+    G.col[k] = j;
+    G.round[k] = round;
+    G.lb[k] = l;
+    G.ub[k] = u;
+  }
+}
+
 // state of the graph-driven fixpoint loop (device memory): which list holds the frontier (0, 1, or 2 = the
 // all-rows list), the lists' sizes, stamps, flags and the bound vectors being propagated
 struct LoopState {
@@ -84,6 +106,7 @@ struct LoopState {
   int status;     // 2: round limit reached
   double* lb;
   double* ub;
+  ChangeLog log;
 };
 struct ListSet {
   int* list[3];

@@ -108,7 +108,7 @@ cudaError_t launchRowsLong(cudaStream_t st, int grid, const Num& s, const Prob& 
                            const double* ub, const int* list, const int* nlong, int cap, Cands C, int* cutoff,
                            unsigned long long* stats);
 cudaError_t launchApply(cudaStream_t st, int grid, const Num& s, const Prob& P, double* lb, double* ub, Cands C,
-                        Front F, int stamp, int* cutoff, unsigned long long* stats);
+                        Front F, int stamp, int* cutoff, unsigned long long* stats, const ChangeLog& G, int round);
 cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* lb, const double* ub, int64_t nseed,
                        const int32_t* cols, const double* oldlb, const double* oldub, Front F, int stamp);
 cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,

@@ -126,7 +126,8 @@ __device__ __forceinline__ void rowsLongBody(const Num& s, const Prob& P, const 
 }
 
 __device__ __forceinline__ void applyBody(const Num& s, const Prob& P, double* lb, double* ub, Cands& C, Front& F,
-                                          int stamp, int* cutoff, unsigned long long* stats) {
+                                          int stamp, int* cutoff, unsigned long long* stats, const ChangeLog& G,
+                                          int round) {
   const int n = *C.ntouched;
   unsigned long long changes = 0;
   bool cut = false;
@@ -147,6 +148,7 @@ __device__ __forceinline__ void applyBody(const Num& s, const Prob& P, double* l
       lb[j] = nl;
       ub[j] = nu;
       changes += (unsigned long long)lbup + (unsigned long long)ubdown;
+      logChange(G, j, round, nl, nu);
       expandColumn(P, F, j, lbup, ubdown, stamp);
     }
   }
@@ -169,8 +171,8 @@ __global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, co
 }
 
 __global__ void __launch_bounds__(256) k_apply(Num s, Prob P, double* lb, double* ub, Cands C, Front F, int stamp,
-                                               int* cutoff, unsigned long long* stats) {
-  applyBody(s, P, lb, ub, C, F, stamp, cutoff, stats);
+                                               int* cutoff, unsigned long long* stats, ChangeLog G, int round) {
+  applyBody(s, P, lb, ub, C, F, stamp, cutoff, stats, G, round);
 }
 
 // ---- graph-driven rounds: the frontier sizes, list parity, stamps and bound pointers live in LoopState
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(256) k_apply_g(Num s, Prob P, Cands C, ListSet
                                                  unsigned long long* stats) {
   const int nxt = S->cur == 1 ? 0 : 1;
   Front F{L.list[nxt], &S->nshort[nxt], &S->nlong[nxt], L.rowstamp, L.cap};
-  applyBody(s, P, S->lb, S->ub, C, F, S->stamp, &S->cutoff, stats);
+  applyBody(s, P, S->lb, S->ub, C, F, S->stamp, &S->cutoff, stats, S->log, S->round);
 }
 
 // end of a round: switch to the list just filled, clear the other one, and tell the graph whether to go on
@@ -616,8 +618,8 @@ cudaError_t launchRowsLong(cudaStream_t st, int grid, const Num& s, const Prob& 
   return cudaGetLastError();
 }
 cudaError_t launchApply(cudaStream_t st, int grid, const Num& s, const Prob& P, double* lb, double* ub, Cands C,
-                        Front F, int stamp, int* cutoff, unsigned long long* stats) {
-  k_apply<<<grid, 256, 0, st>>>(s, P, lb, ub, C, F, stamp, cutoff, stats);
+                        Front F, int stamp, int* cutoff, unsigned long long* stats, const ChangeLog& G, int round) {
+  k_apply<<<grid, 256, 0, st>>>(s, P, lb, ub, C, F, stamp, cutoff, stats, G, round);
   return cudaGetLastError();
 }
 const void* graphKernel(int which) {

@@ -34,7 +34,7 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
-           "gbp_propagate_instances_device", "gbp_set_global_bounds"]
+           "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log"]
 
 
 class GbpParams(ctypes.Structure):
@@ -88,6 +88,8 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_device.argtypes = L.gbp_propagate.argtypes
     L.gbp_row_activities.argtypes = [_P, _P, _P, _P, _P]
     L.gbp_set_global_bounds.argtypes = [_P, _P, _P]
+    L.gbp_set_change_log.argtypes = [_P, ctypes.c_int64]
+    L.gbp_get_change_log.argtypes = [_P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
     L.gbp_propagate_nodes.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
@@ -258,6 +260,24 @@ class Propagator:
         cnt = np.zeros((self.m, 8), dtype=np.int32)
         self._check(self.L.gbp_row_activities(self.h, _ptr(lb), _ptr(ub), _ptr(act), _ptr(cnt)))
         return act, cnt
+
+    def set_change_log(self, capacity: int):
+        """Record every accepted bound change of later plain-path calls (capacity entries; 0: off)."""
+        self._check(self.L.gbp_set_change_log(self.h, int(capacity)))
+
+    def change_log(self, cap: Optional[int] = None):
+        """The last call's change log sorted by (round, column): (col, round, lb, ub) arrays."""
+        n = ctypes.c_int64(0)
+        if cap is None:
+            self._check(self.L.gbp_get_change_log(self.h, 0, None, None, None, None, ctypes.byref(n)),
+                        allow=(GBP_ERR_OVERFLOW,))
+            cap = n.value
+        col = np.zeros(cap, np.int32)
+        rnd = np.zeros(cap, np.int32)
+        lb = np.zeros(cap)
+        ub = np.zeros(cap)
+        self._check(self.L.gbp_get_change_log(self.h, cap, _ptr(col), _ptr(rnd), _ptr(lb), _ptr(ub), ctypes.byref(n)))
+        return col[:n.value], rnd[:n.value], lb[:n.value], ub[:n.value]
 
     def set_global_bounds(self, glb=None, gub=None):
         """Global domain for the binary test of later propagate() calls (None: the propagated bounds, as at the

@@ -1,0 +1,68 @@
+/* Reasons for the bound changes of the gpulinear propagator, for SCIP's conflict analysis.
+ *
+ * The device accepts, per column and round, the best candidate over all rows, so it does not say which row made a
+ * change.  When SCIP asks for the reason of a change (the propagator's resolve callback, type_prop.h:258), this
+ * module finds a row of the column whose other columns' bounds at that time imply the change, and adds the bounds
+ * of that row that cons_linear's addConflictBounds (cons_linear.c:4799-4970) would add for it.
+ *
+ * The module is plain C without SCIP: bounds come in and reason bounds go out through callbacks, so that SCIP's
+ * bound-change history (SCIPgetVarLb/UbAtIndex, SCIPaddConflictLb/Ub) plugs in from the propagator and a test
+ * harness can drive it with arrays. */
+#ifndef GPULINEAR_REASON_H
+#define GPULINEAR_REASON_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* the rows as the propagator uploads them (CSR) and their column view (CSC) */
+typedef struct
+{
+   int64_t m;
+   int64_t n;
+   const int64_t* rowptr;
+   const int32_t* colidx;
+   const double* vals;
+   const double* lhs;
+   const double* rhs;
+   const int8_t* isint;
+   const int64_t* colptr;   /* CSC: rows of column j at rowidx[colptr[j] .. colptr[j+1]) */
+   const int32_t* rowidx;
+   const int64_t* rowpos;   /* position of that entry inside its row's CSR range */
+} gpl_rows;
+
+typedef struct
+{
+   void* ud;
+   double (*lb)(void* ud, int32_t col);    /* local bound when the change was made (before it) */
+   double (*ub)(void* ud, int32_t col);
+   double (*glb)(void* ud, int32_t col);   /* global bound */
+   double (*gub)(void* ud, int32_t col);
+   double (*lbafter)(void* ud, int32_t col);  /* the inferred column's bounds just after the change */
+   double (*ubafter)(void* ud, int32_t col);
+   int (*addlb)(void* ud, int32_t col);    /* add the column's local lower / upper bound to the reason; 0 = ok */
+   int (*addub)(void* ud, int32_t col);
+} gpl_io;
+
+typedef struct
+{
+   double infinity;
+   double feastol;
+   double epsilon;
+} gpl_num;
+
+/* Explains "column col has lower (islower) or upper bound bound" with one row.  Returns the row used (>= 0), -1 if
+ * no row implies the bound (then nothing was added), or -2 if an add callback failed. */
+int64_t gpl_explain(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int32_t col, int islower, double bound);
+
+/* builds colptr/rowidx/rowpos of R from its CSR part; the arrays have n+1, nnz and nnz entries */
+void gpl_build_columns(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx, int64_t* colptr,
+   int32_t* rowidx, int64_t* rowpos);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

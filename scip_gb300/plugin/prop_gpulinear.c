@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include "prop_gpulinear.h"
+#include "gpulinear_reason.h"
 #include "scip/cons_linear.h"
 #include "gbp.h"
 
@@ -43,6 +44,14 @@ struct SCIP_PropData
    double*               glb;                /**< global bounds last passed to the device (binary test) */
    double*               gub;
    SCIP_Bool             haveglobal;
+   int64_t*              colptr;             /**< column view of the rows, for the reasons of conflict analysis */
+   int32_t*              rowidx;
+   int64_t*              rowpos;
+   int64_t               logcap;             /**< change log of the last call: column, round, bounds after */
+   int32_t*              logcol;
+   int32_t*              loground;
+   double*               loglb;
+   double*               logub;
    int32_t*              seeds;
    double*               seedlo;
    double*               seedhi;
@@ -67,6 +76,14 @@ static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIPfreeMemoryArrayNull(scip, &pd->glb);
    SCIPfreeMemoryArrayNull(scip, &pd->gub);
    pd->haveglobal = FALSE;
+   SCIPfreeMemoryArrayNull(scip, &pd->colptr);
+   SCIPfreeMemoryArrayNull(scip, &pd->rowidx);
+   SCIPfreeMemoryArrayNull(scip, &pd->rowpos);
+   SCIPfreeMemoryArrayNull(scip, &pd->logcol);
+   SCIPfreeMemoryArrayNull(scip, &pd->loground);
+   SCIPfreeMemoryArrayNull(scip, &pd->loglb);
+   SCIPfreeMemoryArrayNull(scip, &pd->logub);
+   pd->logcap = 0;
    SCIPfreeMemoryArrayNull(scip, &pd->seeds);
    SCIPfreeMemoryArrayNull(scip, &pd->seedlo);
    SCIPfreeMemoryArrayNull(scip, &pd->seedhi);
@@ -160,6 +177,16 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
       pd->nrows++;
       pd->rowptr[pd->nrows] = p;
    }
+   /* the column view for resolving conflicts, and room for the change log (columns times a few rounds) */
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->colptr, nvars + 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowidx, pd->rowptr[pd->nrows] > 0 ? pd->rowptr[pd->nrows] : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowpos, pd->rowptr[pd->nrows] > 0 ? pd->rowptr[pd->nrows] : 1) );
+   gpl_build_columns(pd->nrows, nvars, pd->rowptr, pd->colidx, pd->colptr, pd->rowidx, pd->rowpos);
+   pd->logcap = 4 * (int64_t)nvars + 4096;
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->logcol, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->loground, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->loglb, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->logub, pd->logcap) );
    return SCIP_OKAY;
 }
 
@@ -203,6 +230,8 @@ static SCIP_RETCODE upload(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_CALL( buildMatrix(scip, pd) );
    SCIP_CALL( setDeviceParams(scip, pd) );
    rc = gbp_upload_problem(pd->ctx, pd->nrows, pd->ncols, pd->rowptr, pd->colidx, pd->vals, pd->lhs, pd->rhs, pd->isint);
+   if( rc == GBP_OK )
+      rc = gbp_set_change_log(pd->ctx, pd->logcap);
    if( rc != GBP_OK )
       disable(scip, pd, "uploading the rows failed", rc);
    pd->havesnap = FALSE;
@@ -361,7 +390,49 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
       return SCIP_OKAY;
    }
 
-   /* the device applied cons_linear's acceptance rules already: force the moves through */
+   /* The device applied cons_linear's acceptance rules already: force the moves through.  The change log hands
+    * them over round by round as inferences of this propagator, so each one's reasons already hold when conflict
+    * analysis asks for them (propRespropGpulinear).  The final loop below then finds nothing left to do, or, when
+    * the log overflowed, moves the final bounds in without reasons. */
+   {
+      int64_t nlog = 0;
+      if( gbp_get_change_log(pd->ctx, pd->logcap, pd->logcol, pd->loground, pd->loglb, pd->logub, &nlog) == GBP_OK )
+      {
+         int64_t k;
+         for( k = 0; k < nlog; ++k )
+         {
+            SCIP_VAR* var = pd->vars[pd->logcol[k]];
+            SCIP_Bool infeasible = FALSE;
+            SCIP_Bool tightened = FALSE;
+            if( pd->logub[k] < SCIPvarGetUbLocal(var) )
+            {
+               SCIP_CALL( SCIPinferVarUbProp(scip, var, pd->logub[k], prop, pd->loground[k], TRUE, &infeasible,
+                     &tightened) );
+               if( infeasible )
+               {
+                  pd->havesnap = FALSE;
+                  *result = SCIP_CUTOFF;
+                  return SCIP_OKAY;
+               }
+               reduced = reduced || tightened;
+               pd->nchgbds += tightened ? 1 : 0;
+            }
+            if( pd->loglb[k] > SCIPvarGetLbLocal(var) )
+            {
+               SCIP_CALL( SCIPinferVarLbProp(scip, var, pd->loglb[k], prop, pd->loground[k], TRUE, &infeasible,
+                     &tightened) );
+               if( infeasible )
+               {
+                  pd->havesnap = FALSE;
+                  *result = SCIP_CUTOFF;
+                  return SCIP_OKAY;
+               }
+               reduced = reduced || tightened;
+               pd->nchgbds += tightened ? 1 : 0;
+            }
+         }
+      }
+   }
    for( j = 0; j < pd->ncols; ++j )
    {
       SCIP_VAR* var = pd->vars[j];
@@ -402,6 +473,96 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    return SCIP_OKAY;
 }
 
+/* SCIP's bound history behind the reason module's callbacks */
+typedef struct
+{
+   SCIP* scip;
+   SCIP_VAR** vars;
+   SCIP_BDCHGIDX* bdchgidx;
+} ReasonCtx;
+
+static double rLb(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPgetVarLbAtIndex(c->scip, c->vars[k], c->bdchgidx, FALSE);
+}
+static double rUb(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPgetVarUbAtIndex(c->scip, c->vars[k], c->bdchgidx, FALSE);
+}
+static double rGlb(void* ud, int32_t k) { return SCIPvarGetLbGlobal(((ReasonCtx*)ud)->vars[k]); }
+static double rGub(void* ud, int32_t k) { return SCIPvarGetUbGlobal(((ReasonCtx*)ud)->vars[k]); }
+static double rLbAfter(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPgetVarLbAtIndex(c->scip, c->vars[k], c->bdchgidx, TRUE);
+}
+static double rUbAfter(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPgetVarUbAtIndex(c->scip, c->vars[k], c->bdchgidx, TRUE);
+}
+static int rAddLb(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPaddConflictLb(c->scip, c->vars[k], c->bdchgidx) == SCIP_OKAY ? 0 : 1;
+}
+static int rAddUb(void* ud, int32_t k)
+{
+   ReasonCtx* c = (ReasonCtx*)ud;
+   return SCIPaddConflictUb(c->scip, c->vars[k], c->bdchgidx) == SCIP_OKAY ? 0 : 1;
+}
+
+/** reason of one of this propagator's bound changes (type_prop.h:258): the bounds of a row that implies it, chosen
+ *  as cons_linear's resolvePropagation / addConflictBounds would for that row (cons_linear.c:5097, :4799) */
+static SCIP_DECL_PROPRESPROP(propRespropGpulinear)
+{
+   SCIP_PROPDATA* pd = SCIPpropGetData(prop);
+   int32_t col = (int32_t)SCIPvarGetProbindex(infervar);
+   ReasonCtx c;
+   gpl_rows R;
+   gpl_num num;
+   gpl_io io;
+   int64_t r;
+
+   *result = SCIP_DIDNOTFIND;
+   if( pd->colptr == NULL || col < 0 || col >= pd->ncols || pd->vars[col] != infervar )
+      return SCIP_OKAY;
+   c.scip = scip;
+   c.vars = pd->vars;
+   c.bdchgidx = bdchgidx;
+   R.m = pd->nrows;
+   R.n = pd->ncols;
+   R.rowptr = pd->rowptr;
+   R.colidx = pd->colidx;
+   R.vals = pd->vals;
+   R.lhs = pd->lhs;
+   R.rhs = pd->rhs;
+   R.isint = pd->isint;
+   R.colptr = pd->colptr;
+   R.rowidx = pd->rowidx;
+   R.rowpos = pd->rowpos;
+   num.infinity = SCIPinfinity(scip);
+   num.feastol = SCIPfeastol(scip);
+   num.epsilon = SCIPepsilon(scip);
+   io.ud = &c;
+   io.lb = rLb;
+   io.ub = rUb;
+   io.glb = rGlb;
+   io.gub = rGub;
+   io.lbafter = rLbAfter;
+   io.ubafter = rUbAfter;
+   io.addlb = rAddLb;
+   io.addub = rAddUb;
+   r = gpl_explain(&R, &num, &io, col, boundtype == SCIP_BOUNDTYPE_LOWER, relaxedbd);
+   if( r == -2 )
+      return SCIP_ERROR;
+   if( r >= 0 )
+      *result = SCIP_SUCCESS;
+   return SCIP_OKAY;
+}
+
 SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
 {
    SCIP_PROPDATA* pd;
@@ -414,6 +575,7 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    SCIP_CALL( SCIPsetPropFree(scip, prop, propFreeGpulinear) );
    SCIP_CALL( SCIPsetPropInitsol(scip, prop, propInitsolGpulinear) );
    SCIP_CALL( SCIPsetPropExitsol(scip, prop, propExitsolGpulinear) );
+   SCIP_CALL( SCIPsetPropResprop(scip, prop, propRespropGpulinear) );
    SCIP_CALL( SCIPaddIntParam(scip, "propagating/" PROP_NAME "/device", "CUDA device ordinal of the GPU",
          &pd->device, FALSE, 0, 0, 1024, NULL, NULL) );
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacelinear",

@@ -252,3 +252,50 @@ def test_binary_test_reads_the_global_domain(gpu_prop, oracle_mod):
     gpu_prop.set_global_bounds(None)
     lb, ub, _, _ = gpu_prop.propagate(inst.lb, inst.ub)
     assert lb[3] == 0.0
+
+
+# ---------------------------------------------------------------------------------------------------------
+# change log of the plain path (the order in which the plugin hands tightenings to SCIP for conflict analysis)
+@pytest.mark.parametrize("hostloop", [False, True])
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_change_log_matches_oracle(gpu_prop, oracle_mod, maxeasy, hostloop):
+    inst = instances.root_mip(1)
+    p = _params(maxeasy)
+    p.flags = gbp.GBP_FLAG_HOSTLOOP if hostloop else 0
+    gpu_prop.set_params(p)
+    gpu_prop.upload(inst)
+    gpu_prop.set_change_log(8 * inst.n)
+    lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
+    col, rnd, llb, lub = gpu_prop.change_log()
+    orc = oracle_mod.Oracle(inst)
+    olb, oub, ores, olog = orc.propagate_logged(inst.lb, inst.ub, oracle_mod.params(maxeasy))
+    assert not cut and np.array_equal(lb, olb) and np.array_equal(ub, oub)
+    assert len(col) == len(olog[0]) > 0
+    for mine, theirs in zip((col, rnd, llb, lub), olog):
+        assert np.array_equal(mine, theirs)
+    # replaying the log in order reproduces the fixpoint
+    rl, ru = inst.lb.copy(), inst.ub.copy()
+    for c, a, b in zip(col, llb, lub):  # later rounds overwrite earlier ones
+        rl[c], ru[c] = a, b
+    assert np.array_equal(rl, lb) and np.array_equal(ru, ub)
+
+    # a seeded node with its global domain
+    nodes = instances.node_batch(inst, lb, ub, 8, seed=5)
+    gpu_prop.set_global_bounds(lb, ub)
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        cols = nodes.col[sl]
+        nlb, nub = lb.copy(), ub.copy()
+        old_l, old_u = nlb[cols].copy(), nub[cols].copy()
+        nlb[cols] = np.maximum(old_l, nodes.lb[sl])
+        nub[cols] = np.minimum(old_u, nodes.ub[sl])
+        _, _, gcut, _ = gpu_prop.propagate(nlb, nub, seed=(cols, old_l, old_u))
+        _, _, er, elog = orc.propagate_logged(nlb, nub, oracle_mod.params(maxeasy), seed=(cols, old_l, old_u),
+                                              glob=(lb, ub))
+        assert gcut == bool(er.cutoff)
+        if not gcut:
+            for mine, theirs in zip(gpu_prop.change_log(), elog):
+                assert np.array_equal(mine, theirs), f"node {k}"
+    gpu_prop.set_global_bounds(None)
+    gpu_prop.set_change_log(0)
+    gpu_prop.set_params(_params(maxeasy))

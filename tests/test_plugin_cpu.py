@@ -31,7 +31,8 @@ def driver(tmp_path_factory):
     out = tmp_path_factory.mktemp("plugin")
     exe = str(out / "plugin_driver")
     src = [os.path.join(ROOT, "tests", "plugin", "plugin_driver.c"),
-           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c")]
+           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c")]
     inc = ["-I" + os.path.join(REF, "include"), "-I/root/reference/src", "-I" + os.path.join(ROOT, "include"),
            "-I" + os.path.join(ROOT, "scip_gb300", "plugin")]
     cmd = ["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", *inc, "-o", exe, *src, LIBSCIP,
