@@ -34,15 +34,17 @@ void gpl_build_columns(int64_t m, int64_t n, const int64_t* rowptr, const int32_
    }
 }
 
-/* addConflictBounds (cons_linear.c:4799-4970) for row r, whose entry at CSR position pinf is the inferred column:
- * for an integral column, bounds are added in row order only until the residual capacity left by the other
- * columns' global bounds is used up; otherwise every other column's responsible bound is added. */
+/* addConflictBounds (cons_linear.c:4799-4970) for row r, whose entry at CSR position pinf is the inferred column
+ * (pinf < 0: no inferred column, the row itself is infeasible): for an integral column, or none, bounds are added in
+ * row order only until the residual capacity left by the other columns' global bounds is used up; otherwise every
+ * other column's responsible bound is added. */
 static int addBounds(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int64_t r, int64_t pinf, int32_t col,
    int reasonisrhs)
 {
-   const double a = R->vals[pinf];
+   const double a = pinf >= 0 ? R->vals[pinf] : 0.0;
    int64_t p;
-   if( R->isint[col] )
+   /* without an inferred column (an infeasible row) the capacity logic applies as for an integral one */
+   if( pinf < 0 || R->isint[col] )
    {
       double gres = 0.0;
       int finite = 1;
@@ -64,10 +66,13 @@ static int addBounds(const gpl_rows* R, const gpl_num* num, const gpl_io* io, in
       if( finite )
       {
          double rescap = (reasonisrhs ? R->rhs[r] : R->lhs[r]) - gres;
-         if( reasonisrhs == (a > 0.0) )
-            rescap -= a * (io->ubafter(io->ud, col) + 1.0);
-         else
-            rescap -= a * (io->lbafter(io->ud, col) - 1.0);
+         if( pinf >= 0 )
+         {
+            if( reasonisrhs == (a > 0.0) )
+               rescap -= a * (io->ubafter(io->ud, col) + 1.0);
+            else
+               rescap -= a * (io->lbafter(io->ud, col) - 1.0);
+         }
          for( p = R->rowptr[r]; p < R->rowptr[r + 1]; ++p )
          {
             double v = R->vals[p];
@@ -146,6 +151,42 @@ int64_t gpl_explain(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int
       if( islower ? implied < bound - tol : implied > bound + tol )
          continue;
       return addBounds(R, num, io, r, pinf, col, reasonisrhs) == 0 ? r : -2;
+   }
+   return -1;
+}
+
+int64_t gpl_explain_infeasible(const gpl_rows* R, const gpl_num* num, const gpl_io* io)
+{
+   int64_t r;
+   for( r = 0; r < R->m; ++r )
+   {
+      double minact = 0.0;
+      double maxact = 0.0;
+      int mininf = 0;
+      int maxinf = 0;
+      int64_t p;
+      for( p = R->rowptr[r]; p < R->rowptr[r + 1]; ++p )
+      {
+         const double v = R->vals[p];
+         const double l = io->lb(io->ud, R->colidx[p]);
+         const double u = io->ub(io->ud, R->colidx[p]);
+         const double bmin = v > 0.0 ? l : u;
+         const double bmax = v > 0.0 ? u : l;
+         if( fabs(bmin) >= num->infinity )
+            mininf = 1;
+         else
+            minact += v * bmin;
+         if( fabs(bmax) >= num->infinity )
+            maxinf = 1;
+         else
+            maxact += v * bmax;
+      }
+      if( !mininf && fabs(R->rhs[r]) < num->infinity
+         && minact - R->rhs[r] > num->feastol * (fabs(R->rhs[r]) > 1.0 ? fabs(R->rhs[r]) : 1.0) )
+         return addBounds(R, num, io, r, -1, -1, 1) == 0 ? r : -2;
+      if( !maxinf && fabs(R->lhs[r]) < num->infinity
+         && R->lhs[r] - maxact > num->feastol * (fabs(R->lhs[r]) > 1.0 ? fabs(R->lhs[r]) : 1.0) )
+         return addBounds(R, num, io, r, -1, -1, 0) == 0 ? r : -2;
    }
    return -1;
 }

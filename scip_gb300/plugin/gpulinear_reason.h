@@ -57,6 +57,12 @@ typedef struct
  * no row implies the bound (then nothing was added), or -2 if an add callback failed. */
 int64_t gpl_explain(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int32_t col, int islower, double bound);
 
+/* A row that the bounds io->lb/io->ub make infeasible (minimal activity above rhs or maximal below lhs, beyond
+ * feastol), explained as cons_linear's analyzeConflict does for an infeasible row (addConflictBounds without an
+ * inferred column, cons_linear.c:4799): returns the row (>= 0) after adding its reason bounds, -1 if no row is
+ * infeasible, -2 if an add callback failed. */
+int64_t gpl_explain_infeasible(const gpl_rows* R, const gpl_num* num, const gpl_io* io);
+
 /* builds colptr/rowidx/rowpos of R from its CSR part; the arrays have n+1, nnz and nnz entries */
 void gpl_build_columns(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx, int64_t* colptr,
    int32_t* rowidx, int64_t* rowpos);

@@ -58,6 +58,9 @@ struct SCIP_PropData
    SCIP_Longint          ncalls;
    SCIP_Longint          nchgbds;
    SCIP_Longint          ncutoffs;
+   SCIP_Longint          nresolves;          /**< conflict-resolution requests for this propagator's changes */
+   SCIP_Longint          nresolved;          /**< ... explained with a row */
+   SCIP_Longint          nconflicts;         /**< cutoffs handed to conflict analysis with an infeasible row */
 };
 
 static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
@@ -210,7 +213,7 @@ static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
    p.hugeval = SCIPgetHugeValue(scip);
    SCIP_CALL( SCIPgetRealParam(scip, "numerics/boundstreps", &v) );
    p.boundstreps = v;
-   SCIP_CALL( SCIPgetRealParam(scip, "numerics/recompfac", &v) );
+   SCIP_CALL( SCIPgetRealParam(scip, "numerics/recomputefac", &v) );
    p.recompfac = v;
    if( SCIPgetRealParam(scip, "constraints/linear/maxeasyactivitydelta", &v) == SCIP_OKAY )
       p.maxeasyactivitydelta = v;
@@ -283,6 +286,78 @@ static SCIP_DECL_PROPEXITSOL(propExitsolGpulinear)
 {
    SCIP_PROPDATA* pd = SCIPpropGetData(prop);
    freeMatrix(scip, pd);
+   return SCIP_OKAY;
+}
+
+/* SCIP's bound history behind the reason module's callbacks */
+typedef struct
+{
+   SCIP* scip;
+   SCIP_VAR** vars;
+   SCIP_BDCHGIDX* bdchgidx;
+} ReasonCtx;
+
+/** the last call's change log as inferences of this propagator, round by round */
+static SCIP_RETCODE applyLog(SCIP* scip, SCIP_PROP* prop, SCIP_PROPDATA* pd, SCIP_Bool* reduced, SCIP_Bool* infeasible)
+{
+   int64_t nlog = 0;
+   int64_t k;
+   *infeasible = FALSE;
+   if( gbp_get_change_log(pd->ctx, pd->logcap, pd->logcol, pd->loground, pd->loglb, pd->logub, &nlog) != GBP_OK )
+      return SCIP_OKAY;
+   for( k = 0; k < nlog && !*infeasible; ++k )
+   {
+      SCIP_VAR* var = pd->vars[pd->logcol[k]];
+      SCIP_Bool tightened = FALSE;
+      if( pd->logub[k] < SCIPvarGetUbLocal(var) )
+      {
+         SCIP_CALL( SCIPinferVarUbProp(scip, var, pd->logub[k], prop, pd->loground[k], TRUE, infeasible, &tightened) );
+         *reduced = *reduced || tightened;
+         pd->nchgbds += tightened ? 1 : 0;
+      }
+      if( !*infeasible && pd->loglb[k] > SCIPvarGetLbLocal(var) )
+      {
+         SCIP_CALL( SCIPinferVarLbProp(scip, var, pd->loglb[k], prop, pd->loground[k], TRUE, infeasible, &tightened) );
+         *reduced = *reduced || tightened;
+         pd->nchgbds += tightened ? 1 : 0;
+      }
+   }
+   return SCIP_OKAY;
+}
+
+/* forward declarations of the reason callbacks (below) */
+static double rLb(void* ud, int32_t k);
+static double rUb(void* ud, int32_t k);
+static double rGlb(void* ud, int32_t k);
+static double rGub(void* ud, int32_t k);
+static double rLbAfter(void* ud, int32_t k);
+static double rUbAfter(void* ud, int32_t k);
+static int rAddLb(void* ud, int32_t k);
+static int rAddUb(void* ud, int32_t k);
+static void reasonSetup(SCIP* scip, SCIP_PROPDATA* pd, SCIP_BDCHGIDX* bdchgidx, void* ctx, gpl_rows* R, gpl_num* num,
+   gpl_io* io);
+
+/** conflict analysis of a cutoff the device found: cons_linear analyses the row that became infeasible
+ *  (analyzeConflict, cons_linear.c:5190); with the logged changes applied, such a row holds under the local bounds */
+static SCIP_RETCODE analyzeCutoff(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   ReasonCtx c;
+   gpl_rows R;
+   gpl_num num;
+   gpl_io io;
+   int64_t r;
+   if( !SCIPisConflictAnalysisApplicable(scip) )
+      return SCIP_OKAY;
+   SCIP_CALL( SCIPinitConflictAnalysis(scip, SCIP_CONFTYPE_PROPAGATION, FALSE) );
+   reasonSetup(scip, pd, NULL, &c, &R, &num, &io);
+   r = gpl_explain_infeasible(&R, &num, &io);
+   if( r == -2 )
+      return SCIP_ERROR;
+   if( r >= 0 )
+   {
+      SCIP_CALL( SCIPanalyzeConflict(scip, 0, NULL) );
+      pd->nconflicts++;
+   }
    return SCIP_OKAY;
 }
 
@@ -384,8 +459,13 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    }
    if( cutoff )
    {
+      /* the changes the rounds before the infeasibility made, then conflict analysis on the infeasible row */
+      SCIP_Bool infeasible = FALSE;
       pd->ncutoffs++;
       pd->havesnap = FALSE;
+      SCIP_CALL( applyLog(scip, prop, pd, &reduced, &infeasible) );
+      if( !infeasible )
+         SCIP_CALL( analyzeCutoff(scip, pd) );
       *result = SCIP_CUTOFF;
       return SCIP_OKAY;
    }
@@ -395,42 +475,13 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
     * analysis asks for them (propRespropGpulinear).  The final loop below then finds nothing left to do, or, when
     * the log overflowed, moves the final bounds in without reasons. */
    {
-      int64_t nlog = 0;
-      if( gbp_get_change_log(pd->ctx, pd->logcap, pd->logcol, pd->loground, pd->loglb, pd->logub, &nlog) == GBP_OK )
+      SCIP_Bool infeasible = FALSE;
+      SCIP_CALL( applyLog(scip, prop, pd, &reduced, &infeasible) );
+      if( infeasible )
       {
-         int64_t k;
-         for( k = 0; k < nlog; ++k )
-         {
-            SCIP_VAR* var = pd->vars[pd->logcol[k]];
-            SCIP_Bool infeasible = FALSE;
-            SCIP_Bool tightened = FALSE;
-            if( pd->logub[k] < SCIPvarGetUbLocal(var) )
-            {
-               SCIP_CALL( SCIPinferVarUbProp(scip, var, pd->logub[k], prop, pd->loground[k], TRUE, &infeasible,
-                     &tightened) );
-               if( infeasible )
-               {
-                  pd->havesnap = FALSE;
-                  *result = SCIP_CUTOFF;
-                  return SCIP_OKAY;
-               }
-               reduced = reduced || tightened;
-               pd->nchgbds += tightened ? 1 : 0;
-            }
-            if( pd->loglb[k] > SCIPvarGetLbLocal(var) )
-            {
-               SCIP_CALL( SCIPinferVarLbProp(scip, var, pd->loglb[k], prop, pd->loground[k], TRUE, &infeasible,
-                     &tightened) );
-               if( infeasible )
-               {
-                  pd->havesnap = FALSE;
-                  *result = SCIP_CUTOFF;
-                  return SCIP_OKAY;
-               }
-               reduced = reduced || tightened;
-               pd->nchgbds += tightened ? 1 : 0;
-            }
-         }
+         pd->havesnap = FALSE;
+         *result = SCIP_CUTOFF;
+         return SCIP_OKAY;
       }
    }
    for( j = 0; j < pd->ncols; ++j )
@@ -473,13 +524,6 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    return SCIP_OKAY;
 }
 
-/* SCIP's bound history behind the reason module's callbacks */
-typedef struct
-{
-   SCIP* scip;
-   SCIP_VAR** vars;
-   SCIP_BDCHGIDX* bdchgidx;
-} ReasonCtx;
 
 static double rLb(void* ud, int32_t k)
 {
@@ -514,6 +558,39 @@ static int rAddUb(void* ud, int32_t k)
    return SCIPaddConflictUb(c->scip, c->vars[k], c->bdchgidx) == SCIP_OKAY ? 0 : 1;
 }
 
+/* the rows, numerics and SCIP's bound history (at bdchgidx; NULL: now) for the reason module */
+static void reasonSetup(SCIP* scip, SCIP_PROPDATA* pd, SCIP_BDCHGIDX* bdchgidx, void* ctx, gpl_rows* R, gpl_num* num,
+   gpl_io* io)
+{
+   ReasonCtx* c = (ReasonCtx*)ctx;
+   c->scip = scip;
+   c->vars = pd->vars;
+   c->bdchgidx = bdchgidx;
+   R->m = pd->nrows;
+   R->n = pd->ncols;
+   R->rowptr = pd->rowptr;
+   R->colidx = pd->colidx;
+   R->vals = pd->vals;
+   R->lhs = pd->lhs;
+   R->rhs = pd->rhs;
+   R->isint = pd->isint;
+   R->colptr = pd->colptr;
+   R->rowidx = pd->rowidx;
+   R->rowpos = pd->rowpos;
+   num->infinity = SCIPinfinity(scip);
+   num->feastol = SCIPfeastol(scip);
+   num->epsilon = SCIPepsilon(scip);
+   io->ud = c;
+   io->lb = rLb;
+   io->ub = rUb;
+   io->glb = rGlb;
+   io->gub = rGub;
+   io->lbafter = rLbAfter;
+   io->ubafter = rUbAfter;
+   io->addlb = rAddLb;
+   io->addub = rAddUb;
+}
+
 /** reason of one of this propagator's bound changes (type_prop.h:258): the bounds of a row that implies it, chosen
  *  as cons_linear's resolvePropagation / addConflictBounds would for that row (cons_linear.c:5097, :4799) */
 static SCIP_DECL_PROPRESPROP(propRespropGpulinear)
@@ -527,39 +604,18 @@ static SCIP_DECL_PROPRESPROP(propRespropGpulinear)
    int64_t r;
 
    *result = SCIP_DIDNOTFIND;
+   pd->nresolves++;
    if( pd->colptr == NULL || col < 0 || col >= pd->ncols || pd->vars[col] != infervar )
       return SCIP_OKAY;
-   c.scip = scip;
-   c.vars = pd->vars;
-   c.bdchgidx = bdchgidx;
-   R.m = pd->nrows;
-   R.n = pd->ncols;
-   R.rowptr = pd->rowptr;
-   R.colidx = pd->colidx;
-   R.vals = pd->vals;
-   R.lhs = pd->lhs;
-   R.rhs = pd->rhs;
-   R.isint = pd->isint;
-   R.colptr = pd->colptr;
-   R.rowidx = pd->rowidx;
-   R.rowpos = pd->rowpos;
-   num.infinity = SCIPinfinity(scip);
-   num.feastol = SCIPfeastol(scip);
-   num.epsilon = SCIPepsilon(scip);
-   io.ud = &c;
-   io.lb = rLb;
-   io.ub = rUb;
-   io.glb = rGlb;
-   io.gub = rGub;
-   io.lbafter = rLbAfter;
-   io.ubafter = rUbAfter;
-   io.addlb = rAddLb;
-   io.addub = rAddUb;
+   reasonSetup(scip, pd, bdchgidx, &c, &R, &num, &io);
    r = gpl_explain(&R, &num, &io, col, boundtype == SCIP_BOUNDTYPE_LOWER, relaxedbd);
    if( r == -2 )
       return SCIP_ERROR;
    if( r >= 0 )
+   {
       *result = SCIP_SUCCESS;
+      pd->nresolved++;
+   }
    return SCIP_OKAY;
 }
 
@@ -610,4 +666,21 @@ SCIP_Bool SCIPgpulinearIsActive(SCIP* scip)
       return FALSE;
    pd = SCIPpropGetData(prop);
    return pd->ctx != NULL && !pd->failed;
+}
+
+SCIP_RETCODE SCIPgetGpulinearStats(SCIP* scip, SCIP_Longint* ncalls, SCIP_Longint* nchgbds, SCIP_Longint* ncutoffs,
+   SCIP_Longint* nconflicts, SCIP_Longint* nresolves, SCIP_Longint* nresolved)
+{
+   SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
+   SCIP_PROPDATA* pd;
+   if( prop == NULL )
+      return SCIP_PLUGINNOTFOUND;
+   pd = SCIPpropGetData(prop);
+   *ncalls = pd->ncalls;
+   *nchgbds = pd->nchgbds;
+   *ncutoffs = pd->ncutoffs;
+   *nconflicts = pd->nconflicts;
+   *nresolves = pd->nresolves;
+   *nresolved = pd->nresolved;
+   return SCIP_OKAY;
 }

@@ -34,6 +34,11 @@ SCIP_RETCODE SCIPgetGpulinearMatrix(SCIP* scip, int* nrows, int* ncols, const in
 /** whether the propagator runs on a GPU (FALSE before PROPINITSOL or after it disabled itself) */
 SCIP_Bool SCIPgpulinearIsActive(SCIP* scip);
 
+/** counters of the propagator: calls, bounds it changed, cutoffs, cutoffs it handed to conflict analysis with an
+ *  infeasible row, conflict-resolution requests for its changes and how many of them it explained with a row */
+SCIP_RETCODE SCIPgetGpulinearStats(SCIP* scip, SCIP_Longint* ncalls, SCIP_Longint* nchgbds, SCIP_Longint* ncutoffs,
+   SCIP_Longint* nconflicts, SCIP_Longint* nresolves, SCIP_Longint* nresolved);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,228 @@
+/* Test double of libgbp for the plugin's SCIP-side tests: the C-ABI calls the propagator plugin makes, answered by
+ * the oracle (oracle/linprop_oracle.c) on the host.  It exists so that SCIP (which builds only where its sources
+ * are) can run the plugin end to end -- write-back of the change log and conflict resolution -- without a GPU.  It
+ * is linked only into tests/plugin/solve_driver.c; the product library libgbp has no host path. */
+#include <stdlib.h>
+#include <string.h>
+
+#include "gbp.h"
+#include "linprop_oracle.h"
+
+struct gbp_ctx
+{
+   lpo_problem P;
+   int64_t* rowptr;
+   int32_t* colidx;
+   double* vals;
+   double* lhs;
+   double* rhs;
+   int8_t* isint;
+   int64_t* colptr;
+   int32_t* rowidx;
+   double* cvals;
+   lpo_params par;
+   double* glb;
+   double* gub;
+   int has_global;
+   lpo_log log;
+   int logon;
+};
+
+int gbp_version(void) { return 0; }
+
+const char* gbp_error_string(int code) { return code == GBP_OK ? "ok" : "error (oracle test double)"; }
+
+const char* gbp_last_error(const gbp_ctx* ctx) { (void)ctx; return "oracle test double"; }
+
+void gbp_default_params(gbp_params* p)
+{
+   p->infinity = 1e20;
+   p->epsilon = 1e-9;
+   p->sumepsilon = 1e-6;
+   p->feastol = 1e-6;
+   p->hugeval = 1e15;
+   p->boundstreps = 0.05;
+   p->recompfac = 1e6;
+   p->maxeasyactivitydelta = 1e6;
+   p->maxrounds = 0;
+   p->flags = 0;
+}
+
+int gbp_create(gbp_ctx** ctx, int device, void* stream)
+{
+   (void)device;
+   (void)stream;
+   *ctx = calloc(1, sizeof(gbp_ctx));
+   if( *ctx == NULL )
+      return GBP_ERR_NOMEM;
+   lpo_default_params(&(*ctx)->par);
+   return GBP_OK;
+}
+
+static void freeProblem(gbp_ctx* c)
+{
+   free(c->rowptr); free(c->colidx); free(c->vals); free(c->lhs); free(c->rhs); free(c->isint);
+   free(c->colptr); free(c->rowidx); free(c->cvals); free(c->glb); free(c->gub);
+   c->rowptr = NULL; c->colidx = NULL; c->vals = NULL; c->lhs = NULL; c->rhs = NULL; c->isint = NULL;
+   c->colptr = NULL; c->rowidx = NULL; c->cvals = NULL; c->glb = NULL; c->gub = NULL;
+   c->has_global = 0;
+}
+
+int gbp_destroy(gbp_ctx* ctx)
+{
+   if( ctx == NULL )
+      return GBP_ERR_INVALID;
+   freeProblem(ctx);
+   free(ctx->log.col); free(ctx->log.round); free(ctx->log.lb); free(ctx->log.ub);
+   free(ctx);
+   return GBP_OK;
+}
+
+int gbp_set_params(gbp_ctx* ctx, const gbp_params* p)
+{
+   ctx->par.infinity = p->infinity;
+   ctx->par.epsilon = p->epsilon;
+   ctx->par.sumepsilon = p->sumepsilon;
+   ctx->par.feastol = p->feastol;
+   ctx->par.hugeval = p->hugeval;
+   ctx->par.boundstreps = p->boundstreps;
+   ctx->par.recompfac = p->recompfac;
+   ctx->par.maxeasyactivitydelta = p->maxeasyactivitydelta;
+   ctx->par.maxrounds = p->maxrounds;
+   ctx->par.flags = (p->flags & GBP_FLAG_NOSORTVARS) ? LPO_FLAG_NOSORTVARS : 0;
+   return GBP_OK;
+}
+
+#define DUP(dst, src, cnt, T) do { dst = malloc(sizeof(T) * (size_t)((cnt) > 0 ? (cnt) : 1)); \
+      if( (cnt) > 0 ) memcpy(dst, src, sizeof(T) * (size_t)(cnt)); } while( 0 )
+
+int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+   const double* vals, const double* lhs, const double* rhs, const int8_t* isint)
+{
+   int64_t nnz = rowptr[m];
+   int64_t i;
+   int64_t p;
+   int64_t* fill;
+   freeProblem(ctx);
+   DUP(ctx->rowptr, rowptr, m + 1, int64_t);
+   DUP(ctx->colidx, colidx, nnz, int32_t);
+   DUP(ctx->vals, vals, nnz, double);
+   DUP(ctx->lhs, lhs, m, double);
+   DUP(ctx->rhs, rhs, m, double);
+   DUP(ctx->isint, isint, n, int8_t);
+   ctx->colptr = calloc((size_t)n + 1, sizeof(int64_t));
+   ctx->rowidx = malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+   ctx->cvals = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+   fill = malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+   for( p = 0; p < nnz; ++p )
+      ctx->colptr[colidx[p] + 1]++;
+   for( i = 0; i < n; ++i )
+      ctx->colptr[i + 1] += ctx->colptr[i];
+   for( i = 0; i < n; ++i )
+      fill[i] = ctx->colptr[i];
+   for( i = 0; i < m; ++i )
+      for( p = rowptr[i]; p < rowptr[i + 1]; ++p )
+      {
+         int64_t q = fill[colidx[p]]++;
+         ctx->rowidx[q] = (int32_t)i;
+         ctx->cvals[q] = vals[p];
+      }
+   free(fill);
+   ctx->P.m = m; ctx->P.n = n; ctx->P.rowptr = ctx->rowptr; ctx->P.colidx = ctx->colidx; ctx->P.vals = ctx->vals;
+   ctx->P.lhs = ctx->lhs; ctx->P.rhs = ctx->rhs; ctx->P.isint = ctx->isint; ctx->P.colptr = ctx->colptr;
+   ctx->P.rowidx = ctx->rowidx; ctx->P.cvals = ctx->cvals;
+   return GBP_OK;
+}
+
+int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub)
+{
+   free(ctx->glb);
+   free(ctx->gub);
+   ctx->glb = NULL;
+   ctx->gub = NULL;
+   ctx->has_global = 0;
+   if( glb == NULL )
+      return GBP_OK;
+   DUP(ctx->glb, glb, ctx->P.n, double);
+   DUP(ctx->gub, gub, ctx->P.n, double);
+   ctx->has_global = 1;
+   return GBP_OK;
+}
+
+int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity)
+{
+   free(ctx->log.col); free(ctx->log.round); free(ctx->log.lb); free(ctx->log.ub);
+   memset(&ctx->log, 0, sizeof(ctx->log));
+   ctx->logon = capacity > 0;
+   if( !ctx->logon )
+      return GBP_OK;
+   ctx->log.cap = capacity;
+   ctx->log.col = malloc(sizeof(int32_t) * (size_t)capacity);
+   ctx->log.round = malloc(sizeof(int32_t) * (size_t)capacity);
+   ctx->log.lb = malloc(sizeof(double) * (size_t)capacity);
+   ctx->log.ub = malloc(sizeof(double) * (size_t)capacity);
+   return GBP_OK;
+}
+
+int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols,
+   const double* oldlb, const double* oldub, int32_t* cutoff, gbp_result* res)
+{
+   lpo_result r;
+   ctx->log.n = 0;
+   *cutoff = 0;
+   if( res != NULL )
+      memset(res, 0, sizeof(*res));
+   if( nseed == 0 )
+      return GBP_OK;
+   if( lpo_propagate_logged(&ctx->P, &ctx->par, lb, ub, nseed < 0 ? 0 : nseed, nseed < 0 ? NULL : seedcols, oldlb,
+         oldub, ctx->has_global ? ctx->glb : NULL, ctx->has_global ? ctx->gub : NULL, &r,
+         ctx->logon ? &ctx->log : NULL) != 0 )
+      return GBP_ERR_NOMEM;
+   *cutoff = r.cutoff;
+   if( res != NULL )
+   {
+      res->cutoff = r.cutoff;
+      res->rounds = r.rounds;
+      res->status = r.status;
+      res->rows = r.rows;
+      res->nnz = r.nnz;
+      res->candidates = r.candidates;
+      res->changes = r.changes;
+   }
+   return r.status == 2 ? GBP_ERR_LIMIT : GBP_OK;
+}
+
+static const lpo_log* sortlog;
+static int byRoundCol(const void* a, const void* b)
+{
+   int64_t x = *(const int64_t*)a;
+   int64_t y = *(const int64_t*)b;
+   if( sortlog->round[x] != sortlog->round[y] )
+      return sortlog->round[x] < sortlog->round[y] ? -1 : 1;
+   return sortlog->col[x] < sortlog->col[y] ? -1 : (sortlog->col[x] > sortlog->col[y] ? 1 : 0);
+}
+
+int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, double* lb, double* ub, int64_t* n)
+{
+   int64_t have;
+   int64_t k;
+   int64_t* ord;
+   *n = ctx->log.n;
+   if( !ctx->logon )
+      return GBP_ERR_STATE;
+   have = ctx->log.n < ctx->log.cap ? ctx->log.n : ctx->log.cap;
+   ord = malloc(sizeof(int64_t) * (size_t)(have > 0 ? have : 1));
+   for( k = 0; k < have; ++k )
+      ord[k] = k;
+   sortlog = &ctx->log;
+   qsort(ord, (size_t)have, sizeof(int64_t), byRoundCol);
+   for( k = 0; k < have && k < cap; ++k )
+   {
+      col[k] = ctx->log.col[ord[k]];
+      round[k] = ctx->log.round[ord[k]];
+      lb[k] = ctx->log.lb[ord[k]];
+      ub[k] = ctx->log.ub[ord[k]];
+   }
+   free(ord);
+   return (ctx->log.n > ctx->log.cap || ctx->log.n > cap) ? GBP_ERR_OVERFLOW : GBP_OK;
+}

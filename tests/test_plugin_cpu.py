@@ -24,7 +24,7 @@ def _has_gpu():
 
 
 @pytest.fixture(scope="module")
-def driver(tmp_path_factory):
+def driver(tmp_path_factory, oracle_mod):
     if not os.path.exists(LIBSCIP):
         pytest.skip("SCIP build (oracle/_ref) not present")
     build_libgbp()
@@ -33,7 +33,8 @@ def driver(tmp_path_factory):
     src = [os.path.join(ROOT, "tests", "plugin", "plugin_driver.c"),
            os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
            os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c")]
-    inc = ["-I" + os.path.join(REF, "include"), "-I/root/reference/src", "-I" + os.path.join(ROOT, "include"),
+    inc = ["-I" + os.path.join(REF, "include"), "-I" + os.path.join(oracle_mod.REFDIR, "src"),
+           "-I" + os.path.join(ROOT, "include"),
            "-I" + os.path.join(ROOT, "scip_gb300", "plugin")]
     cmd = ["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", *inc, "-o", exe, *src, LIBSCIP,
            "-L" + LIBDIR, "-lgbp", "-Wl,-rpath," + LIBDIR, "-lstdc++", "-lm", "-lpthread"]
@@ -70,3 +71,50 @@ def test_replacelinear_switches_cons_linear_propagation_off(driver, tmp_path):
     inst = instances.root_mip(1, m=200, n=500)
     lines, _ = run(driver, inst, tmp_path, "--replace")
     assert lines["propfreq"] == "-1"
+
+
+@pytest.fixture(scope="module")
+def solve_driver(tmp_path_factory, oracle_mod):
+    """tests/plugin/solve_driver.c with the plugin on top of the oracle test double (tests/plugin/gbp_oracle_shim.c):
+    the plugin's SCIP side -- change log write-back, conflict analysis of cutoffs, reasons -- runs inside SCIP."""
+    if not os.path.exists(LIBSCIP):
+        pytest.skip("SCIP build (oracle/_ref) not present")
+    out = tmp_path_factory.mktemp("solve")
+    exe = str(out / "solve_driver")
+    src = [os.path.join(ROOT, "tests", "plugin", "solve_driver.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c"),
+           os.path.join(ROOT, "tests", "plugin", "gbp_oracle_shim.c"),
+           os.path.join(ROOT, "oracle", "linprop_oracle.c")]
+    inc = ["-I" + os.path.join(REF, "include"), "-I" + os.path.join(oracle_mod.REFDIR, "src"),
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "scip_gb300", "plugin"),
+           "-I" + os.path.join(ROOT, "oracle")]
+    cmd = ["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", "-ffp-contract=off", *inc, "-o", exe, *src, LIBSCIP,
+           "-lstdc++", "-lm", "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def _solve(exe, path, mode):
+    r = subprocess.run([exe, path, mode, "200000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return dict(l.split(" ", 1) for l in r.stdout.strip().splitlines() if " " in l)
+
+
+@pytest.mark.parametrize("name", ["enigma", "flugpl", "misc03"])
+def test_plugin_replaces_linear_propagation_in_search(solve_driver, oracle_mod, name):
+    """SCIP searches (propagation and conflict analysis, no LP) once with cons_linear's propagation and once with the
+    gpulinear propagator in its place: both prove the same optimum; every reason SCIP asks the plugin for is
+    explained with a row, and the plugin's cutoffs feed conflict analysis."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    plain = _solve(solve_driver, path, "plain")
+    gpu = _solve(solve_driver, path, "gpulinear")
+    assert plain["status"] == "optimal" and gpu["status"] == "optimal"
+    assert float(plain["obj"]) == float(gpu["obj"])
+    calls, chg, cut, analysed, asked, resolved, _, active = gpu["gpulinear"].split()
+    assert active == "1" and int(calls) > 0 and int(chg) > 0
+    assert asked == resolved
+    if name != "flugpl":  # flugpl is solved without any conflict
+        assert int(resolved) > 0 and int(analysed) > 0 and int(gpu["conflicts"]) > 0
