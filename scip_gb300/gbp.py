@@ -289,19 +289,33 @@ class Propagator:
         gub = np.ascontiguousarray(gub, dtype=np.float64)
         self._check(self.L.gbp_set_global_bounds(self.h, _ptr(glb), _ptr(gub)))
 
-    def propagate_nodes(self, baselb, baseub, nodes, out_cap: Optional[int] = None) -> NodeResults:
-        """Host arrays: nodes is an instances.NodeBatch.  Returns packed per-node results."""
+    @staticmethod
+    def node_outputs(nnodes: int, out_cap: int, alloc=np.empty) -> NodeResults:
+        """Output arrays for propagate_nodes (reusable across calls; alloc may return pinned arrays)."""
+        return NodeResults(alloc(nnodes, np.int8), alloc(nnodes, np.int32), alloc(nnodes, np.int64),
+                           alloc(nnodes, np.int32), alloc(out_cap, np.int32), alloc(out_cap, np.float64),
+                           alloc(out_cap, np.float64), GbpResult())
+
+    def propagate_nodes(self, baselb, baseub, nodes, out_cap: Optional[int] = None,
+                        out: Optional[NodeResults] = None) -> NodeResults:
+        """Host arrays: nodes is an instances.NodeBatch.  Returns packed per-node results (in `out` when given: arrays
+        from node_outputs, of at least nodes.nnodes entries and out_cap packed entries)."""
         N = nodes.nnodes
         if out_cap is None:
-            out_cap = max(1024, 64 * N)
+            out_cap = max(1024, 64 * N) if out is None else len(out.col)
         baselb = np.ascontiguousarray(baselb, dtype=np.float64)
         baseub = np.ascontiguousarray(baseub, dtype=np.float64)
         ptr = np.ascontiguousarray(nodes.ptr, dtype=np.int64)
         col = np.ascontiguousarray(nodes.col, dtype=np.int32)
         nlb = np.ascontiguousarray(nodes.lb, dtype=np.float64)
         nub = np.ascontiguousarray(nodes.ub, dtype=np.float64)
-        r = NodeResults(np.zeros(N, np.int8), np.zeros(N, np.int32), np.zeros(N, np.int64), np.zeros(N, np.int32),
-                        np.zeros(out_cap, np.int32), np.zeros(out_cap), np.zeros(out_cap), GbpResult())
+        if out is None:
+            r = self.node_outputs(N, out_cap)
+        else:
+            if len(out.cutoff) < N or len(out.col) < out_cap:
+                raise ValueError("output arrays too small")
+            r = out
+            r.result = GbpResult()
         rc = self.L.gbp_propagate_nodes(self.h, _ptr(baselb), _ptr(baseub), N, _ptr(ptr), _ptr(col), _ptr(nlb),
                                         _ptr(nub), _ptr(r.cutoff), _ptr(r.rounds), _ptr(r.off), _ptr(r.n),
                                         _ptr(r.col), _ptr(r.lb), _ptr(r.ub), out_cap, ctypes.byref(r.result))
