@@ -142,6 +142,14 @@ int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, 
 int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, const int64_t* col_off,
    const int64_t* rowptr, const int32_t* colidx, const double* vals, const double* lhs, const double* rhs,
    const int8_t* isint);
+/* the same upload from the instances as separate parts, with no host-side concatenation: part k has m_k[k] rows
+ * and n_k[k] columns, its own CSR (rowptr_k[k] with m_k[k] + 1 entries from 0; colidx_k[k] LOCAL column indices in
+ * [0, n_k[k])), sides and integrality.  Each part is copied straight to its place on the device, where one kernel
+ * shifts the row pointers and column indices and fills the instance maps.  The result equals gbp_upload_instances
+ * of the concatenation. */
+int gbp_upload_instance_list(gbp_ctx* ctx, int64_t ninst, const int64_t* m_k, const int64_t* n_k,
+   const int64_t* const* rowptr_k, const int32_t* const* colidx_k, const double* const* vals_k,
+   const double* const* lhs_k, const double* const* rhs_k, const int8_t* const* isint_k);
 int gbp_propagate_instances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
 int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
 

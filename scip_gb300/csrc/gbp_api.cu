@@ -319,33 +319,15 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
   return GBP_OK;
 }
 
-int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
-                       const double* vals, const double* lhs, const double* rhs, const int8_t* isint) {
-  if (!ctx || m < 0 || n < 0 || !rowptr || (m > 0 && (!lhs || !rhs)) || (n > 0 && !isint))
-    return fail(ctx, GBP_ERR_INVALID, "null argument or negative size");
-  if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1)
-    return fail(ctx, GBP_ERR_INVALID, "problem too large (m < 2^30, n < 2^31 required)");
-  if (rowptr[0] != 0) return fail(ctx, GBP_ERR_INVALID, "rowptr[0] must be 0");
-  for (int64_t i = 0; i < m; ++i)
-    if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
-  const int64_t nnz = rowptr[m];
-  if (nnz > 0 && (!colidx || !vals)) return fail(ctx, GBP_ERR_INVALID, "null colidx/vals");
-
+// Upload, part 1: drop the previous problem and make the device arrays large enough for m rows, n columns and nnz
+// entries.
+static int prepareUpload(gbp_ctx* ctx, int64_t m, int64_t n, int64_t nnz) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->has_problem = false;
   ctx->has_global = false;
   ctx->ninst = 0;
   destroyGraphs(ctx);
-
-  // all-rows frontier: short rows from the front, long rows from the back
-  std::vector<int> allrows(std::max<int64_t>(m, 1));
-  int ns = 0, nl = 0;
-  for (int64_t i = 0; i < m; ++i) {
-    if (rowptr[i + 1] - rowptr[i] <= LONGROW) allrows[ns++] = (int)i;
-    else allrows[m - 1 - nl++] = (int)i;
-  }
-
   const size_t mm = (size_t)std::max<int64_t>(m, 1), nn = (size_t)std::max<int64_t>(n, 1),
                zz = (size_t)std::max<int64_t>(nnz, 1);
   if ((int64_t)mm > ctx->cap_m || (int64_t)nn > ctx->cap_n || (int64_t)zz > ctx->cap_nnz) {
@@ -381,20 +363,31 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
     ctx->slot_mem = nullptr;
     ctx->nslots = 0;
   }
+  return GBP_OK;
+}
 
-  CK(cudaMemcpyAsync(ctx->d_rowptr, rowptr, (m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-  if (nnz) {
-    CK(cudaMemcpyAsync(ctx->d_colidx, colidx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_vals, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+// the instance maps (row -> instance, column -> instance) and the per-instance cutoff flags
+static int prepareInstanceMaps(gbp_ctx* ctx, int64_t ninst) {
+  if (!ctx->d_rowinst || ninst > ctx->cap_inst) {
+    if (ctx->d_rowinst) cudaFree(ctx->d_rowinst);
+    if (ctx->d_colinst) cudaFree(ctx->d_colinst);
+    if (ctx->d_instcut) cudaFree(ctx->d_instcut);
+    ctx->d_rowinst = ctx->d_colinst = nullptr;
+    ctx->d_instcut = nullptr;
+    CK(cudaMalloc(&ctx->d_rowinst, ctx->cap_m * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_colinst, ctx->cap_n * sizeof(int32_t)));
+    const int64_t ci = std::max<int64_t>(ninst, ctx->cap_inst + ctx->cap_inst / 4);
+    CK(cudaMalloc(&ctx->d_instcut, ci * sizeof(int)));
+    ctx->cap_inst = ci;
   }
-  if (m) {
-    CK(cudaMemcpyAsync(ctx->d_lhs, lhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_rhs, rhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_allrows, allrows.data(), m * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  }
-  if (n) CK(cudaMemcpyAsync(ctx->d_isint, isint, n, cudaMemcpyHostToDevice, ctx->stream));
+  return GBP_OK;
+}
 
-  // CSC with relevance flags, built on the device: count per column, prefix sum, scatter
+// Upload, part 3 (after the CSR, sides, integrality and the all-rows frontier are on the device): column view,
+// candidate keys, flags.
+static int finishUpload(gbp_ctx* ctx, int64_t m, int64_t n, int64_t nnz, int ns, int nl) {
+  const size_t mm = (size_t)std::max<int64_t>(m, 1), nn = (size_t)std::max<int64_t>(n, 1);
+// CSC with relevance flags, built on the device: count per column, prefix sum, scatter
   {
     unsigned long long* count = nullptr;
     unsigned long long* cursor = nullptr;
@@ -436,6 +429,41 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
   ctx->stamp = 0;
   ctx->has_problem = true;
   return GBP_OK;
+}
+
+int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                       const double* vals, const double* lhs, const double* rhs, const int8_t* isint) {
+  if (!ctx || m < 0 || n < 0 || !rowptr || (m > 0 && (!lhs || !rhs)) || (n > 0 && !isint))
+    return fail(ctx, GBP_ERR_INVALID, "null argument or negative size");
+  if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1)
+    return fail(ctx, GBP_ERR_INVALID, "problem too large (m < 2^30, n < 2^31 required)");
+  if (rowptr[0] != 0) return fail(ctx, GBP_ERR_INVALID, "rowptr[0] must be 0");
+  for (int64_t i = 0; i < m; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return fail(ctx, GBP_ERR_INVALID, "rowptr not monotone");
+  const int64_t nnz = rowptr[m];
+  if (nnz > 0 && (!colidx || !vals)) return fail(ctx, GBP_ERR_INVALID, "null colidx/vals");
+
+  int rc = prepareUpload(ctx, m, n, nnz);
+  if (rc != GBP_OK) return rc;
+  // all-rows frontier: short rows from the front, long rows from the back
+  std::vector<int> allrows(std::max<int64_t>(m, 1));
+  int ns = 0, nl = 0;
+  for (int64_t i = 0; i < m; ++i) {
+    if (rowptr[i + 1] - rowptr[i] <= LONGROW) allrows[ns++] = (int)i;
+    else allrows[m - 1 - nl++] = (int)i;
+  }
+  CK(cudaMemcpyAsync(ctx->d_rowptr, rowptr, (m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  if (nnz) {
+    CK(cudaMemcpyAsync(ctx->d_colidx, colidx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_vals, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (m) {
+    CK(cudaMemcpyAsync(ctx->d_lhs, lhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_rhs, rhs, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_allrows, allrows.data(), m * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (n) CK(cudaMemcpyAsync(ctx->d_isint, isint, n, cudaMemcpyHostToDevice, ctx->stream));
+  return finishUpload(ctx, m, n, nnz, ns, nl);
 }
 
 // ------------------------------------------------------------------------------------------ plain path
@@ -872,18 +900,8 @@ int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, co
   }
   int rc = gbp_upload_problem(ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
   if (rc != GBP_OK) return rc;
-  if (!ctx->d_rowinst || ninst > ctx->cap_inst) {
-    if (ctx->d_rowinst) cudaFree(ctx->d_rowinst);
-    if (ctx->d_colinst) cudaFree(ctx->d_colinst);
-    if (ctx->d_instcut) cudaFree(ctx->d_instcut);
-    ctx->d_rowinst = ctx->d_colinst = nullptr;
-    ctx->d_instcut = nullptr;
-    CK(cudaMalloc(&ctx->d_rowinst, ctx->cap_m * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->d_colinst, ctx->cap_n * sizeof(int32_t)));
-    const int64_t ci = std::max<int64_t>(ninst, ctx->cap_inst + ctx->cap_inst / 4);
-    CK(cudaMalloc(&ctx->d_instcut, ci * sizeof(int)));
-    ctx->cap_inst = ci;
-  }
+  rc = prepareInstanceMaps(ctx, ninst);
+  if (rc != GBP_OK) return rc;
   CK(cudaMemcpyAsync(ctx->d_rowinst, rowinst.data(), rowinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_colinst, colinst.data(), colinst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
@@ -898,6 +916,89 @@ int gbp_upload_instances(gbp_ctx* ctx, int64_t ninst, const int64_t* row_off, co
   if (bad) {
     freeProblem(ctx);
     return fail(ctx, GBP_ERR_INVALID, "a row references a column of another instance");
+  }
+  ctx->ninst = ninst;
+  return GBP_OK;
+}
+
+int gbp_upload_instance_list(gbp_ctx* ctx, int64_t ninst, const int64_t* m_k, const int64_t* n_k,
+                             const int64_t* const* rowptr_k, const int32_t* const* colidx_k,
+                             const double* const* vals_k, const double* const* lhs_k, const double* const* rhs_k,
+                             const int8_t* const* isint_k) {
+  if (!ctx || ninst < 1 || !m_k || !n_k || !rowptr_k || !colidx_k || !vals_k || !lhs_k || !rhs_k || !isint_k)
+    return fail(ctx, GBP_ERR_INVALID, "null argument");
+  if (ninst >= (int64_t(1) << 31) - 1) return fail(ctx, GBP_ERR_INVALID, "too many instances");
+  // offsets: [row_off | col_off | nnz_off], ninst + 1 entries each
+  std::vector<int64_t> off(3 * (ninst + 1) + 1);
+  int64_t* row_off = off.data();
+  int64_t* col_off = row_off + ninst + 1;
+  int64_t* nnz_off = col_off + ninst + 1;
+  row_off[0] = col_off[0] = nnz_off[0] = 0;
+  for (int64_t k = 0; k < ninst; ++k) {
+    const int64_t mk = m_k[k], nk = n_k[k];
+    const int64_t* rp = rowptr_k[k];
+    if (mk < 0 || nk < 0 || !rp || (mk > 0 && (!lhs_k[k] || !rhs_k[k])) || (nk > 0 && !isint_k[k]))
+      return fail(ctx, GBP_ERR_INVALID, "null part or negative part size");
+    if (rp[0] != 0) return fail(ctx, GBP_ERR_INVALID, "a part's rowptr[0] must be 0");
+    for (int64_t i = 0; i < mk; ++i)
+      if (rp[i + 1] < rp[i]) return fail(ctx, GBP_ERR_INVALID, "a part's rowptr is not monotone");
+    if (rp[mk] > 0 && (!colidx_k[k] || !vals_k[k])) return fail(ctx, GBP_ERR_INVALID, "null part colidx/vals");
+    row_off[k + 1] = row_off[k] + mk;
+    col_off[k + 1] = col_off[k] + nk;
+    nnz_off[k + 1] = nnz_off[k] + rp[mk];
+  }
+  const int64_t m = row_off[ninst], n = col_off[ninst], nnz = nnz_off[ninst];
+  if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1)
+    return fail(ctx, GBP_ERR_INVALID, "problem too large (m < 2^30, n < 2^31 required)");
+
+  int rc = prepareUpload(ctx, m, n, nnz);
+  if (rc != GBP_OK) return rc;
+  rc = prepareInstanceMaps(ctx, ninst);
+  if (rc != GBP_OK) return rc;
+  std::vector<int> allrows(std::max<int64_t>(m, 1));
+  int ns = 0, nl = 0;
+  for (int64_t k = 0; k < ninst; ++k) {
+    const int64_t* rp = rowptr_k[k];
+    for (int64_t i = 0; i < m_k[k]; ++i) {
+      if (rp[i + 1] - rp[i] <= LONGROW) allrows[ns++] = (int)(row_off[k] + i);
+      else allrows[m - 1 - nl++] = (int)(row_off[k] + i);
+    }
+  }
+  // each part straight to its place; the last row pointer is the total
+  for (int64_t k = 0; k < ninst; ++k) {
+    const int64_t mk = m_k[k], nk = n_k[k], zk = nnz_off[k + 1] - nnz_off[k];
+    if (mk) {
+      CK(cudaMemcpyAsync(ctx->d_rowptr + row_off[k], rowptr_k[k], mk * sizeof(int64_t), cudaMemcpyHostToDevice,
+                         ctx->stream));
+      CK(cudaMemcpyAsync(ctx->d_lhs + row_off[k], lhs_k[k], mk * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(ctx->d_rhs + row_off[k], rhs_k[k], mk * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (zk) {
+      CK(cudaMemcpyAsync(ctx->d_colidx + nnz_off[k], colidx_k[k], zk * sizeof(int32_t), cudaMemcpyHostToDevice,
+                         ctx->stream));
+      CK(cudaMemcpyAsync(ctx->d_vals + nnz_off[k], vals_k[k], zk * sizeof(double), cudaMemcpyHostToDevice,
+                         ctx->stream));
+    }
+    if (nk) CK(cudaMemcpyAsync(ctx->d_isint + col_off[k], isint_k[k], nk, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaMemcpyAsync(ctx->d_rowptr + m, &nnz_off[ninst], sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  if (m) CK(cudaMemcpyAsync(ctx->d_allrows, allrows.data(), m * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  int64_t* d_off = nullptr;
+  const size_t offbytes = off.size() * sizeof(int64_t);
+  CK(cudaMallocAsync((void**)&d_off, offbytes, ctx->stream));
+  CK(cudaMemcpyAsync(d_off, off.data(), offbytes, cudaMemcpyHostToDevice, ctx->stream));
+  int* d_bad = (int*)(d_off + 3 * (ninst + 1));
+  CK(cudaMemsetAsync(d_bad, 0, sizeof(int64_t), ctx->stream));
+  CK(launchFixParts(ctx->stream, gridFor(ctx, std::max(std::max(m, n), nnz)), ninst, d_off, m, n, nnz, ctx->d_rowptr,
+                    ctx->d_colidx, ctx->d_rowinst, ctx->d_colinst, d_bad));
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaFreeAsync(d_off, ctx->stream));
+  rc = finishUpload(ctx, m, n, nnz, ns, nl);  // synchronises the stream
+  if (rc != GBP_OK) return rc;
+  if (bad) {
+    freeProblem(ctx);
+    return fail(ctx, GBP_ERR_INVALID, "a part's column index is outside its part");
   }
   ctx->ninst = ninst;
   return GBP_OK;

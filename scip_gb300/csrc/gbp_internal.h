@@ -99,6 +99,9 @@ struct NodesArgs {
 // count (clamped to 255) in two launches; hist holds 2 * ORDER_BUCKETS zeroed ints (counts, cursors).
 constexpr int ORDER_BUCKETS = 256;
 cudaError_t launchNodeOrder(cudaStream_t st, int grid, int64_t nnodes, const int64_t* ptr, int* hist, int* order);
+// instance parts: shift local row pointers / column indices by the parts' offsets, fill the instance maps
+cudaError_t launchFixParts(cudaStream_t st, int grid, int64_t ninst, const int64_t* off, int64_t m, int64_t n,
+                           int64_t nnz, int64_t* rowptr, int32_t* colidx, int32_t* rowinst, int32_t* colinst, int* bad);
 
 // launchers (return the cudaError_t of the launch)
 cudaError_t launchRowsShort(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,

@@ -339,6 +339,43 @@ __global__ void k_csc_scatter(int64_t m, const int64_t* rowptr, const int32_t* c
   }
 }
 
+// Instances uploaded part by part (gbp_upload_instance_list): each part's row pointers and column indices are
+// local to the part; shift them by the part's offsets, record each row's and column's instance, and flag column
+// indices outside their part.  off = [row_off | col_off | nnz_off], each ninst + 1 entries.
+__device__ __forceinline__ int64_t partOf(const int64_t* o, int64_t ninst, int64_t x) {
+  int64_t lo = 0, hi = ninst - 1;  // last k with o[k] <= x
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (o[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void k_fix_parts(int64_t ninst, const int64_t* off, int64_t m, int64_t n, int64_t nnz, int64_t* rowptr,
+                            int32_t* colidx, int32_t* rowinst, int32_t* colinst, int* bad) {
+  const int64_t* row_off = off;
+  const int64_t* col_off = off + ninst + 1;
+  const int64_t* nnz_off = off + 2 * (ninst + 1);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    const int64_t k = partOf(row_off, ninst, i);
+    rowptr[i] += nnz_off[k];
+    rowinst[i] = (int32_t)k;
+  }
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += stride)
+    colinst[j] = (int32_t)partOf(col_off, ninst, j);
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += stride) {
+    const int64_t k = partOf(nnz_off, ninst, p);
+    const int64_t c = colidx[p];
+    if (c < 0 || c >= col_off[k + 1] - col_off[k]) {
+      atomicExch(bad, 1);
+      colidx[p] = 0;
+    } else {
+      colidx[p] = (int32_t)(c + col_off[k]);
+    }
+  }
+}
+
 // rows of instance k may only reference columns of instance k
 __global__ void k_check_blocks(int64_t m, const int64_t* rowptr, const int32_t* colidx, const int32_t* rowinst,
                                const int32_t* colinst, int* bad) {
@@ -600,6 +637,11 @@ __global__ void __launch_bounds__(256) k_order_scatter(int64_t nnodes, const int
 }
 
 // ------------------------------------------------------------------------------------------ launchers
+cudaError_t launchFixParts(cudaStream_t st, int grid, int64_t ninst, const int64_t* off, int64_t m, int64_t n,
+                           int64_t nnz, int64_t* rowptr, int32_t* colidx, int32_t* rowinst, int32_t* colinst, int* bad) {
+  k_fix_parts<<<grid, 256, 0, st>>>(ninst, off, m, n, nnz, rowptr, colidx, rowinst, colinst, bad);
+  return cudaGetLastError();
+}
 cudaError_t launchNodeOrder(cudaStream_t st, int grid, int64_t nnodes, const int64_t* ptr, int* hist, int* order) {
   k_order_hist<<<grid, 256, 0, st>>>(nnodes, ptr, hist);
   k_order_scatter<<<grid, 256, 0, st>>>(nnodes, ptr, hist, hist + ORDER_BUCKETS, order);

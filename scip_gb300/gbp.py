@@ -34,7 +34,8 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_set_params", "gbp_get_stream", "gbp_upload_problem", "gbp_propagate", "gbp_propagate_device",
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
-           "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log"]
+           "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log",
+           "gbp_upload_instance_list"]
 
 
 class GbpParams(ctypes.Structure):
@@ -95,6 +96,7 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
     L.gbp_set_batch_shape.argtypes = [_P, ctypes.c_int32, ctypes.c_int32]
     L.gbp_upload_instances.argtypes = [_P, ctypes.c_int64] + [_P] * 8
+    L.gbp_upload_instance_list.argtypes = [_P, ctypes.c_int64] + [_P] * 8
     L.gbp_propagate_instances.argtypes = [_P, _P, _P, _P, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_instances_device.argtypes = L.gbp_propagate_instances.argtypes
     L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
@@ -215,16 +217,34 @@ class Propagator:
         self._check(rc, allow=(GBP_ERR_LIMIT,))
         return lb, ub, bool(cut.value), res
 
-    def upload_instances(self, insts):
-        """Upload several independent instances as one block-diagonal problem; returns (row_off, col_off)."""
+    def upload_instances(self, insts, concat=False):
+        """Upload several independent instances as one block-diagonal problem; returns (row_off, col_off).
+
+        By default each instance's arrays go to the device as they are (gbp_upload_instance_list); concat=True
+        concatenates them on the host first (gbp_upload_instances)."""
         from .instances import concat_instances
 
-        big, row_off, col_off = concat_instances(insts)
+        k = len(insts)
+        if concat:
+            big, row_off, col_off = concat_instances(insts)
+            keep = [np.ascontiguousarray(a) for a in (row_off, col_off, big.rowptr, big.colidx, big.vals, big.lhs,
+                                                       big.rhs, big.isint)]
+            self._check(self.L.gbp_upload_instances(self.h, k, *[_ptr(a) for a in keep]))
+        else:
+            row_off = np.zeros(k + 1, dtype=np.int64)
+            col_off = np.zeros(k + 1, dtype=np.int64)
+            np.cumsum([i.m for i in insts], out=row_off[1:])
+            np.cumsum([i.n for i in insts], out=col_off[1:])
+            mk = np.ascontiguousarray(np.diff(row_off))
+            nk = np.ascontiguousarray(np.diff(col_off))
+            fields = (("rowptr", np.int64), ("colidx", np.int32), ("vals", np.float64), ("lhs", np.float64),
+                      ("rhs", np.float64), ("isint", np.int8))
+            keep = [[np.ascontiguousarray(getattr(i, f), dtype=t) for i in insts] for f, t in fields]
+            tables = [(ctypes.c_void_p * k)(*[a.ctypes.data for a in arrs]) for arrs in keep]
+            self._check(self.L.gbp_upload_instance_list(self.h, k, _ptr(mk), _ptr(nk),
+                                                        *[ctypes.cast(t, ctypes.c_void_p) for t in tables]))
         self._inst_off = (row_off, col_off)
-        keep = [np.ascontiguousarray(a) for a in (row_off, col_off, big.rowptr, big.colidx, big.vals, big.lhs,
-                                                   big.rhs, big.isint)]
-        self._check(self.L.gbp_upload_instances(self.h, len(insts), *[_ptr(a) for a in keep]))
-        self.m, self.n = big.m, big.n
+        self.m, self.n = int(row_off[-1]), int(col_off[-1])
         return row_off, col_off
 
     def propagate_instances(self, lb, ub):

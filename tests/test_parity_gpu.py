@@ -155,6 +155,35 @@ def test_uneven_instances_in_one_problem_match_oracle_per_instance(gpu_prop, ora
             assert np.array_equal(glb[sl], olb) and np.array_equal(gub[sl], oub), f"instance {k}"
 
 
+def test_instance_list_upload_equals_concatenated_upload(gpu_prop):
+    """gbp_upload_instance_list (parts copied to their places, offsets fixed on the device) gives the same results
+    as gbp_upload_instances of the host concatenation, with an empty part and a part of one column among them; a
+    part whose column index is outside the part is rejected."""
+    from scip_gb300.gbp import GbpError
+    from scip_gb300.instances import Instance
+    insts = instances.uneven_batch(seed=10, count=10, rmin=200, rmax=4000)
+    empty = Instance(np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), np.zeros(0),
+                     np.zeros(0), np.zeros(0), np.zeros(0, np.int8), x0=np.zeros(0))
+    lonely = Instance(np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), np.zeros(0),
+                      np.zeros(1), np.ones(1), np.ones(1, np.int8), x0=np.zeros(1))
+    insts[3:3] = [empty, lonely]
+    lb = np.concatenate([i.lb for i in insts])
+    ub = np.concatenate([i.ub for i in insts])
+    gpu_prop.set_params(_params(1e6))
+    got = []
+    for concat in (True, False):
+        row_off, col_off = gpu_prop.upload_instances(insts, concat=concat)
+        got.append(gpu_prop.propagate_instances(lb, ub)[:3] + (row_off, col_off))
+    for a, b in zip(got[0], got[1]):
+        assert np.array_equal(a, b)
+    broken = Instance(np.array([0, 2], np.int64), np.array([0, 2], np.int32), np.ones(2), np.array([-1e20]),
+                      np.array([1.0]), np.zeros(2), np.ones(2), np.ones(2, np.int8), x0=np.zeros(2))
+    with pytest.raises(GbpError):
+        gpu_prop.upload_instances(insts[:2] + [broken])
+    gpu_prop.upload_instances(insts)  # the context stays usable
+    assert np.array_equal(gpu_prop.propagate_instances(lb, ub)[0], got[1][0])
+
+
 def test_uneven_instances_device_variant(gpu_prop, oracle_mod):
     """gbp_propagate_instances_device: bounds and per-instance cutoff flags in device memory."""
     torch = pytest.importorskip("torch")
