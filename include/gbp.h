@@ -63,6 +63,14 @@ typedef struct
  * binary that yields no tightening ends the visit of the binaries, as tightenBounds does
  * (cons_linear.c:7110-7138; order of consdataCompVarProp, cons_linear.c:3229-3254). */
 #define GBP_FLAG_NOSORTVARS 2
+/* constraints/linear/rangedrowpropagation = TRUE (SCIP's default) with rangedrowartcons = FALSE: after its
+ * activity rules, every frontier row with both sides finite runs the gcd-based ranged-row rule
+ * (rangedRowPropagation, cons_linear.c:5715-6695) from the same round-start bounds.  Its bound changes are forced
+ * (SCIPinferVarFixCons / SCIPinferVarLb/UbCons with force = TRUE), and it may declare the row infeasible.  It
+ * walks a row's entries in the order SCIP holds them: with sortvars, consdataCompVarProp on the global domain;
+ * without, the index order (binaries, integers, continuous columns, each by column).  Not available in
+ * gbp_propagate_nodes_noalloc. */
+#define GBP_FLAG_RANGEDROW 4
 
 typedef struct
 {

@@ -427,6 +427,14 @@ typedef struct
    double* rlb;
    uint8_t* rflag;      /* bit0 ub, bit1 forced ub, bit2 lb, bit3 forced lb */
    lpo_log* log;        /* change log, or NULL */
+   /* ranged rows: on/off, and for the row being processed its propagation order (rord[k] = offset of the k-th
+    * entry), merge scratch and gcd membership per order position */
+   int ranged;
+   double* startlb;     /* the bounds the call started from (sortvars off, no global domain), else NULL */
+   double* startub;
+   int32_t* rord;
+   int32_t* rtmp;
+   uint8_t* rmem;
 } Work;
 
 static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
@@ -440,6 +448,10 @@ static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
       if( P->rowptr[i + 1] - P->rowptr[i] > maxlen )
          maxlen = P->rowptr[i + 1] - P->rowptr[i];
    w->binskip = !(par->flags & LPO_FLAG_NOSORTVARS);
+   w->ranged = (par->flags & LPO_FLAG_RANGEDROW) != 0;
+   w->rmem = calloc((size_t)maxlen, 1);
+   w->rord = malloc(sizeof(int32_t) * (size_t)maxlen);
+   w->rtmp = malloc(sizeof(int32_t) * (size_t)maxlen);
    w->rub = malloc(sizeof(double) * (size_t)maxlen);
    w->rlb = malloc(sizeof(double) * (size_t)maxlen);
    w->rflag = calloc((size_t)maxlen, 1);
@@ -464,7 +476,7 @@ static int workInit(Work* w, const lpo_problem* P, const lpo_params* par)
    w->saveub = malloc(sizeof(double) * (size_t)(n + 1));
    return (w->cub && w->clb && w->cubf && w->clbf && w->cflag && w->touched && w->front && w->next && w->rowstamp
       && w->oldlb && w->oldub && w->chg && w->dirty && w->dirtylist && w->savelb && w->saveub && w->rub && w->rlb
-      && w->rflag) ? 0 : -1;
+      && w->rflag && w->rmem && w->rord && w->rtmp) ? 0 : -1;
 }
 
 static void workFree(Work* w)
@@ -472,7 +484,7 @@ static void workFree(Work* w)
    free(w->cub); free(w->clb); free(w->cubf); free(w->clbf); free(w->cflag); free(w->touched);
    free(w->front); free(w->next); free(w->rowstamp); free(w->oldlb); free(w->oldub); free(w->chg);
    free(w->dirty); free(w->dirtylist); free(w->savelb); free(w->saveub);
-   free(w->rub); free(w->rlb); free(w->rflag);
+   free(w->rub); free(w->rlb); free(w->rflag); free(w->rmem); free(w->rord); free(w->rtmp); free(w->startlb); free(w->startub);
 }
 
 static void newStamp(Work* w)
@@ -618,6 +630,392 @@ static void commitRow(Work* w, const double* lb, const double* ub, int64_t p0, i
    }
 }
 
+/* ------------------------------------------------------------------ ranged rows (rangedRowPropagation,
+ * cons_linear.c:5715-6695, with constraints/linear/rangedrowartcons = FALSE) */
+
+/* the order of a row's entries on the global domain dl/du.  sorted (constraints/linear/sortvars, the order
+ * tightenBounds sorts rows into, consdataCompVarProp, cons_linear.c:3191-3254): binaries first (larger |a| first,
+ * ties by column), then integers (larger |a|*(ub-lb) first, ties by column), then continuous columns by column;
+ * keys are compared exactly, as in binBefore.  Not sorted (the index order rows keep from presolving,
+ * consdataCompVar, cons_linear.c:3152-3187): binaries, integers, continuous columns, each by column.  The column
+ * index stands for SCIP's variable index, which follows it when the columns of each type come in index order. */
+static int propBefore(const lpo_problem* P, const double* dl, const double* du, int sorted, int64_t p, int64_t q)
+{
+   int32_t jp = P->colidx[p];
+   int32_t jq = P->colidx[q];
+   int bp = P->isint[jp] != 0 && dl[jp] >= 0.0 && du[jp] <= 1.0;
+   int bq = P->isint[jq] != 0 && dl[jq] >= 0.0 && du[jq] <= 1.0;
+   double kp;
+   double kq;
+   if( bp != bq )
+      return bp;
+   if( bp && sorted )
+      return binBefore(P, p, q);
+   if( (P->isint[jp] != 0) != (P->isint[jq] != 0) )
+      return P->isint[jp] != 0;
+   if( P->isint[jp] == 0 || !sorted )
+      return jp < jq;
+   kp = fabs(P->vals[p] * (du[jp] - dl[jp]));
+   kq = fabs(P->vals[q] * (du[jq] - dl[jq]));
+   if( kp != kq )
+      return kp > kq;
+   return jp < jq;
+}
+
+static void orderMerge(const lpo_problem* P, const double* dl, const double* du, int sorted, int64_t p0, int32_t* a,
+   int32_t* tmp, int64_t n)
+{
+   int64_t h;
+   int64_t x;
+   int64_t y;
+   int64_t k;
+   if( n < 2 )
+      return;
+   h = n / 2;
+   orderMerge(P, dl, du, sorted, p0, a, tmp, h);
+   orderMerge(P, dl, du, sorted, p0, a + h, tmp, n - h);
+   for( x = 0, y = h, k = 0; k < n; ++k )
+   {
+      if( y >= n || (x < h && !propBefore(P, dl, du, sorted, p0 + a[y], p0 + a[x])) )
+         tmp[k] = a[x++];
+      else
+         tmp[k] = a[y++];
+   }
+   memcpy(a, tmp, sizeof(int32_t) * (size_t)n);
+}
+
+static int64_t gcdLL(int64_t a, int64_t b)   /* SCIPcalcGreComDiv (misc.c:9197) computes the same value */
+{
+   while( b != 0 )
+   {
+      int64_t t = a % b;
+      a = b;
+      b = t;
+   }
+   return a;
+}
+/* (SCIP_Longint)(REALABS(val) + feastol) of cons_linear.c:5903/5944/6057; saturated where the cast would
+ * overflow */
+static int64_t coefInt(const Num* s, double v)
+{
+   double x = fabs(v) + s->feastol;
+   return x >= 4.0e18 ? (int64_t)4000000000000000000LL : (int64_t)x;
+}
+static int isIntegral(const Num* s, double x) { return x - floor(x + s->eps) <= s->eps; }  /* EPSISINT */
+static double epsFloor(const Num* s, double x) { return floor(x + s->eps); }              /* SCIPfloor */
+static double epsCeil(const Num* s, double x) { return ceil(x - s->eps); }                /* SCIPceil */
+
+/* each of the two solution-enumeration loops of cons_linear.c:6087-6139 runs at most this many times; a row
+ * that needs more (its residual activity range spans over a million steps) yields no deduction */
+#define RANGED_MAXIT (1 << 20)
+
+/* rangedRowPropagation for frontier row i from the round-start bounds; bound changes become forced
+ * candidates (SCIPinferVarFixCons / SCIPinferVarLb/UbCons with force = TRUE).  Returns 1 on cutoff. */
+static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo_result* res)
+{
+   const lpo_problem* P = w->P;
+   const Num* s = &w->s;
+   const int64_t p0 = P->rowptr[i];
+   const int64_t len = P->rowptr[i + 1] - p0;
+   double fixedact = 0.0;
+   int64_t nfixed = 0;
+   int64_t ninf = 0;
+   int64_t ncont = 0;
+   int64_t first = -1;
+   int gcdisone = 1;
+   int possiblegcd = 1;
+   double lhs;
+   double rhs;
+   int64_t k;
+   int64_t gcd;
+   double minact = 0.0;
+   double maxact = 0.0;
+   double g;
+   double value;
+   double minvalue = 0.0;
+   double maxvalue = 0.0;
+   int nsols = 0;
+   int64_t gcdinf;
+   int64_t it;
+#define RPOS(k) (p0 + w->rord[k])
+#define RFIXED(p) eq(s, lb[P->colidx[p]], ub[P->colidx[p]])
+#define RQUAL(p) (P->isint[P->colidx[p]] != 0 && isIntegral(s, P->vals[p]) && !eq(s, fabs(P->vals[p]), 1.0))
+
+   if( len < 3 || isInf(s, -P->lhs[i]) || isInf(s, P->rhs[i]) )
+      return 0;
+   /* the row in the order SCIP holds it when this runs (after tightenBounds, cons_linear.c:7042-7046), on the
+    * global domain: with sortvars the round-start bounds at the root, where SCIP re-sorts a row whenever one of
+    * its columns becomes binary (cons_linear.c:17327-17333); without, the bounds the call started from, which
+    * the index order of presolving saw */
+   for( k = 0; k < len; ++k )
+      w->rord[k] = (int32_t)k;
+   if( w->glb != NULL )
+      orderMerge(P, w->glb, w->gub, w->binskip, p0, w->rord, w->rtmp, len);
+   else if( w->startlb != NULL )
+      orderMerge(P, w->startlb, w->startub, 0, p0, w->rord, w->rtmp, len);
+   else
+      orderMerge(P, lb, ub, w->binskip, p0, w->rord, w->rtmp, len);
+   /* fixed activity, last entry first (cons_linear.c:5803-5814) */
+   for( k = len - 1; k >= 0; --k )
+   {
+      int64_t p = RPOS(k);
+      if( RFIXED(p) )
+      {
+         fixedact += lb[P->colidx[p]] * P->vals[p];
+         ++nfixed;
+      }
+   }
+   if( isHuge(s, fabs(fixedact)) )
+      return 0;
+   lhs = P->lhs[i] - fixedact;
+   rhs = P->rhs[i] - fixedact;
+
+   /* partition (cons_linear.c:5839-5958): rmem[k] = 1 for the entries that may lead to infeasibility */
+   memset(w->rmem, 0, (size_t)len);
+   k = -1;
+   do
+   {
+      ++k;
+      while( k < len && !RQUAL(RPOS(k)) )
+      {
+         int64_t p = RPOS(k);
+         if( !RFIXED(p) )
+         {
+            if( P->isint[P->colidx[p]] == 0 )
+               ++ncont;
+            gcdisone = gcdisone && eq(s, fabs(P->vals[p]), 1.0);
+            possiblegcd = 0;
+            w->rmem[k] = 1;
+            ++ninf;
+            if( first < 0 )
+               first = k;
+         }
+         ++k;
+      }
+   }
+   while( k < len && RFIXED(RPOS(k)) );
+   if( k == len || ncont + 2 > len - nfixed )
+      return 0;
+   gcd = coefInt(s, P->vals[RPOS(k)]);
+   for( ; k < len; ++k )
+   {
+      int64_t p = RPOS(k);
+      if( RFIXED(p) )
+         continue;
+      if( !RQUAL(p) )
+      {
+         if( P->isint[P->colidx[p]] == 0 )
+            ++ncont;
+         gcdisone = gcdisone && eq(s, fabs(P->vals[p]), 1.0);
+         possiblegcd = 0;
+         w->rmem[k] = 1;
+         ++ninf;
+         if( first < 0 )
+            first = k;
+      }
+      else
+      {
+         int64_t t = gcdLL(gcd, coefInt(s, P->vals[p]));
+         if( t == 1 )
+         {
+            w->rmem[k] = 1;
+            ++ninf;
+            if( first < 0 )
+               first = k;
+         }
+         else
+            gcd = t;
+      }
+   }
+   if( ninf == 0 )
+      return 0;
+
+   /* activity bounds of those entries, last first (cons_linear.c:5975-6015) */
+   for( k = len - 1; k >= 0; --k )
+   {
+      int64_t p;
+      double v;
+      double l;
+      double u;
+      int mininv = 0;
+      int maxinv = 0;
+      if( !w->rmem[k] )
+         continue;
+      p = RPOS(k);
+      v = P->vals[p];
+      l = lb[P->colidx[p]];
+      u = ub[P->colidx[p]];
+      if( isInf(s, -l) )
+      {
+         if( v < 0.0 )
+            maxinv = 1;
+         else
+            mininv = 1;
+      }
+      else if( v < 0.0 )
+         maxact += v * l;
+      else
+         minact += v * l;
+      if( isInf(s, u) )
+      {
+         if( v > 0.0 )
+            maxinv = 1;
+         else
+            mininv = 1;
+      }
+      else if( v > 0.0 )
+         maxact += v * u;
+      else
+         minact += v * u;
+      if( isHuge(s, -minact) )
+         mininv = 1;
+      if( isHuge(s, maxact) )
+         maxinv = 1;
+      if( mininv || maxinv )
+         return 0;
+   }
+
+   /* no multiple of gcd between the sides (cons_linear.c:6033-6045) */
+   g = (double)gcd;
+   if( !isIntegral(s, (lhs - maxact) / g) && gt(s, epsCeil(s, (lhs - maxact) / g) * g, rhs - minact) )
+      return 1;
+   if( ncont != 0 )
+      return 0;
+
+   /* gcd of the other entries (cons_linear.c:6051-6064) */
+   gcdinf = -1;
+   if( possiblegcd )
+   {
+      for( k = len - 1; k >= 0; --k )
+      {
+         if( !w->rmem[k] )
+            continue;
+         gcdinf = gcdinf < 0 ? coefInt(s, P->vals[RPOS(k)]) : gcdLL(gcdinf, coefInt(s, P->vals[RPOS(k)]));
+         if( gcdinf < 2 )
+            break;
+      }
+   }
+   else if( gcdisone )
+      gcdinf = 1;
+   if( gcdinf < 1 )
+      return 0;
+
+   /* feasible values of the other entries' activity (cons_linear.c:6076-6139) */
+   value = epsCeil(s, minact - s->feastol);
+   for( it = 0; le(s, value, maxact); ++it )
+   {
+      double value2;
+      if( it >= RANGED_MAXIT )
+         return 0;
+      value2 = value + g * epsCeil(s, (lhs - value) / g);
+      if( !ge(s, value2, lhs) )
+         value2 += g;
+      if( le(s, value2, rhs) )
+      {
+         ++nsols;
+         if( nsols == 3 )
+            break;
+         if( nsols == 1 )
+            minvalue = value;
+         maxvalue = value;
+      }
+      value += (double)gcdinf;
+   }
+   if( nsols == 3 )
+   {
+      value = epsFloor(s, maxact + s->feastol);
+      for( it = 0; ge(s, value, minact); ++it )
+      {
+         double value2;
+         if( it >= RANGED_MAXIT )
+            return 0;
+         value2 = value + g * epsFloor(s, (rhs - value) / g);
+         if( !le(s, value2, rhs) )
+            value2 -= g;
+         if( ge(s, value2, lhs) )
+         {
+            maxvalue = value;
+            break;
+         }
+         value -= (double)gcdinf;
+      }
+   }
+   if( nsols == 0 )
+      return 1;
+
+   if( ninf == 1 )
+   {
+      /* the single other entry (cons_linear.c:6160-6183 fixes it, :6296-6352 bounds it) */
+      int64_t p = RPOS(first);
+      int32_t j = P->colidx[p];
+      double v = P->vals[p];
+      if( nsols == 1 )
+      {
+         candLb(w, j, maxvalue / v, 1);
+         candUb(w, j, maxvalue / v, 1);
+         res->candidates += 2;
+      }
+      else
+      {
+         double newlb = v < 0.0 ? maxvalue / v : minvalue / v;
+         double newub = v < 0.0 ? minvalue / v : maxvalue / v;
+         if( newlb > lb[j] )
+         {
+            candLb(w, j, newlb, 1);
+            res->candidates++;
+         }
+         if( newub < ub[j] )
+         {
+            candUb(w, j, newub, 1);
+            res->candidates++;
+         }
+      }
+   }
+   else if( ninf == len - nfixed - 1 )
+   {
+      /* the one unfixed entry outside them (cons_linear.c:6184-6283 fixes it, :6354-6552 bounds it) */
+      int64_t p = -1;
+      int32_t j;
+      double v;
+      for( k = 0; k < len; ++k )
+         if( !w->rmem[k] && !RFIXED(RPOS(k)) )
+         {
+            p = RPOS(k);
+            break;
+         }
+      if( p < 0 )
+         return 0;
+      j = P->colidx[p];
+      v = P->vals[p];
+      if( nsols == 1 )
+      {
+         double bound = v < 0.0 ? epsFloor(s, (lhs - maxvalue) / v) : epsCeil(s, (lhs - maxvalue) / v);
+         candLb(w, j, bound, 1);
+         candUb(w, j, bound, 1);
+         res->candidates += 2;
+      }
+      else
+      {
+         double newlb = v < 0.0 ? epsFloor(s, (rhs - minvalue) / v) : epsCeil(s, (lhs - maxvalue) / v);
+         double newub = v < 0.0 ? epsFloor(s, (lhs - maxvalue) / v) : epsCeil(s, (rhs - minvalue) / v);
+         if( newlb > lb[j] )
+         {
+            candLb(w, j, newlb, 1);
+            res->candidates++;
+         }
+         if( newub < ub[j] )
+         {
+            candUb(w, j, newub, 1);
+            res->candidates++;
+         }
+      }
+   }
+#undef RPOS
+#undef RFIXED
+#undef RQUAL
+   return 0;
+}
+
 /* one frontier row: cutoff check of propagateCons (cons_linear.c:7718-7753), skip tests of tightenBounds
  * (cons_linear.c:7017-7083, canTightenBounds :5214-5238) and candidate bounds of tightenVarBounds
  * (:6700-6974, residual rule) or tightenVarBoundsEasy (:5380-5653, slack rule).  Returns 1 on cutoff. */
@@ -648,6 +1046,10 @@ static int processRow(Work* w, const double* lb, const double* ub, int64_t i, lp
       if( feasGt(s, minact, rhs) || feasLt(s, maxact, lhs) )
          return 1;
    }
+
+   /* ranged rows (propagateCons, cons_linear.c:7694-7711): runs whatever tightenBounds' own tests decide */
+   if( w->ranged && rangedRow(w, lb, ub, i, res) )
+      return 1;
 
    /* canTightenBounds */
    if( a.minneginf + a.minposinf + a.minneghuge + a.minposhuge > 1
@@ -1017,6 +1419,20 @@ int lpo_propagate_logged(const lpo_problem* prob, const lpo_params* par, double*
    w.glb = glb;
    w.gub = gub;
    w.log = log;
+   /* without a global domain, rows keep the index order of the bounds the call starts from */
+   if( glb == NULL && w.ranged && !w.binskip )
+   {
+      w.startlb = malloc(sizeof(double) * (size_t)(prob->n > 0 ? prob->n : 1));
+      w.startub = malloc(sizeof(double) * (size_t)(prob->n > 0 ? prob->n : 1));
+      if( w.startlb == NULL || w.startub == NULL )
+      {
+         workFree(&w);
+         return -1;
+      }
+      memcpy(w.startlb, lb, sizeof(double) * (size_t)prob->n);
+      memcpy(w.startub, ub, sizeof(double) * (size_t)prob->n);
+   }
+
    if( log != NULL )
       log->n = 0;
    newStamp(&w);

@@ -38,6 +38,10 @@ typedef struct
 /* constraints/linear/sortvars = FALSE: every entry of a row is tried (no skipping of the binaries that
  * follow one that cannot be tightened, cons_linear.c:7131-7136) */
 #define LPO_FLAG_NOSORTVARS 1
+/* constraints/linear/rangedrowpropagation = TRUE with rangedrowartcons = FALSE: the gcd-based propagation of
+ * ranged rows and equations (rangedRowPropagation, cons_linear.c:5715-6695) runs after each frontier row's
+ * activity rules, from the same round-start bounds; its bound changes are forced ones, as SCIP's are */
+#define LPO_FLAG_RANGEDROW 2
 
 typedef struct
 {

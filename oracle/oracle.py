@@ -31,6 +31,8 @@ class Params(ctypes.Structure):
 
 # Params.flags: constraints/linear/sortvars = FALSE (every entry of a row is tried)
 FLAG_NOSORTVARS = 1
+# Params.flags: ranged-row propagation (rangedRowPropagation, cons_linear.c:5715) without artificial constraints
+FLAG_RANGEDROW = 2
 
 
 class Log(ctypes.Structure):
@@ -77,12 +79,12 @@ def lib():
     return _lib
 
 
-def params(maxeasy: float = 0.0, maxrounds: int = 0, sortvars: bool = True) -> Params:
+def params(maxeasy: float = 0.0, maxrounds: int = 0, sortvars: bool = True, ranged: bool = False) -> Params:
     p = Params()
     lib().lpo_default_params(ctypes.byref(p))
     p.maxeasyactivitydelta = maxeasy
     p.maxrounds = maxrounds
-    p.flags = 0 if sortvars else FLAG_NOSORTVARS
+    p.flags = (0 if sortvars else FLAG_NOSORTVARS) | (FLAG_RANGEDROW if ranged else 0)
     return p
 
 
@@ -193,7 +195,7 @@ class Oracle:
         return out
 
 
-def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None):
+def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False, sortvars=True):
     """Run SCIP itself (oracle/_ref/scip_oracle) on the instance; returns the parsed output of
     scip_gb300.instances.read_oracle_output."""
     from scip_gb300.instances import read_oracle_output
@@ -208,6 +210,7 @@ def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None):
         if nodes is not None:
             npth = os.path.join(d, "nodes.bin")
             nodes.write(npth)
-        cmd = [SCIP_ORACLE, ip, npth, op] + (["--easy"] if easy else []) + ["--repeat", str(repeat)]
+        cmd = ([SCIP_ORACLE, ip, npth, op] + (["--easy"] if easy else []) + (["--ranged"] if ranged else [])
+               + ([] if sortvars else ["--nosort"]) + ["--repeat", str(repeat)])
         subprocess.run(cmd, check=True, capture_output=True)
         return read_oracle_output(op)

@@ -2,7 +2,7 @@
  * writes the resulting bounds, so that fixtures under tests/golden can pin the C restatement
  * (oracle/linprop_oracle.c) and the CUDA path against the reference itself.
  *
- * Usage:  scip_oracle <instance.bin> <nodes.bin|-> <out.bin> [--easy] [--repeat R]
+ * Usage:  scip_oracle <instance.bin> <nodes.bin|-> <out.bin> [--easy] [--ranged] [--nosort] [--repeat R]
  *
  * Pattern (the probing-in-heuristic recipe; see src/scip/scip_probing.c:120-690 and
  * tests/include/scip_test.c:121-133 for the interrupt idiom):
@@ -11,6 +11,8 @@
  *     (constraints/linear/rangedrowpropagation=FALSE, cons_linear.c:155), every other propagator
  *     (propagating/<x>/freq=-1), heuristics, separation, conflict analysis and LP solving, and lift
  *     the propagation round limits (propagating/maxrounds[root]=-1);
+ *   - --ranged switches ranged-row propagation (cons_linear.c:5715) back on, without its artificial
+ *     constraints (constraints/linear/rangedrowartcons=FALSE); --nosort sets constraints/linear/sortvars=FALSE;
  *   - constraints/linear/maxeasyactivitydelta=0 selects the residual rule (cons_linear.c:6700) for
  *     every row; --easy keeps SCIP's default (1e6), i.e. the slack rule of cons_linear.c:5380 for
  *     rows whose largest activity contribution is below 1e6;
@@ -248,7 +250,7 @@ static SCIP_DECL_HEUREXEC(heurExecOracle)
    return SCIP_OKAY;
 }
 
-static SCIP_RETCODE setParams(SCIP* scip, int easy)
+static SCIP_RETCODE setParams(SCIP* scip, int easy, int ranged, int nosort)
 {
    SCIP_PARAM** params = SCIPgetParams(scip);
    int nparams = SCIPgetNParams(scip);
@@ -269,7 +271,10 @@ static SCIP_RETCODE setParams(SCIP* scip, int easy)
       SCIP_CALL( SCIPsetIntParam(scip, pname, -1) );
    }
    SCIP_CALL( SCIPsetIntParam(scip, "presolving/maxrounds", 0) );
-   SCIP_CALL( SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", FALSE) );
+   SCIP_CALL( SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", ranged ? TRUE : FALSE) );
+   SCIP_CALL( SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE) );
+   if( nosort )
+      SCIP_CALL( SCIPsetBoolParam(scip, "constraints/linear/sortvars", FALSE) );
    if( !easy )
       SCIP_CALL( SCIPsetRealParam(scip, "constraints/linear/maxeasyactivitydelta", 0.0) );
    SCIP_CALL( SCIPsetIntParam(scip, "propagating/maxrounds", -1) );
@@ -282,7 +287,8 @@ static SCIP_RETCODE setParams(SCIP* scip, int easy)
    return SCIP_OKAY;
 }
 
-static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* outpath, int easy, int repeat)
+static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* outpath, int easy, int ranged,
+   int nosort, int repeat)
 {
    SCIP* scip = NULL;
    Inst in;
@@ -315,7 +321,7 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
 
    SCIP_CALL( SCIPincludeHeurBasic(scip, &heur, "oracle", "propagation oracle driver", 'o', 1000000, 1, 0, -1,
          SCIP_HEURTIMING_BEFORENODE, FALSE, heurExecOracle, (SCIP_HEURDATA*)&r) );
-   SCIP_CALL( setParams(scip, easy) );
+   SCIP_CALL( setParams(scip, easy, ranged, nosort) );
    /* SCIPsetHeuristics(OFF) above switched the oracle heuristic off as well: switch it back on */
    SCIP_CALL( SCIPsetIntParam(scip, "heuristics/oracle/freq", 1) );
 
@@ -376,24 +382,31 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
 int main(int argc, char** argv)
 {
    int easy = 0;
+   int ranged = 0;
+   int nosort = 0;
    int repeat = 1;
    int a;
    SCIP_RETCODE rc;
    if( argc < 4 )
    {
-      fprintf(stderr, "usage: %s instance.bin nodes.bin|- out.bin [--easy] [--repeat R]\n", argv[0]);
+      fprintf(stderr, "usage: %s instance.bin nodes.bin|- out.bin [--easy] [--ranged] [--nosort] [--repeat R]\n",
+         argv[0]);
       return 2;
    }
    for( a = 4; a < argc; ++a )
    {
       if( strcmp(argv[a], "--easy") == 0 )
          easy = 1;
+      else if( strcmp(argv[a], "--ranged") == 0 )
+         ranged = 1;
+      else if( strcmp(argv[a], "--nosort") == 0 )
+         nosort = 1;
       else if( strcmp(argv[a], "--repeat") == 0 && a + 1 < argc )
          repeat = atoi(argv[++a]);
    }
    if( repeat < 1 )
       repeat = 1;
-   rc = run(argv[1], argv[2], argv[3], easy, repeat);
+   rc = run(argv[1], argv[2], argv[3], easy, ranged, nosort, repeat);
    if( rc != SCIP_OKAY )
    {
       fprintf(stderr, "scip_oracle: SCIP error %d\n", (int)rc);

@@ -47,6 +47,15 @@ struct gbp_ctx {
   double* d_gub = nullptr;
   int64_t cap_glob = 0;
 
+  // ranged rows (GBP_FLAG_RANGEDROW): per-row eligibility, the eligible rows' list, their entry order and merge
+  // scratch (per CSR position); valid until the next upload or parameter change
+  bool ranged_ready = false;
+  uint8_t* d_relig = nullptr;
+  int* d_rlist = nullptr;
+  int32_t* d_rperm = nullptr;
+  int32_t* d_rtmp = nullptr;
+  int nranged = 0;
+
   // plain path
   double* d_lb = nullptr;
   double* d_ub = nullptr;
@@ -129,7 +138,8 @@ static void freeProblem(gbp_ctx* ctx) {
   void* ptrs[] = {ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint, ctx->d_colptr,
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
-                  ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub};
+                  ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub, ctx->d_relig,
+                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -139,18 +149,34 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_allrows = nullptr; ctx->d_base = nullptr; ctx->slot_mem = nullptr; ctx->stage = nullptr;
   ctx->d_rowinst = nullptr; ctx->d_colinst = nullptr; ctx->d_instcut = nullptr; ctx->ninst = 0;
   ctx->d_glb = nullptr; ctx->d_gub = nullptr; ctx->cap_glob = 0; ctx->has_global = false;
+  ctx->d_relig = nullptr; ctx->d_rlist = nullptr; ctx->d_rperm = nullptr; ctx->d_rtmp = nullptr;
+  ctx->ranged_ready = false; ctx->nranged = 0;
   ctx->cap_m = ctx->cap_n = ctx->cap_nnz = ctx->cap_inst = 0;
   ctx->stage_bytes = 0;
   ctx->nslots = 0;
   ctx->has_problem = false;
 }
 
-static Prob devProb(const gbp_ctx* ctx, bool instances = false) {
-  return Prob{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
-              ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity,
-              instances ? ctx->d_rowinst : nullptr, instances ? ctx->d_colinst : nullptr,
-              instances ? ctx->d_instcut : nullptr, (!instances && ctx->has_global) ? ctx->d_glb : nullptr,
-              (!instances && ctx->has_global) ? ctx->d_gub : nullptr};
+static bool rangedOn(const gbp_ctx* ctx) { return (ctx->par.flags & GBP_FLAG_RANGEDROW) != 0; }
+
+// nodes: the batch's global domain is its base bounds, so the ranged rows' order is computed before the call
+static Prob devProb(const gbp_ctx* ctx, bool instances = false, bool nodes = false) {
+  Prob P{ctx->m, ctx->n, ctx->d_rowptr, ctx->d_colidx, ctx->d_vals, ctx->d_lhs, ctx->d_rhs, ctx->d_isint,
+         ctx->d_colptr, ctx->d_cscrow, nullptr, nullptr, ctx->par.infinity,
+         instances ? ctx->d_rowinst : nullptr, instances ? ctx->d_colinst : nullptr,
+         instances ? ctx->d_instcut : nullptr, (!instances && ctx->has_global) ? ctx->d_glb : nullptr,
+         (!instances && ctx->has_global) ? ctx->d_gub : nullptr};
+  if (rangedOn(ctx) && ctx->ranged_ready) {
+    const bool sorted = !(ctx->par.flags & GBP_FLAG_NOSORTVARS);
+    P.relig = ctx->d_relig;
+    P.rperm = ctx->d_rperm;
+    P.rtmp = ctx->d_rtmp;
+    P.rsorted = sorted ? 1 : 0;
+    // the sorted order follows the bounds being propagated when there is no other global domain (at the root
+    // SCIP re-sorts a row whenever one of its columns becomes binary); every other order is fixed for a call
+    P.rlive = (sorted && !nodes && (instances || !ctx->has_global)) ? 1 : 0;
+  }
+  return P;
 }
 
 static int gridFor(const gbp_ctx* ctx, int64_t work, int per_block = 256, int cap_per_sm = 16) {
@@ -204,6 +230,7 @@ int gbp_set_params(gbp_ctx* ctx, const gbp_params* p) {
   ctx->num = Num{p->infinity, p->epsilon, p->sumepsilon, p->feastol, p->hugeval, p->boundstreps, p->recompfac,
                  p->maxeasyactivitydelta, (p->flags & GBP_FLAG_NOSORTVARS) ? 1 : 0};
   destroyGraphs(ctx);  // the numerics are baked into the graphs' kernel arguments
+  ctx->ranged_ready = false;  // eligibility depends on epsilon and infinity
   return GBP_OK;
 }
 
@@ -421,6 +448,7 @@ static int finishUpload(gbp_ctx* ctx, int64_t m, int64_t n, int64_t nnz, int ns,
   CK(cudaMemsetAsync(ctx->d_cflag, 0, nn * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_rowstamp, 0, mm * sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->ranged_ready = false;
   ctx->m = m;
   ctx->n = n;
   ctx->nnz = nnz;
@@ -523,6 +551,43 @@ static int buildGraph(gbp_ctx* ctx, int mode) {
 }
 
 // one fixpoint through the graph: seeds (if any) on the stream, then one graph launch for all rounds
+// Ranged rows: flags and list of the rows the gcd rule can act on (once per upload and parameter set), then, when
+// the entry order is fixed for the call (domain dl/du: explicit global bounds, a node batch's base bounds, or
+// the bounds the call starts from for the index order), that order.  Adds its launches to *launches.
+static int prepareRanged(gbp_ctx* ctx, bool instances, bool nodes, const double* dl, const double* du,
+                         int* launches) {
+  if (!rangedOn(ctx)) return GBP_OK;
+  if (!ctx->ranged_ready) {
+    if (!ctx->d_relig) {
+      CK(cudaStreamSynchronize(ctx->stream));
+      CK(cudaMalloc(&ctx->d_relig, (size_t)ctx->cap_m));
+      CK(cudaMalloc(&ctx->d_rlist, (size_t)ctx->cap_m * sizeof(int)));
+      CK(cudaMalloc(&ctx->d_rperm, (size_t)ctx->cap_nnz * sizeof(int32_t)));
+      CK(cudaMalloc(&ctx->d_rtmp, (size_t)ctx->cap_nnz * sizeof(int32_t)));
+    }
+    destroyGraphs(ctx);  // the graphs hold the ranged rows' pointers
+    int* count = ctx->d_ctr + 6;
+    CK(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
+    if (ctx->m) {
+      const Prob P = devProb(ctx, instances, nodes);
+      CK(launchRangedElig(ctx->stream, gridFor(ctx, ctx->m), ctx->num, P, ctx->d_relig, ctx->d_rlist, count));
+      *launches += 1;
+    }
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->nranged = h;
+    ctx->ranged_ready = true;
+  }
+  const Prob P = devProb(ctx, instances, nodes);
+  if (!P.rlive && ctx->nranged > 0) {
+    CK(launchRangedOrder(ctx->stream, gridFor(ctx, ctx->nranged, 128, 8), P, ctx->d_rlist, ctx->nranged, dl, du,
+                         P.rsorted));
+    *launches += 1;
+  }
+  return GBP_OK;
+}
+
 static int propagateGraph(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
                           const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
   const int mode = ctx->instmode ? 1 : 0;
@@ -600,14 +665,23 @@ static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed
 
 static int propagateCore(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
                          const double* d_oldlb, const double* d_oldub, int32_t* cutoff, gbp_result* res) {
+  int pre = 0;
+  const bool glob = !ctx->instmode && ctx->has_global;
+  int rc = prepareRanged(ctx, ctx->instmode, false, glob ? ctx->d_glb : lb, glob ? ctx->d_gub : ub, &pre);
+  if (rc != GBP_OK) return rc;
   if (!(ctx->par.flags & GBP_FLAG_HOSTLOOP) && !ctx->graph_failed) {
-    int rc = propagateGraph(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
-    if (rc != GBP_ERR_CUDA || ctx->gexec[ctx->instmode ? 1 : 0] != nullptr) return rc;
+    rc = propagateGraph(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
+    if (rc != GBP_ERR_CUDA || ctx->gexec[ctx->instmode ? 1 : 0] != nullptr) {
+      if (res) res->launches += pre;
+      return rc;
+    }
     // graphs unavailable: fall back to the host-driven rounds for the rest of the context's life
     ctx->graph_failed = true;
     cudaGetLastError();
   }
-  return propagateHostLoop(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
+  rc = propagateHostLoop(ctx, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, cutoff, res);
+  if (res) res->launches += pre;
+  return rc;
 }
 
 static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* d_seedcols,
@@ -1139,9 +1213,12 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   CK(launchNodeOrder(ctx->stream, gridFor(ctx, nnodes, 256, 2), nnodes, ptr, ctx->d_orderhist, ctx->d_order));
   CK(launchPack(ctx->stream, gridFor(ctx, ctx->n), baselb, baseub, ctx->d_base, ctx->n));
+  int pre = 0;
+  rc = prepareRanged(ctx, false, true, baselb, baseub, &pre);
+  if (rc) return rc;
   NodesArgs A;
   A.s = ctx->num;
-  A.P = devProb(ctx);
+  A.P = devProb(ctx, false, true);
   A.base = ctx->d_base;
   A.baselb = nullptr;
   A.baseub = nullptr;
@@ -1181,7 +1258,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
     res->cutoff = (int32_t)st[4];
     res->rounds = (int32_t)st[5];
     res->status = (status & 1) ? 2 : 0;
-    res->launches = 4;  // order (2), pack, nodes
+    res->launches = 4 + pre;  // order (2), pack, nodes, and the ranged rows' preparation
     res->rows = (int64_t)st[0];
     res->nnz = (int64_t)st[1];
     res->candidates = (int64_t)st[2];

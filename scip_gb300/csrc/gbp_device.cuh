@@ -43,6 +43,16 @@ struct Prob {
   // global domain for the binary test of the plain path (null: the bounds being propagated, as at the root)
   const double* glb;
   const double* gub;
+  // ranged rows (relig null: the rule is off).  relig[i] = 1 for a row the gcd rule can act on; rperm holds
+  // each such row's entry order (rperm[p0 + k] = offset of its k-th entry), rtmp is merge scratch beside it.
+  // rlive: the order is computed where the row is evaluated, from the global domain of the bounds accessor
+  // (the bounds being propagated at the root); otherwise it was computed before the call.  rsorted: the
+  // order of constraints/linear/sortvars, else the index order.
+  const uint8_t* relig;
+  int32_t* rperm;
+  int32_t* rtmp;
+  int rlive;
+  int rsorted;
 };
 
 // rows of an instance that is already infeasible are skipped
@@ -716,6 +726,322 @@ __device__ __forceinline__ double reliableResidual(const Prob& P, const BND& B, 
   return r;
 }
 
+// ------------------------------------------------------------------------------------------------------
+// Ranged rows: rangedRowPropagation (cons_linear.c:5715-6695) with constraints/linear/rangedrowartcons off.
+// One thread evaluates a row, walking its entries in the order SCIP holds them; the rule is sequential by
+// nature (running gcd, plain double sums in a fixed order) and acts on few rows, so the thread restates it
+// step for step, which keeps it bit-identical with the oracle.
+
+// The order of a row's entries on a global domain D(j, l, u): sorted (consdataCompVarProp,
+// cons_linear.c:3191-3254) -- binaries by larger |a| then column, integers by larger |a|*(ub-lb) then column,
+// continuous columns by column -- or the index order (consdataCompVar, :3152-3187): binaries, integers,
+// continuous columns, each by column.  Keys are compared exactly, so the order is a strict total order.
+template <class DOM>
+__device__ __forceinline__ bool entryBefore(const Prob& P, const DOM& D, bool sorted, int64_t p, int64_t q) {
+  const int jp = P.colidx[p], jq = P.colidx[q];
+  double lp, up, lq, uq;
+  D(jp, lp, up);
+  D(jq, lq, uq);
+  const bool ip = P.isint[jp] != 0, iq = P.isint[jq] != 0;
+  const bool bp = ip && lp >= 0.0 && up <= 1.0, bq = iq && lq >= 0.0 && uq <= 1.0;
+  if (bp != bq) return bp;
+  if (bp && sorted) {
+    const long long a1 = absBitsOf(P.vals[p]), a2 = absBitsOf(P.vals[q]);
+    if (a1 != a2) return a1 > a2;
+    return jp < jq;
+  }
+  if (ip != iq) return ip;
+  if (!ip || !sorted) return jp < jq;
+  const double kp = fabs(P.vals[p] * (up - lp)), kq = fabs(P.vals[q] * (uq - lq));
+  if (kp != kq) return kp > kq;
+  return jp < jq;
+}
+
+// writes row i's order to P.rperm[p0 ..) by a bottom-up merge sort through P.rtmp (one thread)
+template <class DOM>
+__device__ void rowOrder(const Prob& P, const DOM& D, bool sorted, int i) {
+  const int64_t p0 = P.rowptr[i];
+  const int len = (int)(P.rowptr[i + 1] - p0);
+  int32_t* src = P.rperm + p0;
+  int32_t* dst = P.rtmp + p0;
+  for (int k = 0; k < len; ++k) src[k] = k;
+  for (int w = 1; w < len; w *= 2) {
+    for (int lo = 0; lo < len; lo += 2 * w) {
+      const int mid = min(lo + w, len), hi = min(lo + 2 * w, len);
+      int x = lo, y = mid;
+      for (int k = lo; k < hi; ++k) {
+        if (y >= hi || (x < mid && !entryBefore(P, D, sorted, p0 + src[y], p0 + src[x]))) dst[k] = src[x++];
+        else dst[k] = src[y++];
+      }
+    }
+    int32_t* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (src != P.rperm + p0)
+    for (int k = 0; k < len; ++k) P.rperm[p0 + k] = src[k];
+}
+
+// (SCIP_Longint)(REALABS(val) + feastol), cons_linear.c:5903/5944/6057, saturated where the cast would overflow
+__device__ __forceinline__ long long coefInt(const Num& s, double v) {
+  const double x = fabs(v) + s.feastol;
+  return x >= 4.0e18 ? 4000000000000000000LL : (long long)x;
+}
+// greatest common divisor of positive integers (the value SCIPcalcGreComDiv, misc.c:9197, computes)
+__device__ __forceinline__ long long gcd64(long long a, long long b) {
+  while (b != 0) {
+    const long long t = a % b;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+__device__ __forceinline__ bool epsIntegral(const Num& s, double x) { return x - floor(x + s.eps) <= s.eps; }
+__device__ __forceinline__ double epsFloor(const Num& s, double x) { return floor(x + s.eps); }
+__device__ __forceinline__ double epsCeil(const Num& s, double x) { return ceil(x - s.eps); }
+
+// each solution-enumeration loop runs at most this often; a row that needs more yields no deduction
+constexpr long long RANGED_MAXIT = 1LL << 20;
+// the running gcd of the partition changes at most 62 times (it at least halves each time)
+constexpr int RANGED_MAXCHG = 64;
+
+// Row i's ranged-row deductions from the bounds B (forced candidates, as SCIP's come with force = TRUE);
+// returns true on cutoff.  One thread.
+template <class BND>
+__device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+  const int64_t p0 = P.rowptr[i];
+  const int len = (int)(P.rowptr[i + 1] - p0);
+  if (P.rlive) {
+    auto dom = [&](int j, double& l, double& u) { B.glob(P, j, l, u); };
+    rowOrder(P, dom, P.rsorted != 0, i);
+  }
+  const int32_t* ord = P.rperm + p0;
+  auto fixedAt = [&](int k, int64_t& p, int& j, double& v, double& l, double& u) {
+    p = p0 + ord[k];
+    j = P.colidx[p];
+    v = P.vals[p];
+    B.get(j, l, u);
+    return eq(s, l, u);
+  };
+  auto qual = [&](int j, double v) { return P.isint[j] != 0 && epsIntegral(s, v) && !eq(s, fabs(v), 1.0); };
+
+  // fixed activity, last entry first (cons_linear.c:5803-5814)
+  double fixedact = 0.0;
+  int nfixed = 0;
+  for (int k = len - 1; k >= 0; --k) {
+    int64_t p;
+    int j;
+    double v, l, u;
+    if (fixedAt(k, p, j, v, l, u)) {
+      fixedact += l * v;
+      ++nfixed;
+    }
+  }
+  if (isHuge(s, fabs(fixedact))) return false;
+  const double lhs = P.lhs[i] - fixedact, rhs = P.rhs[i] - fixedact;
+
+  // partition (cons_linear.c:5839-5958); membership of position k is recomputed from the running gcd, whose
+  // changes are recorded as (position, gcd after it)
+  int ninf = 0, ncont = 0, first = -1, kstart;
+  bool gcdisone = true, possiblegcd = true;
+  int k = -1;
+  bool fx;
+  do {
+    ++k;
+    while (k < len) {
+      int64_t p;
+      int j;
+      double v, l, u;
+      fx = fixedAt(k, p, j, v, l, u);
+      if (qual(j, v)) break;
+      if (!fx) {
+        if (P.isint[j] == 0) ++ncont;
+        gcdisone = gcdisone && eq(s, fabs(v), 1.0);
+        possiblegcd = false;
+        ++ninf;
+        if (first < 0) first = k;
+      }
+      ++k;
+    }
+    if (k >= len) break;
+    {
+      int64_t p;
+      int j;
+      double v, l, u;
+      fx = fixedAt(k, p, j, v, l, u);
+    }
+  } while (fx);
+  if (k >= len || ncont + 2 > len - nfixed) return false;
+  kstart = k;
+  long long g0;
+  {
+    int64_t p;
+    int j;
+    double v, l, u;
+    fixedAt(k, p, j, v, l, u);
+    g0 = coefInt(s, v);
+  }
+  int chgpos[RANGED_MAXCHG];
+  long long chgval[RANGED_MAXCHG];
+  int nchg = 0;
+  long long gcd = g0;
+  for (; k < len; ++k) {
+    int64_t p;
+    int j;
+    double v, l, u;
+    if (fixedAt(k, p, j, v, l, u)) continue;
+    if (!qual(j, v)) {
+      if (P.isint[j] == 0) ++ncont;
+      gcdisone = gcdisone && eq(s, fabs(v), 1.0);
+      possiblegcd = false;
+      ++ninf;
+      if (first < 0) first = k;
+    } else {
+      const long long t = gcd64(gcd, coefInt(s, v));
+      if (t == 1) {
+        ++ninf;
+        if (first < 0) first = k;
+      } else if (t != gcd) {
+        if (nchg < RANGED_MAXCHG) {
+          chgpos[nchg] = k;
+          chgval[nchg] = t;
+          ++nchg;
+        }
+        gcd = t;
+      }
+    }
+  }
+  if (ninf == 0) return false;
+  // is position k (unfixed) one of the entries that may lead to infeasibility?
+  auto member = [&](int kk, int j, double v) {
+    if (kk < kstart || !qual(j, v)) return true;
+    long long gb = g0;
+    for (int t = 0; t < nchg && chgpos[t] < kk; ++t) gb = chgval[t];
+    return gcd64(gb, coefInt(s, v)) == 1;
+  };
+
+  // activity bounds of those entries, last first (cons_linear.c:5975-6015)
+  double minact = 0.0, maxact = 0.0;
+  for (k = len - 1; k >= 0; --k) {
+    int64_t p;
+    int j;
+    double v, l, u;
+    if (fixedAt(k, p, j, v, l, u) || !member(k, j, v)) continue;
+    bool mininv = false, maxinv = false;
+    if (isInf(s, -l)) {
+      if (v < 0.0) maxinv = true;
+      else mininv = true;
+    } else if (v < 0.0) {
+      maxact += v * l;
+    } else {
+      minact += v * l;
+    }
+    if (isInf(s, u)) {
+      if (v > 0.0) maxinv = true;
+      else mininv = true;
+    } else if (v > 0.0) {
+      maxact += v * u;
+    } else {
+      minact += v * u;
+    }
+    if (isHuge(s, -minact)) mininv = true;
+    if (isHuge(s, maxact)) maxinv = true;
+    if (mininv || maxinv) return false;
+  }
+
+  // no multiple of gcd between the sides (cons_linear.c:6033-6045)
+  const double g = (double)gcd;
+  if (!epsIntegral(s, (lhs - maxact) / g) && gt(s, epsCeil(s, (lhs - maxact) / g) * g, rhs - minact)) return true;
+  if (ncont != 0) return false;
+
+  // gcd of the other entries (cons_linear.c:6051-6064)
+  long long gcdinf = -1;
+  if (possiblegcd) {
+    for (k = len - 1; k >= 0; --k) {
+      int64_t p;
+      int j;
+      double v, l, u;
+      if (fixedAt(k, p, j, v, l, u) || !member(k, j, v)) continue;
+      gcdinf = gcdinf < 0 ? coefInt(s, v) : gcd64(gcdinf, coefInt(s, v));
+      if (gcdinf < 2) break;
+    }
+  } else if (gcdisone) {
+    gcdinf = 1;
+  }
+  if (gcdinf < 1) return false;
+
+  // feasible values of the other entries' activity (cons_linear.c:6076-6139)
+  double minvalue = 0.0, maxvalue = 0.0;
+  int nsols = 0;
+  double value = epsCeil(s, minact - s.feastol);
+  for (long long it = 0; le(s, value, maxact); ++it) {
+    if (it >= RANGED_MAXIT) return false;
+    double value2 = value + g * epsCeil(s, (lhs - value) / g);
+    if (!ge(s, value2, lhs)) value2 += g;
+    if (le(s, value2, rhs)) {
+      ++nsols;
+      if (nsols == 3) break;
+      if (nsols == 1) minvalue = value;
+      maxvalue = value;
+    }
+    value += (double)gcdinf;
+  }
+  if (nsols == 3) {
+    value = epsFloor(s, maxact + s.feastol);
+    for (long long it = 0; ge(s, value, minact); ++it) {
+      if (it >= RANGED_MAXIT) return false;
+      double value2 = value + g * epsFloor(s, (rhs - value) / g);
+      if (!le(s, value2, rhs)) value2 -= g;
+      if (ge(s, value2, lhs)) {
+        maxvalue = value;
+        break;
+      }
+      value -= (double)gcdinf;
+    }
+  }
+  if (nsols == 0) return true;
+
+  int target = -1;
+  if (ninf == 1) {
+    target = first;  // the single other entry (fixed :6160-6183, bounded :6296-6352)
+  } else if (ninf == len - nfixed - 1) {
+    // the one unfixed entry outside them (fixed :6184-6283, bounded :6354-6552)
+    for (k = 0; k < len; ++k) {
+      int64_t p;
+      int j;
+      double v, l, u;
+      if (!fixedAt(k, p, j, v, l, u) && !member(k, j, v)) {
+        target = k;
+        break;
+      }
+    }
+  }
+  if (target < 0) return false;
+  int64_t p;
+  int j;
+  double v, l, u;
+  fixedAt(target, p, j, v, l, u);
+  double newlb, newub;
+  bool fix = nsols == 1;
+  if (ninf == 1) {
+    if (fix) {
+      newlb = newub = maxvalue / v;
+    } else {
+      newlb = v < 0.0 ? maxvalue / v : minvalue / v;
+      newub = v < 0.0 ? minvalue / v : maxvalue / v;
+    }
+  } else if (fix) {
+    newlb = newub = v < 0.0 ? epsFloor(s, (lhs - maxvalue) / v) : epsCeil(s, (lhs - maxvalue) / v);
+  } else {
+    newlb = v < 0.0 ? epsFloor(s, (rhs - minvalue) / v) : epsCeil(s, (lhs - maxvalue) / v);
+    newub = v < 0.0 ? epsFloor(s, (lhs - maxvalue) / v) : epsCeil(s, (rhs - minvalue) / v);
+  }
+  const EmitTo emit{&C, j, &st.cands};
+  if (fix || newlb > l) emit(false, newlb, true);
+  if (fix || newub < u) emit(true, newub, true);
+  return false;
+}
+
 // The CTA processes rows[0..nrows) (all <= LONGROW entries).  All threads of the CTA must call it with the
 // same arguments.  Sets *cut on infeasibility.
 template <int NT, class BND>
@@ -910,6 +1236,14 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
                          relres);
       }
     }
+    // ranged rows of the batch, one thread each, after the activity rules (propagateCons,
+    // cons_linear.c:7694-7711); a batch that found the problem infeasible has nothing left to add
+    if (P.relig != nullptr && *cut == 0) {
+      for (int o = tid; o < cnt; o += NT) {
+        const int i = rb.order[o];
+        if (P.relig[i] != 0 && !rowDead(P, i) && rangedRow(s, P, B, i, C, st)) cutRow(P, i, cut);
+      }
+    }
     __syncthreads();
   }
 }
@@ -918,7 +1252,7 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
 // 32 partials are merged pairwise (k absorbs k+16, k+8, ..., k+1) -- the same order the oracle uses.
 // Returns true (on every lane) on cutoff.
 template <class BND>
-__device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+__device__ bool rowWarpCore(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
   const int lane = threadIdx.x & 31;
   const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
   const double lhs = P.lhs[i], rhs = P.rhs[i];
@@ -1113,6 +1447,16 @@ __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands&
     columnCandidates(s, a, lhs, rhs, easy, false, v, l, u, true, EmitTo{&C, j, &st.cands}, relres);
   }
   return false;
+}
+
+// the activity rules of a long row, then (lane 0) its ranged-row rule; true on every lane on cutoff
+template <class BND>
+__device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
+  if (rowWarpCore(s, P, B, i, C, st)) return true;
+  if (P.relig == nullptr || P.relig[i] == 0) return false;
+  bool cut = false;
+  if ((threadIdx.x & 31) == 0) cut = rangedRow(s, P, B, i, C, st);
+  return __shfl_sync(0xffffffffu, cut ? 1 : 0, 0) != 0;
 }
 
 // Acceptance of column j's best candidates against its round-start bounds [l,u]: upper bound first

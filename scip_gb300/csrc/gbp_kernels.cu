@@ -376,6 +376,36 @@ __global__ void k_fix_parts(int64_t ninst, const int64_t* off, int64_t m, int64_
   }
 }
 
+// Ranged rows: the rows the gcd rule can act on -- three or more entries, both sides finite, and an integral
+// column with an integral coefficient other than +-1 (rangedRowPropagation returns at once for any other row,
+// cons_linear.c:5770-5777, :5839-5869) -- flagged and compacted into list (any order).
+__global__ void k_ranged_elig(Num s, Prob P, uint8_t* elig, int* list, int* count) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.m; i += stride) {
+    const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+    bool ok = p1 - p0 >= 3 && !isInf(s, -P.lhs[i]) && !isInf(s, P.rhs[i]);
+    if (ok) {
+      ok = false;
+      for (int64_t p = p0; p < p1 && !ok; ++p) {
+        const double v = P.vals[p];
+        ok = P.isint[P.colidx[p]] != 0 && epsIntegral(s, v) && !eq(s, fabs(v), 1.0);
+      }
+    }
+    elig[i] = ok ? 1 : 0;
+    if (ok) list[atomicAdd(count, 1)] = (int)i;
+  }
+}
+
+// the entry order of the listed rows on a global domain fixed for the call (one thread per row)
+__global__ void k_ranged_order(Prob P, const int* list, int n, const double* dl, const double* du, int sorted) {
+  auto dom = [&](int j, double& l, double& u) {
+    l = dl[j];
+    u = du[j];
+  };
+  const int stride = gridDim.x * blockDim.x;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) rowOrder(P, dom, sorted != 0, list[t]);
+}
+
 // rows of instance k may only reference columns of instance k
 __global__ void k_check_blocks(int64_t m, const int64_t* rowptr, const int32_t* colidx, const int32_t* rowinst,
                                const int32_t* colinst, int* bad) {
@@ -637,6 +667,17 @@ __global__ void __launch_bounds__(256) k_order_scatter(int64_t nnodes, const int
 }
 
 // ------------------------------------------------------------------------------------------ launchers
+cudaError_t launchRangedElig(cudaStream_t st, int grid, const Num& s, const Prob& P, uint8_t* elig, int* list,
+                             int* count) {
+  k_ranged_elig<<<grid, 256, 0, st>>>(s, P, elig, list, count);
+  return cudaGetLastError();
+}
+cudaError_t launchRangedOrder(cudaStream_t st, int grid, const Prob& P, const int* list, int n, const double* dl,
+                              const double* du, int sorted) {
+  if (n <= 0) return cudaSuccess;
+  k_ranged_order<<<grid, 128, 0, st>>>(P, list, n, dl, du, sorted);
+  return cudaGetLastError();
+}
 cudaError_t launchFixParts(cudaStream_t st, int grid, int64_t ninst, const int64_t* off, int64_t m, int64_t n,
                            int64_t nnz, int64_t* rowptr, int32_t* colidx, int32_t* rowinst, int32_t* colinst, int* bad) {
   k_fix_parts<<<grid, 256, 0, st>>>(ninst, off, m, n, nnz, rowptr, colidx, rowinst, colinst, bad);

@@ -73,6 +73,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
                                            double* out_lb, double* out_ub, int64_t out_cap, const gbp_params* params,
                                            void* stream, gbp_result* res) {
   if (m < 0 || n < 0 || nnodes < 0 || out_cap < 0) return GBP_ERR_INVALID;
+  if (params && (params->flags & GBP_FLAG_RANGEDROW)) return GBP_ERR_INVALID;  // needs a context's row order
   if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1 || nnodes >= (int64_t(1) << 31) - 1)
     return GBP_ERR_TOO_LARGE;
   if (nnodes == 0) {

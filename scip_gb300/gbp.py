@@ -28,6 +28,7 @@ GBP_ERR_STATE = -7
 GBP_ERR_TOO_LARGE = -8
 GBP_FLAG_HOSTLOOP = 1
 GBP_FLAG_NOSORTVARS = 2
+GBP_FLAG_RANGEDROW = 4
 
 # every symbol include/gbp.h declares (checked by the CPU test suite)
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
@@ -107,7 +108,8 @@ def load_library(path: Optional[str] = None):
     return L
 
 
-def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars: bool = True) -> GbpParams:
+def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars: bool = True,
+                   ranged: bool = False) -> GbpParams:
     p = GbpParams()
     load_library().gbp_default_params(ctypes.byref(p))
     if maxeasy is not None:
@@ -115,6 +117,8 @@ def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars
     p.maxrounds = maxrounds
     if not sortvars:
         p.flags |= GBP_FLAG_NOSORTVARS
+    if ranged:
+        p.flags |= GBP_FLAG_RANGEDROW
     return p
 
 

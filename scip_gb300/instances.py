@@ -263,6 +263,51 @@ def indicator_packing(rng: np.random.Generator, m: int, n: int, kmin: int = 4, k
                     name=f"indicator_packing({m}x{n})", x0=np.zeros(n))
 
 
+def gcd_rows(rng: np.random.Generator, m: int, n: int, long_frac: float = 0.0, equations: bool = True) -> Instance:
+    """Ranged rows and equations whose integer part shares a divisor: sum_k g*c_k*x_k + (other entries) in
+    [lhs, rhs] with g in {2, 3, 4, 5, 6, 7, 10, 12} per row and |c_k| in 1..4; about 1.5 other entries per row
+    carry +-1, 2, +-3 or 1.5.  The first 10 % of the columns are binary, the last 5 % continuous.  The sides come from a feasible point with a
+    range narrower than g (half of the rows are equations), so the other entries' activity is confined to one
+    residue class modulo g -- the case rangedRowPropagation (cons_linear.c:5715-6695) works on.  Rows have 3..8
+    entries, or 65..200 for a long_frac share; general integer columns lie in [0, U] with U in 2..10.
+
+    With equations=False every row is ranged, with sides a quarter off the half-integral activities: a residual
+    activity then never equals a side, so tightenVarBounds' minres/rhs != 1 guard (cons_linear.c:6766), which
+    makes the fixpoint depend on the order rows are visited in, never blocks a deduction."""
+    lengths = rng.integers(3, 9, size=m)
+    if long_frac > 0:
+        big = rng.random(m) < long_frac
+        lengths[big] = rng.integers(65, 201, size=int(big.sum()))
+    lengths = np.minimum(lengths, n)
+    rowptr, colidx = _distinct_columns(rng, lengths, n)
+    nnz = colidx.shape[0]
+    g = rng.choice([2, 3, 4, 5, 6, 7, 10, 12], size=m)
+    gp = np.repeat(g, lengths).astype(np.float64)
+    c = rng.integers(1, 5, size=nnz) * np.where(rng.random(nnz) < 0.5, -1, 1)
+    vals = gp * c
+    other = rng.random(nnz) < 1.5 / np.repeat(lengths, lengths)
+    vals[other] = rng.choice([1.0, -1.0, 2.0, -3.0, 3.0, 1.5], size=int(other.sum()))
+    # columns by type -- binaries, general integers, continuous -- so that SCIP's variable indices (it keeps its
+    # variables sorted by type, prob.c:887) follow the column order, on which the order ties are broken here
+    nb, nc = n // 10, n // 20
+    isint = (np.arange(n) < n - nc).astype(np.int8)
+    ub = np.concatenate([np.ones(nb), rng.integers(2, 11, size=n - nb - nc).astype(np.float64), np.full(nc, 10.0)])
+    lb = np.zeros(n)
+    x0 = np.where(isint == 1, np.floor(rng.random(n) * (ub + 1)), rng.uniform(0.0, 10.0, size=n))
+    rows = np.repeat(np.arange(m), lengths)
+    act = np.bincount(rows, weights=vals * x0[colidx], minlength=m)
+    r1 = np.floor(rng.random(m) * (g - 1))
+    r2 = np.floor(rng.random(m) * (g - 1 - r1))
+    if equations:
+        eq = rng.random(m) < 0.5
+        r1[eq] = 0.0
+        r2[eq] = 0.0
+    else:
+        r1 += 0.25
+        r2 += 0.25
+    return Instance(rowptr, colidx, vals, act - r1, act + r2, lb, ub, isint, name=f"gcd_rows({m}x{n})", x0=x0)
+
+
 def multi_knapsack(rng: np.random.Generator, m: int, n: int) -> Instance:
     """Multi-knapsack: integer columns in [0,5], weights U{1..100}, capacity 40 % of the row's max activity."""
     lengths = np.minimum(rng.integers(5, 41, size=m), n)

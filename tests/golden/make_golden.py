@@ -12,6 +12,12 @@ SCIP's per-node cutoff verdicts and changed bounds.  Cases:
   set_cover / knapsack / network   one small instance of each uneven-batch family + 100 nodes
   indicator_packing          2,000 x 4,000 binary packing rows with an indicator (3 % of rows 65..300 long)
                              + 300 nodes: SCIP's binary skip in tightenBounds decides many of them
+  ranged/gcd_rows_indep      3,000 ranged rows over 60,000 columns (rows rarely share a column; 5 % of rows
+                             65..200 long) whose integer part shares a divisor: SCIP's root with ranged-row
+                             propagation on (rangedrowartcons off), sortvars off and on
+  ranged/gcd_rows_shared     2,000 rows over 8,000 columns, half of them equations, the same settings
+  ranged/tiny_cutoffs        60 instances of 12 rows whose equations were shifted off their feasible residue, so
+                             that the ranged rule finds many of them infeasible (concatenated, with offsets)
 
 Usage: python tests/golden/make_golden.py [case ...]   (needs the SCIP sources; writes tests/golden/*.npz;
 no argument builds every case)
@@ -69,6 +75,66 @@ def save_case(name, inst, nnodes=0, node_seed=11):
     print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {nnodes} nodes, {os.path.getsize(path) // 1024} KiB")
 
 
+def save_ranged_case(name, inst):
+    """SCIP's root fixpoint with ranged-row propagation, for sortvars off ("nosort") and on ("sort") and both
+    rules, under tests/golden/ranged (kept apart from the cases above, whose tests run with the rule off)."""
+    out = {"rowptr": inst.rowptr, "colidx": inst.colidx, "vals": inst.vals, "lhs": inst.lhs, "rhs": inst.rhs,
+           "lb": inst.lb, "ub": inst.ub, "isint": inst.isint}
+    for sortvars in (False, True):
+        for easy in (False, True):
+            tag = ("sort" if sortvars else "nosort") + ("_easy" if easy else "_res")
+            rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy, ranged=True, sortvars=sortvars)
+            out[f"{tag}_rootcut"] = np.int8(rcut)
+            out[f"{tag}_rootlb"] = rlb
+            out[f"{tag}_rootub"] = rub
+    os.makedirs(os.path.join(HERE, "ranged"), exist_ok=True)
+    path = os.path.join(HERE, "ranged", f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {os.path.getsize(path) // 1024} KiB")
+
+
+def tiny_cutoff_instances():
+    rng = np.random.default_rng(np.random.PCG64(32))
+    out = []
+    for _ in range(60):
+        inst = instances.gcd_rows(rng, 12, 40, equations=True)
+        shift = rng.integers(0, 3, size=inst.m).astype(np.float64)
+        inst.lhs = inst.lhs + shift
+        inst.rhs = inst.rhs + shift
+        out.append(inst)
+    return out
+
+
+def save_tiny_cutoffs():
+    insts = tiny_cutoff_instances()
+    big, row_off, col_off = instances.concat_instances(insts)
+    out = {"rowptr": big.rowptr, "colidx": big.colidx, "vals": big.vals, "lhs": big.lhs, "rhs": big.rhs,
+           "lb": big.lb, "ub": big.ub, "isint": big.isint, "row_off": row_off, "col_off": col_off}
+    for sortvars in (False, True):
+        tag = "sort" if sortvars else "nosort"
+        cut = np.zeros(len(insts), dtype=np.int8)
+        lb = np.empty(big.n)
+        ub = np.empty(big.n)
+        for k, inst in enumerate(insts):
+            c, l, u, _ = oracle.run_scip(inst, ranged=True, sortvars=sortvars)
+            cut[k] = c
+            lb[col_off[k]:col_off[k + 1]] = l
+            ub[col_off[k]:col_off[k + 1]] = u
+        out[f"{tag}_cut"], out[f"{tag}_lb"], out[f"{tag}_ub"] = cut, lb, ub
+    path = os.path.join(HERE, "ranged", "tiny_cutoffs.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {len(insts)} instances, {int(out['sort_cut'].sum())} infeasible (sortvars)")
+
+
+def ranged_cases():
+    return {
+        "gcd_rows_indep": lambda: instances.gcd_rows(np.random.default_rng(np.random.PCG64(30)), 3000, 60000,
+                                                     long_frac=0.05, equations=False),
+        "gcd_rows_shared": lambda: instances.gcd_rows(np.random.default_rng(np.random.PCG64(31)), 2000, 8000,
+                                                      long_frac=0.03, equations=True),
+    }
+
+
 def cases():
     """name -> (instance builder, nodes); the uneven-family cases share one generator, drawn in this order."""
     out = {}
@@ -97,7 +163,14 @@ def main(names):
     if not os.path.exists(oracle.SCIP_ORACLE):
         raise SystemExit("oracle/_ref/scip_oracle missing: run `make -C oracle ref` where the SCIP sources are")
     all_cases = cases()
-    for name in names or list(all_cases):
+    ranged = ranged_cases()
+    for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs"]:
+        if name == "ranged/tiny_cutoffs":
+            save_tiny_cutoffs()
+            continue
+        if name.startswith("ranged/"):
+            save_ranged_case(name[len("ranged/"):], ranged[name[len("ranged/"):]]())
+            continue
         make, nnodes = all_cases[name]
         save_case(name, make(), nnodes=nnodes)
 
