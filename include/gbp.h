@@ -139,6 +139,12 @@ int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity);
 /* the last call's log sorted by (round, column): up to cap entries into col/round/lb/ub (host arrays), *n = the
  * number of changes the call made.  GBP_ERR_OVERFLOW if the log capacity or cap was smaller than *n. */
 int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, double* lb, double* ub, int64_t* n);
+/* with GBP_FLAG_RANGEDROW, the rows whose ranged-row rule proposed bounds for a column (col) or found the row
+ * infeasible (col = -1) in the last call, with the round: up to cap records sorted by (round, col, row), *n = the
+ * number recorded.  Kept beside the change log (same capacity).  A change that no row's activities explain was
+ * proposed by one of these rows, whose other columns' bounds at that time imply it (cons_linear explains its
+ * ranged-row changes by the bounds of the row's fixed columns, addConflictFixedVars, cons_linear.c:4981). */
+int gbp_get_ranged_log(gbp_ctx* ctx, int64_t cap, int32_t* round, int32_t* col, int32_t* row, int64_t* n);
 
 /* ---------------------------------------------------------------- batched path: distinct instances
  * Uneven independent instances (each a set of linear rows with its own columns) propagated together: instance k

@@ -430,6 +430,7 @@ typedef struct
    /* ranged rows: on/off, and for the row being processed its propagation order (rord[k] = offset of the k-th
     * entry), merge scratch and gcd membership per order position */
    int ranged;
+   int32_t round;       /* the round being processed (ranged-row records) */
    double* startlb;     /* the bounds the call started from (sortvars off, no global domain), else NULL */
    double* startub;
    int32_t* rord;
@@ -709,6 +710,20 @@ static double epsCeil(const Num* s, double x) { return ceil(x - s->eps); }      
  * that needs more (its residual activity range spans over a million steps) yields no deduction */
 #define RANGED_MAXIT (1 << 20)
 
+static void logRanged(Work* w, int64_t row, int32_t col)
+{
+   lpo_log* g = w->log;
+   if( g == NULL || g->rrow == NULL )
+      return;
+   if( g->rn < g->rcap )
+   {
+      g->rrow[g->rn] = (int32_t)row;
+      g->rcol[g->rn] = col;
+      g->rround[g->rn] = w->round;
+   }
+   g->rn++;
+}
+
 /* rangedRowPropagation for frontier row i from the round-start bounds; bound changes become forced
  * candidates (SCIPinferVarFixCons / SCIPinferVarLb/UbCons with force = TRUE).  Returns 1 on cutoff. */
 static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo_result* res)
@@ -878,7 +893,10 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
    /* no multiple of gcd between the sides (cons_linear.c:6033-6045) */
    g = (double)gcd;
    if( !isIntegral(s, (lhs - maxact) / g) && gt(s, epsCeil(s, (lhs - maxact) / g) * g, rhs - minact) )
+   {
+      logRanged(w, i, -1);
       return 1;
+   }
    if( ncont != 0 )
       return 0;
 
@@ -941,7 +959,10 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
       }
    }
    if( nsols == 0 )
+   {
+      logRanged(w, i, -1);
       return 1;
+   }
 
    if( ninf == 1 )
    {
@@ -954,6 +975,7 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
          candLb(w, j, maxvalue / v, 1);
          candUb(w, j, maxvalue / v, 1);
          res->candidates += 2;
+         logRanged(w, i, j);
       }
       else
       {
@@ -969,6 +991,8 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
             candUb(w, j, newub, 1);
             res->candidates++;
          }
+         if( newlb > lb[j] || newub < ub[j] )
+            logRanged(w, i, j);
       }
    }
    else if( ninf == len - nfixed - 1 )
@@ -993,6 +1017,7 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
          candLb(w, j, bound, 1);
          candUb(w, j, bound, 1);
          res->candidates += 2;
+         logRanged(w, i, j);
       }
       else
       {
@@ -1008,6 +1033,8 @@ static int rangedRow(Work* w, const double* lb, const double* ub, int64_t i, lpo
             candUb(w, j, newub, 1);
             res->candidates++;
          }
+         if( newlb > lb[j] || newub < ub[j] )
+            logRanged(w, i, j);
       }
    }
 #undef RPOS
@@ -1342,6 +1369,7 @@ static int fixpoint(Work* w, double* lb, double* ub, lpo_result* res, int track)
       w->nfront = w->nnext;
       w->nnext = 0;
       res->rounds = round + 1;
+      w->round = round;
 
       w->ntouched = 0;
       for( k = 0; k < w->nfront; ++k )
@@ -1434,7 +1462,10 @@ int lpo_propagate_logged(const lpo_problem* prob, const lpo_params* par, double*
    }
 
    if( log != NULL )
+   {
       log->n = 0;
+      log->rn = 0;
+   }
    newStamp(&w);
    w.nnext = 0;
    if( seedcols == NULL )

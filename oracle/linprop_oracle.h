@@ -87,7 +87,10 @@ int lpo_propagate(const lpo_problem* prob, const lpo_params* par, double* lb, do
    const double* gub, lpo_result* res);
 
 /* change log: every accepted bound change with the round that made it and the column's bounds after it,
- * entries grouped by round in the order they are accepted; n counts all changes, at most cap are stored */
+ * entries grouped by round in the order they are accepted; n counts all changes, at most cap are stored.
+ * With LPO_FLAG_RANGEDROW also the ranged-row records: each row whose ranged rule proposed bounds for a column
+ * (rcol) or found itself infeasible (rcol = -1), with the round; rn counts them, at most rcap are stored
+ * (rrow NULL: not recorded) */
 typedef struct
 {
    int64_t cap;
@@ -96,6 +99,11 @@ typedef struct
    int32_t* round;
    double* lb;
    double* ub;
+   int64_t rcap;
+   int64_t rn;
+   int32_t* rrow;
+   int32_t* rcol;
+   int32_t* rround;
 } lpo_log;
 
 /* lpo_propagate that also fills *log (log may be NULL) */

@@ -36,7 +36,8 @@ FLAG_RANGEDROW = 2
 
 
 class Log(ctypes.Structure):
-    _fields_ = [("cap", ctypes.c_int64), ("n", ctypes.c_int64), ("col", _P), ("round", _P), ("lb", _P), ("ub", _P)]
+    _fields_ = [("cap", ctypes.c_int64), ("n", ctypes.c_int64), ("col", _P), ("round", _P), ("lb", _P), ("ub", _P),
+                ("rcap", ctypes.c_int64), ("rn", ctypes.c_int64), ("rrow", _P), ("rcol", _P), ("rround", _P)]
 
 
 class Problem(ctypes.Structure):
@@ -151,7 +152,8 @@ class Oracle:
         cap = cap or 8 * self.inst.n + 1024
         col, rnd = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
         llb, lub = np.zeros(cap), np.zeros(cap)
-        log = Log(cap, 0, _ptr(col), _ptr(rnd), _ptr(llb), _ptr(lub))
+        rrow, rcol, rrnd = np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+        log = Log(cap, 0, _ptr(col), _ptr(rnd), _ptr(llb), _ptr(lub), cap, 0, _ptr(rrow), _ptr(rcol), _ptr(rrnd))
         res = Result()
         glb = gub = None
         if glob is not None:
@@ -165,10 +167,14 @@ class Oracle:
             args = (len(cols), _ptr(cols), _ptr(olb), _ptr(oub))
         lib().lpo_propagate_logged(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), *args, _ptr(glb),
                                    _ptr(gub), ctypes.byref(res), ctypes.byref(log))
-        if log.n > cap:
+        if log.n > cap or log.rn > cap:
             raise MemoryError("oracle change log capacity exceeded")
         n = log.n
         o = np.lexsort((col[:n], rnd[:n]))
+        r = log.rn
+        q = np.lexsort((rrow[:r], rcol[:r], rrnd[:r]))
+        # the ranged-row records, sorted by (round, column, row)
+        self.last_ranged = (rrnd[:r][q], rcol[:r][q], rrow[:r][q])
         return lb, ub, res, (col[:n][o], rnd[:n][o], llb[:n][o], lub[:n][o])
 
     def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1):

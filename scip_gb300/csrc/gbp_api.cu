@@ -38,9 +38,11 @@ struct gbp_ctx {
   int8_t* d_isint = nullptr;
   int64_t* d_colptr = nullptr;
   uint32_t* d_cscrow = nullptr;
-  // change log of the plain path (gbp_set_change_log): device arrays and the entry counter
+  // change log of the plain path (gbp_set_change_log): device arrays and the entry counter, and the ranged-row
+  // records kept beside it (same capacity)
   ChangeLog log{};
   int64_t log_cap = 0;
+  RangedLog rlog{};
   // explicit global bounds of the plain path (gbp_set_global_bounds)
   bool has_global = false;
   double* d_glb = nullptr;
@@ -294,7 +296,8 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->d_next_item) cudaFree(ctx->d_next_item);
   if (ctx->d_orderhist) cudaFree(ctx->d_orderhist);
   {
-    void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub};
+    void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub,
+                  ctx->rlog.n, ctx->rlog.row, ctx->rlog.col, ctx->rlog.round};
     for (void* p : lp)
       if (p) cudaFree(p);
   }
@@ -498,7 +501,7 @@ int gbp_upload_problem(gbp_ctx* ctx, int64_t m, int64_t n, const int64_t* rowptr
 static Cands plainCands(gbp_ctx* ctx) {
   const size_t n = (size_t)ctx->cap_n;
   return Cands{ctx->d_cand, ctx->d_cand + n, ctx->d_cand + 2 * n, ctx->d_cand + 3 * n, ctx->d_cflag,
-               ctx->d_touched, ctx->d_ctr + 4};
+               ctx->d_touched, ctx->d_ctr + 4, ctx->rlog, 0};
 }
 
 static int nextStamp(gbp_ctx* ctx) {
@@ -610,6 +613,7 @@ static int propagateGraph(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, c
   hs.ub = ub;
   hs.log = ctx->log;
   if (ctx->log.n) CK(cudaMemsetAsync(ctx->log.n, 0, sizeof(int), ctx->stream));
+  if (ctx->rlog.n) CK(cudaMemsetAsync(ctx->rlog.n, 0, sizeof(int), ctx->stream));
   int seedstamp = 0;
   if (nseed < 0) {
     hs.cur = 2;
@@ -694,6 +698,7 @@ static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed
   CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, 8 * sizeof(int), ctx->stream));
   if (ctx->log.n) CK(cudaMemsetAsync(ctx->log.n, 0, sizeof(int), ctx->stream));
+  if (ctx->rlog.n) CK(cudaMemsetAsync(ctx->rlog.n, 0, sizeof(int), ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
 
   int* cur = nullptr;
@@ -735,6 +740,7 @@ static int propagateHostLoop(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed
     CK(cudaMemsetAsync(ctx->d_ctr + nxt, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->d_ctr + 2 + nxt, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->d_ctr + 4, 0, sizeof(int), ctx->stream));
+    C.round = rounds;
     if (ns > 0) {
       CK(launchRowsShort(ctx->stream, gridFor(ctx, ns, 128), s, P, lb, ub, cur, ctx->d_ctr + curidx, C, ctx->d_ctr + 5,
                          ctx->d_stats));
@@ -901,10 +907,13 @@ int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity) {
   if (!ctx || capacity < 0 || capacity >= (int64_t(1) << 31)) return fail(ctx, GBP_ERR_INVALID, "bad log capacity");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub};
+  destroyGraphs(ctx);  // the graphs hold the ranged-row records' pointers
+  void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub,
+                ctx->rlog.n, ctx->rlog.row, ctx->rlog.col, ctx->rlog.round};
   for (void* p : lp)
     if (p) cudaFree(p);
   ctx->log = ChangeLog{};
+  ctx->rlog = RangedLog{};
   ctx->log_cap = 0;
   if (capacity == 0) return GBP_OK;
   ChangeLog G{};
@@ -916,7 +925,51 @@ int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity) {
   CK(cudaMalloc(&G.ub, capacity * sizeof(double)));
   CK(cudaMemset(G.n, 0, sizeof(int)));
   ctx->log = G;
+  RangedLog R{};
+  R.cap = capacity;
+  CK(cudaMalloc(&R.n, sizeof(int)));
+  CK(cudaMalloc(&R.row, capacity * sizeof(int32_t)));
+  CK(cudaMalloc(&R.col, capacity * sizeof(int32_t)));
+  CK(cudaMalloc(&R.round, capacity * sizeof(int32_t)));
+  CK(cudaMemset(R.n, 0, sizeof(int)));
+  ctx->rlog = R;
   ctx->log_cap = capacity;
+  return GBP_OK;
+}
+
+int gbp_get_ranged_log(gbp_ctx* ctx, int64_t cap, int32_t* round, int32_t* col, int32_t* row, int64_t* n) {
+  if (!ctx || !n || cap < 0 || (cap > 0 && (!round || !col || !row))) return fail(ctx, GBP_ERR_INVALID, "null argument");
+  *n = 0;
+  if (!ctx->rlog.n) return fail(ctx, GBP_ERR_STATE, "no change log (gbp_set_change_log)");
+  CK(cudaSetDevice(ctx->device));
+  int cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, ctx->rlog.n, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *n = cnt;
+  const int64_t have = std::min<int64_t>(cnt, ctx->log_cap);
+  std::vector<int32_t> w(have), c(have), r(have);
+  if (have > 0) {
+    CK(cudaMemcpyAsync(w.data(), ctx->rlog.round, have * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(c.data(), ctx->rlog.col, have * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(r.data(), ctx->rlog.row, have * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  // records in (round, column, row) order: the threads of a round append in any order
+  std::vector<int64_t> ord(have);
+  for (int64_t k = 0; k < have; ++k) ord[k] = k;
+  std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
+    if (w[a] != w[b]) return w[a] < w[b];
+    if (c[a] != c[b]) return c[a] < c[b];
+    return r[a] < r[b];
+  });
+  const int64_t out = std::min<int64_t>(have, cap);
+  for (int64_t k = 0; k < out; ++k) {
+    round[k] = w[ord[k]];
+    col[k] = c[ord[k]];
+    row[k] = r[ord[k]];
+  }
+  if (cnt > ctx->log_cap) return fail(ctx, GBP_ERR_OVERFLOW, "change log capacity exceeded");
+  if (cnt > cap) return fail(ctx, GBP_ERR_OVERFLOW, "output arrays too small for the ranged-row records");
   return GBP_OK;
 }
 

@@ -65,15 +65,36 @@ __device__ __forceinline__ void cutRow(const Prob& P, int i, int* cut) {
   else *cut = 1;
 }
 
+// Ranged-row records of the plain path (row null: off): each row whose ranged rule proposed bounds for a column
+// (col) or found itself infeasible (col -1), with the round -- the rows conflict analysis needs as reasons
+struct RangedLog {
+  int* n;          // records written (may exceed cap)
+  int64_t cap;
+  int32_t* row;
+  int32_t* col;
+  int32_t* round;
+};
+
 struct Cands {
   long long* cub;   // best non-forced upper bound candidate (key), KEY_NONE_UB when empty
   long long* clb;   // best non-forced lower bound candidate (key), KEY_NONE_LB when empty
-  long long* cubf;  // forced (single-entry row) candidates
+  long long* cubf;  // forced candidates (single-entry rows, ranged rows)
   long long* clbf;
   int* cflag;       // bit0 ub, bit1 ubf, bit2 lb, bit3 lbf; 0 when the column is untouched this round
   int* touched;     // list of touched columns
   int* ntouched;    // its length (global or shared counter)
+  RangedLog rlog;   // ranged-row records (plain path with a change log), else row == nullptr
+  int round;        // the round the candidates are for (ranged-row records)
 };
+__device__ __forceinline__ void logRanged(const Cands& C, int row, int col) {
+  if (C.rlog.row == nullptr) return;
+  const int k = atomicAdd(C.rlog.n, 1);
+  if (k < C.rlog.cap) {
+    C.rlog.row[k] = row;
+    C.rlog.col[k] = col;
+    C.rlog.round[k] = C.round;
+  }
+}
 
 struct Stats {
   long long rows, nnz, cands, live;  // live: rows that passed the skip tests
@@ -951,7 +972,10 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
 
   // no multiple of gcd between the sides (cons_linear.c:6033-6045)
   const double g = (double)gcd;
-  if (!epsIntegral(s, (lhs - maxact) / g) && gt(s, epsCeil(s, (lhs - maxact) / g) * g, rhs - minact)) return true;
+  if (!epsIntegral(s, (lhs - maxact) / g) && gt(s, epsCeil(s, (lhs - maxact) / g) * g, rhs - minact)) {
+    logRanged(C, i, -1);
+    return true;
+  }
   if (ncont != 0) return false;
 
   // gcd of the other entries (cons_linear.c:6051-6064)
@@ -999,7 +1023,10 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
       value -= (double)gcdinf;
     }
   }
-  if (nsols == 0) return true;
+  if (nsols == 0) {
+    logRanged(C, i, -1);
+    return true;
+  }
 
   int target = -1;
   if (ninf == 1) {
@@ -1039,12 +1066,14 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   const EmitTo emit{&C, j, &st.cands};
   if (fix || newlb > l) emit(false, newlb, true);
   if (fix || newub < u) emit(true, newub, true);
+  if (fix || newlb > l || newub < u) logRanged(C, i, j);
   return false;
 }
 
 // The CTA processes rows[0..nrows) (all <= LONGROW entries).  All threads of the CTA must call it with the
 // same arguments.  Sets *cut on infeasibility.
-template <int NT, class BND>
+// RANGED: the ranged-row rule runs for rows that carry it (P.relig); false compiles it out
+template <int NT, bool RANGED = true, class BND>
 __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, const int* rows, int nrows, Cands& C,
                                  Stats& st, RowBatch<NT>& rb, int* cut) {
   const int tid = threadIdx.x;
@@ -1238,7 +1267,7 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
     }
     // ranged rows of the batch, one thread each, after the activity rules (propagateCons,
     // cons_linear.c:7694-7711); a batch that found the problem infeasible has nothing left to add
-    if (P.relig != nullptr && *cut == 0) {
+    if (RANGED && P.relig != nullptr && *cut == 0) {
       for (int o = tid; o < cnt; o += NT) {
         const int i = rb.order[o];
         if (P.relig[i] != 0 && !rowDead(P, i) && rangedRow(s, P, B, i, C, st)) cutRow(P, i, cut);
@@ -1450,10 +1479,10 @@ __device__ bool rowWarpCore(const Num& s, const Prob& P, const BND& B, int i, Ca
 }
 
 // the activity rules of a long row, then (lane 0) its ranged-row rule; true on every lane on cutoff
-template <class BND>
+template <bool RANGED = true, class BND>
 __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
   if (rowWarpCore(s, P, B, i, C, st)) return true;
-  if (P.relig == nullptr || P.relig[i] == 0) return false;
+  if (!RANGED || P.relig == nullptr || P.relig[i] == 0) return false;
   bool cut = false;
   if ((threadIdx.x & 31) == 0) cut = rangedRow(s, P, B, i, C, st);
   return __shfl_sync(0xffffffffu, cut ? 1 : 0, 0) != 0;

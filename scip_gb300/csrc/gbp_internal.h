@@ -125,6 +125,10 @@ cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n);
 cudaError_t launchNodes(cudaStream_t st, int grid, int threads, const NodesArgs& A);
 cudaError_t nodesOccupancy(int threads, int minblocks, int* blocksPerSm);
+// the node kernel with the ranged-row rule compiled in (gbp_nodes_ranged.cu); launchNodes picks it when the
+// problem carries ranged rows
+cudaError_t launchNodesRanged(cudaStream_t st, int grid, int threads, const NodesArgs& A);
+cudaError_t nodesOccupancyRanged(int threads, int minblocks, int* blocksPerSm);
 cudaError_t launchCscFlags(cudaStream_t st, int grid, int64_t nnz, const double* cvals, const int32_t* rowidx,
                            const double* lhs, const double* rhs, double inf, uint32_t* out);
 cudaError_t launchFill64(cudaStream_t st, int grid, long long* p, int64_t n, long long v);

@@ -36,7 +36,7 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
            "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log",
-           "gbp_upload_instance_list"]
+           "gbp_upload_instance_list", "gbp_get_ranged_log"]
 
 
 class GbpParams(ctypes.Structure):
@@ -92,6 +92,7 @@ def load_library(path: Optional[str] = None):
     L.gbp_set_global_bounds.argtypes = [_P, _P, _P]
     L.gbp_set_change_log.argtypes = [_P, ctypes.c_int64]
     L.gbp_get_change_log.argtypes = [_P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
+    L.gbp_get_ranged_log.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
     L.gbp_propagate_nodes.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                       ctypes.c_int64, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_nodes_device.argtypes = L.gbp_propagate_nodes.argtypes
@@ -302,6 +303,19 @@ class Propagator:
         ub = np.zeros(cap)
         self._check(self.L.gbp_get_change_log(self.h, cap, _ptr(col), _ptr(rnd), _ptr(lb), _ptr(ub), ctypes.byref(n)))
         return col[:n.value], rnd[:n.value], lb[:n.value], ub[:n.value]
+
+    def ranged_log(self, cap: Optional[int] = None):
+        """The last call's ranged-row records sorted by (round, column, row): (round, col, row) arrays."""
+        n = ctypes.c_int64(0)
+        if cap is None:
+            self._check(self.L.gbp_get_ranged_log(self.h, 0, None, None, None, ctypes.byref(n)),
+                        allow=(GBP_ERR_OVERFLOW,))
+            cap = n.value
+        rnd = np.zeros(cap, np.int32)
+        col = np.zeros(cap, np.int32)
+        row = np.zeros(cap, np.int32)
+        self._check(self.L.gbp_get_ranged_log(self.h, cap, _ptr(rnd), _ptr(col), _ptr(row), ctypes.byref(n)))
+        return rnd[:n.value], col[:n.value], row[:n.value]
 
     def set_global_bounds(self, glb=None, gub=None):
         """Global domain for the binary test of later propagate() calls (None: the propagated bounds, as at the

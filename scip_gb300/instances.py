@@ -263,7 +263,8 @@ def indicator_packing(rng: np.random.Generator, m: int, n: int, kmin: int = 4, k
                     name=f"indicator_packing({m}x{n})", x0=np.zeros(n))
 
 
-def gcd_rows(rng: np.random.Generator, m: int, n: int, long_frac: float = 0.0, equations: bool = True) -> Instance:
+def gcd_rows(rng: np.random.Generator, m: int, n: int, long_frac: float = 0.0, equations: bool = True,
+             continuous: bool = True) -> Instance:
     """Ranged rows and equations whose integer part shares a divisor: sum_k g*c_k*x_k + (other entries) in
     [lhs, rhs] with g in {2, 3, 4, 5, 6, 7, 10, 12} per row and |c_k| in 1..4; about 1.5 other entries per row
     carry +-1, 2, +-3 or 1.5.  The first 10 % of the columns are binary, the last 5 % continuous.  The sides come from a feasible point with a
@@ -273,7 +274,8 @@ def gcd_rows(rng: np.random.Generator, m: int, n: int, long_frac: float = 0.0, e
 
     With equations=False every row is ranged, with sides a quarter off the half-integral activities: a residual
     activity then never equals a side, so tightenVarBounds' minres/rhs != 1 guard (cons_linear.c:6766), which
-    makes the fixpoint depend on the order rows are visited in, never blocks a deduction."""
+    makes the fixpoint depend on the order rows are visited in, never blocks a deduction.  continuous=False makes
+    the last 5 % of the columns general integers in [0, 10] instead."""
     lengths = rng.integers(3, 9, size=m)
     if long_frac > 0:
         big = rng.random(m) < long_frac
@@ -290,7 +292,7 @@ def gcd_rows(rng: np.random.Generator, m: int, n: int, long_frac: float = 0.0, e
     # columns by type -- binaries, general integers, continuous -- so that SCIP's variable indices (it keeps its
     # variables sorted by type, prob.c:887) follow the column order, on which the order ties are broken here
     nb, nc = n // 10, n // 20
-    isint = (np.arange(n) < n - nc).astype(np.int8)
+    isint = (np.arange(n) < n - nc).astype(np.int8) if continuous else np.ones(n, dtype=np.int8)
     ub = np.concatenate([np.ones(nb), rng.integers(2, 11, size=n - nb - nc).astype(np.float64), np.full(nc, 10.0)])
     lb = np.zeros(n)
     x0 = np.where(isint == 1, np.floor(rng.random(n) * (ub + 1)), rng.uniform(0.0, 10.0, size=n))

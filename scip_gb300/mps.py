@@ -161,3 +161,66 @@ def read_mps(path: str) -> Instance:
     return Instance(rowptr, np.array(colidx, dtype=np.int32), np.array(vals, dtype=np.float64), lhs[keep].copy(),
                     rh[keep].copy(), np.array(lb, dtype=np.float64), np.array(ub, dtype=np.float64),
                     np.array(isint, dtype=np.int8), name=path.rsplit("/", 1)[-1])
+
+
+def write_mps(inst: Instance, path: str, obj=None, name: str = "INSTANCE") -> None:
+    """Writes inst (and an objective, default 0) as a free-format MPS file that read_mps and SCIP's reader read back
+    to the same rows, columns, integrality and bounds: rows with both sides finite and different become L rows
+    with a RANGES entry; integer columns go in one MARKER block and get explicit bounds (UP 1 alone for a [0, 1]
+    column, which keeps it binary)."""
+    m, n = inst.m, inst.n
+    obj = np.zeros(n) if obj is None else np.asarray(obj, dtype=np.float64)
+    rows = [f"r{i}" for i in range(m)]
+    cols = [f"x{j}" for j in range(n)]
+    kind, rhs, rngs = [], [], {}
+    for i in range(m):
+        lo, hi = inst.lhs[i], inst.rhs[i]
+        if lo <= -INF:
+            kind.append("L")
+            rhs.append(hi)
+        elif hi >= INF:
+            kind.append("G")
+            rhs.append(lo)
+        elif lo == hi:
+            kind.append("E")
+            rhs.append(hi)
+        else:
+            kind.append("L")
+            rhs.append(hi)
+            rngs[i] = hi - lo
+    colrows: List[List] = [[] for _ in range(n)]
+    for i in range(m):
+        for p in range(inst.rowptr[i], inst.rowptr[i + 1]):
+            colrows[inst.colidx[p]].append((i, inst.vals[p]))
+    out = [f"NAME {name}", "ROWS", " N obj"] + [f" {kind[i]} {rows[i]}" for i in range(m)] + ["COLUMNS"]
+    order = [j for j in range(n) if inst.isint[j]] + [j for j in range(n) if not inst.isint[j]]
+    nint = int(np.count_nonzero(inst.isint))
+    for k, j in enumerate(order):
+        if k == 0 and nint:
+            out.append(" MARKER 'MARKER' 'INTORG'")
+        if k == nint and nint:
+            out.append(" MARKER 'MARKER' 'INTEND'")
+        out.append(f" {cols[j]} obj {float(obj[j])!r}")
+        for i, v in colrows[j]:
+            out.append(f" {cols[j]} {rows[i]} {float(v)!r}")
+    if nint == n and nint:
+        out.append(" MARKER 'MARKER' 'INTEND'")
+    out.append("RHS")
+    out += [f" rhs {rows[i]} {float(rhs[i])!r}" for i in range(m) if rhs[i] != 0.0]
+    if rngs:
+        out.append("RANGES")
+        out += [f" rng {rows[i]} {float(r)!r}" for i, r in rngs.items()]
+    out.append("BOUNDS")
+    for j in range(n):
+        lo, hi = inst.lb[j], inst.ub[j]
+        if inst.isint[j] and lo == 0.0 and hi == 1.0:
+            out.append(f" UP bnd {cols[j]} 1.0")
+            continue
+        if lo <= -INF and hi >= INF:
+            out.append(f" FR bnd {cols[j]}")
+            continue
+        out.append(f" MI bnd {cols[j]}" if lo <= -INF else f" LO bnd {cols[j]} {float(lo)!r}")
+        out.append(f" PL bnd {cols[j]}" if hi >= INF else f" UP bnd {cols[j]} {float(hi)!r}")
+    out.append("ENDATA")
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")

@@ -190,3 +190,18 @@ int64_t gpl_explain_infeasible(const gpl_rows* R, const gpl_num* num, const gpl_
    }
    return -1;
 }
+
+int gpl_explain_ranged(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int64_t row, int32_t col)
+{
+   int64_t p;
+   (void)col;
+   for( p = R->rowptr[row]; p < R->rowptr[row + 1]; ++p )
+   {
+      const int32_t k = R->colidx[p];
+      if( fabs(io->lb(io->ud, k) - io->glb(io->ud, k)) > num->epsilon && io->addlb(io->ud, k) )
+         return -2;
+      if( fabs(io->ub(io->ud, k) - io->gub(io->ud, k)) > num->epsilon && io->addub(io->ud, k) )
+         return -2;
+   }
+   return 0;
+}

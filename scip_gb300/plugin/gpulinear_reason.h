@@ -63,6 +63,14 @@ int64_t gpl_explain(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int
  * infeasible, -2 if an add callback failed. */
 int64_t gpl_explain_infeasible(const gpl_rows* R, const gpl_num* num, const gpl_io* io);
 
+/* Reason of a change made by row `row`'s ranged-row rule (col = the inferred column), or of that row found
+ * infeasible by it (col = -1): every bound of the row's columns that differs from the column's global bound --
+ * cons_linear's addConflictFixedVars (cons_linear.c:4981-5037) widened from the fixed columns to all, since the rule
+ * reads the bounds of every unfixed column too.  The inferred column's own bounds before the change are included.
+ * Valid whenever the bounds io reads are at least as tight as those the rule ran on.  Returns 0, or -2 if an add
+ * callback failed. */
+int gpl_explain_ranged(const gpl_rows* R, const gpl_num* num, const gpl_io* io, int64_t row, int32_t col);
+
 /* builds colptr/rowidx/rowpos of R from its CSR part; the arrays have n+1, nnz and nnz entries */
 void gpl_build_columns(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx, int64_t* colptr,
    int32_t* rowidx, int64_t* rowpos);

@@ -5,6 +5,7 @@
  * SCIPtightenVarLb/Ub for every moved bound.
  */
 #include <float.h>
+#include <limits.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -55,12 +56,24 @@ struct SCIP_PropData
    int32_t*              seeds;
    double*               seedlo;
    double*               seedhi;
+   SCIP_Bool             ranged;             /**< the device runs the ranged-row rule (GBP_FLAG_RANGEDROW) */
+   int64_t               rcap;               /**< ranged-row records of the recent calls, sorted by (call, round,
+                                              *   column, row): the rows that explain ranged-row changes */
+   int64_t               rn;
+   SCIP_Longint*         rcall;
+   int32_t*              rround;
+   int32_t*              rcol;              /**< -1: the row was found infeasible */
+   int32_t*              rrow;
+   int32_t*              tround;             /**< one call's records as fetched (logcap entries) */
+   int32_t*              tcol;
+   int32_t*              trow;
    SCIP_Longint          ncalls;
    SCIP_Longint          nchgbds;
    SCIP_Longint          ncutoffs;
    SCIP_Longint          nresolves;          /**< conflict-resolution requests for this propagator's changes */
    SCIP_Longint          nresolved;          /**< ... explained with a row */
    SCIP_Longint          nconflicts;         /**< cutoffs handed to conflict analysis with an infeasible row */
+   SCIP_Longint          nrangedreasons;     /**< ... of the resolved changes and analysed cutoffs: by a ranged row */
 };
 
 static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
@@ -90,6 +103,15 @@ static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIPfreeMemoryArrayNull(scip, &pd->seeds);
    SCIPfreeMemoryArrayNull(scip, &pd->seedlo);
    SCIPfreeMemoryArrayNull(scip, &pd->seedhi);
+   SCIPfreeMemoryArrayNull(scip, &pd->rcall);
+   SCIPfreeMemoryArrayNull(scip, &pd->rround);
+   SCIPfreeMemoryArrayNull(scip, &pd->rcol);
+   SCIPfreeMemoryArrayNull(scip, &pd->rrow);
+   SCIPfreeMemoryArrayNull(scip, &pd->tround);
+   SCIPfreeMemoryArrayNull(scip, &pd->tcol);
+   SCIPfreeMemoryArrayNull(scip, &pd->trow);
+   pd->rcap = 0;
+   pd->rn = 0;
    pd->nrows = 0;
    pd->ncols = 0;
    pd->havesnap = FALSE;
@@ -190,6 +212,15 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->loground, pd->logcap) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->loglb, pd->logcap) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->logub, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->tround, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->tcol, pd->logcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->trow, pd->logcap) );
+   pd->rcap = 4 * pd->logcap;
+   pd->rn = 0;
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rcall, pd->rcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rround, pd->rcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rcol, pd->rcap) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rrow, pd->rcap) );
    return SCIP_OKAY;
 }
 
@@ -222,15 +253,90 @@ static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
       if( SCIPgetBoolParam(scip, "constraints/linear/sortvars", &sortvars) == SCIP_OKAY && !sortvars )
          p.flags |= GBP_FLAG_NOSORTVARS;
    }
+   if( pd->ranged )
+      p.flags |= GBP_FLAG_RANGEDROW;
    if( gbp_set_params(pd->ctx, &p) != GBP_OK )
       return SCIP_INVALIDDATA;
    return SCIP_OKAY;
+}
+
+/** whether cons_linear would run ranged-row propagation now (consPropLinear, cons_linear.c:16159-16170): its
+ *  parameter, the depth limit and frequency, not in repropagation -- and not in probing, where SCIP keeps the
+ *  rows' rangedrowpropagated marks (cons_linear.c:17222-17224) so that rows already ranged-propagated are not
+ *  visited again */
+static SCIP_Bool wantRanged(SCIP* scip)
+{
+   SCIP_Bool on = TRUE;
+   int maxdepth = INT_MAX;
+   int freq = 1;
+   int depth = SCIPgetDepth(scip);
+   if( SCIPgetBoolParam(scip, "constraints/linear/rangedrowpropagation", &on) != SCIP_OKAY )
+      on = FALSE;
+   (void)SCIPgetIntParam(scip, "constraints/linear/rangedrowmaxdepth", &maxdepth);
+   (void)SCIPgetIntParam(scip, "constraints/linear/rangedrowfreq", &freq);
+   if( !on || SCIPinProbing(scip) || SCIPinRepropagation(scip) || depth > maxdepth || freq < 0 )
+      return FALSE;
+   return (freq == 0 && depth == 0) || (freq >= 1 && depth % freq == 0);
+}
+
+/* inference information of a logged change: the call (its low 20 bits) and the device round (rounds from 2047 on
+ * share the last value, which no ranged-row record matches) */
+#define INFO_ROUNDBITS 11
+#define INFO_CALLMASK 0xfffff
+static int encodeInfo(SCIP_Longint call, int32_t round)
+{
+   const int32_t r = round < (1 << INFO_ROUNDBITS) - 1 ? round : (1 << INFO_ROUNDBITS) - 1;
+   return (int)(((call & INFO_CALLMASK) << INFO_ROUNDBITS) | r);
+}
+
+/** keeps the last call's ranged-row records (call id pd->ncalls) behind those of earlier calls */
+static void storeRanged(SCIP_PROPDATA* pd)
+{
+   int64_t nr = 0;
+   int64_t k;
+   if( !pd->ranged || gbp_get_ranged_log(pd->ctx, pd->logcap, pd->tround, pd->tcol, pd->trow, &nr) != GBP_OK )
+      return;
+   if( nr > pd->rcap )
+      return;
+   /* the oldest records go when the room is used up, or before their call numbers could alias in the inference
+    * information; their changes are then not explained */
+   if( pd->rn + nr > pd->rcap || (pd->rn > 0 && pd->ncalls - pd->rcall[0] > INFO_CALLMASK / 2) )
+      pd->rn = 0;
+   for( k = 0; k < nr; ++k )
+   {
+      pd->rcall[pd->rn] = pd->ncalls;
+      pd->rround[pd->rn] = pd->tround[k];
+      pd->rcol[pd->rn] = pd->tcol[k];
+      pd->rrow[pd->rn] = pd->trow[k];
+      pd->rn++;
+   }
+}
+
+/** the row of a ranged-row record (call, round, col), or -1: binary search over the sorted records */
+static int64_t findRanged(SCIP_PROPDATA* pd, SCIP_Longint call, int32_t round, int32_t col)
+{
+   int64_t lo = 0;
+   int64_t hi = pd->rn;
+   while( lo < hi )
+   {
+      int64_t mid = (lo + hi) / 2;
+      SCIP_Bool before = pd->rcall[mid] < call || (pd->rcall[mid] == call && (pd->rround[mid] < round
+         || (pd->rround[mid] == round && pd->rcol[mid] < col)));
+      if( before )
+         lo = mid + 1;
+      else
+         hi = mid;
+   }
+   if( lo < pd->rn && pd->rcall[lo] == call && pd->rround[lo] == round && pd->rcol[lo] == col )
+      return pd->rrow[lo];
+   return -1;
 }
 
 static SCIP_RETCODE upload(SCIP* scip, SCIP_PROPDATA* pd)
 {
    int rc;
    SCIP_CALL( buildMatrix(scip, pd) );
+   pd->ranged = FALSE;   /* switched on by the first call that wants it */
    SCIP_CALL( setDeviceParams(scip, pd) );
    rc = gbp_upload_problem(pd->ctx, pd->nrows, pd->ncols, pd->rowptr, pd->colidx, pd->vals, pd->lhs, pd->rhs, pd->isint);
    if( rc == GBP_OK )
@@ -311,13 +417,15 @@ static SCIP_RETCODE applyLog(SCIP* scip, SCIP_PROP* prop, SCIP_PROPDATA* pd, SCI
       SCIP_Bool tightened = FALSE;
       if( pd->logub[k] < SCIPvarGetUbLocal(var) )
       {
-         SCIP_CALL( SCIPinferVarUbProp(scip, var, pd->logub[k], prop, pd->loground[k], TRUE, infeasible, &tightened) );
+         SCIP_CALL( SCIPinferVarUbProp(scip, var, pd->logub[k], prop, encodeInfo(pd->ncalls, pd->loground[k]), TRUE,
+               infeasible, &tightened) );
          *reduced = *reduced || tightened;
          pd->nchgbds += tightened ? 1 : 0;
       }
       if( !*infeasible && pd->loglb[k] > SCIPvarGetLbLocal(var) )
       {
-         SCIP_CALL( SCIPinferVarLbProp(scip, var, pd->loglb[k], prop, pd->loground[k], TRUE, infeasible, &tightened) );
+         SCIP_CALL( SCIPinferVarLbProp(scip, var, pd->loglb[k], prop, encodeInfo(pd->ncalls, pd->loground[k]), TRUE,
+               infeasible, &tightened) );
          *reduced = *reduced || tightened;
          pd->nchgbds += tightened ? 1 : 0;
       }
@@ -351,6 +459,17 @@ static SCIP_RETCODE analyzeCutoff(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_CALL( SCIPinitConflictAnalysis(scip, SCIP_CONFTYPE_PROPAGATION, FALSE) );
    reasonSetup(scip, pd, NULL, &c, &R, &num, &io);
    r = gpl_explain_infeasible(&R, &num, &io);
+   if( r == -1 )
+   {
+      /* no row's activities show it: a ranged row of the last call did (its records with column -1) */
+      int64_t k;
+      for( k = pd->rn - 1; k >= 0 && pd->rcall[k] == pd->ncalls && r == -1; --k )
+         if( pd->rcol[k] == -1 )
+         {
+            r = gpl_explain_ranged(&R, &num, &io, pd->rrow[k], -1) == 0 ? pd->rrow[k] : -2;
+            pd->nrangedreasons++;
+         }
+   }
    if( r == -2 )
       return SCIP_ERROR;
    if( r >= 0 )
@@ -449,6 +568,16 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
       }
    }
 
+   /* ranged-row propagation where cons_linear would run it (switching it rebuilds the device's loop) */
+   if( wantRanged(scip) != pd->ranged )
+   {
+      pd->ranged = !pd->ranged;
+      if( setDeviceParams(scip, pd) != SCIP_OKAY )
+      {
+         disable(scip, pd, "setting the ranged-row rule failed", GBP_ERR_INVALID);
+         return SCIP_OKAY;
+      }
+   }
    rc = gbp_propagate(pd->ctx, pd->lb, pd->ub, nseed, nseed > 0 ? pd->seeds : NULL, nseed > 0 ? pd->seedlo : NULL,
       nseed > 0 ? pd->seedhi : NULL, &cutoff, &res);
    pd->ncalls++;
@@ -457,6 +586,7 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
       disable(scip, pd, "propagation call failed", rc);
       return SCIP_OKAY;
    }
+   storeRanged(pd);
    if( cutoff )
    {
       /* the changes the rounds before the infeasibility made, then conflict analysis on the infeasible row */
@@ -609,6 +739,19 @@ static SCIP_DECL_PROPRESPROP(propRespropGpulinear)
       return SCIP_OKAY;
    reasonSetup(scip, pd, bdchgidx, &c, &R, &num, &io);
    r = gpl_explain(&R, &num, &io, col, boundtype == SCIP_BOUNDTYPE_LOWER, relaxedbd);
+   if( r == -1 )
+   {
+      /* no row's activities imply it: the ranged row that proposed it in that call and round, if still on record */
+      const SCIP_Longint lo = ((SCIP_Longint)inferinfo >> INFO_ROUNDBITS) & INFO_CALLMASK;
+      const SCIP_Longint call = pd->ncalls - ((pd->ncalls - lo) & INFO_CALLMASK);
+      const int32_t round = inferinfo & ((1 << INFO_ROUNDBITS) - 1);
+      const int64_t row = round < (1 << INFO_ROUNDBITS) - 1 ? findRanged(pd, call, round, col) : -1;
+      if( row >= 0 )
+      {
+         r = gpl_explain_ranged(&R, &num, &io, row, col) == 0 ? row : -2;
+         pd->nrangedreasons++;
+      }
+   }
    if( r == -2 )
       return SCIP_ERROR;
    if( r >= 0 )
@@ -683,4 +826,10 @@ SCIP_RETCODE SCIPgetGpulinearStats(SCIP* scip, SCIP_Longint* ncalls, SCIP_Longin
    *nresolves = pd->nresolves;
    *nresolved = pd->nresolved;
    return SCIP_OKAY;
+}
+
+SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip)
+{
+   SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
+   return prop == NULL ? 0 : SCIPpropGetData(prop)->nrangedreasons;
 }

@@ -39,6 +39,10 @@ SCIP_Bool SCIPgpulinearIsActive(SCIP* scip);
 SCIP_RETCODE SCIPgetGpulinearStats(SCIP* scip, SCIP_Longint* ncalls, SCIP_Longint* nchgbds, SCIP_Longint* ncutoffs,
    SCIP_Longint* nconflicts, SCIP_Longint* nresolves, SCIP_Longint* nresolved);
 
+/** how many of the explained changes and analysed cutoffs were explained by a ranged row's record
+ *  (constraints/linear/rangedrowpropagation) */
+SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip);
+
 #ifdef __cplusplus
 }
 #endif

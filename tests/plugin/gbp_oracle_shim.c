@@ -74,6 +74,7 @@ int gbp_destroy(gbp_ctx* ctx)
       return GBP_ERR_INVALID;
    freeProblem(ctx);
    free(ctx->log.col); free(ctx->log.round); free(ctx->log.lb); free(ctx->log.ub);
+   free(ctx->log.rrow); free(ctx->log.rcol); free(ctx->log.rround);
    free(ctx);
    return GBP_OK;
 }
@@ -89,7 +90,8 @@ int gbp_set_params(gbp_ctx* ctx, const gbp_params* p)
    ctx->par.recompfac = p->recompfac;
    ctx->par.maxeasyactivitydelta = p->maxeasyactivitydelta;
    ctx->par.maxrounds = p->maxrounds;
-   ctx->par.flags = (p->flags & GBP_FLAG_NOSORTVARS) ? LPO_FLAG_NOSORTVARS : 0;
+   ctx->par.flags = ((p->flags & GBP_FLAG_NOSORTVARS) ? LPO_FLAG_NOSORTVARS : 0)
+      | ((p->flags & GBP_FLAG_RANGEDROW) ? LPO_FLAG_RANGEDROW : 0);
    return GBP_OK;
 }
 
@@ -152,6 +154,7 @@ int gbp_set_global_bounds(gbp_ctx* ctx, const double* glb, const double* gub)
 int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity)
 {
    free(ctx->log.col); free(ctx->log.round); free(ctx->log.lb); free(ctx->log.ub);
+   free(ctx->log.rrow); free(ctx->log.rcol); free(ctx->log.rround);
    memset(&ctx->log, 0, sizeof(ctx->log));
    ctx->logon = capacity > 0;
    if( !ctx->logon )
@@ -161,6 +164,10 @@ int gbp_set_change_log(gbp_ctx* ctx, int64_t capacity)
    ctx->log.round = malloc(sizeof(int32_t) * (size_t)capacity);
    ctx->log.lb = malloc(sizeof(double) * (size_t)capacity);
    ctx->log.ub = malloc(sizeof(double) * (size_t)capacity);
+   ctx->log.rcap = capacity;
+   ctx->log.rrow = malloc(sizeof(int32_t) * (size_t)capacity);
+   ctx->log.rcol = malloc(sizeof(int32_t) * (size_t)capacity);
+   ctx->log.rround = malloc(sizeof(int32_t) * (size_t)capacity);
    return GBP_OK;
 }
 
@@ -225,4 +232,39 @@ int gbp_get_change_log(gbp_ctx* ctx, int64_t cap, int32_t* col, int32_t* round, 
    }
    free(ord);
    return (ctx->log.n > ctx->log.cap || ctx->log.n > cap) ? GBP_ERR_OVERFLOW : GBP_OK;
+}
+
+static int byRoundColRow(const void* a, const void* b)
+{
+   int64_t x = *(const int64_t*)a;
+   int64_t y = *(const int64_t*)b;
+   if( sortlog->rround[x] != sortlog->rround[y] )
+      return sortlog->rround[x] < sortlog->rround[y] ? -1 : 1;
+   if( sortlog->rcol[x] != sortlog->rcol[y] )
+      return sortlog->rcol[x] < sortlog->rcol[y] ? -1 : 1;
+   return sortlog->rrow[x] < sortlog->rrow[y] ? -1 : (sortlog->rrow[x] > sortlog->rrow[y] ? 1 : 0);
+}
+
+int gbp_get_ranged_log(gbp_ctx* ctx, int64_t cap, int32_t* round, int32_t* col, int32_t* row, int64_t* n)
+{
+   int64_t have;
+   int64_t k;
+   int64_t* ord;
+   *n = ctx->log.rn;
+   if( !ctx->logon )
+      return GBP_ERR_STATE;
+   have = ctx->log.rn < ctx->log.rcap ? ctx->log.rn : ctx->log.rcap;
+   ord = malloc(sizeof(int64_t) * (size_t)(have > 0 ? have : 1));
+   for( k = 0; k < have; ++k )
+      ord[k] = k;
+   sortlog = &ctx->log;
+   qsort(ord, (size_t)have, sizeof(int64_t), byRoundColRow);
+   for( k = 0; k < have && k < cap; ++k )
+   {
+      round[k] = ctx->log.rround[ord[k]];
+      col[k] = ctx->log.rcol[ord[k]];
+      row[k] = ctx->log.rrow[ord[k]];
+   }
+   free(ord);
+   return (ctx->log.rn > ctx->log.rcap || ctx->log.rn > cap) ? GBP_ERR_OVERFLOW : GBP_OK;
 }

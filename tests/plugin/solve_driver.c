@@ -1,11 +1,13 @@
 /* Solves an MPS instance with SCIP (built from the reference sources), either with cons_linear's own propagation
  * ("plain") or with the gpulinear propagator replacing it ("gpulinear", linked against the oracle test double
- * tests/plugin/gbp_oracle_shim.c).  Presolving, linear upgrades, ranged-row propagation and LP solving are off in
- * both modes, so the search runs on propagation and conflict analysis alone.  Prints, one item per line:
+ * tests/plugin/gbp_oracle_shim.c).  Presolving, linear upgrades, ranged-row propagation (unless asked for) and LP
+ * solving are off in both modes, so the search runs on propagation and conflict analysis alone.  Prints, one item
+ * per line:
  *   status <SCIP status>    obj <primal bound>    nodes <n>
  *   gpulinear <calls> <bound changes> <cutoffs> <cutoffs analysed> <resolve requests> <resolved> active <0|1>
- *   conflicts <conflicts found>
- * Usage: solve_driver <instance.mps> <plain|gpulinear> [node limit] */
+ *   conflicts <conflicts found>    rangedreasons <changes and cutoffs explained by a ranged row>
+ * With a fourth argument "ranged" ranged-row propagation is on in both modes (without artificial constraints).
+ * Usage: solve_driver <instance.mps> <plain|gpulinear> [node limit] [ranged] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -41,7 +43,8 @@ int main(int argc, char** argv)
             SCIPsetBoolParam(scip, SCIPparamGetName(params[k]), FALSE);
    }
    SCIPsetIntParam(scip, "presolving/maxrounds", 0);
-   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", FALSE);
+   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", argc > 4 && strcmp(argv[4], "ranged") == 0);
+   SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);
    SCIPsetBoolParam(scip, "conflict/enable", TRUE);
    SCIPsetLongintParam(scip, "limits/nodes", nodelimit);
@@ -71,6 +74,7 @@ int main(int argc, char** argv)
          return 5;
       printf("gpulinear %lld %lld %lld %lld %lld %lld active %d\n", (long long)c, (long long)b, (long long)x,
          (long long)a, (long long)q, (long long)r, SCIPgpulinearIsActive(scip) ? 1 : 0);
+      printf("rangedreasons %lld\n", (long long)SCIPgetGpulinearRangedReasons(scip));
    }
    SCIPfree(&scip);
    return 0;

@@ -5,6 +5,8 @@ SCIP build is absent."""
 import os
 import subprocess
 
+import numpy as np
+
 import pytest
 
 from scip_gb300 import instances
@@ -95,8 +97,9 @@ def solve_driver(tmp_path_factory, oracle_mod):
     return exe
 
 
-def _solve(exe, path, mode):
-    r = subprocess.run([exe, path, mode, "200000"], capture_output=True, text=True, timeout=600)
+def _solve(exe, path, mode, ranged=False):
+    r = subprocess.run([exe, path, mode, "200000"] + (["ranged"] if ranged else []), capture_output=True, text=True,
+                       timeout=600)
     assert r.returncode == 0, r.stderr
     return dict(l.split(" ", 1) for l in r.stdout.strip().splitlines() if " " in l)
 
@@ -118,3 +121,24 @@ def test_plugin_replaces_linear_propagation_in_search(solve_driver, oracle_mod, 
     assert asked == resolved
     if name != "flugpl":  # flugpl is solved without any conflict
         assert int(resolved) > 0 and int(analysed) > 0 and int(gpu["conflicts"]) > 0
+
+
+@pytest.mark.parametrize("seed", [5, 6, 7])
+def test_plugin_ranged_rows_in_search(solve_driver, tmp_path, seed):
+    """Ranged-row propagation on (without artificial constraints) on rows whose integer part shares a divisor: SCIP
+    with cons_linear and SCIP with the plugin prove the same optimum, and the plugin explains the changes and
+    cutoffs of its ranged rows to conflict analysis with the rows it recorded (gbp_get_ranged_log)."""
+    from scip_gb300 import instances, mps
+    # no continuous columns: the search has no LP solver for them (LP solver none)
+    inst = instances.gcd_rows(np.random.default_rng(seed), 30, 80, equations=True, continuous=False)
+    path = str(tmp_path / "gcd.mps")
+    mps.write_mps(inst, path, obj=np.random.default_rng(seed + 100).integers(-5, 6, inst.n))
+    plain = _solve(solve_driver, path, "plain", ranged=True)
+    gpu = _solve(solve_driver, path, "gpulinear", ranged=True)
+    assert plain["status"] == gpu["status"] and plain["status"] in ("optimal", "infeasible")
+    if plain["status"] == "optimal":
+        assert float(plain["obj"]) == float(gpu["obj"])
+    calls, chg, cut, analysed, asked, resolved, _, active = gpu["gpulinear"].split()
+    assert active == "1" and int(calls) > 0
+    assert asked == resolved
+    assert int(gpu["rangedreasons"]) > 0

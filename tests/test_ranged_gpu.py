@@ -112,3 +112,37 @@ def test_ranged_fixture_matches_scip(gpu_prop, maxeasy):
     assert cut == bool(z[f"{tag}_rootcut"])
     il = inst.isint != 0
     assert np.array_equal(lb[il], z[f"{tag}_rootlb"][il]) and np.array_equal(ub[il], z[f"{tag}_rootub"][il])
+
+
+@pytest.mark.parametrize("hostloop", [False, True])
+def test_ranged_records_match_oracle(gpu_prop, oracle_mod, hostloop):
+    """With a change log, the rows whose ranged rule proposed bounds or found themselves infeasible are recorded
+    with their round (the reasons conflict analysis asks for); records and changes equal the oracle's."""
+    inst = _inst(seed=43)
+    gpu_prop.set_params(_gp(0.0, True, hostloop))
+    gpu_prop.upload(inst)
+    gpu_prop.set_change_log(8 * inst.n)
+    lb, ub, cut, _ = gpu_prop.propagate(inst.lb, inst.ub)
+    mine = gpu_prop.change_log()
+    rec = gpu_prop.ranged_log()
+    orc = oracle_mod.Oracle(inst)
+    olb, oub, ores, olog = orc.propagate_logged(inst.lb, inst.ub, oracle_mod.params(0.0, ranged=True))
+    assert cut == bool(ores.cutoff) and np.array_equal(lb, olb) and np.array_equal(ub, oub)
+    for a, b in zip(mine, olog):
+        assert np.array_equal(a, b)
+    assert len(rec[0]) > 50
+    for a, b in zip(rec, orc.last_ranged):
+        assert np.array_equal(a, b)
+    # infeasibility found by a ranged row is recorded with column -1
+    insts, z = load_tiny()
+    k = int(np.flatnonzero(z["sort_cut"])[0])
+    gpu_prop.upload(insts[k])
+    gpu_prop.set_change_log(1024)
+    _, _, cut, _ = gpu_prop.propagate(insts[k].lb, insts[k].ub)
+    orc = oracle_mod.Oracle(insts[k])
+    orc.propagate_logged(insts[k].lb, insts[k].ub, oracle_mod.params(0.0, ranged=True))
+    rec = gpu_prop.ranged_log()
+    assert cut
+    for a, b in zip(rec, orc.last_ranged):
+        assert np.array_equal(a, b)
+    gpu_prop.set_change_log(0)
