@@ -116,9 +116,12 @@ def algorithmic_bytes(rows, nnz, changes, avg_col_len):
     return 28.0 * nnz + 40.0 * rows + 16.0 * changes + 8.0 * changes * avg_col_len
 
 
-def build_workload(seed=2, nnodes=NNODES, m=200_000, n=400_000):
+def build_workload(seed=2, nnodes=NNODES, m=200_000, n=400_000, family="mip"):
     from scip_gb300 import instances
 
+    if family == "gcd":
+        # ranged rows and equations whose integer part shares a divisor (1 % of rows 65..200 long)
+        return instances.gcd_rows(np.random.default_rng(seed), m, n, long_frac=0.01, equations=True)
     inst = instances.node_mip(seed=seed, m=m, n=n)
     return inst
 
@@ -302,6 +305,9 @@ def main():
                     help="nodes: batched B&B nodes (headline); uneven: 512 distinct instances in one problem; "
                          "zipf: one 1M x 2M instance through the plain path")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--family", default="mip", choices=["mip", "gcd"],
+                    help="nodes workload matrix: mip (log-uniform coefficients) or gcd (ranged rows sharing a divisor)")
+    ap.add_argument("--ranged", action="store_true", help="ranged-row propagation on (GBP_FLAG_RANGEDROW)")
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serving: arrival rates (req/s)")
     ap.add_argument("--duration", type=float, default=1.0, help="serving: seconds of arrivals per rate")
     args = ap.parse_args()
@@ -316,7 +322,10 @@ def main():
     from scip_gb300 import instances
 
     config = {"workload": "batched B&B nodes: 200,000 x 400,000 rows/cols, ~4.5M nnz, 4,096 nodes fixing 1-64 "
-                          "integer columns each, every node to fixpoint",
+                          "integer columns each, every node to fixpoint" if args.family == "mip" else
+                          "batched B&B nodes: 200,000 x 400,000 gcd rows (3..8 entries, 1 % 65..200; half equations), "
+                          "4,096 nodes fixing 1-64 integer columns each, every node to fixpoint",
+              "ranged_rows": bool(args.ranged),
               "rows": 200000, "cols": 400000, "nodes_per_step": args.nodes, "rule": "residual (maxeasyactivitydelta="
               f"{args.maxeasy:g})", "l2": "flushed between timed steps (256 MiB write)",
               "parallelism": f"replicas x{world}"}
@@ -327,9 +336,9 @@ def main():
         import oracle as orc
 
         orc.build()
-        inst = build_workload()
+        inst = build_workload(family=args.family)
         o = orc.Oracle(inst)
-        par = orc.params(args.maxeasy)
+        par = orc.params(args.maxeasy, ranged=args.ranged)
         rlb, rub, _ = o.propagate(inst.lb, inst.ub, par)
         nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3)
         threads = os.cpu_count() or 1
@@ -362,8 +371,8 @@ def main():
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
 
-    inst = build_workload()
-    prop = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy))
+    inst = build_workload(family=args.family)
+    prop = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy, ranged=args.ranged))
     prop.upload(inst)
     rlb, rub, rcut, rres = prop.propagate(inst.lb, inst.ub)
     nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3 + rank)
@@ -439,7 +448,7 @@ def main():
     peak, peak_kind = measured_peak()
     achieved = algo / (ms / 1e3) / 1e9
     cutoffs = stats[-1]["cutoff"]
-    traffic, traffic_src = measured_traffic(N, shape)
+    traffic, traffic_src = measured_traffic(N, shape) if args.family == "mip" and not args.ranged else (None, None)
 
     # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
@@ -500,7 +509,7 @@ def main():
             import oracle as orc
 
             orc.build()
-            par = orc.params(args.maxeasy)
+            par = orc.params(args.maxeasy, ranged=args.ranged)
             cpu_v, sample = cpu_arm(inst, rlb, rub, nodes, par, os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
                                     "kind": "port", "sample": sample}

@@ -133,7 +133,8 @@ def test_ranged_records_match_oracle(gpu_prop, oracle_mod, hostloop):
     assert len(rec[0]) > 50
     for a, b in zip(rec, orc.last_ranged):
         assert np.array_equal(a, b)
-    # infeasibility found by a ranged row is recorded with column -1
+    # infeasibility found by a ranged row is recorded with column -1.  The oracle stops at the first infeasible
+    # row of the round; the device evaluates the whole round, so its records hold the oracle's and may hold more
     insts, z = load_tiny()
     k = int(np.flatnonzero(z["sort_cut"])[0])
     gpu_prop.upload(insts[k])
@@ -141,8 +142,8 @@ def test_ranged_records_match_oracle(gpu_prop, oracle_mod, hostloop):
     _, _, cut, _ = gpu_prop.propagate(insts[k].lb, insts[k].ub)
     orc = oracle_mod.Oracle(insts[k])
     orc.propagate_logged(insts[k].lb, insts[k].ub, oracle_mod.params(0.0, ranged=True))
-    rec = gpu_prop.ranged_log()
-    assert cut
-    for a, b in zip(rec, orc.last_ranged):
-        assert np.array_equal(a, b)
+    rec = set(zip(*[a.tolist() for a in gpu_prop.ranged_log()]))
+    theirs = set(zip(*[a.tolist() for a in orc.last_ranged]))
+    assert cut and any(c == -1 for _, c, _ in theirs)
+    assert theirs <= rec
     gpu_prop.set_change_log(0)
