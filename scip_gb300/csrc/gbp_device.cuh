@@ -1265,9 +1265,8 @@ __device__ void processShortRows(const Num& s, const Prob& P, const BND& B, cons
                          relres);
       }
     }
-    // ranged rows of the batch, one thread each, after the activity rules (propagateCons,
-    // cons_linear.c:7694-7711); a batch that found the problem infeasible has nothing left to add
-    if (RANGED && P.relig != nullptr && *cut == 0) {
+    // ranged rows of the batch, one thread each, after the activity rules (propagateCons, cons_linear.c:7694-7711)
+    if (RANGED && P.relig != nullptr) {
       for (int o = tid; o < cnt; o += NT) {
         const int i = rb.order[o];
         if (P.relig[i] != 0 && !rowDead(P, i) && rangedRow(s, P, B, i, C, st)) cutRow(P, i, cut);
