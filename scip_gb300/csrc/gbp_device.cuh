@@ -1480,11 +1480,11 @@ __device__ bool rowWarpCore(const Num& s, const Prob& P, const BND& B, int i, Ca
 // the activity rules of a long row, then (lane 0) its ranged-row rule; true on every lane on cutoff
 template <bool RANGED = true, class BND>
 __device__ bool rowWarp(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
-  if (rowWarpCore(s, P, B, i, C, st)) return true;
-  if (!RANGED || P.relig == nullptr || P.relig[i] == 0) return false;
-  bool cut = false;
-  if ((threadIdx.x & 31) == 0) cut = rangedRow(s, P, B, i, C, st);
-  return __shfl_sync(0xffffffffu, cut ? 1 : 0, 0) != 0;
+  const bool cut = rowWarpCore(s, P, B, i, C, st);
+  if (!RANGED || P.relig == nullptr || P.relig[i] == 0) return cut;
+  bool rcut = false;
+  if ((threadIdx.x & 31) == 0) rcut = rangedRow(s, P, B, i, C, st);
+  return cut || __shfl_sync(0xffffffffu, rcut ? 1 : 0, 0) != 0;
 }
 
 // Acceptance of column j's best candidates against its round-start bounds [l,u]: upper bound first
