@@ -12,6 +12,10 @@
 #include "prop_gpulinear.h"
 #include "gpulinear_reason.h"
 #include "scip/cons_linear.h"
+#include "scip/cons_knapsack.h"
+#include "scip/cons_logicor.h"
+#include "scip/cons_setppc.h"
+#include "scip/cons_varbound.h"
 #include "gbp.h"
 
 #define PROP_NAME     "gpulinear"
@@ -27,7 +31,9 @@ struct SCIP_PropData
    int                   device;             /**< CUDA device ordinal */
    SCIP_Bool             replacelinear;      /**< switch cons_linear's propagation off at include time */
    SCIP_Bool             failed;             /**< the GPU path failed or is unavailable: do not run */
-   int                   nconss;             /**< number of linear constraints the matrix was built from */
+   int                   nconss;             /**< number of constraints the matrix was built from */
+   SCIP_Bool             specialised;        /**< also the rows of setppc, logicor, knapsack, varbound constraints */
+   SCIP_Bool             replacespecialised; /**< switch those handlers' propagation off at include time */
    int                   nrows;              /**< rows in the matrix */
    int                   ncols;              /**< columns = transformed variables */
    SCIP_VAR**            vars;               /**< column -> variable */
@@ -117,25 +123,127 @@ static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    pd->havesnap = FALSE;
 }
 
-/** copies the linear constraints into CSR form: active variables become columns (SCIPvarGetProbindex),
- *  fixed variables move into the sides, constraints with other variables are left to cons_linear */
+/* the linear-constraint handlers whose rows the propagator reads: cons_linear always, and with `specialised` the
+ * handlers SCIP's presolving upgrades linear rows to (cons_setppc, cons_logicor, cons_knapsack, cons_varbound),
+ * whose rows are linear too */
+static const char* const HDLRS[] = {"linear", "setppc", "logicor", "knapsack", "varbound"};
+#define NHDLRS 5
+
+static int numHandlers(SCIP_PROPDATA* pd) { return pd->specialised ? NHDLRS : 1; }
+
+/** whether the propagator reads constraint cons: globally valid rows only -- not local constraints (valid in a
+ *  subtree), not conflict constraints (SCIP adds and deletes them all the time; their handler propagates them),
+ *  not modifiable ones */
+static SCIP_Bool readsCons(SCIP_CONS* cons)
+{
+   return !SCIPconsIsLocal(cons) && !SCIPconsIsConflict(cons) && !SCIPconsIsModifiable(cons);
+}
+
+/** the constraints of the handlers the propagator reads (rebuild test) */
+static int countConss(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   int h;
+   int n = 0;
+   for( h = 0; h < numHandlers(pd); ++h )
+   {
+      SCIP_CONSHDLR* c = SCIPfindConshdlr(scip, HDLRS[h]);
+      SCIP_CONS** conss = c == NULL ? NULL : SCIPconshdlrGetConss(c);
+      int nc = c == NULL ? 0 : SCIPconshdlrGetNConss(c);
+      int k;
+      for( k = 0; k < nc; ++k )
+         n += readsCons(conss[k]) ? 1 : 0;
+   }
+   return n;
+}
+
+/** the row of constraint cons of handler h as coefficients of (possibly non-active) variables and sides: vars and
+ *  vals receive at most size entries (*n = the number needed) */
+static SCIP_RETCODE consRow(SCIP* scip, int h, SCIP_CONS* cons, SCIP_VAR** vars, SCIP_Real* vals, int size, int* n,
+   SCIP_Real* lhs, SCIP_Real* rhs)
+{
+   int k;
+   SCIP_VAR** cv = NULL;
+   *n = 0;
+   switch( h )
+   {
+   case 0:   /* linear: lhs <= sum a x <= rhs */
+      *n = SCIPgetNVarsLinear(scip, cons);
+      if( *n <= size && *n > 0 )
+      {
+         memcpy(vars, SCIPgetVarsLinear(scip, cons), sizeof(SCIP_VAR*) * (size_t)*n);
+         memcpy(vals, SCIPgetValsLinear(scip, cons), sizeof(SCIP_Real) * (size_t)*n);
+      }
+      *lhs = SCIPgetLhsLinear(scip, cons);
+      *rhs = SCIPgetRhsLinear(scip, cons);
+      return SCIP_OKAY;
+   case 1:   /* setppc: sum x = 1 (partitioning), <= 1 (packing), >= 1 (covering), cons_setppc.h:47-52 */
+      *n = SCIPgetNVarsSetppc(scip, cons);
+      cv = SCIPgetVarsSetppc(scip, cons);
+      *lhs = SCIPgetTypeSetppc(scip, cons) == SCIP_SETPPCTYPE_PACKING ? -SCIPinfinity(scip) : 1.0;
+      *rhs = SCIPgetTypeSetppc(scip, cons) == SCIP_SETPPCTYPE_COVERING ? SCIPinfinity(scip) : 1.0;
+      break;
+   case 2:   /* logicor: sum x >= 1 */
+      *n = SCIPgetNVarsLogicor(scip, cons);
+      cv = SCIPgetVarsLogicor(scip, cons);
+      *lhs = 1.0;
+      *rhs = SCIPinfinity(scip);
+      break;
+   case 3:   /* knapsack: sum w x <= capacity */
+   {
+      SCIP_Longint* w = SCIPgetWeightsKnapsack(scip, cons);
+      *n = SCIPgetNVarsKnapsack(scip, cons);
+      if( *n <= size && *n > 0 )
+      {
+         memcpy(vars, SCIPgetVarsKnapsack(scip, cons), sizeof(SCIP_VAR*) * (size_t)*n);
+         for( k = 0; k < *n; ++k )
+            vals[k] = (SCIP_Real)w[k];
+      }
+      *lhs = -SCIPinfinity(scip);
+      *rhs = (SCIP_Real)SCIPgetCapacityKnapsack(scip, cons);
+      return SCIP_OKAY;
+   }
+   default:  /* varbound: lhs <= x + c y <= rhs */
+      *n = 2;
+      if( size >= 2 )
+      {
+         vars[0] = SCIPgetVarVarbound(scip, cons);
+         vals[0] = 1.0;
+         vars[1] = SCIPgetVbdvarVarbound(scip, cons);
+         vals[1] = SCIPgetVbdcoefVarbound(scip, cons);
+      }
+      *lhs = SCIPgetLhsVarbound(scip, cons);
+      *rhs = SCIPgetRhsVarbound(scip, cons);
+      return SCIP_OKAY;
+   }
+   if( *n <= size && *n > 0 )
+   {
+      memcpy(vars, cv, sizeof(SCIP_VAR*) * (size_t)*n);
+      for( k = 0; k < *n; ++k )
+         vals[k] = 1.0;
+   }
+   return SCIP_OKAY;
+}
+
+/** copies the rows of the handlers into CSR form over the active variables (columns = SCIPvarGetProbindex): fixed,
+ *  aggregated, multi-aggregated and negated variables are replaced by their active variables
+ *  (SCIPgetProbvarLinearSum), constants move into the sides; modifiable constraints are left to their handler */
 static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
 {
-   SCIP_CONSHDLR* conshdlr = SCIPfindConshdlr(scip, "linear");
-   SCIP_CONS** conss;
-   int nconss;
    int nvars = SCIPgetNVars(scip);
    SCIP_VAR** vars = SCIPgetVars(scip);
    int64_t nnz = 0;
    int64_t cap;
-   int c;
+   int ntotal = 0;
+   int bufsize = 16;
+   SCIP_VAR** bv;
+   SCIP_Real* bc;
+   int64_t* where;   /* position of a column's entry in the row being built (< the row's start: none) */
+   int h;
    int j;
 
    freeMatrix(scip, pd);
-   nconss = conshdlr == NULL ? 0 : SCIPconshdlrGetNConss(conshdlr);
-   conss = conshdlr == NULL ? NULL : SCIPconshdlrGetConss(conshdlr);
-   pd->nconss = nconss;
    pd->ncols = nvars;
+   pd->nconss = countConss(scip, pd);
 
    SCIP_CALL( SCIPduplicateMemoryArray(scip, &pd->vars, vars, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->isint, nvars > 0 ? nvars : 1) );
@@ -151,57 +259,126 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    for( j = 0; j < nvars; ++j )
       pd->isint[j] = SCIPvarIsIntegral(vars[j]) ? 1 : 0;
 
-   for( c = 0; c < nconss; ++c )
-      nnz += SCIPgetNVarsLinear(scip, conss[c]);
+   /* sizes: constraints and their entries before mapping to active variables */
+   for( h = 0; h < numHandlers(pd); ++h )
+   {
+      SCIP_CONSHDLR* hdlr = SCIPfindConshdlr(scip, HDLRS[h]);
+      SCIP_CONS** conss = hdlr == NULL ? NULL : SCIPconshdlrGetConss(hdlr);
+      int nc = hdlr == NULL ? 0 : SCIPconshdlrGetNConss(hdlr);
+      int c;
+      ntotal += nc;
+      for( c = 0; c < nc; ++c )
+      {
+         int n = 0;
+         SCIP_Real l;
+         SCIP_Real r;
+         SCIP_CALL( consRow(scip, h, conss[c], NULL, NULL, 0, &n, &l, &r) );
+         nnz += n;
+      }
+   }
    cap = nnz > 0 ? nnz : 1;
-   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowptr, nconss + 1) );
-   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->lhs, nconss > 0 ? nconss : 1) );
-   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rhs, nconss > 0 ? nconss : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowptr, ntotal + 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->lhs, ntotal > 0 ? ntotal : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rhs, ntotal > 0 ? ntotal : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->vals, cap) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->colidx, cap) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &bv, bufsize) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &bc, bufsize) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &where, nvars > 0 ? nvars : 1) );
+   for( j = 0; j < nvars; ++j )
+      where[j] = -1;
 
    pd->rowptr[0] = 0;
    pd->nrows = 0;
-   for( c = 0; c < nconss; ++c )
+   for( h = 0; h < numHandlers(pd); ++h )
    {
-      SCIP_CONS* cons = conss[c];
-      SCIP_VAR** cvars = SCIPgetVarsLinear(scip, cons);
-      SCIP_Real* cvals = SCIPgetValsLinear(scip, cons);
-      int cn = SCIPgetNVarsLinear(scip, cons);
-      SCIP_Real l = SCIPgetLhsLinear(scip, cons);
-      SCIP_Real r = SCIPgetRhsLinear(scip, cons);
-      int64_t start = pd->rowptr[pd->nrows];
-      int64_t p = start;
-      SCIP_Bool ok = !SCIPconsIsModifiable(cons);
-      int q;
-
-      for( q = 0; q < cn && ok; ++q )
+      SCIP_CONSHDLR* hdlr = SCIPfindConshdlr(scip, HDLRS[h]);
+      SCIP_CONS** conss = hdlr == NULL ? NULL : SCIPconshdlrGetConss(hdlr);
+      int nc = hdlr == NULL ? 0 : SCIPconshdlrGetNConss(hdlr);
+      int c;
+      for( c = 0; c < nc; ++c )
       {
-         SCIP_VAR* v = cvars[q];
-         if( SCIPvarIsActive(v) )
+         SCIP_CONS* cons = conss[c];
+         SCIP_Real l;
+         SCIP_Real r;
+         SCIP_Real constant = 0.0;
+         int n = 0;
+         int need = 0;
+         int q;
+         int64_t start = pd->rowptr[pd->nrows];
+         int64_t p = start;
+         if( !readsCons(cons) )
+            continue;
+         SCIP_CALL( consRow(scip, h, cons, bv, bc, bufsize, &n, &l, &r) );
+         if( n > bufsize )
          {
-            pd->colidx[p] = (int32_t)SCIPvarGetProbindex(v);
-            pd->vals[p] = cvals[q];
-            ++p;
+            bufsize = 2 * n;
+            SCIP_CALL( SCIPreallocBufferArray(scip, &bv, bufsize) );
+            SCIP_CALL( SCIPreallocBufferArray(scip, &bc, bufsize) );
+            SCIP_CALL( consRow(scip, h, cons, bv, bc, bufsize, &n, &l, &r) );
          }
-         else if( SCIPvarGetStatus(v) == SCIP_VARSTATUS_FIXED )
+         SCIP_CALL( SCIPgetProbvarLinearSum(scip, bv, bc, &n, bufsize, &constant, &need) );
+         if( need > bufsize )
          {
-            SCIP_Real shift = cvals[q] * SCIPvarGetLbGlobal(v);
-            if( !SCIPisInfinity(scip, -l) )
-               l -= shift;
-            if( !SCIPisInfinity(scip, r) )
-               r -= shift;
+            bufsize = 2 * need;
+            SCIP_CALL( SCIPreallocBufferArray(scip, &bv, bufsize) );
+            SCIP_CALL( SCIPreallocBufferArray(scip, &bc, bufsize) );
+            SCIP_CALL( consRow(scip, h, cons, bv, bc, bufsize, &n, &l, &r) );
+            constant = 0.0;
+            SCIP_CALL( SCIPgetProbvarLinearSum(scip, bv, bc, &n, bufsize, &constant, &need) );
          }
-         else
-            ok = FALSE;
+         if( p + n > cap )
+         {
+            cap = 2 * (p + n);
+            SCIP_CALL( SCIPreallocMemoryArray(scip, &pd->vals, cap) );
+            SCIP_CALL( SCIPreallocMemoryArray(scip, &pd->colidx, cap) );
+         }
+         /* one entry per column: a variable that several entries map to gets their sum */
+         for( q = 0; q < n; ++q )
+         {
+            const int32_t col = (int32_t)SCIPvarGetProbindex(bv[q]);
+            if( bc[q] == 0.0 || col < 0 )
+               continue;
+            if( where[col] >= start )
+               pd->vals[where[col]] += bc[q];
+            else
+            {
+               where[col] = p;
+               pd->colidx[p] = col;
+               pd->vals[p] = bc[q];
+               ++p;
+            }
+         }
+         {
+            /* drop entries that cancelled */
+            int64_t w = start;
+            int64_t t;
+            for( t = start; t < p; ++t )
+            {
+               if( pd->vals[t] != 0.0 )
+               {
+                  pd->colidx[w] = pd->colidx[t];
+                  pd->vals[w] = pd->vals[t];
+                  ++w;
+               }
+            }
+            p = w;
+         }
+         if( p == start )
+            continue;
+         if( !SCIPisInfinity(scip, -l) )
+            l -= constant;
+         if( !SCIPisInfinity(scip, r) )
+            r -= constant;
+         pd->lhs[pd->nrows] = SCIPisInfinity(scip, -l) ? -SCIPinfinity(scip) : l;
+         pd->rhs[pd->nrows] = SCIPisInfinity(scip, r) ? SCIPinfinity(scip) : r;
+         pd->nrows++;
+         pd->rowptr[pd->nrows] = p;
       }
-      if( !ok || p == start )
-         continue;
-      pd->lhs[pd->nrows] = SCIPisInfinity(scip, -l) ? -SCIPinfinity(scip) : l;
-      pd->rhs[pd->nrows] = SCIPisInfinity(scip, r) ? SCIPinfinity(scip) : r;
-      pd->nrows++;
-      pd->rowptr[pd->nrows] = p;
    }
+   SCIPfreeBufferArray(scip, &where);
+   SCIPfreeBufferArray(scip, &bc);
+   SCIPfreeBufferArray(scip, &bv);
    /* the column view for resolving conflicts, and room for the change log (columns times a few rounds) */
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->colptr, nvars + 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->rowidx, pd->rowptr[pd->nrows] > 0 ? pd->rowptr[pd->nrows] : 1) );
@@ -357,6 +534,23 @@ static SCIP_DECL_PARAMCHGD(paramChgdReplacelinear)
    return SCIP_OKAY;
 }
 
+/** replacespecialised = TRUE switches the propagation of setppc, logicor, knapsack and varbound off (their rows are
+ *  then propagated here, with `specialised` on) */
+static SCIP_DECL_PARAMCHGD(paramChgdReplacespecialised)
+{
+   if( SCIPparamGetBool(param) )
+   {
+      int h;
+      for( h = 1; h < NHDLRS; ++h )
+      {
+         char name[SCIP_MAXSTRLEN];
+         (void)SCIPsnprintf(name, SCIP_MAXSTRLEN, "constraints/%s/propfreq", HDLRS[h]);
+         SCIP_CALL( SCIPsetIntParam(scip, name, -1) );
+      }
+   }
+   return SCIP_OKAY;
+}
+
 static SCIP_DECL_PROPFREE(propFreeGpulinear)
 {
    SCIP_PROPDATA* pd = SCIPpropGetData(prop);
@@ -483,7 +677,6 @@ static SCIP_RETCODE analyzeCutoff(SCIP* scip, SCIP_PROPDATA* pd)
 static SCIP_DECL_PROPEXEC(propExecGpulinear)
 {
    SCIP_PROPDATA* pd = SCIPpropGetData(prop);
-   SCIP_CONSHDLR* conshdlr;
    int64_t nseed = -1;
    int32_t cutoff = 0;
    gbp_result res;
@@ -496,8 +689,7 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
       return SCIP_OKAY;
 
    /* constraints added or removed since the upload: rebuild */
-   conshdlr = SCIPfindConshdlr(scip, "linear");
-   if( (conshdlr == NULL ? 0 : SCIPconshdlrGetNConss(conshdlr)) != pd->nconss || SCIPgetNVars(scip) != pd->ncols )
+   if( countConss(scip, pd) != pd->nconss || SCIPgetNVars(scip) != pd->ncols )
    {
       SCIP_CALL( upload(scip, pd) );
       if( pd->failed )
@@ -780,6 +972,12 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacelinear",
          "switch off cons_linear's own propagation (constraints/linear/propfreq = -1) when included",
          &pd->replacelinear, FALSE, FALSE, paramChgdReplacelinear, NULL) );
+   SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/specialised",
+         "also propagate the rows of setppc, logicor, knapsack and varbound constraints (presolving upgrades linear "
+         "rows to these handlers)", &pd->specialised, FALSE, TRUE, NULL, NULL) );
+   SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacespecialised",
+         "switch off the propagation of setppc, logicor, knapsack and varbound (constraints/<handler>/propfreq = -1)",
+         &pd->replacespecialised, FALSE, FALSE, paramChgdReplacespecialised, NULL) );
    return SCIP_OKAY;
 }
 

@@ -6,8 +6,10 @@
  *   status <SCIP status>    obj <primal bound>    nodes <n>
  *   gpulinear <calls> <bound changes> <cutoffs> <cutoffs analysed> <resolve requests> <resolved> active <0|1>
  *   conflicts <conflicts found>    rangedreasons <changes and cutoffs explained by a ranged row>
- * With a fourth argument "ranged" ranged-row propagation is on in both modes (without artificial constraints).
- * Usage: solve_driver <instance.mps> <plain|gpulinear> [node limit] [ranged] */
+ * Flags after the node limit: "ranged" switches ranged-row propagation on in both modes (without artificial
+ * constraints); "presolve" keeps SCIP's presolving and its upgrades of linear rows to the specialised handlers
+ * (setppc, logicor, knapsack, varbound), whose propagation the plugin then replaces as well.
+ * Usage: solve_driver <instance file> <plain|gpulinear> [node limit] [ranged] [presolve] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -21,10 +23,18 @@ int main(int argc, char** argv)
    SCIP* scip = NULL;
    int gpulinear;
    long long nodelimit;
+   int ranged = 0;
+   int presolve = 0;
+   int k;
    if( argc < 3 )
       return 2;
    gpulinear = strcmp(argv[2], "gpulinear") == 0;
    nodelimit = argc > 3 ? atoll(argv[3]) : 200000;
+   for( k = 4; k < argc; ++k )
+   {
+      ranged = ranged || strcmp(argv[k], "ranged") == 0;
+      presolve = presolve || strcmp(argv[k], "presolve") == 0;
+   }
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( gpulinear )
@@ -32,18 +42,21 @@ int main(int argc, char** argv)
       if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
          return 1;
       SCIPsetBoolParam(scip, "propagating/gpulinear/replacelinear", TRUE);
+      if( presolve )
+         SCIPsetBoolParam(scip, "propagating/gpulinear/replacespecialised", TRUE);
    }
    if( SCIPreadProb(scip, argv[1], NULL) != SCIP_OKAY )
       return 3;
+   if( !presolve )
    {
       SCIP_PARAM** params = SCIPgetParams(scip);
-      int np = SCIPgetNParams(scip), k;
+      int np = SCIPgetNParams(scip);
       for( k = 0; k < np; ++k )
          if( strncmp(SCIPparamGetName(params[k]), "constraints/linear/upgrade/", 27) == 0 )
             SCIPsetBoolParam(scip, SCIPparamGetName(params[k]), FALSE);
+      SCIPsetIntParam(scip, "presolving/maxrounds", 0);
    }
-   SCIPsetIntParam(scip, "presolving/maxrounds", 0);
-   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", argc > 4 && strcmp(argv[4], "ranged") == 0);
+   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", ranged);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);
    SCIPsetBoolParam(scip, "conflict/enable", TRUE);

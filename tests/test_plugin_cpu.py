@@ -97,9 +97,9 @@ def solve_driver(tmp_path_factory, oracle_mod):
     return exe
 
 
-def _solve(exe, path, mode, ranged=False):
-    r = subprocess.run([exe, path, mode, "200000"] + (["ranged"] if ranged else []), capture_output=True, text=True,
-                       timeout=600)
+def _solve(exe, path, mode, ranged=False, presolve=False):
+    flags = (["ranged"] if ranged else []) + (["presolve"] if presolve else [])
+    r = subprocess.run([exe, path, mode, "200000"] + flags, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     return dict(l.split(" ", 1) for l in r.stdout.strip().splitlines() if " " in l)
 
@@ -142,3 +142,21 @@ def test_plugin_ranged_rows_in_search(solve_driver, tmp_path, seed):
     assert active == "1" and int(calls) > 0
     assert asked == resolved
     assert int(gpu["rangedreasons"]) > 0
+
+
+@pytest.mark.parametrize("name", ["enigma", "flugpl", "misc03"])
+def test_plugin_replaces_the_specialised_handlers_after_presolving(solve_driver, oracle_mod, name):
+    """SCIP's presolving on: linear rows are upgraded to setppc, logicor, knapsack and varbound constraints.  The
+    plugin reads their rows (over active variables: negated, aggregated and fixed variables resolved) and, with
+    replacespecialised, replaces those handlers' propagation as well as cons_linear's.  Both searches prove the same
+    optimum, and every reason SCIP asks for is explained."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    plain = _solve(solve_driver, path, "plain", presolve=True)
+    gpu = _solve(solve_driver, path, "gpulinear", presolve=True)
+    assert plain["status"] == "optimal" and gpu["status"] == "optimal"
+    assert float(plain["obj"]) == float(gpu["obj"])
+    calls, chg, cut, analysed, asked, resolved, _, active = gpu["gpulinear"].split()
+    assert active == "1" and int(calls) > 0 and int(chg) > 0
+    assert asked == resolved
