@@ -808,14 +808,24 @@ __device__ __forceinline__ long long coefInt(const Num& s, double v) {
   const double x = fabs(v) + s.feastol;
   return x >= 4.0e18 ? 4000000000000000000LL : (long long)x;
 }
-// greatest common divisor of positive integers (the value SCIPcalcGreComDiv, misc.c:9197, computes)
+// greatest common divisor of non-negative integers (the value SCIPcalcGreComDiv, misc.c:9197, computes), by the
+// binary method: shifts and subtractions instead of 64-bit divisions, which the GPU emulates in software
 __device__ __forceinline__ long long gcd64(long long a, long long b) {
-  while (b != 0) {
-    const long long t = a % b;
-    a = b;
-    b = t;
-  }
-  return a;
+  unsigned long long u = (unsigned long long)a, v = (unsigned long long)b;
+  if (u == 0) return (long long)v;
+  if (v == 0) return (long long)u;
+  const int shift = __ffsll((long long)(u | v)) - 1;
+  u >>= __ffsll((long long)u) - 1;
+  do {
+    v >>= __ffsll((long long)v) - 1;
+    if (u > v) {
+      const unsigned long long t = u;
+      u = v;
+      v = t;
+    }
+    v -= u;
+  } while (v != 0);
+  return (long long)(u << shift);
 }
 __device__ __forceinline__ bool epsIntegral(const Num& s, double x) { return x - floor(x + s.eps) <= s.eps; }
 __device__ __forceinline__ double epsFloor(const Num& s, double x) { return floor(x + s.eps); }
@@ -861,10 +871,11 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   if (isHuge(s, fabs(fixedact))) return false;
   const double lhs = P.lhs[i] - fixedact, rhs = P.rhs[i] - fixedact;
 
-  // partition (cons_linear.c:5839-5958); membership of position k is recomputed from the running gcd, whose
-  // changes are recorded as (position, gcd after it)
+  // partition (cons_linear.c:5839-5958); membership of position k is kept as a bit for the first 64 positions and
+  // recomputed beyond from the running gcd, whose changes are recorded as (position, gcd after it)
   int ninf = 0, ncont = 0, first = -1, kstart;
   bool gcdisone = true, possiblegcd = true;
+  unsigned long long memb = 0ull;  // membership of the first 64 positions
   int k = -1;
   bool fx;
   do {
@@ -881,6 +892,7 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
         possiblegcd = false;
         ++ninf;
         if (first < 0) first = k;
+        if (k < 64) memb |= 1ull << k;
       }
       ++k;
     }
@@ -917,11 +929,13 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
       possiblegcd = false;
       ++ninf;
       if (first < 0) first = k;
+      if (k < 64) memb |= 1ull << k;
     } else {
       const long long t = gcd64(gcd, coefInt(s, v));
       if (t == 1) {
         ++ninf;
         if (first < 0) first = k;
+        if (k < 64) memb |= 1ull << k;
       } else if (t != gcd) {
         if (nchg < RANGED_MAXCHG) {
           chgpos[nchg] = k;
@@ -935,6 +949,7 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   if (ninf == 0) return false;
   // is position k (unfixed) one of the entries that may lead to infeasibility?
   auto member = [&](int kk, int j, double v) {
+    if (kk < 64) return ((memb >> kk) & 1ull) != 0;
     if (kk < kstart || !qual(j, v)) return true;
     long long gb = g0;
     for (int t = 0; t < nchg && chgpos[t] < kk; ++t) gb = chgval[t];
