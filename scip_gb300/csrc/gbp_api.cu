@@ -57,6 +57,10 @@ struct gbp_ctx {
   int32_t* d_rperm = nullptr;
   int32_t* d_rtmp = nullptr;
   int nranged = 0;
+  long long* d_rcoef = nullptr;  // per entry of a ranged row: its classification (Prob::rcoef)
+  double2* d_rdom = nullptr;   // the domain d_rperm was sorted on (a fixed-domain order is reused while it holds)
+  int* d_rchanged = nullptr;
+  bool rdom_valid = false;
 
   // plain path
   double* d_lb = nullptr;
@@ -141,7 +145,7 @@ static void freeProblem(gbp_ctx* ctx) {
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
                   ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub, ctx->d_relig,
-                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp};
+                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp, ctx->d_rdom, ctx->d_rchanged, ctx->d_rcoef};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -153,6 +157,7 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_glb = nullptr; ctx->d_gub = nullptr; ctx->cap_glob = 0; ctx->has_global = false;
   ctx->d_relig = nullptr; ctx->d_rlist = nullptr; ctx->d_rperm = nullptr; ctx->d_rtmp = nullptr;
   ctx->ranged_ready = false; ctx->nranged = 0;
+  ctx->d_rdom = nullptr; ctx->d_rchanged = nullptr; ctx->rdom_valid = false; ctx->d_rcoef = nullptr;
   ctx->cap_m = ctx->cap_n = ctx->cap_nnz = ctx->cap_inst = 0;
   ctx->stage_bytes = 0;
   ctx->nslots = 0;
@@ -173,6 +178,7 @@ static Prob devProb(const gbp_ctx* ctx, bool instances = false, bool nodes = fal
     P.relig = ctx->d_relig;
     P.rperm = ctx->d_rperm;
     P.rtmp = ctx->d_rtmp;
+    P.rcoef = ctx->d_rcoef;
     P.rsorted = sorted ? 1 : 0;
     // the sorted order follows the bounds being propagated when there is no other global domain (at the root
     // SCIP re-sorts a row whenever one of its columns becomes binary); every other order is fixed for a call
@@ -567,13 +573,18 @@ static int prepareRanged(gbp_ctx* ctx, bool instances, bool nodes, const double*
       CK(cudaMalloc(&ctx->d_rlist, (size_t)ctx->cap_m * sizeof(int)));
       CK(cudaMalloc(&ctx->d_rperm, (size_t)ctx->cap_nnz * sizeof(int32_t)));
       CK(cudaMalloc(&ctx->d_rtmp, (size_t)ctx->cap_nnz * sizeof(int32_t)));
+      CK(cudaMalloc(&ctx->d_rdom, (size_t)ctx->cap_n * sizeof(double2)));
+      CK(cudaMalloc(&ctx->d_rcoef, (size_t)ctx->cap_nnz * sizeof(long long)));
+      CK(cudaMalloc(&ctx->d_rchanged, sizeof(int)));
     }
+    ctx->rdom_valid = false;
     destroyGraphs(ctx);  // the graphs hold the ranged rows' pointers
     int* count = ctx->d_ctr + 6;
     CK(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
     if (ctx->m) {
       const Prob P = devProb(ctx, instances, nodes);
-      CK(launchRangedElig(ctx->stream, gridFor(ctx, ctx->m), ctx->num, P, ctx->d_relig, ctx->d_rlist, count));
+      CK(launchRangedElig(ctx->stream, gridFor(ctx, ctx->m), ctx->num, P, ctx->d_relig, ctx->d_rlist, count,
+                          ctx->d_rcoef));
       *launches += 1;
     }
     int h = 0;
@@ -583,10 +594,15 @@ static int prepareRanged(gbp_ctx* ctx, bool instances, bool nodes, const double*
     ctx->ranged_ready = true;
   }
   const Prob P = devProb(ctx, instances, nodes);
-  if (!P.rlive && ctx->nranged > 0) {
+  if (P.rlive) {
+    ctx->rdom_valid = false;  // the rows' order is rewritten where they are evaluated
+  } else if (ctx->nranged > 0) {
+    // the order is sorted again only if the domain differs from the one it was sorted on
+    CK(cudaMemsetAsync(ctx->d_rchanged, ctx->rdom_valid ? 0 : 0xff, sizeof(int), ctx->stream));
     CK(launchRangedOrder(ctx->stream, gridFor(ctx, ctx->nranged, 128, 8), P, ctx->d_rlist, ctx->nranged, dl, du,
-                         P.rsorted));
-    *launches += 1;
+                         P.rsorted, ctx->d_rdom, ctx->d_rchanged, gridFor(ctx, ctx->n, 256, 8)));
+    ctx->rdom_valid = true;
+    *launches += 2;
   }
   return GBP_OK;
 }

@@ -51,6 +51,8 @@ struct Prob {
   const uint8_t* relig;
   int32_t* rperm;
   int32_t* rtmp;
+  const long long* rcoef;  // per entry of such a row: >= 0 (long long)(|a| + feastol) of an integral column with an
+                           // integral coefficient other than +-1; -1 another entry with |a| = 1; -2 any other entry
   int rlive;
   int rsorted;
 };
@@ -836,8 +838,16 @@ constexpr long long RANGED_MAXIT = 1LL << 20;
 // the running gcd of the partition changes at most 62 times (it at least halves each time)
 constexpr int RANGED_MAXCHG = 64;
 
+// what an entry is to the ranged-row rule (the per-entry values of Prob::rcoef)
+__device__ __forceinline__ long long rangedCoef(const Num& s, bool isint, double v) {
+  if (isint && epsIntegral(s, v) && !eq(s, fabs(v), 1.0)) return coefInt(s, v);
+  return eq(s, fabs(v), 1.0) ? -1 : -2;
+}
+
 // Row i's ranged-row deductions from the bounds B (forced candidates, as SCIP's come with force = TRUE);
-// returns true on cutoff.  One thread.
+// returns true on cutoff.  One thread.  The entries' classification comes precomputed (P.rcoef); which entries are
+// fixed is kept as bits for the first 64 positions, so that the passes after the first read bounds only where they
+// need the values.
 template <class BND>
 __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cands& C, Stats& st) {
   const int64_t p0 = P.rowptr[i];
@@ -854,11 +864,11 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     B.get(j, l, u);
     return eq(s, l, u);
   };
-  auto qual = [&](int j, double v) { return P.isint[j] != 0 && epsIntegral(s, v) && !eq(s, fabs(v), 1.0); };
 
   // fixed activity, last entry first (cons_linear.c:5803-5814)
   double fixedact = 0.0;
   int nfixed = 0;
+  unsigned long long fixm = 0ull;  // fixed entries among the first 64 positions
   for (int k = len - 1; k >= 0; --k) {
     int64_t p;
     int j;
@@ -866,10 +876,19 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     if (fixedAt(k, p, j, v, l, u)) {
       fixedact += l * v;
       ++nfixed;
+      if (k < 64) fixm |= 1ull << k;
     }
   }
   if (isHuge(s, fabs(fixedact))) return false;
   const double lhs = P.lhs[i] - fixedact, rhs = P.rhs[i] - fixedact;
+  auto isFixed = [&](int k) {
+    if (k < 64) return ((fixm >> k) & 1ull) != 0;
+    double l, u;
+    B.get(P.colidx[p0 + ord[k]], l, u);
+    return eq(s, l, u);
+  };
+  auto coefAt = [&](int k) { return P.rcoef[p0 + ord[k]]; };
+  auto contAt = [&](int k) { return P.isint[P.colidx[p0 + ord[k]]] == 0; };
 
   // partition (cons_linear.c:5839-5958); membership of position k is kept as a bit for the first 64 positions and
   // recomputed beyond from the running gcd, whose changes are recorded as (position, gcd after it)
@@ -877,18 +896,12 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   bool gcdisone = true, possiblegcd = true;
   unsigned long long memb = 0ull;  // membership of the first 64 positions
   int k = -1;
-  bool fx;
   do {
     ++k;
-    while (k < len) {
-      int64_t p;
-      int j;
-      double v, l, u;
-      fx = fixedAt(k, p, j, v, l, u);
-      if (qual(j, v)) break;
-      if (!fx) {
-        if (P.isint[j] == 0) ++ncont;
-        gcdisone = gcdisone && eq(s, fabs(v), 1.0);
+    while (k < len && coefAt(k) < 0) {
+      if (!isFixed(k)) {
+        if (contAt(k)) ++ncont;
+        gcdisone = gcdisone && coefAt(k) == -1;
         possiblegcd = false;
         ++ninf;
         if (first < 0) first = k;
@@ -896,42 +909,26 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
       }
       ++k;
     }
-    if (k >= len) break;
-    {
-      int64_t p;
-      int j;
-      double v, l, u;
-      fx = fixedAt(k, p, j, v, l, u);
-    }
-  } while (fx);
+  } while (k < len && isFixed(k));
   if (k >= len || ncont + 2 > len - nfixed) return false;
   kstart = k;
-  long long g0;
-  {
-    int64_t p;
-    int j;
-    double v, l, u;
-    fixedAt(k, p, j, v, l, u);
-    g0 = coefInt(s, v);
-  }
+  const long long g0 = coefAt(k);
   int chgpos[RANGED_MAXCHG];
   long long chgval[RANGED_MAXCHG];
   int nchg = 0;
   long long gcd = g0;
   for (; k < len; ++k) {
-    int64_t p;
-    int j;
-    double v, l, u;
-    if (fixedAt(k, p, j, v, l, u)) continue;
-    if (!qual(j, v)) {
-      if (P.isint[j] == 0) ++ncont;
-      gcdisone = gcdisone && eq(s, fabs(v), 1.0);
+    if (isFixed(k)) continue;
+    const long long ck = coefAt(k);
+    if (ck < 0) {
+      if (contAt(k)) ++ncont;
+      gcdisone = gcdisone && ck == -1;
       possiblegcd = false;
       ++ninf;
       if (first < 0) first = k;
       if (k < 64) memb |= 1ull << k;
     } else {
-      const long long t = gcd64(gcd, coefInt(s, v));
+      const long long t = gcd64(gcd, ck);
       if (t == 1) {
         ++ninf;
         if (first < 0) first = k;
@@ -947,13 +944,14 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     }
   }
   if (ninf == 0) return false;
-  // is position k (unfixed) one of the entries that may lead to infeasibility?
-  auto member = [&](int kk, int j, double v) {
+  // is position kk (unfixed) one of the entries that may lead to infeasibility?
+  auto member = [&](int kk) {
     if (kk < 64) return ((memb >> kk) & 1ull) != 0;
-    if (kk < kstart || !qual(j, v)) return true;
+    const long long ck = coefAt(kk);
+    if (kk < kstart || ck < 0) return true;
     long long gb = g0;
     for (int t = 0; t < nchg && chgpos[t] < kk; ++t) gb = chgval[t];
-    return gcd64(gb, coefInt(s, v)) == 1;
+    return gcd64(gb, ck) == 1;
   };
 
   // activity bounds of those entries, last first (cons_linear.c:5975-6015)
@@ -962,7 +960,8 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     int64_t p;
     int j;
     double v, l, u;
-    if (fixedAt(k, p, j, v, l, u) || !member(k, j, v)) continue;
+    if (isFixed(k) || !member(k)) continue;
+    fixedAt(k, p, j, v, l, u);
     bool mininv = false, maxinv = false;
     if (isInf(s, -l)) {
       if (v < 0.0) maxinv = true;
@@ -997,11 +996,8 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   long long gcdinf = -1;
   if (possiblegcd) {
     for (k = len - 1; k >= 0; --k) {
-      int64_t p;
-      int j;
-      double v, l, u;
-      if (fixedAt(k, p, j, v, l, u) || !member(k, j, v)) continue;
-      gcdinf = gcdinf < 0 ? coefInt(s, v) : gcd64(gcdinf, coefInt(s, v));
+      if (isFixed(k) || !member(k)) continue;
+      gcdinf = gcdinf < 0 ? coefAt(k) : gcd64(gcdinf, coefAt(k));
       if (gcdinf < 2) break;
     }
   } else if (gcdisone) {
@@ -1049,10 +1045,7 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
   } else if (ninf == len - nfixed - 1) {
     // the one unfixed entry outside them (fixed :6184-6283, bounded :6354-6552)
     for (k = 0; k < len; ++k) {
-      int64_t p;
-      int j;
-      double v, l, u;
-      if (!fixedAt(k, p, j, v, l, u) && !member(k, j, v)) {
+      if (!isFixed(k) && !member(k)) {
         target = k;
         break;
       }

@@ -102,9 +102,10 @@ cudaError_t launchNodeOrder(cudaStream_t st, int grid, int64_t nnodes, const int
 // ranged rows: flag the rows the gcd rule can act on and list them (count must be zeroed); the entry order of
 // listed rows on the global domain dl/du
 cudaError_t launchRangedElig(cudaStream_t st, int grid, const Num& s, const Prob& P, uint8_t* elig, int* list,
-                             int* count);
+                             int* count, long long* coef);
+// (saved: the domain of the last order, *changed preset to 1 to force the sort; both kernels on st)
 cudaError_t launchRangedOrder(cudaStream_t st, int grid, const Prob& P, const int* list, int n, const double* dl,
-                              const double* du, int sorted);
+                              const double* du, int sorted, double2* saved, int* changed, int dgrid);
 // instance parts: shift local row pointers / column indices by the parts' offsets, fill the instance maps
 cudaError_t launchFixParts(cudaStream_t st, int grid, int64_t ninst, const int64_t* off, int64_t m, int64_t n,
                            int64_t nnz, int64_t* rowptr, int32_t* colidx, int32_t* rowinst, int32_t* colinst, int* bad);

@@ -317,17 +317,18 @@ __global__ void k_fix_parts(int64_t ninst, const int64_t* off, int64_t m, int64_
 
 // Ranged rows: the rows the gcd rule can act on -- three or more entries, both sides finite, and an integral
 // column with an integral coefficient other than +-1 (rangedRowPropagation returns at once for any other row,
-// cons_linear.c:5770-5777, :5839-5869) -- flagged and compacted into list (any order).
-__global__ void k_ranged_elig(Num s, Prob P, uint8_t* elig, int* list, int* count) {
+// cons_linear.c:5770-5777, :5839-5869) -- flagged and compacted into list (any order), with the classification of
+// their entries (coef, see Prob::rcoef).
+__global__ void k_ranged_elig(Num s, Prob P, uint8_t* elig, int* list, int* count, long long* coef) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.m; i += stride) {
     const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
-    bool ok = p1 - p0 >= 3 && !isInf(s, -P.lhs[i]) && !isInf(s, P.rhs[i]);
-    if (ok) {
-      ok = false;
-      for (int64_t p = p0; p < p1 && !ok; ++p) {
-        const double v = P.vals[p];
-        ok = P.isint[P.colidx[p]] != 0 && epsIntegral(s, v) && !eq(s, fabs(v), 1.0);
+    bool ok = false;
+    if (p1 - p0 >= 3 && !isInf(s, -P.lhs[i]) && !isInf(s, P.rhs[i])) {
+      for (int64_t p = p0; p < p1; ++p) {
+        const long long c = rangedCoef(s, P.isint[P.colidx[p]] != 0, P.vals[p]);
+        coef[p] = c;
+        ok = ok || c >= 0;
       }
     }
     elig[i] = ok ? 1 : 0;
@@ -335,8 +336,27 @@ __global__ void k_ranged_elig(Num s, Prob P, uint8_t* elig, int* list, int* coun
   }
 }
 
-// the entry order of the listed rows on a global domain fixed for the call (one thread per row)
-__global__ void k_ranged_order(Prob P, const int* list, int n, const double* dl, const double* du, int sorted) {
+// the domain the rows' order was last computed on (saved) against this call's: *changed becomes nonzero if any
+// column differs, and saved takes the new values
+__global__ void k_ranged_domain(const double* dl, const double* du, double2* saved, int64_t n, int* changed) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  bool diff = false;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += stride) {
+    const double2 o = saved[j];
+    const double l = dl[j], u = du[j];
+    if (__double_as_longlong(o.x) != __double_as_longlong(l) || __double_as_longlong(o.y) != __double_as_longlong(u)) {
+      diff = true;
+      saved[j] = make_double2(l, u);
+    }
+  }
+  if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+
+// the entry order of the listed rows on a global domain fixed for the call (one thread per row), when that domain
+// changed since the order was last computed
+__global__ void k_ranged_order(Prob P, const int* list, int n, const double* dl, const double* du, int sorted,
+                               const int* changed) {
+  if (*changed == 0) return;
   auto dom = [&](int j, double& l, double& u) {
     l = dl[j];
     u = du[j];
@@ -402,14 +422,15 @@ __global__ void __launch_bounds__(256) k_order_scatter(int64_t nnodes, const int
 
 // ------------------------------------------------------------------------------------------ launchers
 cudaError_t launchRangedElig(cudaStream_t st, int grid, const Num& s, const Prob& P, uint8_t* elig, int* list,
-                             int* count) {
-  k_ranged_elig<<<grid, 256, 0, st>>>(s, P, elig, list, count);
+                             int* count, long long* coef) {
+  k_ranged_elig<<<grid, 256, 0, st>>>(s, P, elig, list, count, coef);
   return cudaGetLastError();
 }
 cudaError_t launchRangedOrder(cudaStream_t st, int grid, const Prob& P, const int* list, int n, const double* dl,
-                              const double* du, int sorted) {
+                              const double* du, int sorted, double2* saved, int* changed, int dgrid) {
   if (n <= 0) return cudaSuccess;
-  k_ranged_order<<<grid, 128, 0, st>>>(P, list, n, dl, du, sorted);
+  k_ranged_domain<<<dgrid, 256, 0, st>>>(dl, du, saved, P.n, changed);
+  k_ranged_order<<<grid, 128, 0, st>>>(P, list, n, dl, du, sorted, changed);
   return cudaGetLastError();
 }
 cudaError_t launchFixParts(cudaStream_t st, int grid, int64_t ninst, const int64_t* off, int64_t m, int64_t n,
