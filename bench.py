@@ -308,6 +308,8 @@ def main():
     ap.add_argument("--family", default="mip", choices=["mip", "gcd"],
                     help="nodes workload matrix: mip (log-uniform coefficients) or gcd (ranged rows sharing a divisor)")
     ap.add_argument("--ranged", action="store_true", help="ranged-row propagation on (GBP_FLAG_RANGEDROW)")
+    ap.add_argument("--rows", type=int, default=200_000,
+                    help="nodes workload: rows of the matrix (columns = 2 x rows); smaller for profiling captures")
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serving: arrival rates (req/s)")
     ap.add_argument("--duration", type=float, default=1.0, help="serving: seconds of arrivals per rate")
     args = ap.parse_args()
@@ -321,12 +323,13 @@ def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from scip_gb300 import instances
 
-    config = {"workload": "batched B&B nodes: 200,000 x 400,000 rows/cols, ~4.5M nnz, 4,096 nodes fixing 1-64 "
+    size = f"{args.rows:,} x {2 * args.rows:,}"
+    config = {"workload": f"batched B&B nodes: {size} rows/cols, ~4.5M nnz, {args.nodes:,} nodes fixing 1-64 "
                           "integer columns each, every node to fixpoint" if args.family == "mip" else
-                          "batched B&B nodes: 200,000 x 400,000 gcd rows (3..8 entries, 1 % 65..200; half equations), "
-                          "4,096 nodes fixing 1-64 integer columns each, every node to fixpoint",
+                          f"batched B&B nodes: {size} gcd rows (3..8 entries, 1 % 65..200; half equations), "
+                          f"{args.nodes:,} nodes fixing 1-64 integer columns each, every node to fixpoint",
               "ranged_rows": bool(args.ranged),
-              "rows": 200000, "cols": 400000, "nodes_per_step": args.nodes, "rule": "residual (maxeasyactivitydelta="
+              "rows": args.rows, "cols": 2 * args.rows, "nodes_per_step": args.nodes, "rule": "residual (maxeasyactivitydelta="
               f"{args.maxeasy:g})", "l2": "flushed between timed steps (256 MiB write)",
               "parallelism": f"replicas x{world}"}
 
@@ -336,7 +339,7 @@ def main():
         import oracle as orc
 
         orc.build()
-        inst = build_workload(family=args.family)
+        inst = build_workload(family=args.family, m=args.rows, n=2 * args.rows)
         o = orc.Oracle(inst)
         par = orc.params(args.maxeasy, ranged=args.ranged)
         rlb, rub, _ = o.propagate(inst.lb, inst.ub, par)
@@ -371,7 +374,7 @@ def main():
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
 
-    inst = build_workload(family=args.family)
+    inst = build_workload(family=args.family, m=args.rows, n=2 * args.rows)
     prop = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy, ranged=args.ranged))
     prop.upload(inst)
     rlb, rub, rcut, rres = prop.propagate(inst.lb, inst.ub)
