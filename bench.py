@@ -162,6 +162,12 @@ def other_workload(args):
         cfg = {"workload": f"{units} distinct instances (set cover / multi-knapsack / network flow), rows log-uniform "
                            "in [1e3, 2e5], all in one block-diagonal problem, every instance to its root fixpoint",
                "rows": big.m, "cols": big.n, "nnz": big.nnz}
+    elif args.workload == "root":
+        big = instances.root_mip(seed=0)
+        units = 1
+        cfg = {"workload": "one 2,000 x 5,000 instance (row lengths 5..15, integer coefficients, 10 % ranged rows and "
+                           "10 % equations), root fixpoint through the plain path", "rows": big.m, "cols": big.n,
+               "nnz": big.nnz}
     else:
         big = instances.zipf_mip(seed=1)
         units = 1
@@ -232,6 +238,19 @@ def other_workload(args):
         line["cpu_baseline"] = {"value": len(take) / dt, "unit": "instance-fixpoints/s", "cores": os.cpu_count() or 1,
                                 "kind": "port", "sample": f"{len(take)} of {len(insts)} instances, {dt:.2f} s "
                                                           "(includes the oracle's CSC build per instance)"}
+    if args.workload == "root" and not args.quick:
+        import oracle as orc
+
+        orc.build()
+        o = orc.Oracle(big)
+        par = orc.params(args.maxeasy)
+        k, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 2.0:
+            o.propagate(big.lb, big.ub, par)
+            k += 1
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": k / dt, "unit": "instance-fixpoints/s", "cores": 1, "kind": "port",
+                                "sample": f"{k} root fixpoints in {dt:.2f} s on one thread"}
     print(json.dumps(line))
     prop.close()
 
@@ -301,9 +320,10 @@ def main():
     ap.add_argument("--maxeasy", type=float, default=0.0)
     ap.add_argument("--quick", action="store_true", help="skip the plain-path and CPU arms (profiling runs)")
     ap.add_argument("--shape", default="", help="threads_per_node,ctas_per_sm instead of autotuning (e.g. 128,0)")
-    ap.add_argument("--workload", default="nodes", choices=["nodes", "uneven", "zipf", "serving"],
+    ap.add_argument("--workload", default="nodes", choices=["nodes", "uneven", "zipf", "root", "serving"],
                     help="nodes: batched B&B nodes (headline); uneven: 512 distinct instances in one problem; "
-                         "zipf: one 1M x 2M instance through the plain path")
+                         "zipf: one 1M x 2M instance through the plain path; root: the 2,000 x 5,000 instance "
+                         "through the plain path")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--family", default="mip", choices=["mip", "gcd"],
                     help="nodes workload matrix: mip (log-uniform coefficients) or gcd (ranged rows sharing a divisor)")
