@@ -551,6 +551,15 @@ static SCIP_DECL_PARAMCHGD(paramChgdReplacespecialised)
    return SCIP_OKAY;
 }
 
+/** copies the propagator into sub-SCIPs (heuristics' sub-MIPs, concurrent solvers): they copy the parameters,
+ *  including constraints/linear/propfreq = -1 when replacelinear is set, so they need the propagator as well; each
+ *  copy opens its own context on the device */
+static SCIP_DECL_PROPCOPY(propCopyGpulinear)
+{
+   SCIP_CALL( SCIPincludePropGpulinear(scip) );
+   return SCIP_OKAY;
+}
+
 static SCIP_DECL_PROPFREE(propFreeGpulinear)
 {
    SCIP_PROPDATA* pd = SCIPpropGetData(prop);
@@ -963,6 +972,7 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    memset(pd, 0, sizeof(*pd));
    SCIP_CALL( SCIPincludePropBasic(scip, &prop, PROP_NAME, PROP_DESC, PROP_PRIORITY, PROP_FREQ, PROP_DELAY,
          PROP_TIMING, propExecGpulinear, pd) );
+   SCIP_CALL( SCIPsetPropCopy(scip, prop, propCopyGpulinear) );
    SCIP_CALL( SCIPsetPropFree(scip, prop, propFreeGpulinear) );
    SCIP_CALL( SCIPsetPropInitsol(scip, prop, propInitsolGpulinear) );
    SCIP_CALL( SCIPsetPropExitsol(scip, prop, propExitsolGpulinear) );
