@@ -1320,7 +1320,8 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  ctx->slot_stamp_budget += (nnodes / std::max(grid, 1) + 1) * ((int64_t)st[5] + 2);
+  // the queue is dynamic: one slot may have run every node of the call, not just its average share
+  ctx->slot_stamp_budget += (nnodes + 1) * ((int64_t)st[5] + 2);
   if (res) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
