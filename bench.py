@@ -126,33 +126,45 @@ def build_workload(seed=2, nnodes=NNODES, m=200_000, n=400_000, family="mip"):
     return inst
 
 
-def cpu_arm(inst, rlb, rub, nodes, par, nthreads, budget_s=15.0, min_wall_s=0.0):
-    """Oracle over a bounded sample of nodes: the first nodes of the batch, growing until the sample takes a
-    quarter of budget_s or is the whole batch; a whole batch that takes less than min_wall_s is repeated until it
-    does.  Returns (node-fixpoints/s, sample description)."""
-    import oracle as orc
-    from scip_gb300.instances import NodeBatch
+class CpuArm:
+    """The oracle over a bounded sample of the node batch.  plan() fixes the sample once: the first nodes of the
+    batch, growing until they take a quarter of budget_s or are the whole batch, and a whole batch that takes less
+    than min_wall_s is repeated until it does.  run() times one sample and returns (node-fixpoints/s, sample
+    description)."""
 
-    o = orc.Oracle(inst)
-    take = 256
-    while True:
-        k = min(take, nodes.nnodes)
-        sub = NodeBatch(nodes.ptr[:k + 1].copy(), nodes.col[:nodes.ptr[k]], nodes.lb[:nodes.ptr[k]],
-                        nodes.ub[:nodes.ptr[k]])
+    def __init__(self, inst, rlb, rub, nodes, par, nthreads):
+        import oracle as orc
+
+        self.o = orc.Oracle(inst)
+        self.rlb, self.rub, self.nodes, self.par, self.nthreads = rlb, rub, nodes, par, nthreads
+        self.sub, self.k, self.reps = None, 0, 1
+
+    def _once(self):
         t0 = time.perf_counter()
-        o.propagate_nodes(rlb, rub, sub, par, cap=1, nthreads=nthreads)
-        dt = time.perf_counter() - t0
-        if dt > budget_s / 4 or k == nodes.nnodes:
-            break
-        take *= 4
-    reps = 1
-    if k == nodes.nnodes and dt < min_wall_s:
-        reps = int(np.ceil(min_wall_s / max(dt, 1e-6)))
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            o.propagate_nodes(rlb, rub, sub, par, cap=1, nthreads=nthreads)
-        dt = time.perf_counter() - t0
-    return k * reps / dt, f"{reps} x {k} of {nodes.nnodes} nodes, {nthreads} threads, {dt:.2f} s wall"
+        self.o.propagate_nodes(self.rlb, self.rub, self.sub, self.par, cap=1, nthreads=self.nthreads)
+        return time.perf_counter() - t0
+
+    def plan(self, budget_s=15.0, min_wall_s=0.0):
+        from scip_gb300.instances import NodeBatch
+
+        nodes = self.nodes
+        take = 256
+        while True:
+            k = min(take, nodes.nnodes)
+            self.sub = NodeBatch(nodes.ptr[:k + 1].copy(), nodes.col[:nodes.ptr[k]], nodes.lb[:nodes.ptr[k]],
+                                 nodes.ub[:nodes.ptr[k]])
+            dt = self._once()
+            if dt > budget_s / 4 or k == nodes.nnodes:
+                break
+            take *= 4
+        self.k = k
+        self.reps = int(np.ceil(min_wall_s / max(dt, 1e-6))) if k == nodes.nnodes and dt < min_wall_s else 1
+        return self
+
+    def run(self):
+        dt = sum(self._once() for _ in range(self.reps))
+        return self.k * self.reps / dt, (f"{self.reps} x {self.k} of {self.nodes.nnodes} nodes, {self.nthreads} "
+                                         f"threads, {dt:.2f} s wall")
 
 
 def other_workload(args):
@@ -375,14 +387,15 @@ def main():
         rlb, rub, _ = o.propagate(inst.lb, inst.ub, par)
         nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3)
         threads = os.cpu_count() or 1
-        # each step a bounded sample, sized so that the whole run takes about a minute and a half
-        per_step = min(1.0, max(0.05, 90.0 / max(args.steps, 1)))
+        # each step a bounded sample, sized so that the whole run takes a minute or two
+        per_step = min(1.0, max(0.05, 60.0 / max(args.steps, 1)))
+        arm = CpuArm(inst, rlb, rub, nodes, par, threads).plan(budget_s=4.0 * per_step, min_wall_s=per_step)
         for _ in range(args.warmup):
-            cpu_arm(inst, rlb, rub, nodes, par, threads, budget_s=4.0 * per_step, min_wall_s=per_step)
+            arm.run()
         rates = []
         sample = ""
         for _ in range(args.steps):
-            r, sample = cpu_arm(inst, rlb, rub, nodes, par, threads, budget_s=4.0 * per_step, min_wall_s=per_step)
+            r, sample = arm.run()
             rates.append(r)
         v = float(np.mean(rates))
         print(json.dumps({"impl": "reference", "metric": "node-fixpoints/sec", "value": v, "unit": "node-fixpoints/s",
@@ -545,7 +558,7 @@ def main():
 
             orc.build()
             par = orc.params(args.maxeasy, ranged=args.ranged)
-            cpu_v, sample = cpu_arm(inst, rlb, rub, nodes, par, os.cpu_count() or 1, min_wall_s=1.0)
+            cpu_v, sample = CpuArm(inst, rlb, rub, nodes, par, os.cpu_count() or 1).plan(min_wall_s=1.0).run()
             line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
                                     "kind": "port", "sample": sample}
         print(json.dumps(line))
