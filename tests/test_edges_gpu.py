@@ -1,0 +1,116 @@
+"""Edge cases of the CUDA path against the oracle, through the C ABI: empty, free and single-entry rows, a problem
+without rows, degenerate node batches (no nodes, nodes without changes, changes outside the base domain), and
+bounds at the huge and infinite thresholds (numerics/hugeval 1e15, numerics/infinity 1e20)."""
+import numpy as np
+import pytest
+
+from scip_gb300 import gbp, instances
+from scip_gb300.instances import INF, Instance, NodeBatch
+from test_parity_gpu import _nodes_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _inst(rows, lb, ub, isint):
+    rowptr, cols, vals, lhs, rhs = [0], [], [], [], []
+    for c, v, lo, hi in rows:
+        cols += c
+        vals += v
+        rowptr.append(len(cols))
+        lhs.append(lo)
+        rhs.append(hi)
+    n = len(lb)
+    return Instance(np.array(rowptr, np.int64), np.array(cols, np.int32), np.array(vals, float), np.array(lhs, float),
+                    np.array(rhs, float), np.array(lb, float), np.array(ub, float), np.array(isint, np.int8),
+                    x0=np.zeros(n))
+
+
+def _same_root(gpu_prop, oracle_mod, inst, maxeasy=0.0):
+    gpu_prop.set_params(gbp.default_params(maxeasy=maxeasy))
+    gpu_prop.upload(inst)
+    lb, ub, cut, res = gpu_prop.propagate(inst.lb, inst.ub)
+    olb, oub, ores = oracle_mod.Oracle(inst).propagate(inst.lb, inst.ub, oracle_mod.params(maxeasy))
+    assert cut == bool(ores.cutoff)
+    assert res.rounds == ores.rounds
+    if not cut:
+        assert np.array_equal(lb, olb) and np.array_equal(ub, oub)
+    return lb, ub, cut
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_empty_free_and_single_entry_rows(gpu_prop, oracle_mod, maxeasy):
+    # an empty row whose sides hold 0, a free row, two single-entry rows (SCIP forces their bounds,
+    # cons_linear.c:7029): 2 x2 in [1, 3] gives x2 = 1 (integral), -x3 <= -0.5 gives x3 = 1
+    inst = _inst([([], [], -1.0, 1.0), ([0, 1], [1.0, 2.0], -INF, INF), ([2], [2.0], 1.0, 3.0),
+                  ([3], [-1.0], -INF, -0.5)], [0, 0, 0, 0], [10, 10, 10, 1], [1, 0, 1, 1])
+    lb, ub, cut = _same_root(gpu_prop, oracle_mod, inst, maxeasy)
+    assert not cut
+    assert list(lb) == [0, 0, 1, 1] and list(ub) == [10, 10, 1, 1]
+
+
+def test_empty_row_outside_its_sides_is_infeasible(gpu_prop, oracle_mod):
+    inst = _inst([([], [], 1.0, 2.0)], [0.0], [1.0], [1])
+    _, _, cut = _same_root(gpu_prop, oracle_mod, inst)
+    assert cut
+
+
+def test_problem_without_rows(gpu_prop, oracle_mod):
+    inst = Instance(np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), np.zeros(0),
+                    np.zeros(3), np.full(3, 5.0), np.ones(3, np.int8), x0=np.zeros(3))
+    lb, ub, cut = _same_root(gpu_prop, oracle_mod, inst)
+    assert not cut and np.array_equal(lb, inst.lb) and np.array_equal(ub, inst.ub)
+    # nodes: none changed, one tightened, one looser than the base (no change), one outside the base (cut off)
+    nodes = NodeBatch(np.array([0, 0, 1, 2, 3], np.int64), np.array([0, 1, 2], np.int32), np.array([2.0, -3.0, 6.0]),
+                      np.array([3.0, 9.0, 7.0]))
+    r = gpu_prop.propagate_nodes(inst.lb, inst.ub, nodes)
+    o = oracle_mod.Oracle(inst).propagate_nodes(inst.lb, inst.ub, nodes, oracle_mod.params(0.0), cap=inst.n)
+    _nodes_equal(r, o, nodes.nnodes)
+    assert list(r.cutoff) == [0, 0, 0, 1] and list(r.n[:3]) == [0, 1, 0]
+
+
+def test_degenerate_node_batches(gpu_prop, oracle_mod):
+    inst = instances.root_mip(3)
+    par = oracle_mod.params(0.0)
+    orc = oracle_mod.Oracle(inst)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    gpu_prop.set_params(gbp.default_params(maxeasy=0.0))
+    gpu_prop.upload(inst)
+    # no nodes at all
+    empty = NodeBatch(np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
+    r = gpu_prop.propagate_nodes(rlb, rub, empty)
+    assert len(r.cutoff) == 0 and r.result.cutoff == 0
+    # nodes without changes between ordinary ones, and a change outside the base domain
+    nodes = instances.node_batch(inst, rlb, rub, 40, seed=5)
+    ptr = np.concatenate([[0, 0], nodes.ptr, [nodes.ptr[-1]] * 2])
+    j = int(np.flatnonzero(rub < 1e19)[0])
+    col = np.concatenate([nodes.col, [j]]).astype(np.int32)
+    nlb = np.concatenate([nodes.lb, [rub[j] + 1.0]])
+    nub = np.concatenate([nodes.ub, [rub[j] + 2.0]])
+    ptr[-1] += 1
+    batch = NodeBatch(ptr.astype(np.int64), col, nlb, nub)
+    r = gpu_prop.propagate_nodes(rlb, rub, batch)
+    o = orc.propagate_nodes(rlb, rub, batch, par, cap=inst.n)
+    _nodes_equal(r, o, batch.nnodes)
+    assert r.cutoff[0] == 0 and r.n[0] == 0 and r.rounds[0] == 0
+    assert r.cutoff[-1] == 1
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_bounds_at_the_huge_and_infinite_thresholds(gpu_prop, oracle_mod, maxeasy):
+    """Bounds just below and at hugeval (1e15) and at infinity (1e20): the contributions move between the
+    finite sums and the huge/infinite counters, the residual rule skips what SCIP skips."""
+    inst = instances.root_mip(5)
+    rng = np.random.default_rng(12)
+    lb, ub = inst.lb.copy(), inst.ub.copy()
+    cont = np.flatnonzero(inst.isint == 0)
+    pick = rng.choice(cont, size=min(len(cont), 400), replace=False)
+    vals = np.array([9.9e14, 1e15, 3e16, 1e20])
+    ub[pick] = vals[rng.integers(0, 4, len(pick))]
+    lb[pick[::3]] = -ub[pick[::3]]
+    inst = Instance(inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, lb, ub, inst.isint, x0=inst.x0)
+    _same_root(gpu_prop, oracle_mod, inst, maxeasy)
+    gpu_prop.upload(inst)
+    act, cnt = gpu_prop.activities(lb, ub)
+    oact, ocnt = oracle_mod.Oracle(inst).activities(lb, ub)
+    assert np.array_equal(cnt, ocnt) and np.array_equal(act, oact)
+    assert (ocnt != 0).any()
