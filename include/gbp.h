@@ -175,7 +175,8 @@ int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t*
  * persistent launch.  Per node: out_cutoff[k], out_rounds[k] and the columns whose final bounds differ from
  * the base: out_n[k] entries at out_col/out_lb/out_ub[out_off[k] ..].  Node results are packed in completion
  * order into arrays of out_cap entries; a node that does not fit gets out_n[k] = -1 and the call returns
- * GBP_ERR_OVERFLOW. */
+ * GBP_ERR_OVERFLOW.  A change column outside [0, n) is caught by the kernel: that node is given up
+ * (out_cutoff[k] = 1) and the call returns GBP_ERR_INVALID. */
 int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
    const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
    int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,

@@ -101,6 +101,7 @@ struct gbp_ctx {
   int* d_next_item = nullptr;
   int* d_status = nullptr;
   unsigned long long* d_out_used = nullptr;
+  unsigned long long last_out_used = 0;  // packed entries the last batched call wrote (read with its statistics)
   // staging for the host-pointer node API
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -1319,6 +1320,8 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   int status = 0;
   CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&ctx->last_out_used, ctx->d_out_used, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   // the queue is dynamic: one slot may have run every node of the call, not just its average share
   ctx->slot_stamp_budget += (nnodes + 1) * ((int64_t)st[5] + 2);
@@ -1336,6 +1339,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
     res->live_rows = (int64_t)st[6];
     res->kernel_ms = ms;
   }
+  if (status & 4) return fail(ctx, GBP_ERR_INVALID, "change column out of range");
   if (status & 2) return fail(ctx, GBP_ERR_OVERFLOW, "node output arrays too small");
   if (status & 1) return GBP_ERR_LIMIT;
   return GBP_OK;
@@ -1359,8 +1363,7 @@ int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub
     if (ptr[k + 1] < ptr[k]) return fail(ctx, GBP_ERR_INVALID, "ptr not monotone");
   const int64_t nchg = ptr[nnodes];
   if (nchg > 0 && (!chg_col || !chg_lb || !chg_ub)) return fail(ctx, GBP_ERR_INVALID, "null change arrays");
-  for (int64_t q = 0; q < nchg; ++q)
-    if (chg_col[q] < 0 || chg_col[q] >= ctx->n) return fail(ctx, GBP_ERR_INVALID, "change column out of range");
+  // change columns are checked by the kernel (GBP_ERR_INVALID)
   CK(cudaSetDevice(ctx->device));
   // one staging allocation for inputs and outputs
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -1401,20 +1404,18 @@ int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub
                                       (int32_t*)(b + o_n), (int32_t*)(b + o_ocol), (double*)(b + o_olb),
                                       (double*)(b + o_oub), out_cap, res);
   if (rc != GBP_OK && rc != GBP_ERR_LIMIT && rc != GBP_ERR_OVERFLOW) return rc;
-  unsigned long long used = 0;
-  CK(cudaMemcpyAsync(&used, ctx->d_out_used, sizeof(used), cudaMemcpyDeviceToHost, ctx->stream));
+  // the device call has waited for the kernels and read how many packed entries they wrote
   CK(cudaMemcpyAsync(out_cutoff, b + o_cut, nnodes, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(out_rounds, b + o_rnd, nnodes * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(out_off, b + o_off, nnodes * 8, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(out_n, b + o_n, nnodes * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  const size_t cnt = (size_t)std::min<unsigned long long>(used, (unsigned long long)out_cap);
+  const size_t cnt = (size_t)std::min<unsigned long long>(ctx->last_out_used, (unsigned long long)out_cap);
   if (cnt) {
     CK(cudaMemcpyAsync(out_col, b + o_ocol, cnt * 4, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_lb, b + o_olb, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_ub, b + o_oub, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
   }
+  CK(cudaStreamSynchronize(ctx->stream));
   return rc;
 }
 

@@ -89,7 +89,7 @@ struct NodesArgs {
   const int* order;              // queue position -> node (longest expected work first), or null: identity
   SlotArrays S;
   unsigned long long* stats;     // rows, nnz, candidates, changes, cutoffs, max rounds
-  int* status;                   // bit0 round limit, bit1 output overflow
+  int* status;                   // bit0 round limit, bit1 output overflow, bit2 a change column out of range
   int minblocks;                 // register-budget variant of the kernel (1 = unconstrained)
 };
 

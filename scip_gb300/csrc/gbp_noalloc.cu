@@ -182,6 +182,7 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   res->changes = (int64_t)h.stats[3];
   res->live_rows = (int64_t)h.stats[6];
   res->kernel_ms = 0.0;
+  if (h.status & 4) return GBP_ERR_INVALID;
   if (h.status & 2) return GBP_ERR_OVERFLOW;
   if (h.status & 1) return GBP_ERR_LIMIT;
   return GBP_OK;

@@ -159,6 +159,11 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
       Front F{lists[0], &s_ns[0], &s_nl[0], rowstamp, m};
       for (int64_t q = A.ptr[item] + tid; q < A.ptr[item + 1]; q += NT) {
         int j = A.chg_col[q];
+        if (j < 0 || j >= (int)A.P.n) {  // not a column: the call fails, the node is given up
+          atomicOr(A.status, 4);
+          s_cut = 1;
+          continue;
+        }
         double nl = A.chg_lb[q], nu = A.chg_ub[q];
         double l0, u0;
         B.get(j, l0, u0);

@@ -114,3 +114,41 @@ def test_bounds_at_the_huge_and_infinite_thresholds(gpu_prop, oracle_mod, maxeas
     oact, ocnt = oracle_mod.Oracle(inst).activities(lb, ub)
     assert np.array_equal(cnt, ocnt) and np.array_equal(act, oact)
     assert (ocnt != 0).any()
+
+
+def test_change_column_out_of_range_fails_and_the_context_recovers(gpu_prop, oracle_mod):
+    """A node change naming no column: the kernel gives that node up and the call returns GBP_ERR_INVALID, through
+    the host and the device entry points alike; the next call on the same context is exact again."""
+    import torch
+
+    inst = instances.root_mip(3)
+    par = oracle_mod.params(0.0)
+    orc = oracle_mod.Oracle(inst)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    gpu_prop.set_params(gbp.default_params(maxeasy=0.0))
+    gpu_prop.upload(inst)
+    nodes = instances.node_batch(inst, rlb, rub, 16, seed=6)
+    for bad in (inst.n, -1):
+        col = nodes.col.copy()
+        col[int(nodes.ptr[3])] = bad
+        with pytest.raises(gbp.GbpError) as e:
+            gpu_prop.propagate_nodes(rlb, rub, NodeBatch(nodes.ptr, col, nodes.lb, nodes.ub))
+        assert e.value.code == gbp.GBP_ERR_INVALID
+    d = torch.device("cuda:0")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(d)
+    col = nodes.col.copy()
+    col[0] = inst.n + 5
+    cap = inst.n * 4
+    out = {"cutoff": torch.zeros(16, dtype=torch.int8, device=d), "rounds": torch.zeros(16, dtype=torch.int32, device=d),
+           "off": torch.zeros(16, dtype=torch.int64, device=d), "n": torch.zeros(16, dtype=torch.int32, device=d),
+           "col": torch.zeros(cap, dtype=torch.int32, device=d), "lb": torch.zeros(cap, dtype=torch.float64, device=d),
+           "ub": torch.zeros(cap, dtype=torch.float64, device=d)}
+    args = (t(rlb), t(rub), 16, t(nodes.ptr), t(col), t(nodes.lb), t(nodes.ub), out, cap)
+    torch.cuda.synchronize()  # the inputs and zeroed outputs are ready before the library's stream uses them
+    with pytest.raises(gbp.GbpError) as e:
+        gpu_prop.propagate_nodes_device(*args)
+    assert e.value.code == gbp.GBP_ERR_INVALID
+    torch.cuda.synchronize()
+    r = gpu_prop.propagate_nodes(rlb, rub, nodes)
+    o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+    _nodes_equal(r, o, nodes.nnodes)
