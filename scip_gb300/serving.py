@@ -74,7 +74,9 @@ class PropagationServer:
         self.hbm_cap = hbm_cap
         self.inflight = 0
         self.params = params or gbp.default_params(maxeasy=0.0)
-        self.lock = threading.Condition()
+        # one lock; each kind of request has its own condition, so that a submission wakes one worker of its kind
+        self.lock = threading.Lock()
+        self.ready = {"node": threading.Condition(self.lock), "inst": threading.Condition(self.lock)}
         self.queues = {"node": collections.deque(), "inst": collections.deque()}
         self.stop = False
         self.batches = []  # (kind, size, t_start, t_end)
@@ -98,13 +100,14 @@ class PropagationServer:
             req.t_arrive = time.perf_counter()
         with self.lock:
             self.queues[kind].append((req, fut))
-            self.lock.notify_all()
+            self.ready[kind].notify()
         return fut
 
     def close(self):
         with self.lock:
             self.stop = True
-            self.lock.notify_all()
+            for cv in self.ready.values():
+                cv.notify_all()
         for t, _ in self.workers:
             t.join(timeout=60)
         for _, prop in self.workers:
@@ -131,13 +134,16 @@ class PropagationServer:
                     est += b
                 if batch:
                     self.inflight += est
+                    if q:  # more of this kind is waiting: another free worker may take it
+                        self.ready[kind].notify()
                     return batch, est
-                self.lock.wait(timeout=0.05)
+                self.ready[kind].wait(timeout=0.05)
 
     def _release(self, est):
         with self.lock:
             self.inflight -= est
-            self.lock.notify_all()
+            for cv in self.ready.values():  # memory freed: waiting batches may now fit
+                cv.notify_all()
 
     def _work(self, kind, prop):
         while True:
@@ -170,14 +176,23 @@ class PropagationServer:
         ub = np.concatenate([r.ub for r, _ in batch])
         res = prop.propagate_nodes(self.root_lb, self.root_ub, instances.NodeBatch(ptr, col, lb, ub),
                                    out_cap=max(1024, 512 * len(batch)))
+        # every node's moved columns, gathered from the packed output into node order and sorted by column
+        nb = len(batch)
+        live = res.cutoff[:nb] == 0
+        cnt = np.where(live, res.n[:nb], 0).astype(np.int64)
+        first = np.cumsum(cnt) - cnt
+        idx = np.repeat(res.off[:nb] - first, cnt) + np.arange(int(cnt.sum()))
+        node = np.repeat(np.arange(nb), cnt)
+        c = res.col[idx]
+        o = np.lexsort((c, node))
+        c, l, u = c[o], res.lb[idx][o], res.ub[idx][o]
         out = []
-        for k in range(len(batch)):
-            if res.cutoff[k]:
+        for k in range(nb):
+            if not live[k]:
                 out.append(Reply(True))
             else:
-                c, l, u = res.node(k)
-                o = np.argsort(c)
-                out.append(Reply(False, c[o].copy(), l[o].copy(), u[o].copy()))
+                sl = slice(first[k], first[k] + cnt[k])
+                out.append(Reply(False, c[sl], l[sl], u[sl]))
         return out
 
     def _run_instances(self, prop, batch):
@@ -264,6 +279,16 @@ def make_stream(matrix, root_lb, root_ub, pool: List[instances.Instance], rate: 
     return Stream(times, reqs)
 
 
+def _wait_until(t):
+    """Wait for time t without holding the interpreter lock: a spinning client would keep the worker threads
+    from running until the interpreter's switch interval (5 ms) takes the lock away from it."""
+    while True:
+        d = t - time.perf_counter()
+        if d <= 0:
+            return
+        time.sleep(d if d > 2e-4 else 0)
+
+
 def replay(server, stream: Stream, served: bool = True):
     """Submit the stream at its arrival times (served) or answer it one request at a time in arrival order
     (plain, which still waits for each arrival).  Returns (replies, latencies in seconds, wall seconds)."""
@@ -273,8 +298,7 @@ def replay(server, stream: Stream, served: bool = True):
         futs = []
         for q, req in enumerate(stream.reqs):
             due = t0 + stream.times[q]
-            while time.perf_counter() < due:
-                pass
+            _wait_until(due)
             req.t_arrive = due
             futs.append(server.submit(req))
         for q, f in enumerate(futs):
@@ -284,8 +308,7 @@ def replay(server, stream: Stream, served: bool = True):
     else:
         for q, req in enumerate(stream.reqs):
             due = t0 + stream.times[q]
-            while time.perf_counter() < due:
-                pass
+            _wait_until(due)
             r = server.answer(req)
             r.t_done = time.perf_counter()
             replies[q] = r
