@@ -167,6 +167,25 @@ int gbp_upload_instance_list(gbp_ctx* ctx, int64_t ninst, const int64_t* m_k, co
 int gbp_propagate_instances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
 int gbp_propagate_instances_device(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res);
 
+/* ---------------------------------------------------------------- plain path, sparse form
+ * For a host that keeps its bounds on the device between calls, as a SCIP propagator does from node to node:
+ * gbp_set_bounds copies lb/ub (length n) to the context once; each gbp_propagate_changes then sends only the
+ * columns whose bounds the host changed since (cols[k] takes [newlb[k], newub[k]]; tightening or loosening; a
+ * column at most once) and propagates from them as gbp_propagate does with seeds: a change marks the rows for
+ * which it tightens a bound relative to seedlb[k]/seedub[k], or, when those are NULL, relative to the device's
+ * bounds before the call.  (Moving from one search node to another, SCIP relaxes to the common ancestor and
+ * tightens from there; a host that passes the ancestor's or the global bounds as seeds marks the rows SCIP marks,
+ * or more, with the same results.)  Returns the columns whose bounds propagation moved, sorted by column, with
+ * their bounds: *nout of them in outcols/outlb/outub (capacity cap).  The device copy then holds the propagated
+ * bounds.  On a cutoff (*cutoff = 1, also when a change has newlb > newub) or when more than cap columns moved
+ * (GBP_ERR_OVERFLOW, *nout = the capacity needed) it holds the bounds after the host's changes, so that the call
+ * can be repeated.  gbp_propagate, gbp_row_activities and the instance calls use the same device arrays: after
+ * them, gbp_set_bounds again. */
+int gbp_set_bounds(gbp_ctx* ctx, const double* lb, const double* ub);
+int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const double* newlb, const double* newub,
+   const double* seedlb, const double* seedub, int64_t cap, int64_t* nout, int32_t* outcols, double* outlb,
+   double* outub, int32_t* cutoff, gbp_result* res);
+
 /* ---------------------------------------------------------------- batched path: branch-and-bound nodes
  * nnodes nodes share the uploaded rows and the base bounds baselb/baseub (length n); node k applies the
  * bound changes chg_col/chg_lb/chg_ub[ptr[k] .. ptr[k+1]) (tightenings, as SCIPchgVarLb/UbProbing; a column

@@ -102,6 +102,14 @@ struct gbp_ctx {
   int* d_status = nullptr;
   unsigned long long* d_out_used = nullptr;
   unsigned long long last_out_used = 0;  // packed entries the last batched call wrote (read with its statistics)
+  // sparse plain calls (gbp_set_bounds / gbp_propagate_changes): d_lb/d_ub hold the caller's bounds between calls
+  bool bounds_set = false;
+  double* d_snap = nullptr;      // [2n] bounds after the caller's changes
+  double* d_chgb = nullptr;      // [2 chgcap] new bounds of the changes
+  int64_t chgcap = 0;
+  char* d_moved = nullptr;       // moved columns: cols [movedcap], lb [movedcap], ub [movedcap]
+  int64_t movedcap = 0;
+  unsigned long long* d_count = nullptr;
   // staging for the host-pointer node API
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -146,7 +154,7 @@ static void freeProblem(gbp_ctx* ctx) {
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
                   ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub, ctx->d_relig,
-                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp, ctx->d_rdom, ctx->d_rchanged, ctx->d_rcoef};
+                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp, ctx->d_rdom, ctx->d_rchanged, ctx->d_rcoef, ctx->d_snap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -161,6 +169,8 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_rdom = nullptr; ctx->d_rchanged = nullptr; ctx->rdom_valid = false; ctx->d_rcoef = nullptr;
   ctx->cap_m = ctx->cap_n = ctx->cap_nnz = ctx->cap_inst = 0;
   ctx->stage_bytes = 0;
+  ctx->d_snap = nullptr;
+  ctx->bounds_set = false;
   ctx->nslots = 0;
   ctx->has_problem = false;
 }
@@ -301,6 +311,9 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->d_ctr) cudaFree(ctx->d_ctr);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   if (ctx->d_next_item) cudaFree(ctx->d_next_item);
+  if (ctx->d_chgb) cudaFree(ctx->d_chgb);
+  if (ctx->d_moved) cudaFree(ctx->d_moved);
+  if (ctx->d_count) cudaFree(ctx->d_count);
   if (ctx->d_orderhist) cudaFree(ctx->d_orderhist);
   {
     void* lp[] = {ctx->log.n, ctx->log.col, ctx->log.round, ctx->log.lb, ctx->log.ub,
@@ -833,6 +846,7 @@ int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int
   for (int64_t k = 0; k < nseed; ++k)
     if (seedcols[k] < 0 || seedcols[k] >= ctx->n) return fail(ctx, GBP_ERR_INVALID, "seed column out of range");
   CK(cudaSetDevice(ctx->device));
+  ctx->bounds_set = false;  // the device bound arrays are this call's scratch
   const size_t nb = (size_t)ctx->n * sizeof(double);
   if (nb) {
     CK(cudaMemcpyAsync(ctx->d_lb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
@@ -856,6 +870,140 @@ int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int
   return rc;
 }
 
+// ------------------------------------------------------------------------------------------ sparse plain path
+int gbp_set_bounds(gbp_ctx* ctx, const double* lb, const double* ub) {
+  if (!ctx || !ctx->has_problem || ctx->instmode) return fail(ctx, GBP_ERR_INVALID, "no single problem uploaded");
+  if (ctx->n > 0 && (!lb || !ub)) return fail(ctx, GBP_ERR_INVALID, "null bounds");
+  CK(cudaSetDevice(ctx->device));
+  const size_t nb = (size_t)ctx->n * sizeof(double);
+  if (nb) {
+    CK(cudaMemcpyAsync(ctx->d_lb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_ub, ub, nb, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->bounds_set = true;
+  return GBP_OK;
+}
+
+// moved-column lists of capacity cap: columns, then (256-byte aligned) lower and upper bounds
+static size_t movedLbOffset(int64_t cap) { return ((size_t)cap * sizeof(int32_t) + 255) & ~size_t(255); }
+
+// scratch of the sparse call: snapshot, change bounds, moved-column lists and their counter
+static int ensureSparseBufs(gbp_ctx* ctx, int64_t nchg, int64_t cap) {
+  if (!ctx->d_snap && ctx->n > 0) CK(cudaMalloc(&ctx->d_snap, 2 * (size_t)ctx->n * sizeof(double)));
+  if (!ctx->d_count) CK(cudaMalloc(&ctx->d_count, sizeof(unsigned long long)));
+  if (nchg > ctx->chgcap) {
+    if (ctx->d_chgb) cudaFree(ctx->d_chgb);
+    ctx->d_chgb = nullptr;
+    ctx->chgcap = 0;
+    CK(cudaMalloc(&ctx->d_chgb, 2 * (size_t)nchg * sizeof(double)));
+    ctx->chgcap = nchg;
+  }
+  if (cap > ctx->movedcap) {
+    if (ctx->d_moved) cudaFree(ctx->d_moved);
+    ctx->d_moved = nullptr;
+    ctx->movedcap = 0;
+    CK(cudaMalloc(&ctx->d_moved, movedLbOffset(cap) + 2 * (size_t)cap * sizeof(double)));
+    ctx->movedcap = cap;
+  }
+  return ensureSeedBuf(ctx, std::max<int64_t>(nchg, 1));
+}
+
+int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const double* newlb, const double* newub,
+                          const double* seedlb, const double* seedub, int64_t cap, int64_t* nout, int32_t* outcols,
+                          double* outlb, double* outub, int32_t* cutoff, gbp_result* res) {
+  if (!ctx || !ctx->has_problem || ctx->instmode) return fail(ctx, GBP_ERR_INVALID, "no single problem uploaded");
+  if (!ctx->bounds_set) return fail(ctx, GBP_ERR_INVALID, "gbp_set_bounds first");
+  if (nchg < 0 || cap < 0 || !nout || !cutoff) return fail(ctx, GBP_ERR_INVALID, "bad sizes or null outputs");
+  if (nchg > 0 && (!cols || !newlb || !newub)) return fail(ctx, GBP_ERR_INVALID, "null change arrays");
+  if ((seedlb == nullptr) != (seedub == nullptr)) return fail(ctx, GBP_ERR_INVALID, "give both seed arrays or neither");
+  if (cap > 0 && (!outcols || !outlb || !outub)) return fail(ctx, GBP_ERR_INVALID, "null output arrays");
+  *nout = 0;
+  *cutoff = 0;
+  if (res) std::memset(res, 0, sizeof(*res));
+  for (int64_t k = 0; k < nchg; ++k) {
+    if (cols[k] < 0 || cols[k] >= ctx->n) return fail(ctx, GBP_ERR_INVALID, "change column out of range");
+    if (newlb[k] > newub[k]) {  // an empty domain: infeasible before any row is looked at
+      *cutoff = 1;
+      if (res) res->cutoff = 1, res->status = 1;
+      return GBP_OK;
+    }
+  }
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensureSparseBufs(ctx, nchg, cap);
+  if (rc) return rc;
+  const int64_t n = ctx->n;
+  const size_t nb = (size_t)n * sizeof(double);
+  double* slb = ctx->d_snap;
+  double* sub = ctx->d_snap + n;
+  if (nchg > 0) {
+    CK(cudaMemcpyAsync(ctx->d_seedcols, cols, nchg * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_chgb, newlb, nchg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_chgb + nchg, newub, nchg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (seedlb) {
+      CK(cudaMemcpyAsync(ctx->d_seedold, seedlb, nchg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(ctx->d_seedold + nchg, seedub, nchg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(launchSetChanges(ctx->stream, gridFor(ctx, nchg), nchg, ctx->d_seedcols, ctx->d_chgb, ctx->d_chgb + nchg,
+                        ctx->d_lb, ctx->d_ub, ctx->d_seedold, ctx->d_seedold + nchg, seedlb != nullptr));
+  }
+  if (nb) {
+    CK(cudaMemcpyAsync(slb, ctx->d_lb, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(sub, ctx->d_ub, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  auto restore = [&]() -> int {  // back to the bounds after the caller's changes
+    if (nb) {
+      CK(cudaMemcpyAsync(ctx->d_lb, slb, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(ctx->d_ub, sub, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GBP_OK;
+  };
+  rc = propagateCore(ctx, ctx->d_lb, ctx->d_ub, nchg, ctx->d_seedcols, ctx->d_seedold, ctx->d_seedold + nchg, cutoff,
+                     res);
+  if (rc != GBP_OK && rc != GBP_ERR_LIMIT) {
+    restore();
+    return rc;
+  }
+  if (*cutoff) {
+    const int r2 = restore();
+    return r2 ? r2 : rc;
+  }
+  // the columns that propagation moved, against the snapshot
+  int32_t* mcols = (int32_t*)ctx->d_moved;
+  double* mlb = (double*)(ctx->d_moved + movedLbOffset(ctx->movedcap));
+  double* mub = mlb + ctx->movedcap;
+  CK(cudaMemsetAsync(ctx->d_count, 0, sizeof(unsigned long long), ctx->stream));
+  if (n > 0)
+    CK(launchMoved(ctx->stream, gridFor(ctx, n), n, ctx->d_lb, ctx->d_ub, slb, sub, ctx->d_count, cap, mcols, mlb,
+                   mub));
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, ctx->d_count, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *nout = (int64_t)cnt;
+  if ((int64_t)cnt > cap) {  // the caller retries with room for *nout columns from the same state
+    const int r2 = restore();
+    return r2 ? r2 : fail(ctx, GBP_ERR_OVERFLOW, "moved-column arrays too small (nout is the count needed)");
+  }
+  if (cnt > 0) {
+    std::vector<int32_t> c(cnt);
+    std::vector<double> l(cnt), u(cnt);
+    CK(cudaMemcpyAsync(c.data(), mcols, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(l.data(), mlb, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(u.data(), mub, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::vector<int64_t> idx(cnt);
+    for (size_t q = 0; q < cnt; ++q) idx[q] = (int64_t)q;
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return c[a] < c[b]; });
+    for (size_t q = 0; q < cnt; ++q) {
+      outcols[q] = c[idx[q]];
+      outlb[q] = l[idx[q]];
+      outub[q] = u[idx[q]];
+    }
+  }
+  return rc;
+}
+
 int gbp_propagate_device(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int32_t* seedcols,
                          const double* oldlb, const double* oldub, int32_t* cutoff, gbp_result* res) {
   if (!ctx || !ctx->has_problem || (ctx->n > 0 && (!lb || !ub)))
@@ -875,6 +1023,7 @@ int gbp_row_activities(gbp_ctx* ctx, const double* lb, const double* ub, double*
   int32_t* d_cnt = nullptr;
   CK(cudaMalloc(&d_act, std::max<size_t>(m, 1) * 4 * sizeof(double)));
   CK(cudaMalloc(&d_cnt, std::max<size_t>(m, 1) * 8 * sizeof(int32_t)));
+  ctx->bounds_set = false;  // the device bound arrays are this call's scratch
   if (nb) {
     CK(cudaMemcpyAsync(ctx->d_lb, lb, nb, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_ub, ub, nb, cudaMemcpyHostToDevice, ctx->stream));
@@ -1156,6 +1305,7 @@ static int propagateInstances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst
   double* dlb = lb;
   double* dub = ub;
   if (host) {
+    ctx->bounds_set = false;  // the device bound arrays are this call's scratch
     dlb = ctx->d_lb;
     dub = ctx->d_ub;
     if (nb) {

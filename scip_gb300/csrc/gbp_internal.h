@@ -124,6 +124,11 @@ cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* l
 cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
                              const double* ub, double* act, int32_t* cnt);
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n);
+cudaError_t launchSetChanges(cudaStream_t st, int grid, int64_t nchg, const int32_t* cols, const double* nlb,
+                             const double* nub, double* lb, double* ub, double* oldlb, double* oldub, int keepold);
+cudaError_t launchMoved(cudaStream_t st, int grid, int64_t n, const double* lb, const double* ub, const double* slb,
+                        const double* sub, unsigned long long* count, int64_t cap, int32_t* cols, double* olb,
+                        double* oub);
 cudaError_t launchNodes(cudaStream_t st, int grid, int threads, const NodesArgs& A);
 cudaError_t nodesOccupancy(int threads, int minblocks, int* blocksPerSm);
 // the node kernel with the ranged-row rule compiled in (gbp_nodes_ranged.cu); launchNodes picks it when the

@@ -239,6 +239,39 @@ __global__ void k_pack(const double* lb, const double* ub, double2* out, int64_t
     out[j] = make_double2(lb[j], ub[j]);
 }
 
+// the sparse plain call (gbp_propagate_changes): column cols[k] takes bounds [nlb[k], nub[k]]; its previous
+// bounds become the call's seeds
+// (keepold: the seeds' old bounds are already in oldlb/oldub)
+__global__ void k_set_changes(int64_t nchg, const int32_t* cols, const double* nlb, const double* nub, double* lb,
+                              double* ub, double* oldlb, double* oldub, int keepold) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nchg; k += (int64_t)gridDim.x * blockDim.x) {
+    const int j = cols[k];
+    if (!keepold) {
+      oldlb[k] = lb[j];
+      oldub[k] = ub[j];
+    }
+    lb[j] = nlb[k];
+    ub[j] = nub[k];
+  }
+}
+
+// columns whose bounds differ from the snapshot, appended in no particular order while they fit cap; count
+// reaches the number of such columns
+__global__ void k_moved(int64_t n, const double* lb, const double* ub, const double* slb, const double* sub,
+                        unsigned long long* count, int64_t cap, int32_t* cols, double* olb, double* oub) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const double l = lb[j], u = ub[j];
+    if (l != slb[j] || u != sub[j]) {
+      const unsigned long long pos = atomicAdd(count, 1ull);
+      if ((int64_t)pos < cap) {
+        cols[pos] = (int32_t)j;
+        olb[pos] = l;
+        oub[pos] = u;
+      }
+    }
+  }
+}
+
 __global__ void k_flags8(const int* in, int8_t* out, int64_t n) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
     out[j] = in[j] != 0 ? 1 : 0;
@@ -477,6 +510,17 @@ cudaError_t launchSeed(cudaStream_t st, int grid, const Prob& P, const double* l
 cudaError_t launchActivities(cudaStream_t st, int grid, const Num& s, const Prob& P, const double* lb,
                              const double* ub, double* act, int32_t* cnt) {
   k_activities<<<grid, 256, 0, st>>>(s, P, PlainBnd{lb, ub}, act, cnt);
+  return cudaGetLastError();
+}
+cudaError_t launchSetChanges(cudaStream_t st, int grid, int64_t nchg, const int32_t* cols, const double* nlb,
+                             const double* nub, double* lb, double* ub, double* oldlb, double* oldub, int keepold) {
+  k_set_changes<<<grid, 256, 0, st>>>(nchg, cols, nlb, nub, lb, ub, oldlb, oldub, keepold);
+  return cudaGetLastError();
+}
+cudaError_t launchMoved(cudaStream_t st, int grid, int64_t n, const double* lb, const double* ub, const double* slb,
+                        const double* sub, unsigned long long* count, int64_t cap, int32_t* cols, double* olb,
+                        double* oub) {
+  k_moved<<<grid, 256, 0, st>>>(n, lb, ub, slb, sub, count, cap, cols, olb, oub);
   return cudaGetLastError();
 }
 cudaError_t launchPack(cudaStream_t st, int grid, const double* lb, const double* ub, double2* out, int64_t n) {

@@ -36,7 +36,7 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
            "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log",
-           "gbp_upload_instance_list", "gbp_get_ranged_log"]
+           "gbp_upload_instance_list", "gbp_get_ranged_log", "gbp_set_bounds", "gbp_propagate_changes"]
 
 
 class GbpParams(ctypes.Structure):
@@ -89,6 +89,10 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(GbpResult)]
     L.gbp_propagate_device.argtypes = L.gbp_propagate.argtypes
     L.gbp_row_activities.argtypes = [_P, _P, _P, _P, _P]
+    L.gbp_set_bounds.argtypes = [_P, _P, _P]
+    L.gbp_propagate_changes.argtypes = [_P, ctypes.c_int64, _P, _P, _P, _P, _P, ctypes.c_int64,
+                                        ctypes.POINTER(ctypes.c_int64), _P, _P, _P, ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(GbpResult)]
     L.gbp_set_global_bounds.argtypes = [_P, _P, _P]
     L.gbp_set_change_log.argtypes = [_P, ctypes.c_int64]
     L.gbp_get_change_log.argtypes = [_P, ctypes.c_int64, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
@@ -203,6 +207,35 @@ class Propagator:
                                               _ptr(rh), _ptr(ii)))
         self._keep = None
         self.m, self.n = inst.m, inst.n
+
+    def set_bounds(self, lb, ub):
+        """the context's device copy of the bounds, for propagate_changes"""
+        lb = np.ascontiguousarray(lb, dtype=np.float64)
+        ub = np.ascontiguousarray(ub, dtype=np.float64)
+        self._check(self.L.gbp_set_bounds(self.h, _ptr(lb), _ptr(ub)))
+
+    def propagate_changes(self, cols, newlb, newub, cap: Optional[int] = None, seed=None):
+        """Sparse plain call: the listed columns take the given bounds on the device copy, propagation runs from
+        them (tightenings relative to seed = (seedlb, seedub) per change, else to the device's previous bounds).
+        Returns (cutoff, moved columns sorted, their lb, their ub, GbpResult)."""
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        newlb = np.ascontiguousarray(newlb, dtype=np.float64)
+        newub = np.ascontiguousarray(newub, dtype=np.float64)
+        slb = sub = None
+        if seed is not None:
+            slb = np.ascontiguousarray(seed[0], dtype=np.float64)
+            sub = np.ascontiguousarray(seed[1], dtype=np.float64)
+        cap = self.n if cap is None else cap
+        if getattr(self, "_chg_out", None) is None or len(self._chg_out[0]) < cap:  # reused between calls
+            self._chg_out = (np.zeros(cap, np.int32), np.zeros(cap), np.zeros(cap))
+        oc, ol, ou = self._chg_out
+        nout, cut, res = ctypes.c_int64(0), ctypes.c_int32(0), GbpResult()
+        rc = self.L.gbp_propagate_changes(self.h, len(cols), _ptr(cols), _ptr(newlb), _ptr(newub), _ptr(slb),
+                                          _ptr(sub), cap, ctypes.byref(nout), _ptr(oc), _ptr(ol), _ptr(ou),
+                                          ctypes.byref(cut), ctypes.byref(res))
+        self._check(rc, allow=(GBP_ERR_LIMIT,))
+        k = nout.value
+        return bool(cut.value), oc[:k].copy(), ol[:k].copy(), ou[:k].copy(), res
 
     def propagate(self, lb, ub, seed=None):
         """Host arrays; returns (lb, ub, cutoff, GbpResult).  seed = (cols, oldlb, oldub) or None (all rows)."""

@@ -328,3 +328,56 @@ def test_change_log_matches_oracle(gpu_prop, oracle_mod, maxeasy, hostloop):
     gpu_prop.set_global_bounds(None)
     gpu_prop.set_change_log(0)
     gpu_prop.set_params(_params(maxeasy))
+
+
+@pytest.mark.parametrize("maxeasy", [0.0, 1e6])
+def test_sparse_plain_calls_walk_nodes_like_a_search(gpu_prop, oracle_mod, maxeasy):
+    """gbp_set_bounds once, then one gbp_propagate_changes per node as a search moves between nodes: each call
+    sends the previous node's columns back to the root bounds plus the node's own changes, seeded from the root
+    bounds, and gets back the columns propagation moved.  Every node's result equals the oracle's batched-node
+    result bit for bit; a cutoff leaves the device copy at the bounds after the changes; a too-small output
+    reports the count needed."""
+    inst = instances.node_mip(seed=2, m=20000, n=40000)
+    orc = oracle_mod.Oracle(inst)
+    par = oracle_mod.params(maxeasy)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    nodes = instances.node_batch(inst, rlb, rub, 160, seed=12)
+    o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
+    gpu_prop.set_params(_params(maxeasy))
+    gpu_prop.upload(inst)
+    gpu_prop.set_global_bounds(rlb, rub)  # a node's global domain: the root fixpoint
+    gpu_prop.set_bounds(rlb, rub)
+    dirty = np.zeros(0, np.int32)  # columns that differ from the root on the device
+    ncut = 0
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        chg = {int(j): (rlb[j], rub[j]) for j in dirty}
+        for j, l, u in zip(nodes.col[sl], nodes.lb[sl], nodes.ub[sl]):
+            chg[int(j)] = (max(rlb[j], l), min(rub[j], u))
+        cols = np.array(sorted(chg), np.int32)
+        nlb = np.array([chg[j][0] for j in cols])
+        nub = np.array([chg[j][1] for j in cols])
+        alb, aub = rlb.copy(), rub.copy()  # the bounds after the changes
+        alb[cols], aub[cols] = nlb, nub
+        seed = (rlb[cols], rub[cols])  # tightenings relative to the root: the rows the full-vector call marks
+        if o["cutoff"][k]:
+            cut, mc, _, _, _ = gpu_prop.propagate_changes(cols, nlb, nub, seed=seed)
+            assert cut and len(mc) == 0, f"node {k}"
+            ncut += 1
+            dirty = cols[(nlb != rlb[cols]) | (nub != rub[cols])]
+            continue
+        n = o["n"][k]
+        flb, fub = rlb.copy(), rub.copy()  # the oracle's final bounds of the node
+        flb[o["col"][k, :n]], fub[o["col"][k, :n]] = o["lb"][k, :n], o["ub"][k, :n]
+        want = np.flatnonzero((flb != alb) | (fub != aub))  # what propagation moved
+        if len(want) > 1:  # room for one moved column only: the call reports the count needed and leaves the
+            with pytest.raises(gbp.GbpError) as e:  # device copy so that it can be repeated
+                gpu_prop.propagate_changes(cols, nlb, nub, cap=1, seed=seed)
+            assert e.value.code == gbp.GBP_ERR_OVERFLOW
+        cut, mc, ml, mu, res = gpu_prop.propagate_changes(cols, nlb, nub, seed=seed)
+        assert not cut and res.rounds == o["rounds"][k], f"node {k}"
+        assert np.array_equal(mc, want), f"node {k}"
+        assert np.array_equal(ml, flb[want]) and np.array_equal(mu, fub[want]), f"node {k}"
+        dirty = np.flatnonzero((flb != rlb) | (fub != rub)).astype(np.int32)
+    assert nodes.nnodes > ncut
+    gpu_prop.set_global_bounds(None)
