@@ -1,8 +1,9 @@
 /* prop_gpulinear.c -- SCIP propagator plugin over libgbp (see prop_gpulinear.h).
  *
- * Call path: SCIPpropExec (src/scip/prop.c:646) -> propExecGpulinear -> gbp_propagate (C ABI, one device
- * round trip per call: local bounds and changed columns in, tightened bounds and the cutoff flag out) ->
- * SCIPtightenVarLb/Ub for every moved bound.
+ * Call path: SCIPpropExec (src/scip/prop.c:646) -> propExecGpulinear -> gbp_propagate_changes (C ABI, one device
+ * round trip per call: the columns whose local bounds differ from the device's copy in, the columns propagation
+ * moved and the cutoff flag out; the first call after an upload or a cutoff sends every bound through
+ * gbp_propagate) -> SCIPinferVarLb/UbProp or SCIPtightenVarLb/Ub for every moved bound.
  */
 #include <float.h>
 #include <limits.h>
@@ -45,8 +46,13 @@ struct SCIP_PropData
    int8_t*               isint;
    double*               lb;                 /**< bounds handed to the device / returned from it */
    double*               ub;
-   double*               snaplb;             /**< local bounds after the previous call */
+   double*               snaplb;             /**< the device's copy of the bounds after the previous call */
    double*               snapub;
+   double*               chglb;              /**< bounds of the columns sent to the device (gbp_propagate_changes) */
+   double*               chgub;
+   int32_t*              outcols;            /**< columns the device moved, with their bounds */
+   double*               outlb;
+   double*               outub;
    SCIP_Bool             havesnap;
    double*               glb;                /**< global bounds last passed to the device (binary test) */
    double*               gub;
@@ -95,6 +101,11 @@ static void freeMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIPfreeMemoryArrayNull(scip, &pd->ub);
    SCIPfreeMemoryArrayNull(scip, &pd->snaplb);
    SCIPfreeMemoryArrayNull(scip, &pd->snapub);
+   SCIPfreeMemoryArrayNull(scip, &pd->chglb);
+   SCIPfreeMemoryArrayNull(scip, &pd->chgub);
+   SCIPfreeMemoryArrayNull(scip, &pd->outcols);
+   SCIPfreeMemoryArrayNull(scip, &pd->outlb);
+   SCIPfreeMemoryArrayNull(scip, &pd->outub);
    SCIPfreeMemoryArrayNull(scip, &pd->glb);
    SCIPfreeMemoryArrayNull(scip, &pd->gub);
    pd->haveglobal = FALSE;
@@ -251,6 +262,11 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->ub, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snaplb, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->snapub, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->chglb, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->chgub, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->outcols, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->outlb, nvars > 0 ? nvars : 1) );
+   SCIP_CALL( SCIPallocMemoryArray(scip, &pd->outub, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->glb, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->gub, nvars > 0 ? nvars : 1) );
    SCIP_CALL( SCIPallocMemoryArray(scip, &pd->seeds, nvars > 0 ? nvars : 1) );
@@ -749,14 +765,17 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    }
    if( pd->havesnap )
    {
-      /* columns that moved in either direction since the last call: their rows are re-propagated (a relaxed
-       * column can be re-tightened by its own rows after SCIP switched to another node) */
+      /* columns whose local bounds differ from the device's copy: only they are sent, and their rows are
+       * re-propagated in both directions (a relaxed column can be re-tightened by its own rows after SCIP switched
+       * to another node) */
       nseed = 0;
       for( j = 0; j < pd->ncols; ++j )
       {
          if( pd->lb[j] != pd->snaplb[j] || pd->ub[j] != pd->snapub[j] )
          {
             pd->seeds[nseed] = j;
+            pd->chglb[nseed] = pd->lb[j];
+            pd->chgub[nseed] = pd->ub[j];
             pd->seedlo[nseed] = -DBL_MAX;
             pd->seedhi[nseed] = DBL_MAX;
             ++nseed;
@@ -779,8 +798,33 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
          return SCIP_OKAY;
       }
    }
-   rc = gbp_propagate(pd->ctx, pd->lb, pd->ub, nseed, nseed > 0 ? pd->seeds : NULL, nseed > 0 ? pd->seedlo : NULL,
-      nseed > 0 ? pd->seedhi : NULL, &cutoff, &res);
+   if( pd->havesnap )
+   {
+      /* the device keeps the bounds between calls: the changed columns go in, the moved ones come back */
+      int64_t nout = 0;
+      int64_t q;
+      rc = gbp_propagate_changes(pd->ctx, nseed, pd->seeds, pd->chglb, pd->chgub, pd->seedlo, pd->seedhi,
+         (int64_t)pd->ncols, &nout, pd->outcols, pd->outlb, pd->outub, &cutoff, &res);
+      if( (rc == GBP_OK || rc == GBP_ERR_LIMIT) && !cutoff )
+      {
+         for( q = 0; q < nout; ++q )
+         {
+            pd->lb[pd->outcols[q]] = pd->outlb[q];
+            pd->ub[pd->outcols[q]] = pd->outub[q];
+         }
+      }
+   }
+   else
+   {
+      /* every row from the current bounds, which then stay on the device */
+      rc = gbp_propagate(pd->ctx, pd->lb, pd->ub, -1, NULL, NULL, NULL, &cutoff, &res);
+      if( (rc == GBP_OK || rc == GBP_ERR_LIMIT) && !cutoff )
+      {
+         int rc2 = gbp_set_bounds(pd->ctx, pd->lb, pd->ub);
+         if( rc2 != GBP_OK )
+            rc = rc2;
+      }
+   }
    pd->ncalls++;
    if( rc != GBP_OK && rc != GBP_ERR_LIMIT )
    {
@@ -845,10 +889,12 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
          pd->nchgbds += tightened ? 1 : 0;
       }
    }
+   /* the device's copy: a column whose local bound SCIP did not take as proposed differs from it and is sent
+    * again at the next call */
    for( j = 0; j < pd->ncols; ++j )
    {
-      pd->snaplb[j] = SCIPvarGetLbLocal(pd->vars[j]);
-      pd->snapub[j] = SCIPvarGetUbLocal(pd->vars[j]);
+      pd->snaplb[j] = pd->lb[j];
+      pd->snapub[j] = pd->ub[j];
    }
    pd->havesnap = TRUE;
    *result = reduced ? SCIP_REDUCEDDOM : SCIP_DIDNOTFIND;

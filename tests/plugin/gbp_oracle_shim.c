@@ -26,6 +26,9 @@ struct gbp_ctx
    int has_global;
    lpo_log log;
    int logon;
+   double* dlb;   /* bounds kept between sparse calls (gbp_set_bounds / gbp_propagate_changes) */
+   double* dub;
+   int bset;
 };
 
 int gbp_version(void) { return 0; }
@@ -66,6 +69,8 @@ static void freeProblem(gbp_ctx* c)
    c->rowptr = NULL; c->colidx = NULL; c->vals = NULL; c->lhs = NULL; c->rhs = NULL; c->isint = NULL;
    c->colptr = NULL; c->rowidx = NULL; c->cvals = NULL; c->glb = NULL; c->gub = NULL;
    c->has_global = 0;
+   free(c->dlb); free(c->dub);
+   c->dlb = NULL; c->dub = NULL; c->bset = 0;
 }
 
 int gbp_destroy(gbp_ctx* ctx)
@@ -197,6 +202,110 @@ int gbp_propagate(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, const int
       res->changes = r.changes;
    }
    return r.status == 2 ? GBP_ERR_LIMIT : GBP_OK;
+}
+
+int gbp_set_bounds(gbp_ctx* ctx, const double* lb, const double* ub)
+{
+   size_t nb = sizeof(double) * (size_t)(ctx->P.n > 0 ? ctx->P.n : 1);
+   if( ctx->dlb == NULL )
+   {
+      ctx->dlb = malloc(nb);
+      ctx->dub = malloc(nb);
+      if( ctx->dlb == NULL || ctx->dub == NULL )
+         return GBP_ERR_NOMEM;
+   }
+   if( ctx->P.n > 0 )
+   {
+      memcpy(ctx->dlb, lb, sizeof(double) * (size_t)ctx->P.n);
+      memcpy(ctx->dub, ub, sizeof(double) * (size_t)ctx->P.n);
+   }
+   ctx->bset = 1;
+   return GBP_OK;
+}
+
+/* the sparse call as include/gbp.h states it: changes applied to the kept bounds, propagation from them, the
+ * columns it moved returned by column; the kept bounds are left after the changes on a cutoff or an overflow */
+int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const double* newlb, const double* newub,
+   const double* seedlb, const double* seedub, int64_t cap, int64_t* nout, int32_t* outcols, double* outlb,
+   double* outub, int32_t* cutoff, gbp_result* res)
+{
+   int64_t n = ctx->P.n;
+   int64_t k;
+   int64_t j;
+   int64_t cnt = 0;
+   double* lb;
+   double* ub;
+   double* olb;
+   double* oub;
+   int rc;
+   if( !ctx->bset )
+      return GBP_ERR_INVALID;
+   *nout = 0;
+   *cutoff = 0;
+   for( k = 0; k < nchg; ++k )
+   {
+      if( cols[k] < 0 || cols[k] >= n )
+         return GBP_ERR_INVALID;
+      if( newlb[k] > newub[k] )
+      {
+         *cutoff = 1;
+         if( res != NULL )
+         {
+            memset(res, 0, sizeof(*res));
+            res->cutoff = 1;
+            res->status = 1;
+         }
+         return GBP_OK;
+      }
+   }
+   olb = malloc(sizeof(double) * (size_t)(nchg > 0 ? nchg : 1));
+   oub = malloc(sizeof(double) * (size_t)(nchg > 0 ? nchg : 1));
+   lb = malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+   ub = malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+   if( olb == NULL || oub == NULL || lb == NULL || ub == NULL )
+   {
+      free(olb); free(oub); free(lb); free(ub);
+      return GBP_ERR_NOMEM;
+   }
+   for( k = 0; k < nchg; ++k )
+   {
+      olb[k] = seedlb != NULL ? seedlb[k] : ctx->dlb[cols[k]];
+      oub[k] = seedub != NULL ? seedub[k] : ctx->dub[cols[k]];
+      ctx->dlb[cols[k]] = newlb[k];
+      ctx->dub[cols[k]] = newub[k];
+   }
+   if( n > 0 )
+   {
+      memcpy(lb, ctx->dlb, sizeof(double) * (size_t)n);
+      memcpy(ub, ctx->dub, sizeof(double) * (size_t)n);
+   }
+   rc = gbp_propagate(ctx, lb, ub, nchg, cols, olb, oub, cutoff, res);
+   if( (rc == GBP_OK || rc == GBP_ERR_LIMIT) && !*cutoff )
+   {
+      for( j = 0; j < n; ++j )
+         cnt += (lb[j] != ctx->dlb[j] || ub[j] != ctx->dub[j]) ? 1 : 0;
+      *nout = cnt;
+      if( cnt > cap )
+         rc = GBP_ERR_OVERFLOW;
+      else
+      {
+         cnt = 0;
+         for( j = 0; j < n; ++j )
+         {
+            if( lb[j] != ctx->dlb[j] || ub[j] != ctx->dub[j] )
+            {
+               outcols[cnt] = (int32_t)j;
+               outlb[cnt] = lb[j];
+               outub[cnt] = ub[j];
+               ++cnt;
+            }
+         }
+         memcpy(ctx->dlb, lb, sizeof(double) * (size_t)n);
+         memcpy(ctx->dub, ub, sizeof(double) * (size_t)n);
+      }
+   }
+   free(olb); free(oub); free(lb); free(ub);
+   return rc;
 }
 
 static const lpo_log* sortlog;
