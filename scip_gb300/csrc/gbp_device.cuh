@@ -698,27 +698,6 @@ __device__ __forceinline__ int finishRow(const Num& s, int len, double lhs, doub
   return 0;
 }
 
-// Pass 1 of a short row by one thread (both halves in turn); the first half's activity waits in *stash.
-template <class BND>
-__device__ __forceinline__ int scanRow(const Num& s, const Prob& P, const BND& B, int i, Act& a, bool& easy,
-                                       unsigned char (&sel)[MAXSEL], int& nsel, bool& full, Stats& st, Act* stash) {
-  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
-  const int len = (int)(p1 - p0);
-  const int64_t ph = p0 + (len + 1) / 2;
-  ScanOut so;
-  long long mad;
-  scanInit(a, so, mad);
-  scanEntries(s, P, B, p0, p0, ph, a, so, mad);
-  // the second half continues the same list, specials and maxima; only its activity is a separate partial
-  *stash = a;
-  actZero(a);
-  scanEntries(s, P, B, p0, ph, p1, a, so, mad);
-  Act whole = *stash;
-  actMerge(whole, a);
-  a = whole;
-  return finishRow(s, len, P.lhs[i], P.rhs[i], a, so, mad, easy, sel, nsel, full, st, true);
-}
-
 // work item w of a batch belongs to the last batch row o with prefix[o] <= w
 template <int NT>
 __device__ __forceinline__ int itemOwner(const RowBatch<NT>& rb, int w) {
