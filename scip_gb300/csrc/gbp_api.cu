@@ -378,6 +378,13 @@ static int prepareUpload(gbp_ctx* ctx, int64_t m, int64_t n, int64_t nnz) {
   ctx->has_global = false;
   ctx->ninst = 0;
   destroyGraphs(ctx);
+  // the sparse calls' bounds and snapshot belong to the previous problem (the snapshot is sized for its n, and
+  // the arrays below may be reused for a larger one)
+  ctx->bounds_set = false;
+  if (ctx->d_snap) {
+    cudaFree(ctx->d_snap);
+    ctx->d_snap = nullptr;
+  }
   const size_t mm = (size_t)std::max<int64_t>(m, 1), nn = (size_t)std::max<int64_t>(n, 1),
                zz = (size_t)std::max<int64_t>(nnz, 1);
   if ((int64_t)mm > ctx->cap_m || (int64_t)nn > ctx->cap_n || (int64_t)zz > ctx->cap_nnz) {

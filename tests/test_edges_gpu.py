@@ -152,3 +152,28 @@ def test_change_column_out_of_range_fails_and_the_context_recovers(gpu_prop, ora
     r = gpu_prop.propagate_nodes(rlb, rub, nodes)
     o = orc.propagate_nodes(rlb, rub, nodes, par, cap=inst.n)
     _nodes_equal(r, o, nodes.nnodes)
+
+
+def test_sparse_calls_across_uploads(gpu_prop, oracle_mod):
+    """The resident bounds of the sparse call belong to one problem: an upload drops them (a call before
+    gbp_set_bounds fails), and after uploads of a larger, a smaller and again the larger problem (the device
+    arrays are reused) the sparse call equals the full-vector call."""
+    big = instances.root_mip(6)
+    small = _inst([([0, 1], [1.0, 1.0], -INF, 1.0)], [0, 0], [1, 1], [1, 1])
+    gpu_prop.set_params(gbp.default_params(maxeasy=0.0))
+    for inst in (big, small, big):
+        gpu_prop.upload(inst)
+        with pytest.raises(gbp.GbpError):
+            gpu_prop.propagate_changes(np.array([0], np.int32), inst.lb[:1], inst.ub[:1])
+        rlb, rub, cut, _ = gpu_prop.propagate(inst.lb, inst.ub)
+        assert not cut
+        gpu_prop.set_bounds(rlb, rub)
+        j = int(np.flatnonzero((inst.isint == 1) & (rub > rlb))[0])
+        cut, mc, ml, mu, _ = gpu_prop.propagate_changes(np.array([j], np.int32), rub[j:j + 1], rub[j:j + 1])
+        lb, ub = rlb.copy(), rub.copy()
+        lb[j] = rub[j]
+        flb, fub, fcut, _ = gpu_prop.propagate(lb, ub, seed=(np.array([j], np.int32), rlb[j:j + 1], rub[j:j + 1]))
+        assert cut == fcut
+        if not cut:
+            lb[mc], ub[mc] = ml, mu
+            assert np.array_equal(lb, flb) and np.array_equal(ub, fub)
