@@ -56,6 +56,7 @@ typedef struct
    const int64_t* colptr;
    const int32_t* rowidx;
    const double* cvals;
+   const int32_t* varidx;   /* SCIP's problem index of each column (ties of consdataCompVarProp), NULL: the column */
 } lpo_problem;
 
 typedef struct
@@ -66,8 +67,9 @@ typedef struct
    int32_t reserved;
    int64_t rows;        /* frontier rows processed over all rounds */
    int64_t nnz;         /* nonzeros of those rows */
-   int64_t candidates;  /* candidate bounds emitted */
+   int64_t candidates;  /* candidate bounds emitted (sequential order: entries evaluated) */
    int64_t changes;     /* accepted bound changes (lower and upper counted separately) */
+   int64_t live_rows;   /* sequential order: rows whose tightenBounds got past its skip tests */
 } lpo_result;
 
 void lpo_default_params(lpo_params* p);
@@ -119,6 +121,39 @@ int lpo_propagate_nodes(const lpo_problem* prob, const lpo_params* par, const do
    int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
    int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb, double* out_ub,
    int32_t cap, int32_t nthreads, lpo_result* total);
+
+/* ------------------------------------------------------------------ SCIP's own order (linprop_seq.c)
+ * SCIP walks the rows marked for propagation one at a time and applies every tightening at once; the bound-change
+ * events update the other rows' activities incrementally and mark them.  These entry points restate that order:
+ *   - marked rows are processed in SCIP's propconss order: a newly marked row is appended; unmarking moves the last
+ *     marked row into the freed place; marks, unmarks and deletions made while consPropLinear runs are applied
+ *     after it, the last one first;
+ *   - per row, tightenBounds visits the entries in the row's order (up to 10 passes, stopping at the entry of the
+ *     last change, binaries skipped after the first unfixed binary that did not tighten);
+ *   - activities are computed on first use in the row's order and then updated incrementally by every bound change
+ *     of the row's columns, with SCIP's reliability test (recomputed last entry first when unreliable);
+ *   - a propagation round is one pass over the rows marked at its start; rounds repeat until one changes nothing.
+ *
+ * lpo_propagate_seq: the root (depth 0).  Every row starts marked, in row order; bound changes are global, so a
+ * column that turns into an unfixed binary unsorts its rows; rows are sorted (consdataCompVarProp on the current
+ * bounds) when tightenBounds first needs them; a redundant row is deleted.  out_order (nnz entries, or NULL)
+ * receives each row's final order: out_order[rowptr[i] + k] = CSR position of the row's k-th entry.
+ *
+ * lpo_propagate_nodes_seq: branch-and-bound nodes (depth >= 1) on top of base bounds that are a fixpoint (SCIP's
+ * root).  Each row's entries are taken in storage order, which must be the order SCIP holds the row in (out_order
+ * of lpo_propagate_seq, or SCIP's own, or consdataCompVarProp on the base bounds); with sortvars its leading
+ * binaries (under the base bounds) are SCIP's nbinvars.  A node applies its changes as SCIPchgVarLb/UbProbing do
+ * (each change's events mark rows at once), then propagates; a row counts as tightened at the root until a change
+ * that its finite sides can use.  Rows redundant under the base bounds are the rows SCIP's root deleted
+ * (lpo_root_deleted_rows): they take no part.  Outputs as lpo_propagate_nodes. */
+int lpo_propagate_seq(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub, int32_t* out_order,
+   lpo_result* res);
+void lpo_root_deleted_rows(const lpo_problem* prob, const lpo_params* par, const double* lb, const double* ub,
+   uint8_t* del);
+int lpo_propagate_nodes_seq(const lpo_problem* prob, const lpo_params* par, const double* baselb,
+   const double* baseub, int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb,
+   const double* chg_ub, int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int32_t cap, int32_t nthreads, lpo_result* total);
 
 #ifdef __cplusplus
 }

@@ -16,8 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liblinprop_oracle.so")
 SCIP_ORACLE = os.path.join(HERE, "_ref", "scip_oracle")
-# the SCIP source tree the Makefile's `ref` target compiles (same default as its REFDIR)
-REFDIR = os.environ.get("REFDIR", "/root/reference")
+# the SCIP source tree the Makefile's `ref` target compiles; unset means the sources are not available and the
+# tests that read them skip
+REFDIR = os.environ.get("REFDIR", "")
 
 _P = ctypes.c_void_p
 
@@ -42,13 +43,14 @@ class Log(ctypes.Structure):
 
 class Problem(ctypes.Structure):
     _fields_ = [("m", ctypes.c_int64), ("n", ctypes.c_int64), ("rowptr", _P), ("colidx", _P), ("vals", _P),
-                ("lhs", _P), ("rhs", _P), ("isint", _P), ("colptr", _P), ("rowidx", _P), ("cvals", _P)]
+                ("lhs", _P), ("rhs", _P), ("isint", _P), ("colptr", _P), ("rowidx", _P), ("cvals", _P),
+                ("varidx", _P)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("cutoff", ctypes.c_int32), ("rounds", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("rows", ctypes.c_int64), ("nnz", ctypes.c_int64),
-                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64)]
+                ("candidates", ctypes.c_int64), ("changes", ctypes.c_int64), ("live_rows", ctypes.c_int64)]
 
 
 def build() -> str:
@@ -76,6 +78,10 @@ def lib():
         L.lpo_propagate_nodes.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, ctypes.c_int64,
                                           _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(Result)]
+        L.lpo_propagate_seq.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P,
+                                        ctypes.POINTER(Result)]
+        L.lpo_propagate_nodes_seq.argtypes = L.lpo_propagate_nodes.argtypes
+        L.lpo_root_deleted_rows.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P]
         _lib = L
     return _lib
 
@@ -96,8 +102,11 @@ def _ptr(a):
 class Oracle:
     """Keeps an instance (and its CSC copy) alive for repeated oracle calls."""
 
-    def __init__(self, inst):
+    def __init__(self, inst, varidx=None):
+        """varidx: SCIP's problem index of each column (instances.scip_var_index), the tie-break of the order SCIP
+        sorts rows into; None uses the column index."""
         self.inst = inst
+        self.varidx = None if varidx is None else np.ascontiguousarray(varidx, dtype=np.int32)
         self.rowptr = np.ascontiguousarray(inst.rowptr, dtype=np.int64)
         self.colidx = np.ascontiguousarray(inst.colidx, dtype=np.int32)
         self.vals = np.ascontiguousarray(inst.vals, dtype=np.float64)
@@ -107,7 +116,8 @@ class Oracle:
         cp, ri, cv = inst.csc()
         self.colptr, self.rowidx, self.cvals = cp, ri, cv
         self.prob = Problem(inst.m, inst.n, _ptr(self.rowptr), _ptr(self.colidx), _ptr(self.vals), _ptr(self.lhs),
-                            _ptr(self.rhs), _ptr(self.isint), _ptr(self.colptr), _ptr(self.rowidx), _ptr(self.cvals))
+                            _ptr(self.rhs), _ptr(self.isint), _ptr(self.colptr), _ptr(self.rowidx), _ptr(self.cvals),
+                            _ptr(self.varidx))
 
     def activities(self, lb, ub, rows=None, par=None):
         par = par or params()
@@ -177,8 +187,32 @@ class Oracle:
         self.last_ranged = (rrnd[:r][q], rcol[:r][q], rrow[:r][q])
         return lb, ub, res, (col[:n][o], rnd[:n][o], llb[:n][o], lub[:n][o])
 
-    def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1):
-        """Node batch; returns dict with cutoff [N], rounds [N], n [N], col/lb/ub [N, cap] and totals."""
+    def propagate_seq(self, lb, ub, par=None):
+        """Root fixpoint in SCIP's own order (lpo_propagate_seq); returns (lb, ub, Result, order) where order[p]
+        for p in row i's CSR range is the CSR position of the row's entries in the order SCIP holds them at the end."""
+        par = par or params()
+        lb = np.array(lb, dtype=np.float64)
+        ub = np.array(ub, dtype=np.float64)
+        order = np.zeros(max(1, self.inst.nnz), dtype=np.int32)
+        res = Result()
+        if lib().lpo_propagate_seq(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), _ptr(order),
+                                   ctypes.byref(res)) != 0:
+            raise MemoryError("oracle allocation failed")
+        return lb, ub, res, order[:self.inst.nnz]
+
+    def root_deleted_rows(self, lb, ub, par=None):
+        """Rows redundant under lb/ub: the rows SCIP's root deletes (lpo_root_deleted_rows)."""
+        par = par or params()
+        lb = np.ascontiguousarray(lb, dtype=np.float64)
+        ub = np.ascontiguousarray(ub, dtype=np.float64)
+        out = np.zeros(self.inst.m, dtype=np.uint8)
+        lib().lpo_root_deleted_rows(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), _ptr(out))
+        return out.astype(bool)
+
+    def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1, seq=False):
+        """Node batch; returns dict with cutoff [N], rounds [N], n [N], col/lb/ub [N, cap] and totals.
+        seq: SCIP's own order (lpo_propagate_nodes_seq; each row's entries in storage order are taken as the order
+        SCIP holds the row in) instead of rounds."""
         par = par or params()
         N = nodes.nnodes
         baselb = np.ascontiguousarray(baselb, dtype=np.float64)
@@ -191,19 +225,44 @@ class Oracle:
                    n=np.zeros(N, dtype=np.int32), col=np.zeros((N, cap), dtype=np.int32),
                    lb=np.zeros((N, cap)), ub=np.zeros((N, cap)))
         tot = Result()
-        rc = lib().lpo_propagate_nodes(ctypes.byref(self.prob), ctypes.byref(par), _ptr(baselb), _ptr(baseub), N,
-                                       _ptr(ptr), _ptr(col), _ptr(nlb), _ptr(nub), _ptr(out["cutoff"]),
-                                       _ptr(out["rounds"]), _ptr(out["n"]), _ptr(out["col"]), _ptr(out["lb"]),
-                                       _ptr(out["ub"]), cap, nthreads, ctypes.byref(tot))
+        fn = lib().lpo_propagate_nodes_seq if seq else lib().lpo_propagate_nodes
+        rc = fn(ctypes.byref(self.prob), ctypes.byref(par), _ptr(baselb), _ptr(baseub), N,
+                _ptr(ptr), _ptr(col), _ptr(nlb), _ptr(nub), _ptr(out["cutoff"]), _ptr(out["rounds"]), _ptr(out["n"]),
+                _ptr(out["col"]), _ptr(out["lb"]), _ptr(out["ub"]), cap, nthreads, ctypes.byref(tot))
         if rc != 0:
             raise MemoryError("oracle node batch failed")
         out["total"] = tot
         return out
 
 
-def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False, sortvars=True):
+def _read_order(inst, path):
+    """SCIP's row order file (scip_driver.c --order) as CSR positions into inst, and the rows SCIP deleted."""
+    raw = np.fromfile(path, dtype=np.int32)
+    m = int(raw[:2].view(np.int64)[0])
+    assert m == inst.m
+    order = np.arange(inst.nnz, dtype=np.int32)
+    deleted = np.zeros(m, dtype=bool)
+    off = 2
+    for i in range(m):
+        ln = int(raw[off])
+        off += 1
+        if ln < 0:
+            deleted[i] = True
+            continue
+        cols = raw[off:off + ln]
+        off += ln
+        p0, p1 = inst.rowptr[i], inst.rowptr[i + 1]
+        pos = {int(c): p for p, c in zip(range(p0, p1), inst.colidx[p0:p1])}
+        order[p0:p1] = [pos[int(c)] for c in cols]
+    return order, deleted
+
+
+def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False, sortvars=True, fresh=False,
+             order=False):
     """Run SCIP itself (oracle/_ref/scip_oracle) on the instance; returns the parsed output of
-    scip_gb300.instances.read_oracle_output."""
+    scip_gb300.instances.read_oracle_output, plus (with order=True) SCIP's row order after the root as a CSR
+    position array (order[p] for p in row i's range: the position of the row's k-th entry; rows deleted at the
+    root keep their storage order) and the mask of the rows the root deleted.  fresh: every node from a newly transformed problem (scip_driver.c --fresh)."""
     from scip_gb300.instances import read_oracle_output
 
     if not os.path.exists(SCIP_ORACLE):
@@ -217,6 +276,9 @@ def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False,
             npth = os.path.join(d, "nodes.bin")
             nodes.write(npth)
         cmd = ([SCIP_ORACLE, ip, npth, op] + (["--easy"] if easy else []) + (["--ranged"] if ranged else [])
-               + ([] if sortvars else ["--nosort"]) + ["--repeat", str(repeat)])
+               + ([] if sortvars else ["--nosort"]) + ["--repeat", str(repeat)] + (["--fresh"] if fresh else [])
+               + (["--order", os.path.join(d, "order.bin")] if order else []))
         subprocess.run(cmd, check=True, capture_output=True)
+        if order:
+            return read_oracle_output(op) + _read_order(inst, os.path.join(d, "order.bin"))
         return read_oracle_output(op)

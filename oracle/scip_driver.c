@@ -3,6 +3,7 @@
  * (oracle/linprop_oracle.c) and the CUDA path against the reference itself.
  *
  * Usage:  scip_oracle <instance.bin> <nodes.bin|-> <out.bin> [--easy] [--ranged] [--nosort] [--repeat R]
+ *                      [--fresh] [--order order.bin]
  *
  * Pattern (the probing-in-heuristic recipe; see src/scip/scip_probing.c:120-690 and
  * tests/include/scip_test.c:121-133 for the interrupt idiom):
@@ -19,7 +20,13 @@
  *   - the root fixpoint is what SCIP's root propagation (solve.c:723) leaves in the local bounds when
  *     the BEFORENODE heuristic runs (solve.c:5296-5303);
  *   - each node: SCIPnewProbingNode, SCIPchgVarLb/UbProbing for its bound changes,
- *     SCIPpropagateProbing(-1) (scip_probing.c:581), read SCIPvarGetLb/UbLocal, SCIPbacktrackProbing(0).
+ *     SCIPpropagateProbing(-1) (scip_probing.c:581), read SCIPvarGetLb/UbLocal, SCIPbacktrackProbing(0);
+ *   - --fresh: every node starts from a newly transformed problem (SCIPfreeTransform, then the root again), so a
+ *     node's result does not depend on the nodes before it (SCIP keeps activities, which drift under incremental
+ *     updates, marks left by a cut-off node, and per-row flags across the nodes of one probing session);
+ *   - --order: after the (first) root, each row's variables in the order SCIP holds them (SCIPgetVarsLinear on the
+ *     transformed constraint), the order the next propagation visits them in: int64 m, then per row int32 len and
+ *     int32 columns[len] (len = -1 for a row deleted at the root).
  *
  * Instance file (little endian): "LPINST01", int64 m, n, nnz, flags; int64 rowptr[m+1]; int32 col[nnz];
  * f64 val[nnz]; f64 lhs[m]; f64 rhs[m]; f64 lb[n]; f64 ub[n]; int8 vartype[n] (0 continuous, 1 integer).
@@ -59,9 +66,16 @@ typedef struct
 {
    Inst* inst;
    SCIP_VAR** vars;
+   SCIP_CONS** conss;
    FILE* out;
    int done;
    int repeat;
+   int64_t k0;          /* nodes [k0, k1) are propagated in this solve */
+   int64_t k1;
+   int rootdone;        /* the root record was written */
+   double* rootlb;
+   double* rootub;
+   const char* orderpath;
 } Run;
 
 static void die(const char* msg)
@@ -134,6 +148,40 @@ static void loadNodes(const char* path, Inst* in)
    fclose(f);
 }
 
+/* each row's variables in the order the transformed constraint holds them (columns), -1 for a deleted row */
+static SCIP_RETCODE writeOrder(SCIP* scip, Run* run)
+{
+   Inst* in = run->inst;
+   FILE* f = fopen(run->orderpath, "wb");
+   int64_t i;
+   if( f == NULL )
+      die("cannot open order output");
+   fwrite(&in->m, 8, 1, f);
+   for( i = 0; i < in->m; ++i )
+   {
+      SCIP_CONS* tc = NULL;
+      int32_t len = -1;
+      SCIP_CALL( SCIPgetTransformedCons(scip, run->conss[i], &tc) );
+      if( tc != NULL && !SCIPconsIsDeleted(tc) )
+      {
+         SCIP_VAR** vars = SCIPgetVarsLinear(scip, tc);
+         int q;
+         len = SCIPgetNVarsLinear(scip, tc);
+         fwrite(&len, 4, 1, f);
+         for( q = 0; q < len; ++q )
+         {
+            /* transformed variables are named t_<original name>, and the original names are x<column> */
+            int32_t c = (int32_t)strtol(SCIPvarGetName(vars[q]) + 3, NULL, 10);
+            fwrite(&c, 4, 1, f);
+         }
+      }
+      else
+         fwrite(&len, 4, 1, f);
+   }
+   fclose(f);
+   return SCIP_OKAY;
+}
+
 /* the work happens the first time SCIP calls the heuristic, right after the root propagation loop */
 static SCIP_DECL_HEUREXEC(heurExecOracle)
 {
@@ -151,22 +199,28 @@ static SCIP_DECL_HEUREXEC(heurExecOracle)
       return SCIP_OKAY;
    run->done = 1;
 
-   rootlb = malloc(sizeof(double) * (size_t)in->n);
-   rootub = malloc(sizeof(double) * (size_t)in->n);
-   for( j = 0; j < in->n; ++j )
+   rootlb = run->rootlb;
+   rootub = run->rootub;
+   if( !run->rootdone )
    {
-      SCIP_VAR* tv;
-      SCIP_CALL( SCIPgetTransformedVar(scip, run->vars[j], &tv) );
-      rootlb[j] = SCIPvarGetLbLocal(tv);
-      rootub[j] = SCIPvarGetUbLocal(tv);
+      for( j = 0; j < in->n; ++j )
+      {
+         SCIP_VAR* tv;
+         SCIP_CALL( SCIPgetTransformedVar(scip, run->vars[j], &tv) );
+         rootlb[j] = SCIPvarGetLbLocal(tv);
+         rootub[j] = SCIPvarGetUbLocal(tv);
+      }
+      fwrite(&flag, 1, 1, run->out);
+      fwrite(&roottime, 8, 1, run->out);
+      fwrite(rootlb, 8, (size_t)in->n, run->out);
+      fwrite(rootub, 8, (size_t)in->n, run->out);
+      if( run->orderpath != NULL )
+         SCIP_CALL( writeOrder(scip, run) );
+      run->rootdone = 1;
    }
-   fwrite(&flag, 1, 1, run->out);
-   fwrite(&roottime, 8, 1, run->out);
-   fwrite(rootlb, 8, (size_t)in->n, run->out);
-   fwrite(rootub, 8, (size_t)in->n, run->out);
 
    SCIP_CALL( SCIPstartProbing(scip) );
-   for( k = 0; k < in->nnodes; ++k )
+   for( k = run->k0; k < run->k1; ++k )
    {
       SCIP_Bool cutoff = FALSE;
       SCIP_Longint ndomreds = 0;
@@ -242,8 +296,6 @@ static SCIP_DECL_HEUREXEC(heurExecOracle)
       SCIP_CALL( SCIPbacktrackProbing(scip, 0) );
    }
    SCIP_CALL( SCIPendProbing(scip) );
-   free(rootlb);
-   free(rootub);
 
    SCIP_CALL( SCIPinterruptSolve(scip) );
    *result = SCIP_DIDNOTFIND;
@@ -288,7 +340,7 @@ static SCIP_RETCODE setParams(SCIP* scip, int easy, int ranged, int nosort)
 }
 
 static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* outpath, int easy, int ranged,
-   int nosort, int repeat)
+   int nosort, int repeat, int fresh, const char* orderpath)
 {
    SCIP* scip = NULL;
    Inst in;
@@ -310,6 +362,12 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
    memset(&r, 0, sizeof(r));
    r.inst = &in;
    r.repeat = repeat;
+   r.orderpath = orderpath;
+   r.k0 = 0;
+   r.k1 = fresh ? (in.nnodes > 0 ? 1 : 0) : in.nnodes;
+   r.rootlb = malloc(sizeof(double) * (size_t)(in.n + 1));
+   r.rootub = malloc(sizeof(double) * (size_t)(in.n + 1));
+   r.conss = malloc(sizeof(SCIP_CONS*) * (size_t)(in.m + 1));
    r.vars = malloc(sizeof(SCIP_VAR*) * (size_t)in.n);
    r.out = fopen(outpath, "wb");
    if( r.out == NULL )
@@ -349,15 +407,20 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
          (void)SCIPsnprintf(name, 32, "r%lld", (long long)i);
          SCIP_CALL( SCIPcreateConsBasicLinear(scip, &cons, name, len, rowvars, &in.val[p0], in.lhs[i], in.rhs[i]) );
          SCIP_CALL( SCIPaddCons(scip, cons) );
-         SCIP_CALL( SCIPreleaseCons(scip, &cons) );
+         r.conss[i] = cons;   /* kept captured, for the order output */
       }
       free(rowvars);
    }
 
+   SCIP_CALL( SCIPsolve(scip) );
+   /* --fresh: every further node gets a newly transformed problem and its own root */
+   while( fresh && r.done && r.k1 < in.nnodes )
    {
-      double t0 = now();
+      SCIP_CALL( SCIPfreeTransform(scip) );
+      r.done = 0;
+      r.k0 = r.k1;
+      r.k1 = r.k0 + 1;
       SCIP_CALL( SCIPsolve(scip) );
-      (void)t0;
    }
 
    if( !r.done )
@@ -372,9 +435,14 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
    }
    fclose(r.out);
 
+   for( i = 0; i < in.m; ++i )
+      SCIP_CALL( SCIPreleaseCons(scip, &r.conss[i]) );
    for( j = 0; j < in.n; ++j )
       SCIP_CALL( SCIPreleaseVar(scip, &r.vars[j]) );
    free(r.vars);
+   free(r.conss);
+   free(r.rootlb);
+   free(r.rootub);
    SCIP_CALL( SCIPfree(&scip) );
    return SCIP_OKAY;
 }
@@ -385,12 +453,14 @@ int main(int argc, char** argv)
    int ranged = 0;
    int nosort = 0;
    int repeat = 1;
+   int fresh = 0;
+   const char* orderpath = NULL;
    int a;
    SCIP_RETCODE rc;
    if( argc < 4 )
    {
-      fprintf(stderr, "usage: %s instance.bin nodes.bin|- out.bin [--easy] [--ranged] [--nosort] [--repeat R]\n",
-         argv[0]);
+      fprintf(stderr, "usage: %s instance.bin nodes.bin|- out.bin [--easy] [--ranged] [--nosort] [--repeat R] [--fresh]"
+         " [--order order.bin]\n", argv[0]);
       return 2;
    }
    for( a = 4; a < argc; ++a )
@@ -403,10 +473,14 @@ int main(int argc, char** argv)
          nosort = 1;
       else if( strcmp(argv[a], "--repeat") == 0 && a + 1 < argc )
          repeat = atoi(argv[++a]);
+      else if( strcmp(argv[a], "--fresh") == 0 )
+         fresh = 1;
+      else if( strcmp(argv[a], "--order") == 0 && a + 1 < argc )
+         orderpath = argv[++a];
    }
    if( repeat < 1 )
       repeat = 1;
-   rc = run(argv[1], argv[2], argv[3], easy, ranged, nosort, repeat);
+   rc = run(argv[1], argv[2], argv[3], easy, ranged, nosort, repeat, fresh, orderpath);
    if( rc != SCIP_OKAY )
    {
       fprintf(stderr, "scip_oracle: SCIP error %d\n", (int)rc);

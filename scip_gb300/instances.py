@@ -403,6 +403,49 @@ def concat_instances(insts: List[Instance]):
 
 
 # ---------------------------------------------------------------- result files of the SCIP oracle
+def scip_var_index(isint: np.ndarray, lb: np.ndarray, ub: np.ndarray) -> np.ndarray:
+    """SCIP's problem index of each column when the columns are added to a SCIP problem in column order and the
+    problem is then transformed, as a host program (the oracle driver, or a user building the problem) does.
+
+    SCIP keeps a problem's variables grouped by type -- binaries, integers, continuous (prob.c: probProvidePos,
+    probInsertVar) -- and makes room for an inserted variable by moving the first variable of each later group to
+    that group's end, so within a group the index does not follow the column.  An integral column with bounds in
+    {0, 1} is created as a binary variable (var.c: SCIPvarCreateOriginal's [0,1]-integer conversion).  The
+    transformed problem adds the original variables in their index order (prob.c: SCIPprobTransform).  This index
+    breaks ties in the order tightenBounds visits a row's entries (cons_linear.c: consdataCompVarProp)."""
+    n = len(isint)
+    kind = np.where(np.asarray(isint) != 0, 1, 2)
+    kind[(kind == 1) & np.isin(lb, (0.0, 1.0)) & np.isin(ub, (0.0, 1.0))] = 0
+
+    def insert(seq):
+        arr = np.empty(n, dtype=np.int64)
+        nb = ni = nv = 0
+        for v in seq:
+            pos = nv
+            t = kind[v]
+            if t != 2:
+                cs = nb + ni
+                if pos > cs:
+                    arr[pos] = arr[cs]
+                    pos = cs
+                if t == 0 and pos > nb:
+                    arr[pos] = arr[nb]
+                    pos = nb
+                if t == 0:
+                    nb += 1
+                else:
+                    ni += 1
+            arr[pos] = v
+            nv += 1
+        return arr
+
+    orig = insert(range(n))
+    trans = insert(orig)
+    idx = np.empty(n, dtype=np.int32)
+    idx[trans] = np.arange(n, dtype=np.int32)
+    return idx
+
+
 def read_oracle_output(path: str):
     """Parse the oracle driver's output: (rootcutoff, rootlb, rootub, nodes) where nodes is a list of
     (cutoff, seconds, cols, lb, ub) with the columns whose bounds differ from the root fixpoint."""
