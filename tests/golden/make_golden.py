@@ -2,8 +2,11 @@
 
 Runs oracle/_ref/scip_oracle (SCIP built from the reference sources by `make -C oracle ref`) in the
 probing-in-heuristic pattern described in oracle/scip_driver.c and stores, per case, the instance arrays
-(so that the fixtures do not depend on numpy's generator streams), SCIP's root fixpoint, and for node cases
-SCIP's per-node cutoff verdicts and changed bounds.  Cases:
+(so that the fixtures do not depend on numpy's generator streams), SCIP's root fixpoint, the order SCIP holds
+each row's entries in after the root (`<rule>_order`: CSR positions) and the rows it deleted there
+(`<rule>_rowdel`), and for node cases SCIP's per-node cutoff verdicts and changed bounds.  Every node starts from
+a newly transformed problem (scip_driver.c --fresh), so that its result does not depend on the nodes SCIP
+propagated before it.  Cases:
 
   root_mip_s{0,1,2}          2,000 x 5,000 root fixpoint, residual rule (maxeasyactivitydelta 0) and easy rule
   root_mip_s0_nodes          200 branch-and-bound nodes on top of SCIP's root fixpoint
@@ -54,10 +57,12 @@ def save_case(name, inst, nnodes=0, node_seed=11):
            "lb": inst.lb, "ub": inst.ub, "isint": inst.isint}
     for easy in (False, True):
         tag = "easy" if easy else "res"
-        rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy)
+        rcut, rlb, rub, _, order, rowdel = oracle.run_scip(inst, easy=easy, order=True)
         out[f"{tag}_rootcut"] = np.int8(rcut)
         out[f"{tag}_rootlb"] = rlb
         out[f"{tag}_rootub"] = rub
+        out[f"{tag}_order"] = order
+        out[f"{tag}_rowdel"] = rowdel.astype(np.int8)
     if nnodes:
         # nodes start from SCIP's own root fixpoint (residual rule) so that node results compare node work only
         rlb, rub = out["res_rootlb"], out["res_rootub"]
@@ -65,7 +70,7 @@ def save_case(name, inst, nnodes=0, node_seed=11):
         out["node_ptr"], out["node_col"], out["node_lb"], out["node_ub"] = nodes.ptr, nodes.col, nodes.lb, nodes.ub
         for easy in (False, True):
             tag = "easy" if easy else "res"
-            _, rlb2, rub2, res = oracle.run_scip(inst, nodes, easy=easy)
+            _, rlb2, rub2, res = oracle.run_scip(inst, nodes, easy=easy, fresh=True)
             assert np.array_equal(rlb2, out[f"{tag}_rootlb"]) and np.array_equal(rub2, out[f"{tag}_rootub"])
             cut, ptr, col, lb, ub = node_arrays(res)
             out[f"{tag}_ncut"], out[f"{tag}_nptr"], out[f"{tag}_ncol"] = cut, ptr, col

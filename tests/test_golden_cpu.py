@@ -1,10 +1,12 @@
-"""The oracle (C restatement of cons_linear propagation) against SCIP 11's own results (tests/golden).
+"""The round-based oracle (oracle/linprop_oracle.c, the checker of the CUDA round kernels) against SCIP 11's own
+results (tests/golden).
 
-SCIP applies tightenings one at a time in its constraint order; the oracle (and the CUDA path, which is
-bit-identical to it) applies them in rounds.  Under SCIP's minimal-improvement test (set.c:7711-7753) both stop
-at valid fixpoints of the same rule that can differ for continuous columns, so the contract checked here is:
-cutoff verdicts identical, integer bounds identical on every node, SCIP's own fixpoint is a fixpoint of the
-oracle's rules, and the continuous agreement recorded below does not regress.
+SCIP applies tightenings one at a time in its constraint order; the round mode applies them in rounds.  Under
+SCIP's minimal-improvement test (set.c:7711-7753) both stop at valid fixpoints of the same rule that can differ for
+continuous columns, so the contract checked here is: cutoff verdicts identical, integer bounds identical on every
+node, SCIP's own fixpoint is a fixpoint of the oracle's rules, and the continuous agreement recorded below does not
+regress.  SCIP's own order (oracle/linprop_seq.c, the checker of the CUDA sequential node kernel) meets the exact
+contract with no recorded allowance: tests/test_seq_cpu.py.
 """
 import numpy as np
 import pytest
