@@ -71,6 +71,18 @@ typedef struct
  * without, the index order (binaries, integers, continuous columns, each by column).  Not available in
  * gbp_propagate_nodes_noalloc. */
 #define GBP_FLAG_RANGEDROW 4
+/* batched nodes (gbp_propagate_nodes / gbp_propagate_nodes_device) in SCIP's own order instead of rounds: the rows
+ * marked for propagation one at a time in SCIP's order (SCIPconshdlrPropagate, cons.c:3905-4080, with
+ * conshdlrProcessUpdates, cons.c:1689), every tightening applied at once and the other rows' activities updated
+ * incrementally by its bound-change event (consPropLinear, cons_linear.c:16126; tightenBounds :6976-7154;
+ * eventExecLinear :17162-17363), so that a node's final bounds are the ones SCIP's own propagation reaches, not only
+ * a valid fixpoint of the same rules.  Each row's entries are visited in storage order, which must be the order
+ * SCIP holds the row in (SCIPgetVarsLinear during solving; consdataCompVarProp, cons_linear.c:3191-3254, on the
+ * base bounds for rows SCIP has not re-sorted); with sortvars a row's leading binaries under the base bounds are its
+ * nbinvars.  The base bounds must be a propagated fixpoint (SCIP's root): rows redundant under them are the rows
+ * SCIP's root deleted and take no part, and every row counts as already tightened there until a change that one of
+ * its finite sides can use.  Does not combine with GBP_FLAG_RANGEDROW. */
+#define GBP_FLAG_SCIPORDER 8
 
 typedef struct
 {

@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "--fmad=false", "-std=c++17",
               "-Xcompiler", "-fPIC", "-I" + INCLUDE]
-CU_SOURCES = ["gbp_kernels.cu", "gbp_nodes_ranged.cu", "gbp_api.cu", "gbp_noalloc.cu"]
+CU_SOURCES = ["gbp_kernels.cu", "gbp_nodes_ranged.cu", "gbp_api.cu", "gbp_noalloc.cu", "gbp_seq.cu"]
 
 
 def _nvcc() -> str:

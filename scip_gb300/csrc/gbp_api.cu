@@ -122,6 +122,18 @@ struct gbp_ctx {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool graph_failed = false;
 
+  // SCIP's own order for batched nodes (GBP_FLAG_SCIPORDER): the column-major copy with each column's rows ascending
+  // (built on first use after an upload), the per-row preparation of a call, and per-warp slots
+  bool seq_csc_ready = false;
+  int32_t* d_sq_crow = nullptr;
+  double* d_sq_cval = nullptr;
+  int64_t sq_cap_nnz = 0;
+  int* d_sq_prep = nullptr;
+  int64_t sq_cap_m = 0;
+  void* seq_mem = nullptr;
+  SeqSlots seqslots{};
+  int64_t seq_epoch_budget = 0;
+
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -154,7 +166,8 @@ static void freeProblem(gbp_ctx* ctx) {
                   ctx->d_cscrow, ctx->d_lb, ctx->d_ub, ctx->d_cand, ctx->d_cflag, ctx->d_touched, ctx->d_list[0],
                   ctx->d_list[1], ctx->d_rowstamp, ctx->d_allrows, ctx->d_base, ctx->slot_mem, ctx->stage,
                   ctx->d_rowinst, ctx->d_colinst, ctx->d_instcut, ctx->d_glb, ctx->d_gub, ctx->d_relig,
-                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp, ctx->d_rdom, ctx->d_rchanged, ctx->d_rcoef, ctx->d_snap};
+                  ctx->d_rlist, ctx->d_rperm, ctx->d_rtmp, ctx->d_rdom, ctx->d_rchanged, ctx->d_rcoef, ctx->d_snap,
+                  ctx->d_sq_crow, ctx->d_sq_cval, ctx->d_sq_prep, ctx->seq_mem};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ctx->d_rowptr = nullptr; ctx->d_colidx = nullptr; ctx->d_vals = nullptr; ctx->d_lhs = nullptr;
@@ -172,6 +185,9 @@ static void freeProblem(gbp_ctx* ctx) {
   ctx->d_snap = nullptr;
   ctx->bounds_set = false;
   ctx->nslots = 0;
+  ctx->d_sq_crow = nullptr; ctx->d_sq_cval = nullptr; ctx->sq_cap_nnz = 0; ctx->seq_csc_ready = false;
+  ctx->d_sq_prep = nullptr; ctx->sq_cap_m = 0;
+  ctx->seq_mem = nullptr; ctx->seqslots = SeqSlots{};
   ctx->has_problem = false;
 }
 
@@ -419,6 +435,12 @@ static int prepareUpload(gbp_ctx* ctx, int64_t m, int64_t n, int64_t nnz) {
     CK(cudaFree(ctx->slot_mem));
     ctx->slot_mem = nullptr;
     ctx->nslots = 0;
+  }
+  ctx->seq_csc_ready = false;
+  if (ctx->seq_mem && (ctx->seqslots.nstride < (int64_t)nn || ctx->seqslots.mstride < (int64_t)mm)) {
+    CK(cudaFree(ctx->seq_mem));
+    ctx->seq_mem = nullptr;
+    ctx->seqslots = SeqSlots{};
   }
   return GBP_OK;
 }
@@ -1398,6 +1420,166 @@ static int ensureSlots(gbp_ctx* ctx, int64_t nnodes) {
   return GBP_OK;
 }
 
+// ------------------------------------------------------------------------------------------ SCIP's own order
+// the column-major copy with each column's rows ascending and their coefficients (once per upload)
+static int ensureSeqCsc(gbp_ctx* ctx) {
+  if (ctx->seq_csc_ready) return GBP_OK;
+  const int64_t zz = std::max<int64_t>(ctx->nnz, 1);
+  if (zz > ctx->sq_cap_nnz) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_sq_crow) cudaFree(ctx->d_sq_crow);
+    if (ctx->d_sq_cval) cudaFree(ctx->d_sq_cval);
+    ctx->d_sq_crow = nullptr;
+    ctx->d_sq_cval = nullptr;
+    ctx->sq_cap_nnz = 0;
+    CK(cudaMalloc(&ctx->d_sq_crow, ctx->cap_nnz * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_sq_cval, ctx->cap_nnz * sizeof(double)));
+    ctx->sq_cap_nnz = ctx->cap_nnz;
+  }
+  if (ctx->cap_m > ctx->sq_cap_m) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_sq_prep) cudaFree(ctx->d_sq_prep);
+    ctx->d_sq_prep = nullptr;
+    CK(cudaMalloc(&ctx->d_sq_prep, ctx->cap_m * sizeof(int)));
+    ctx->sq_cap_m = ctx->cap_m;
+  }
+  CK(launchSeqCsc(ctx->stream, gridFor(ctx, ctx->nnz), ctx->m, ctx->n, ctx->nnz, ctx->d_rowptr, ctx->d_colidx,
+                  ctx->d_vals, ctx->d_sq_crow, ctx->d_sq_cval));
+  ctx->seq_csc_ready = true;
+  return GBP_OK;
+}
+
+// per-warp scratch for min(resident warps, nnodes) nodes at a time; grown when a later call has more nodes
+static int ensureSeqSlots(gbp_ctx* ctx, int64_t nnodes) {
+  int occ = 0;
+  CK(nodesSeqOccupancy(&occ));
+  const int64_t want = std::min<int64_t>((int64_t)ctx->sms * std::max(occ, 1) * SEQ_WARPS, std::max<int64_t>(nnodes, 1));
+  if (ctx->seq_mem && ctx->seqslots.nslots >= want) return GBP_OK;
+  if (ctx->seq_mem) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->seq_mem);
+    ctx->seq_mem = nullptr;
+    ctx->seqslots = SeqSlots{};
+  }
+  const int64_t ns = std::max<int64_t>(ctx->n, 1), ms = std::max<int64_t>(ctx->m, 1);
+  const size_t per_slot = seqSlotLayout(ns, ms, 1, nullptr, nullptr);
+  size_t freeb = 0, totalb = 0;
+  CK(cudaMemGetInfo(&freeb, &totalb));
+  int64_t nslots = want;
+  const size_t budget = freeb / 3;
+  while (nslots > 1 && (size_t)nslots * per_slot > budget) nslots -= 1;
+  if ((size_t)nslots * per_slot > budget) return fail(ctx, GBP_ERR_NOMEM, "not enough device memory for one slot");
+  const size_t bytes = seqSlotLayout(ns, ms, nslots, nullptr, nullptr);
+  char* base = nullptr;
+  CK(cudaMalloc(&base, bytes));
+  ctx->seq_mem = base;
+  SeqSlots& A = ctx->seqslots;
+  seqSlotLayout(ns, ms, nslots, base, &A);
+  const size_t S = (size_t)nslots;
+  CK(cudaMemsetAsync(A.rows, 0, S * ms * sizeof(SeqRow), ctx->stream));
+  CK(cudaMemsetAsync(A.ost, 0, S * ns * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(A.counter, 0, S * sizeof(int), ctx->stream));
+  ctx->seq_epoch_budget = 0;
+  return GBP_OK;
+}
+
+static int propagateNodesSeq(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
+                             const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+                             int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n,
+                             int32_t* out_col, double* out_lb, double* out_ub, int64_t out_cap, gbp_result* res) {
+  if (rangedOn(ctx)) return fail(ctx, GBP_ERR_INVALID, "GBP_FLAG_SCIPORDER does not combine with GBP_FLAG_RANGEDROW");
+  int rc = ensureSeqCsc(ctx);
+  if (rc) return rc;
+  rc = ensureSeqSlots(ctx, nnodes);
+  if (rc) return rc;
+  const SeqSlots& SL = ctx->seqslots;
+  // every node takes a new epoch in its slot; re-zero the stamps long before a counter wraps
+  if (ctx->seq_epoch_budget + nnodes > (int64_t(1) << 30)) {
+    CK(cudaMemsetAsync(SL.rows, 0, (size_t)SL.nslots * SL.mstride * sizeof(SeqRow), ctx->stream));
+    CK(cudaMemsetAsync(SL.ost, 0, (size_t)SL.nslots * SL.nstride * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(SL.counter, 0, (size_t)SL.nslots * sizeof(int), ctx->stream));
+    ctx->seq_epoch_budget = 0;
+  }
+  CK(cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_next_item, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_out_used, 0, sizeof(unsigned long long), ctx->stream));
+  if (nnodes > ctx->order_cap) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_order) cudaFree(ctx->d_order);
+    ctx->d_order = nullptr;
+    ctx->order_cap = 0;
+    const int64_t cap = std::max<int64_t>(nnodes, 4096);
+    CK(cudaMalloc(&ctx->d_order, cap * sizeof(int)));
+    ctx->order_cap = cap;
+  }
+  CK(cudaMemsetAsync(ctx->d_orderhist, 0, 2 * ORDER_BUCKETS * sizeof(int), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launchNodeOrder(ctx->stream, gridFor(ctx, nnodes, 256, 2), nnodes, ptr, ctx->d_orderhist, ctx->d_order));
+  CK(launchPack(ctx->stream, gridFor(ctx, ctx->n), baselb, baseub, ctx->d_base, ctx->n));
+  const Prob P = devProb(ctx, false, true);
+  CK(launchSeqPrepare(ctx->stream, gridFor(ctx, ctx->m), ctx->num, P, ctx->d_base, ctx->d_sq_prep));
+  SeqArgs A;
+  A.s = ctx->num;
+  A.P = P;
+  A.ccolptr = ctx->d_colptr;
+  A.crow = ctx->d_sq_crow;
+  A.cval = ctx->d_sq_cval;
+  A.prep = ctx->d_sq_prep;
+  A.base = ctx->d_base;
+  A.nnodes = nnodes;
+  A.ptr = ptr;
+  A.chg_col = chg_col;
+  A.chg_lb = chg_lb;
+  A.chg_ub = chg_ub;
+  A.out_cutoff = out_cutoff;
+  A.out_rounds = out_rounds;
+  A.out_off = out_off;
+  A.out_n = out_n;
+  A.out_col = out_col;
+  A.out_lb = out_lb;
+  A.out_ub = out_ub;
+  A.out_cap = out_cap;
+  A.out_used = ctx->d_out_used;
+  A.maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
+  A.next_item = ctx->d_next_item;
+  A.order = ctx->d_order;
+  A.S = SL;
+  A.stats = ctx->d_stats;
+  A.status = ctx->d_status;
+  const int64_t warps = std::min<int64_t>(SL.nslots, nnodes);
+  const int grid = (int)((warps + SEQ_WARPS - 1) / SEQ_WARPS);
+  CK(launchNodesSeq(ctx->stream, grid, A));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  unsigned long long st[8];
+  int status = 0;
+  CK(cudaMemcpyAsync(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&ctx->last_out_used, ctx->d_out_used, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // the queue is dynamic: one slot may have run every node of the call
+  ctx->seq_epoch_budget += nnodes;
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->cutoff = (int32_t)st[4];
+    res->rounds = (int32_t)st[5];
+    res->status = (status & 1) ? 2 : 0;
+    res->launches = 5;  // order (2), pack, row preparation, nodes
+    res->rows = (int64_t)st[0];
+    res->nnz = (int64_t)st[1];
+    res->candidates = (int64_t)st[2];
+    res->changes = (int64_t)st[3];
+    res->live_rows = (int64_t)st[6];
+    res->kernel_ms = ms;
+  }
+  if (status & 4) return fail(ctx, GBP_ERR_INVALID, "change column out of range");
+  if (status & 2) return fail(ctx, GBP_ERR_OVERFLOW, "node output arrays too small");
+  if (status & 1) return GBP_ERR_LIMIT;
+  return GBP_OK;
+}
+
 int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
                                const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
                                int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n,
@@ -1412,6 +1594,9 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
       (out_cap > 0 && (!out_col || !out_lb || !out_ub)))
     return fail(ctx, GBP_ERR_INVALID, "null argument");
   CK(cudaSetDevice(ctx->device));
+  if (ctx->par.flags & GBP_FLAG_SCIPORDER)
+    return propagateNodesSeq(ctx, baselb, baseub, nnodes, ptr, chg_col, chg_lb, chg_ub, out_cutoff, out_rounds,
+                             out_off, out_n, out_col, out_lb, out_ub, out_cap, res);
   int rc = ensureSlots(ctx, nnodes);
   if (rc) return rc;
   const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;

@@ -94,6 +94,98 @@ struct NodesArgs {
 };
 
 
+// ------------------------------------------------------------------------------------------ SCIP's own order
+// State of one row in one node of the sequential kernel (gbp_seq.cu): struct SCIP_ConsData's activities, counters,
+// maxactdelta and flags, plus the node's marking bookkeeping; valid while stamp equals the node's epoch.
+struct SeqRow {
+  double minhi, minlo, maxhi, maxlo;
+  double lastmin, lastmax, maxdelta;
+  int minposinf, minneginf, minposhuge, minneghuge;
+  int maxposinf, maxneginf, maxposhuge, maxneghuge;
+  int maxdeltacol, mpos, stamp;
+  unsigned flags;
+};
+static_assert(sizeof(SeqRow) == 104, "SeqRow layout");
+
+// warps (one node each) per CTA of the sequential kernel
+constexpr int SEQ_WARPS = 4;
+
+// per-warp scratch of the sequential kernel: `nslots` copies of row- and column-sized arrays
+struct SeqSlots {
+  int64_t nslots;
+  int64_t nstride;     // columns per slot
+  int64_t mstride;     // rows per slot
+  SeqRow* rows;        // [mstride]
+  double2* ovl;        // [nstride] node bounds that differ from the base (valid where ost == the node's epoch)
+  int* ost;
+  int* M;              // [mstride] marked rows, in propagation order
+  int* U;              // [mstride] rows with delayed updates
+  int* dirty;          // [nstride] columns changed in the node
+  int* counter;        // [nslots] epoch counter of each slot (persists across launches)
+};
+
+inline size_t seqSlotLayout(int64_t ns, int64_t ms, int64_t nslots, char* base, SeqSlots* out) {
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t S = (size_t)nslots, N = (size_t)ns, M = (size_t)ms;
+  size_t off = 0;
+  const size_t o_rows = off; off = align(off + S * M * sizeof(SeqRow));
+  const size_t o_ovl = off; off = align(off + S * N * sizeof(double2));
+  const size_t o_ost = off; off = align(off + S * N * sizeof(int));
+  const size_t o_m = off; off = align(off + S * M * sizeof(int));
+  const size_t o_u = off; off = align(off + S * M * sizeof(int));
+  const size_t o_dirty = off; off = align(off + S * N * sizeof(int));
+  const size_t o_ctr = off; off = align(off + S * sizeof(int));
+  if (base != nullptr && out != nullptr) {
+    out->nslots = nslots;
+    out->nstride = ns;
+    out->mstride = ms;
+    out->rows = (SeqRow*)(base + o_rows);
+    out->ovl = (double2*)(base + o_ovl);
+    out->ost = (int*)(base + o_ost);
+    out->M = (int*)(base + o_m);
+    out->U = (int*)(base + o_u);
+    out->dirty = (int*)(base + o_dirty);
+    out->counter = (int*)(base + o_ctr);
+  }
+  return off;
+}
+
+struct SeqArgs {
+  Num s;
+  Prob P;                  // rows (CSR) and sides; the entries of a row in the order SCIP holds them
+  const int64_t* ccolptr;  // column-major copy with each column's rows ascending
+  const int32_t* crow;
+  const double* cval;
+  const int* prep;         // per row: leading binaries under the base domain; negative: deleted at the root
+  const double2* base;     // packed base bounds
+  int64_t nnodes;
+  const int64_t* ptr;
+  const int32_t* chg_col;
+  const double* chg_lb;
+  const double* chg_ub;
+  int8_t* out_cutoff;
+  int32_t* out_rounds;
+  int64_t* out_off;
+  int32_t* out_n;
+  int32_t* out_col;
+  double* out_lb;
+  double* out_ub;
+  int64_t out_cap;
+  unsigned long long* out_used;
+  int maxrounds;
+  int* next_item;
+  const int* order;
+  SeqSlots S;
+  unsigned long long* stats;     // rows, nnz, entries visited, changes, cutoffs, max rounds, live rows
+  int* status;                   // bit0 round limit, bit1 output overflow, bit2 a change column out of range
+};
+
+cudaError_t launchSeqCsc(cudaStream_t st, int grid, int64_t m, int64_t n, int64_t nnz, const int64_t* rowptr,
+                         const int32_t* colidx, const double* vals, int32_t* crow, double* cval);
+cudaError_t launchSeqPrepare(cudaStream_t st, int grid, const Num& s, const Prob& P, const double2* base, int* prep);
+cudaError_t launchNodesSeq(cudaStream_t st, int grid, const SeqArgs& A);
+cudaError_t nodesSeqOccupancy(int* blocksPerSm);
+
 // Node order for the queue: more branching changes first (a node's work grows with its changes), so that the
 // longest nodes start early and the batch does not end waiting for one of them.  Counting sort on the change
 // count (clamped to 255) in two launches; hist holds 2 * ORDER_BUCKETS zeroed ints (counts, cursors).

@@ -29,6 +29,7 @@ GBP_ERR_TOO_LARGE = -8
 GBP_FLAG_HOSTLOOP = 1
 GBP_FLAG_NOSORTVARS = 2
 GBP_FLAG_RANGEDROW = 4
+GBP_FLAG_SCIPORDER = 8
 
 # every symbol include/gbp.h declares (checked by the CPU test suite)
 EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "gbp_destroy", "gbp_default_params",
@@ -114,7 +115,9 @@ def load_library(path: Optional[str] = None):
 
 
 def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars: bool = True,
-                   ranged: bool = False) -> GbpParams:
+                   ranged: bool = False, scip_order: bool = False) -> GbpParams:
+    """gbp_default_params with the given changes; scip_order: batched nodes in SCIP's own order
+    (GBP_FLAG_SCIPORDER; rows must be uploaded in the order SCIP holds them, see instances.scip_row_order)."""
     p = GbpParams()
     load_library().gbp_default_params(ctypes.byref(p))
     if maxeasy is not None:
@@ -124,6 +127,8 @@ def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars
         p.flags |= GBP_FLAG_NOSORTVARS
     if ranged:
         p.flags |= GBP_FLAG_RANGEDROW
+    if scip_order:
+        p.flags |= GBP_FLAG_SCIPORDER
     return p
 
 

@@ -446,6 +446,32 @@ def scip_var_index(isint: np.ndarray, lb: np.ndarray, ub: np.ndarray) -> np.ndar
     return idx
 
 
+def scip_row_order(inst: "Instance", glb: np.ndarray, gub: np.ndarray,
+                   varidx: Optional[np.ndarray] = None) -> np.ndarray:
+    """The order SCIP sorts each row's entries into for propagation (cons_linear.c: consdataSort with
+    consdataCompVarProp), on the global domain glb/gub: binaries first (integral columns with the domain inside
+    [0, 1]) by decreasing |a|, then integers by decreasing |a| * (ub - lb), then continuous columns; ties by SCIP's
+    problem index (varidx, see scip_var_index; default the column).  Keys are compared exactly, where SCIP treats
+    values within 1e-9 as ties.  Returns CSR positions: order[p] for p in row i's range is the position of the
+    row's entry that comes at p; inst.colidx[order], inst.vals[order] is the CSR in that order, which the batched
+    node path's SCIP order (GBP_FLAG_SCIPORDER) expects."""
+    col = inst.colidx
+    vidx = np.arange(inst.n, dtype=np.int64) if varidx is None else np.asarray(varidx, dtype=np.int64)
+    isint = np.asarray(inst.isint) != 0
+    binary = isint & (glb >= 0.0) & (gub <= 1.0)
+    group = np.where(binary[col], 0, np.where(isint[col], 1, 2))
+    absa = np.abs(inst.vals)
+    key = np.where(group == 0, -absa, np.where(group == 1, -np.abs(inst.vals * (gub[col] - glb[col])), 0.0))
+    rows = np.repeat(np.arange(inst.m, dtype=np.int64), np.diff(inst.rowptr))
+    return np.lexsort((vidx[col], key, group, rows)).astype(np.int32)
+
+
+def in_order(inst: "Instance", order: np.ndarray) -> "Instance":
+    """The instance with each row's entries rearranged by order (CSR positions, as scip_row_order returns)."""
+    return Instance(inst.rowptr, inst.colidx[order], inst.vals[order], inst.lhs, inst.rhs, inst.lb, inst.ub,
+                    inst.isint, name=inst.name)
+
+
 def read_oracle_output(path: str):
     """Parse the oracle driver's output: (rootcutoff, rootlb, rootub, nodes) where nodes is a list of
     (cutoff, seconds, cols, lb, ub) with the columns whose bounds differ from the root fixpoint."""
