@@ -992,7 +992,10 @@ static int tightenBounds(Seq* q, int32_t i, RowSt* r)
    int nrounds;
    int64_t lastchange = -1;
 
-   /* canTightenBounds reads the counters as they are: before the first computation they are -1 */
+   /* canTightenBounds reads the counters as they are: at the root, before the first computation, they are -1 (the
+    * test passes); below the root SCIP's activities are always valid, computed here on first use */
+   if( !q->root )
+      ensureAct(q, i, r);
    if( r->valid )
    {
       const Act* a = &r->a;

@@ -258,11 +258,13 @@ def _read_order(inst, path):
 
 
 def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False, sortvars=True, fresh=False,
-             order=False):
+             order=False, unmark=False):
     """Run SCIP itself (oracle/_ref/scip_oracle) on the instance; returns the parsed output of
     scip_gb300.instances.read_oracle_output, plus (with order=True) SCIP's row order after the root as a CSR
     position array (order[p] for p in row i's range: the position of the row's k-th entry; rows deleted at the
-    root keep their storage order) and the mask of the rows the root deleted.  fresh: every node from a newly transformed problem (scip_driver.c --fresh)."""
+    root keep their storage order) and the mask of the rows the root deleted.  fresh: every node from a newly
+    transformed problem (scip_driver.c --fresh); unmark: nodes in one probing session, each without the marks a
+    cut-off node left (--unmark)."""
     from scip_gb300.instances import read_oracle_output
 
     if not os.path.exists(SCIP_ORACLE):
@@ -277,7 +279,7 @@ def run_scip(inst, nodes=None, easy=False, repeat=1, workdir=None, ranged=False,
             nodes.write(npth)
         cmd = ([SCIP_ORACLE, ip, npth, op] + (["--easy"] if easy else []) + (["--ranged"] if ranged else [])
                + ([] if sortvars else ["--nosort"]) + ["--repeat", str(repeat)] + (["--fresh"] if fresh else [])
-               + (["--order", os.path.join(d, "order.bin")] if order else []))
+               + (["--order", os.path.join(d, "order.bin")] if order else []) + (["--unmark"] if unmark else []))
         subprocess.run(cmd, check=True, capture_output=True)
         if order:
             return read_oracle_output(op) + _read_order(inst, os.path.join(d, "order.bin"))

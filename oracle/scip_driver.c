@@ -3,7 +3,7 @@
  * (oracle/linprop_oracle.c) and the CUDA path against the reference itself.
  *
  * Usage:  scip_oracle <instance.bin> <nodes.bin|-> <out.bin> [--easy] [--ranged] [--nosort] [--repeat R]
- *                      [--fresh] [--order order.bin]
+ *                      [--fresh] [--order order.bin] [--unmark]
  *
  * Pattern (the probing-in-heuristic recipe; see src/scip/scip_probing.c:120-690 and
  * tests/include/scip_test.c:121-133 for the interrupt idiom):
@@ -24,6 +24,8 @@
  *   - --fresh: every node starts from a newly transformed problem (SCIPfreeTransform, then the root again), so a
  *     node's result does not depend on the nodes before it (SCIP keeps activities, which drift under incremental
  *     updates, marks left by a cut-off node, and per-row flags across the nodes of one probing session);
+ *   - --unmark: before each node (in one probing session), unmark the linear rows a cut-off node left marked, so
+ *     that every node starts from the root's marks (none) -- the part of --fresh that is cheap for large problems;
  *   - --order: after the (first) root, each row's variables in the order SCIP holds them (SCIPgetVarsLinear on the
  *     transformed constraint), the order the next propagation visits them in: int64 m, then per row int32 len and
  *     int32 columns[len] (len = -1 for a row deleted at the root).
@@ -76,6 +78,7 @@ typedef struct
    double* rootlb;
    double* rootub;
    const char* orderpath;
+   int unmark;
 } Run;
 
 static void die(const char* msg)
@@ -231,6 +234,17 @@ static SCIP_DECL_HEUREXEC(heurExecOracle)
       double best = 1e300;
       int rep;
 
+      if( run->unmark )
+      {
+         /* rows a cut-off node left marked for propagation (its loop stopped before reaching them) */
+         SCIP_CONSHDLR* lin = SCIPfindConshdlr(scip, "linear");
+         SCIP_CONS** lc = SCIPconshdlrGetConss(lin);
+         int nlc = SCIPconshdlrGetNConss(lin);
+         int c;
+         for( c = 0; c < nlc; ++c )
+            if( SCIPconsIsMarkedPropagate(lc[c]) )
+               SCIP_CALL( SCIPunmarkConsPropagate(scip, lc[c]) );
+      }
       for( rep = 0; rep < run->repeat; ++rep )
       {
          int64_t q;
@@ -340,7 +354,7 @@ static SCIP_RETCODE setParams(SCIP* scip, int easy, int ranged, int nosort)
 }
 
 static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* outpath, int easy, int ranged,
-   int nosort, int repeat, int fresh, const char* orderpath)
+   int nosort, int repeat, int fresh, const char* orderpath, int unmark)
 {
    SCIP* scip = NULL;
    Inst in;
@@ -363,6 +377,7 @@ static SCIP_RETCODE run(const char* instpath, const char* nodepath, const char* 
    r.inst = &in;
    r.repeat = repeat;
    r.orderpath = orderpath;
+   r.unmark = unmark;
    r.k0 = 0;
    r.k1 = fresh ? (in.nnodes > 0 ? 1 : 0) : in.nnodes;
    r.rootlb = malloc(sizeof(double) * (size_t)(in.n + 1));
@@ -455,12 +470,13 @@ int main(int argc, char** argv)
    int repeat = 1;
    int fresh = 0;
    const char* orderpath = NULL;
+   int unmark = 0;
    int a;
    SCIP_RETCODE rc;
    if( argc < 4 )
    {
       fprintf(stderr, "usage: %s instance.bin nodes.bin|- out.bin [--easy] [--ranged] [--nosort] [--repeat R] [--fresh]"
-         " [--order order.bin]\n", argv[0]);
+         " [--order order.bin] [--unmark]\n", argv[0]);
       return 2;
    }
    for( a = 4; a < argc; ++a )
@@ -477,10 +493,12 @@ int main(int argc, char** argv)
          fresh = 1;
       else if( strcmp(argv[a], "--order") == 0 && a + 1 < argc )
          orderpath = argv[++a];
+      else if( strcmp(argv[a], "--unmark") == 0 )
+         unmark = 1;
    }
    if( repeat < 1 )
       repeat = 1;
-   rc = run(argv[1], argv[2], argv[3], easy, ranged, nosort, repeat, fresh, orderpath);
+   rc = run(argv[1], argv[2], argv[3], easy, ranged, nosort, repeat, fresh, orderpath, unmark);
    if( rc != SCIP_OKAY )
    {
       fprintf(stderr, "scip_oracle: SCIP error %d\n", (int)rc);

@@ -15,6 +15,11 @@ propagated before it.  Cases:
   set_cover / knapsack / network   one small instance of each uneven-batch family + 100 nodes
   indicator_packing          2,000 x 4,000 binary packing rows with an indicator (3 % of rows 65..300 long)
                              + 300 nodes: SCIP's binary skip in tightenBounds decides many of them
+  workload/node_workload_scip  the batched-node benchmark workload itself (200,000 x 400,000, seed 2) and its 4,096
+                             nodes (seed 3, drawn from SCIP's root): SCIP's node results in full, its root bounds and
+                             row orders as SHA-256 digests (the test recomputes them with the oracle, whose root is
+                             checked against the digests); nodes in one probing session with the marks of cut-off
+                             nodes cleared (scip_driver.c --unmark), which equals --fresh on every fixture above
   ranged/gcd_rows_indep      3,000 ranged rows over 60,000 columns (rows rarely share a column; 5 % of rows
                              65..200 long) whose integer part shares a divisor: SCIP's root with ranged-row
                              propagation on (rangedrowartcons off), sortvars off and on
@@ -131,6 +136,39 @@ def save_tiny_cutoffs():
     print(f"{path}: {len(insts)} instances, {int(out['sort_cut'].sum())} infeasible (sortvars)")
 
 
+def digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        if a.dtype.kind == "f":
+            a = a + 0.0  # -0.0 and +0.0 are the same bound (SCIP reports some zero bounds as -0.0)
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def save_node_workload():
+    inst = instances.node_mip(seed=2)
+    rcut, rlb, rub, _, order, rowdel = oracle.run_scip(inst, order=True)
+    assert not rcut
+    nodes = instances.node_batch(inst, rlb, rub, 4096, seed=3)
+    _, rlb2, rub2, res = oracle.run_scip(inst, nodes, unmark=True)
+    assert np.array_equal(rlb2, rlb) and np.array_equal(rub2, rub)
+    cut, ptr, col, lb, ub = node_arrays(res)
+    live = ~np.repeat(rowdel, np.diff(inst.rowptr))
+    out = {"instance_sha256": digest(inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, inst.lb, inst.ub,
+                                     inst.isint),
+           "root_sha256": digest(rlb, rub), "order_sha256": digest(order[live]),
+           "rowdel": np.nonzero(rowdel)[0].astype(np.int32),
+           "nodes_sha256": digest(nodes.ptr, nodes.col, nodes.lb, nodes.ub),
+           "res_ncut": cut, "res_nptr": ptr, "res_ncol": col, "res_nlb": lb, "res_nub": ub}
+    os.makedirs(os.path.join(HERE, "workload"), exist_ok=True)
+    path = os.path.join(HERE, "workload", "node_workload_scip.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {nodes.nnodes} nodes ({int(cut.sum())} cut off), "
+          f"{os.path.getsize(path) // 1024} KiB")
+
+
 def ranged_cases():
     return {
         "gcd_rows_indep": lambda: instances.gcd_rows(np.random.default_rng(np.random.PCG64(30)), 3000, 60000,
@@ -169,7 +207,11 @@ def main(names):
         raise SystemExit("oracle/_ref/scip_oracle missing: run `make -C oracle ref` where the SCIP sources are")
     all_cases = cases()
     ranged = ranged_cases()
-    for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs"]:
+    for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs",
+                                                                             "node_workload_scip"]:
+        if name == "node_workload_scip":
+            save_node_workload()
+            continue
         if name == "ranged/tiny_cutoffs":
             save_tiny_cutoffs()
             continue

@@ -17,8 +17,44 @@ REL_TOL = 1e-9
 ABS_TOL = 1e-6
 
 
+def _digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        if a.dtype.kind == "f":
+            a = a + 0.0  # -0.0 and +0.0 are the same bound (SCIP reports some zero bounds as -0.0)
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def load_node_workload(oracle_mod):
+    """The batched-node benchmark workload (200,000 x 400,000, 4,096 nodes) with SCIP's results
+    (golden/workload/node_workload_scip.npz).  The instance is regenerated from its seed and checked against the
+    fixture's digest; SCIP's root bounds and row orders come from the oracle's restatement of SCIP's order, checked
+    against the digests of SCIP's own.  Returns (inst, rows in SCIP's order, root lb, root ub, nodes, fixture)."""
+    from scip_gb300 import instances
+
+    with np.load(os.path.join(GOLDEN, "workload", "node_workload_scip.npz")) as f:
+        z = dict(f)  # an archive's arrays are decompressed on every access: read them once
+    inst = instances.node_mip(seed=2)
+    assert _digest(inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, inst.lb, inst.ub,
+                   inst.isint) == str(z["instance_sha256"]), "the regenerated instance differs from the fixture's"
+    vidx = instances.scip_var_index(inst.isint, inst.lb, inst.ub)
+    lb, ub, r, order = oracle_mod.Oracle(inst, vidx).propagate_seq(inst.lb, inst.ub, oracle_mod.params(0.0))
+    assert not r.cutoff and _digest(lb, ub) == str(z["root_sha256"]), "root bounds differ from SCIP's"
+    deleted = np.zeros(inst.m, dtype=bool)
+    deleted[z["rowdel"]] = True
+    live = ~np.repeat(deleted, np.diff(inst.rowptr))
+    assert _digest(order[live]) == str(z["order_sha256"]), "row orders differ from SCIP's"
+    nodes = instances.node_batch(inst, lb, ub, 4096, seed=3)
+    assert _digest(nodes.ptr, nodes.col, nodes.lb, nodes.ub) == str(z["nodes_sha256"])
+    return inst, instances.in_order(inst, order), lb, ub, nodes, z
+
+
 def load(name):
-    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as f:
+        z = dict(f)  # an archive's arrays are decompressed on every access: read them once
     inst = Instance(z["rowptr"], z["colidx"], z["vals"], z["lhs"], z["rhs"], z["lb"], z["ub"], z["isint"], name=name)
     return inst, z
 
@@ -27,6 +63,15 @@ def nodes_of(z):
     if "node_ptr" not in z:
         return None
     return NodeBatch(z["node_ptr"], z["node_col"], z["node_lb"], z["node_ub"])
+
+
+def scip_node_sparse(z, tag, k):
+    """SCIP's changed columns of node k as (cols, lb, ub), or None if cut off."""
+    if z[f"{tag}_ncut"][k]:
+        return None
+    p = z[f"{tag}_nptr"]
+    sl = slice(p[k], p[k + 1])
+    return z[f"{tag}_ncol"][sl], z[f"{tag}_nlb"][sl], z[f"{tag}_nub"][sl]
 
 
 def scip_node(z, tag, k, rlb, rub):
@@ -49,6 +94,20 @@ class Agreement:
     int_cols_diff: int = 0
     cont_cols: int = 0
     cont_cols_out_of_tol: int = 0
+
+    def add_sparse(self, isint, rlb, rub, a, b):
+        """add() for results given as the columns that differ from the base (cols, lb, ub), or None for cutoff: only
+        the columns either side changed are compared (the rest equal the base on both sides)."""
+        if a is None or b is None:
+            self.add(isint, a, b)
+            return
+        cols = np.union1d(a[0], b[0])
+        al, au = rlb[cols].copy(), rub[cols].copy()
+        bl, bu = al.copy(), au.copy()
+        ia, ib = np.searchsorted(cols, a[0]), np.searchsorted(cols, b[0])
+        al[ia], au[ia] = a[1], a[2]
+        bl[ib], bu[ib] = b[1], b[2]
+        self.add(isint[cols], (al, au), (bl, bu))
 
     def add(self, isint, a, b):
         """a, b: (lb, ub) of ours and SCIP's, or None for cutoff."""

@@ -63,6 +63,24 @@ def test_nodes_in_scip_order_agree_with_scip(oracle_mod, case, tag):
     assert agree.cont_cols_out_of_tol == 0, "continuous bounds outside tolerance"
 
 
+def test_node_workload_in_scip_order_agrees_with_scip(oracle_mod):
+    """The batched-node benchmark workload itself: the oracle's root equals SCIP's bit for bit (digest), each row
+    ends in SCIP's order, and on all 4,096 nodes cutoff verdicts and integer bounds equal SCIP's, continuous bounds
+    within tolerance."""
+    import os
+
+    inst, ordered, rlb, rub, nodes, z = G.load_node_workload(oracle_mod)
+    out = oracle_mod.Oracle(ordered).propagate_nodes(rlb, rub, nodes, _par(oracle_mod, "res"), cap=1024,
+                                                     nthreads=os.cpu_count() or 1, seq=True)
+    agree = G.Agreement()
+    for k in range(nodes.nnodes):
+        n = out["n"][k]
+        mine = None if out["cutoff"][k] else (out["col"][k, :n], out["lb"][k, :n], out["ub"][k, :n])
+        agree.add_sparse(inst.isint, rlb, rub, mine, G.scip_node_sparse(z, "res", k))
+    assert agree.problems == 4096 and agree.cutoff_mismatch == 0
+    assert agree.int_exact == agree.problems and agree.cont_cols_out_of_tol == 0
+
+
 def test_scip_variable_index():
     """SCIP groups a problem's variables by type and makes room for an inserted one by moving the first variable of
     each later group to that group's end (prob.c probProvidePos); a [0,1] integer column is a binary variable."""

@@ -84,6 +84,24 @@ def test_nodes_in_scip_order_from_a_fresh_sort(gpu_prop, oracle_mod, case, sortv
     _assert_equal_nodes(r, o, nb.nnodes, case)
 
 
+def test_node_workload_in_scip_order(gpu_prop, oracle_mod):
+    """The batched-node benchmark workload (200,000 x 400,000, all 4,096 nodes) in SCIP's order: equal to the oracle
+    bit for bit, and to SCIP's own results within the exact contract."""
+    import os
+
+    inst, ordered, rlb, rub, nodes, z = G.load_node_workload(oracle_mod)
+    gpu_prop.set_params(_params(0.0))
+    gpu_prop.upload(ordered)
+    r = gpu_prop.propagate_nodes(rlb, rub, nodes, out_cap=4096 * 256)
+    o = oracle_mod.Oracle(ordered).propagate_nodes(rlb, rub, nodes, oracle_mod.params(0.0), cap=1024,
+                                                   nthreads=os.cpu_count() or 1, seq=True)
+    _assert_equal_nodes(r, o, nodes.nnodes, "node workload")
+    agree = G.Agreement()
+    for k in range(nodes.nnodes):
+        agree.add_sparse(inst.isint, rlb, rub, None if r.cutoff[k] else r.node(k), G.scip_node_sparse(z, "res", k))
+    assert agree.cutoff_mismatch == 0 and agree.int_exact == agree.problems and agree.cont_cols_out_of_tol == 0
+
+
 def test_scip_order_edge_cases(gpu_prop, oracle_mod):
     inst, z = G.load("root_mip_s0")
     ordered = _scip_ordered(z, inst, "res")
