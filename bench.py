@@ -332,6 +332,58 @@ def serving_workload(args):
                       "mean_batch": float(np.mean([b[1] for b in batches])) if batches else 0.0}))
 
 
+def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world):
+    """Node-fixpoints/s of the batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER) on the same workload: the rows
+    in the order consdataCompVarProp sorts them into on the base bounds, inputs resident in HBM, CUDA events around
+    each step, the L2 flushed between steps."""
+    import torch
+    from scip_gb300 import gbp, instances
+
+    if args.ranged:
+        return None
+    order = instances.scip_row_order(inst, rlb, rub, instances.scip_var_index(inst.isint, inst.lb, inst.ub))
+    p = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy, scip_order=True))
+    p.upload(instances.in_order(inst, order))
+    d = torch.device("cuda", dev)
+    t = {k: torch.from_numpy(v).to(d) for k, v in (("lb", rlb), ("ub", rub), ("ptr", nodes.ptr), ("col", nodes.col),
+                                                 ("nlb", nodes.lb), ("nub", nodes.ub))}
+    cap = 256 * N
+    out = {"cutoff": torch.zeros(N, dtype=torch.int8, device=d), "rounds": torch.zeros(N, dtype=torch.int32, device=d),
+           "off": torch.zeros(N, dtype=torch.int64, device=d), "n": torch.zeros(N, dtype=torch.int32, device=d),
+           "col": torch.zeros(cap, dtype=torch.int32, device=d), "lb": torch.zeros(cap, dtype=torch.float64, device=d),
+           "ub": torch.zeros(cap, dtype=torch.float64, device=d)}
+    stream = torch.cuda.ExternalStream(p.stream())
+
+    def step():
+        return p.propagate_nodes_device(t["lb"], t["ub"], N, t["ptr"], t["col"], t["nlb"], t["nub"], out, cap)
+
+    for _ in range(args.warmup):
+        step()
+    steps = max(3, min(args.steps, 50))
+    evs, stats = [], []
+    torch.cuda.synchronize()
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        res = step()
+        e1.record(stream)
+        evs.append((e0, e1))
+        stats.append(res.asdict())
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    p.close()
+    st = stats[-1]
+    return {"value": world * N / (ms / 1e3), "unit": "node-fixpoints/s", "ms_per_step": ms, "steps": steps,
+            "kernel_ms": float(np.mean([x["kernel_ms"] for x in stats])), "rows_processed": st["rows"],
+            "entries_visited": st["candidates"], "changes": st["changes"], "nodes_cut_off": st["cutoff"],
+            "max_rounds": st["rounds"], "gpu_launches": int(sum(x["launches"] for x in stats)),
+            "call": "gbp_propagate_nodes_device with GBP_FLAG_SCIPORDER (SCIP's own order; integer bounds and "
+                    "cutoffs equal SCIP's)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -498,6 +550,10 @@ def main():
     cutoffs = stats[-1]["cutoff"]
     traffic, traffic_src = measured_traffic(N, shape) if args.family == "mip" and not args.ranged else (None, None)
 
+    # the same nodes in SCIP's own order (GBP_FLAG_SCIPORDER): rows uploaded in the order SCIP sorts them into on the
+    # base domain, device-resident inputs, the same timing
+    scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world)
+
     # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
     h_lb, h_ub = pin(rlb), pin(rub)
@@ -568,6 +624,7 @@ def main():
                              "call": "gbp_propagate_changes (bounds resident, changed columns only)"},
             "plain": {"value": plain_v, "unit": "node-fixpoints/s", "sample_nodes": plain_nodes,
                       "root_ms": rres.kernel_ms, "root_rounds": rres.rounds},
+            "scip_order": scip_order,
             }
     if rank == 0:
         if not args.quick:

@@ -200,8 +200,9 @@ int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const
 
 /* ---------------------------------------------------------------- batched path: branch-and-bound nodes
  * nnodes nodes share the uploaded rows and the base bounds baselb/baseub (length n); node k applies the
- * bound changes chg_col/chg_lb/chg_ub[ptr[k] .. ptr[k+1]) (tightenings, as SCIPchgVarLb/UbProbing; a column
- * appears at most once per node) and propagates to its own fixpoint -- the per-node work SCIP does in
+ * bound changes chg_col/chg_lb/chg_ub[ptr[k] .. ptr[k+1]) (tightenings, as SCIPchgVarLb/UbProbing; a column named
+ * more than once in a node takes the tightest of its bounds, and a node whose bounds for a column cross is cut off)
+ * and propagates to its own fixpoint -- the per-node work SCIP does in
  * SCIPpropagateProbing (src/scip/scip_probing.c:581) or at each branch-and-bound node.  All nodes run in one
  * persistent launch.  Per node: out_cutoff[k], out_rounds[k] and the columns whose final bounds differ from
  * the base: out_n[k] entries at out_col/out_lb/out_ub[out_off[k] ..].  Node results are packed in completion
@@ -227,9 +228,11 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * No counterpart in the reference: an addition for callers that cannot let a library allocate device memory
  * -- applications that give all device memory to their own pool allocator at start-up, and callers that must
  * not trigger the implicit device-wide synchronisation of cudaMalloc/cudaFree (for example a propagation
- * callback running while other streams of the host application are busy).  It computes exactly what
- * gbp_propagate_nodes_device computes, without a context: every array argument is a device pointer supplied
- * by the caller (the rows in CSR and plain CSC form: colptr[n+1], rowidx[nnz], cvals[nnz]), and the scratch
+ * callback running while other streams of the host application are busy).  It computes what
+ * gbp_propagate_nodes_device computes in rounds (GBP_FLAG_SCIPORDER and GBP_FLAG_RANGEDROW are refused with
+ * GBP_ERR_INVALID; the binary test of sortvars reads the base bounds, as the batched path does), without a context:
+ * every array argument is a device pointer supplied by the caller (the rows in CSR and plain CSC form:
+ * colptr[n+1], rowidx[nnz], cvals[nnz]; the arrays must hold the entries their pointers describe), and the scratch
  * is one fixed __device__ array of GBP_NOALLOC_SCRATCH_BYTES inside libgbp that every GPU loading the library
  * holds until exit.  The call allocates nothing (no cudaMalloc, cudaFree or allocating library routine).
  * Limits: one node slot needs about 64*n + 12*m bytes; the call uses as many slots as fit (at most one per
@@ -237,10 +240,14 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * only problems far below that limit run with useful parallelism.
  * The first call on a device (with that device current) looks up the array's address; make it before any
  * stream capture.  All calls on a device share the array, so calls that overlap on the GPU race and must be
- * serialised by the caller.  stream: a cudaStream_t or NULL.  With res == NULL the call only enqueues work
- * (an overfull output shows as out_n[k] = -1); with res != NULL it waits for the stream, fills res and
- * returns GBP_ERR_LIMIT / GBP_ERR_OVERFLOW like gbp_propagate_nodes_device.  params == NULL uses the defaults
- * of gbp_default_params. */
+ * serialised by the caller.  Before any node runs, two kernels check the pointers (starting at 0, monotone, the same
+ * number of entries) and the indices (columns in [0, n), rows in [0, m)); if a check fails no node runs, every
+ * node reports out_n[k] = -1 and the call returns GBP_ERR_INVALID.  stream: a cudaStream_t or NULL.  With
+ * res == NULL the call only enqueues work and returns GBP_OK: the outputs are then the only report (a node that
+ * did not fit the output or whose arrays failed the checks shows out_n[k] = -1; a node with a change column outside
+ * [0, n) shows out_cutoff[k] = 1; a node stopped at the round limit holds valid bounds); with res != NULL it waits
+ * for the stream, fills res and returns GBP_ERR_INVALID / GBP_ERR_LIMIT / GBP_ERR_OVERFLOW like
+ * gbp_propagate_nodes_device.  params == NULL uses the defaults of gbp_default_params. */
 #define GBP_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
    const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const int64_t* colptr,

@@ -1286,11 +1286,12 @@ static void* nodeWorker(void* arg)
          double nl = J->chg_lb[q];
          double nu = J->chg_ub[q];
          double l0 = lb[j], u0 = ub[j];
-         if( nl > u0 || nu < l0 )
+         if( nl > u0 || nu < l0 || nl > nu )
             cut = 1;
          else
          {
-            /* branching bound changes tighten only (SCIPchgVarLb/UbProbing semantics) */
+            /* branching bound changes tighten only (SCIPchgVarLb/UbProbing semantics); a column named again
+             * tightens further, and its bounds crossing cuts the node off */
             if( nl > l0 || nu < u0 )
             {
                markDirty(&w, j, l0, u0);
@@ -1298,6 +1299,8 @@ static void* nodeWorker(void* arg)
                   lb[j] = nl;
                if( nu < u0 )
                   ub[j] = nu;
+               if( lb[j] > ub[j] )
+                  cut = 1;
             }
          }
       }

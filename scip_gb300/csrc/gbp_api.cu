@@ -1655,6 +1655,7 @@ int gbp_propagate_nodes_device(gbp_ctx* ctx, const double* baselb, const double*
   A.stats = ctx->d_stats;
   A.status = ctx->d_status;
   A.minblocks = ctx->ctas_per_sm;
+  A.abort_flag = nullptr;  // uploads checked the rows and columns
   const int grid = (int)std::min<int64_t>(ctx->nslots, nnodes);
   CK(launchNodes(ctx->stream, grid, ctx->node_threads, A));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -91,6 +91,7 @@ struct NodesArgs {
   unsigned long long* stats;     // rows, nnz, candidates, changes, cutoffs, max rounds
   int* status;                   // bit0 round limit, bit1 output overflow, bit2 a change column out of range
   int minblocks;                 // register-budget variant of the kernel (1 = unconstrained)
+  const int* abort_flag;         // null, or a status word whose bit 3 (set by an input check) means: run no node
 };
 
 

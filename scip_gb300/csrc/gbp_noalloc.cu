@@ -11,10 +11,19 @@
 // an allocating library routine.
 //
 // Set-up: the first call on a device (with that device current) looks up the array's device address with
-// cudaGetSymbolAddress and caches it; make that first call before any stream capture.
+// cudaGetSymbolAddress and caches it together with the device's current driver context; make that first call
+// before any stream capture.  A later call in another context of the device (after a cudaDeviceReset, whose new
+// primary context maps the array elsewhere) looks the address up again.
+// Input checks: the caller's arrays are device memory the library cannot check on the host, so two kernels check
+// them first (row and column pointers start at 0, never decrease and describe the same number of entries; every
+// column index lies in [0, n), every row index in [0, m)) and set a bit in the scratch header; when it is set no
+// node runs, every node reports out_n[k] = -1, and the call returns GBP_ERR_INVALID (with res) -- never a read out
+// of bounds.  The arrays must hold the entries their pointers describe: rowptr[m] column indices and values,
+// colptr[n] row indices and values.
 // Sharing: every call on a device uses the same array and leaves its contents behind; each call clears what
 // must start at zero before it launches.  Calls whose work overlaps on the GPU (two streams, two host
 // threads) race on the array and must be serialised by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +42,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[GBP_NOALLOC_SCR
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
+CUcontext g_scratch_ctx[kMaxDevices] = {nullptr};  // the driver context the cached address belongs to
 
 // header at the start of the array: work-queue head, status bits, packed-output counter, statistics
 struct Header {
@@ -49,16 +59,55 @@ constexpr int kBudget = 4;  // compiled variant: 128 threads per node, 4 residen
 int scratchAddress(int device, void** out) {
   if (device < 0 || device >= kMaxDevices) return GBP_ERR_NODEVICE;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_ptr[device] == nullptr) {
+  // the driver's cuCtxGetCurrent through the runtime (libgbp links no driver library)
+  static CUresult (*ctxGetCurrent)(CUcontext*) = nullptr;
+  if (ctxGetCurrent == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || fn == nullptr) {
+      cudaGetLastError();
+      return GBP_ERR_CUDA;
+    }
+    ctxGetCurrent = (CUresult(*)(CUcontext*))fn;
+  }
+  // before the runtime has made a context current, cuCtxGetCurrent reports none: the lookup below then
+  // initialises the device's primary context
+  CUcontext cur = nullptr;
+  if (ctxGetCurrent(&cur) != CUDA_SUCCESS) cur = nullptr;
+  if (g_scratch_ptr[device] == nullptr || cur == nullptr || g_scratch_ctx[device] != cur) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
       cudaGetLastError();
       return GBP_ERR_CUDA;
     }
+    if (ctxGetCurrent(&cur) != CUDA_SUCCESS || cur == nullptr) return GBP_ERR_CUDA;
     g_scratch_ptr[device] = p;
+    g_scratch_ctx[device] = cur;
   }
   *out = g_scratch_ptr[device];
   return GBP_OK;
+}
+
+// input checks (status bit 3): the pointer arrays first, reading only their m + 1 and n + 1 entries
+__global__ void k_check_pointers(int64_t m, int64_t n, const int64_t* rowptr, const int64_t* colptr, int* status) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t0 == 0 && (rowptr[0] != 0 || colptr[0] != 0 || rowptr[m] != colptr[n])) atomicOr(status, 8);
+  for (int64_t i = t0; i < m; i += stride)
+    if (rowptr[i + 1] < rowptr[i]) atomicOr(status, 8);
+  for (int64_t j = t0; j < n; j += stride)
+    if (colptr[j + 1] < colptr[j]) atomicOr(status, 8);
+}
+// then, when the pointers hold, the indices they describe
+__global__ void k_check_indices(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                                const int32_t* rowidx, int* status) {
+  if (*status & 8) return;
+  const int64_t nnz = rowptr[m];
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t j = colidx[p], i = rowidx[p];
+    if (j < 0 || j >= n || i < 0 || i >= m) atomicOr(status, 8);
+  }
 }
 
 }  // namespace
@@ -73,7 +122,8 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
                                            double* out_lb, double* out_ub, int64_t out_cap, const gbp_params* params,
                                            void* stream, gbp_result* res) {
   if (m < 0 || n < 0 || nnodes < 0 || out_cap < 0) return GBP_ERR_INVALID;
-  if (params && (params->flags & GBP_FLAG_RANGEDROW)) return GBP_ERR_INVALID;  // needs a context's row order
+  // ranged rows need a context's row order, and SCIP's own order the context's row-ordered column copy
+  if (params && (params->flags & (GBP_FLAG_RANGEDROW | GBP_FLAG_SCIPORDER))) return GBP_ERR_INVALID;
   if (m >= (int64_t(1) << 30) || n >= (int64_t(1) << 31) - 1 || nnodes >= (int64_t(1) << 31) - 1)
     return GBP_ERR_TOO_LARGE;
   if (nnodes == 0) {
@@ -164,6 +214,10 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   A.stats = hdr->stats;
   A.status = &hdr->status;
   A.minblocks = kBudget;
+  A.abort_flag = &hdr->status;
+  k_check_pointers<<<sms, 256, 0, st>>>(m, n, rowptr, colptr, &hdr->status);
+  k_check_indices<<<sms * 4, 256, 0, st>>>(m, n, rowptr, colidx, rowidx, &hdr->status);
+  if (cudaGetLastError() != cudaSuccess) return GBP_ERR_CUDA;
   if (launchNodes(st, (int)nslots, kThreads, A) != cudaSuccess) return GBP_ERR_CUDA;
   if (res == nullptr) return GBP_OK;
 
@@ -175,14 +229,16 @@ extern "C" int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* 
   res->cutoff = (int32_t)h.stats[4];
   res->rounds = (int32_t)h.stats[5];
   res->status = (h.status & 1) ? 2 : 0;
-  res->launches = orderhist != nullptr ? 8 : 6;
+  // kernels of the call: the four candidate-slot fills, the node order (two, when it fits), the two input
+  // checks and the node kernel (the context path fills its slots once, when it allocates them)
+  res->launches = orderhist != nullptr ? 9 : 7;
   res->rows = (int64_t)h.stats[0];
   res->nnz = (int64_t)h.stats[1];
   res->candidates = (int64_t)h.stats[2];
   res->changes = (int64_t)h.stats[3];
   res->live_rows = (int64_t)h.stats[6];
   res->kernel_ms = 0.0;
-  if (h.status & 4) return GBP_ERR_INVALID;
+  if (h.status & (4 | 8)) return GBP_ERR_INVALID;
   if (h.status & 2) return GBP_ERR_OVERFLOW;
   if (h.status & 1) return GBP_ERR_LIMIT;
   return GBP_OK;

@@ -129,6 +129,16 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
   C.round = 0;
   const int m = (int)A.P.m;
 
+  if (A.abort_flag != nullptr && (*A.abort_flag & 8)) {
+    // the caller's arrays failed the input checks: no node runs, each reports that its result was not written
+    for (int64_t k = (int64_t)blockIdx.x * NT + tid; k < A.nnodes; k += (int64_t)gridDim.x * NT) {
+      A.out_n[k] = -1;
+      A.out_off[k] = 0;
+      A.out_cutoff[k] = 0;
+      A.out_rounds[k] = 0;
+    }
+    return;
+  }
   int counter = 0;
   if (tid == 0) counter = S.counter[slot];
   Stats st{0, 0, 0, 0};
@@ -164,10 +174,21 @@ __global__ void __launch_bounds__(NT, MINB) k_nodes(NodesArgs A) {
           s_cut = 1;
           continue;
         }
+        // a column named more than once: its first occurrence applies them all (the tightest bounds), which is
+        // what applying them one after the other gives
+        const int64_t q0 = A.ptr[item], q1 = A.ptr[item + 1];
+        bool first = true;
+        for (int64_t r2 = q0; r2 < q && first; ++r2) first = A.chg_col[r2] != j;
+        if (!first) continue;
         double nl = A.chg_lb[q], nu = A.chg_ub[q];
+        for (int64_t r2 = q + 1; r2 < q1; ++r2)
+          if (A.chg_col[r2] == j) {
+            nl = fmax(nl, A.chg_lb[r2]);
+            nu = fmin(nu, A.chg_ub[r2]);
+          }
         double l0, u0;
         B.get(j, l0, u0);
-        if (nl > u0 || nu < l0) {
+        if (nl > u0 || nu < l0 || nl > nu) {
           s_cut = 1;
         } else if (nl > l0 || nu < u0) {
           ovlSet(B, dirty, &s_ndirty, j, nl > l0 ? nl : l0, nu < u0 ? nu : u0);

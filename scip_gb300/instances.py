@@ -101,6 +101,45 @@ class NodeBatch:
 
 
 # ----------------------------------------------------------------------------------------------
+# Seeded draws that every machine reproduces bit for bit: numpy's generators are exact, but its vectorised
+# exp / log round differently on different CPUs, so log-uniform values are built from exactly rounded operations only.
+_POW_TABLES = {}
+
+
+def _pow_tables(ratio: float):
+    """ratio^(i/2^10) and ratio^(j/2^20) for i, j in 0..1023, each the double nearest to the exact value (decimal
+    arithmetic at 40 digits, then one correctly rounded conversion)."""
+    if ratio not in _POW_TABLES:
+        import decimal
+
+        ctx = decimal.Context(prec=40)
+        r = decimal.Decimal(repr(ratio))
+        coarse = np.array([float(ctx.power(r, decimal.Decimal(i) / 1024)) for i in range(1024)])
+        fine = np.array([float(ctx.power(r, decimal.Decimal(j) / (1 << 20))) for j in range(1024)])
+        _POW_TABLES[ratio] = (coarse, fine)
+    return _POW_TABLES[ratio]
+
+
+def log_uniform(rng: np.random.Generator, lo: float, hi: float, size: int) -> np.ndarray:
+    """lo * (hi / lo)^u with u uniform on a grid of 2^20 steps in [0, 1): a product of two table entries, so the
+    same on every machine."""
+    coarse, fine = _pow_tables(hi / lo)
+    k = rng.integers(0, 1 << 20, size=size)
+    return lo * coarse[k >> 10] * fine[k & 1023]
+
+
+def log_uniform_count(rng: np.random.Generator, kmax: int, size: int) -> np.ndarray:
+    """floor((kmax + 1)^u) for u uniform in [0, 1), i.e. the number of j in 1..kmax with ln j / ln(kmax + 1) <= u;
+    the thresholds are exact decimal quotients rounded once, so the same on every machine."""
+    import decimal
+
+    ctx = decimal.Context(prec=40)
+    den = ctx.ln(decimal.Decimal(kmax + 1))
+    thr = np.array([float(ctx.divide(ctx.ln(decimal.Decimal(j)), den)) for j in range(1, kmax + 1)])
+    u = rng.random(size)
+    return np.searchsorted(thr, u, side="right").astype(np.int64)
+
+
 def _distinct_columns(rng: np.random.Generator, lengths: np.ndarray, n: int) -> np.ndarray:
     """Uniform columns per row without repeats inside a row (rows keep their sampling order)."""
     m = lengths.shape[0]
@@ -175,7 +214,7 @@ def _general_columns(rng, n):
 def _general_mip(rng, lengths, n, name):
     rowptr, colidx = _distinct_columns(rng, lengths, n)
     nnz = colidx.shape[0]
-    mag = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), size=nnz))
+    mag = log_uniform(rng, 1e-2, 1e2, nnz)
     vals = np.where(rng.random(nnz) < 0.5, -mag, mag)
     isint, lb, ub, x0 = _general_columns(rng, n)
     lhs, rhs = _sides_from_point(rng, rowptr, colidx, vals, x0, 0.85, 0.10, 5.0)
@@ -213,8 +252,7 @@ def node_batch(inst: Instance, lb: np.ndarray, ub: np.ndarray, nnodes: int, seed
     if intcols.shape[0] == 0:
         raise ValueError("no unfixed finite integer columns")
     kmax = min(kmax, intcols.shape[0])
-    ks = np.floor(np.exp(rng.uniform(0.0, np.log(kmax + 1), size=nnodes))).astype(np.int64)
-    ks = np.clip(ks, 1, kmax)
+    ks = log_uniform_count(rng, kmax, nnodes)
     ptr = np.zeros(nnodes + 1, dtype=np.int64)
     np.cumsum(ks, out=ptr[1:])
     cols = np.empty(int(ptr[-1]), dtype=np.int32)
@@ -366,7 +404,7 @@ def network_flow(rng: np.random.Generator, m: int) -> Instance:
 def uneven_batch(seed: int = 4, count: int = 512, rmin: int = 1000, rmax: int = 200_000) -> List[Instance]:
     """Distinct instances with log-uniform row counts; families cycle set cover / knapsack / network."""
     rng = np.random.default_rng(np.random.PCG64(seed))
-    rows = np.floor(np.exp(rng.uniform(np.log(rmin), np.log(rmax), size=count))).astype(np.int64)
+    rows = np.floor(log_uniform(rng, float(rmin), float(rmax), count)).astype(np.int64)
     out = []
     for k in range(count):
         m = int(rows[k])

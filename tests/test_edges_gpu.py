@@ -95,6 +95,53 @@ def test_degenerate_node_batches(gpu_prop, oracle_mod):
     assert r.cutoff[-1] == 1
 
 
+def _with_repeats(nodes, rlb, rub, rng):
+    """The batch with every node's changes named again (a second, looser or tighter change on the same column in
+    random order), plus nodes whose repeated changes cross."""
+    ptr, col, lb, ub = [0], [], [], []
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        c, l, u = list(nodes.col[sl]), list(nodes.lb[sl]), list(nodes.ub[sl])
+        for j in list(c):
+            lo, hi = rlb[j], rub[j]
+            c.append(j)
+            l.append(lo)   # a looser repeat: no effect
+            u.append(hi)
+        if k % 7 == 3 and c:
+            j = c[0]
+            c.append(j)     # a repeat that crosses the first: the node is cut off
+            l.append(min(rub[j], l[0] + 1.0) if l[0] < rub[j] else rlb[j])
+            u.append(min(rub[j], l[0] + 1.0) if l[0] < rub[j] else rlb[j])
+        perm = rng.permutation(len(c))
+        col += [c[i] for i in perm]
+        lb += [l[i] for i in perm]
+        ub += [u[i] for i in perm]
+        ptr.append(len(col))
+    return NodeBatch(np.array(ptr, np.int64), np.array(col, np.int32), np.array(lb), np.array(ub))
+
+
+@pytest.mark.parametrize("scip_order", [False, True])
+def test_node_changes_naming_a_column_twice(gpu_prop, oracle_mod, scip_order):
+    """A node may name a column more than once: the tightest bounds apply, and crossing bounds cut it off -- the
+    same as applying the changes one after the other, on the GPU and in the oracle, in both orders."""
+    inst = instances.root_mip(3)
+    par = oracle_mod.params(0.0)
+    orc = oracle_mod.Oracle(inst)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    if scip_order:
+        order = instances.scip_row_order(inst, rlb, rub, instances.scip_var_index(inst.isint, inst.lb, inst.ub))
+        inst = instances.in_order(inst, order)
+        orc = oracle_mod.Oracle(inst)
+    batch = _with_repeats(instances.node_batch(inst, rlb, rub, 60, seed=8), rlb, rub, np.random.default_rng(3))
+    gpu_prop.set_params(gbp.default_params(maxeasy=0.0, scip_order=scip_order))
+    gpu_prop.upload(inst)
+    r = gpu_prop.propagate_nodes(rlb, rub, batch)
+    o = orc.propagate_nodes(rlb, rub, batch, par, cap=inst.n, seq=scip_order)
+    _nodes_equal(r, o, batch.nnodes)
+    assert 0 < int(r.cutoff.sum()) < batch.nnodes
+    gpu_prop.set_params(gbp.default_params(maxeasy=0.0))
+
+
 @pytest.mark.parametrize("maxeasy", [0.0, 1e6])
 def test_bounds_at_the_huge_and_infinite_thresholds(gpu_prop, oracle_mod, maxeasy):
     """Bounds just below and at hugeval (1e15) and at infinity (1e20): the contributions move between the

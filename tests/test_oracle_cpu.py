@@ -139,3 +139,30 @@ def test_binary_test_uses_the_global_domain(oracle_mod):
     l1, _, _ = orc.propagate(lb, ub, oracle_mod.params(0.0), glob=(glb, wide))
     l2, _, _ = orc.propagate(lb, ub, oracle_mod.params(0.0), glob=(glb, ub))
     assert l1[3] == 1.0 and l2[3] == 0.0
+
+
+def test_node_changes_naming_a_column_twice(oracle_mod):
+    """A column named twice in a node takes the tightest bounds; crossing bounds cut the node off."""
+    from scip_gb300.instances import NodeBatch, root_mip
+
+    inst = root_mip(0, m=200, n=500)
+    par = oracle_mod.params(0.0)
+    orc = oracle_mod.Oracle(inst)
+    rlb, rub, _ = orc.propagate(inst.lb, inst.ub, par)
+    j = int(np.flatnonzero((inst.isint == 1) & (rub - rlb >= 4))[0])
+    lo = rlb[j]
+    once = NodeBatch(np.array([0, 1], np.int64), np.array([j], np.int32), np.array([lo + 1.0]), np.array([lo + 2.0]))
+    twice = NodeBatch(np.array([0, 2], np.int64), np.array([j, j], np.int32), np.array([lo, lo + 1.0]),
+                      np.array([lo + 2.0, lo + 3.0]))
+    crossing = NodeBatch(np.array([0, 2], np.int64), np.array([j, j], np.int32), np.array([lo, lo + 3.0]),
+                         np.array([lo + 1.0, lo + 3.0]))
+    for seq in (False, True):
+        a = orc.propagate_nodes(rlb, rub, once, par, cap=inst.n, seq=seq)
+        b = orc.propagate_nodes(rlb, rub, twice, par, cap=inst.n, seq=seq)
+        n = a["n"][0]
+        assert not a["cutoff"][0] and not b["cutoff"][0] and b["n"][0] == n
+        o1, o2 = np.argsort(a["col"][0, :n]), np.argsort(b["col"][0, :n])
+        assert np.array_equal(a["col"][0, :n][o1], b["col"][0, :n][o2])
+        assert np.array_equal(a["lb"][0, :n][o1], b["lb"][0, :n][o2])
+        assert np.array_equal(a["ub"][0, :n][o1], b["ub"][0, :n][o2])
+        assert orc.propagate_nodes(rlb, rub, crossing, par, cap=inst.n, seq=seq)["cutoff"][0] == 1

@@ -38,7 +38,7 @@ def _per_node(out):
     return nodes
 
 
-def test_noalloc_matches_context_entry_point():
+def test_noalloc_matches_context_entry_point(oracle_mod):
     torch = pytest.importorskip("torch")
     L = gbp.load_library()
     inst = instances.node_mip(seed=5, m=6000, n=12000)
@@ -65,6 +65,16 @@ def test_noalloc_matches_context_entry_point():
     torch.cuda.synchronize()
     expect = _per_node(ref)
     assert sum(e[0] for e in expect) < N
+    # the context entry point itself against the oracle
+    o = oracle_mod.Oracle(inst).propagate_nodes(rlb, rub, nodes, oracle_mod.params(0.0), cap=inst.n)
+    for k, e in enumerate(expect):
+        assert e[0] == o["cutoff"][k], f"node {k}: cutoff differs from the oracle"
+        if e[0]:
+            continue
+        n = o["n"][k]
+        srt = np.argsort(o["col"][k, :n])
+        assert np.array_equal(e[2], o["col"][k, :n][srt]), f"node {k}: changed columns differ from the oracle"
+        assert np.array_equal(e[3], o["lb"][k, :n][srt]) and np.array_equal(e[4], o["ub"][k, :n][srt])
 
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     for call in range(2):
@@ -88,6 +98,23 @@ def test_noalloc_matches_context_entry_point():
             assert np.array_equal(e[3], g[3]) and np.array_equal(e[4], g[4]), f"call {call}, node {k}: bounds differ"
         assert (res.rows, res.nnz, res.candidates, res.changes, res.cutoff) == \
                (rref.rows, rref.nnz, rref.candidates, rref.changes, rref.cutoff)
+        # kernels: four slot fills, the node order (two), two input checks, the nodes; the context path: the order
+        # (two), the base packing, the nodes
+        assert res.launches == 9 and rref.launches == 4
+
+    # a column index outside [0, n) in the caller's rows: the checks refuse the arrays before any node reads them
+    bad = A["colidx"].clone()
+    bad[5] = inst.n + 7
+    out = _outputs(torch, d, N, cap)
+    res = gbp.GbpResult()
+    rc = L.gbp_propagate_nodes_noalloc(inst.m, inst.n, p(A["rowptr"]), p(bad), p(A["vals"]), p(A["lhs"]),
+                                       p(A["rhs"]), p(A["isint"]), p(A["colptr"]), p(A["rowidx"]), p(A["cvals"]),
+                                       p(A["lb"]), p(A["ub"]), N, p(A["ptr"]), p(A["col"]), p(A["nlb"]), p(A["nub"]),
+                                       p(out["cutoff"]), p(out["rounds"]), p(out["off"]), p(out["n"]),
+                                       p(out["col"]), p(out["lb"]), p(out["ub"]), cap, ctypes.byref(params), None,
+                                       ctypes.byref(res))
+    assert rc == gbp.GBP_ERR_INVALID
+    assert bool((out["n"] == -1).all().item())
     prop.close()
 
 
