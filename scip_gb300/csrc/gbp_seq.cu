@@ -13,7 +13,9 @@
 //   - tightenBounds' visit of a row's entries: the lanes evaluate 32 consecutive entries without changing any
 //     state, and the first entry that would change something (a tightening, a cutoff, the recomputation of an
 //     activity) or ends the visit of the binaries is then run for real; the entries before it change nothing, so
-//     the outcome is the sequential one.
+//     the outcome is the sequential one.  The evaluation may also report an entry it cannot settle cheaply (an
+//     unreliable residual, which SCIP recomputes from scratch): running an entry that then changes nothing
+//     advances the visit exactly as skipping it does.
 // Per-node state lives in per-warp slots in HBM: a state record per row (stamped with the node's epoch, so a new
 // node needs no clearing), the column bounds that differ from the base, and the marked-row and update lists.
 //
@@ -103,7 +105,7 @@ __device__ __forceinline__ Act actOf(const SeqRow& r) {
 
 // ------------------------------------------------------------------------------------------ activities
 // calcActivities: every entry in the row's order through the counters or the compensated sum
-__device__ void calcActivities(const W& w, int i, SeqRow& r) {
+__device__ __noinline__ void calcActivities(const W& w, int i, SeqRow& r) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p0 = P.rowptr[i];
@@ -149,7 +151,7 @@ __device__ void calcActivities(const W& w, int i, SeqRow& r) {
 }
 
 // recomputeSide: the finite non-huge part of one side, last entry first
-__device__ void recomputeSide(const W& w, int i, SeqRow& r, bool ismin) {
+__device__ __noinline__ void recomputeSide(const W& w, int i, SeqRow& r, bool ismin) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p0 = P.rowptr[i];
@@ -245,7 +247,7 @@ __device__ __forceinline__ ResArgs resArgs(const Num& s, const SeqRow& r, double
 }
 
 // reliableRes: plain double sum in the row's order, skipping the column (uniform: lanes load, lane order sums)
-__device__ double reliableResWarp(const W& w, int i, int skipcol, bool ismin) {
+__device__ __noinline__ double reliableResWarp(const W& w, int i, int skipcol, bool ismin) {
   const Prob& P = w.A->P;
   const int64_t p0 = P.rowptr[i];
   const int len = (int)(P.rowptr[i + 1] - p0);
@@ -272,22 +274,8 @@ __device__ double reliableResWarp(const W& w, int i, int skipcol, bool ismin) {
   }
   return res;
 }
-// the same sum by one lane alone (speculative evaluation of an entry)
-__device__ double reliableResLane(const W& w, int i, int skipcol, bool ismin) {
-  const Prob& P = w.A->P;
-  double res = 0.0;
-  for (int64_t p = P.rowptr[i]; p < P.rowptr[i + 1]; ++p) {
-    const int j = P.colidx[p];
-    if (j == skipcol) continue;
-    const double v = P.vals[p];
-    const double2 b = bnd(w, j);
-    res += v > 0.0 ? (ismin ? v * b.x : v * b.y) : (ismin ? v * b.y : v * b.x);
-  }
-  return res;
-}
-
 // recomputeMaxDelta, last entry first (uniform)
-__device__ void recomputeMaxDelta(const W& w, int i, SeqRow& r) {
+__device__ __noinline__ void recomputeMaxDelta(const W& w, int i, SeqRow& r) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p0 = P.rowptr[i];
@@ -449,7 +437,7 @@ __device__ __forceinline__ void disableRow(W& w, int i, SeqRow& r) {
   addUpdate(w, i, r);
 }
 // conshdlrProcessUpdates: the delayed updates, the last added first (uniform)
-__device__ void processUpdates(W& w) {
+__device__ __noinline__ void processUpdates(W& w) {
   for (int k = w.nu - 1; k >= 0; --k) {
     const int i = w.U[k];
     SeqRow r = w.rs[i];
@@ -484,7 +472,7 @@ __device__ __forceinline__ void setBound(W& w, int j, double l, double u) {
 }
 
 // boundEvent: eventExecLinear for every row of column j, in row order (uniform; the lanes take the rows)
-__device__ void boundEvent(W& w, int j, bool islb, double oldb, double newb) {
+__device__ __noinline__ void boundEvent(W& w, int j, bool islb, double oldb, double newb) {
   const SeqArgs& A = *w.A;
   const Num& s = A.s;
   const int64_t q0 = A.ccolptr[j], q1 = A.ccolptr[j + 1];
@@ -537,7 +525,7 @@ __device__ void boundEvent(W& w, int j, bool islb, double oldb, double newb) {
 }
 
 // inferUb / inferLb (uniform); return true on infeasibility, *tightened when the bound moved
-__device__ bool inferUb(W& w, int j, double newub, bool force, bool& tightened) {
+__device__ __noinline__ bool inferUb(W& w, int j, double newub, bool force, bool& tightened) {
   const Num& s = w.A->s;
   const bool isint = w.A->P.isint[j] != 0;
   const double2 b = bnd(w, j);
@@ -554,7 +542,7 @@ __device__ bool inferUb(W& w, int j, double newub, bool force, bool& tightened) 
   tightened = true;
   return false;
 }
-__device__ bool inferLb(W& w, int j, double newlb, bool force, bool& tightened) {
+__device__ __noinline__ bool inferLb(W& w, int j, double newlb, bool force, bool& tightened) {
   const Num& s = w.A->s;
   const bool isint = w.A->P.isint[j] != 0;
   const double2 b = bnd(w, j);
@@ -617,24 +605,15 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newub = (rhs - minres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
-        bool unrel = updateUnreliable(s, minres, r.lastmin);
-        if (unrel) {
-          const double mr = reliableResLane(w, i, j, true);
-          newub = (rhs - mr) / val;
-          unrel = isInf(s, -mr) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
-        }
-        if (!unrel && wouldInferUb(s, isint, l, u, newub, force)) return true;
+        // an unreliable residual is recomputed from scratch: the entry counts as a hit, run for real
+        if (updateUnreliable(s, minres, r.lastmin)) return true;
+        if (wouldInferUb(s, isint, l, u, newub, force)) return true;
       }
     }
     if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newlb = (lhs - maxres) / val;
       if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
-        if (updateUnreliable(s, maxres, r.lastmax)) {
-          const double mr = reliableResLane(w, i, j, false);
-          newlb = (lhs - mr) / val;
-          if (isInf(s, mr) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l))))
-            return false;
-        }
+        if (updateUnreliable(s, maxres, r.lastmax)) return true;
         if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
       }
     }
@@ -642,25 +621,14 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newlb = (rhs - minres) / val;
       if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
-        bool unrel = updateUnreliable(s, minres, r.lastmin);
-        if (unrel) {
-          const double mr = reliableResLane(w, i, j, true);
-          newlb = (rhs - mr) / val;
-          unrel = isInf(s, -mr) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
-        }
-        if (!unrel && wouldInferLb(s, isint, l, u, newlb, force)) return true;
+        if (updateUnreliable(s, minres, r.lastmin)) return true;
+        if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
       }
     }
     if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newub = (lhs - maxres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
-        if (updateUnreliable(s, maxres, r.lastmax)) {
-          const double mr = reliableResLane(w, i, j, false);
-          newub = (lhs - mr) / val;
-          // cons_linear.c:6936 joins the middle condition with && where the other three branches use ||
-          if (isInf(s, mr) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) && !isint) && (!force || !lt(s, newub, u))))
-            return false;
-        }
+        if (updateUnreliable(s, maxres, r.lastmax)) return true;
         if (wouldInferUb(s, isint, l, u, newub, force)) return true;
       }
     }
@@ -669,7 +637,7 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
 }
 
 // tightenVarBounds, run for real (uniform); returns true on cutoff.  r is reloaded after every change.
-__device__ bool residualRun(W& w, int i, SeqRow& r, int k, bool force) {
+__device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool force) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p = P.rowptr[i] + k;
@@ -830,7 +798,7 @@ __device__ __forceinline__ bool easyLb(W& w, int j, double newlb, double oldlb, 
 }
 
 // tightenVarBoundsEasy, run for real (uniform); returns true on cutoff
-__device__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) {
+__device__ __noinline__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p = P.rowptr[i] + k;
@@ -902,9 +870,153 @@ __device__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) {
   return false;
 }
 
+// ------------------------------------------------------------------------------------------ one row, one lane
+// Most marked rows never reach tightenBounds' visit of their entries: SCIP's own tests (a tightened row, a largest
+// activity delta within the slack) end them after a few activity computations.  The lanes run those computations
+// for 32 consecutive rows of a call at once, each on a private copy of its row's record; a row that changes no bound
+// changes nothing but its own record, so the rows before the first one that changes a bound end exactly as running
+// them one after the other leaves them.  Every function restates its counterpart of oracle/linprop_seq.c step for
+// step, one lane alone.
+
+__device__ __noinline__ void laneCalc(const W& w, int i, SeqRow& r) {  // calcActivities
+  const Prob& P = w.A->P;
+  Act a;
+  actZero(a);
+  for (int64_t p = P.rowptr[i]; p < P.rowptr[i + 1]; ++p) {
+    const double2 b = bnd(w, P.colidx[p]);
+    addTerm(w.A->s, a, P.vals[p], b.x, b.y);
+  }
+  r.minhi = a.minhi; r.minlo = a.minlo; r.maxhi = a.maxhi; r.maxlo = a.maxlo;
+  r.minposinf = a.minposinf; r.minneginf = a.minneginf; r.minposhuge = a.minposhuge; r.minneghuge = a.minneghuge;
+  r.maxposinf = a.maxposinf; r.maxneginf = a.maxneginf; r.maxposhuge = a.maxposhuge; r.maxneghuge = a.maxneghuge;
+  r.flags |= RS_VALID | RS_VMIN | RS_VMAX;
+  r.lastmin = r.minhi + r.minlo;
+  r.lastmax = r.maxhi + r.maxlo;
+}
+
+__device__ __noinline__ void laneRecompute(const W& w, int i, SeqRow& r, bool ismin) {  // recomputeSide
+  const Prob& P = w.A->P;
+  const Num& s = w.A->s;
+  double hi = 0.0, lo = 0.0;
+  for (int64_t p = P.rowptr[i + 1] - 1; p >= P.rowptr[i]; --p) {
+    const double v = P.vals[p];
+    const double2 b = bnd(w, P.colidx[p]);
+    const double bb = (v > 0.0) == ismin ? b.x : b.y;
+    if (!isInf(s, bb) && !isInf(s, -bb) && !isHuge(s, v * bb) && !isHuge(s, -v * bb)) sum21(hi, lo, v * bb);
+  }
+  if (ismin) {
+    r.minhi = hi; r.minlo = lo; r.flags |= RS_VMIN; r.lastmin = hi + lo;
+  } else {
+    r.maxhi = hi; r.maxlo = lo; r.flags |= RS_VMAX; r.lastmax = hi + lo;
+  }
+}
+
+__device__ __forceinline__ void laneMin(const W& w, int i, SeqRow& r, int posinf, int neginf, int poshuge,
+                                        int neghuge, double delta, bool goodrelax, double& val, bool& tight,
+                                        bool& settoinf) {
+  if (minRecomputes(r, posinf, neginf, poshuge, neghuge, goodrelax)) laneRecompute(w, i, r, true);
+  getMinAct(w.A->s, actOf(r), posinf, neginf, poshuge, neghuge, delta, goodrelax, val, tight, settoinf);
+}
+__device__ __forceinline__ void laneMax(const W& w, int i, SeqRow& r, int posinf, int neginf, int poshuge,
+                                        int neghuge, double delta, bool goodrelax, double& val, bool& tight,
+                                        bool& settoinf) {
+  if (maxRecomputes(r, posinf, neginf, poshuge, neghuge, goodrelax)) laneRecompute(w, i, r, false);
+  getMaxAct(w.A->s, actOf(r), posinf, neginf, poshuge, neghuge, delta, goodrelax, val, tight, settoinf);
+}
+__device__ __forceinline__ void laneBounds(const W& w, int i, SeqRow& r, bool goodrelax, double& minact,
+                                           double& maxact, bool& mint, bool& maxt, bool& mininf, bool& maxinf) {
+  if (!(r.flags & RS_VALID)) laneCalc(w, i, r);
+  laneMin(w, i, r, r.minposinf, r.minneginf, r.minposhuge, r.minneghuge, 0.0, goodrelax, minact, mint, mininf);
+  laneMax(w, i, r, r.maxposinf, r.maxneginf, r.maxposhuge, r.maxneghuge, 0.0, goodrelax, maxact, maxt, maxinf);
+}
+
+__device__ __noinline__ void laneMaxDelta(const W& w, int i, SeqRow& r) {  // recomputeMaxDelta
+  const Prob& P = w.A->P;
+  const Num& s = w.A->s;
+  const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
+  r.maxdelta = 0.0;
+  if (!(r.flags & RS_NBV)) {
+    bool nonbin = false;
+    for (int64_t p = p0; p < p1; ++p) nonbin |= !isBinaryCol(w, P.colidx[p]);
+    r.flags = (r.flags & ~RS_HNB) | (nonbin ? RS_HNB : 0u) | RS_NBV;
+  }
+  if (!(r.flags & RS_HNB)) {
+    for (int64_t p = p1 - 1; p >= p0; --p) {
+      const int j = P.colidx[p];
+      const double2 b = bnd(w, j);
+      if (b.x < 0.5 && b.y > 0.5) {
+        const double d = fabs(P.vals[p]);
+        if (d > r.maxdelta) {
+          r.maxdelta = d;
+          r.maxdeltacol = j;
+        }
+      }
+    }
+    return;
+  }
+  for (int64_t p = p1 - 1; p >= p0; --p) {
+    const int j = P.colidx[p];
+    const double2 b = bnd(w, j);
+    if (isInf(s, -b.x) || isInf(s, b.y)) {
+      r.maxdelta = s.inf;
+      r.maxdeltacol = j;
+      break;
+    }
+    const double d = fabs(P.vals[p]) * (b.y - b.x);
+    if (d > r.maxdelta) {
+      r.maxdelta = d;
+      r.maxdeltacol = j;
+    }
+  }
+}
+
+// The head and tail of propagateCons, one lane: tightenBounds up to its visit of the entries, and -- for a row
+// that does not reach the visit -- the infeasibility and redundancy tests.  Returns
+//   ROW_DONE  the row changes nothing but its own record (r holds it; RS_INUPD set if it joined the update list);
+//   ROW_LIVE  the row reaches the visit of its entries (r holds the record the visit starts from);
+//   ROW_CUT   the row finds the node infeasible (it is then run for real).
+constexpr int ROW_DONE = 0, ROW_LIVE = 1, ROW_CUT = 2;
+
+__device__ __noinline__ int laneHead(const W& w, int i, SeqRow& r) {
+  const Prob& P = w.A->P;
+  const Num& s = w.A->s;
+  const int len = (int)(P.rowptr[i + 1] - P.rowptr[i]);
+  const bool force = (len == 1);
+  const unsigned tightenmode = 1;
+  // tightenBounds
+  bool skip = false;
+  if (!(r.flags & RS_VALID)) laneCalc(w, i, r);
+  if (r.minneginf + r.minposinf + r.minneghuge + r.minposhuge > 1 &&
+      r.maxneginf + r.maxposinf + r.maxneghuge + r.maxposhuge > 1)
+    skip = true;
+  if (!skip && !force && btOf(r.flags) >= tightenmode) skip = true;
+  if (!skip && r.maxdelta == SEQ_INVALID) laneMaxDelta(w, i, r);
+  if (!skip && feasZero(s, r.maxdelta)) skip = true;
+  if (!skip && !isInf(s, r.maxdelta)) {
+    double minact, maxact;
+    bool t1, t2, f1, f2;
+    laneBounds(w, i, r, false, minact, maxact, t1, t2, f1, f2);
+    const double slack = (isInf(s, P.rhs[i]) || f1) ? s.inf : P.rhs[i] - minact;
+    const double surplus = (isInf(s, -P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
+    if (le(s, r.maxdelta, dmin(slack, surplus))) skip = true;
+  }
+  if (!skip) return ROW_LIVE;
+  // propagateCons: the infeasibility and redundancy tests
+  double minact, maxact;
+  bool t1, t2, f1, f2;
+  laneBounds(w, i, r, true, minact, maxact, t1, t2, f1, f2);
+  if (feasGt(s, minact, P.rhs[i]) || feasLt(s, maxact, P.lhs[i])) return ROW_CUT;
+  // a redundant row is deleted locally (disableRow: joins the update list unless it is there)
+  if (ge(s, minact, P.lhs[i]) && le(s, maxact, P.rhs[i]) && !(r.flags & RS_UD) && (r.flags & RS_EN))
+    r.flags |= RS_UD | RS_INUPD;
+  return ROW_DONE;
+}
+
 // ------------------------------------------------------------------------------------------ one row
+__device__ __noinline__ bool tightenVisit(W& w, int i, SeqRow r);
+
 // tightenBounds (uniform); returns true on cutoff
-__device__ bool tightenBounds(W& w, int i) {
+__device__ __noinline__ bool tightenBounds(W& w, int i) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int len = (int)(P.rowptr[i + 1] - P.rowptr[i]);
@@ -931,6 +1043,16 @@ __device__ bool tightenBounds(W& w, int i) {
     const double surplus = (isInf(s, -P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
     if (le(s, r.maxdelta, dmin(slack, surplus))) return false;
   }
+  return tightenVisit(w, i, r);
+}
+
+// tightenBounds from its visit of the entries on (the row passed the tests before it; r is its record then)
+__device__ __noinline__ bool tightenVisit(W& w, int i, SeqRow r) {
+  const Prob& P = w.A->P;
+  const Num& s = w.A->s;
+  const int len = (int)(P.rowptr[i + 1] - P.rowptr[i]);
+  const bool force = (len == 1);
+  const unsigned tightenmode = 1;
   const bool easy = lt(s, r.maxdelta, s.maxeasy);
   const bool sorted = !s.nosort;
   const int nbin = nbinOf(w, i);
@@ -989,13 +1111,22 @@ __device__ bool tightenBounds(W& w, int i) {
   return false;
 }
 
+__device__ __noinline__ bool propagateTail(W& w, int i);
+
 // propagateCons without ranged rows (uniform); returns true on cutoff
-__device__ bool propagateCons(W& w, int i) {
+__device__ __noinline__ bool propagateCons(W& w, int i) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   w.rows += 1;
   w.nnz += P.rowptr[i + 1] - P.rowptr[i];
   if (tightenBounds(w, i)) return true;
+  return propagateTail(w, i);
+}
+
+// propagateCons after tightenBounds: the infeasibility and redundancy tests (uniform); returns true on cutoff
+__device__ __noinline__ bool propagateTail(W& w, int i) {
+  const Prob& P = w.A->P;
+  const Num& s = w.A->s;
   SeqRow r = loadRow(w, i);
   double minact, maxact;
   bool t1, t2, f1, f2;
@@ -1011,8 +1142,12 @@ __device__ bool propagateCons(W& w, int i) {
 }
 
 // propagateRounds: consPropLinear over the marked rows until a call changes nothing (uniform);
-// 0 fixpoint, 1 cutoff, 2 round limit
+// 0 fixpoint, 1 cutoff, 2 round limit.  The rows of a call are taken 32 at a time, one per lane, through laneHead;
+// walking them in order, the rows it ends are committed as they stand, a row that reaches the visit of its entries
+// is visited by the warp, and a row that finds the node infeasible is run for real.  After a visit that changed a
+// bound the next rows are taken afresh.
 __device__ int propagateRounds(W& w, int maxrounds, int& rounds) {
+  const Prob& P = w.A->P;
   rounds = 0;
   for (int round = 0; round < maxrounds; ++round) {
     const int nmarked = w.nm;
@@ -1020,12 +1155,59 @@ __device__ int propagateRounds(W& w, int maxrounds, int& rounds) {
     w.nchg = 0;
     w.indelay = true;
     bool cut = false;
-    for (int k = 0; k < nmarked && !cut; ++k) {
-      const int i = w.M[k];
-      SeqRow r = loadRow(w, i);
-      unmarkProp(w, i, r);
-      storeRow(w, i, r);
-      cut = propagateCons(w, i);
+    for (int k = 0; k < nmarked && !cut;) {
+      const int cnt = min(32, nmarked - k);
+      const bool has = w.lane < cnt;
+      int i = -1, cls = ROW_DONE;
+      bool wasin = false;
+      SeqRow r;
+      if (has) {
+        i = w.M[k + w.lane];
+        r = loadRow(w, i);
+        wasin = (r.flags & RS_INUPD) != 0;
+        // unmarkProp
+        if (!((r.flags & RS_UU) || (!(r.flags & RS_MP) && !(r.flags & RS_UM))))
+          r.flags = (r.flags & ~RS_UM) | RS_UU | RS_INUPD;
+        cls = laneHead(w, i, r);
+      }
+      const unsigned stop = __ballot_sync(FULL, has && cls != ROW_DONE);
+      const unsigned below = (1u << w.lane) - 1u;
+      int pos = 0;
+      bool fresh = false;  // a bound changed: the rows after pos are taken afresh
+      while (pos < cnt && !cut && !fresh) {
+        const unsigned rest = stop & ~((1u << pos) - 1u);
+        const int q = rest ? __ffs(rest) - 1 : cnt;
+        // rows [pos, q) are committed as they stand, and row q's unmark and head too when it is live
+        const int qcls = __shfl_sync(FULL, cls, q & 31);
+        const int upto = (q < cnt && qcls == ROW_LIVE) ? q + 1 : q;
+        const bool commit = w.lane >= pos && w.lane < upto;
+        const bool app = commit && !wasin && (r.flags & RS_INUPD);
+        const unsigned am = __ballot_sync(FULL, app);
+        if (app) w.U[w.nu + __popc(am & below)] = i;
+        if (commit) w.rs[i] = r;
+        w.nu += __popc(am);
+        const unsigned cm = __ballot_sync(FULL, commit);
+        w.rows += __popc(cm);
+        w.nnz += __reduce_add_sync(FULL, commit ? (unsigned)(P.rowptr[i + 1] - P.rowptr[i]) : 0u);
+        __syncwarp();
+        if (q >= cnt) {
+          pos = cnt;
+          break;
+        }
+        const int iq = __shfl_sync(FULL, i, q);
+        const long long old = w.nchg;
+        if (qcls == ROW_LIVE) {
+          cut = tightenVisit(w, iq, w.rs[iq]) || propagateTail(w, iq);
+        } else {
+          SeqRow rr = loadRow(w, iq);
+          unmarkProp(w, iq, rr);
+          storeRow(w, iq, rr);
+          cut = propagateCons(w, iq);
+        }
+        pos = q + 1;
+        fresh = w.nchg > old;
+      }
+      k += pos;
     }
     w.indelay = false;
     processUpdates(w);
