@@ -259,11 +259,13 @@ void gbp_default_params(gbp_params* p) {
 
 int gbp_set_params(gbp_ctx* ctx, const gbp_params* p) {
   if (!ctx || !p) return GBP_ERR_INVALID;
-  if (!(p->infinity > 0) || !(p->epsilon >= 0) || !(p->feastol >= 0) || !(p->hugeval > 0) || !(p->boundstreps >= 0))
+  if (!(p->infinity > 0) || !(p->epsilon >= 0) || !(p->sumepsilon >= 0) || !(p->feastol >= 0) ||
+      !(p->hugeval > 0) || !(p->boundstreps >= 0) || !(p->recompfac > 0))
     return fail(ctx, GBP_ERR_INVALID, "invalid numerics");
   ctx->par = *p;
-  ctx->num = Num{p->infinity, p->epsilon, p->sumepsilon, p->feastol, p->hugeval, p->boundstreps, p->recompfac,
-                 p->maxeasyactivitydelta, (p->flags & GBP_FLAG_NOSORTVARS) ? 1 : 0};
+  // + 0.0 stores a -0 as +0: the device tests compare the tolerances' bit patterns, which needs them >= +0
+  ctx->num = Num{p->infinity, p->epsilon + 0.0, p->sumepsilon + 0.0, p->feastol + 0.0, p->hugeval,
+                 p->boundstreps + 0.0, p->recompfac, p->maxeasyactivitydelta, (p->flags & GBP_FLAG_NOSORTVARS) ? 1 : 0};
   destroyGraphs(ctx);  // the numerics are baked into the graphs' kernel arguments
   ctx->ranged_ready = false;  // eligibility depends on epsilon and infinity
   return GBP_OK;

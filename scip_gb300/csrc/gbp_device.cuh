@@ -258,7 +258,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
         }
       }
     }
-    if (!isInf(s, -lhs)) {
+    if (!isNegInf(s, lhs)) {
       if (feasLt(s, maxact, lhs)) return true;
       double slack = maxact - lhs;
       if (!positive(s, slack)) slack = 0.0;
@@ -280,7 +280,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
   bool mintight, maxtight, mininf, maxinf;
   residuals(s, a, val, l, u, minres, maxres, mintight, maxtight, mininf, maxinf);
   bool rhsok = !mininf && !isInf(s, rhs) && mintight && (lt(s, fabs(rhs), 1.0) || !quotNear1(minres, rhs, s.eps));
-  bool lhsok = !maxinf && !isInf(s, -lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !quotNear1(maxres, lhs, s.eps));
+  bool lhsok = !maxinf && !isNegInf(s, lhs) && maxtight && (lt(s, fabs(lhs), 1.0) || !quotNear1(maxres, lhs, s.eps));
   // Every acceptance test of a new upper bound (forced LT, integral FeasLT, UbBetter) needs newub < u, and of a
   // new lower bound newlb > l.  A side whose exact quotient misses that by more than the rounding of the
   // product bound*val is skipped before its division (the quotient would round to the same side of the
@@ -305,7 +305,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
         if (unrel) {
           minres = relres(true);
           newub = (rhs - minres) / val;
-          unrel = isInf(s, -minres) ||
+          unrel = isNegInf(s, minres) ||
                   (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
         }
         if (!unrel) emit(true, newub, force);
@@ -313,7 +313,7 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
     }
     if (lhsok) {
       double newlb = (lhs - maxres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         bool skip = false;
         if (updateUnreliable(s, maxres, a.maxhi + a.maxlo)) {
           maxres = relres(false);
@@ -327,12 +327,12 @@ __device__ __forceinline__ bool columnCandidates(const Num& s, const Act& a, dou
   } else {
     if (rhsok) {
       double newlb = (rhs - minres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         bool unrel = updateUnreliable(s, minres, a.minhi + a.minlo);
         if (unrel) {
           minres = relres(true);
           newlb = (rhs - minres) / val;
-          unrel = isInf(s, -minres) ||
+          unrel = isNegInf(s, minres) ||
                   (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
         }
         if (!unrel) emit(false, newlb, force);
@@ -377,7 +377,7 @@ __device__ __forceinline__ int rowTests(const Num& s, const Act& a, double lhs, 
       getMaxAct(s, a, a.maxposinf, a.maxneginf, a.maxposhuge, a.maxneghuge, 0.0, false, maxact, t2, f2);
     }
     double slack = (isInf(s, rhs) || f1) ? s.inf : rhs - minact;
-    double surplus = (isInf(s, -lhs) || f2) ? s.inf : maxact - lhs;
+    double surplus = (isNegInf(s, lhs) || f2) ? s.inf : maxact - lhs;
     if (le(s, maxactdelta, dmin(slack, surplus))) return 0;
   }
   easy = lt(s, maxactdelta, s.maxeasy);
@@ -387,7 +387,7 @@ __device__ __forceinline__ int rowTests(const Num& s, const Act& a, double lhs, 
 // maximal activity contribution of one entry (consdataRecomputeMaxActivityDelta, cons_linear.c:1542-1599);
 // returns -1 for an infinite bound
 __device__ __forceinline__ double entryDelta(const Num& s, double val, double l, double u) {
-  if (isInf(s, -l) || isInf(s, u)) return -1.0;
+  if (isNegInf(s, l) || isInf(s, u)) return -1.0;
   return fabs(val) * (u - l);
 }
 
@@ -447,7 +447,7 @@ __device__ __forceinline__ void loadChunk(const Prob& P, const BND& B, int64_t p
 // bit pattern of a non-negative double (order-preserving as a signed integer); +inf for an entry with an
 // infinite bound
 __device__ __forceinline__ long long deltaBits(const Num& s, double val, double l, double u) {
-  if (isInf(s, -l) || isInf(s, u)) return 0x7ff0000000000000LL;
+  if (isNegInf(s, l) || isInf(s, u)) return 0x7ff0000000000000LL;
   return __double_as_longlong(fabs(val) * (u - l));
 }
 __device__ __forceinline__ long long absBits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
@@ -476,7 +476,7 @@ __device__ __forceinline__ int selectEntries(const Num& s, const Act& a, const S
     full = true;
     return 1;
   }
-  const bool rhsfin = !isInf(s, rhs), lhsfin = !isInf(s, -lhs);
+  const bool rhsfin = !isInf(s, rhs), lhsfin = !isNegInf(s, lhs);
   const int mintot = a.minposinf + a.minneginf + a.minposhuge + a.minneghuge;
   const int maxtot = a.maxposinf + a.maxneginf + a.maxposhuge + a.maxneghuge;
   double thrR = s.inf, thrL = s.inf;  // entries with delta > thr qualify
@@ -691,7 +691,7 @@ __device__ __forceinline__ int finishRow(const Num& s, int len, double lhs, doub
   if (count) st.live += 1;
   if (easy) {
     // the slack rule's own infeasibility test (tightenVarBoundsEasy), independent of the entry
-    if ((!isInf(s, rhs) && feasLt(s, rhs, a.minhi + a.minlo)) || (!isInf(s, -lhs) && feasLt(s, a.maxhi + a.maxlo, lhs)))
+    if ((!isInf(s, rhs) && feasLt(s, rhs, a.minhi + a.minlo)) || (!isNegInf(s, lhs) && feasLt(s, a.maxhi + a.maxlo, lhs)))
       return 1;
   }
   nsel = selectEntries(s, a, so, lhs, rhs, len, easy, sel, full);
@@ -942,7 +942,7 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     if (isFixed(k) || !member(k)) continue;
     fixedAt(k, p, j, v, l, u);
     bool mininv = false, maxinv = false;
-    if (isInf(s, -l)) {
+    if (isNegInf(s, l)) {
       if (v < 0.0) maxinv = true;
       else mininv = true;
     } else if (v < 0.0) {
@@ -958,7 +958,7 @@ __device__ bool rangedRow(const Num& s, const Prob& P, const BND& B, int i, Cand
     } else {
       minact += v * u;
     }
-    if (isHuge(s, -minact)) mininv = true;
+    if (isNegHuge(s, minact)) mininv = true;
     if (isHuge(s, maxact)) maxinv = true;
     if (mininv || maxinv) return false;
   }
@@ -1343,7 +1343,7 @@ __device__ bool rowWarpCore(const Num& s, const Prob& P, const BND& B, int i, Ca
   if (t == 1) return true;
   if (t == 0) return false;
   if (lane == 0) st.live += 1;
-  const bool rhsfin = !isInf(s, rhs), lhsfin = !isInf(s, -lhs);
+  const bool rhsfin = !isInf(s, rhs), lhsfin = !isNegInf(s, lhs);
   if (easy && ((rhsfin && feasLt(s, rhs, a.minhi + a.minlo)) || (lhsfin && feasLt(s, a.maxhi + a.maxlo, lhs))))
     return true;  // the slack rule's own infeasibility test (tightenVarBoundsEasy)
 
@@ -1495,7 +1495,7 @@ __device__ __forceinline__ bool applyColumn(const Num& s, bool isint, double l, 
     const bool force = (k == 1);
     if (!(f & (force ? 2 : 1))) continue;
     double c = adjUb(s, isint, keyd(force ? kubf : kub));
-    if (isInf(s, -c) || feasLt(s, c, l)) { cut = true; continue; }
+    if (isNegInf(s, c) || feasLt(s, c, l)) { cut = true; continue; }
     c = dmax(c, l);
     if (force ? !ge(s, c, u) : ubBetter(s, c, l, u)) nu = dmin(nu, c);
   }

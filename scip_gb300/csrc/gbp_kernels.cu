@@ -357,7 +357,7 @@ __global__ void k_ranged_elig(Num s, Prob P, uint8_t* elig, int* list, int* coun
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.m; i += stride) {
     const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
     bool ok = false;
-    if (p1 - p0 >= 3 && !isInf(s, -P.lhs[i]) && !isInf(s, P.rhs[i])) {
+    if (p1 - p0 >= 3 && !isNegInf(s, P.lhs[i]) && !isInf(s, P.rhs[i])) {
       for (int64_t p = p0; p < p1; ++p) {
         const long long c = rangedCoef(s, P.isint[P.colidx[p]] != 0, P.vals[p]);
         coef[p] = c;

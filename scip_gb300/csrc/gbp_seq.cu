@@ -31,6 +31,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr double SEQ_INVALID = 1e99;  // SCIP_INVALID
+__device__ __forceinline__ bool isInvalid(double x) { return dbits(x) == dbits(SEQ_INVALID); }
 constexpr int MAXTIGHTENROUNDS = 10;  // cons_linear.c:6976
 
 // SeqRow::flags
@@ -68,7 +69,7 @@ __device__ __forceinline__ double2 bnd(const W& w, int j) {
 
 __device__ __forceinline__ bool isBinaryCol(const W& w, int j) {  // SCIPvarIsBinary on the base domain
   const double2 b = w.A->base[j];
-  return w.A->P.isint[j] != 0 && b.x >= 0.0 && b.y <= 1.0;
+  return w.A->P.isint[j] != 0 && !dneg(b.x) && !gtc(b.y, 1.0);
 }
 
 // rowSt: the row's record, initialised on the node's first touch
@@ -122,11 +123,11 @@ __device__ __noinline__ void calcActivities(const W& w, int i, SeqRow& r) {
       const double2 b = bnd(w, P.colidx[p0 + k]);
       // the counters of this entry, and its finite contributions (added below in order)
       double hi = 0.0, lo = 0.0;
-      addContribution(s, v, v > 0.0 ? b.x : b.y, hi, lo, mine.minposinf, mine.minneginf, mine.minposhuge,
+      addContribution(s, v, dpos(v) ? b.x : b.y, hi, lo, mine.minposinf, mine.minneginf, mine.minposhuge,
                       mine.minneghuge);
       cmin = hi;
       hi = 0.0;
-      addContribution(s, v, v > 0.0 ? b.y : b.x, hi, lo, mine.maxposinf, mine.maxneginf, mine.maxposhuge,
+      addContribution(s, v, dpos(v) ? b.y : b.x, hi, lo, mine.maxposinf, mine.maxneginf, mine.maxposhuge,
                       mine.maxneghuge);
       cmax = hi;
     }
@@ -138,8 +139,8 @@ __device__ __noinline__ void calcActivities(const W& w, int i, SeqRow& r) {
     for (int t = 0; t < cnt; ++t) {
       const double x = __shfl_sync(FULL, cmin, t);
       const double y = __shfl_sync(FULL, cmax, t);
-      if (x != 0.0) sum21f(a.minhi, a.minlo, x);
-      if (y != 0.0) sum21f(a.maxhi, a.maxlo, y);
+      if (dmag(x) != 0) sum21f(a.minhi, a.minlo, x);
+      if (dmag(y) != 0) sum21f(a.maxhi, a.maxlo, y);
     }
   }
   r.minhi = a.minhi; r.minlo = a.minlo; r.maxhi = a.maxhi; r.maxlo = a.maxlo;
@@ -165,8 +166,8 @@ __device__ __noinline__ void recomputeSide(const W& w, int i, SeqRow& r, bool is
     if (k >= 0) {
       const double v = P.vals[p0 + k];
       const double2 b = bnd(w, P.colidx[p0 + k]);
-      const double bb = (v > 0.0) == ismin ? b.x : b.y;
-      if (!isInf(s, bb) && !isInf(s, -bb) && !isHuge(s, v * bb) && !isHuge(s, -v * bb)) {
+      const double bb = (dpos(v)) == ismin ? b.x : b.y;
+      if (!isInf(s, bb) && !isNegInf(s, bb) && !isHuge(s, v * bb) && !isNegHuge(s, v * bb)) {
         c = v * bb;
         use = true;
       }
@@ -229,19 +230,19 @@ struct ResArgs {
 };
 __device__ __forceinline__ ResArgs resArgs(const Num& s, const SeqRow& r, double val, double l, double u) {
   double minb, maxb, absval;
-  if (val > 0.0) { minb = l; maxb = u; absval = val; }
+  if (dpos(val)) { minb = l; maxb = u; absval = val; }
   else { minb = -u; maxb = -l; absval = -val; }
   ResArgs a{r.minposinf, r.minneginf, r.minposhuge, r.minneghuge, 0.0,
             r.maxposinf, r.maxneginf, r.maxposhuge, r.maxneghuge, 0.0};
   if (isInf(s, minb)) a.mp -= 1;
-  else if (isInf(s, -minb)) a.mn -= 1;
+  else if (isNegInf(s, minb)) a.mn -= 1;
   else if (isHuge(s, minb * absval)) a.mph -= 1;
-  else if (isHuge(s, -minb * absval)) a.mnh -= 1;
+  else if (isNegHuge(s, minb * absval)) a.mnh -= 1;
   else a.md = absval * minb;
-  if (isInf(s, -maxb)) a.xn -= 1;
+  if (isNegInf(s, maxb)) a.xn -= 1;
   else if (isInf(s, maxb)) a.xp -= 1;
   else if (isHuge(s, absval * maxb)) a.xph -= 1;
-  else if (isHuge(s, -absval * maxb)) a.xnh -= 1;
+  else if (isNegHuge(s, absval * maxb)) a.xnh -= 1;
   else a.xd = absval * maxb;
   return a;
 }
@@ -261,7 +262,7 @@ __device__ __noinline__ double reliableResWarp(const W& w, int i, int skipcol, b
       if (j != skipcol) {
         const double v = P.vals[p0 + k];
         const double2 b = bnd(w, j);
-        c = v > 0.0 ? (ismin ? v * b.x : v * b.y) : (ismin ? v * b.y : v * b.x);
+        c = dpos(v) ? (ismin ? v * b.x : v * b.y) : (ismin ? v * b.y : v * b.x);
         use = true;
       }
     }
@@ -298,16 +299,16 @@ __device__ __noinline__ void recomputeMaxDelta(const W& w, int i, SeqRow& r) {
     const double2 b = bnd(w, j);
     double d;
     if (binonly) {
-      if (!(b.x < 0.5 && b.y > 0.5)) continue;
-      d = fabs(P.vals[p0 + k]);
+      if (gec(b.x, 0.5) || !gtc(b.y, 0.5)) continue;  // not b.x < 0.5 < b.y
+      d = dabs(P.vals[p0 + k]);
     } else {
-      if (isInf(s, -b.x) || isInf(s, b.y)) {
+      if (isNegInf(s, b.x) || isInf(s, b.y)) {
         infk = k;  // k grows within the lane: the lane's largest
         continue;
       }
-      d = fabs(P.vals[p0 + k]) * (b.y - b.x);
+      d = dabs(P.vals[p0 + k]) * (b.y - b.x);
     }
-    if (d > best || (d == best && d > 0.0)) {  // later positions win ties
+    if (dgt(d, best) || (!dlt(d, best) && dpos(d))) {  // later positions win ties
       best = d;
       bestk = k;
     }
@@ -334,62 +335,63 @@ __device__ __noinline__ void recomputeMaxDelta(const W& w, int i, SeqRow& r) {
 
 // consdataUpdateActivities for a local bound change, checkreliability TRUE (one lane, one row)
 __device__ void updateActivities(const Num& s, SeqRow& r, double val, double oldb, double newb, bool islb) {
-  const bool ismin = islb == (val > 0.0);
+  const bool ismin = islb == (dpos(val));
   double *hi, *lo, *last;
   int *posinf, *neginf, *poshuge, *neghuge;
   bool validact;
   if (ismin) {
     hi = &r.minhi; lo = &r.minlo; last = &r.lastmin; validact = (r.flags & RS_VMIN) != 0;
     poshuge = &r.minposhuge; neghuge = &r.minneghuge;
-    posinf = val > 0.0 ? &r.minposinf : &r.minneginf;
-    neginf = val > 0.0 ? &r.minneginf : &r.minposinf;
+    posinf = dpos(val) ? &r.minposinf : &r.minneginf;
+    neginf = dpos(val) ? &r.minneginf : &r.minposinf;
   } else {
     hi = &r.maxhi; lo = &r.maxlo; last = &r.lastmax; validact = (r.flags & RS_VMAX) != 0;
     poshuge = &r.maxposhuge; neghuge = &r.maxneghuge;
-    posinf = val > 0.0 ? &r.maxposinf : &r.maxneginf;
-    neginf = val > 0.0 ? &r.maxneginf : &r.maxposinf;
+    posinf = dpos(val) ? &r.maxposinf : &r.maxneginf;
+    neginf = dpos(val) ? &r.maxneginf : &r.maxposinf;
   }
   double dhi = 0.0, dlo = 0.0;
   const double oldc = val * oldb, newc = val * newb;
-  const bool hugenew = isHuge(s, fabs(newc));
-  const bool finnew = !isInf(s, fabs(newb));
-  if (isInf(s, fabs(oldb))) {
-    if (oldb > 0.0) {
-      if (finnew || newb < 0.0) {
+  const bool hugenew = isHuge(s, dabs(newc));
+  const bool finnew = !isInf(s, dabs(newb));
+  if (isInf(s, dabs(oldb))) {
+    if (dpos(oldb)) {
+      if (finnew || dneg(newb)) {
         (*posinf)--;
-        if (!finnew && newb < 0.0) (*neginf)++;
-        else if (hugenew) { if (newc > 0.0) (*poshuge)++; else (*neghuge)++; }
+        if (!finnew && dneg(newb)) (*neginf)++;
+        else if (hugenew) { if (dpos(newc)) (*poshuge)++; else (*neghuge)++; }
         else dhi = newc;
       }
     } else {
-      if (finnew || newb > 0.0) {
+      if (finnew || dpos(newb)) {
         (*neginf)--;
-        if (!finnew && newb > 0.0) (*posinf)++;
-        else if (hugenew) { if (newc > 0.0) (*poshuge)++; else (*neghuge)++; }
+        if (!finnew && dpos(newb)) (*posinf)++;
+        else if (hugenew) { if (dpos(newc)) (*poshuge)++; else (*neghuge)++; }
         else dhi = newc;
       }
     }
-  } else if (isHuge(s, fabs(oldc))) {
-    if (oldc > 0.0) (*poshuge)--; else (*neghuge)--;
-    if (!finnew) { if (newb > 0.0) (*posinf)++; else (*neginf)++; }
-    else if (hugenew) { if (newc > 0.0) (*poshuge)++; else (*neghuge)++; }
+  } else if (isHuge(s, dabs(oldc))) {
+    if (dpos(oldc)) (*poshuge)--; else (*neghuge)--;
+    if (!finnew) { if (dpos(newb)) (*posinf)++; else (*neginf)++; }
+    else if (hugenew) { if (dpos(newc)) (*poshuge)++; else (*neghuge)++; }
     else dhi = newc;
   } else {
     if (!finnew) {
-      if (newb > 0.0) (*posinf)++; else (*neginf)++;
+      if (dpos(newb)) (*posinf)++; else (*neginf)++;
       dhi = -oldc;
     } else if (hugenew) {
-      if (newc > 0.0) (*poshuge)++; else (*neghuge)++;
+      if (dpos(newc)) (*poshuge)++; else (*neghuge)++;
       dhi = -oldc;
     } else {
       dhi = newc;
       sum21(dhi, dlo, -oldc);
     }
   }
-  if (validact && dhi + dlo != 0.0) {
-    sum21(*hi, *lo, dhi + dlo);
+  const double dsum = dhi + dlo;
+  if (validact && dmag(dsum) != 0) {
+    sum21(*hi, *lo, dsum);
     const double cur = *hi + *lo;
-    if (fabs(*last) < fabs(cur)) *last = cur;
+    if (dmag(*last) < dmag(cur)) *last = cur;
     else if (updateUnreliable(s, cur, *last)) r.flags &= ismin ? ~RS_VMIN : ~RS_VMAX;
   }
 }
@@ -505,8 +507,8 @@ __device__ __noinline__ void boundEvent(W& w, int j, bool islb, double oldb, dou
           r.maxdeltacol = -1;
         }
         if (btOf(r.flags) > 0) {
-          const bool rhsfin = !isInf(s, A.P.rhs[i]), lhsfin = !isInf(s, -A.P.lhs[i]);
-          if (islb ? (a > 0.0 ? rhsfin : lhsfin) : (a > 0.0 ? lhsfin : rhsfin)) r.flags = withBt(r.flags, 0);
+          const bool rhsfin = !isInf(s, A.P.rhs[i]), lhsfin = !isNegInf(s, A.P.lhs[i]);
+          if (islb ? (dpos(a) ? rhsfin : lhsfin) : (dpos(a) ? lhsfin : rhsfin)) r.flags = withBt(r.flags, 0);
         }
       }
     }
@@ -531,7 +533,7 @@ __device__ __noinline__ bool inferUb(W& w, int j, double newub, bool force, bool
   const double2 b = bnd(w, j);
   tightened = false;
   newub = adjUb(s, isint, newub);
-  if (isInf(s, -newub) || feasLt(s, newub, b.x)) return true;
+  if (isNegInf(s, newub) || feasLt(s, newub, b.x)) return true;
   newub = dmax(newub, b.x);
   if ((force && ge(s, newub, b.y)) || (!force && !ubBetter(s, newub, b.x, b.y))) return false;
   if (!lt(s, newub, b.y)) return false;
@@ -562,7 +564,7 @@ __device__ __noinline__ bool inferLb(W& w, int j, double newlb, bool force, bool
 // what inferUb / inferLb would do, without doing it: 0 nothing, 1 a change or infeasibility
 __device__ __forceinline__ bool wouldInferUb(const Num& s, bool isint, double l, double u, double newub, bool force) {
   newub = adjUb(s, isint, newub);
-  if (isInf(s, -newub) || feasLt(s, newub, l)) return true;
+  if (isNegInf(s, newub) || feasLt(s, newub, l)) return true;
   newub = dmax(newub, l);
   if ((force && ge(s, newub, u)) || (!force && !ubBetter(s, newub, l, u))) return false;
   return lt(s, newub, u);
@@ -578,7 +580,7 @@ __device__ __forceinline__ bool wouldInferLb(const Num& s, bool isint, double l,
 // ------------------------------------------------------------------------------------------ one entry
 // the side guard of the residual rule (cons_linear.c:6765-6766): a small side, or a residual not equal to it
 __device__ __forceinline__ bool sideOk(const Num& s, double side, double res) {
-  return lt(s, fabs(side), 1.0) || !eq(s, res / side, 1.0);
+  return lt(s, dabs(side), 1.0) || !quotNear1(res, side, s.eps);
 }
 
 // tightenVarBounds without effects (one lane, entry k of the row in r): true if running it would change anything
@@ -601,7 +603,7 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
   bool mint, maxt, mininf, maxinf;
   getMinAct(s, a, ra.mp, ra.mn, ra.mph, ra.mnh, ra.md, false, minres, mint, mininf);
   getMaxAct(s, a, ra.xp, ra.xn, ra.xph, ra.xnh, ra.xd, false, maxres, maxt, maxinf);
-  if (val > 0.0) {
+  if (dpos(val)) {
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newub = (rhs - minres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
@@ -610,9 +612,9 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
         if (wouldInferUb(s, isint, l, u, newub, force)) return true;
       }
     }
-    if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
+    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newlb = (lhs - maxres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         if (updateUnreliable(s, maxres, r.lastmax)) return true;
         if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
       }
@@ -620,12 +622,12 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
   } else {
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newlb = (rhs - minres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         if (updateUnreliable(s, minres, r.lastmin)) return true;
         if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
       }
     }
-    if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
+    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newub = (lhs - maxres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
         if (updateUnreliable(s, maxres, r.lastmax)) return true;
@@ -655,7 +657,7 @@ __device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool for
     storeRow(w, i, r);
   }
   double l = b.x, u = b.y;
-  if (val > 0.0) {
+  if (dpos(val)) {
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newub = (rhs - minres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
@@ -663,7 +665,7 @@ __device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool for
         if (unrel) {
           minres = reliableResWarp(w, i, j, true);
           newub = (rhs - minres) / val;
-          unrel = isInf(s, -minres) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
+          unrel = isNegInf(s, minres) || (!ubBetter(s, newub, l, u) && (!feasLt(s, newub, u) || !isint) && (!force || !lt(s, newub, u)));
         }
         if (!unrel) {
           if (inferUb(w, j, newub, force, tightened)) return true;
@@ -672,9 +674,9 @@ __device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool for
         }
       }
     }
-    if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
+    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newlb = (lhs - maxres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         if (updateUnreliable(s, maxres, r.lastmax)) {
           maxres = reliableResWarp(w, i, j, false);
           newlb = (lhs - maxres) / val;
@@ -688,12 +690,12 @@ __device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool for
   } else {
     if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
       double newlb = (rhs - minres) / val;
-      if (!isInf(s, -newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
+      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
         bool unrel = updateUnreliable(s, minres, r.lastmin);
         if (unrel) {
           minres = reliableResWarp(w, i, j, true);
           newlb = (rhs - minres) / val;
-          unrel = isInf(s, -minres) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
+          unrel = isNegInf(s, minres) || (!lbBetter(s, newlb, l, u) && (!feasGt(s, newlb, l) || !isint) && (!force || !gt(s, newlb, l)));
         }
         if (!unrel) {
           if (inferLb(w, j, newlb, force, tightened)) return true;
@@ -702,7 +704,7 @@ __device__ __noinline__ bool residualRun(W& w, int i, SeqRow& r, int k, bool for
         }
       }
     }
-    if (!maxinf && !isInf(s, -lhs) && maxt && sideOk(s, lhs, maxres)) {
+    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
       double newub = (lhs - maxres) / val;
       if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
         if (updateUnreliable(s, maxres, r.lastmax)) {
@@ -731,7 +733,7 @@ __device__ bool easyWould(const W& w, int i, const SeqRow& r, int k, bool force)
   const double2 b = bnd(w, j);
   const double l = b.x, u = b.y;
   if (!(r.flags & RS_VMIN)) return true;
-  if (val > 0.0) {
+  if (dpos(val)) {
     if (!isInf(s, rhs)) {
       const double minact = r.minhi + r.minlo;
       if (feasLt(s, rhs, minact)) return true;
@@ -743,7 +745,7 @@ __device__ bool easyWould(const W& w, int i, const SeqRow& r, int k, bool force)
         if ((force || ubBetter(s, nu, l, u)) && wouldInferUb(s, isint, l, u, nu, force)) return true;
       }
     }
-    if (!isInf(s, -lhs)) {
+    if (!isNegInf(s, lhs)) {
       if (!(r.flags & RS_VMAX)) return true;
       const double maxact = r.maxhi + r.maxlo;
       if (feasLt(s, maxact, lhs)) return true;
@@ -767,7 +769,7 @@ __device__ bool easyWould(const W& w, int i, const SeqRow& r, int k, bool force)
         if ((force || lbBetter(s, nl, l, u)) && wouldInferLb(s, isint, l, u, nl, force)) return true;
       }
     }
-    if (!isInf(s, -lhs)) {
+    if (!isNegInf(s, lhs)) {
       if (!(r.flags & RS_VMAX)) return true;
       const double maxact = r.maxhi + r.maxlo;
       if (feasLt(s, maxact, lhs)) return true;
@@ -810,7 +812,7 @@ __device__ __noinline__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) 
   ensureAct(w, i, r);
   if (!(r.flags & RS_VMIN)) recomputeSide(w, i, r, true);
   storeRow(w, i, r);
-  if (val > 0.0) {
+  if (dpos(val)) {
     if (!isInf(s, rhs)) {
       const double minact = r.minhi + r.minlo;
       if (feasLt(s, rhs, minact)) return true;
@@ -823,7 +825,7 @@ __device__ __noinline__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) 
         u = bnd(w, j).y;
       }
     }
-    if (!isInf(s, -lhs)) {
+    if (!isNegInf(s, lhs)) {
       if (!(r.flags & RS_VMAX)) {
         recomputeSide(w, i, r, false);
         storeRow(w, i, r);
@@ -851,7 +853,7 @@ __device__ __noinline__ bool easyRun(W& w, int i, SeqRow& r, int k, bool force) 
         l = bnd(w, j).x;
       }
     }
-    if (!isInf(s, -lhs)) {
+    if (!isNegInf(s, lhs)) {
       if (!(r.flags & RS_VMAX)) {
         recomputeSide(w, i, r, false);
         storeRow(w, i, r);
@@ -901,8 +903,8 @@ __device__ __noinline__ void laneRecompute(const W& w, int i, SeqRow& r, bool is
   for (int64_t p = P.rowptr[i + 1] - 1; p >= P.rowptr[i]; --p) {
     const double v = P.vals[p];
     const double2 b = bnd(w, P.colidx[p]);
-    const double bb = (v > 0.0) == ismin ? b.x : b.y;
-    if (!isInf(s, bb) && !isInf(s, -bb) && !isHuge(s, v * bb) && !isHuge(s, -v * bb)) sum21(hi, lo, v * bb);
+    const double bb = (dpos(v)) == ismin ? b.x : b.y;
+    if (!isInf(s, bb) && !isNegInf(s, bb) && !isHuge(s, v * bb) && !isNegHuge(s, v * bb)) sum21(hi, lo, v * bb);
   }
   if (ismin) {
     r.minhi = hi; r.minlo = lo; r.flags |= RS_VMIN; r.lastmin = hi + lo;
@@ -944,9 +946,9 @@ __device__ __noinline__ void laneMaxDelta(const W& w, int i, SeqRow& r) {  // re
     for (int64_t p = p1 - 1; p >= p0; --p) {
       const int j = P.colidx[p];
       const double2 b = bnd(w, j);
-      if (b.x < 0.5 && b.y > 0.5) {
-        const double d = fabs(P.vals[p]);
-        if (d > r.maxdelta) {
+      if (!gec(b.x, 0.5) && gtc(b.y, 0.5)) {
+        const double d = dabs(P.vals[p]);
+        if (dgt(d, r.maxdelta)) {
           r.maxdelta = d;
           r.maxdeltacol = j;
         }
@@ -957,13 +959,13 @@ __device__ __noinline__ void laneMaxDelta(const W& w, int i, SeqRow& r) {  // re
   for (int64_t p = p1 - 1; p >= p0; --p) {
     const int j = P.colidx[p];
     const double2 b = bnd(w, j);
-    if (isInf(s, -b.x) || isInf(s, b.y)) {
+    if (isNegInf(s, b.x) || isInf(s, b.y)) {
       r.maxdelta = s.inf;
       r.maxdeltacol = j;
       break;
     }
-    const double d = fabs(P.vals[p]) * (b.y - b.x);
-    if (d > r.maxdelta) {
+    const double d = dabs(P.vals[p]) * (b.y - b.x);
+    if (dgt(d, r.maxdelta)) {
       r.maxdelta = d;
       r.maxdeltacol = j;
     }
@@ -990,14 +992,14 @@ __device__ __noinline__ int laneHead(const W& w, int i, SeqRow& r) {
       r.maxneginf + r.maxposinf + r.maxneghuge + r.maxposhuge > 1)
     skip = true;
   if (!skip && !force && btOf(r.flags) >= tightenmode) skip = true;
-  if (!skip && r.maxdelta == SEQ_INVALID) laneMaxDelta(w, i, r);
+  if (!skip && isInvalid(r.maxdelta)) laneMaxDelta(w, i, r);
   if (!skip && feasZero(s, r.maxdelta)) skip = true;
   if (!skip && !isInf(s, r.maxdelta)) {
     double minact, maxact;
     bool t1, t2, f1, f2;
     laneBounds(w, i, r, false, minact, maxact, t1, t2, f1, f2);
     const double slack = (isInf(s, P.rhs[i]) || f1) ? s.inf : P.rhs[i] - minact;
-    const double surplus = (isInf(s, -P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
+    const double surplus = (isNegInf(s, P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
     if (le(s, r.maxdelta, dmin(slack, surplus))) skip = true;
   }
   if (!skip) return ROW_LIVE;
@@ -1029,7 +1031,7 @@ __device__ __noinline__ bool tightenBounds(W& w, int i) {
       r.maxneginf + r.maxposinf + r.maxneghuge + r.maxposhuge > 1)
     return false;
   if (!force && btOf(r.flags) >= tightenmode) return false;
-  if (r.maxdelta == SEQ_INVALID) {
+  if (isInvalid(r.maxdelta)) {
     recomputeMaxDelta(w, i, r);
     storeRow(w, i, r);
   }
@@ -1040,7 +1042,7 @@ __device__ __noinline__ bool tightenBounds(W& w, int i) {
     activityBounds(w, i, r, false, minact, maxact, t1, t2, f1, f2);
     storeRow(w, i, r);
     const double slack = (isInf(s, P.rhs[i]) || f1) ? s.inf : P.rhs[i] - minact;
-    const double surplus = (isInf(s, -P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
+    const double surplus = (isNegInf(s, P.lhs[i]) || f2) ? s.inf : maxact - P.lhs[i];
     if (le(s, r.maxdelta, dmin(slack, surplus))) return false;
   }
   return tightenVisit(w, i, r);
@@ -1281,7 +1283,7 @@ __global__ void __launch_bounds__(WPB * 32) k_nodes_seq(const __grid_constant__ 
       b = bnd(w, j);
       if (nu < b.y) {
         double v = adjUb(s, isint, nu);
-        if (!isInf(s, -v)) {
+        if (!isNegInf(s, v)) {
           v = dmax(v, b.x);
           if (lt(s, v, b.y)) {
             setBound(w, j, b.x, v);
@@ -1367,7 +1369,7 @@ __global__ void k_seq_prepare(Num s, Prob P, const double2* base, int* prep) {
     for (int64_t p = p0; p < p1; ++p) {
       const int j = P.colidx[p];
       const double2 b = base[j];
-      if (lead && P.isint[j] != 0 && b.x >= 0.0 && b.y <= 1.0) ++nbin;
+      if (lead && P.isint[j] != 0 && !dneg(b.x) && !gtc(b.y, 1.0)) ++nbin;
       else lead = false;
       addTerm(s, a, P.vals[p], b.x, b.y);
     }
