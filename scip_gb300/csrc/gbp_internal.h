@@ -105,8 +105,9 @@ struct SeqRow {
   int maxposinf, maxneginf, maxposhuge, maxneghuge;
   int maxdeltacol, mpos, stamp;
   unsigned flags;
+  int evc;  // bound-change events that reached the row in this node (lanes detect records that changed under them)
 };
-static_assert(sizeof(SeqRow) == 104, "SeqRow layout");
+static_assert(sizeof(SeqRow) == 112, "SeqRow layout");
 
 // warps (one node each) per CTA of the sequential kernel
 constexpr int SEQ_WARPS = 4;

@@ -83,6 +83,7 @@ __device__ __forceinline__ SeqRow loadRow(const W& w, int i) {
     r.maxposinf = r.maxneginf = r.maxposhuge = r.maxneghuge = 0;
     r.maxdeltacol = -1;
     r.mpos = -1;
+    r.evc = 0;
     r.stamp = w.epoch;
     // a node starts from the root's fixpoint: rows count as tightened there (tightenmode 2)
     r.flags = RS_EN | (2u << RS_BTSHIFT);
@@ -502,6 +503,7 @@ __device__ __noinline__ void boundEvent(W& w, int j, bool islb, double oldb, dou
             appM = true;
           }
         }
+        r.evc += 1;
         if (r.maxdeltacol == j) {
           r.maxdelta = SEQ_INVALID;
           r.maxdeltacol = -1;
@@ -932,43 +934,82 @@ __device__ __forceinline__ void laneBounds(const W& w, int i, SeqRow& r, bool go
   laneMax(w, i, r, r.maxposinf, r.maxneginf, r.maxposhuge, r.maxneghuge, 0.0, goodrelax, maxact, maxt, maxinf);
 }
 
-__device__ __noinline__ void laneMaxDelta(const W& w, int i, SeqRow& r) {  // recomputeMaxDelta
+// The largest activity delta of a row as recomputeMaxDelta finds it, gathered in one forward pass: the reverse scan
+// keeps the first maximum it meets (the largest position among equal deltas, a delta > 0), and without binaries
+// only the first infinite domain it meets (the largest such position) ends it with infinity.
+struct MaxDeltaScan {
+  double bbest, gbest;  // over the unfixed binaries (|a|), over all entries (|a| * (u - l))
+  int bcol, gcol, infcol;
+  bool nonbin;
+};
+
+// One pass over a row's entries for laneHead: calcActivities (calc) and the candidates of recomputeMaxDelta (md).
+// The loads of an entry (its column, coefficient, bounds, base domain and type) are independent of the sums, so
+// the pass is unrolled to keep several entries' loads in flight.
+__device__ __noinline__ void laneScan(const W& w, int i, SeqRow& r, bool calc, bool md, MaxDeltaScan& m) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
-  r.maxdelta = 0.0;
-  if (!(r.flags & RS_NBV)) {
-    bool nonbin = false;
-    for (int64_t p = p0; p < p1; ++p) nonbin |= !isBinaryCol(w, P.colidx[p]);
-    r.flags = (r.flags & ~RS_HNB) | (nonbin ? RS_HNB : 0u) | RS_NBV;
-  }
-  if (!(r.flags & RS_HNB)) {
-    for (int64_t p = p1 - 1; p >= p0; --p) {
-      const int j = P.colidx[p];
-      const double2 b = bnd(w, j);
+  Act a;
+  actZero(a);
+  m.bbest = m.gbest = 0.0;
+  m.bcol = m.gcol = m.infcol = -1;
+  m.nonbin = false;
+#pragma unroll 4
+  for (int64_t p = p0; p < p1; ++p) {
+    const int j = P.colidx[p];
+    const double v = P.vals[p];
+    const int st = w.ost[j];
+    const double2 o = w.ovl[j];
+    const double2 base = w.A->base[j];
+    const bool isint = P.isint[j] != 0;
+    const double2 b = st == w.epoch ? o : base;
+    if (calc) addTerm(s, a, v, b.x, b.y);
+    if (md) {
+      m.nonbin |= !(isint && !dneg(base.x) && !gtc(base.y, 1.0));
       if (!gec(b.x, 0.5) && gtc(b.y, 0.5)) {
-        const double d = dabs(P.vals[p]);
-        if (dgt(d, r.maxdelta)) {
-          r.maxdelta = d;
-          r.maxdeltacol = j;
+        const double d = dabs(v);
+        if (!dlt(d, m.bbest) && dpos(d)) {
+          m.bbest = d;
+          m.bcol = j;
+        }
+      }
+      if (isNegInf(s, b.x) || isInf(s, b.y)) {
+        m.infcol = j;
+      } else {
+        const double d = dabs(v) * (b.y - b.x);
+        if (!dlt(d, m.gbest) && dpos(d)) {
+          m.gbest = d;
+          m.gcol = j;
         }
       }
     }
-    return;
   }
-  for (int64_t p = p1 - 1; p >= p0; --p) {
-    const int j = P.colidx[p];
-    const double2 b = bnd(w, j);
-    if (isNegInf(s, b.x) || isInf(s, b.y)) {
-      r.maxdelta = s.inf;
-      r.maxdeltacol = j;
-      break;
+  if (calc) {
+    r.minhi = a.minhi; r.minlo = a.minlo; r.maxhi = a.maxhi; r.maxlo = a.maxlo;
+    r.minposinf = a.minposinf; r.minneginf = a.minneginf; r.minposhuge = a.minposhuge; r.minneghuge = a.minneghuge;
+    r.maxposinf = a.maxposinf; r.maxneginf = a.maxneginf; r.maxposhuge = a.maxposhuge; r.maxneghuge = a.maxneghuge;
+    r.flags |= RS_VALID | RS_VMIN | RS_VMAX;
+    r.lastmin = r.minhi + r.minlo;
+    r.lastmax = r.maxhi + r.maxlo;
+  }
+}
+
+// recomputeMaxDelta from the pass's candidates
+__device__ __forceinline__ void laneMaxDelta(const Num& s, SeqRow& r, const MaxDeltaScan& m) {
+  r.maxdelta = 0.0;
+  if (!(r.flags & RS_NBV)) r.flags = (r.flags & ~RS_HNB) | (m.nonbin ? RS_HNB : 0u) | RS_NBV;
+  if (!(r.flags & RS_HNB)) {
+    if (m.bcol >= 0) {
+      r.maxdelta = m.bbest;
+      r.maxdeltacol = m.bcol;
     }
-    const double d = dabs(P.vals[p]) * (b.y - b.x);
-    if (dgt(d, r.maxdelta)) {
-      r.maxdelta = d;
-      r.maxdeltacol = j;
-    }
+  } else if (m.infcol >= 0) {
+    r.maxdelta = s.inf;
+    r.maxdeltacol = m.infcol;
+  } else if (m.gcol >= 0) {
+    r.maxdelta = m.gbest;
+    r.maxdeltacol = m.gcol;
   }
 }
 
@@ -987,12 +1028,15 @@ __device__ __noinline__ int laneHead(const W& w, int i, SeqRow& r) {
   const unsigned tightenmode = 1;
   // tightenBounds
   bool skip = false;
-  if (!(r.flags & RS_VALID)) laneCalc(w, i, r);
+  // the activities, and the largest delta's candidates in the same pass (used only if the tests reach it)
+  const bool calc = !(r.flags & RS_VALID), md = isInvalid(r.maxdelta);
+  MaxDeltaScan m;
+  if (calc || md) laneScan(w, i, r, calc, md, m);
   if (r.minneginf + r.minposinf + r.minneghuge + r.minposhuge > 1 &&
       r.maxneginf + r.maxposinf + r.maxneghuge + r.maxposhuge > 1)
     skip = true;
   if (!skip && !force && btOf(r.flags) >= tightenmode) skip = true;
-  if (!skip && isInvalid(r.maxdelta)) laneMaxDelta(w, i, r);
+  if (!skip && md) laneMaxDelta(s, r, m);
   if (!skip && feasZero(s, r.maxdelta)) skip = true;
   if (!skip && !isInf(s, r.maxdelta)) {
     double minact, maxact;
@@ -1146,8 +1190,9 @@ __device__ __noinline__ bool propagateTail(W& w, int i) {
 // propagateRounds: consPropLinear over the marked rows until a call changes nothing (uniform);
 // 0 fixpoint, 1 cutoff, 2 round limit.  The rows of a call are taken 32 at a time, one per lane, through laneHead;
 // walking them in order, the rows it ends are committed as they stand, a row that reaches the visit of its entries
-// is visited by the warp, and a row that finds the node infeasible is run for real.  After a visit that changed a
-// bound the next rows are taken afresh.
+// is visited by the warp, and a row that finds the node infeasible is run for real.  A bound change reaches only the
+// rows of its column (their records count the events): after one, the rows still ahead whose records changed are
+// taken afresh, and the others' outcomes stand.
 __device__ int propagateRounds(W& w, int maxrounds, int& rounds) {
   const Prob& P = w.A->P;
   rounds = 0;
@@ -1172,11 +1217,10 @@ __device__ int propagateRounds(W& w, int maxrounds, int& rounds) {
           r.flags = (r.flags & ~RS_UM) | RS_UU | RS_INUPD;
         cls = laneHead(w, i, r);
       }
-      const unsigned stop = __ballot_sync(FULL, has && cls != ROW_DONE);
       const unsigned below = (1u << w.lane) - 1u;
       int pos = 0;
-      bool fresh = false;  // a bound changed: the rows after pos are taken afresh
-      while (pos < cnt && !cut && !fresh) {
+      while (pos < cnt && !cut) {
+        const unsigned stop = __ballot_sync(FULL, has && cls != ROW_DONE);
         const unsigned rest = stop & ~((1u << pos) - 1u);
         const int q = rest ? __ffs(rest) - 1 : cnt;
         // rows [pos, q) are committed as they stand, and row q's unmark and head too when it is live
@@ -1207,7 +1251,14 @@ __device__ int propagateRounds(W& w, int maxrounds, int& rounds) {
           cut = propagateCons(w, iq);
         }
         pos = q + 1;
-        fresh = w.nchg > old;
+        if (!cut && w.nchg > old && has && w.lane > q && w.rs[i].evc != r.evc) {
+          r = loadRow(w, i);
+          wasin = (r.flags & RS_INUPD) != 0;
+          if (!((r.flags & RS_UU) || (!(r.flags & RS_MP) && !(r.flags & RS_UM))))
+            r.flags = (r.flags & ~RS_UM) | RS_UU | RS_INUPD;
+          cls = laneHead(w, i, r);
+        }
+        __syncwarp();
       }
       k += pos;
     }
