@@ -1492,7 +1492,11 @@ static int propagateNodesSeq(gbp_ctx* ctx, const double* baselb, const double* b
   if (rangedOn(ctx)) return fail(ctx, GBP_ERR_INVALID, "GBP_FLAG_SCIPORDER does not combine with GBP_FLAG_RANGEDROW");
   int rc = ensureSeqCsc(ctx);
   if (rc) return rc;
-  rc = ensureSeqSlots(ctx, nnodes);
+  // one CTA of SEQ_WARPS warps per SM: a node's logic is a long chain of dependent steps, and a warp that shares its
+  // SM sub-partition with others waits on their FP64 and memory traffic -- the batch ends with its longest node,
+  // so fewer, faster warps finish it sooner (and need fewer slots)
+  const int64_t maxwarps = (int64_t)ctx->sms * SEQ_WARPS;
+  rc = ensureSeqSlots(ctx, std::min<int64_t>(nnodes, maxwarps));
   if (rc) return rc;
   const SeqSlots& SL = ctx->seqslots;
   // every node takes a new epoch in its slot; re-zero the stamps long before a counter wraps
@@ -1549,7 +1553,7 @@ static int propagateNodesSeq(gbp_ctx* ctx, const double* baselb, const double* b
   A.S = SL;
   A.stats = ctx->d_stats;
   A.status = ctx->d_status;
-  const int64_t warps = std::min<int64_t>(SL.nslots, nnodes);
+  const int64_t warps = std::min<int64_t>(std::min<int64_t>(SL.nslots, nnodes), maxwarps);
   const int grid = (int)((warps + SEQ_WARPS - 1) / SEQ_WARPS);
   CK(launchNodesSeq(ctx->stream, grid, A));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -585,14 +585,23 @@ __device__ __forceinline__ bool sideOk(const Num& s, double side, double res) {
   return lt(s, dabs(side), 1.0) || !quotNear1(res, side, s.eps);
 }
 
-// tightenVarBounds without effects (one lane, entry k of the row in r): true if running it would change anything
-// -- recompute an activity, tighten a bound, or find the node infeasible
+// tightenVarBounds without effects (one lane, entry k of the row in r): true if running it might change anything
+// -- recompute an activity, tighten a bound, or find the node infeasible.  A true answer only sends the entry to
+// the real run, so cases it cannot settle cheaply (a zero coefficient) answer true.
+//
+// Both sides are tested as upper bounds on z = x or z = -x: a lower bound nl on x is the upper bound -nl on -x
+// over [-u, -l], and every test of tightenVarBounds on a lower bound (gt, feasGt, lbBetter, the inference) is its
+// upper-bound test on the negated values, bit for bit (negation is exact and the rules are symmetric).  The
+// candidate is then fl(num / |a|) with num = rhs - minres (z = x when a > 0) or maxres - lhs (z = x when a < 0),
+// so lanes with coefficients of either sign run the same instructions.  A candidate that does not undercut the
+// upper bound of z passes none of the tests; that is decided on the quotient before dividing.
 __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool force) {
   const Prob& P = w.A->P;
   const Num& s = w.A->s;
   const int64_t p = P.rowptr[i] + k;
   const int j = P.colidx[p];
   const double val = P.vals[p];
+  if (dmag(val) == 0) return true;
   const double lhs = P.lhs[i], rhs = P.rhs[i];
   const bool isint = P.isint[j] != 0;
   const double2 b = bnd(w, j);
@@ -605,37 +614,24 @@ __device__ bool residualWould(const W& w, int i, const SeqRow& r, int k, bool fo
   bool mint, maxt, mininf, maxinf;
   getMinAct(s, a, ra.mp, ra.mn, ra.mph, ra.mnh, ra.md, false, minres, mint, mininf);
   getMaxAct(s, a, ra.xp, ra.xn, ra.xph, ra.xnh, ra.xd, false, maxres, maxt, maxinf);
-  if (dpos(val)) {
-    if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
-      double newub = (rhs - minres) / val;
-      if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
-        // an unreliable residual is recomputed from scratch: the entry counts as a hit, run for real
-        if (updateUnreliable(s, minres, r.lastmin)) return true;
-        if (wouldInferUb(s, isint, l, u, newub, force)) return true;
-      }
-    }
-    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
-      double newlb = (lhs - maxres) / val;
-      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
-        if (updateUnreliable(s, maxres, r.lastmax)) return true;
-        if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
-      }
-    }
-  } else {
-    if (!mininf && !isInf(s, rhs) && mint && sideOk(s, rhs, minres)) {
-      double newlb = (rhs - minres) / val;
-      if (!isNegInf(s, newlb) && ((force && gt(s, newlb, l)) || (isint && feasGt(s, newlb, l)) || lbBetter(s, newlb, l, u))) {
-        if (updateUnreliable(s, minres, r.lastmin)) return true;
-        if (wouldInferLb(s, isint, l, u, newlb, force)) return true;
-      }
-    }
-    if (!maxinf && !isNegInf(s, lhs) && maxt && sideOk(s, lhs, maxres)) {
-      double newub = (lhs - maxres) / val;
-      if (!isInf(s, newub) && ((force && lt(s, newub, u)) || (isint && feasLt(s, newub, u)) || ubBetter(s, newub, l, u))) {
-        if (updateUnreliable(s, maxres, r.lastmax)) return true;
-        if (wouldInferUb(s, isint, l, u, newub, force)) return true;
-      }
-    }
+  const bool pos = dpos(val);
+  const double aval = dabs(val);
+#pragma unroll 1
+  for (int side = 0; side < 2; ++side) {
+    const bool rs = side == 0;  // the right-hand side with the minimal residual, else the left with the maximal
+    if (rs ? (mininf || isInf(s, rhs) || !mint) : (maxinf || isNegInf(s, lhs) || !maxt)) continue;
+    const double sd = rs ? rhs : lhs, res = rs ? minres : maxres;
+    if (!sideOk(s, sd, res)) continue;
+    const bool zx = rs == pos;
+    const double lz = zx ? l : -u, uz = zx ? u : -l;
+    const double num = rs ? rhs - minres : maxres - lhs;
+    if (!quotLt(num, aval, uz)) continue;
+    const double nu = num / aval;
+    if (isInf(s, nu)) continue;
+    if (!((force && lt(s, nu, uz)) || (isint && feasLt(s, nu, uz)) || ubBetter(s, nu, lz, uz))) continue;
+    // an unreliable residual is recomputed from scratch: the entry counts as a hit, run for real
+    if (updateUnreliable(s, res, rs ? r.lastmin : r.lastmax)) return true;
+    if (wouldInferUb(s, isint, lz, uz, nu, force)) return true;
   }
   return false;
 }
