@@ -43,20 +43,49 @@ def measured_peak():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def measured_traffic(nnodes, shape):
-    """DRAM bytes (read + write) of one k_nodes launch of the default node workload, from the committed one-pass ncu
-    capture (profiles/k_nodes_traffic.json), when this run is that workload; else None."""
+def measured_traffic(algo_bytes, shape):
+    """DRAM bytes (read + write) and FP64 warp-instructions of one k_nodes launch, from the committed ncu capture of a
+    small case of the same generator (profiles/k_nodes_traffic.json), scaled to this launch by its algorithmic bytes
+    (both grow with the rows, nonzeros and changes a launch processes)."""
     p = os.path.join(ROOT, "profiles", "k_nodes_traffic.json")
     try:
         with open(p) as f:
             d = json.load(f)
+        scale = algo_bytes / float(d["algorithmic_bytes"])
+    except Exception:
+        return None, None, None
+    src = {"from": "profiles/k_nodes_traffic.json", "case": d["case"], "command": d["command"],
+           "scaled_by": scale, "case_launch_shape": d["launch_shape"], "this_run_shape": list(shape)}
+    traffic = (int(d["dram_bytes_read"]) + int(d["dram_bytes_write"])) * scale
+    fp64 = float(d["fp64_warp_inst"]) * scale if "fp64_warp_inst" in d else None
+    return traffic, fp64, src
+
+
+def scip_calibration():
+    """SCIP 11's own speed on this workload against the port's, both on one x86 core of the build container
+    (profiles/cpu_calibration_x86.json, written by oracle/calibrate.py): SCIP is not built on the GPU machine, so the
+    ratio is carried over to read the port's figures as SCIP's."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "cpu_calibration_x86.json")) as f:
+            d = json.load(f)
+        return {"scip_over_port": d["scip_over_port_jacobi_1core"],
+                "scip_over_port_source": {"from": "profiles/cpu_calibration_x86.json", "machine": d["machine"],
+                                          "scip_1core": d["scip_1core"]["value"],
+                                          "port_1core": d["port_jacobi_1core"]["value"],
+                                          "command": d["command"]}}
+    except Exception:
+        return {}
+
+
+def fp64_rate():
+    """The GPU's FP64 issue rate in warp-instructions/s, measured by tests/native/fp64_issue.cu
+    (profiles/fp64_issue.json); None when absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_issue.json")) as f:
+            d = json.load(f)
+        return float(d["gpu_warp_inst_per_s"]), d
     except Exception:
         return None, None
-    if nnodes != NNODES:
-        return None, None
-    src = {"from": "profiles/k_nodes_traffic.json", "launch_shape": d["launch_shape"], "command": d["command"],
-           "this_run_shape": list(shape)}
-    return int(d["dram_bytes_read"]) + int(d["dram_bytes_write"]), src
 
 
 class ClockSampler:
@@ -332,16 +361,27 @@ def serving_workload(args):
                       "mean_batch": float(np.mean([b[1] for b in batches])) if batches else 0.0}))
 
 
-def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world):
-    """Node-fixpoints/s of the batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER) on the same workload: the rows
-    in the order consdataCompVarProp sorts them into on the base bounds, inputs resident in HBM, CUDA events around
-    each step, the L2 flushed between steps."""
+def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed):
+    """Node-fixpoints/s of the batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER), inputs resident in HBM, CUDA
+    events around each step, the L2 flushed between steps.  On the default instance the nodes start from SCIP's own
+    root fixpoint with the rows in SCIP's orders (the compact base in tests/golden/workload, whose 4,096 nodes equal
+    SCIP's results); otherwise from the same root as the Jacobi arm, with the rows in the order consdataCompVarProp
+    sorts them into on it."""
     import torch
     from scip_gb300 import gbp, instances
 
     if args.ranged:
         return None
-    order = instances.scip_row_order(inst, rlb, rub, instances.scip_var_index(inst.isint, inst.lb, inst.ub))
+    base = instances.pinned_node_base(inst, os.path.join(ROOT, "tests", "golden", "workload", "node_workload_base.npz"))
+    if base is not None:
+        rlb, rub, order = base
+        nodes = instances.node_batch(inst, rlb, rub, N, seed=seed)
+        workload = (f"SCIP's root fixpoint and row orders of this instance (tests/golden/workload/node_workload_base.npz),"
+                    f" {N} nodes drawn from that root (seed {seed}); at 4,096 nodes, seed 3, every node's result "
+                    f"equals SCIP's (tests/test_seq_gpu.py)")
+    else:
+        order = instances.scip_row_order(inst, rlb, rub, instances.scip_var_index(inst.isint, inst.lb, inst.ub))
+        workload = "the Jacobi arm's root fixpoint and nodes; rows sorted as consdataCompVarProp sorts them on it"
     p = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy, scip_order=True))
     p.upload(instances.in_order(inst, order))
     d = torch.device("cuda", dev)
@@ -381,7 +421,7 @@ def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world):
             "entries_visited": st["candidates"], "changes": st["changes"], "nodes_cut_off": st["cutoff"],
             "max_rounds": st["rounds"], "gpu_launches": int(sum(x["launches"] for x in stats)),
             "call": "gbp_propagate_nodes_device with GBP_FLAG_SCIPORDER (SCIP's own order; integer bounds and "
-                    "cutoffs equal SCIP's)"}
+                    "cutoffs equal SCIP's)", "workload": workload}
 
 
 def main():
@@ -455,8 +495,8 @@ def main():
                           "ms_per_step": 1e3 * args.nodes / v, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
                           "config": config,
-                          "cpu_baseline": {"value": v, "unit": "node-fixpoints/s", "cores": threads, "kind": "port",
-                                           "sample": sample},
+                          "cpu_baseline": dict({"value": v, "unit": "node-fixpoints/s", "cores": threads,
+                                                "kind": "port", "sample": sample}, **scip_calibration()),
                           "e2e": {"value": v, "unit": "node-fixpoints/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
@@ -548,11 +588,19 @@ def main():
     peak, peak_kind = measured_peak()
     achieved = algo / (ms / 1e3) / 1e9
     cutoffs = stats[-1]["cutoff"]
-    traffic, traffic_src = measured_traffic(N, shape) if args.family == "mip" and not args.ranged else (None, None)
+    traffic, fp64_inst, traffic_src = (measured_traffic(algo, shape) if args.family == "mip" and not args.ranged
+                                       else (None, None, None))
+    rate, _ = fp64_rate()
+    fp64_issue = None
+    if fp64_inst is not None and rate is not None:
+        ach = fp64_inst / (kern_ms / 1e3)
+        fp64_issue = {"achieved": ach, "peak": rate, "unit": "FP64 warp-instructions/s", "frac": ach / rate,
+                      "fp64_warp_inst_per_launch": fp64_inst,
+                      "peak_source": "profiles/fp64_issue.json (tests/native/fp64_issue.cu)"}
 
     # the same nodes in SCIP's own order (GBP_FLAG_SCIPORDER): rows uploaded in the order SCIP sorts them into on the
     # base domain, device-resident inputs, the same timing
-    scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world)
+    scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed=3 + rank)
 
     # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
@@ -616,7 +664,7 @@ def main():
             "gpu_launches": int(sum(st["launches"] for st in stats)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "traffic_source": traffic_src, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_step": algo, "kernel": "k_nodes"},
+                         "algorithmic_bytes_per_step": algo, "kernel": "k_nodes", "fp64_issue": fp64_issue},
             "clocks": clk,
             "nnz_per_s": nnz / (ms / 1e3), "kernel_ms": kern_ms, "wall_s": wall,
             "nodes_cut_off": int(cutoffs), "max_rounds": int(stats[-1]["rounds"]),
@@ -633,8 +681,11 @@ def main():
             orc.build()
             par = orc.params(args.maxeasy, ranged=args.ranged)
             cpu_v, sample = CpuArm(inst, rlb, rub, nodes, par, os.cpu_count() or 1).plan(min_wall_s=1.0).run()
+            one_v, one_sample = CpuArm(inst, rlb, rub, nodes, par, 1).plan(budget_s=8.0).run()
             line["cpu_baseline"] = {"value": cpu_v, "unit": "node-fixpoints/s", "cores": os.cpu_count() or 1,
-                                    "kind": "port", "sample": sample}
+                                    "kind": "port", "sample": sample,
+                                    "one_core": {"value": one_v, "sample": one_sample}}
+            line["cpu_baseline"].update(scip_calibration())
         print(json.dumps(line))
     prop.close()
     if world > 1:

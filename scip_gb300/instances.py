@@ -504,6 +504,35 @@ def scip_row_order(inst: "Instance", glb: np.ndarray, gub: np.ndarray,
     return np.lexsort((vidx[col], key, group, rows)).astype(np.int32)
 
 
+def pinned_node_base(inst: "Instance", path: str):
+    """SCIP's root fixpoint and row orders of an instance from a compact file (tests/golden/make_golden.py,
+    save_node_workload_base): returns (root lb, root ub, order) with order as scip_row_order returns it, or None
+    when the file is absent or belongs to another instance."""
+    import hashlib
+    import os
+
+    if not os.path.exists(path):
+        return None
+    with np.load(path) as f:
+        z = dict(f)
+    h = hashlib.sha256()
+    for a in (inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, inst.lb, inst.ub, inst.isint):
+        a = np.ascontiguousarray(a)
+        h.update((a + 0.0 if a.dtype.kind == "f" else a).tobytes())
+    if h.hexdigest() != str(z["instance_sha256"]):
+        return None
+    lb, ub = inst.lb.copy(), inst.ub.copy()
+    lb[z["root_cols"]] = z["root_lb"]
+    ub[z["root_cols"]] = z["root_ub"]
+    order = scip_row_order(inst, inst.lb, inst.ub, scip_var_index(inst.isint, inst.lb, inst.ub))
+    at = 0
+    for i in z["order_rows"]:
+        p0, p1 = int(inst.rowptr[i]), int(inst.rowptr[i + 1])
+        order[p0:p1] = p0 + z["order_pos"][at:at + p1 - p0].astype(np.int64)
+        at += p1 - p0
+    return lb, ub, order
+
+
 def in_order(inst: "Instance", order: np.ndarray) -> "Instance":
     """The instance with each row's entries rearranged by order (CSR positions, as scip_row_order returns)."""
     return Instance(inst.rowptr, inst.colidx[order], inst.vals[order], inst.lhs, inst.rhs, inst.lb, inst.ub,

@@ -169,6 +169,36 @@ def save_node_workload():
           f"{os.path.getsize(path) // 1024} KiB")
 
 
+def save_node_workload_base():
+    """SCIP's root fixpoint and row orders of the batched-node workload in compact form, for the SCIP-order arm of
+    bench.py (which starts its nodes from them, with no oracle): the columns the root moved, and the rows whose
+    order differs from the host sort on the instance's own bounds (instances.scip_row_order), with their orders.
+    Computed by the oracle's restatement of SCIP's order and checked against the digests of SCIP's own results in
+    node_workload_scip.npz."""
+    inst = instances.node_mip(seed=2)
+    vidx = instances.scip_var_index(inst.isint, inst.lb, inst.ub)
+    lb, ub, r, order = oracle.Oracle(inst, vidx).propagate_seq(inst.lb, inst.ub, oracle.params(0.0))
+    with np.load(os.path.join(HERE, "workload", "node_workload_scip.npz")) as f:
+        z = dict(f)
+    assert not r.cutoff and digest(lb, ub) == str(z["root_sha256"])
+    deleted = np.zeros(inst.m, dtype=bool)
+    deleted[z["rowdel"]] = True
+    live = ~np.repeat(deleted, np.diff(inst.rowptr))
+    assert digest(order[live]) == str(z["order_sha256"])
+    host = instances.scip_row_order(inst, inst.lb, inst.ub, vidx)
+    row_of = np.repeat(np.arange(inst.m, dtype=np.int64), np.diff(inst.rowptr))
+    rows = np.unique(row_of[order != host]).astype(np.int32)
+    pos = np.concatenate([order[inst.rowptr[i]:inst.rowptr[i + 1]] - inst.rowptr[i] for i in rows]).astype(np.int16)
+    cols = np.nonzero((lb != inst.lb) | (ub != inst.ub))[0].astype(np.int32)
+    out = {"instance_sha256": digest(inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, inst.lb, inst.ub,
+                                     inst.isint),
+           "root_sha256": z["root_sha256"], "order_sha256": z["order_sha256"],
+           "root_cols": cols, "root_lb": lb[cols], "root_ub": ub[cols], "order_rows": rows, "order_pos": pos}
+    path = os.path.join(HERE, "workload", "node_workload_base.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {len(cols)} root columns, {len(rows)} reordered rows, {os.path.getsize(path) // 1024} KiB")
+
+
 def ranged_cases():
     return {
         "gcd_rows_indep": lambda: instances.gcd_rows(np.random.default_rng(np.random.PCG64(30)), 3000, 60000,
@@ -208,9 +238,13 @@ def main(names):
     all_cases = cases()
     ranged = ranged_cases()
     for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs",
-                                                                             "node_workload_scip"]:
+                                                                             "node_workload_scip",
+                                                                             "node_workload_base"]:
         if name == "node_workload_scip":
             save_node_workload()
+            continue
+        if name == "node_workload_base":
+            save_node_workload_base()
             continue
         if name == "ranged/tiny_cutoffs":
             save_tiny_cutoffs()

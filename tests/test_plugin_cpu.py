@@ -29,6 +29,8 @@ def _has_gpu():
 def driver(tmp_path_factory, oracle_mod):
     if not os.path.exists(LIBSCIP):
         pytest.skip("SCIP build (oracle/_ref) not present")
+    if not oracle_mod.REFDIR or not os.path.exists(os.path.join(oracle_mod.REFDIR, "src", "scip", "scip.h")):
+        pytest.skip("SCIP headers not present (REFDIR names the SCIP source tree)")
     build_libgbp()
     out = tmp_path_factory.mktemp("plugin")
     exe = str(out / "plugin_driver")
@@ -81,6 +83,8 @@ def solve_driver(tmp_path_factory, oracle_mod):
     the plugin's SCIP side -- change log write-back, conflict analysis of cutoffs, reasons -- runs inside SCIP."""
     if not os.path.exists(LIBSCIP):
         pytest.skip("SCIP build (oracle/_ref) not present")
+    if not oracle_mod.REFDIR or not os.path.exists(os.path.join(oracle_mod.REFDIR, "src", "scip", "scip.h")):
+        pytest.skip("SCIP headers not present (REFDIR names the SCIP source tree)")
     out = tmp_path_factory.mktemp("solve")
     exe = str(out / "solve_driver")
     src = [os.path.join(ROOT, "tests", "plugin", "solve_driver.c"),

@@ -96,3 +96,23 @@ def test_scip_variable_index():
     assert set(idx[[1, 4]].tolist()) == {0, 1}
     assert idx[3] == 2
     assert set(idx[[0, 2, 5]].tolist()) == {3, 4, 5}
+
+
+def test_pinned_node_base_reproduces_scips_root_and_orders():
+    """The compact base the bench's SCIP-order arm starts its nodes from (tests/golden/workload/
+    node_workload_base.npz) gives SCIP's root bounds and row orders of the batched-node workload exactly."""
+    import os
+
+    from scip_gb300 import instances
+
+    inst = instances.node_mip(seed=2)
+    lb, ub, order = instances.pinned_node_base(inst, os.path.join(G.GOLDEN, "workload", "node_workload_base.npz"))
+    with np.load(os.path.join(G.GOLDEN, "workload", "node_workload_scip.npz")) as f:
+        z = dict(f)
+    assert G._digest(lb, ub) == str(z["root_sha256"])
+    deleted = np.zeros(inst.m, dtype=bool)
+    deleted[z["rowdel"]] = True
+    live = ~np.repeat(deleted, np.diff(inst.rowptr))
+    assert G._digest(order[live]) == str(z["order_sha256"])
+    nodes = instances.node_batch(inst, lb, ub, 4096, seed=3)
+    assert G._digest(nodes.ptr, nodes.col, nodes.lb, nodes.ub) == str(z["nodes_sha256"])
