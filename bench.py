@@ -416,7 +416,10 @@ def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed):
     ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
     p.close()
     st = stats[-1]
-    return {"value": world * N / (ms / 1e3), "unit": "node-fixpoints/s", "ms_per_step": ms, "steps": steps,
+    from scip_gb300 import replicas
+
+    ms = replicas.max_over_ranks(ms, device=d)
+    return {"value": replicas.aggregate_rate(N, world, ms), "unit": "node-fixpoints/s", "ms_per_step": ms, "steps": steps,
             "kernel_ms": float(np.mean([x["kernel_ms"] for x in stats])), "rows_processed": st["rows"],
             "entries_visited": st["candidates"], "changes": st["changes"], "nodes_cut_off": st["cutoff"],
             "max_rounds": st["rounds"], "gpu_launches": int(sum(x["launches"] for x in stats)),
@@ -452,13 +455,14 @@ def main():
     if args.workload != "nodes":
         return other_workload(args)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from scip_gb300 import replicas
+
+    rank, world, local_rank = replicas.rank_env()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from scip_gb300 import instances
 
     size = f"{args.rows:,} x {2 * args.rows:,}"
-    config = {"workload": f"batched B&B nodes: {size} rows/cols, ~4.5M nnz, {args.nodes:,} nodes fixing 1-64 "
+    config = {"workload": f"batched B&B nodes: {size} rows/cols, ~{22.5 * args.rows / 1e6:.2f}M nnz, {args.nodes:,} nodes fixing 1-64 "
                           "integer columns each, every node to fixpoint" if args.family == "mip" else
                           f"batched B&B nodes: {size} gcd rows (3..8 entries, 1 % 65..200; half equations), "
                           f"{args.nodes:,} nodes fixing 1-64 integer columns each, every node to fixpoint",
@@ -508,14 +512,14 @@ def main():
     build_libgbp()
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = local_rank
     torch.cuda.set_device(dev)
 
     inst = build_workload(family=args.family, m=args.rows, n=2 * args.rows)
     prop = gbp.Propagator(dev, params=gbp.default_params(maxeasy=args.maxeasy, ranged=args.ranged))
     prop.upload(inst)
     rlb, rub, rcut, rres = prop.propagate(inst.lb, inst.ub)
-    nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=3 + rank)
+    nodes = instances.node_batch(inst, rlb, rub, args.nodes, seed=replicas.node_seed(3, rank))
     N = nodes.nnodes
     avg_col_len = inst.nnz / inst.n
 
@@ -573,13 +577,11 @@ def main():
     wall = time.perf_counter() - t_wall
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = float(np.mean(step_ms))
+    ms = replicas.max_over_ranks(ms, device=d)  # the slowest replica sets the step time
     if world > 1:
-        t = torch.tensor([ms], device=d)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.barrier()
-        ms = float(t.item())
     clk = clocks.stop()
-    value = world * N / (ms / 1e3)
+    value = replicas.aggregate_rate(N, world, ms)
     kern_ms = float(np.mean([s["kernel_ms"] for s in stats]))
     rows = stats[-1]["rows"]
     nnz = stats[-1]["nnz"]
@@ -600,7 +602,7 @@ def main():
 
     # the same nodes in SCIP's own order (GBP_FLAG_SCIPORDER): rows uploaded in the order SCIP sorts them into on the
     # base domain, device-resident inputs, the same timing
-    scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed=3 + rank)
+    scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed=replicas.node_seed(3, rank))
 
     # e2e through the host-pointer C ABI (pinned host buffers), copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
@@ -620,7 +622,7 @@ def main():
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_ms.append(1e3 * (t1 - t0))
-    e2e_v = world * N / (np.mean(e2e_ms) / 1e3)
+    e2e_v = replicas.aggregate_rate(N, world, replicas.max_over_ranks(float(np.mean(e2e_ms)), device=d))
     h2d = 16 * inst.n + 8 * (N + 1) + 20 * len(nodes.col)
     used = int(r_host.n[r_host.n > 0].sum())
     d2h = N * (1 + 4 + 8 + 4) + 20 * used
