@@ -245,23 +245,77 @@ def node_mip(seed: int = 2, m: int = 200_000, n: int = 400_000) -> Instance:
 
 
 def node_batch(inst: Instance, lb: np.ndarray, ub: np.ndarray, nnodes: int, seed: int = 3,
-               kmax: int = 64) -> NodeBatch:
-    """Nodes fixing 1..kmax integer columns (count log-uniform) to random values inside [lb, ub]."""
+               kmax: int = 64, tight: float = 0.0) -> NodeBatch:
+    """Nodes fixing 1..kmax integer columns (count log-uniform) to random values inside [lb, ub].
+
+    tight > 0: that fraction of the nodes first fixes, against one row whose right-hand side the root fixpoint
+    leaves reachable and whose integer columns can pass it, the row's integer columns one by one (in random order)
+    at the bound that raises the row's minimal activity, up to the first fixing that carries it past the side -- a
+    dive that branches one row into infeasibility -- and then makes the random fixings.  On the 200,000 x 400,000
+    workload tight = 0.15 cuts off about 15 % of the nodes (0.4 % without).  The default (tight = 0) draws exactly
+    the stream of the plain generator."""
     rng = np.random.default_rng(np.random.PCG64(seed))
     intcols = np.flatnonzero((inst.isint == 1) & (ub > lb) & (ub < INF) & (lb > -INF))
     if intcols.shape[0] == 0:
         raise ValueError("no unfixed finite integer columns")
     kmax = min(kmax, intcols.shape[0])
     ks = log_uniform_count(rng, kmax, nnodes)
-    ptr = np.zeros(nnodes + 1, dtype=np.int64)
-    np.cumsum(ks, out=ptr[1:])
-    cols = np.empty(int(ptr[-1]), dtype=np.int32)
+    chosen = []
     for k in range(nnodes):
-        cols[ptr[k]:ptr[k + 1]] = np.sort(rng.choice(intcols, size=int(ks[k]), replace=False))
-    lo = lb[cols]
-    hi = ub[cols]
-    v = np.floor(lo + rng.random(cols.shape[0]) * (hi - lo + 1.0))
-    v = np.minimum(v, hi)
+        chosen.append(np.sort(rng.choice(intcols, size=int(ks[k]), replace=False)))
+    lo_all, hi_all = lb, ub
+    pushed = [None] * nnodes
+    if tight > 0.0:
+        trng = np.random.default_rng(np.random.PCG64(seed + 7919))
+        fin = np.isfinite(lb) & np.isfinite(ub) & (np.abs(lb) < INF) & (np.abs(ub) < INF)
+        a = inst.vals
+        c = inst.colidx
+        lo_c = np.where(a > 0, lb[c], ub[c])
+        minact = np.add.reduceat(a * np.where(fin[c], lo_c, 0.0), inst.rowptr[:-1].astype(np.int64))
+        rowfin = np.add.reduceat((~fin[c]).astype(np.int64), inst.rowptr[:-1].astype(np.int64)) == 0
+        movable = (inst.isint[c] == 1) & (ub[c] > lb[c]) & fin[c]
+        raise_int = np.add.reduceat(np.where(movable, np.abs(a) * (ub[c] - lb[c]), 0.0),
+                                    inst.rowptr[:-1].astype(np.int64))
+        cand = np.flatnonzero(rowfin & (inst.rhs < INF) & (np.diff(inst.rowptr) > 0) & (minact <= inst.rhs)
+                              & (minact + raise_int > inst.rhs))
+        for k in range(nnodes):
+            if trng.random() >= tight or cand.shape[0] == 0:
+                continue
+            i = int(cand[trng.integers(cand.shape[0])])
+            p0, p1 = int(inst.rowptr[i]), int(inst.rowptr[i + 1])
+            act = float(minact[i])
+            fix_c, fix_v = [], []
+            for p in p0 + trng.permutation(p1 - p0):
+                j = int(c[p])
+                if inst.isint[j] != 1 or not (ub[j] > lb[j]):
+                    continue
+                v = ub[j] if a[p] > 0 else lb[j]
+                step = a[p] * (v - (lb[j] if a[p] > 0 else ub[j]))
+                act += step
+                fix_c.append(j)
+                fix_v.append(v)
+                if act > inst.rhs[i]:
+                    break
+            if fix_c:
+                pushed[k] = (np.array(fix_c, dtype=np.int64), np.array(fix_v))
+    ptr = np.zeros(nnodes + 1, dtype=np.int64)
+    cols_l, vals_l = [], []
+    for k in range(nnodes):
+        base = chosen[k]
+        lo = lo_all[base]
+        hi = hi_all[base]
+        v = np.minimum(np.floor(lo + rng.random(base.shape[0]) * (hi - lo + 1.0)), hi)
+        if pushed[k] is not None:
+            pc, pv = pushed[k]
+            keep = ~np.isin(base, pc)
+            base, v = np.concatenate([pc, base[keep]]), np.concatenate([pv, v[keep]])
+            o = np.argsort(base, kind="stable")
+            base, v = base[o], v[o]
+        cols_l.append(base)
+        vals_l.append(v)
+        ptr[k + 1] = ptr[k] + base.shape[0]
+    cols = np.concatenate(cols_l).astype(np.int32) if cols_l else np.zeros(0, np.int32)
+    v = np.concatenate(vals_l) if vals_l else np.zeros(0)
     return NodeBatch(ptr, cols, v.copy(), v.copy())
 
 

@@ -52,3 +52,30 @@ def test_oracle_fixpoint_keeps_the_feasible_point(oracle_mod, make):
     assert not r.cutoff
     tol = 1e-6 * np.maximum(1.0, np.abs(inst.x0))
     assert (inst.x0 >= lb - tol).all() and (inst.x0 <= ub + tol).all()
+
+
+def test_node_generator_tight_option_cuts_off_about_15_percent(oracle_mod):
+    """node_batch(tight=0.15) on the 200,000 x 400,000 workload: about 15 % of the nodes are infeasible (the
+    workload's stated rate), against about 0.5 % for the plain generator, whose stream the option leaves alone."""
+    import os
+
+    import numpy as np
+
+    from scip_gb300 import instances
+
+    inst = instances.node_mip(seed=2)
+    o = oracle_mod.Oracle(inst)
+    par = oracle_mod.params(0.0)
+    rlb, rub, _ = o.propagate(inst.lb, inst.ub, par)
+    plain = instances.node_batch(inst, rlb, rub, 4096, seed=3)
+    again = instances.node_batch(inst, rlb, rub, 4096, seed=3, tight=0.0)
+    assert np.array_equal(plain.ptr, again.ptr) and np.array_equal(plain.col, again.col)
+    assert np.array_equal(plain.lb, again.lb)
+    tight = instances.node_batch(inst, rlb, rub, 4096, seed=3, tight=0.15)
+    for k in range(tight.nnodes):  # every node names a column once, fixes it inside the root domain
+        c = tight.col[tight.ptr[k]:tight.ptr[k + 1]]
+        assert np.all(np.diff(c) > 0)
+    assert np.all(tight.lb >= rlb[tight.col]) and np.all(tight.ub <= rub[tight.col])
+    rate = o.propagate_nodes(rlb, rub, tight, par, cap=1, nthreads=os.cpu_count() or 1)["cutoff"].mean()
+    base = o.propagate_nodes(rlb, rub, plain, par, cap=1, nthreads=os.cpu_count() or 1)["cutoff"].mean()
+    assert 0.12 <= rate <= 0.18 and base < 0.02
