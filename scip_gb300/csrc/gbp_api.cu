@@ -22,6 +22,7 @@ struct gbp_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int sms = 0;
+  int coop_grid = -1;  // blocks of the cooperative all-rounds kernel (-1 not yet known, 0 unavailable)
   gbp_params par{};
   Num num{};
   std::string err;
@@ -118,6 +119,23 @@ struct gbp_ctx {
   // while-node repeats rows -> apply -> advance until the frontier is empty, cut off or at the round cap
   LoopState* d_state = nullptr;
   LoopState* h_state = nullptr;  // pinned
+
+  // gbp_propagate_changes in one cooperative launch: per-column first-move stamps and the moved log (n entries),
+  // the changes in (device and pinned host), the header and moved columns out (device and pinned host)
+  int sparse_grid = -1;
+  int* d_mstamp = nullptr;
+  int64_t mcap = 0;  // columns the stamps and the moved log hold
+  int mepoch = 0;
+  int* d_mcount = nullptr;
+  int32_t* d_mcol = nullptr;
+  double* d_mlb = nullptr;
+  double* d_mub = nullptr;
+  char* d_sin = nullptr;
+  char* h_sin = nullptr;
+  size_t sin_bytes = 0;
+  char* d_sout = nullptr;
+  char* h_sout = nullptr;
+  int64_t sout_cap = 0;
   cudaGraph_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool graph_failed = false;
@@ -345,6 +363,13 @@ int gbp_destroy(gbp_ctx* ctx) {
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
   if (ctx->d_state) cudaFree(ctx->d_state);
   if (ctx->h_state) cudaFreeHost(ctx->h_state);
+  {
+    void* dp[] = {ctx->d_mstamp, ctx->d_mcount, ctx->d_mcol, ctx->d_mlb, ctx->d_mub, ctx->d_sin, ctx->d_sout};
+    for (void* p : dp)
+      if (p) cudaFree(p);
+    if (ctx->h_sin) cudaFreeHost(ctx->h_sin);
+    if (ctx->h_sout) cudaFreeHost(ctx->h_sout);
+  }
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -563,6 +588,21 @@ static int nextStamp(gbp_ctx* ctx) {
   return ++ctx->stamp;
 }
 
+// blocks of the cooperative all-rounds kernel: every co-resident block (0: cooperative launches unavailable)
+static int coopGrid(gbp_ctx* ctx) {
+  if (ctx->coop_grid < 0) {
+    int ok = 0, per = 0;
+    if (cudaDeviceGetAttribute(&ok, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !ok ||
+        plainCoopOccupancy(&per) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      ctx->coop_grid = 0;
+    } else {
+      ctx->coop_grid = per * ctx->sms;
+    }
+  }
+  return ctx->coop_grid;
+}
+
 static int buildGraph(gbp_ctx* ctx, int mode) {
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
@@ -695,7 +735,15 @@ static int propagateGraph(gbp_ctx* ctx, double* lb, double* ub, int64_t nseed, c
     CK(launchSeed(ctx->stream, gridFor(ctx, nseed), P, lb, ub, nseed, d_seedcols, d_oldlb, d_oldub, F, seedstamp));
     ++launches;
   }
-  if (nseed != 0) {
+  if (nseed > 0 && coopGrid(ctx) > 0) {
+    // a seeded call: all rounds in one cooperative launch (the graph's per-kernel costs dominate small frontiers)
+    Cands C = plainCands(ctx);
+    C.ntouched = &ctx->d_state->ntouched;
+    const ListSet L{{ctx->d_list[0], ctx->d_list[1], ctx->d_allrows}, ctx->d_rowstamp, (int)ctx->m};
+    CK(launchPlainCoop(ctx->stream, coopGrid(ctx), ctx->num, devProb(ctx, ctx->instmode), C, L, ctx->d_state,
+                       ctx->d_stats));
+    ++launches;
+  } else if (nseed != 0) {
     CK(cudaGraphLaunch(ctx->gexec[mode], ctx->stream));
     ++launches;
   }
@@ -940,6 +988,169 @@ static int ensureSparseBufs(gbp_ctx* ctx, int64_t nchg, int64_t cap) {
   return ensureSeedBuf(ctx, std::max<int64_t>(nchg, 1));
 }
 
+static int sparseGrid(gbp_ctx* ctx) {
+  if (ctx->sparse_grid < 0) {
+    int ok = 0, per = 0;
+    if (cudaDeviceGetAttribute(&ok, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !ok ||
+        sparseCoopOccupancy(&per) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      ctx->sparse_grid = 0;
+    } else {
+      ctx->sparse_grid = per * ctx->sms;
+    }
+  }
+  return ctx->sparse_grid;
+}
+
+// gbp_propagate_changes as one copy in, one cooperative launch (k_sparse_coop) and one copy out: the same changes,
+// seeds, rounds and moved-column report as the multi-launch path below, without its snapshot of every bound
+static int propagateChangesCoop(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const double* newlb,
+                                const double* newub, const double* seedlb, const double* seedub, int64_t cap,
+                                int64_t* nout, int32_t* outcols, double* outlb, double* outub, int32_t* cutoff,
+                                gbp_result* res) {
+  const int64_t n = ctx->n;
+  if (!ctx->d_mcount) CK(cudaMalloc(&ctx->d_mcount, sizeof(int)));
+  if (n > ctx->mcap) {  // sized by the problem's columns: a later, larger upload grows them
+    void* dp[] = {ctx->d_mstamp, ctx->d_mcol, ctx->d_mlb, ctx->d_mub};
+    for (void* q : dp)
+      if (q) cudaFree(q);
+    ctx->d_mstamp = nullptr;
+    ctx->d_mcol = nullptr;
+    ctx->d_mlb = ctx->d_mub = nullptr;
+    ctx->mcap = 0;
+    CK(cudaMalloc(&ctx->d_mstamp, (size_t)n * sizeof(int)));
+    CK(cudaMemsetAsync(ctx->d_mstamp, 0, (size_t)n * sizeof(int), ctx->stream));
+    CK(cudaMalloc(&ctx->d_mcol, (size_t)n * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_mlb, (size_t)n * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_mub, (size_t)n * sizeof(double)));
+    ctx->mcap = n;
+    ctx->mepoch = 0;
+  }
+  const size_t inb = (size_t)nchg * (4 * sizeof(double) + sizeof(int32_t));
+  if (inb > ctx->sin_bytes) {
+    if (ctx->d_sin) cudaFree(ctx->d_sin);
+    if (ctx->h_sin) cudaFreeHost(ctx->h_sin);
+    ctx->d_sin = ctx->h_sin = nullptr;
+    ctx->sin_bytes = 0;
+    const size_t want = std::max<size_t>(inb, 64 << 10);
+    CK(cudaMalloc(&ctx->d_sin, want));
+    CK(cudaMallocHost(&ctx->h_sin, want));
+    ctx->sin_bytes = want;
+  }
+  const int64_t outcap = std::max<int64_t>(cap, 1);
+  if (outcap > ctx->sout_cap) {
+    if (ctx->d_sout) cudaFree(ctx->d_sout);
+    if (ctx->h_sout) cudaFreeHost(ctx->h_sout);
+    ctx->d_sout = ctx->h_sout = nullptr;
+    ctx->sout_cap = 0;
+    const size_t bytes = SPARSE_HEADER + (size_t)outcap * sizeof(SparseOut);
+    CK(cudaMalloc(&ctx->d_sout, bytes));
+    CK(cudaMallocHost(&ctx->h_sout, bytes));
+    ctx->sout_cap = outcap;
+  }
+  // the changes: lb, ub, seed (or scratch for the replaced bounds) lb, ub, columns -- one copy
+  double* hd = (double*)ctx->h_sin;
+  if (nchg > 0) {
+    std::memcpy(hd, newlb, nchg * sizeof(double));
+    std::memcpy(hd + nchg, newub, nchg * sizeof(double));
+    if (seedlb) {
+      std::memcpy(hd + 2 * nchg, seedlb, nchg * sizeof(double));
+      std::memcpy(hd + 3 * nchg, seedub, nchg * sizeof(double));
+    }
+    std::memcpy(hd + 4 * nchg, cols, nchg * sizeof(int32_t));
+    CK(cudaMemcpyAsync(ctx->d_sin, ctx->h_sin, inb, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (++ctx->mepoch >= 0x7ffffff0) {
+    if (ctx->mcap > 0) CK(cudaMemsetAsync(ctx->d_mstamp, 0, (size_t)ctx->mcap * sizeof(int), ctx->stream));
+    ctx->mepoch = 1;
+  }
+  const int maxrounds = ctx->par.maxrounds > 0 ? ctx->par.maxrounds : 1000000;
+  if ((int64_t)ctx->stamp > (int64_t)0x7fffffff - maxrounds - 16) {
+    CK(cudaMemsetAsync(ctx->d_rowstamp, 0, (size_t)std::max<int64_t>(ctx->m, 1) * sizeof(int), ctx->stream));
+    ctx->stamp = 0;
+  }
+  SparseArgs A{};
+  A.s = ctx->num;
+  A.P = devProb(ctx, false);
+  A.C = plainCands(ctx);
+  A.C.ntouched = &ctx->d_state->ntouched;
+  A.L = ListSet{{ctx->d_list[0], ctx->d_list[1], ctx->d_allrows}, ctx->d_rowstamp, (int)ctx->m};
+  A.S = ctx->d_state;
+  std::memset(&A.init, 0, sizeof(A.init));
+  A.init.maxrounds = maxrounds;
+  A.init.lb = ctx->d_lb;
+  A.init.ub = ctx->d_ub;
+  A.init.log = ctx->log;
+  A.seedstamp = ++ctx->stamp;
+  A.init.stamp = ++ctx->stamp;
+  A.stats = ctx->d_stats;
+  A.lb = ctx->d_lb;
+  A.ub = ctx->d_ub;
+  A.nchg = nchg;
+  double* dd = (double*)ctx->d_sin;
+  A.nlb = dd;
+  A.nub = dd + nchg;
+  A.oldlb = dd + 2 * nchg;
+  A.oldub = dd + 3 * nchg;
+  A.cols = (const int32_t*)(dd + 4 * nchg);
+  A.keepold = seedlb != nullptr;
+  A.moved = MovedLog{ctx->d_mstamp, ctx->mepoch, ctx->d_mcount, ctx->d_mcol, ctx->d_mlb, ctx->d_mub};
+  A.cap = cap;
+  A.header = (int*)ctx->d_sout;
+  A.out = (SparseOut*)(ctx->d_sout + SPARSE_HEADER);
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launchSparseCoop(ctx->stream, sparseGrid(ctx), A));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  // the header and a first stretch of moved columns in one copy; the rest (rare) in a second
+  const int64_t first = std::min<int64_t>(cap, 2048);
+  CK(cudaMemcpyAsync(ctx->h_sout, ctx->d_sout, SPARSE_HEADER + (size_t)first * sizeof(SparseOut),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int* h = (const int*)ctx->h_sout;
+  const unsigned long long* st = (const unsigned long long*)(ctx->h_sout + 8 * sizeof(int));
+  const bool cut = h[0] != 0;
+  const int status = cut ? 1 : (h[1] == 2 ? 2 : 0);
+  const int64_t cnt = h[4];
+  ctx->stamp = std::max(ctx->stamp, h[3]);
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->cutoff = cut ? 1 : 0;
+    res->rounds = h[2];
+    res->status = status;
+    res->launches = 1;
+    res->rows = (int64_t)st[0];
+    res->nnz = (int64_t)st[1];
+    res->candidates = (int64_t)st[2];
+    res->changes = (int64_t)st[3];
+    res->live_rows = (int64_t)st[6];
+    res->kernel_ms = ms;
+  }
+  const int rc = status == 2 ? GBP_ERR_LIMIT : GBP_OK;
+  if (cut) {  // the kernel put the bounds back to the caller's changes
+    *cutoff = 1;
+    return rc;
+  }
+  *nout = cnt;
+  if (cnt > cap) return fail(ctx, GBP_ERR_OVERFLOW, "moved-column arrays too small (nout is the count needed)");
+  const SparseOut* o = (const SparseOut*)(ctx->h_sout + SPARSE_HEADER);
+  if (cnt > first) {
+    CK(cudaMemcpyAsync(ctx->h_sout + SPARSE_HEADER + (size_t)first * sizeof(SparseOut),
+                       ctx->d_sout + SPARSE_HEADER + (size_t)first * sizeof(SparseOut),
+                       (size_t)(cnt - first) * sizeof(SparseOut), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  std::vector<int32_t> idx((size_t)cnt);
+  for (int64_t q = 0; q < cnt; ++q) idx[q] = (int32_t)q;
+  std::sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return o[a].col < o[b].col; });
+  for (int64_t q = 0; q < cnt; ++q) {
+    outcols[q] = o[idx[q]].col;
+    outlb[q] = o[idx[q]].lb;
+    outub[q] = o[idx[q]].ub;
+  }
+  return rc;
+}
+
 int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const double* newlb, const double* newub,
                           const double* seedlb, const double* seedub, int64_t cap, int64_t* nout, int32_t* outcols,
                           double* outlb, double* outub, int32_t* cutoff, gbp_result* res) {
@@ -961,6 +1172,9 @@ int gbp_propagate_changes(gbp_ctx* ctx, int64_t nchg, const int32_t* cols, const
     }
   }
   CK(cudaSetDevice(ctx->device));
+  if (!rangedOn(ctx) && !(ctx->par.flags & GBP_FLAG_HOSTLOOP) && sparseGrid(ctx) > 0)
+    return propagateChangesCoop(ctx, nchg, cols, newlb, newub, seedlb, seedub, cap, nout, outcols, outlb, outub,
+                                cutoff, res);
   int rc = ensureSparseBufs(ctx, nchg, cap);
   if (rc) return rc;
   const int64_t n = ctx->n;

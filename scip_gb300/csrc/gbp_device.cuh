@@ -137,9 +137,19 @@ struct LoopState {
   int maxrounds;
   int stamp;      // row stamp of the list being filled
   int status;     // 2: round limit reached
+  int more;       // the cooperative loop: another round follows
   double* lb;
   double* ub;
   ChangeLog log;
+};
+// the first move of each column in a sparse call (stamp[j] == epoch once recorded) and its bounds before it
+struct MovedLog {
+  int* stamp = nullptr;
+  int epoch = 0;
+  int* count = nullptr;
+  int32_t* col = nullptr;
+  double* lb = nullptr;
+  double* ub = nullptr;
 };
 struct ListSet {
   int* list[3];

@@ -242,6 +242,42 @@ cudaError_t launchCheckBlocks(cudaStream_t st, int grid, int64_t m, const int64_
                               const int32_t* rowinst, const int32_t* colinst, int* bad);
 // kernels of the graph-driven loop: 0 rows (short), 1 rows (long), 2 apply, 3 advance
 const void* graphKernel(int which);
+struct SparseOut {
+  int32_t col, pad;
+  double lb, ub;
+};
+// gbp_propagate_changes in one cooperative launch (k_sparse_coop).  Header (SPARSE_HEADER bytes): int cutoff, status,
+// rounds, last row stamp, moved columns, 3 unused; then the 8 statistics counters; then the moved columns.
+constexpr size_t SPARSE_HEADER = 8 * sizeof(int) + 8 * sizeof(unsigned long long);
+struct SparseArgs {
+  Num s;
+  Prob P;
+  Cands C;
+  ListSet L;
+  LoopState* S;
+  LoopState init;  // the loop state the call starts from (its log, bounds, stamps and round limit)
+  unsigned long long* stats;
+  double* lb;
+  double* ub;
+  int64_t nchg;
+  const int32_t* cols;
+  const double* nlb;
+  const double* nub;
+  double* oldlb;  // the bounds each change replaces (filled unless keepold: then the caller's seed bounds)
+  double* oldub;
+  int keepold;
+  int seedstamp;
+  MovedLog moved;
+  int64_t cap;
+  SparseOut* out;  // the moved columns with their bounds, right after the header
+  int* header;
+};
+cudaError_t launchSparseCoop(cudaStream_t st, int grid, const SparseArgs& A);
+cudaError_t sparseCoopOccupancy(int* blocksPerSm);
+// all rounds of a seeded plain call in one cooperative launch (grid <= co-resident blocks)
+cudaError_t launchPlainCoop(cudaStream_t st, int grid, const Num& s, const Prob& P, const Cands& C, const ListSet& L,
+                            LoopState* S, unsigned long long* stats);
+cudaError_t plainCoopOccupancy(int* blocksPerSm);
 constexpr int ROW_THREADS_G = 128;
 cudaError_t columnPointers(cudaStream_t st, const unsigned long long* count, unsigned long long* colptr, int64_t n);
 

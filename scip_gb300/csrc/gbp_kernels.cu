@@ -8,9 +8,13 @@
 //   k_nodes       persistent; each CTA takes branch-and-bound nodes off a queue and runs a node's whole
 //                 fixpoint with CTA-wide barriers between the phases of a round.  A node's bounds are the
 //                 shared base vector plus a per-CTA overlay (ovl/ostamp), so nodes cost what they touch.
+#include <cooperative_groups.h>
+
 #include "gbp_nodes.cuh"
 
 namespace gbp {
+
+namespace cg = cooperative_groups;
 
 struct PlainBnd {
   const double* lb;
@@ -64,7 +68,7 @@ __device__ __forceinline__ void rowsLongBody(const Num& s, const Prob& P, const 
 
 __device__ __forceinline__ void applyBody(const Num& s, const Prob& P, double* lb, double* ub, Cands& C, Front& F,
                                           int stamp, int* cutoff, unsigned long long* stats, const ChangeLog& G,
-                                          int round) {
+                                          int round, const MovedLog& M = MovedLog{}) {
   const int n = *C.ntouched;
   unsigned long long changes = 0;
   bool cut = false;
@@ -82,6 +86,13 @@ __device__ __forceinline__ void applyBody(const Num& s, const Prob& P, double* l
     }
     bool lbup = nl > l, ubdown = nu < u;
     if (lbup || ubdown) {
+      // the sparse call's record of a column's first move: its bounds before the call's propagation
+      if (M.stamp != nullptr && atomicExch(&M.stamp[j], M.epoch) != M.epoch) {
+        const int k = atomicAdd(M.count, 1);
+        M.col[k] = j;
+        M.lb[k] = l;
+        M.ub[k] = u;
+      }
       lb[j] = nl;
       ub[j] = nu;
       changes += (unsigned long long)lbup + (unsigned long long)ubdown;
@@ -136,8 +147,8 @@ __global__ void __launch_bounds__(256) k_apply_g(Num s, Prob P, Cands C, ListSet
   applyBody(s, P, S->lb, S->ub, C, F, S->stamp, &S->cutoff, stats, S->log, S->round);
 }
 
-// end of a round: switch to the list just filled, clear the other one, and tell the graph whether to go on
-__global__ void k_advance_g(LoopState* S, cudaGraphConditionalHandle h) {
+// end of a round: switch to the list just filled, clear the other one; returns whether another round follows
+__device__ __forceinline__ int advanceRound(LoopState* S) {
   const int ran = S->nshort[S->cur] + S->nlong[S->cur];
   if (ran > 0) S->worked += 1;
   S->round += 1;
@@ -153,7 +164,36 @@ __global__ void k_advance_g(LoopState* S, cudaGraphConditionalHandle h) {
     S->status = 2;
     more = 0;
   }
-  cudaGraphSetConditional(h, more ? 1u : 0u);
+  return more;
+}
+__global__ void k_advance_g(LoopState* S, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, advanceRound(S) ? 1u : 0u);
+}
+
+// ---- all rounds in one cooperative launch: the graph's round body, with grid-wide barriers (cooperative groups,
+// the launch guarantees every block is resident) between its phases instead of kernel boundaries.  For seeded
+// calls, whose frontiers are small, the launch and per-kernel costs of the graph dominate.
+__global__ void __launch_bounds__(ROW_THREADS) k_plain_coop(Num s, Prob P, Cands C, ListSet L, LoopState* S,
+                                                           unsigned long long* stats) {
+  __shared__ RowBatch<ROW_THREADS> rb;
+  __shared__ int s_cut;
+  cg::grid_group grid = cg::this_grid();
+  volatile LoopState* V = S;
+  for (;;) {
+    const int cur = V->cur;
+    C.round = V->round;
+    const PlainBnd B{S->lb, S->ub};
+    rowsShortBody(s, P, B, L.list[cur], V->nshort[cur], C, &S->cutoff, stats, rb, &s_cut);
+    rowsLongBody(s, P, B, L.list[cur], V->nlong[cur], L.cap, C, &S->cutoff, stats);
+    grid.sync();
+    const int nxt = cur == 1 ? 0 : 1;
+    Front F{L.list[nxt], &S->nshort[nxt], &S->nlong[nxt], L.rowstamp, L.cap};
+    applyBody(s, P, S->lb, S->ub, C, F, V->stamp, &S->cutoff, stats, S->log, V->round);
+    grid.sync();
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->more = advanceRound(S);
+    grid.sync();
+    if (!V->more) break;
+  }
 }
 
 __global__ void k_seed(Prob P, const double* lb, const double* ub, int64_t nseed, const int32_t* cols,
@@ -492,6 +532,110 @@ cudaError_t launchApply(cudaStream_t st, int grid, const Num& s, const Prob& P, 
                         Front F, int stamp, int* cutoff, unsigned long long* stats, const ChangeLog& G, int round) {
   k_apply<<<grid, 256, 0, st>>>(s, P, lb, ub, C, F, stamp, cutoff, stats, G, round);
   return cudaGetLastError();
+}
+// ---- gbp_propagate_changes in one cooperative launch: the caller's changes, the seeds, every round, and the moved
+// columns (restored when the call ends in a cutoff or overflows the caller's capacity), so that the call costs one
+// copy in, one launch and one copy out
+__global__ void __launch_bounds__(ROW_THREADS) k_sparse_coop(const __grid_constant__ SparseArgs A) {
+  __shared__ RowBatch<ROW_THREADS> rb;
+  __shared__ int s_cut;
+  cg::grid_group grid = cg::this_grid();
+  LoopState* S = A.S;
+  volatile LoopState* V = S;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  if (tid == 0) {
+    *S = A.init;
+    for (int k = 0; k < 8; ++k) A.stats[k] = 0;
+    *A.moved.count = 0;
+    if (A.init.log.n != nullptr) *A.init.log.n = 0;
+    if (A.C.rlog.n != nullptr) *A.C.rlog.n = 0;
+  }
+  // the caller's changes, with the bounds they replace (or the caller's seed bounds)
+  for (int64_t k = tid; k < A.nchg; k += nth) {
+    const int j = A.cols[k];
+    if (!A.keepold) {
+      A.oldlb[k] = A.lb[j];
+      A.oldub[k] = A.ub[j];
+    }
+    A.lb[j] = A.nlb[k];
+    A.ub[j] = A.nub[k];
+  }
+  grid.sync();
+  {
+    Front F0{A.L.list[0], &S->nshort[0], &S->nlong[0], A.L.rowstamp, A.L.cap};
+    for (int64_t k = tid; k < A.nchg; k += nth) {
+      const int j = A.cols[k];
+      expandColumn(A.P, F0, j, A.lb[j] > A.oldlb[k], A.ub[j] < A.oldub[k], A.seedstamp);
+    }
+  }
+  grid.sync();
+  Cands C = A.C;
+  const bool any = A.nchg > 0;
+  while (any) {
+    const int cur = V->cur;
+    C.round = V->round;
+    const PlainBnd B{A.lb, A.ub};
+    rowsShortBody(A.s, A.P, B, A.L.list[cur], V->nshort[cur], C, &S->cutoff, A.stats, rb, &s_cut);
+    rowsLongBody(A.s, A.P, B, A.L.list[cur], V->nlong[cur], A.L.cap, C, &S->cutoff, A.stats);
+    grid.sync();
+    const int nxt = cur == 1 ? 0 : 1;
+    Front F{A.L.list[nxt], &S->nshort[nxt], &S->nlong[nxt], A.L.rowstamp, A.L.cap};
+    applyBody(A.s, A.P, A.lb, A.ub, C, F, V->stamp, &S->cutoff, A.stats, A.init.log, V->round, A.moved);
+    grid.sync();
+    if (tid == 0) S->more = advanceRound(S);
+    grid.sync();
+    if (!V->more) break;
+  }
+  // a cutoff, or more moved columns than the caller has room for: back to the bounds after the caller's changes
+  const int cnt = *(volatile int*)A.moved.count;
+  const bool back = V->cutoff || cnt > A.cap;
+  for (int64_t k = tid; k < cnt; k += nth) {
+    const int j = A.moved.col[k];
+    if (back) {
+      A.lb[j] = A.moved.lb[k];
+      A.ub[j] = A.moved.ub[k];
+    } else {
+      SparseOut o;
+      o.col = j;
+      o.pad = 0;
+      o.lb = A.lb[j];
+      o.ub = A.ub[j];
+      A.out[k] = o;
+    }
+  }
+  if (tid == 0) {
+    A.header[0] = V->cutoff;
+    A.header[1] = V->status;
+    A.header[2] = V->worked;
+    A.header[3] = V->stamp;
+    A.header[4] = cnt;
+    unsigned long long* hs = (unsigned long long*)(A.header + 8);
+    for (int k = 0; k < 8; ++k) hs[k] = ((volatile unsigned long long*)A.stats)[k];
+  }
+}
+cudaError_t launchSparseCoop(cudaStream_t st, int grid, const SparseArgs& A) {
+  SparseArgs a = A;
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void*)k_sparse_coop, dim3(grid), dim3(ROW_THREADS), args, 0, st);
+}
+cudaError_t sparseCoopOccupancy(int* blocksPerSm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_sparse_coop, ROW_THREADS, 0);
+}
+
+cudaError_t launchPlainCoop(cudaStream_t st, int grid, const Num& s, const Prob& P, const Cands& C, const ListSet& L,
+                            LoopState* S, unsigned long long* stats) {
+  Num a0 = s;
+  Prob a1 = P;
+  Cands a2 = C;
+  ListSet a3 = L;
+  LoopState* a4 = S;
+  unsigned long long* a5 = stats;
+  void* args[] = {&a0, &a1, &a2, &a3, &a4, &a5};
+  return cudaLaunchCooperativeKernel((const void*)k_plain_coop, dim3(grid), dim3(ROW_THREADS), args, 0, st);
+}
+cudaError_t plainCoopOccupancy(int* blocksPerSm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, k_plain_coop, ROW_THREADS, 0);
 }
 const void* graphKernel(int which) {
   switch (which) {
