@@ -85,6 +85,25 @@ def save_case(name, inst, nnodes=0, node_seed=11):
     print(f"{path}: {inst.m}x{inst.n}, {inst.nnz} nnz, {nnodes} nodes, {os.path.getsize(path) // 1024} KiB")
 
 
+MIPLIB = ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03", "p0548", "rgn"]
+
+
+def save_miplib_cases():
+    """The MIPLIB instances the reference ships (check/instances/MIP, read with scip_gb300/mps.py as SCIP reads
+    them): SCIP's root and 100 nodes per instance, both rules, like the seeded cases, under tests/golden/miplib so
+    that the GPU machine (which has no reference sources) runs them too."""
+    from scip_gb300 import mps
+
+    d = os.path.join(oracle.REFDIR, "check", "instances", "MIP")
+    if not os.path.isdir(d):
+        raise SystemExit("REFDIR must name the SCIP source tree (check/instances/MIP)")
+    os.makedirs(os.path.join(HERE, "miplib"), exist_ok=True)
+    for name in MIPLIB:
+        path = os.path.join(d, name + ".mps")
+        if os.path.exists(path):
+            save_case(os.path.join("miplib", name), mps.read_mps(path), nnodes=100)
+
+
 def save_ranged_case(name, inst):
     """SCIP's root fixpoint with ranged-row propagation, for sortvars off ("nosort") and on ("sort") and both
     rules, under tests/golden/ranged (kept apart from the cases above, whose tests run with the rule off)."""
@@ -239,12 +258,15 @@ def main(names):
     ranged = ranged_cases()
     for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs",
                                                                              "node_workload_scip",
-                                                                             "node_workload_base"]:
+                                                                             "node_workload_base", "miplib"]:
         if name == "node_workload_scip":
             save_node_workload()
             continue
         if name == "node_workload_base":
             save_node_workload_base()
+            continue
+        if name == "miplib":
+            save_miplib_cases()
             continue
         if name == "ranged/tiny_cutoffs":
             save_tiny_cutoffs()

@@ -11,6 +11,9 @@ from scip_gb300.instances import Instance, NodeBatch
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# the MIPLIB instances the reference ships, with SCIP's results (tests/golden/make_golden.py miplib)
+MIPLIB_CASES = sorted("miplib/" + os.path.splitext(os.path.basename(p))[0]
+                      for p in glob.glob(os.path.join(GOLDEN, "miplib", "*.npz")))
 
 # continuous bounds: equal within 1e-9 relative or feastol absolute
 REL_TOL = 1e-9

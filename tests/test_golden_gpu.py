@@ -1,6 +1,6 @@
-"""The CUDA path on the golden fixtures: bit-identical to the oracle on every fixture instance (root fixpoint
-through the plain path, nodes through the batched kernel), hence the same agreement with SCIP's own results
-that tests/test_golden_cpu.py records."""
+"""The CUDA path on the golden fixtures, the seeded cases and the MIPLIB instances the reference ships: bit-identical
+to the oracle on every fixture instance (root fixpoint through the plain path, nodes through the batched kernel),
+hence the same agreement with SCIP's own results that tests/test_golden_cpu.py and tests/test_mps_cpu.py record."""
 import numpy as np
 import pytest
 
@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-@pytest.mark.parametrize("case", G.CASES)
+@pytest.mark.parametrize("case", G.CASES + G.MIPLIB_CASES)
 def test_gpu_equals_oracle_on_golden(gpu_prop, oracle_mod, case, tag):
     inst, z = G.load(case)
     maxeasy = 0.0 if tag == "res" else 1e6

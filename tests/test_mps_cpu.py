@@ -1,6 +1,7 @@
 """MPS reader semantics, and the oracle against SCIP itself on the MIPLIB instances that the reference ships
 (check/instances/MIP/*.mps).  The second part runs only where the reference sources and the SCIP driver
-built from them are present; no instance data is copied into this repository."""
+built from them are present; the fixtures under tests/golden/miplib (written by tests/golden/make_golden.py from
+those files and SCIP's results) carry the same instances to the GPU tests."""
 import glob
 import os
 

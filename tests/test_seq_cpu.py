@@ -20,7 +20,7 @@ def _par(oracle_mod, tag):
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-@pytest.mark.parametrize("case", G.CASES)
+@pytest.mark.parametrize("case", G.CASES + G.MIPLIB_CASES)
 def test_root_in_scip_order_equals_scip(oracle_mod, case, tag):
     inst, z = G.load(case)
     vidx = scip_var_index(inst.isint, inst.lb, inst.ub)
@@ -38,7 +38,7 @@ def test_root_in_scip_order_equals_scip(oracle_mod, case, tag):
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-@pytest.mark.parametrize("case", [c for c in G.CASES if "node_ptr" in G.load(c)[1]])
+@pytest.mark.parametrize("case", [c for c in G.CASES + G.MIPLIB_CASES if "node_ptr" in G.load(c)[1]])
 def test_nodes_in_scip_order_agree_with_scip(oracle_mod, case, tag):
     inst, z = G.load(case)
     nb = G.nodes_of(z)

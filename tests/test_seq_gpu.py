@@ -2,8 +2,9 @@
 
 * against the oracle's restatement of that order (oracle/linprop_seq.c) bit for bit -- cutoff verdicts, rounds, and
   every changed column's bounds -- on every golden instance, both rules, with and without sortvars;
-* against SCIP 11's own node results (tests/golden, each node from a fresh transform, rows in the order SCIP held
-  them): cutoff verdicts and integer bounds exact, continuous bounds within 1e-9 relative or feastol absolute;
+* against SCIP 11's own node results (tests/golden, the seeded cases and the MIPLIB instances the reference ships,
+  each node from a fresh transform, rows in the order SCIP held them): cutoff verdicts and integer bounds exact,
+  continuous bounds within 1e-9 relative or feastol absolute;
 * edge cases: empty nodes and batches, a change outside the column range (GBP_ERR_INVALID, after which the context
   is still exact), a change that conflicts with the base domain, and the round limit.
 """
@@ -40,7 +41,7 @@ def _scip_ordered(z, inst, tag):
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-@pytest.mark.parametrize("case", [c for c in G.CASES if "node_ptr" in G.load(c)[1]])
+@pytest.mark.parametrize("case", [c for c in G.CASES + G.MIPLIB_CASES if "node_ptr" in G.load(c)[1]])
 def test_nodes_in_scip_order_equal_oracle_and_scip(gpu_prop, oracle_mod, case, tag):
     inst, z = G.load(case)
     nb = G.nodes_of(z)
