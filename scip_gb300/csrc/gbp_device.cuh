@@ -222,13 +222,36 @@ __device__ __forceinline__ void pushRow(const Prob& P, Front& F, int row, int st
   }
 }
 
-// rows of column j made relevant by a raised lower bound (lbup) and/or a lowered upper bound (ubdown)
+// rows of column j made relevant by a raised lower bound (lbup) and/or a lowered upper bound (ubdown).  The stamp
+// exchanges, length reads and list appends of up to 8 rows are issued together: each is a dependent round trip to
+// memory, and one thread expands a column
 __device__ __forceinline__ void expandColumn(const Prob& P, Front& F, int j, bool lbup, bool ubdown, int stamp) {
   if (P.cscrow != nullptr) {
-    uint32_t need = (lbup ? CSC_LBUP : 0u) | (ubdown ? CSC_UBDOWN : 0u);
-    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
-      uint32_t e = P.cscrow[q];
-      if (e & need) pushRow(P, F, (int)(e & CSC_ROW), stamp);
+    const uint32_t need = (lbup ? CSC_LBUP : 0u) | (ubdown ? CSC_UBDOWN : 0u);
+    const int64_t q0 = P.colptr[j], q1 = P.colptr[j + 1];
+    for (int64_t qb = q0; qb < q1; qb += 8) {
+      int rows[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        rows[t] = -1;
+        if (qb + t < q1) {
+          const uint32_t e = P.cscrow[qb + t];
+          if (e & need) rows[t] = (int)(e & CSC_ROW);
+        }
+      }
+      bool fresh[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) fresh[t] = rows[t] >= 0 && atomicExch(&F.rowstamp[rows[t]], stamp) != stamp;
+      bool shortrow[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) shortrow[t] = fresh[t] && P.rowptr[rows[t] + 1] - P.rowptr[rows[t]] <= LONGROW;
+      int slot[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        slot[t] = !fresh[t] ? -1 : (shortrow[t] ? atomicAdd(F.nshort, 1) : F.cap - 1 - atomicAdd(F.nlong, 1));
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        if (slot[t] >= 0) F.list[slot[t]] = rows[t];
     }
   } else {
     for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {

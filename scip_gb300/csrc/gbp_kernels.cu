@@ -40,8 +40,11 @@ __device__ __forceinline__ void rowsShortBody(const Num& s, const Prob& P, const
   if (threadIdx.x == 0) *s_cut = 0;
   __syncthreads();
   Stats st{0, 0, 0, 0};
-  for (int base = blockIdx.x * ROW_THREADS; base < n; base += gridDim.x * ROW_THREADS) {
-    const int cnt = (n - base) < ROW_THREADS ? (n - base) : ROW_THREADS;
+  // a frontier smaller than the grid's threads is spread over every block (a batch's latency grows with its rows:
+  // each row's scan is sequential, and its candidates share the block's threads); larger ones go in full batches
+  const int per = n < (int)gridDim.x * ROW_THREADS ? (n + (int)gridDim.x - 1) / (int)gridDim.x : ROW_THREADS;
+  for (int base = blockIdx.x * per; base < n; base += gridDim.x * per) {
+    const int cnt = (n - base) < per ? (n - base) : per;
     processShortRows<ROW_THREADS>(s, P, B, list + base, cnt, C, st, rb, s_cut);
   }
   __syncthreads();
