@@ -35,6 +35,7 @@ struct SCIP_PropData
    int                   nconss;             /**< number of constraints the matrix was built from */
    SCIP_Bool             specialised;        /**< also the rows of setppc, logicor, knapsack, varbound constraints */
    SCIP_Bool             replacespecialised; /**< switch those handlers' propagation off at include time */
+   SCIP_Bool             inprobing;          /**< also propagate in probing nodes */
    int                   nrows;              /**< rows in the matrix */
    int                   ncols;              /**< columns = transformed variables */
    SCIP_VAR**            vars;               /**< column -> variable */
@@ -710,7 +711,7 @@ static SCIP_DECL_PROPEXEC(propExecGpulinear)
    SCIP_Bool reduced = FALSE;
 
    *result = SCIP_DIDNOTRUN;
-   if( pd->failed || pd->ctx == NULL )
+   if( pd->failed || pd->ctx == NULL || (!pd->inprobing && SCIPinProbing(scip)) )
       return SCIP_OKAY;
 
    /* constraints added or removed since the upload: rebuild */
@@ -1031,6 +1032,9 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/specialised",
          "also propagate the rows of setppc, logicor, knapsack and varbound constraints (presolving upgrades linear "
          "rows to these handlers)", &pd->specialised, FALSE, TRUE, NULL, NULL) );
+   SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/probing",
+         "also propagate in probing nodes (SCIPpropagateProbing); SCIPpropagateGpulinearNodes serves many probing "
+         "candidates at once", &pd->inprobing, FALSE, TRUE, NULL, NULL) );
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacespecialised",
          "switch off the propagation of setppc, logicor, knapsack and varbound (constraints/<handler>/propfreq = -1)",
          &pd->replacespecialised, FALSE, FALSE, paramChgdReplacespecialised, NULL) );
@@ -1087,3 +1091,118 @@ SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip)
    SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
    return prop == NULL ? 0 : SCIPpropGetData(prop)->nrangedreasons;
 }
+
+/* Many nodes at once on top of the current local bounds (the batched path of libgbp, gbp_propagate_nodes): for
+ * callers that hold many candidate nodes -- probing, strong branching, a lookahead of open nodes.  Below the root the
+ * global bounds go to the device for the binary test, as in PROPEXEC. */
+SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* nodebeg, SCIP_VAR** vars,
+   const SCIP_Real* lbs, const SCIP_Real* ubs, int outcap, SCIP_Bool* cutoff, int* outbeg, SCIP_VAR** outvars,
+   SCIP_Real* outlbs, SCIP_Real* outubs, SCIP_Bool* success)
+{
+   SCIP_PROP* prop = SCIPfindProp(scip, PROP_NAME);
+   SCIP_PROPDATA* pd;
+   int64_t* ptr = NULL;
+   int32_t* col = NULL;
+   int8_t* ocut = NULL;
+   int32_t* orounds = NULL;
+   int64_t* ooff = NULL;
+   int32_t* on = NULL;
+   int32_t* ocol = NULL;
+   double* olb = NULL;
+   double* oub = NULL;
+   gbp_result res;
+   int nchg;
+   int rc;
+   int j;
+   int k;
+   int at;
+
+   if( prop == NULL )
+      return SCIP_PLUGINNOTFOUND;
+   if( nnodes < 0 || nodebeg == NULL || cutoff == NULL || outbeg == NULL || success == NULL || outcap < 0 )
+      return SCIP_INVALIDDATA;
+   *success = FALSE;
+   pd = SCIPpropGetData(prop);
+   if( pd->failed || pd->ctx == NULL || nnodes == 0 )
+      return SCIP_OKAY;
+   nchg = nodebeg[nnodes];
+   for( j = 0; j < pd->ncols; ++j )
+   {
+      pd->lb[j] = SCIPvarGetLbLocal(pd->vars[j]);
+      pd->ub[j] = SCIPvarGetUbLocal(pd->vars[j]);
+   }
+   if( SCIPgetDepth(scip) > 0 )
+   {
+      for( j = 0; j < pd->ncols; ++j )
+      {
+         pd->glb[j] = SCIPvarGetLbGlobal(pd->vars[j]);
+         pd->gub[j] = SCIPvarGetUbGlobal(pd->vars[j]);
+      }
+      rc = gbp_set_global_bounds(pd->ctx, pd->glb, pd->gub);
+      pd->haveglobal = rc == GBP_OK;
+   }
+   else
+   {
+      rc = gbp_set_global_bounds(pd->ctx, NULL, NULL);
+      pd->haveglobal = FALSE;
+   }
+   if( rc != GBP_OK )
+      return SCIP_OKAY;
+   SCIP_CALL( SCIPallocBufferArray(scip, &ptr, nnodes + 1) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &col, MAX(nchg, 1)) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &ocut, nnodes) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &orounds, nnodes) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &ooff, nnodes) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &on, nnodes) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &ocol, MAX(outcap, 1)) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &olb, MAX(outcap, 1)) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &oub, MAX(outcap, 1)) );
+   rc = GBP_OK;
+   for( k = 0; k <= nnodes; ++k )
+      ptr[k] = nodebeg[k];
+   /* a node's variables are columns: active problem variables (column j is SCIPgetVars(scip)[j]) */
+   for( k = 0; k < nchg && rc == GBP_OK; ++k )
+   {
+      j = SCIPvarGetProbindex(vars[k]);
+      if( j < 0 || j >= pd->ncols || pd->vars[j] != vars[k] )
+         rc = GBP_ERR_INVALID;
+      else
+         col[k] = j;
+   }
+   if( rc == GBP_OK )
+      rc = gbp_propagate_nodes(pd->ctx, pd->lb, pd->ub, nnodes, ptr, col, lbs, ubs, ocut, orounds, ooff, on, ocol, olb,
+         oub, outcap, &res);
+   if( rc == GBP_OK || rc == GBP_ERR_LIMIT )
+   {
+      at = 0;
+      for( k = 0; k < nnodes; ++k )
+      {
+         int t;
+         cutoff[k] = ocut[k] != 0;
+         outbeg[k] = at;
+         if( cutoff[k] )
+            continue;
+         for( t = 0; t < on[k]; ++t, ++at )
+         {
+            outvars[at] = pd->vars[ocol[ooff[k] + t]];
+            outlbs[at] = olb[ooff[k] + t];
+            outubs[at] = oub[ooff[k] + t];
+         }
+      }
+      outbeg[nnodes] = at;
+      *success = TRUE;
+   }
+   SCIPfreeBufferArray(scip, &oub);
+   SCIPfreeBufferArray(scip, &olb);
+   SCIPfreeBufferArray(scip, &ocol);
+   SCIPfreeBufferArray(scip, &on);
+   SCIPfreeBufferArray(scip, &ooff);
+   SCIPfreeBufferArray(scip, &orounds);
+   SCIPfreeBufferArray(scip, &ocut);
+   SCIPfreeBufferArray(scip, &col);
+   SCIPfreeBufferArray(scip, &ptr);
+   if( rc == GBP_ERR_INVALID )
+      return SCIP_INVALIDDATA;
+   return SCIP_OKAY;
+}
+

@@ -8,9 +8,10 @@
  * SCIPtightenVarLb/SCIPtightenVarUb (src/scip/scip_var.c:6402/6652) or reports SCIP_CUTOFF.  The device runs
  * the propagation rules of cons_linear (tightenVarBounds / tightenVarBoundsEasy) to a fixpoint.
  *
- * Parameters (propagating/gpulinear/...): device (CUDA ordinal, default 0) and replacelinear (default FALSE:
+ * Parameters (propagating/gpulinear/...): device (CUDA ordinal, default 0), replacelinear (default FALSE:
  * if TRUE, SCIPincludePropGpulinear sets constraints/linear/propfreq = -1 so that the GPU replaces
- * cons_linear's own propagation; cons_linear keeps checking, enforcing and presolving).
+ * cons_linear's own propagation; cons_linear keeps checking, enforcing and presolving) and probing (default TRUE:
+ * also propagate in probing nodes).
  * Without a usable GPU the propagator disables itself with a warning and SCIP continues with cons_linear.
  */
 #ifndef PROP_GPULINEAR_H
@@ -42,6 +43,17 @@ SCIP_RETCODE SCIPgetGpulinearStats(SCIP* scip, SCIP_Longint* ncalls, SCIP_Longin
 /** how many of the explained changes and analysed cutoffs were explained by a ranged row's record
  *  (constraints/linear/rangedrowpropagation) */
 SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip);
+
+/** propagates nnodes nodes at once on the GPU (libgbp's batched path, gbp_propagate_nodes), each on top of the
+ *  current local bounds -- for callers that hold many candidate nodes (probing, strong branching, a lookahead of open
+ *  nodes).  Node k tightens the bounds of vars[nodebeg[k] .. nodebeg[k+1]) to [lbs, ubs] (active problem
+ *  variables; SCIP_INVALIDDATA otherwise) and runs linear propagation to its fixpoint; SCIP's bounds are not
+ *  changed.  Per node: cutoff[k], and the variables whose bounds propagation moved against the local bounds, with
+ *  their bounds, at outvars/outlbs/outubs[outbeg[k] .. outbeg[k+1]) (outcap entries in all; a cut-off node has
+ *  none).  *success is FALSE when the propagator is inactive (no GPU) or the outputs did not fit. */
+SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* nodebeg, SCIP_VAR** vars,
+   const SCIP_Real* lbs, const SCIP_Real* ubs, int outcap, SCIP_Bool* cutoff, int* outbeg, SCIP_VAR** outvars,
+   SCIP_Real* outlbs, SCIP_Real* outubs, SCIP_Bool* success);
 
 #ifdef __cplusplus
 }

@@ -377,3 +377,64 @@ int gbp_get_ranged_log(gbp_ctx* ctx, int64_t cap, int32_t* round, int32_t* col, 
    free(ord);
    return (ctx->log.rn > ctx->log.rcap || ctx->log.rn > cap) ? GBP_ERR_OVERFLOW : GBP_OK;
 }
+
+/* the batched-node call: the oracle's nodes (binary test on the base bounds), packed in node order */
+int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub, int64_t nnodes,
+   const int64_t* ptr, const int32_t* chg_col, const double* chg_lb, const double* chg_ub,
+   int8_t* out_cutoff, int32_t* out_rounds, int64_t* out_off, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int64_t out_cap, gbp_result* res)
+{
+   const int64_t n = ctx->P.n > 0 ? ctx->P.n : 1;
+   int32_t* tn = malloc(sizeof(int32_t) * (size_t)(nnodes > 0 ? nnodes : 1));
+   int32_t* tc = malloc(sizeof(int32_t) * (size_t)(nnodes * n + 1));
+   double* tl = malloc(sizeof(double) * (size_t)(nnodes * n + 1));
+   double* tu = malloc(sizeof(double) * (size_t)(nnodes * n + 1));
+   lpo_result tot;
+   int64_t at = 0;
+   int64_t k;
+   int over = 0;
+   int rc;
+   if( res != NULL )
+      memset(res, 0, sizeof(*res));
+   if( tn == NULL || tc == NULL || tl == NULL || tu == NULL )
+      rc = GBP_ERR_NOMEM;
+   else if( lpo_propagate_nodes(&ctx->P, &ctx->par, baselb, baseub, nnodes, ptr, chg_col, chg_lb, chg_ub, out_cutoff,
+               out_rounds, tn, tc, tl, tu, (int32_t)n, 1, &tot) != 0 )
+      rc = GBP_ERR_NOMEM;
+   else
+   {
+      for( k = 0; k < nnodes; ++k )
+      {
+         int64_t t;
+         out_off[k] = at;
+         if( at + tn[k] > out_cap )
+         {
+            out_n[k] = -1;
+            over = 1;
+            continue;
+         }
+         for( t = 0; t < tn[k]; ++t, ++at )
+         {
+            out_col[at] = tc[k * n + t];
+            out_lb[at] = tl[k * n + t];
+            out_ub[at] = tu[k * n + t];
+         }
+         out_n[k] = tn[k];
+      }
+      if( res != NULL )
+      {
+         res->cutoff = tot.cutoff;
+         res->rounds = tot.rounds;
+         res->rows = tot.rows;
+         res->nnz = tot.nnz;
+         res->candidates = tot.candidates;
+         res->changes = tot.changes;
+      }
+      rc = over ? GBP_ERR_OVERFLOW : GBP_OK;
+   }
+   free(tn);
+   free(tc);
+   free(tl);
+   free(tu);
+   return rc;
+}

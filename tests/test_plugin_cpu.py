@@ -164,3 +164,49 @@ def test_plugin_replaces_the_specialised_handlers_after_presolving(solve_driver,
     calls, chg, cut, analysed, asked, resolved, _, active = gpu["gpulinear"].split()
     assert active == "1" and int(calls) > 0 and int(chg) > 0
     assert asked == resolved
+
+
+@pytest.fixture(scope="module")
+def nodes_driver(tmp_path_factory, oracle_mod):
+    """tests/plugin/nodes_driver.c: the plugin's batched entry (SCIPpropagateGpulinearNodes) inside SCIP, on the
+    oracle test double, against SCIP's own probing."""
+    if not os.path.exists(LIBSCIP):
+        pytest.skip("SCIP build (oracle/_ref) not present")
+    if not oracle_mod.REFDIR or not os.path.exists(os.path.join(oracle_mod.REFDIR, "src", "scip", "scip.h")):
+        pytest.skip("SCIP headers not present (REFDIR names the SCIP source tree)")
+    out = tmp_path_factory.mktemp("nodes")
+    exe = str(out / "nodes_driver")
+    src = [os.path.join(ROOT, "tests", "plugin", "nodes_driver.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c"),
+           os.path.join(ROOT, "tests", "plugin", "gbp_oracle_shim.c"),
+           os.path.join(ROOT, "oracle", "linprop_oracle.c"),
+           os.path.join(ROOT, "oracle", "linprop_seq.c")]
+    inc = ["-I" + os.path.join(REF, "include"), "-I" + os.path.join(oracle_mod.REFDIR, "src"),
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "scip_gb300", "plugin"),
+           "-I" + os.path.join(ROOT, "oracle")]
+    cmd = ["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", "-ffp-contract=off", *inc, "-o", exe, *src, LIBSCIP,
+           "-lstdc++", "-lm", "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+@pytest.mark.parametrize("name", ["enigma", "flugpl", "lseu", "misc03", "p0548"])
+def test_batched_plugin_entry_agrees_with_scip_probing(nodes_driver, oracle_mod, name):
+    """SCIPpropagateGpulinearNodes propagates 200 nodes of integer fixings in one call on top of the root's local
+    bounds; SCIP then propagates each of them through SCIPpropagateProbing with cons_linear's propagation: the same
+    cutoff verdicts and the same integer bounds on every node."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    r = subprocess.run([nodes_driver, path, "200"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")]
+    assert line, r.stdout
+    f = line[0].split()
+    got = {f[i]: f[i + 1] for i in range(len(f) - 1) if not f[i].lstrip("-").isdigit()}
+    assert got["success"] == "1"
+    assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0", line[0]
+    assert int(got["moved"]) > 0
+
