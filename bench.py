@@ -225,7 +225,10 @@ def other_workload(args):
         cfg = {"workload": "one 1,000,000 x 2,000,000 instance, Zipf(1.5) row lengths in [2, 5000], root fixpoint "
                            "through the plain path", "rows": big.m, "cols": big.n, "nnz": big.nnz}
     gen_s = time.perf_counter() - t0
-    prop = gbp.Propagator(0, params=gbp.default_params(maxeasy=args.maxeasy))
+    params = gbp.default_params(maxeasy=args.maxeasy)
+    if args.hostloop:  # host-driven rounds: one launch per kernel per round (kernel-level timings, ncu launch lists)
+        params.flags |= gbp.GBP_FLAG_HOSTLOOP
+    prop = gbp.Propagator(0, params=params)
     t0 = time.perf_counter()
     if args.workload == "uneven":
         prop.upload_instances(insts)
@@ -445,6 +448,8 @@ def main():
     ap.add_argument("--family", default="mip", choices=["mip", "gcd"],
                     help="nodes workload matrix: mip (log-uniform coefficients) or gcd (ranged rows sharing a divisor)")
     ap.add_argument("--ranged", action="store_true", help="ranged-row propagation on (GBP_FLAG_RANGEDROW)")
+    ap.add_argument("--hostloop", action="store_true",
+                    help="root/zipf/uneven: host-driven rounds (GBP_FLAG_HOSTLOOP) instead of the device loop")
     ap.add_argument("--rows", type=int, default=200_000,
                     help="nodes workload: rows of the matrix (columns = 2 x rows); smaller for profiling captures")
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serving: arrival rates (req/s)")

@@ -116,7 +116,9 @@ __global__ void __launch_bounds__(ROW_THREADS) k_rows_short(Num s, Prob P, Plain
   rowsShortBody(s, P, B, list, *nshort, C, cutoff, stats, rb, &s_cut);
 }
 
-__global__ void __launch_bounds__(256) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
+// two CTAs per SM (at most 128 registers a thread): one warp walks a long row with a dependent chain per lane, so
+// the SM needs the second CTA's warps to hide it (cfg1's Zipf root: 146.5 -> 116.3 ms)
+__global__ void __launch_bounds__(256, 2) k_rows_long(Num s, Prob P, PlainBnd B, const int* list, const int* nlong,
                                                    int cap, Cands C, int* cutoff, unsigned long long* stats) {
   rowsLongBody(s, P, B, list, *nlong, cap, C, cutoff, stats);
 }
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(ROW_THREADS) k_rows_short_g(Num s, Prob P, Can
   rowsShortBody(s, P, PlainBnd{S->lb, S->ub}, L.list[cur], S->nshort[cur], C, &S->cutoff, stats, rb, &s_cut);
 }
 
-__global__ void __launch_bounds__(256) k_rows_long_g(Num s, Prob P, Cands C, ListSet L, LoopState* S,
+__global__ void __launch_bounds__(256, 2) k_rows_long_g(Num s, Prob P, Cands C, ListSet L, LoopState* S,
                                                      unsigned long long* stats) {
   const int cur = S->cur;
   C.round = S->round;
