@@ -364,6 +364,61 @@ def serving_workload(args):
                       "mean_batch": float(np.mean([b[1] for b in batches])) if batches else 0.0}))
 
 
+def time_served(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), duration=0.3):
+    """libgbp's serving loop (gbp_server_*, C worker threads merging node requests into batched launches): open-loop
+    Poisson arrivals of single-node requests (the bench's nodes in turn) at each offered rate for `duration` seconds,
+    then every reply collected.  Latency = the server's time from admitting a request to finishing its batch;
+    throughput = requests / (last finish - first admission)."""
+    import ctypes
+
+    from scip_gb300 import gbp
+
+    srv = gbp.Server(inst, rlb, rub, params=params, workers=2, max_batch=4096)
+    L = srv.L
+    reqs = []
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        arrs = (np.ascontiguousarray(nodes.col[sl], np.int32), np.ascontiguousarray(nodes.lb[sl]),
+                np.ascontiguousarray(nodes.ub[sl]))
+        reqs.append((len(arrs[0]), arrs, [a.ctypes.data_as(ctypes.c_void_p) for a in arrs]))
+    out = {}
+    t = ctypes.c_int64()
+    try:
+        for rate in rates:
+            rng = np.random.default_rng(np.random.PCG64(rate))
+            n = int(rate * duration)
+            due = np.cumsum(rng.exponential(1.0 / rate, n))
+            tickets = []
+            t0 = time.perf_counter()
+            lag = 0.0
+            for i in range(n):
+                while time.perf_counter() - t0 < due[i]:
+                    pass
+                lag = max(lag, time.perf_counter() - t0 - due[i])
+                nc, _, ptrs = reqs[i % len(reqs)]
+                rc = L.gbp_server_submit(srv.h, nc, ptrs[0], ptrs[1], ptrs[2], ctypes.byref(t))
+                if rc != gbp.GBP_OK:
+                    raise gbp.GbpError(rc, "submit")
+                tickets.append(t.value)
+            sub_s = time.perf_counter() - t0
+            ts, td = [], []
+            for tk in tickets:
+                r = srv.poll(tk)
+                ts.append(r[4])
+                td.append(r[5])
+            ts, td = np.array(ts), np.array(td)
+            lat = (td - ts) / 1e6
+            out[str(rate)] = {"offered_req_s": rate, "requests": n, "submitted_req_s": n / sub_s,
+                              "max_submit_lag_ms": 1e3 * lag,
+                              "throughput_req_s": n / ((td.max() - ts.min()) / 1e9),
+                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+        out["stats"] = srv.stats()
+        out["call"] = "gbp_server_submit / gbp_server_poll (2 worker threads, batched node launches)"
+    finally:
+        srv.close()
+    return out
+
+
 def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed):
     """Node-fixpoints/s of the batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER), inputs resident in HBM, CUDA
     events around each step, the L2 flushed between steps.  On the default instance the nodes start from SCIP's own
@@ -633,6 +688,11 @@ def main():
                         "generator": "instances.node_batch(..., tight=0.15): 15 % of the nodes dive one row past "
                                      "its right-hand side first"}
 
+    # served form: single-node requests through libgbp's C serving loop at 1k, 10k and 50k req/s offered
+    served = None
+    if not args.ranged and world == 1:
+        served = time_served(inst, rlb, rub, nodes, gbp.default_params(maxeasy=args.maxeasy))
+
     # the same nodes in SCIP's own order (GBP_FLAG_SCIPORDER): rows uploaded in the order SCIP sorts them into on the
     # base domain, device-resident inputs, the same timing
     scip_order = time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed=replicas.node_seed(3, rank))
@@ -709,6 +769,7 @@ def main():
                       "root_ms": rres.kernel_ms, "root_rounds": rres.rounds},
             "scip_order": scip_order,
             "infeasible_15pct": infeasible15,
+            "served": served,
             }
     if rank == 0:
         if not args.quick:

@@ -36,6 +36,7 @@ extern "C" {
 #define GBP_ERR_OVERFLOW   -6   /* an output list was too small (out_n reports -1 for that node) */
 #define GBP_ERR_STATE      -7   /* the device reported an inconsistent state (a bounded loop gave up) */
 #define GBP_ERR_TOO_LARGE  -8   /* the problem does not fit the fixed scratch of gbp_propagate_nodes_noalloc */
+#define GBP_ERR_BUSY       -9   /* gbp_server_poll: the reply is not ready within the wait */
 
 typedef struct gbp_ctx gbp_ctx;
 
@@ -248,6 +249,35 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * [0, n) shows out_cutoff[k] = 1; a node stopped at the round limit holds valid bounds); with res != NULL it waits
  * for the stream, fills res and returns GBP_ERR_INVALID / GBP_ERR_LIMIT / GBP_ERR_OVERFLOW like
  * gbp_propagate_nodes_device.  params == NULL uses the defaults of gbp_default_params. */
+/* ---------------------------------------------------------------- serving
+ * A request loop inside libgbp for branch-and-bound node requests against one resident problem and its root bounds
+ * (the served form of the batched path).  A client thread submits a node -- bound changes, as one node of
+ * gbp_propagate_nodes -- and gets a ticket at once.  nworkers worker threads, each with its own context and stream,
+ * take everything queued (up to max_batch nodes) and propagate it in one batched launch, so that requests arriving
+ * together share a launch and the batches of different workers overlap on the device.  Admission: at creation every
+ * worker runs a first batch (its slot memory is allocated then); the budget for the device bytes of batches in flight
+ * is the smaller of hbm_cap (bytes, 0: 150 GB) and the free device memory that remains (cudaMemGetInfo).  A worker
+ * takes requests only while its batch's bytes fit what the budget has left; a request that alone exceeds the budget is
+ * refused at submission (GBP_ERR_NOMEM).  A node change column outside [0, n) is refused at submission
+ * (GBP_ERR_INVALID).  gbp_server_poll waits up to wait_ms (negative: without limit) for a ticket's reply: GBP_OK with
+ * *cutoff and the columns whose bounds moved against the root bounds (sorted, *nout of them in cols/lb/ub of capacity
+ * cap), GBP_ERR_OVERFLOW with *nout the capacity needed (the reply stays available), GBP_ERR_BUSY when the wait ended
+ * first.  A reply is released once read.  t_submit_ns / t_done_ns (may be NULL): when the server took the request and
+ * when its batch finished (ns of a steady clock started with the server). */
+typedef struct gbp_server gbp_server;
+int gbp_server_create(gbp_server** out, int device, int nworkers, int64_t max_batch, int64_t hbm_cap,
+   const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals,
+   const double* lhs, const double* rhs, const int8_t* isint, const double* rootlb, const double* rootub);
+int gbp_server_submit(gbp_server* srv, int64_t nchg, const int32_t* cols, const double* lb, const double* ub,
+   int64_t* ticket);
+int gbp_server_poll(gbp_server* srv, int64_t ticket, int wait_ms, int32_t* cutoff, int64_t cap, int64_t* nout,
+   int32_t* cols, double* lb, double* ub, int64_t* t_submit_ns, int64_t* t_done_ns);
+/* batches launched, requests served, the largest batch, the admission budget in bytes */
+int gbp_server_stats(const gbp_server* srv, int64_t* batches, int64_t* requests, int64_t* max_batch_seen,
+   int64_t* budget);
+/* finishes the queued requests, stops the workers and frees everything */
+int gbp_server_destroy(gbp_server* srv);
+
 #define GBP_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int gbp_propagate_nodes_noalloc(int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
    const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const int64_t* colptr,

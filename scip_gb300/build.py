@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "--fmad=false", "-std=c++17",
               "-Xcompiler", "-fPIC", "-I" + INCLUDE]
-CU_SOURCES = ["gbp_kernels.cu", "gbp_nodes_ranged.cu", "gbp_api.cu", "gbp_noalloc.cu", "gbp_seq.cu"]
+CU_SOURCES = ["gbp_kernels.cu", "gbp_nodes_ranged.cu", "gbp_api.cu", "gbp_noalloc.cu", "gbp_seq.cu", "gbp_server.cu"]
 
 
 def _nvcc() -> str:
@@ -54,7 +54,7 @@ def build_libgbp(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
-    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", LIBGBP] + objs + ["-lcudart"]
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", LIBGBP] + objs + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -255,6 +255,7 @@ const char* gbp_error_string(int code) {
     case GBP_ERR_OVERFLOW: return "output list too small";
     case GBP_ERR_STATE: return "inconsistent device state";
     case GBP_ERR_TOO_LARGE: return "problem too large for the no-alloc scratch";
+    case GBP_ERR_BUSY: return "reply not ready";
     default: return "unknown error";
   }
 }

@@ -1,0 +1,354 @@
+// The serving loop of libgbp (gbp_server_*): node requests against one resident problem and its root bounds, merged
+// by worker threads into batched launches (gbp_propagate_nodes), each worker with its own context and stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gbp.h"
+
+namespace {
+
+struct Req {
+  std::vector<int32_t> cols;
+  std::vector<double> lb, ub;
+  int64_t t_submit = 0, t_done = 0;
+  int done = 0;
+  int rc = GBP_OK;
+  int32_t cutoff = 0;
+  std::vector<int32_t> ocols;
+  std::vector<double> olb, oub;
+  int64_t bytes = 0;
+};
+
+// pinned host buffers of one worker, grown as needed
+template <class T>
+struct Pinned {
+  T* p = nullptr;
+  size_t cap = 0;
+  bool grow(size_t n) {
+    if (n <= cap) return true;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
+    cap = std::max<size_t>(n, 1);
+    return true;
+  }
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+struct Worker {
+  gbp_ctx* ctx = nullptr;
+  std::thread th;
+  Pinned<int64_t> ptr, off;
+  Pinned<int32_t> col, rounds, n, ocol;
+  Pinned<double> lb, ub, olb, oub;
+  Pinned<int8_t> cut;
+};
+
+}  // namespace
+
+struct gbp_server {
+  int device = 0;
+  int64_t m = 0, n = 0;
+  int64_t max_batch = 0;
+  std::vector<double> rootlb, rootub;
+  std::vector<Worker> workers;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<int64_t> queue;
+  std::unordered_map<int64_t, Req> reqs;
+  int64_t next_ticket = 1;
+  bool stop = false;
+  int64_t budget = 0, inflight = 0;
+  int64_t batches = 0, served = 0, max_seen = 0;
+  std::chrono::steady_clock::time_point t0;
+
+  int64_t now() const {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+// device bytes of a request inside a batch: its changes in, its share of the packed output (one entry per column it
+// may move, bounded by 256 as the batch reserves), the per-node outputs
+int64_t requestBytes(int64_t nchg) { return 20 * nchg + 256 * 20 + 32; }
+
+// propagate one batch of requests on a worker; fills each request's reply
+void runBatch(gbp_server* S, Worker& W, std::vector<Req*>& batch) {
+  const int64_t nb = (int64_t)batch.size();
+  int64_t nchg = 0;
+  for (Req* r : batch) nchg += (int64_t)r->cols.size();
+  int64_t cap = 256 * nb;
+  bool ok = W.ptr.grow(nb + 1) && W.off.grow(nb) && W.col.grow(nchg) && W.rounds.grow(nb) && W.n.grow(nb) &&
+            W.lb.grow(nchg) && W.ub.grow(nchg) && W.cut.grow(nb) && W.ocol.grow(cap) && W.olb.grow(cap) &&
+            W.oub.grow(cap);
+  if (!ok) {
+    for (Req* r : batch) r->rc = GBP_ERR_NOMEM;
+    return;
+  }
+  int64_t at = 0;
+  W.ptr.p[0] = 0;
+  for (int64_t k = 0; k < nb; ++k) {
+    const Req* r = batch[k];
+    const size_t c = r->cols.size();
+    std::memcpy(W.col.p + at, r->cols.data(), c * sizeof(int32_t));
+    std::memcpy(W.lb.p + at, r->lb.data(), c * sizeof(double));
+    std::memcpy(W.ub.p + at, r->ub.data(), c * sizeof(double));
+    at += (int64_t)c;
+    W.ptr.p[k + 1] = at;
+  }
+  gbp_result res;
+  int rc = gbp_propagate_nodes(W.ctx, S->rootlb.data(), S->rootub.data(), nb, W.ptr.p, W.col.p, W.lb.p, W.ub.p,
+                               W.cut.p, W.rounds.p, W.off.p, W.n.p, W.ocol.p, W.olb.p, W.oub.p, cap, &res);
+  std::vector<Req*> again;  // nodes whose results did not fit the batch's packed output
+  for (int64_t k = 0; k < nb; ++k) {
+    Req* r = batch[k];
+    if (rc != GBP_OK && rc != GBP_ERR_LIMIT && rc != GBP_ERR_OVERFLOW) {
+      r->rc = rc;
+      continue;
+    }
+    if (W.n.p[k] < 0) {
+      again.push_back(r);
+      continue;
+    }
+    r->cutoff = W.cut.p[k];
+    const int64_t cnt = r->cutoff ? 0 : W.n.p[k];
+    std::vector<int64_t> idx((size_t)cnt);
+    for (int64_t q = 0; q < cnt; ++q) idx[q] = W.off.p[k] + q;
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return W.ocol.p[a] < W.ocol.p[b]; });
+    r->ocols.resize((size_t)cnt);
+    r->olb.resize((size_t)cnt);
+    r->oub.resize((size_t)cnt);
+    for (int64_t q = 0; q < cnt; ++q) {
+      r->ocols[q] = W.ocol.p[idx[q]];
+      r->olb[q] = W.olb.p[idx[q]];
+      r->oub[q] = W.oub.p[idx[q]];
+    }
+  }
+  for (Req* r : again) {  // alone, with room for every column
+    if (!W.ocol.grow((size_t)S->n) || !W.olb.grow((size_t)S->n) || !W.oub.grow((size_t)S->n)) {
+      r->rc = GBP_ERR_NOMEM;
+      continue;
+    }
+    std::vector<Req*> one{r};
+    const int64_t c = (int64_t)r->cols.size();
+    W.ptr.p[0] = 0;
+    W.ptr.p[1] = c;
+    std::memcpy(W.col.p, r->cols.data(), c * sizeof(int32_t));
+    std::memcpy(W.lb.p, r->lb.data(), c * sizeof(double));
+    std::memcpy(W.ub.p, r->ub.data(), c * sizeof(double));
+    int rc2 = gbp_propagate_nodes(W.ctx, S->rootlb.data(), S->rootub.data(), 1, W.ptr.p, W.col.p, W.lb.p, W.ub.p,
+                                  W.cut.p, W.rounds.p, W.off.p, W.n.p, W.ocol.p, W.olb.p, W.oub.p, S->n, &res);
+    if (rc2 != GBP_OK && rc2 != GBP_ERR_LIMIT) {
+      r->rc = rc2;
+      continue;
+    }
+    r->cutoff = W.cut.p[0];
+    const int64_t cnt = r->cutoff ? 0 : W.n.p[0];
+    std::vector<int64_t> idx((size_t)cnt);
+    for (int64_t q = 0; q < cnt; ++q) idx[q] = W.off.p[0] + q;
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return W.ocol.p[a] < W.ocol.p[b]; });
+    r->ocols.resize((size_t)cnt);
+    r->olb.resize((size_t)cnt);
+    r->oub.resize((size_t)cnt);
+    for (int64_t q = 0; q < cnt; ++q) {
+      r->ocols[q] = W.ocol.p[idx[q]];
+      r->olb[q] = W.olb.p[idx[q]];
+      r->oub[q] = W.oub.p[idx[q]];
+    }
+  }
+}
+
+void workerLoop(gbp_server* S, Worker* W) {
+  cudaSetDevice(S->device);
+  std::vector<Req*> batch;
+  std::vector<int64_t> tickets;
+  for (;;) {
+    int64_t bytes = 0;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait(lk, [&] {
+        return S->stop || (!S->queue.empty() && S->inflight + S->reqs[S->queue.front()].bytes <= S->budget);
+      });
+      if (S->queue.empty()) {
+        if (S->stop) return;
+        continue;
+      }
+      batch.clear();
+      tickets.clear();
+      while (!S->queue.empty() && (int64_t)batch.size() < S->max_batch) {
+        Req& r = S->reqs[S->queue.front()];
+        if (S->inflight + bytes + r.bytes > S->budget) break;
+        bytes += r.bytes;
+        batch.push_back(&r);
+        tickets.push_back(S->queue.front());
+        S->queue.pop_front();
+      }
+      S->inflight += bytes;
+    }
+    runBatch(S, *W, batch);  // Req objects stay put: only this worker and the pollers of done tickets touch them
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      const int64_t t = S->now();
+      for (Req* r : batch) {
+        r->t_done = t;
+        r->done = 1;
+      }
+      S->inflight -= bytes;
+      S->batches += 1;
+      S->served += (int64_t)batch.size();
+      S->max_seen = std::max<int64_t>(S->max_seen, (int64_t)batch.size());
+    }
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbp_server_create(gbp_server** out, int device, int nworkers, int64_t max_batch, int64_t hbm_cap,
+                      const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                      const double* vals, const double* lhs, const double* rhs, const int8_t* isint,
+                      const double* rootlb, const double* rootub) {
+  if (!out || nworkers < 1 || max_batch < 1 || hbm_cap < 0 || m < 0 || n < 0 || (n > 0 && (!rootlb || !rootub)))
+    return GBP_ERR_INVALID;
+  *out = nullptr;
+  gbp_server* S = new (std::nothrow) gbp_server();
+  if (!S) return GBP_ERR_NOMEM;
+  S->device = device;
+  S->m = m;
+  S->n = n;
+  S->max_batch = max_batch;
+  S->rootlb.assign(rootlb, rootlb + n);
+  S->rootub.assign(rootub, rootub + n);
+  S->t0 = std::chrono::steady_clock::now();
+  S->workers.resize((size_t)nworkers);
+  int rc = GBP_OK;
+  for (Worker& W : S->workers) {
+    rc = gbp_create(&W.ctx, device, nullptr);
+    if (rc == GBP_OK && params) rc = gbp_set_params(W.ctx, params);
+    if (rc == GBP_OK) rc = gbp_upload_problem(W.ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
+    if (rc != GBP_OK) break;
+    // a first batch (a node without changes) allocates the worker's slots before the budget is measured
+    std::vector<Req> warm(1);
+    std::vector<Req*> wb{&warm[0]};
+    runBatch(S, W, wb);
+    if (warm[0].rc != GBP_OK) {
+      rc = warm[0].rc;
+      break;
+    }
+  }
+  if (rc != GBP_OK) {
+    for (Worker& W : S->workers)
+      if (W.ctx) gbp_destroy(W.ctx);
+    delete S;
+    return rc;
+  }
+  size_t freeb = 0, totalb = 0;
+  cudaSetDevice(device);
+  if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) {
+    for (Worker& W : S->workers) gbp_destroy(W.ctx);
+    delete S;
+    return GBP_ERR_CUDA;
+  }
+  const int64_t cap = hbm_cap > 0 ? hbm_cap : (int64_t)150 << 30;
+  S->budget = std::min<int64_t>(cap, (int64_t)freeb);
+  for (Worker& W : S->workers) W.th = std::thread(workerLoop, S, &W);
+  *out = S;
+  return GBP_OK;
+}
+
+int gbp_server_submit(gbp_server* S, int64_t nchg, const int32_t* cols, const double* lb, const double* ub,
+                      int64_t* ticket) {
+  if (!S || !ticket || nchg < 0 || (nchg > 0 && (!cols || !lb || !ub))) return GBP_ERR_INVALID;
+  for (int64_t k = 0; k < nchg; ++k)
+    if (cols[k] < 0 || cols[k] >= S->n) return GBP_ERR_INVALID;
+  const int64_t bytes = requestBytes(nchg);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) return GBP_ERR_INVALID;
+    if (bytes > S->budget) return GBP_ERR_NOMEM;
+    const int64_t t = S->next_ticket++;
+    Req& r = S->reqs[t];
+    r.cols.assign(cols, cols + nchg);
+    r.lb.assign(lb, lb + nchg);
+    r.ub.assign(ub, ub + nchg);
+    r.bytes = bytes;
+    r.t_submit = S->now();
+    S->queue.push_back(t);
+    *ticket = t;
+  }
+  S->cv_work.notify_one();
+  return GBP_OK;
+}
+
+int gbp_server_poll(gbp_server* S, int64_t ticket, int wait_ms, int32_t* cutoff, int64_t cap, int64_t* nout,
+                    int32_t* cols, double* lb, double* ub, int64_t* t_submit_ns, int64_t* t_done_ns) {
+  if (!S || !cutoff || !nout || cap < 0 || (cap > 0 && (!cols || !lb || !ub))) return GBP_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return GBP_ERR_INVALID;
+  auto ready = [&] { return it->second.done != 0; };
+  if (wait_ms < 0)
+    S->cv_done.wait(lk, ready);
+  else if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), ready))
+    return GBP_ERR_BUSY;
+  Req& r = it->second;
+  if (t_submit_ns) *t_submit_ns = r.t_submit;
+  if (t_done_ns) *t_done_ns = r.t_done;
+  if (r.rc != GBP_OK) {
+    const int rc = r.rc;
+    S->reqs.erase(it);
+    return rc;
+  }
+  *cutoff = r.cutoff;
+  *nout = (int64_t)r.ocols.size();
+  if (*nout > cap) return GBP_ERR_OVERFLOW;
+  std::memcpy(cols, r.ocols.data(), r.ocols.size() * sizeof(int32_t));
+  std::memcpy(lb, r.olb.data(), r.olb.size() * sizeof(double));
+  std::memcpy(ub, r.oub.data(), r.oub.size() * sizeof(double));
+  S->reqs.erase(it);
+  return GBP_OK;
+}
+
+int gbp_server_stats(const gbp_server* S, int64_t* batches, int64_t* requests, int64_t* max_batch_seen,
+                     int64_t* budget) {
+  if (!S) return GBP_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(const_cast<gbp_server*>(S)->mu);
+  if (batches) *batches = S->batches;
+  if (requests) *requests = S->served;
+  if (max_batch_seen) *max_batch_seen = S->max_seen;
+  if (budget) *budget = S->budget;
+  return GBP_OK;
+}
+
+int gbp_server_destroy(gbp_server* S) {
+  if (!S) return GBP_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  for (Worker& W : S->workers)
+    if (W.th.joinable()) W.th.join();
+  for (Worker& W : S->workers)
+    if (W.ctx) gbp_destroy(W.ctx);
+  delete S;
+  return GBP_OK;
+}
+
+}  // extern "C"

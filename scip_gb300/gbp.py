@@ -26,6 +26,7 @@ GBP_ERR_LIMIT = -5
 GBP_ERR_OVERFLOW = -6
 GBP_ERR_STATE = -7
 GBP_ERR_TOO_LARGE = -8
+GBP_ERR_BUSY = -9
 GBP_FLAG_HOSTLOOP = 1
 GBP_FLAG_NOSORTVARS = 2
 GBP_FLAG_RANGEDROW = 4
@@ -37,7 +38,8 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_row_activities", "gbp_propagate_nodes", "gbp_propagate_nodes_device", "gbp_set_batch_shape",
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
            "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log",
-           "gbp_upload_instance_list", "gbp_get_ranged_log", "gbp_set_bounds", "gbp_propagate_changes"]
+           "gbp_upload_instance_list", "gbp_get_ranged_log", "gbp_set_bounds", "gbp_propagate_changes",
+           "gbp_server_create", "gbp_server_submit", "gbp_server_poll", "gbp_server_stats", "gbp_server_destroy"]
 
 
 class GbpParams(ctypes.Structure):
@@ -109,6 +111,14 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
                                               + [_P] * 11 + [ctypes.c_int64, ctypes.POINTER(GbpParams), _P,
                                                               ctypes.POINTER(GbpResult)])
+    L.gbp_server_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                    ctypes.POINTER(GbpParams), ctypes.c_int64, ctypes.c_int64] + [_P] * 8
+    L.gbp_server_submit.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
+    L.gbp_server_poll.argtypes = [_P, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
+                                  ctypes.POINTER(ctypes.c_int64), _P, _P, _P, ctypes.POINTER(ctypes.c_int64),
+                                  ctypes.POINTER(ctypes.c_int64)]
+    L.gbp_server_stats.argtypes = [_P] + [ctypes.POINTER(ctypes.c_int64)] * 4
+    L.gbp_server_destroy.argtypes = [_P]
     if path is None:
         _lib = L
     return L
@@ -407,3 +417,61 @@ class Propagator:
                                                _ptr(out["ub"]), out_cap, ctypes.byref(res))
         self._check(rc, allow=(GBP_ERR_LIMIT,))
         return res
+
+
+class Server:
+    """libgbp's serving loop (gbp_server_*): node requests against one resident problem and its root bounds, merged
+    by worker threads inside libgbp into batched launches."""
+
+    def __init__(self, inst, rootlb, rootub, params: Optional[GbpParams] = None, device: int = 0, workers: int = 2,
+                 max_batch: int = 4096, hbm_cap: int = 0):
+        self.L = load_library()
+        self.n = inst.n
+        self._keep = [np.ascontiguousarray(a) for a in (inst.rowptr.astype(np.int64), inst.colidx.astype(np.int32),
+                                                        inst.vals, inst.lhs, inst.rhs, inst.isint.astype(np.int8),
+                                                        np.asarray(rootlb, np.float64), np.asarray(rootub, np.float64))]
+        h = _P()
+        par = params if params is not None else default_params()
+        rc = self.L.gbp_server_create(ctypes.byref(h), device, workers, max_batch, hbm_cap, ctypes.byref(par),
+                                      inst.m, inst.n, *[_ptr(a) for a in self._keep])
+        if rc != GBP_OK:
+            raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        self.h = h
+        self._out = (np.empty(self.n, np.int32), np.empty(self.n), np.empty(self.n))
+
+    def submit(self, cols, lb, ub) -> int:
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        lb = np.ascontiguousarray(lb, dtype=np.float64)
+        ub = np.ascontiguousarray(ub, dtype=np.float64)
+        t = ctypes.c_int64()
+        rc = self.L.gbp_server_submit(self.h, len(cols), _ptr(cols), _ptr(lb), _ptr(ub), ctypes.byref(t))
+        if rc != GBP_OK:
+            raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = -1):
+        """(cutoff, cols, lb, ub, t_submit_ns, t_done_ns), or None when the wait ended first."""
+        c, l, u = self._out
+        cut = ctypes.c_int32()
+        n = ctypes.c_int64()
+        ts = ctypes.c_int64()
+        td = ctypes.c_int64()
+        rc = self.L.gbp_server_poll(self.h, ticket, wait_ms, ctypes.byref(cut), self.n, ctypes.byref(n), _ptr(c),
+                                    _ptr(l), _ptr(u), ctypes.byref(ts), ctypes.byref(td))
+        if rc == GBP_ERR_BUSY:
+            return None
+        if rc not in (GBP_OK, GBP_ERR_LIMIT):
+            raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        k = n.value
+        return bool(cut.value), c[:k].copy(), l[:k].copy(), u[:k].copy(), ts.value, td.value
+
+    def stats(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        self.L.gbp_server_stats(self.h, *[ctypes.byref(x) for x in v])
+        return {"batches": v[0].value, "requests": v[1].value, "max_batch": v[2].value, "budget": v[3].value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gbp_server_destroy(self.h)
+            self.h = None
+
