@@ -398,29 +398,6 @@ __device__ void updateActivities(const Num& s, SeqRow& r, double val, double old
 }
 
 // ------------------------------------------------------------------------------------------ marked rows
-// conshdlrMarkConsPropagate / conshdlrUnmarkConsPropagate on a record the caller stores (uniform)
-__device__ __forceinline__ void hdlrMark(W& w, int i, SeqRow& r) {
-  if (!(r.flags & RS_EN) || (r.flags & RS_MP)) return;
-  r.flags |= RS_MP;
-  r.mpos = w.nm;
-  if (w.lane == 0) w.M[w.nm] = i;
-  w.nm += 1;
-}
-__device__ __forceinline__ void hdlrUnmark(W& w, SeqRow& r) {
-  if (!(r.flags & RS_EN) || !(r.flags & RS_MP)) return;
-  r.flags &= ~RS_MP;
-  const int pos = r.mpos;
-  r.mpos = -1;
-  w.nm -= 1;
-  if (pos < w.nm) {
-    const int last = w.M[w.nm];
-    if (w.lane == 0) {
-      w.M[pos] = last;
-      w.rs[last].mpos = pos;
-    }
-  }
-  __syncwarp();
-}
 __device__ __forceinline__ void addUpdate(W& w, int i, SeqRow& r) {
   if (r.flags & RS_INUPD) return;
   r.flags |= RS_INUPD;
@@ -439,22 +416,47 @@ __device__ __forceinline__ void disableRow(W& w, int i, SeqRow& r) {
   r.flags |= RS_UD;
   addUpdate(w, i, r);
 }
-// conshdlrProcessUpdates: the delayed updates, the last added first (uniform)
+// conshdlrProcessUpdates: the delayed updates, the last added first
 __device__ __noinline__ void processUpdates(W& w) {
-  for (int k = w.nu - 1; k >= 0; --k) {
-    const int i = w.U[k];
-    SeqRow r = w.rs[i];
-    if (r.flags & RS_UD) {
-      hdlrUnmark(w, r);
-      r.flags &= ~(RS_EN | RS_UD);
+  // scalar list work on two fields of each record (flags, list position): one lane does it, the others wait
+  int nm = w.nm;
+  if (w.lane == 0) {
+    for (int k = w.nu - 1; k >= 0; --k) {
+      const int i = w.U[k];
+      unsigned f = w.rs[i].flags;
+      int mpos = w.rs[i].mpos;  // an earlier unmark in this loop may have moved the row
+      auto unmark = [&]() {     // conshdlrUnmarkConsPropagate: the last marked row moves into the hole
+        if (!(f & RS_EN) || !(f & RS_MP)) return;
+        f &= ~RS_MP;
+        const int pos = mpos;
+        mpos = -1;
+        nm -= 1;
+        if (pos < nm) {
+          const int last = w.M[nm];
+          w.M[pos] = last;
+          w.rs[last].mpos = pos;
+        }
+      };
+      if (f & RS_UD) {
+        unmark();
+        f &= ~(RS_EN | RS_UD);
+      }
+      if (f & RS_UM) {  // conshdlrMarkConsPropagate: append
+        if ((f & RS_EN) && !(f & RS_MP)) {
+          f |= RS_MP;
+          mpos = nm;
+          w.M[nm] = i;
+          nm += 1;
+        }
+      } else if (f & RS_UU) {
+        unmark();
+      }
+      w.rs[i].flags = f & ~(RS_UM | RS_UU | RS_INUPD);
+      w.rs[i].mpos = mpos;
     }
-    if (r.flags & RS_UM) hdlrMark(w, i, r);
-    else if (r.flags & RS_UU) hdlrUnmark(w, r);
-    r.flags &= ~(RS_UM | RS_UU | RS_INUPD);
-    // hdlrUnmark of another row may have rewritten this row's mpos field in memory: only this row's own
-    // operations change its record here, so store the whole record
-    storeRow(w, i, r);
   }
+  __syncwarp();
+  w.nm = __shfl_sync(FULL, nm, 0);
   w.nu = 0;
 }
 
