@@ -783,6 +783,20 @@ def main():
                                     "kind": "port", "sample": sample,
                                     "one_core": {"value": one_v, "sample": one_sample}}
             line["cpu_baseline"].update(scip_calibration())
+            if scip_order is not None:
+                # the oracle's restatement of SCIP's order on the arm's nodes (SCIP's root and orders), all host cores
+                base = instances.pinned_node_base(inst, os.path.join(ROOT, "tests", "golden", "workload",
+                                                                     "node_workload_base.npz"))
+                if base is not None:
+                    blb, bub, border = base
+                    bnodes = instances.node_batch(inst, blb, bub, N, seed=replicas.node_seed(3, rank))
+                    so = orc.Oracle(instances.in_order(inst, border))
+                    t0 = time.perf_counter()
+                    so.propagate_nodes(blb, bub, bnodes, par, cap=1, nthreads=os.cpu_count() or 1, seq=True)
+                    dt = time.perf_counter() - t0
+                    scip_order["cpu_baseline"] = {"value": N / dt, "unit": "node-fixpoints/s",
+                                                  "cores": os.cpu_count() or 1, "kind": "port",
+                                                  "sample": f"all {N} nodes once, {dt:.2f} s wall"}
         print(json.dumps(line))
     prop.close()
     if world > 1:
