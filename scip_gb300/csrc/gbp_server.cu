@@ -64,7 +64,7 @@ struct gbp_server {
   int64_t max_batch = 0;
   std::vector<double> rootlb, rootub;
   std::vector<Worker> workers;
-  std::mutex mu;
+  mutable std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<int64_t> queue;
   std::unordered_map<int64_t, Req> reqs;
@@ -328,7 +328,7 @@ int gbp_server_poll(gbp_server* S, int64_t ticket, int wait_ms, int32_t* cutoff,
 int gbp_server_stats(const gbp_server* S, int64_t* batches, int64_t* requests, int64_t* max_batch_seen,
                      int64_t* budget) {
   if (!S) return GBP_ERR_INVALID;
-  std::lock_guard<std::mutex> lk(const_cast<gbp_server*>(S)->mu);
+  std::lock_guard<std::mutex> lk(S->mu);
   if (batches) *batches = S->batches;
   if (requests) *requests = S->served;
   if (max_batch_seen) *max_batch_seen = S->max_seen;

@@ -72,3 +72,30 @@ def test_noalloc_argument_checks_need_no_device(lib):
     assert rc == gbp.GBP_ERR_INVALID
     rc = lib.gbp_propagate_nodes_noalloc(10, 10, *([None] * 11), 1, *([None] * 11), 0, None, None, ctypes.byref(res))
     assert rc == gbp.GBP_ERR_INVALID
+
+
+def test_server_argument_checks_need_no_device(lib):
+    """The serving loop's calls reject bad arguments before anything touches a device, and a server cannot be
+    created without one."""
+    import numpy as np
+
+    h = ctypes.c_void_p()
+    par = gbp.default_params()
+    # no workers, a negative cap, missing root bounds
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 0, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+        gbp.GBP_ERR_INVALID
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 16, -1, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+        gbp.GBP_ERR_INVALID
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+        gbp.GBP_ERR_INVALID
+    assert lib.gbp_server_submit(None, 0, None, None, None, None) == gbp.GBP_ERR_INVALID
+    assert lib.gbp_server_destroy(None) == gbp.GBP_ERR_INVALID
+    assert lib.gbp_error_string(gbp.GBP_ERR_BUSY).decode() == "reply not ready"
+    if not _has_gpu():
+        from scip_gb300 import instances
+
+        inst = instances.root_mip(0, m=50, n=100)
+        with pytest.raises(gbp.GbpError) as e:
+            gbp.Server(inst, inst.lb, inst.ub, workers=1)
+        assert e.value.code == gbp.GBP_ERR_NODEVICE
+        assert np.isfinite(inst.lb).all()
