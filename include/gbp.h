@@ -251,7 +251,7 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * gbp_propagate_nodes_device.  params == NULL uses the defaults of gbp_default_params. */
 /* ---------------------------------------------------------------- serving
  * A request loop inside libgbp for branch-and-bound node requests against one resident problem and its root bounds
- * (the served form of the batched path).  A client thread submits a node -- bound changes, as one node of
+ * (the served form of the batched path), and for instance requests (below).  A client thread submits a node -- bound changes, as one node of
  * gbp_propagate_nodes -- and gets a ticket at once.  nworkers worker threads, each with its own context and stream,
  * take everything queued (up to max_batch nodes) and propagate it in one batched launch, so that requests arriving
  * together share a launch and the batches of different workers overlap on the device.  Admission: at creation every
@@ -265,11 +265,20 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * first.  A reply is released once read.  t_submit_ns / t_done_ns (may be NULL): when the server took the request and
  * when its batch finished (ns of a steady clock started with the server). */
 typedef struct gbp_server gbp_server;
-int gbp_server_create(gbp_server** out, int device, int nworkers, int64_t max_batch, int64_t hbm_cap,
-   const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals,
-   const double* lhs, const double* rhs, const int8_t* isint, const double* rootlb, const double* rootub);
+int gbp_server_create(gbp_server** out, int device, int nworkers, int ninstworkers, int64_t max_batch,
+   int64_t hbm_cap, const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+   const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const double* rootlb,
+   const double* rootub);
 int gbp_server_submit(gbp_server* srv, int64_t nchg, const int32_t* cols, const double* lb, const double* ub,
    int64_t* ticket);
+/* an instance request: a problem of its own (m rows in CSR over its n local columns, sides, integrality, bounds),
+ * answered with its root fixpoint -- the reply's columns are 0..n-1 in order with their final bounds, or a cutoff.
+ * ninstworkers worker threads (each with its own context) upload everything queued as parts of one block-diagonal
+ * problem (gbp_upload_instance_list) and propagate it in one batched launch (gbp_propagate_instances).  A server
+ * created without instance workers refuses instance requests (GBP_ERR_INVALID). */
+int gbp_server_submit_instance(gbp_server* srv, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+   const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const double* lb,
+   const double* ub, int64_t* ticket);
 int gbp_server_poll(gbp_server* srv, int64_t ticket, int wait_ms, int32_t* cutoff, int64_t cap, int64_t* nout,
    int32_t* cols, double* lb, double* ub, int64_t* t_submit_ns, int64_t* t_done_ns);
 /* batches launched, requests served, the largest batch, the admission budget in bytes */

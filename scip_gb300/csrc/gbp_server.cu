@@ -17,8 +17,15 @@
 namespace {
 
 struct Req {
+  int kind = 0;  // 0 node, 1 instance
   std::vector<int32_t> cols;
   std::vector<double> lb, ub;
+  // an instance request: its rows (CSR over local columns) and integrality; lb/ub above are its bounds
+  int64_t m = 0;
+  std::vector<int64_t> rowptr;
+  std::vector<int32_t> colidx;
+  std::vector<double> vals, lhs, rhs;
+  std::vector<int8_t> isint;
   int64_t t_submit = 0, t_done = 0;
   int done = 0;
   int rc = GBP_OK;
@@ -49,6 +56,7 @@ struct Pinned {
 
 struct Worker {
   gbp_ctx* ctx = nullptr;
+  int kind = 0;  // 0 node requests, 1 instance requests
   std::thread th;
   Pinned<int64_t> ptr, off;
   Pinned<int32_t> col, rounds, n, ocol;
@@ -66,7 +74,8 @@ struct gbp_server {
   std::vector<Worker> workers;
   mutable std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<int64_t> queue;
+  std::deque<int64_t> queue;   // node requests
+  std::deque<int64_t> iqueue;  // instance requests
   std::unordered_map<int64_t, Req> reqs;
   int64_t next_ticket = 1;
   bool stop = false;
@@ -171,8 +180,57 @@ void runBatch(gbp_server* S, Worker& W, std::vector<Req*>& batch) {
   }
 }
 
+// propagate a batch of instance requests on an instance worker: one upload of the instances as parts of a
+// block-diagonal problem, one batched root fixpoint, each request's bounds back
+void runInstances(Worker& W, std::vector<Req*>& batch) {
+  const size_t k = batch.size();
+  std::vector<int64_t> mk(k), nk(k);
+  std::vector<const int64_t*> rp(k);
+  std::vector<const int32_t*> ci(k);
+  std::vector<const double*> va(k), lh(k), rh(k);
+  std::vector<const int8_t*> it(k);
+  std::vector<double> lb, ub;
+  for (size_t q = 0; q < k; ++q) {
+    const Req* r = batch[q];
+    mk[q] = r->m;
+    nk[q] = (int64_t)r->lb.size();
+    rp[q] = r->rowptr.data();
+    ci[q] = r->colidx.data();
+    va[q] = r->vals.data();
+    lh[q] = r->lhs.data();
+    rh[q] = r->rhs.data();
+    it[q] = r->isint.data();
+    lb.insert(lb.end(), r->lb.begin(), r->lb.end());
+    ub.insert(ub.end(), r->ub.begin(), r->ub.end());
+  }
+  std::vector<int8_t> cut(k, 0);
+  gbp_result res;
+  int rc = gbp_upload_instance_list(W.ctx, (int64_t)k, mk.data(), nk.data(), rp.data(), ci.data(), va.data(),
+                                    lh.data(), rh.data(), it.data());
+  if (rc == GBP_OK) rc = gbp_propagate_instances(W.ctx, lb.data(), ub.data(), cut.data(), &res);
+  int64_t at = 0;
+  for (size_t q = 0; q < k; ++q) {
+    Req* r = batch[q];
+    const int64_t n = nk[q];
+    if (rc != GBP_OK && rc != GBP_ERR_LIMIT) {
+      r->rc = rc;
+    } else {
+      r->cutoff = cut[q];
+      if (!r->cutoff) {  // the whole bound vector: every column in order
+        r->ocols.resize((size_t)n);
+        for (int64_t j = 0; j < n; ++j) r->ocols[j] = (int32_t)j;
+        r->olb.assign(lb.begin() + at, lb.begin() + at + n);
+        r->oub.assign(ub.begin() + at, ub.begin() + at + n);
+      }
+    }
+    at += n;
+  }
+}
+
 void workerLoop(gbp_server* S, Worker* W) {
   cudaSetDevice(S->device);
+  std::deque<int64_t>& Q = W->kind == 0 ? S->queue : S->iqueue;
+  const int64_t maxb = W->kind == 0 ? S->max_batch : std::max<int64_t>(1, S->max_batch / 8);
   std::vector<Req*> batch;
   std::vector<int64_t> tickets;
   for (;;) {
@@ -180,25 +238,29 @@ void workerLoop(gbp_server* S, Worker* W) {
     {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv_work.wait(lk, [&] {
-        return S->stop || (!S->queue.empty() && S->inflight + S->reqs[S->queue.front()].bytes <= S->budget);
+        return S->stop || (!Q.empty() && S->inflight + S->reqs[Q.front()].bytes <= S->budget);
       });
-      if (S->queue.empty()) {
+      if (Q.empty()) {
         if (S->stop) return;
         continue;
       }
       batch.clear();
       tickets.clear();
-      while (!S->queue.empty() && (int64_t)batch.size() < S->max_batch) {
-        Req& r = S->reqs[S->queue.front()];
+      while (!Q.empty() && (int64_t)batch.size() < maxb) {
+        Req& r = S->reqs[Q.front()];
         if (S->inflight + bytes + r.bytes > S->budget) break;
         bytes += r.bytes;
         batch.push_back(&r);
-        tickets.push_back(S->queue.front());
-        S->queue.pop_front();
+        tickets.push_back(Q.front());
+        Q.pop_front();
       }
       S->inflight += bytes;
     }
-    runBatch(S, *W, batch);  // Req objects stay put: only this worker and the pollers of done tickets touch them
+    // Req objects stay put: only this worker and the pollers of done tickets touch them
+    if (W->kind == 0)
+      runBatch(S, *W, batch);
+    else
+      runInstances(*W, batch);
     {
       std::lock_guard<std::mutex> lk(S->mu);
       const int64_t t = S->now();
@@ -220,11 +282,12 @@ void workerLoop(gbp_server* S, Worker* W) {
 
 extern "C" {
 
-int gbp_server_create(gbp_server** out, int device, int nworkers, int64_t max_batch, int64_t hbm_cap,
-                      const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
-                      const double* vals, const double* lhs, const double* rhs, const int8_t* isint,
-                      const double* rootlb, const double* rootub) {
-  if (!out || nworkers < 1 || max_batch < 1 || hbm_cap < 0 || m < 0 || n < 0 || (n > 0 && (!rootlb || !rootub)))
+int gbp_server_create(gbp_server** out, int device, int nworkers, int ninstworkers, int64_t max_batch,
+                      int64_t hbm_cap, const gbp_params* params, int64_t m, int64_t n, const int64_t* rowptr,
+                      const int32_t* colidx, const double* vals, const double* lhs, const double* rhs,
+                      const int8_t* isint, const double* rootlb, const double* rootub) {
+  if (!out || nworkers < 1 || ninstworkers < 0 || max_batch < 1 || hbm_cap < 0 || m < 0 || n < 0 ||
+      (n > 0 && (!rootlb || !rootub)))
     return GBP_ERR_INVALID;
   *out = nullptr;
   gbp_server* S = new (std::nothrow) gbp_server();
@@ -236,12 +299,16 @@ int gbp_server_create(gbp_server** out, int device, int nworkers, int64_t max_ba
   S->rootlb.assign(rootlb, rootlb + n);
   S->rootub.assign(rootub, rootub + n);
   S->t0 = std::chrono::steady_clock::now();
-  S->workers.resize((size_t)nworkers);
+  S->workers.resize((size_t)(nworkers + ninstworkers));
   int rc = GBP_OK;
-  for (Worker& W : S->workers) {
+  for (size_t q = 0; q < S->workers.size(); ++q) {
+    Worker& W = S->workers[q];
+    W.kind = (int)q < nworkers ? 0 : 1;
     rc = gbp_create(&W.ctx, device, nullptr);
     if (rc == GBP_OK && params) rc = gbp_set_params(W.ctx, params);
-    if (rc == GBP_OK) rc = gbp_upload_problem(W.ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
+    if (rc != GBP_OK) break;
+    if (W.kind == 1) continue;  // an instance worker uploads each batch's instances
+    rc = gbp_upload_problem(W.ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
     if (rc != GBP_OK) break;
     // a first batch (a node without changes) allocates the worker's slots before the budget is measured
     std::vector<Req> warm(1);
@@ -292,7 +359,48 @@ int gbp_server_submit(gbp_server* S, int64_t nchg, const int32_t* cols, const do
     S->queue.push_back(t);
     *ticket = t;
   }
-  S->cv_work.notify_one();
+  S->cv_work.notify_all();
+  return GBP_OK;
+}
+
+int gbp_server_submit_instance(gbp_server* S, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                               const double* vals, const double* lhs, const double* rhs, const int8_t* isint,
+                               const double* lb, const double* ub, int64_t* ticket) {
+  if (!S || !ticket || m < 0 || n < 0 || !rowptr || (m > 0 && (!lhs || !rhs)) || (n > 0 && (!isint || !lb || !ub)))
+    return GBP_ERR_INVALID;
+  if (rowptr[0] != 0) return GBP_ERR_INVALID;
+  for (int64_t i = 0; i < m; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return GBP_ERR_INVALID;
+  const int64_t nnz = rowptr[m];
+  if (nnz > 0 && (!colidx || !vals)) return GBP_ERR_INVALID;
+  for (int64_t p = 0; p < nnz; ++p)
+    if (colidx[p] < 0 || colidx[p] >= n) return GBP_ERR_INVALID;
+  const int64_t bytes = 28 * nnz + 64 * m + 64 * n + 4096;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) return GBP_ERR_INVALID;
+    bool any = false;
+    for (const Worker& W : S->workers) any |= W.kind == 1;
+    if (!any) return GBP_ERR_INVALID;  // the server has no instance workers
+    if (bytes > S->budget) return GBP_ERR_NOMEM;
+    const int64_t t = S->next_ticket++;
+    Req& r = S->reqs[t];
+    r.kind = 1;
+    r.m = m;
+    r.rowptr.assign(rowptr, rowptr + m + 1);
+    r.colidx.assign(colidx, colidx + nnz);
+    r.vals.assign(vals, vals + nnz);
+    r.lhs.assign(lhs, lhs + m);
+    r.rhs.assign(rhs, rhs + m);
+    r.isint.assign(isint, isint + n);
+    r.lb.assign(lb, lb + n);
+    r.ub.assign(ub, ub + n);
+    r.bytes = bytes;
+    r.t_submit = S->now();
+    S->iqueue.push_back(t);
+    *ticket = t;
+  }
+  S->cv_work.notify_all();
   return GBP_OK;
 }
 

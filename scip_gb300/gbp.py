@@ -39,7 +39,8 @@ EXPORTS = ["gbp_version", "gbp_error_string", "gbp_last_error", "gbp_create", "g
            "gbp_propagate_nodes_noalloc", "gbp_upload_instances", "gbp_propagate_instances",
            "gbp_propagate_instances_device", "gbp_set_global_bounds", "gbp_set_change_log", "gbp_get_change_log",
            "gbp_upload_instance_list", "gbp_get_ranged_log", "gbp_set_bounds", "gbp_propagate_changes",
-           "gbp_server_create", "gbp_server_submit", "gbp_server_poll", "gbp_server_stats", "gbp_server_destroy"]
+           "gbp_server_create", "gbp_server_submit", "gbp_server_submit_instance", "gbp_server_poll", "gbp_server_stats",
+           "gbp_server_destroy"]
 
 
 class GbpParams(ctypes.Structure):
@@ -111,9 +112,11 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
                                               + [_P] * 11 + [ctypes.c_int64, ctypes.POINTER(GbpParams), _P,
                                                               ctypes.POINTER(GbpResult)])
-    L.gbp_server_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
-                                    ctypes.POINTER(GbpParams), ctypes.c_int64, ctypes.c_int64] + [_P] * 8
+    L.gbp_server_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.POINTER(GbpParams), ctypes.c_int64, ctypes.c_int64] + [_P] * 8
     L.gbp_server_submit.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
+    L.gbp_server_submit_instance.argtypes = [_P, ctypes.c_int64, ctypes.c_int64] + [_P] * 8 + [
+        ctypes.POINTER(ctypes.c_int64)]
     L.gbp_server_poll.argtypes = [_P, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
                                   ctypes.POINTER(ctypes.c_int64), _P, _P, _P, ctypes.POINTER(ctypes.c_int64),
                                   ctypes.POINTER(ctypes.c_int64)]
@@ -424,7 +427,7 @@ class Server:
     by worker threads inside libgbp into batched launches."""
 
     def __init__(self, inst, rootlb, rootub, params: Optional[GbpParams] = None, device: int = 0, workers: int = 2,
-                 max_batch: int = 4096, hbm_cap: int = 0):
+                 max_batch: int = 4096, hbm_cap: int = 0, inst_workers: int = 0):
         self.L = load_library()
         self.n = inst.n
         self._keep = [np.ascontiguousarray(a) for a in (inst.rowptr.astype(np.int64), inst.colidx.astype(np.int32),
@@ -432,8 +435,8 @@ class Server:
                                                         np.asarray(rootlb, np.float64), np.asarray(rootub, np.float64))]
         h = _P()
         par = params if params is not None else default_params()
-        rc = self.L.gbp_server_create(ctypes.byref(h), device, workers, max_batch, hbm_cap, ctypes.byref(par),
-                                      inst.m, inst.n, *[_ptr(a) for a in self._keep])
+        rc = self.L.gbp_server_create(ctypes.byref(h), device, workers, inst_workers, max_batch, hbm_cap,
+                                      ctypes.byref(par), inst.m, inst.n, *[_ptr(a) for a in self._keep])
         if rc != GBP_OK:
             raise GbpError(rc, self.L.gbp_error_string(rc).decode())
         self.h = h
@@ -449,14 +452,29 @@ class Server:
             raise GbpError(rc, self.L.gbp_error_string(rc).decode())
         return t.value
 
-    def poll(self, ticket: int, wait_ms: int = -1):
-        """(cutoff, cols, lb, ub, t_submit_ns, t_done_ns), or None when the wait ended first."""
+    def submit_instance(self, inst) -> int:
+        """An instance request (a problem of its own, answered with its root fixpoint); needs inst_workers > 0."""
+        arrs = [np.ascontiguousarray(a) for a in (inst.rowptr.astype(np.int64), inst.colidx.astype(np.int32),
+                                                  inst.vals.astype(np.float64), inst.lhs.astype(np.float64),
+                                                  inst.rhs.astype(np.float64), inst.isint.astype(np.int8),
+                                                  inst.lb.astype(np.float64), inst.ub.astype(np.float64))]
+        t = ctypes.c_int64()
+        rc = self.L.gbp_server_submit_instance(self.h, inst.m, inst.n, *[_ptr(a) for a in arrs], ctypes.byref(t))
+        if rc != GBP_OK:
+            raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = -1, cap: Optional[int] = None):
+        """(cutoff, cols, lb, ub, t_submit_ns, t_done_ns), or None when the wait ended first.  An instance reply
+        holds every column of the instance: give cap >= its columns when they exceed the resident problem's."""
+        if cap is not None and cap > len(self._out[0]):
+            self._out = (np.empty(cap, np.int32), np.empty(cap), np.empty(cap))
         c, l, u = self._out
         cut = ctypes.c_int32()
         n = ctypes.c_int64()
         ts = ctypes.c_int64()
         td = ctypes.c_int64()
-        rc = self.L.gbp_server_poll(self.h, ticket, wait_ms, ctypes.byref(cut), self.n, ctypes.byref(n), _ptr(c),
+        rc = self.L.gbp_server_poll(self.h, ticket, wait_ms, ctypes.byref(cut), len(c), ctypes.byref(n), _ptr(c),
                                     _ptr(l), _ptr(u), ctypes.byref(ts), ctypes.byref(td))
         if rc == GBP_ERR_BUSY:
             return None

@@ -82,13 +82,14 @@ def test_server_argument_checks_need_no_device(lib):
     h = ctypes.c_void_p()
     par = gbp.default_params()
     # no workers, a negative cap, missing root bounds
-    assert lib.gbp_server_create(ctypes.byref(h), 0, 0, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 0, 0, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
         gbp.GBP_ERR_INVALID
-    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 16, -1, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 0, 16, -1, ctypes.byref(par), 1, 1, *([None] * 8)) == \
         gbp.GBP_ERR_INVALID
-    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
+    assert lib.gbp_server_create(ctypes.byref(h), 0, 1, 0, 16, 0, ctypes.byref(par), 1, 1, *([None] * 8)) == \
         gbp.GBP_ERR_INVALID
     assert lib.gbp_server_submit(None, 0, None, None, None, None) == gbp.GBP_ERR_INVALID
+    assert lib.gbp_server_submit_instance(None, 0, 0, *([None] * 8), None) == gbp.GBP_ERR_INVALID
     assert lib.gbp_server_destroy(None) == gbp.GBP_ERR_INVALID
     assert lib.gbp_error_string(gbp.GBP_ERR_BUSY).decode() == "reply not ready"
     if not _has_gpu():

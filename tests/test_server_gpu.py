@@ -79,3 +79,31 @@ def test_admission_and_bad_requests(oracle_mod):
         assert r is not None and r[0] == bool(want["cutoff"][1])
     finally:
         srv.close()
+
+
+def test_instance_requests_beside_node_requests(oracle_mod):
+    """Instance requests (problems of their own) go to instance workers, which upload what is queued as one
+    block-diagonal problem and propagate it in one launch; every reply equals the oracle's root fixpoint of that
+    instance bit for bit, while node requests are served beside them."""
+    inst, rlb, rub, nodes, want = _setup(oracle_mod, m=5000, nnodes=64)
+    pool = instances.uneven_batch(seed=41, count=24)
+    pool = [p for p in pool if p.m <= 20000][:12]
+    srv = gbp.Server(inst, rlb, rub, params=gbp.default_params(maxeasy=0.0), workers=1, inst_workers=2)
+    try:
+        tk_i = [srv.submit_instance(p) for p in pool]
+        tk_n = []
+        for k in range(nodes.nnodes):
+            sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+            tk_n.append(srv.submit(nodes.col[sl], nodes.lb[sl], nodes.ub[sl]))
+        for p, t in zip(pool, tk_i):
+            cut, c, l, u, _, _ = srv.poll(t, cap=max(p.n, inst.n))
+            olb, oub, ores = oracle_mod.Oracle(p).propagate(p.lb, p.ub, oracle_mod.params(0.0))
+            assert cut == bool(ores.cutoff)
+            if not cut:
+                assert np.array_equal(c, np.arange(p.n)) and np.array_equal(l, olb) and np.array_equal(u, oub)
+        for k, t in enumerate(tk_n):
+            cut, c, _, _, _, _ = srv.poll(t)
+            assert cut == bool(want["cutoff"][k])
+    finally:
+        srv.close()
+
