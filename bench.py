@@ -419,6 +419,103 @@ def time_served(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), durat
     return out
 
 
+def time_served_mix(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), duration=0.2, node_frac=0.8):
+    """The served mix through libgbp's C serving loop: open-loop Poisson arrivals, node_frac of them single-node
+    requests (the bench's nodes in turn) and the rest new instances drawn from 24 instances of the uneven-instance
+    generator (rows log-uniform in [1e3, 2e5]), at each offered rate for `duration` seconds.  Two node workers merge
+    node requests into batched k_nodes launches; two instance workers upload queued instances as one block-diagonal
+    problem each and propagate it in one launch.  Instance arrays are borrowed by the server (no host copy), so each
+    instance request costs its upload: host-to-device bytes bound the instance side.  Latency = the server's time
+    from admitting a request to finishing its batch, per kind and overall."""
+    import ctypes
+
+    from scip_gb300 import gbp, instances
+
+    pool = instances.uneven_batch(seed=41, count=24)
+    parts = []
+    for p in pool:
+        arrs = [np.ascontiguousarray(a, dtype=d) for a, d in ((p.rowptr, np.int64), (p.colidx, np.int32),
+                                                             (p.vals, np.float64), (p.lhs, np.float64),
+                                                             (p.rhs, np.float64), (p.isint, np.int8),
+                                                             (p.lb, np.float64), (p.ub, np.float64))]
+        parts.append((p.m, p.n, arrs, [a.ctypes.data_as(ctypes.c_void_p) for a in arrs],
+                      sum(a.nbytes for a in arrs)))
+    node_reqs = []
+    for k in range(nodes.nnodes):
+        sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+        arrs = (np.ascontiguousarray(nodes.col[sl], np.int32), np.ascontiguousarray(nodes.lb[sl]),
+                np.ascontiguousarray(nodes.ub[sl]))
+        node_reqs.append((len(arrs[0]), arrs, [a.ctypes.data_as(ctypes.c_void_p) for a in arrs]))
+    cap = max(max(p.n for p in pool), inst.n)
+    oc, ol, ou = np.empty(cap, np.int32), np.empty(cap), np.empty(cap)
+    ocp, olp, oup = (a.ctypes.data_as(ctypes.c_void_p) for a in (oc, ol, ou))
+    srv = gbp.Server(inst, rlb, rub, params=params, workers=2, inst_workers=2, max_batch=4096)
+    L = srv.L
+    out = {}
+    t = ctypes.c_int64()
+    cut, nout, ts, td = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    try:
+        # warm-up: every pool instance once, so that the instance workers' contexts hold a first allocation
+        warm = []
+        for m_, n_, _, ptrs, _ in parts:
+            if L.gbp_server_submit_instance(srv.h, m_, n_, *ptrs, ctypes.byref(t)) != gbp.GBP_OK:
+                raise gbp.GbpError(gbp.GBP_ERR_INVALID, "warm-up submit")
+            warm.append(t.value)
+        for tk in warm:
+            L.gbp_server_poll(srv.h, tk, -1, ctypes.byref(cut), cap, ctypes.byref(nout), ocp, olp, oup, None, None)
+        for rate in rates:
+            rng = np.random.default_rng(np.random.PCG64(rate + 7))
+            n = int(rate * duration)
+            due = np.cumsum(rng.exponential(1.0 / rate, n))
+            isnode = rng.random(n) < node_frac
+            pick = rng.integers(0, len(parts), n)
+            tickets, h2d = [], 0
+            t0 = time.perf_counter()
+            lag = 0.0
+            for i in range(n):
+                while time.perf_counter() - t0 < due[i]:
+                    pass
+                lag = max(lag, time.perf_counter() - t0 - due[i])
+                if isnode[i]:
+                    nc, _, ptrs = node_reqs[i % len(node_reqs)]
+                    rc = L.gbp_server_submit(srv.h, nc, ptrs[0], ptrs[1], ptrs[2], ctypes.byref(t))
+                else:
+                    m_, n_, _, ptrs, nbytes = parts[pick[i]]
+                    rc = L.gbp_server_submit_instance(srv.h, m_, n_, *ptrs, ctypes.byref(t))
+                    h2d += nbytes
+                if rc != gbp.GBP_OK:
+                    raise gbp.GbpError(rc, "submit")
+                tickets.append(t.value)
+            sub_s = time.perf_counter() - t0
+            tsa, tda, errs = np.zeros(n, np.int64), np.zeros(n, np.int64), 0
+            for q, tk in enumerate(tickets):
+                rc = L.gbp_server_poll(srv.h, tk, -1, ctypes.byref(cut), cap, ctypes.byref(nout), ocp, olp, oup,
+                                       ctypes.byref(ts), ctypes.byref(td))
+                errs += rc not in (gbp.GBP_OK, gbp.GBP_ERR_LIMIT)
+                tsa[q], tda[q] = ts.value, td.value
+            lat = (tda - tsa) / 1e6
+            wall = (tda.max() - tsa.min()) / 1e9
+            row = {"offered_req_s": rate, "requests": n, "instance_requests": int((~isnode).sum()),
+                   "submitted_req_s": n / sub_s, "max_submit_lag_ms": 1e3 * lag, "errors": errs,
+                   "throughput_req_s": n / wall, "p50_ms": float(np.percentile(lat, 50)),
+                   "p99_ms": float(np.percentile(lat, 99)), "instance_h2d_gb_s": h2d / wall / 1e9}
+            for kind, sel in (("node", isnode), ("instance", ~isnode)):
+                if sel.any():
+                    row[kind] = {"p50_ms": float(np.percentile(lat[sel], 50)),
+                                 "p99_ms": float(np.percentile(lat[sel], 99)),
+                                 "served_req_s": int(sel.sum()) / ((tda[sel].max() - tsa[sel].min()) / 1e9)}
+            out[str(rate)] = row
+        out["stats"] = srv.stats()
+        out["call"] = ("gbp_server_submit / gbp_server_submit_instance / gbp_server_poll (2 node + 2 instance "
+                       "worker threads)")
+        out["mix"] = f"{node_frac:.0%} node requests, the rest instances of the uneven-instance generator " \
+                     f"({sum(p.m for p in pool) // len(pool):,} rows and {sum(p.nnz for p in pool) // len(pool):,} " \
+                     "nonzeros on average)"
+    finally:
+        srv.close()
+    return out
+
+
 def time_scip_order(args, inst, rlb, rub, nodes, N, dev, flush, world, seed):
     """Node-fixpoints/s of the batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER), inputs resident in HBM, CUDA
     events around each step, the L2 flushed between steps.  On the default instance the nodes start from SCIP's own
@@ -692,6 +789,11 @@ def main():
     served = None
     if not args.ranged and world == 1:
         served = time_served(inst, rlb, rub, nodes, gbp.default_params(maxeasy=args.maxeasy))
+        # the 80 % node / 20 % instance mix through the same loop
+        try:
+            served["mix"] = time_served_mix(inst, rlb, rub, nodes, gbp.default_params(maxeasy=args.maxeasy))
+        except gbp.GbpError as e:
+            served["mix"] = {"error": str(e)}
 
     # the same nodes in SCIP's own order (GBP_FLAG_SCIPORDER): rows uploaded in the order SCIP sorts them into on the
     # base domain, device-resident inputs, the same timing

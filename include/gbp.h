@@ -251,8 +251,8 @@ int gbp_set_batch_shape(gbp_ctx* ctx, int32_t threads_per_node, int32_t ctas_per
  * gbp_propagate_nodes_device.  params == NULL uses the defaults of gbp_default_params. */
 /* ---------------------------------------------------------------- serving
  * A request loop inside libgbp for branch-and-bound node requests against one resident problem and its root bounds
- * (the served form of the batched path), and for instance requests (below).  A client thread submits a node -- bound changes, as one node of
- * gbp_propagate_nodes -- and gets a ticket at once.  nworkers worker threads, each with its own context and stream,
+ * (the served form of the batched path), and for instance requests (below).  A client thread submits a node -- bound
+ * changes, as one node of gbp_propagate_nodes -- and gets a ticket at once; the node's arrays are copied.  nworkers worker threads, each with its own context and stream,
  * take everything queued (up to max_batch nodes) and propagate it in one batched launch, so that requests arriving
  * together share a launch and the batches of different workers overlap on the device.  Admission: at creation every
  * worker runs a first batch (its slot memory is allocated then); the budget for the device bytes of batches in flight
@@ -274,8 +274,14 @@ int gbp_server_submit(gbp_server* srv, int64_t nchg, const int32_t* cols, const 
 /* an instance request: a problem of its own (m rows in CSR over its n local columns, sides, integrality, bounds),
  * answered with its root fixpoint -- the reply's columns are 0..n-1 in order with their final bounds, or a cutoff.
  * ninstworkers worker threads (each with its own context) upload everything queued as parts of one block-diagonal
- * problem (gbp_upload_instance_list) and propagate it in one batched launch (gbp_propagate_instances).  A server
- * created without instance workers refuses instance requests (GBP_ERR_INVALID). */
+ * problem (gbp_upload_instance_list) and propagate it in one batched launch (gbp_propagate_instances), taking up to
+ * max_batch / 8 instances at once.  The instance's arrays are BORROWED, not copied: they must stay valid and
+ * unchanged until gbp_server_poll has returned this ticket's reply (or an error other than GBP_ERR_BUSY and
+ * GBP_ERR_OVERFLOW).  Submission checks the pointers and rowptr[0] == 0; the upload checks that the row pointers do
+ * not decrease and that every column index lies in [0, n), and a request that fails them is answered
+ * GBP_ERR_INVALID by gbp_server_poll while the rest of its batch is served.  A server created without instance
+ * workers refuses instance requests (GBP_ERR_INVALID).  The device memory an instance worker's context holds for
+ * its largest batch stays allocated until gbp_server_destroy and is not counted against the admission budget. */
 int gbp_server_submit_instance(gbp_server* srv, int64_t m, int64_t n, const int64_t* rowptr, const int32_t* colidx,
    const double* vals, const double* lhs, const double* rhs, const int8_t* isint, const double* lb,
    const double* ub, int64_t* ticket);

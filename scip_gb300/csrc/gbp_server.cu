@@ -1,5 +1,7 @@
 // The serving loop of libgbp (gbp_server_*): node requests against one resident problem and its root bounds, merged
-// by worker threads into batched launches (gbp_propagate_nodes), each worker with its own context and stream.
+// by node workers into batched launches (gbp_propagate_nodes), and instance requests (problems of their own),
+// merged by instance workers into block-diagonal launches (gbp_propagate_instances); each worker has its own
+// context and stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,12 +22,13 @@ struct Req {
   int kind = 0;  // 0 node, 1 instance
   std::vector<int32_t> cols;
   std::vector<double> lb, ub;
-  // an instance request: its rows (CSR over local columns) and integrality; lb/ub above are its bounds
-  int64_t m = 0;
-  std::vector<int64_t> rowptr;
-  std::vector<int32_t> colidx;
-  std::vector<double> vals, lhs, rhs;
-  std::vector<int8_t> isint;
+  // an instance request: its rows (CSR over local columns), integrality and bounds, borrowed from the caller
+  // until the reply has been polled
+  int64_t m = 0, n = 0;
+  const int64_t* rowptr = nullptr;
+  const int32_t* colidx = nullptr;
+  const double *vals = nullptr, *lhs = nullptr, *rhs = nullptr, *ilb = nullptr, *iub = nullptr;
+  const int8_t* isint = nullptr;
   int64_t t_submit = 0, t_done = 0;
   int done = 0;
   int rc = GBP_OK;
@@ -181,9 +184,10 @@ void runBatch(gbp_server* S, Worker& W, std::vector<Req*>& batch) {
 }
 
 // propagate a batch of instance requests on an instance worker: one upload of the instances as parts of a
-// block-diagonal problem, one batched root fixpoint, each request's bounds back
-void runInstances(Worker& W, std::vector<Req*>& batch) {
-  const size_t k = batch.size();
+// block-diagonal problem, one batched root fixpoint, each request's bounds back.  The upload checks every part
+// (row pointers on the host, column indices on the device) and refuses the whole batch for one bad part: the
+// batch then runs again one request at a time, so that only the bad request is answered GBP_ERR_INVALID.
+int runInstanceList(Worker& W, Req* const* batch, size_t k) {
   std::vector<int64_t> mk(k), nk(k);
   std::vector<const int64_t*> rp(k);
   std::vector<const int32_t*> ci(k);
@@ -193,25 +197,26 @@ void runInstances(Worker& W, std::vector<Req*>& batch) {
   for (size_t q = 0; q < k; ++q) {
     const Req* r = batch[q];
     mk[q] = r->m;
-    nk[q] = (int64_t)r->lb.size();
-    rp[q] = r->rowptr.data();
-    ci[q] = r->colidx.data();
-    va[q] = r->vals.data();
-    lh[q] = r->lhs.data();
-    rh[q] = r->rhs.data();
-    it[q] = r->isint.data();
-    lb.insert(lb.end(), r->lb.begin(), r->lb.end());
-    ub.insert(ub.end(), r->ub.begin(), r->ub.end());
+    nk[q] = r->n;
+    rp[q] = r->rowptr;
+    ci[q] = r->colidx;
+    va[q] = r->vals;
+    lh[q] = r->lhs;
+    rh[q] = r->rhs;
+    it[q] = r->isint;
+    lb.insert(lb.end(), r->ilb, r->ilb + r->n);
+    ub.insert(ub.end(), r->iub, r->iub + r->n);
   }
   std::vector<int8_t> cut(k, 0);
   gbp_result res;
   int rc = gbp_upload_instance_list(W.ctx, (int64_t)k, mk.data(), nk.data(), rp.data(), ci.data(), va.data(),
                                     lh.data(), rh.data(), it.data());
+  if (rc == GBP_ERR_INVALID) return rc;
   if (rc == GBP_OK) rc = gbp_propagate_instances(W.ctx, lb.data(), ub.data(), cut.data(), &res);
   int64_t at = 0;
   for (size_t q = 0; q < k; ++q) {
     Req* r = batch[q];
-    const int64_t n = nk[q];
+    const int64_t n = r->n;
     if (rc != GBP_OK && rc != GBP_ERR_LIMIT) {
       r->rc = rc;
     } else {
@@ -225,6 +230,13 @@ void runInstances(Worker& W, std::vector<Req*>& batch) {
     }
     at += n;
   }
+  return GBP_OK;
+}
+
+void runInstances(Worker& W, std::vector<Req*>& batch) {
+  if (runInstanceList(W, batch.data(), batch.size()) != GBP_ERR_INVALID) return;
+  for (Req* r : batch)
+    if (runInstanceList(W, &r, 1) == GBP_ERR_INVALID) r->rc = GBP_ERR_INVALID;
 }
 
 void workerLoop(gbp_server* S, Worker* W) {
@@ -237,13 +249,12 @@ void workerLoop(gbp_server* S, Worker* W) {
     int64_t bytes = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
+      // a stopping server still serves what is queued; every request fits the budget alone (submission refuses
+      // the rest), so the front fits once the other workers' batches have finished
       S->cv_work.wait(lk, [&] {
-        return S->stop || (!Q.empty() && S->inflight + S->reqs[Q.front()].bytes <= S->budget);
+        return (S->stop && Q.empty()) || (!Q.empty() && S->inflight + S->reqs[Q.front()].bytes <= S->budget);
       });
-      if (Q.empty()) {
-        if (S->stop) return;
-        continue;
-      }
+      if (Q.empty()) return;
       batch.clear();
       tickets.clear();
       while (!Q.empty() && (int64_t)batch.size() < maxb) {
@@ -368,13 +379,10 @@ int gbp_server_submit_instance(gbp_server* S, int64_t m, int64_t n, const int64_
                                const double* lb, const double* ub, int64_t* ticket) {
   if (!S || !ticket || m < 0 || n < 0 || !rowptr || (m > 0 && (!lhs || !rhs)) || (n > 0 && (!isint || !lb || !ub)))
     return GBP_ERR_INVALID;
-  if (rowptr[0] != 0) return GBP_ERR_INVALID;
-  for (int64_t i = 0; i < m; ++i)
-    if (rowptr[i + 1] < rowptr[i]) return GBP_ERR_INVALID;
+  // the rest of the checks (row pointers non-decreasing, column indices inside the instance) run on the worker,
+  // off the submitting thread, when the batch is uploaded
   const int64_t nnz = rowptr[m];
-  if (nnz > 0 && (!colidx || !vals)) return GBP_ERR_INVALID;
-  for (int64_t p = 0; p < nnz; ++p)
-    if (colidx[p] < 0 || colidx[p] >= n) return GBP_ERR_INVALID;
+  if (rowptr[0] != 0 || nnz < 0 || (nnz > 0 && (!colidx || !vals))) return GBP_ERR_INVALID;
   const int64_t bytes = 28 * nnz + 64 * m + 64 * n + 4096;
   {
     std::lock_guard<std::mutex> lk(S->mu);
@@ -387,14 +395,15 @@ int gbp_server_submit_instance(gbp_server* S, int64_t m, int64_t n, const int64_
     Req& r = S->reqs[t];
     r.kind = 1;
     r.m = m;
-    r.rowptr.assign(rowptr, rowptr + m + 1);
-    r.colidx.assign(colidx, colidx + nnz);
-    r.vals.assign(vals, vals + nnz);
-    r.lhs.assign(lhs, lhs + m);
-    r.rhs.assign(rhs, rhs + m);
-    r.isint.assign(isint, isint + n);
-    r.lb.assign(lb, lb + n);
-    r.ub.assign(ub, ub + n);
+    r.n = n;
+    r.rowptr = rowptr;
+    r.colidx = colidx;
+    r.vals = vals;
+    r.lhs = lhs;
+    r.rhs = rhs;
+    r.isint = isint;
+    r.ilb = lb;
+    r.iub = ub;
     r.bytes = bytes;
     r.t_submit = S->now();
     S->iqueue.push_back(t);

@@ -441,6 +441,7 @@ class Server:
             raise GbpError(rc, self.L.gbp_error_string(rc).decode())
         self.h = h
         self._out = (np.empty(self.n, np.int32), np.empty(self.n), np.empty(self.n))
+        self._borrowed = {}  # ticket -> the arrays of an instance request, alive until its reply is read
 
     def submit(self, cols, lb, ub) -> int:
         cols = np.ascontiguousarray(cols, dtype=np.int32)
@@ -453,15 +454,17 @@ class Server:
         return t.value
 
     def submit_instance(self, inst) -> int:
-        """An instance request (a problem of its own, answered with its root fixpoint); needs inst_workers > 0."""
-        arrs = [np.ascontiguousarray(a) for a in (inst.rowptr.astype(np.int64), inst.colidx.astype(np.int32),
-                                                  inst.vals.astype(np.float64), inst.lhs.astype(np.float64),
-                                                  inst.rhs.astype(np.float64), inst.isint.astype(np.int8),
-                                                  inst.lb.astype(np.float64), inst.ub.astype(np.float64))]
+        """An instance request (a problem of its own, answered with its root fixpoint); needs inst_workers > 0.
+        libgbp borrows the arrays: they are kept alive here until the reply has been read."""
+        arrs = [np.ascontiguousarray(a, dtype=d) for a, d in ((inst.rowptr, np.int64), (inst.colidx, np.int32),
+                                                             (inst.vals, np.float64), (inst.lhs, np.float64),
+                                                             (inst.rhs, np.float64), (inst.isint, np.int8),
+                                                             (inst.lb, np.float64), (inst.ub, np.float64))]
         t = ctypes.c_int64()
         rc = self.L.gbp_server_submit_instance(self.h, inst.m, inst.n, *[_ptr(a) for a in arrs], ctypes.byref(t))
         if rc != GBP_OK:
             raise GbpError(rc, self.L.gbp_error_string(rc).decode())
+        self._borrowed[t.value] = arrs
         return t.value
 
     def poll(self, ticket: int, wait_ms: int = -1, cap: Optional[int] = None):
@@ -476,8 +479,11 @@ class Server:
         td = ctypes.c_int64()
         rc = self.L.gbp_server_poll(self.h, ticket, wait_ms, ctypes.byref(cut), len(c), ctypes.byref(n), _ptr(c),
                                     _ptr(l), _ptr(u), ctypes.byref(ts), ctypes.byref(td))
+        if rc == GBP_ERR_OVERFLOW:  # the reply stays available: read it with room for every column it holds
+            return self.poll(ticket, 0, n.value)
         if rc == GBP_ERR_BUSY:
             return None
+        self._borrowed.pop(ticket, None)
         if rc not in (GBP_OK, GBP_ERR_LIMIT):
             raise GbpError(rc, self.L.gbp_error_string(rc).decode())
         k = n.value
@@ -490,6 +496,7 @@ class Server:
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.gbp_server_destroy(self.h)
+            self.L.gbp_server_destroy(self.h)  # joins the workers: nothing borrowed is read after this
             self.h = None
+            self._borrowed.clear()
 

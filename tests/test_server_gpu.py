@@ -84,19 +84,25 @@ def test_admission_and_bad_requests(oracle_mod):
 def test_instance_requests_beside_node_requests(oracle_mod):
     """Instance requests (problems of their own) go to instance workers, which upload what is queued as one
     block-diagonal problem and propagate it in one launch; every reply equals the oracle's root fixpoint of that
-    instance bit for bit, while node requests are served beside them."""
+    instance bit for bit, while node requests are served beside them.  A request whose column index lies outside
+    its instance is answered GBP_ERR_INVALID and the rest of its batch is still served."""
+    from scip_gb300.instances import Instance
     inst, rlb, rub, nodes, want = _setup(oracle_mod, m=5000, nnodes=64)
     pool = instances.uneven_batch(seed=41, count=24)
     pool = [p for p in pool if p.m <= 20000][:12]
+    bad = Instance(np.array([0, 2], np.int64), np.array([0, 5], np.int32), np.array([1.0, 1.0]), np.array([1.0]),
+                   np.array([1e20]), np.zeros(2), np.full(2, 2.0), np.ones(2, np.int8), x0=np.zeros(2))
     srv = gbp.Server(inst, rlb, rub, params=gbp.default_params(maxeasy=0.0), workers=1, inst_workers=2)
     try:
-        tk_i = [srv.submit_instance(p) for p in pool]
+        tk_i = [srv.submit_instance(p) for p in pool[:6]]
+        tk_bad = srv.submit_instance(bad)
+        tk_i += [srv.submit_instance(p) for p in pool[6:]]
         tk_n = []
         for k in range(nodes.nnodes):
             sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
             tk_n.append(srv.submit(nodes.col[sl], nodes.lb[sl], nodes.ub[sl]))
         for p, t in zip(pool, tk_i):
-            cut, c, l, u, _, _ = srv.poll(t, cap=max(p.n, inst.n))
+            cut, c, l, u, _, _ = srv.poll(t)
             olb, oub, ores = oracle_mod.Oracle(p).propagate(p.lb, p.ub, oracle_mod.params(0.0))
             assert cut == bool(ores.cutoff)
             if not cut:
@@ -104,6 +110,9 @@ def test_instance_requests_beside_node_requests(oracle_mod):
         for k, t in enumerate(tk_n):
             cut, c, _, _, _, _ = srv.poll(t)
             assert cut == bool(want["cutoff"][k])
+        with pytest.raises(gbp.GbpError) as e:
+            srv.poll(tk_bad)
+        assert e.value.code == gbp.GBP_ERR_INVALID
     finally:
         srv.close()
 
