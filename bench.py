@@ -419,12 +419,13 @@ def time_served(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), durat
     return out
 
 
-def time_served_mix(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), duration=0.2, node_frac=0.8):
+def time_served_mix(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), duration=0.2, node_frac=0.8,
+                    inst_workers=4):
     """The served mix through libgbp's C serving loop: open-loop Poisson arrivals, node_frac of them single-node
     requests (the bench's nodes in turn) and the rest new instances drawn from 24 instances of the uneven-instance
     generator (rows log-uniform in [1e3, 2e5]), at each offered rate for `duration` seconds.  Two node workers merge
-    node requests into batched k_nodes launches; two instance workers upload queued instances as one block-diagonal
-    problem each and propagate it in one launch.  Instance arrays are borrowed by the server (no host copy), so each
+    node requests into batched k_nodes launches; inst_workers instance workers upload queued instances as one
+    block-diagonal problem each and propagate it in one launch.  Instance arrays are borrowed by the server (no host copy), so each
     instance request costs its upload: host-to-device bytes bound the instance side.  Latency = the server's time
     from admitting a request to finishing its batch, per kind and overall."""
     import ctypes
@@ -449,7 +450,7 @@ def time_served_mix(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), d
     cap = max(max(p.n for p in pool), inst.n)
     oc, ol, ou = np.empty(cap, np.int32), np.empty(cap), np.empty(cap)
     ocp, olp, oup = (a.ctypes.data_as(ctypes.c_void_p) for a in (oc, ol, ou))
-    srv = gbp.Server(inst, rlb, rub, params=params, workers=2, inst_workers=2, max_batch=4096)
+    srv = gbp.Server(inst, rlb, rub, params=params, workers=2, inst_workers=inst_workers, max_batch=4096)
     L = srv.L
     out = {}
     t = ctypes.c_int64()
@@ -506,8 +507,8 @@ def time_served_mix(inst, rlb, rub, nodes, params, rates=(1000, 10000, 50000), d
                                  "served_req_s": int(sel.sum()) / ((tda[sel].max() - tsa[sel].min()) / 1e9)}
             out[str(rate)] = row
         out["stats"] = srv.stats()
-        out["call"] = ("gbp_server_submit / gbp_server_submit_instance / gbp_server_poll (2 node + 2 instance "
-                       "worker threads)")
+        out["call"] = ("gbp_server_submit / gbp_server_submit_instance / gbp_server_poll (2 node + "
+                       f"{inst_workers} instance worker threads)")
         out["mix"] = f"{node_frac:.0%} node requests, the rest instances of the uneven-instance generator " \
                      f"({sum(p.m for p in pool) // len(pool):,} rows and {sum(p.nnz for p in pool) // len(pool):,} " \
                      "nonzeros on average)"
