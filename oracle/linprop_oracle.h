@@ -15,6 +15,7 @@
 #ifndef LINPROP_ORACLE_H
 #define LINPROP_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -154,6 +155,30 @@ int lpo_propagate_nodes_seq(const lpo_problem* prob, const lpo_params* par, cons
    const double* baseub, int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb,
    const double* chg_ub, int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb,
    double* out_ub, int32_t cap, int32_t nthreads, lpo_result* total);
+
+/* Carrying the root's activities into the nodes, as SCIP does.  lpo_propagate_nodes_seq starts each row of a node
+ * with activities computed afresh on first use; SCIP's node rows keep the activities the root's incremental updates
+ * left (consdataUpdateActivities, cons_linear.c:1604-1992, run by the root's bound-change events, with validity
+ * flags and reliability references that survive into the probing node).  The two differ only in the last bits of
+ * those activities, which a row with coefficients of very different magnitudes can amplify past the continuous
+ * tolerance.  lpo_propagate_seq_states is lpo_propagate_seq that also copies the final row states into out_states
+ * (lpo_seq_state_bytes(m) bytes; an opaque record per row); lpo_propagate_nodes_seq_from is lpo_propagate_nodes_seq
+ * whose rows start from those states (root_states NULL: afresh), and whose rows deleted at the root are the rows
+ * the root restatement deleted (lpo_seq_states_deleted) instead of the rows redundant under the base bounds
+ * (lpo_root_deleted_rows, which differs from SCIP's deletions both ways on some instances: SCIP deletes a redundant
+ * row only when it propagates the row again after its last column change, and a change that only lowers a
+ * one-sided row's slack does not mark it; and SCIP's redundancy test reads incrementally updated activities, which
+ * can pass by a last-bit margin where activities computed afresh do not).  The rows of
+ * prob may be stored in another order than the root's problem (the order SCIP holds them in after the root); row
+ * indices must be the same. */
+size_t lpo_seq_state_bytes(int64_t m);
+void lpo_seq_states_deleted(const void* states, int64_t m, uint8_t* del);
+int lpo_propagate_seq_states(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int32_t* out_order, lpo_result* res, void* out_states);
+int lpo_propagate_nodes_seq_from(const lpo_problem* prob, const lpo_params* par, const double* baselb,
+   const double* baseub, int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb,
+   const double* chg_ub, int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int32_t cap, int32_t nthreads, lpo_result* total, const void* root_states);
 
 #ifdef __cplusplus
 }

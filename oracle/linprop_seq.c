@@ -85,6 +85,7 @@ typedef struct
    int32_t* dirtylist;
    int64_t ndirty;
    const uint8_t* rowdel; /* nodes: rows deleted at the root (redundant under the base bounds) */
+   const RowSt* rootst;   /* nodes: the root's final row states, whose activities a node starts from (or NULL) */
    lpo_result* res;
 } Seq;
 
@@ -112,6 +113,21 @@ static RowSt* rowSt(Seq* q, int32_t i)
       {
          r->del = 1;
          r->en = 0;
+      }
+      if( q->rootst != NULL )
+      {
+         /* SCIP keeps a row's activities across the root and into a node: the node starts from the values the
+          * root's incremental updates left (with their reliability references and the largest activity delta)
+          * instead of recomputing them on first use */
+         const RowSt* o = &q->rootst[i];
+         r->a = o->a;
+         r->lastmin = o->lastmin;
+         r->lastmax = o->lastmax;
+         r->maxdelta = o->maxdelta;
+         r->maxdeltacol = o->maxdeltacol;
+         r->valid = o->valid;
+         r->validmin = o->validmin;
+         r->validmax = o->validmax;
       }
       if( !q->root && q->sortvars )
       {
@@ -1157,6 +1173,25 @@ static void seqFree(Seq* q)
 int lpo_propagate_seq(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub, int32_t* out_order,
    lpo_result* res)
 {
+   return lpo_propagate_seq_states(prob, par, lb, ub, out_order, res, NULL);
+}
+
+size_t lpo_seq_state_bytes(int64_t m)
+{
+   return sizeof(RowSt) * (size_t)(m + 1);
+}
+
+void lpo_seq_states_deleted(const void* states, int64_t m, uint8_t* del)
+{
+   const RowSt* rs = states;
+   int64_t i;
+   for( i = 0; i < m; ++i )
+      del[i] = rs[i].del;
+}
+
+int lpo_propagate_seq_states(const lpo_problem* prob, const lpo_params* par, double* lb, double* ub,
+   int32_t* out_order, lpo_result* res, void* out_states)
+{
    Seq q;
    int64_t i;
    int st;
@@ -1179,6 +1214,8 @@ int lpo_propagate_seq(const lpo_problem* prob, const lpo_params* par, double* lb
    res->cutoff = st == 1;
    if( out_order != NULL )
       memcpy(out_order, q.ord, sizeof(int32_t) * (size_t)prob->rowptr[prob->m]);
+   if( out_states != NULL )
+      memcpy(out_states, q.rs, lpo_seq_state_bytes(prob->m));
    seqFree(&q);
    return 0;
 }
@@ -1189,6 +1226,7 @@ typedef struct
    const lpo_problem* P;
    const lpo_params* par;
    const uint8_t* rowdel;
+   const RowSt* rootst;
    const double* baselb;
    const double* baseub;
    const int64_t* ptr;
@@ -1228,6 +1266,7 @@ static void* seqNodeWorker(void* arg)
    }
    s = &q.s;
    q.rowdel = J->rowdel;
+   q.rootst = J->rootst;
    memcpy(lb, J->baselb, sizeof(double) * (size_t)P->n);
    memcpy(ub, J->baseub, sizeof(double) * (size_t)P->n);
    q.lb = lb;
@@ -1379,6 +1418,15 @@ int lpo_propagate_nodes_seq(const lpo_problem* prob, const lpo_params* par, cons
    const double* chg_ub, int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb,
    double* out_ub, int32_t cap, int32_t nthreads, lpo_result* total)
 {
+   return lpo_propagate_nodes_seq_from(prob, par, baselb, baseub, nnodes, ptr, chg_col, chg_lb, chg_ub, out_cutoff,
+      out_rounds, out_n, out_col, out_lb, out_ub, cap, nthreads, total, NULL);
+}
+
+int lpo_propagate_nodes_seq_from(const lpo_problem* prob, const lpo_params* par, const double* baselb,
+   const double* baseub, int64_t nnodes, const int64_t* ptr, const int32_t* chg_col, const double* chg_lb,
+   const double* chg_ub, int8_t* out_cutoff, int32_t* out_rounds, int32_t* out_n, int32_t* out_col, double* out_lb,
+   double* out_ub, int32_t cap, int32_t nthreads, lpo_result* total, const void* root_states)
+{
    SeqJob* jobs;
    pthread_t* th;
    uint8_t* rowdel;
@@ -1398,11 +1446,14 @@ int lpo_propagate_nodes_seq(const lpo_problem* prob, const lpo_params* par, cons
       free(rowdel);
       return -1;
    }
-   lpo_root_deleted_rows(prob, par, baselb, baseub, rowdel);
+   if( root_states != NULL )
+      lpo_seq_states_deleted(root_states, prob->m, rowdel);  /* the rows the root itself deleted */
+   else
+      lpo_root_deleted_rows(prob, par, baselb, baseub, rowdel);
    for( t = 0; t < nthreads; ++t )
    {
       SeqJob* J = &jobs[t];
-      J->P = prob; J->par = par; J->rowdel = rowdel; J->baselb = baselb; J->baseub = baseub; J->ptr = ptr; J->chg_col = chg_col;
+      J->P = prob; J->par = par; J->rowdel = rowdel; J->rootst = (const RowSt*)root_states; J->baselb = baselb; J->baseub = baseub; J->ptr = ptr; J->chg_col = chg_col;
       J->chg_lb = chg_lb; J->chg_ub = chg_ub; J->out_cutoff = out_cutoff; J->out_rounds = out_rounds;
       J->out_n = out_n; J->out_col = out_col; J->out_lb = out_lb; J->out_ub = out_ub; J->cap = cap;
       J->k0 = nnodes * t / nthreads;

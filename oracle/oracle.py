@@ -81,6 +81,11 @@ def lib():
         L.lpo_propagate_seq.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P,
                                         ctypes.POINTER(Result)]
         L.lpo_propagate_nodes_seq.argtypes = L.lpo_propagate_nodes.argtypes
+        L.lpo_seq_state_bytes.argtypes = [ctypes.c_int64]
+        L.lpo_seq_state_bytes.restype = ctypes.c_size_t
+        L.lpo_propagate_seq_states.argtypes = L.lpo_propagate_seq.argtypes + [_P]
+        L.lpo_propagate_nodes_seq_from.argtypes = L.lpo_propagate_nodes.argtypes + [_P]
+        L.lpo_seq_states_deleted.argtypes = [_P, ctypes.c_int64, _P]
         L.lpo_root_deleted_rows.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Params), _P, _P, _P]
         _lib = L
     return _lib
@@ -187,18 +192,28 @@ class Oracle:
         self.last_ranged = (rrnd[:r][q], rcol[:r][q], rrow[:r][q])
         return lb, ub, res, (col[:n][o], rnd[:n][o], llb[:n][o], lub[:n][o])
 
-    def propagate_seq(self, lb, ub, par=None):
+    def propagate_seq(self, lb, ub, par=None, states=False):
         """Root fixpoint in SCIP's own order (lpo_propagate_seq); returns (lb, ub, Result, order) where order[p]
-        for p in row i's CSR range is the CSR position of the row's entries in the order SCIP holds them at the end."""
+        for p in row i's CSR range is the CSR position of the row's entries in the order SCIP holds them at the end.
+        states: also return the root's final row states (opaque bytes for propagate_nodes(root_states=...))."""
         par = par or params()
         lb = np.array(lb, dtype=np.float64)
         ub = np.array(ub, dtype=np.float64)
         order = np.zeros(max(1, self.inst.nnz), dtype=np.int32)
         res = Result()
-        if lib().lpo_propagate_seq(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), _ptr(order),
-                                   ctypes.byref(res)) != 0:
+        st = np.zeros(lib().lpo_seq_state_bytes(self.inst.m), dtype=np.uint8) if states else None
+        if lib().lpo_propagate_seq_states(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub),
+                                          _ptr(order), ctypes.byref(res), _ptr(st)) != 0:
             raise MemoryError("oracle allocation failed")
+        if states:
+            return lb, ub, res, order[:self.inst.nnz], st
         return lb, ub, res, order[:self.inst.nnz]
+
+    def states_deleted_rows(self, states):
+        """The rows the root restatement deleted, from the row states of propagate_seq(..., states=True)."""
+        out = np.zeros(self.inst.m, dtype=np.uint8)
+        lib().lpo_seq_states_deleted(_ptr(states), self.inst.m, _ptr(out))
+        return out.astype(bool)
 
     def root_deleted_rows(self, lb, ub, par=None):
         """Rows redundant under lb/ub: the rows SCIP's root deletes (lpo_root_deleted_rows)."""
@@ -209,10 +224,11 @@ class Oracle:
         lib().lpo_root_deleted_rows(ctypes.byref(self.prob), ctypes.byref(par), _ptr(lb), _ptr(ub), _ptr(out))
         return out.astype(bool)
 
-    def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1, seq=False):
+    def propagate_nodes(self, baselb, baseub, nodes, par=None, cap=4096, nthreads=1, seq=False, root_states=None):
         """Node batch; returns dict with cutoff [N], rounds [N], n [N], col/lb/ub [N, cap] and totals.
         seq: SCIP's own order (lpo_propagate_nodes_seq; each row's entries in storage order are taken as the order
-        SCIP holds the row in) instead of rounds."""
+        SCIP holds the row in) instead of rounds.  root_states (seq only): the row states of propagate_seq(...,
+        states=True) on the same rows, which each node's rows start from as SCIP's do (default: afresh)."""
         par = par or params()
         N = nodes.nnodes
         baselb = np.ascontiguousarray(baselb, dtype=np.float64)
@@ -225,10 +241,15 @@ class Oracle:
                    n=np.zeros(N, dtype=np.int32), col=np.zeros((N, cap), dtype=np.int32),
                    lb=np.zeros((N, cap)), ub=np.zeros((N, cap)))
         tot = Result()
-        fn = lib().lpo_propagate_nodes_seq if seq else lib().lpo_propagate_nodes
-        rc = fn(ctypes.byref(self.prob), ctypes.byref(par), _ptr(baselb), _ptr(baseub), N,
+        args = (ctypes.byref(self.prob), ctypes.byref(par), _ptr(baselb), _ptr(baseub), N,
                 _ptr(ptr), _ptr(col), _ptr(nlb), _ptr(nub), _ptr(out["cutoff"]), _ptr(out["rounds"]), _ptr(out["n"]),
                 _ptr(out["col"]), _ptr(out["lb"]), _ptr(out["ub"]), cap, nthreads, ctypes.byref(tot))
+        if root_states is not None:
+            if not seq or len(root_states) != lib().lpo_seq_state_bytes(self.inst.m):
+                raise ValueError("root_states: the row states of propagate_seq on the same rows, seq mode only")
+            rc = lib().lpo_propagate_nodes_seq_from(*args, _ptr(root_states))
+        else:
+            rc = (lib().lpo_propagate_nodes_seq if seq else lib().lpo_propagate_nodes)(*args)
         if rc != 0:
             raise MemoryError("oracle node batch failed")
         out["total"] = tot

@@ -472,6 +472,81 @@ def uneven_batch(seed: int = 4, count: int = 512, rmin: int = 1000, rmax: int = 
     return out
 
 
+def mixed_small(rng: np.random.Generator) -> Instance:
+    """A small random MIP (2..24 columns, up to twice as many rows of 1..8 entries) that mixes what makes
+    activity arithmetic delicate: coefficients from small integers over normal reals to magnitudes 1e3..1e7 and
+    1e-5..1e-1 in one row, infinite and huge bounds, free and half-bounded columns, equations and ranged rows.
+    Sides come from a point inside the bounds, so most instances are feasible; one in ten gets one row whose sides
+    cross (an infeasible instance)."""
+    n = int(rng.integers(2, 25))
+    m = int(rng.integers(1, 2 * n))
+    style = int(rng.integers(0, 4))  # 0: small integers only; 1..3: mixed magnitudes
+    rowptr, cols, vals = [0], [], []
+    for _ in range(m):
+        k = int(rng.integers(1, min(n, 8) + 1))
+        for c in np.sort(rng.choice(n, k, replace=False)):
+            t = rng.random()
+            if style == 0 or t < 0.5:
+                v = float(rng.integers(-9, 10)) or 1.0
+            elif t < 0.7:
+                v = float(rng.normal() * 10)
+            elif t < 0.85:
+                v = float(rng.choice([-1, 1]) * 10 ** rng.uniform(3, 7))
+            else:
+                v = float(rng.choice([-1, 1]) * 10 ** rng.uniform(-5, -1))
+            cols.append(int(c))
+            vals.append(v)
+        rowptr.append(len(cols))
+    isint = (rng.random(n) < (0.9, 0.5, 0.2, 0.7)[style]).astype(np.int8)
+    lb, ub = np.empty(n), np.empty(n)
+    for j in range(n):
+        t = rng.random()
+        if isint[j]:
+            if t < 0.5:
+                lb[j], ub[j] = 0.0, 1.0
+            elif t < 0.8:
+                lb[j] = float(rng.integers(-10, 5))
+                ub[j] = lb[j] + float(rng.integers(0, 30))
+            elif t < 0.9:
+                lb[j], ub[j] = 0.0, INF
+            else:
+                lb[j], ub[j] = -INF, float(rng.integers(-5, 50))
+        else:
+            if t < 0.4:
+                lb[j] = float(rng.uniform(-10, 0))
+                ub[j] = lb[j] + float(rng.uniform(0, 40))
+            elif t < 0.6:
+                lb[j], ub[j] = 0.0, INF
+            elif t < 0.7:
+                lb[j], ub[j] = -INF, INF
+            elif t < 0.8:
+                lb[j], ub[j] = -INF, float(rng.uniform(-5, 50))
+            else:
+                lb[j], ub[j] = 0.0, float(10 ** rng.uniform(-3, 6))
+    x = np.clip(rng.uniform(-5, 20, n), np.where(lb > -INF, lb, -50), np.where(ub < INF, ub, 50))
+    x = np.where(isint == 1, np.clip(np.round(x), lb, ub), x)
+    lhs, rhs = np.empty(m), np.empty(m)
+    for i in range(m):
+        a = np.array(vals[rowptr[i]:rowptr[i + 1]])
+        act = float(a @ x[np.array(cols[rowptr[i]:rowptr[i + 1]])])
+        t = rng.random()
+        slack = abs(rng.normal()) * (0.0, 1.0, 5.0)[int(rng.integers(0, 3))]
+        if t < 0.4:
+            lhs[i], rhs[i] = -INF, act + slack
+        elif t < 0.7:
+            lhs[i], rhs[i] = act - slack, INF
+        elif t < 0.75:
+            lhs[i] = rhs[i] = act
+        else:
+            lhs[i], rhs[i] = act - slack, act + slack + 1.0
+    if rng.random() < 0.1:
+        i = int(rng.integers(0, m))
+        if lhs[i] > -INF:
+            rhs[i] = lhs[i] - 1e-3
+    return Instance(np.array(rowptr, np.int64), np.array(cols, np.int32), np.array(vals), lhs, rhs, lb, ub, isint,
+                    name="mixed_small")
+
+
 def concat_instances(insts: List[Instance]):
     """Block-diagonal union of independent instances: (instance, row_off, col_off) with instance k owning rows
     row_off[k]:row_off[k+1] and columns col_off[k]:col_off[k+1]."""

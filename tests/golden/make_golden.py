@@ -26,6 +26,8 @@ propagated before it.  Cases:
   ranged/gcd_rows_shared     2,000 rows over 8,000 columns, half of them equations, the same settings
   ranged/tiny_cutoffs        60 instances of 12 rows whose equations were shifted off their feasible residue, so
                              that the ranged rule finds many of them infeasible (concatenated, with offsets)
+  fuzz/mixed_small           300 small random MIPs with coefficient magnitudes 1e-5..1e7 in one row, infinite
+                             bounds and equations (concatenated, with offsets), SCIP's root and up to 8 nodes each
 
 Usage: python tests/golden/make_golden.py [case ...]   (needs the SCIP sources; writes tests/golden/*.npz;
 no argument builds every case)
@@ -155,6 +157,69 @@ def save_tiny_cutoffs():
     print(f"{path}: {len(insts)} instances, {int(out['sort_cut'].sum())} infeasible (sortvars)")
 
 
+MIXED_SEEDS = range(5000, 5300)
+
+
+def save_mixed_small():
+    """300 small random MIPs of instances.mixed_small (seeds 5000..5299; coefficient magnitudes 1e-5..1e7 in one
+    row, infinite bounds, equations), concatenated with offsets, with SCIP's root (bounds, row orders, deleted
+    rows) for both rules and up to 8 nodes per feasible instance (1..4 fixings, from SCIP's residual-rule root,
+    every node from a newly transformed problem), under tests/golden/fuzz."""
+    insts = [instances.mixed_small(np.random.default_rng(np.random.PCG64(s))) for s in MIXED_SEEDS]
+    big, row_off, col_off = instances.concat_instances(insts)
+    out = {"rowptr": big.rowptr, "colidx": big.colidx, "vals": big.vals, "lhs": big.lhs, "rhs": big.rhs,
+           "lb": big.lb, "ub": big.ub, "isint": big.isint, "row_off": row_off, "col_off": col_off,
+           "seeds": np.array(list(MIXED_SEEDS), np.int64)}
+    K = len(insts)
+    nodes = []
+    for k, inst in enumerate(insts):
+        for easy in (False, True):
+            tag = "easy" if easy else "res"
+            rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy)
+            if rcut:
+                order, rowdel = np.arange(inst.nnz, dtype=np.int32), np.zeros(inst.m, bool)
+            else:
+                _, _, _, _, order, rowdel = oracle.run_scip(inst, easy=easy, order=True)
+            out.setdefault(f"{tag}_rootcut", np.zeros(K, np.int8))[k] = rcut
+            out.setdefault(f"{tag}_rootlb", np.empty(big.n))[col_off[k]:col_off[k + 1]] = rlb
+            out.setdefault(f"{tag}_rootub", np.empty(big.n))[col_off[k]:col_off[k + 1]] = rub
+            out.setdefault(f"{tag}_order", np.empty(big.nnz, np.int32))[big.rowptr[row_off[k]]:
+                                                                         big.rowptr[row_off[k + 1]]] = order
+            out.setdefault(f"{tag}_rowdel", np.zeros(big.m, np.int8))[row_off[k]:row_off[k + 1]] = rowdel
+        nb = None
+        if not out["res_rootcut"][k]:
+            rlb = out["res_rootlb"][col_off[k]:col_off[k + 1]]
+            rub = out["res_rootub"][col_off[k]:col_off[k + 1]]
+            try:
+                nb = instances.node_batch(inst, rlb, rub, 8, seed=int(MIXED_SEEDS[k]), kmax=4)
+            except ValueError:  # no unfixed integer column with finite bounds
+                nb = None
+        res = {}
+        if nb is not None:
+            for easy in (False, True):
+                _, _, _, res["easy" if easy else "res"] = oracle.run_scip(inst, nb, easy=easy, fresh=True)
+        nodes.append((nb, res))
+    # nodes: node_inst[q] = the instance of node q; node columns and SCIP's changed columns are instance-local
+    cnt = [0 if nb is None else nb.nnodes for nb, _ in nodes]
+    out["node_inst"] = np.repeat(np.arange(K), cnt).astype(np.int32)
+    parts = [nb for nb, _ in nodes if nb is not None]
+    counts = np.concatenate([np.diff(nb.ptr) for nb in parts]) if parts else np.zeros(0, np.int64)
+    out["node_ptr"] = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    out["node_col"] = np.concatenate([nb.col for nb in parts]).astype(np.int32)
+    out["node_lb"] = np.concatenate([nb.lb for nb in parts])
+    out["node_ub"] = np.concatenate([nb.ub for nb in parts])
+    for tag in ("res", "easy"):
+        allres = [r for nb, rr in nodes if nb is not None for r in rr[tag]]
+        cut, ptr, col, lb, ub = node_arrays(allres)
+        out[f"{tag}_ncut"], out[f"{tag}_nptr"], out[f"{tag}_ncol"] = cut, ptr, col
+        out[f"{tag}_nlb"], out[f"{tag}_nub"] = lb, ub
+    os.makedirs(os.path.join(HERE, "fuzz"), exist_ok=True)
+    path = os.path.join(HERE, "fuzz", "mixed_small.npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {K} instances, {int(out['res_rootcut'].sum())} infeasible roots, {len(out['node_inst'])} nodes, "
+          f"{os.path.getsize(path) // 1024} KiB")
+
+
 def digest(*arrays):
     import hashlib
     h = hashlib.sha256()
@@ -258,7 +323,8 @@ def main(names):
     ranged = ranged_cases()
     for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs",
                                                                              "node_workload_scip",
-                                                                             "node_workload_base", "miplib"]:
+                                                                             "node_workload_base", "miplib",
+                                                                             "fuzz/mixed_small"]:
         if name == "node_workload_scip":
             save_node_workload()
             continue
@@ -267,6 +333,9 @@ def main(names):
             continue
         if name == "miplib":
             save_miplib_cases()
+            continue
+        if name == "fuzz/mixed_small":
+            save_mixed_small()
             continue
         if name == "ranged/tiny_cutoffs":
             save_tiny_cutoffs()

@@ -31,11 +31,12 @@ def _digest(*arrays):
     return h.hexdigest()
 
 
-def load_node_workload(oracle_mod):
+def load_node_workload(oracle_mod, with_states=False):
     """The batched-node benchmark workload (200,000 x 400,000, 4,096 nodes) with SCIP's results
     (golden/workload/node_workload_scip.npz).  The instance is regenerated from its seed and checked against the
     fixture's digest; SCIP's root bounds and row orders come from the oracle's restatement of SCIP's order, checked
-    against the digests of SCIP's own.  Returns (inst, rows in SCIP's order, root lb, root ub, nodes, fixture)."""
+    against the digests of SCIP's own.  Returns (inst, rows in SCIP's order, root lb, root ub, nodes, fixture), and
+    with_states the root's final row states after them."""
     from scip_gb300 import instances
 
     with np.load(os.path.join(GOLDEN, "workload", "node_workload_scip.npz")) as f:
@@ -44,7 +45,8 @@ def load_node_workload(oracle_mod):
     assert _digest(inst.rowptr, inst.colidx, inst.vals, inst.lhs, inst.rhs, inst.lb, inst.ub,
                    inst.isint) == str(z["instance_sha256"]), "the regenerated instance differs from the fixture's"
     vidx = instances.scip_var_index(inst.isint, inst.lb, inst.ub)
-    lb, ub, r, order = oracle_mod.Oracle(inst, vidx).propagate_seq(inst.lb, inst.ub, oracle_mod.params(0.0))
+    lb, ub, r, order, *states = oracle_mod.Oracle(inst, vidx).propagate_seq(inst.lb, inst.ub, oracle_mod.params(0.0),
+                                                                           states=with_states)
     assert not r.cutoff and _digest(lb, ub) == str(z["root_sha256"]), "root bounds differ from SCIP's"
     deleted = np.zeros(inst.m, dtype=bool)
     deleted[z["rowdel"]] = True
@@ -52,7 +54,7 @@ def load_node_workload(oracle_mod):
     assert _digest(order[live]) == str(z["order_sha256"]), "row orders differ from SCIP's"
     nodes = instances.node_batch(inst, lb, ub, 4096, seed=3)
     assert _digest(nodes.ptr, nodes.col, nodes.lb, nodes.ub) == str(z["nodes_sha256"])
-    return inst, instances.in_order(inst, order), lb, ub, nodes, z
+    return (inst, instances.in_order(inst, order), lb, ub, nodes, z) + tuple(states)
 
 
 def load(name):
@@ -131,3 +133,43 @@ class Agreement:
         out = c & ((np.abs(a[0] - b[0]) > tol_l) | (np.abs(a[1] - b[1]) > tol_u))
         self.cont_cols += int(c.sum())
         self.cont_cols_out_of_tol += int(out.sum())
+
+
+def load_mixed_small():
+    """golden/fuzz/mixed_small.npz split into its 300 instances: per instance a dict with the instance, its seed,
+    per rule ("res", "easy") SCIP's root (cut, lb, ub, order, rowdel) and its nodes' results (a list of
+    (cutoff, cols, lb, ub) with instance-local columns that differ from that rule's root), and the nodes
+    (instance-local NodeBatch, or None)."""
+    with np.load(os.path.join(GOLDEN, "fuzz", "mixed_small.npz")) as f:
+        z = dict(f)
+    ro, co = z["row_off"], z["col_off"]
+    K = len(ro) - 1
+    ninst = z["node_inst"]
+    first = np.searchsorted(ninst, np.arange(K + 1))
+    out = []
+    for k in range(K):
+        r0, r1, c0, c1 = int(ro[k]), int(ro[k + 1]), int(co[k]), int(co[k + 1])
+        p0, p1 = int(z["rowptr"][r0]), int(z["rowptr"][r1])
+        inst = Instance(z["rowptr"][r0:r1 + 1] - p0, z["colidx"][p0:p1] - c0, z["vals"][p0:p1], z["lhs"][r0:r1],
+                        z["rhs"][r0:r1], z["lb"][c0:c1], z["ub"][c0:c1], z["isint"][c0:c1],
+                        name=f"mixed_small/{int(z['seeds'][k])}")
+        q0, q1 = int(first[k]), int(first[k + 1])
+        nb = None
+        if q1 > q0:
+            ptr = z["node_ptr"][q0:q1 + 1]
+            sl = slice(int(ptr[0]), int(ptr[-1]))
+            nb = NodeBatch(ptr - ptr[0], z["node_col"][sl], z["node_lb"][sl], z["node_ub"][sl])
+        d = {"inst": inst, "seed": int(z["seeds"][k]), "nodes": nb}
+        for tag in ("res", "easy"):
+            root = {"cut": bool(z[f"{tag}_rootcut"][k]), "lb": z[f"{tag}_rootlb"][c0:c1],
+                    "ub": z[f"{tag}_rootub"][c0:c1], "order": z[f"{tag}_order"][p0:p1],
+                    "rowdel": z[f"{tag}_rowdel"][r0:r1].astype(bool)}
+            res = []
+            for q in range(q0, q1):
+                a, b = int(z[f"{tag}_nptr"][q]), int(z[f"{tag}_nptr"][q + 1])
+                res.append((bool(z[f"{tag}_ncut"][q]), z[f"{tag}_ncol"][a:b], z[f"{tag}_nlb"][a:b],
+                            z[f"{tag}_nub"][a:b]))
+            d[tag] = {"root": root, "nodes": res}
+        out.append(d)
+    return out
+
