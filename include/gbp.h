@@ -80,7 +80,10 @@ typedef struct
  * a valid fixpoint of the same rules.  Each row's entries are visited in storage order, which must be the order
  * SCIP holds the row in (SCIPgetVarsLinear during solving; consdataCompVarProp, cons_linear.c:3191-3254, on the
  * base bounds for rows SCIP has not re-sorted); with sortvars a row's leading binaries under the base bounds are its
- * nbinvars.  The base bounds must be a propagated fixpoint (SCIP's root): rows redundant under them are the rows
+ * nbinvars.  Rows are marked in ascending row index for each changed column, so the rows must be uploaded in the
+ * order a variable's bound-change events reach SCIP's constraints: the order SCIP created them (its handler array
+ * loses that order once constraints are deleted).  The base bounds must be a propagated fixpoint (SCIP's root):
+ * rows redundant under them are the rows
  * SCIP's root deleted and take no part, and every row counts as already tightened there until a change that one of
  * its finite sides can use.  Does not combine with GBP_FLAG_RANGEDROW. */
 #define GBP_FLAG_SCIPORDER 8

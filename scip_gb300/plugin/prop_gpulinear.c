@@ -36,6 +36,8 @@ struct SCIP_PropData
    SCIP_Bool             specialised;        /**< also the rows of setppc, logicor, knapsack, varbound constraints */
    SCIP_Bool             replacespecialised; /**< switch those handlers' propagation off at include time */
    SCIP_Bool             inprobing;          /**< also propagate in probing nodes */
+   SCIP_Bool             sciporder;          /**< batched nodes in SCIP's own order (GBP_FLAG_SCIPORDER) */
+   int                   nspecialrows;       /**< rows of the matrix from handlers other than linear */
    int                   nrows;              /**< rows in the matrix */
    int                   ncols;              /**< columns = transformed variables */
    SCIP_VAR**            vars;               /**< column -> variable */
@@ -236,6 +238,37 @@ static SCIP_RETCODE consRow(SCIP* scip, int h, SCIP_CONS* cons, SCIP_VAR** vars,
    return SCIP_OKAY;
 }
 
+/** the constraints of a handler in the order SCIP created them, which is the order a variable's bound-change events
+ *  reach them (each constraint catches its variables' events when it is transformed): the transformed constraints
+ *  of the original ones in the original order, then the others in the handler's order.  The handler's array loses
+ *  that order once constraints are deleted (the last entry moves into the hole, conshdlrDelCons in cons.c). */
+static SCIP_RETCODE creationOrder(SCIP* scip, SCIP_CONS** conss, int nc, SCIP_CONS** out)
+{
+   SCIP_CONS** orig = SCIPgetOrigConss(scip);
+   int norig = SCIPgetNOrigConss(scip);
+   SCIP_HASHMAP* rank;
+   int* key;
+   int k;
+   SCIP_CALL( SCIPhashmapCreate(&rank, SCIPblkmem(scip), MAX(norig, 1)) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &key, MAX(nc, 1)) );
+   for( k = 0; k < norig; ++k )
+   {
+      SCIP_CONS* t = NULL;
+      SCIP_CALL( SCIPgetTransformedCons(scip, orig[k], &t) );
+      if( t != NULL && !SCIPhashmapExists(rank, (void*)t) )
+         SCIP_CALL( SCIPhashmapInsertInt(rank, (void*)t, k) );
+   }
+   for( k = 0; k < nc; ++k )
+   {
+      out[k] = conss[k];
+      key[k] = SCIPhashmapExists(rank, (void*)conss[k]) ? SCIPhashmapGetImageInt(rank, (void*)conss[k]) : norig + k;
+   }
+   SCIPsortIntPtr(key, (void**)out, nc);
+   SCIPfreeBufferArray(scip, &key);
+   SCIPhashmapFree(&rank);
+   return SCIP_OKAY;
+}
+
 /** copies the rows of the handlers into CSR form over the active variables (columns = SCIPvarGetProbindex): fixed,
  *  aggregated, multi-aggregated and negated variables are replaced by their active variables
  *  (SCIPgetProbvarLinearSum), constants move into the sides; modifiable constraints are left to their handler */
@@ -307,12 +340,21 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
 
    pd->rowptr[0] = 0;
    pd->nrows = 0;
+   pd->nspecialrows = 0;
    for( h = 0; h < numHandlers(pd); ++h )
    {
       SCIP_CONSHDLR* hdlr = SCIPfindConshdlr(scip, HDLRS[h]);
       SCIP_CONS** conss = hdlr == NULL ? NULL : SCIPconshdlrGetConss(hdlr);
+      SCIP_CONS** ordered = NULL;
       int nc = hdlr == NULL ? 0 : SCIPconshdlrGetNConss(hdlr);
       int c;
+      if( pd->sciporder && nc > 0 )
+      {
+         /* SCIP's order marks a variable's rows in the order its bound-change events reach them */
+         SCIP_CALL( SCIPallocBufferArray(scip, &ordered, nc) );
+         SCIP_CALL( creationOrder(scip, conss, nc, ordered) );
+         conss = ordered;
+      }
       for( c = 0; c < nc; ++c )
       {
          SCIP_CONS* cons = conss[c];
@@ -390,8 +432,11 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
          pd->lhs[pd->nrows] = SCIPisInfinity(scip, -l) ? -SCIPinfinity(scip) : l;
          pd->rhs[pd->nrows] = SCIPisInfinity(scip, r) ? SCIPinfinity(scip) : r;
          pd->nrows++;
+         pd->nspecialrows += h > 0 ? 1 : 0;
          pd->rowptr[pd->nrows] = p;
       }
+      if( ordered != NULL )
+         SCIPfreeBufferArray(scip, &ordered);
    }
    SCIPfreeBufferArray(scip, &where);
    SCIPfreeBufferArray(scip, &bc);
@@ -425,12 +470,13 @@ static void disable(SCIP* scip, SCIP_PROPDATA* pd, const char* why, int rc)
    pd->failed = TRUE;
 }
 
-/** numerics of the running SCIP (set.c / def.h) for the device rules */
-static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
+/** numerics of the running SCIP (set.c / def.h) for the device rules, plus the mode flags in extraflags */
+static SCIP_RETCODE setDeviceParamsWith(SCIP* scip, SCIP_PROPDATA* pd, int32_t extraflags)
 {
    gbp_params p;
    SCIP_Real v;
    gbp_default_params(&p);
+   p.flags |= extraflags;
    p.infinity = SCIPinfinity(scip);
    p.epsilon = SCIPepsilon(scip);
    p.sumepsilon = SCIPsumepsilon(scip);
@@ -452,6 +498,11 @@ static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
    if( gbp_set_params(pd->ctx, &p) != GBP_OK )
       return SCIP_INVALIDDATA;
    return SCIP_OKAY;
+}
+
+static SCIP_RETCODE setDeviceParams(SCIP* scip, SCIP_PROPDATA* pd)
+{
+   return setDeviceParamsWith(scip, pd, 0);
 }
 
 /** whether cons_linear would run ranged-row propagation now (consPropLinear, cons_linear.c:16159-16170): its
@@ -1035,6 +1086,11 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/probing",
          "also propagate in probing nodes (SCIPpropagateProbing); SCIPpropagateGpulinearNodes serves many probing "
          "candidates at once", &pd->inprobing, FALSE, TRUE, NULL, NULL) );
+   SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/sciporder",
+         "SCIPpropagateGpulinearNodes propagates its nodes in SCIP's own order (one marked row at a time, every "
+         "tightening applied at once) instead of rounds, with the rows re-read in the order SCIP holds them; only "
+         "for matrices of linear rows alone and without ranged-row propagation", &pd->sciporder, FALSE, FALSE, NULL,
+         NULL) );
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacespecialised",
          "switch off the propagation of setppc, logicor, knapsack and varbound (constraints/<handler>/propfreq = -1)",
          &pd->replacespecialised, FALSE, FALSE, paramChgdReplacespecialised, NULL) );
@@ -1125,6 +1181,20 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
    pd = SCIPpropGetData(prop);
    if( pd->failed || pd->ctx == NULL || nnodes == 0 )
       return SCIP_OKAY;
+   if( pd->sciporder )
+   {
+      /* SCIP's order visits a row's entries in the order SCIP holds them now (consdataSort has sorted the rows it
+       * propagated since the matrix was built): read the rows again */
+      SCIP_CALL( upload(scip, pd) );
+      if( pd->failed )
+         return SCIP_OKAY;
+      if( pd->nspecialrows > 0 || wantRanged(scip) )
+      {
+         SCIPwarningMessage(scip, "propagator <%s>: SCIP's order needs linear rows alone and no ranged-row "
+            "propagation; batched nodes not propagated\n", PROP_NAME);
+         return SCIP_OKAY;
+      }
+   }
    nchg = nodebeg[nnodes];
    for( j = 0; j < pd->ncols; ++j )
    {
@@ -1169,9 +1239,14 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
       else
          col[k] = j;
    }
+   if( rc == GBP_OK && pd->sciporder && setDeviceParamsWith(scip, pd, GBP_FLAG_SCIPORDER) != SCIP_OKAY )
+      rc = GBP_ERR_CUDA;
    if( rc == GBP_OK )
       rc = gbp_propagate_nodes(pd->ctx, pd->lb, pd->ub, nnodes, ptr, col, lbs, ubs, ocut, orounds, ooff, on, ocol, olb,
          oub, outcap, &res);
+   /* the propagator's own calls run in rounds */
+   if( pd->sciporder && setDeviceParams(scip, pd) != SCIP_OKAY )
+      disable(scip, pd, "restoring the device parameters failed", GBP_ERR_INVALID);
    if( rc == GBP_OK || rc == GBP_ERR_LIMIT )
    {
       at = 0;

@@ -50,7 +50,13 @@ SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip);
  *  variables; SCIP_INVALIDDATA otherwise) and runs linear propagation to its fixpoint; SCIP's bounds are not
  *  changed.  Per node: cutoff[k], and the variables whose bounds propagation moved against the local bounds, with
  *  their bounds, at outvars/outlbs/outubs[outbeg[k] .. outbeg[k+1]) (outcap entries in all; a cut-off node has
- *  none).  *success is FALSE when the propagator is inactive (no GPU) or the outputs did not fit. */
+ *  none).  *success is FALSE when the propagator is inactive (no GPU) or the outputs did not fit.
+ *  With propagating/gpulinear/sciporder the nodes run in SCIP's own order (GBP_FLAG_SCIPORDER): the call reads the
+ *  rows again in the order SCIP holds them and uploads them, and each node starts from the local bounds with no row
+ *  marked, so that its cutoff verdict and integer bounds are the ones SCIP's own propagation of the node reaches
+ *  (continuous bounds within 1e-9 relative or feastol absolute).  That mode needs a matrix of linear rows alone
+ *  (no rows of setppc, logicor, knapsack or varbound constraints) and ranged-row propagation off; otherwise
+ *  *success is FALSE. */
 SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* nodebeg, SCIP_VAR** vars,
    const SCIP_Real* lbs, const SCIP_Real* ubs, int outcap, SCIP_Bool* cutoff, int* outbeg, SCIP_VAR** outvars,
    SCIP_Real* outlbs, SCIP_Real* outubs, SCIP_Bool* success);

@@ -1,7 +1,8 @@
 /* Test double of libgbp for the plugin's SCIP-side tests: the C-ABI calls the propagator plugin makes, answered by
  * the oracle (oracle/linprop_oracle.c) on the host.  It exists so that SCIP (which builds only where its sources
  * are) can run the plugin end to end -- write-back of the change log and conflict resolution -- without a GPU.  It
- * is linked only into tests/plugin/solve_driver.c; the product library libgbp has no host path. */
+ * is linked only into the SCIP-side test drivers (tests/plugin/*_driver.c); the product library libgbp has no host
+ * path. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -29,6 +30,7 @@ struct gbp_ctx
    double* dlb;   /* bounds kept between sparse calls (gbp_set_bounds / gbp_propagate_changes) */
    double* dub;
    int bset;
+   int sciporder;  /* GBP_FLAG_SCIPORDER: batched nodes through the restatement of SCIP's order */
 };
 
 int gbp_version(void) { return 0; }
@@ -97,6 +99,9 @@ int gbp_set_params(gbp_ctx* ctx, const gbp_params* p)
    ctx->par.maxrounds = p->maxrounds;
    ctx->par.flags = ((p->flags & GBP_FLAG_NOSORTVARS) ? LPO_FLAG_NOSORTVARS : 0)
       | ((p->flags & GBP_FLAG_RANGEDROW) ? LPO_FLAG_RANGEDROW : 0);
+   if( (p->flags & GBP_FLAG_SCIPORDER) && (p->flags & GBP_FLAG_RANGEDROW) )
+      return GBP_ERR_INVALID;
+   ctx->sciporder = (p->flags & GBP_FLAG_SCIPORDER) != 0;
    return GBP_OK;
 }
 
@@ -398,8 +403,8 @@ int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub
       memset(res, 0, sizeof(*res));
    if( tn == NULL || tc == NULL || tl == NULL || tu == NULL )
       rc = GBP_ERR_NOMEM;
-   else if( lpo_propagate_nodes(&ctx->P, &ctx->par, baselb, baseub, nnodes, ptr, chg_col, chg_lb, chg_ub, out_cutoff,
-               out_rounds, tn, tc, tl, tu, (int32_t)n, 1, &tot) != 0 )
+   else if( (ctx->sciporder ? lpo_propagate_nodes_seq : lpo_propagate_nodes)(&ctx->P, &ctx->par, baselb, baseub, nnodes,
+               ptr, chg_col, chg_lb, chg_ub, out_cutoff, out_rounds, tn, tc, tl, tu, (int32_t)n, 1, &tot) != 0 )
       rc = GBP_ERR_NOMEM;
    else
    {

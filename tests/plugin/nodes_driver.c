@@ -5,7 +5,11 @@
  * SCIPpropagateProbing with cons_linear's propagation (the plugin does not run in probing:
  * propagating/gpulinear/probing = FALSE).  Prints:
  *   nodes <n> success <0|1> cutoffs <batched> <probing> cutoffmismatch <k> intmismatch <k> moved <total>
- * Usage: nodes_driver <instance.mps> [nodes] */
+ *   ... contmismatch <k>   (nodes with a continuous bound outside 1e-9 relative / feastol absolute)
+ * With "sciporder" after the node count the batched call runs in SCIP's own order
+ * (propagating/gpulinear/sciporder), and before each probing node the rows a cut-off node left marked are unmarked,
+ * so that every node starts with no row marked, as that mode assumes.
+ * Usage: nodes_driver <instance.mps> [nodes] [sciporder] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -16,6 +20,7 @@
 
 static int nwant = 200;
 static int done = 0;
+static int sciporder = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -43,7 +48,7 @@ static SCIP_DECL_HEUREXEC(heurExecCheck)
    int outcap;
    int k;
    int j;
-   int ncutb = 0, ncutp = 0, cutmis = 0, intmis = 0;
+   int ncutb = 0, ncutp = 0, cutmis = 0, intmis = 0, contmis = 0;
 
    (void)heur;
    (void)nodeinfeasible;
@@ -117,6 +122,17 @@ static SCIP_DECL_HEUREXEC(heurExecCheck)
       {
          SCIP_Bool pcut = FALSE;
          int q;
+         if( sciporder )
+         {
+            /* rows a cut-off node left marked (its propagation stopped before reaching them) */
+            SCIP_CONSHDLR* lin = SCIPfindConshdlr(scip, "linear");
+            SCIP_CONS** lc = SCIPconshdlrGetConss(lin);
+            int nlc = SCIPconshdlrGetNConss(lin);
+            int c;
+            for( c = 0; c < nlc; ++c )
+               if( SCIPconsIsMarkedPropagate(lc[c]) )
+                  SCIP_CALL( SCIPunmarkConsPropagate(scip, lc[c]) );
+         }
          SCIP_CALL( SCIPnewProbingNode(scip) );
          for( q = beg[k]; q < beg[k + 1] && !pcut; ++q )
          {
@@ -157,6 +173,23 @@ static SCIP_DECL_HEUREXEC(heurExecCheck)
                   intmis++;
                   break;
                }
+            for( j = 0; j < nvars; ++j )
+            {
+               SCIP_Real sl = SCIPvarGetLbLocal(vars[j]);
+               SCIP_Real su = SCIPvarGetUbLocal(vars[j]);
+               if( SCIPvarGetType(vars[j]) == SCIP_VARTYPE_CONTINUOUS
+                  && (REALABS(elb[j] - sl) > MAX(1e-9 * REALABS(sl), 1e-6)
+                     || REALABS(eub[j] - su) > MAX(1e-9 * REALABS(su), 1e-6)) )
+               {
+                  int last = k - 1;  /* the last cut-off node before this one */
+                  while( last >= 0 && !cut[last] )
+                     --last;
+                  fprintf(stderr, "node %d column %d: batched [%.17g, %.17g] probing [%.17g, %.17g] base [%.17g, "
+                     "%.17g]; last cut-off node before it: %d\n", k, j, elb[j], eub[j], sl, su, rlb[j], rub[j], last);
+                  contmis++;
+                  break;
+               }
+            }
          }
          SCIP_CALL( SCIPbacktrackProbing(scip, 0) );
       }
@@ -166,8 +199,8 @@ static SCIP_DECL_HEUREXEC(heurExecCheck)
       SCIPfreeBufferArray(scip, &eub);
       SCIPfreeBufferArray(scip, &elb);
    }
-   printf("nodes %d success %d cutoffs %d %d cutoffmismatch %d intmismatch %d moved %d\n", nwant, success ? 1 : 0, ncutb,
-      ncutp, cutmis, intmis, success ? obeg[nwant] : -1);
+   printf("nodes %d success %d cutoffs %d %d cutoffmismatch %d intmismatch %d contmismatch %d moved %d\n", nwant,
+      success ? 1 : 0, ncutb, ncutp, cutmis, intmis, contmis, success ? obeg[nwant] : -1);
    SCIPfreeBufferArray(scip, &ou);
    SCIPfreeBufferArray(scip, &ol);
    SCIPfreeBufferArray(scip, &ov);
@@ -193,11 +226,14 @@ int main(int argc, char** argv)
       return 2;
    if( argc > 2 )
       nwant = atoi(argv[2]);
+   if( argc > 3 && strcmp(argv[3], "sciporder") == 0 )
+      sciporder = 1;
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
       return 1;
    SCIPsetBoolParam(scip, "propagating/gpulinear/probing", FALSE);
+   SCIPsetBoolParam(scip, "propagating/gpulinear/sciporder", sciporder ? TRUE : FALSE);
    if( SCIPincludeHeurBasic(scip, &heur, "nodecheck", "batched-node check", 'c', 1000000, 1, 0, -1,
          SCIP_HEURTIMING_BEFORENODE, FALSE, heurExecCheck, NULL) != SCIP_OKAY )
       return 1;

@@ -91,7 +91,8 @@ def solve_driver(tmp_path_factory, oracle_mod):
            os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
            os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c"),
            os.path.join(ROOT, "tests", "plugin", "gbp_oracle_shim.c"),
-           os.path.join(ROOT, "oracle", "linprop_oracle.c")]
+           os.path.join(ROOT, "oracle", "linprop_oracle.c"),
+           os.path.join(ROOT, "oracle", "linprop_seq.c")]
     inc = ["-I" + os.path.join(REF, "include"), "-I" + os.path.join(oracle_mod.REFDIR, "src"),
            "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "scip_gb300", "plugin"),
            "-I" + os.path.join(ROOT, "oracle")]
@@ -209,4 +210,23 @@ def test_batched_plugin_entry_agrees_with_scip_probing(nodes_driver, oracle_mod,
     assert got["success"] == "1"
     assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0", line[0]
     assert int(got["moved"]) > 0
+
+
+@pytest.mark.parametrize("name", ["bell5", "egout", "enigma", "flugpl", "lseu", "misc03", "p0548", "rgn"])
+def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_driver, oracle_mod, name):
+    """propagating/gpulinear/sciporder: the batched entry reads the rows again in the order SCIP holds them and
+    propagates 200 nodes in SCIP's own order; SCIP propagates each node in probing with no row marked at its start:
+    the same cutoff verdicts and integer bounds on every node, continuous bounds within 1e-9 relative or feastol."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    r = subprocess.run([nodes_driver, path, "200", "sciporder"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")]
+    assert line, r.stdout + r.stderr[-2000:]
+    f = line[0].split()
+    got = {f[i]: f[i + 1] for i in range(len(f) - 1) if not f[i].lstrip("-").isdigit()}
+    assert got["success"] == "1", r.stderr[-2000:]
+    assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0" and got["contmismatch"] == "0", \
+        line[0] + "\n" + r.stderr[-1500:]
 
