@@ -547,6 +547,34 @@ def mixed_small(rng: np.random.Generator) -> Instance:
                     name="mixed_small")
 
 
+def mixed_huge(rng: np.random.Generator) -> Instance:
+    """mixed_small with contributions past SCIP's hugeval (1e15): a fifth of the coefficients scaled by 1e3..1e7
+    (up to about 1e14) and three in ten of the bounded continuous columns widened to 1e5..1e9, so that activities
+    count huge contributions (the neghuge/poshuge counters) besides infinite ones; sides again from a point inside
+    the bounds."""
+    inst = mixed_small(rng)
+    vals = inst.vals.copy()
+    sel = rng.random(len(vals)) < 0.2
+    vals[sel] *= 10 ** rng.uniform(3, 7, int(sel.sum()))
+    lb, ub = inst.lb.copy(), inst.ub.copy()
+    wide = (inst.isint == 0) & (ub < INF) & (lb > -INF) & (rng.random(inst.n) < 0.3)
+    ub[wide] = lb[wide] + 10 ** rng.uniform(5, 9, int(wide.sum()))
+    x = np.clip(rng.uniform(-5, 20, inst.n), np.where(lb > -INF, lb, -50), np.where(ub < INF, ub, 50))
+    x = np.where(inst.isint == 1, np.clip(np.round(x), lb, ub), x)
+    lhs, rhs = inst.lhs.copy(), inst.rhs.copy()
+    for i in range(inst.m):
+        sl = slice(int(inst.rowptr[i]), int(inst.rowptr[i + 1]))
+        act = float(vals[sl] @ x[inst.colidx[sl]])
+        if lhs[i] > -INF and rhs[i] < INF:
+            w = rhs[i] - lhs[i]
+            lhs[i], rhs[i] = act - w / 2, act + w / 2
+        elif lhs[i] > -INF:
+            lhs[i] = act - abs(rng.normal())
+        elif rhs[i] < INF:
+            rhs[i] = act + abs(rng.normal())
+    return Instance(inst.rowptr, inst.colidx, vals, lhs, rhs, lb, ub, inst.isint, name="mixed_huge")
+
+
 def concat_instances(insts: List[Instance]):
     """Block-diagonal union of independent instances: (instance, row_off, col_off) with instance k owning rows
     row_off[k]:row_off[k+1] and columns col_off[k]:col_off[k+1]."""

@@ -28,6 +28,7 @@ propagated before it.  Cases:
                              that the ranged rule finds many of them infeasible (concatenated, with offsets)
   fuzz/mixed_small           300 small random MIPs with coefficient magnitudes 1e-5..1e7 in one row, infinite
                              bounds and equations (concatenated, with offsets), SCIP's root and up to 8 nodes each
+  fuzz/mixed_huge            the same with contributions past hugeval (coefficients to ~1e14, bounds to 1e9)
 
 Usage: python tests/golden/make_golden.py [case ...]   (needs the SCIP sources; writes tests/golden/*.npz;
 no argument builds every case)
@@ -157,15 +158,18 @@ def save_tiny_cutoffs():
     print(f"{path}: {len(insts)} instances, {int(out['sort_cut'].sum())} infeasible (sortvars)")
 
 
-MIXED_SEEDS = range(5000, 5300)
+MIXED = {"mixed_small": (instances.mixed_small, range(5000, 5300)),
+         "mixed_huge": (instances.mixed_huge, range(7000, 7300))}
 
 
-def save_mixed_small():
+def save_mixed(name):
     """300 small random MIPs of instances.mixed_small (seeds 5000..5299; coefficient magnitudes 1e-5..1e7 in one
-    row, infinite bounds, equations), concatenated with offsets, with SCIP's root (bounds, row orders, deleted
-    rows) for both rules and up to 8 nodes per feasible instance (1..4 fixings, from SCIP's residual-rule root,
-    every node from a newly transformed problem), under tests/golden/fuzz."""
-    insts = [instances.mixed_small(np.random.default_rng(np.random.PCG64(s))) for s in MIXED_SEEDS]
+    row, infinite bounds, equations) or instances.mixed_huge (seeds 7000..7299; contributions past hugeval too),
+    concatenated with offsets, with SCIP's root (bounds, row orders, deleted rows) for both rules and up to 8 nodes
+    per feasible instance (1..4 fixings, from SCIP's residual-rule root, every node from a newly transformed
+    problem), under tests/golden/fuzz/<name>.npz."""
+    make, MIXED_SEEDS = MIXED[name]
+    insts = [make(np.random.default_rng(np.random.PCG64(s))) for s in MIXED_SEEDS]
     big, row_off, col_off = instances.concat_instances(insts)
     out = {"rowptr": big.rowptr, "colidx": big.colidx, "vals": big.vals, "lhs": big.lhs, "rhs": big.rhs,
            "lb": big.lb, "ub": big.ub, "isint": big.isint, "row_off": row_off, "col_off": col_off,
@@ -214,7 +218,7 @@ def save_mixed_small():
         out[f"{tag}_ncut"], out[f"{tag}_nptr"], out[f"{tag}_ncol"] = cut, ptr, col
         out[f"{tag}_nlb"], out[f"{tag}_nub"] = lb, ub
     os.makedirs(os.path.join(HERE, "fuzz"), exist_ok=True)
-    path = os.path.join(HERE, "fuzz", "mixed_small.npz")
+    path = os.path.join(HERE, "fuzz", f"{name}.npz")
     np.savez_compressed(path, **out)
     print(f"{path}: {K} instances, {int(out['res_rootcut'].sum())} infeasible roots, {len(out['node_inst'])} nodes, "
           f"{os.path.getsize(path) // 1024} KiB")
@@ -324,7 +328,7 @@ def main(names):
     for name in names or list(all_cases) + ["ranged/" + k for k in ranged] + ["ranged/tiny_cutoffs",
                                                                              "node_workload_scip",
                                                                              "node_workload_base", "miplib",
-                                                                             "fuzz/mixed_small"]:
+                                                                             "fuzz/mixed_small", "fuzz/mixed_huge"]:
         if name == "node_workload_scip":
             save_node_workload()
             continue
@@ -334,8 +338,8 @@ def main(names):
         if name == "miplib":
             save_miplib_cases()
             continue
-        if name == "fuzz/mixed_small":
-            save_mixed_small()
+        if name.startswith("fuzz/"):
+            save_mixed(name[len("fuzz/"):])
             continue
         if name == "ranged/tiny_cutoffs":
             save_tiny_cutoffs()

@@ -136,11 +136,15 @@ class Agreement:
 
 
 def load_mixed_small():
-    """golden/fuzz/mixed_small.npz split into its 300 instances: per instance a dict with the instance, its seed,
+    return load_mixed("mixed_small")
+
+
+def load_mixed(name):
+    """golden/fuzz/<name>.npz split into its 300 instances: per instance a dict with the instance, its seed,
     per rule ("res", "easy") SCIP's root (cut, lb, ub, order, rowdel) and its nodes' results (a list of
     (cutoff, cols, lb, ub) with instance-local columns that differ from that rule's root), and the nodes
     (instance-local NodeBatch, or None)."""
-    with np.load(os.path.join(GOLDEN, "fuzz", "mixed_small.npz")) as f:
+    with np.load(os.path.join(GOLDEN, "fuzz", f"{name}.npz")) as f:
         z = dict(f)
     ro, co = z["row_off"], z["col_off"]
     K = len(ro) - 1
@@ -152,7 +156,7 @@ def load_mixed_small():
         p0, p1 = int(z["rowptr"][r0]), int(z["rowptr"][r1])
         inst = Instance(z["rowptr"][r0:r1 + 1] - p0, z["colidx"][p0:p1] - c0, z["vals"][p0:p1], z["lhs"][r0:r1],
                         z["rhs"][r0:r1], z["lb"][c0:c1], z["ub"][c0:c1], z["isint"][c0:c1],
-                        name=f"mixed_small/{int(z['seeds'][k])}")
+                        name=f"{name}/{int(z['seeds'][k])}")
         q0, q1 = int(first[k]), int(first[k + 1])
         nb = None
         if q1 > q0:

@@ -5,12 +5,15 @@ starts (oracle/linprop_seq.c):
 
 - carried (lpo_propagate_seq_states, then lpo_propagate_nodes_seq_from): every node equals SCIP's bit for bit --
   cutoffs and every bound, continuous columns included -- on the golden cases, the MIPLIB instances, the 4,096 nodes
-  of the batched-node workload and 1,616 nodes of 300 small mixed-magnitude instances;
+  of the batched-node workload, 1,616 nodes of 300 small mixed-magnitude instances and 1,544 nodes of 300 more
+  with contributions past hugeval;
 - afresh (lpo_propagate_nodes_seq, the start the device kernel k_nodes_seq computes): activities are recomputed on
-  a row's first use in the node, so continuous bounds can differ in the last bits.  That meets the exact contract
-  (cutoffs and integer bounds equal, continuous bounds within 1e-9 relative or feastol absolute) everywhere except
-  one node of the mixed-magnitude instances, where a row with coefficients 8.3e-4 .. 7.2e6 turns a last-bit
-  difference of a residual activity into 6.7e-6 on a continuous bound.
+  a row's first use in the node, so continuous bounds can differ in the last bits.  Cutoff verdicts and integer
+  bounds stay equal everywhere.  Continuous bounds stay within 1e-9 relative or feastol absolute on the golden
+  cases and the workload, but not everywhere: on one node of the mixed-magnitude instances a row with coefficients
+  8.3e-4 .. 7.2e6 turns a last-bit difference of a residual activity into 6.7e-6 on a continuous bound, and with
+  contributions past hugeval 10 (residual rule) and 13 (easy rule) of 1,544 nodes, in 4 instances, leave the
+  tolerance.
 """
 import numpy as np
 import pytest
@@ -87,18 +90,31 @@ def test_workload_nodes_from_the_roots_activities_equal_scip_bit_for_bit(oracle_
         assert np.array_equal(out["ub"][k, :n][o], theirs[2][p]), f"node {k}"
 
 
-@pytest.fixture(scope="module")
-def mixed():
-    return G.load_mixed_small()
+_MIXED = {}
+
+
+def _mixed(name):
+    if name not in _MIXED:
+        _MIXED[name] = G.load_mixed(name)
+    return _MIXED[name]
+
+
+# afresh nodes outside the continuous tolerance, (seed, node), per fixture and rule
+_HUGE_RES = {(7018, 5), (7233, 1), (7233, 2), (7233, 3), (7233, 4), (7233, 5), (7233, 7), (7294, 3), (7294, 4),
+             (7294, 5)}
+KNOWN_AFRESH = {("mixed_small", "res"): {(5056, 4)}, ("mixed_small", "easy"): {(5056, 4)},
+                ("mixed_huge", "res"): _HUGE_RES,
+                ("mixed_huge", "easy"): _HUGE_RES | {(7156, 1), (7156, 2), (7156, 6)}}
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-def test_mixed_small_roots_equal_scip(oracle_mod, mixed, tag):
-    """300 small instances mixing coefficient magnitudes 1e-5..1e7 in one row, infinite bounds and equations: the
-    restatement's root equals SCIP's bit for bit -- cutoff verdict, every bound, each row's final order and the
-    rows deleted as redundant."""
+@pytest.mark.parametrize("name", ["mixed_small", "mixed_huge"])
+def test_mixed_roots_equal_scip(oracle_mod, name, tag):
+    """300 small instances mixing coefficient magnitudes 1e-5..1e7 in one row, infinite bounds and equations
+    (mixed_small), and 300 more with contributions past hugeval (mixed_huge): the restatement's root equals SCIP's
+    bit for bit -- cutoff verdict, every bound, each row's final order and the rows deleted as redundant."""
     par = _par(oracle_mod, tag)
-    for c in mixed:
+    for c in _mixed(name):
         inst, root = c["inst"], c[tag]["root"]
         vidx = scip_var_index(inst.isint, inst.lb, inst.ub)
         orc = oracle_mod.Oracle(inst, vidx)
@@ -113,11 +129,12 @@ def test_mixed_small_roots_equal_scip(oracle_mod, mixed, tag):
 
 
 @pytest.mark.parametrize("tag", ["res", "easy"])
-def test_mixed_small_nodes_carried_and_afresh(oracle_mod, mixed, tag):
+@pytest.mark.parametrize("name", ["mixed_small", "mixed_huge"])
+def test_mixed_nodes_carried_and_afresh(oracle_mod, name, tag):
     par = _par(oracle_mod, tag)
     outside = set()
     nodes = 0
-    for c in mixed:
+    for c in _mixed(name):
         inst, nb, root = c["inst"], c["nodes"], c[tag]["root"]
         if nb is None or root["cut"]:
             continue
@@ -134,4 +151,4 @@ def test_mixed_small_nodes_carried_and_afresh(oracle_mod, mixed, tag):
             if ag.cont_cols_out_of_tol:
                 outside.add((c["seed"], k))
     assert nodes > 1500
-    assert outside == {(5056, 4)}
+    assert outside == KNOWN_AFRESH[(name, tag)]
