@@ -1194,6 +1194,20 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
             "propagation; batched nodes not propagated\n", PROP_NAME);
          return SCIP_OKAY;
       }
+      /* the device takes a row's leading binaries under the base (local) bounds; SCIP's are binary in the global
+       * domain (SCIPvarIsBinary).  Below the root they differ for an integer column whose local domain lies in
+       * [0,1] and whose global domain does not. */
+      for( j = 0; j < pd->ncols && SCIPgetDepth(scip) > 0; ++j )
+      {
+         SCIP_VAR* v = pd->vars[j];
+         if( pd->isint[j] && SCIPvarGetLbLocal(v) >= 0.0 && SCIPvarGetUbLocal(v) <= 1.0
+            && (SCIPvarGetLbGlobal(v) < 0.0 || SCIPvarGetUbGlobal(v) > 1.0) )
+         {
+            SCIPwarningMessage(scip, "propagator <%s>: <%s> is binary in the local domain only; SCIP's order "
+               "not available at this node\n", PROP_NAME, SCIPvarGetName(v));
+            return SCIP_OKAY;
+         }
+      }
    }
    nchg = nodebeg[nnodes];
    for( j = 0; j < pd->ncols; ++j )

@@ -55,8 +55,9 @@ SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip);
  *  rows again in the order SCIP holds them and uploads them, and each node starts from the local bounds with no row
  *  marked, so that its cutoff verdict and integer bounds are the ones SCIP's own propagation of the node reaches
  *  (continuous bounds within 1e-9 relative or feastol absolute).  That mode needs a matrix of linear rows alone
- *  (no rows of setppc, logicor, knapsack or varbound constraints) and ranged-row propagation off; otherwise
- *  *success is FALSE. */
+ *  (no rows of setppc, logicor, knapsack or varbound constraints), ranged-row propagation off, and below the root
+ *  no integer variable that is binary in its local domain only (the device takes a row's binaries under the local
+ *  bounds, SCIP under the global ones); otherwise *success is FALSE. */
 SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* nodebeg, SCIP_VAR** vars,
    const SCIP_Real* lbs, const SCIP_Real* ubs, int outcap, SCIP_Bool* cutoff, int* outbeg, SCIP_VAR** outvars,
    SCIP_Real* outlbs, SCIP_Real* outubs, SCIP_Bool* success);
