@@ -9,7 +9,9 @@
  * With "sciporder" after the node count the batched call runs in SCIP's own order
  * (propagating/gpulinear/sciporder), and before each probing node the rows a cut-off node left marked are unmarked,
  * so that every node starts with no row marked, as that mode assumes.
- * Usage: nodes_driver <instance.mps> [nodes] [sciporder] */
+ * With "easy" last, cons_linear and the plugin use SCIP's default rule choice (maxeasyactivitydelta 1e6) instead of
+ * the residual rule everywhere (0).
+ * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -21,6 +23,7 @@
 static int nwant = 200;
 static int done = 0;
 static int sciporder = 0;
+static int easyrule = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -228,6 +231,8 @@ int main(int argc, char** argv)
       nwant = atoi(argv[2]);
    if( argc > 3 && strcmp(argv[3], "sciporder") == 0 )
       sciporder = 1;
+   if( argc > 4 && strcmp(argv[4], "easy") == 0 )
+      easyrule = 1;
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
@@ -255,7 +260,7 @@ int main(int argc, char** argv)
    SCIPsetIntParam(scip, "presolving/maxrounds", 0);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);
-   SCIPsetRealParam(scip, "constraints/linear/maxeasyactivitydelta", 0.0);
+   SCIPsetRealParam(scip, "constraints/linear/maxeasyactivitydelta", easyrule ? 1e6 : 0.0);
    /* an infeasible probing node must not tighten the root's bounds for the nodes after it (conflict analysis of
     * a cutoff can fix a variable globally) */
    SCIPsetBoolParam(scip, "conflict/enable", FALSE);

@@ -212,15 +212,19 @@ def test_batched_plugin_entry_agrees_with_scip_probing(nodes_driver, oracle_mod,
     assert int(got["moved"]) > 0
 
 
-@pytest.mark.parametrize("name", ["bell5", "egout", "enigma", "flugpl", "lseu", "misc03", "p0548", "rgn"])
-def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_driver, oracle_mod, name):
+@pytest.mark.parametrize("rule", ["res", "easy"])
+@pytest.mark.parametrize("name", ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03",
+                                  "p0548", "rgn"])
+def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_driver, oracle_mod, name, rule):
     """propagating/gpulinear/sciporder: the batched entry reads the rows again in the order SCIP holds them and
     propagates 200 nodes in SCIP's own order; SCIP propagates each node in probing with no row marked at its start:
-    the same cutoff verdicts and integer bounds on every node, continuous bounds within 1e-9 relative or feastol."""
+    the same cutoff verdicts and integer bounds on every node, continuous bounds within 1e-9 relative or feastol.
+    Every MIPLIB instance the reference ships (but semicon1), the residual rule and SCIP's default rule choice."""
     path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
     if not os.path.exists(path):
         pytest.skip(f"{name}.mps not shipped")
-    r = subprocess.run([nodes_driver, path, "200", "sciporder"], capture_output=True, text=True, timeout=600)
+    args = [nodes_driver, path, "200", "sciporder"] + (["easy"] if rule == "easy" else [])
+    r = subprocess.run(args, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")]
     assert line, r.stdout + r.stderr[-2000:]
