@@ -1,5 +1,5 @@
 """The oracle's restatement of SCIP's own propagation order (oracle/linprop_seq.c) against SCIP 11's results
-(tests/golden).  This is the exact contract of the benchmark spec, with no recorded allowance:
+(tests/golden).  This is the exact parity contract, with no recorded allowance:
 
 - root: cutoff verdicts equal and every bound equal bit for bit; each row ends in the order SCIP holds it in, and
   the rows SCIP deleted as redundant are the rows the restatement deleted;
