@@ -30,6 +30,19 @@ def test_compensated_activity(oracle_mod):
     assert not cnt.any()
 
 
+def test_double_double_sum_known_answer(oracle_mod):
+    """The known answer of SCIP's own double-double test (tests/src/misc/dbldblarith.c, test "sum"): c + b + a + a
+    with a = 0.000000034567, b = 2.34567, c = 12345678.9 is 1.2345681245670069507e7 when summed compensated, which a
+    plain double sum misses.  A row of four unit coefficients with columns fixed at c, b, a, a sums the same terms."""
+    a, b, c = 0.000000034567, 2.34567, 12345678.9
+    want = 1.2345681245670069507e7
+    inst = single_rows([([0, 1, 2, 3], [1.0, 1.0, 1.0, 1.0], -INF, INF)], [c, b, a, a], [c, b, a, a], [0, 0, 0, 0])
+    act, cnt = oracle_mod.Oracle(inst).activities(inst.lb, inst.ub)
+    assert act[0, 0] + act[0, 1] == want and act[0, 2] + act[0, 3] == want
+    assert ((c + b) + a) + a != want
+    assert not cnt.any()
+
+
 def test_infinity_and_huge_counters(oracle_mod):
     # x0 in (-inf, 1], x1 in [0, inf), x2 in [2e15, 3e15] (huge contributions), x3 in [1, 2]
     inst = single_rows([([0, 1, 2, 3], [2.0, -3.0, 1.0, 1.0], -INF, INF)],
