@@ -234,3 +234,36 @@ def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_drive
     assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0" and got["contmismatch"] == "0", \
         line[0] + "\n" + r.stderr[-1500:]
 
+
+def test_constraint_with_a_fixed_variable_added_while_solving(tmp_path, oracle_mod):
+    """SCIP's own scenario tests/src/cons/linear/fixedvar.c with the propagator in place: after bell5's root a
+    variable fixed to 0 and a linear constraint over it and five more variables are added, and the search continues
+    to node 5 with cons_linear's propagation delayed to depth 3.  The propagator takes up the new row (one more row;
+    the fixed variable becomes a constant) and keeps running."""
+    if not os.path.exists(LIBSCIP):
+        pytest.skip("SCIP build (oracle/_ref) not present")
+    if not oracle_mod.REFDIR or not os.path.exists(os.path.join(oracle_mod.REFDIR, "src", "scip", "scip.h")):
+        pytest.skip("SCIP headers not present (REFDIR names the SCIP source tree)")
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", "bell5.mps")
+    if not os.path.exists(path):
+        pytest.skip("bell5.mps not shipped")
+    exe = str(tmp_path / "fixedvar_driver")
+    src = [os.path.join(ROOT, "tests", "plugin", "fixedvar_driver.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "prop_gpulinear.c"),
+           os.path.join(ROOT, "scip_gb300", "plugin", "gpulinear_reason.c"),
+           os.path.join(ROOT, "tests", "plugin", "gbp_oracle_shim.c"),
+           os.path.join(ROOT, "oracle", "linprop_oracle.c"),
+           os.path.join(ROOT, "oracle", "linprop_seq.c")]
+    inc = ["-I" + os.path.join(REF, "include"), "-I" + os.path.join(oracle_mod.REFDIR, "src"),
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "scip_gb300", "plugin"),
+           "-I" + os.path.join(ROOT, "oracle")]
+    subprocess.run(["gcc", "-std=c99", "-O1", "-D_XOPEN_SOURCE=600", "-ffp-contract=off", *inc, "-o", exe, *src,
+                    LIBSCIP, "-lstdc++", "-lm", "-lpthread"], check=True, capture_output=True)
+    r = subprocess.run([exe, path], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    f = r.stdout.split()
+    got = {f[i]: f[i + 1:i + 3] for i in range(len(f)) if f[i] in ("rows", "nnz", "active", "calls", "status")}
+    before, after = int(got["rows"][0]), int(got["rows"][1])
+    assert before > 0 and after == before + 1
+    assert got["active"][0] == "1" and int(got["calls"][0]) > 0
+
