@@ -112,6 +112,16 @@ def load_library(path: Optional[str] = None):
     L.gbp_propagate_nodes_noalloc.argtypes = ([ctypes.c_int64, ctypes.c_int64] + [_P] * 11 + [ctypes.c_int64]
                                               + [_P] * 11 + [ctypes.c_int64, ctypes.POINTER(GbpParams), _P,
                                                               ctypes.POINTER(GbpResult)])
+    declare_server(L)
+    if path is None:
+        _lib = L
+    return L
+
+
+def declare_server(L):
+    """Argument types of the serving loop's calls (gbp_server_*) on a loaded library."""
+    L.gbp_error_string.restype = ctypes.c_char_p
+    L.gbp_error_string.argtypes = [ctypes.c_int]
     L.gbp_server_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
                                     ctypes.c_int64, ctypes.POINTER(GbpParams), ctypes.c_int64, ctypes.c_int64] + [_P] * 8
     L.gbp_server_submit.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)]
@@ -122,9 +132,6 @@ def load_library(path: Optional[str] = None):
                                   ctypes.POINTER(ctypes.c_int64)]
     L.gbp_server_stats.argtypes = [_P] + [ctypes.POINTER(ctypes.c_int64)] * 4
     L.gbp_server_destroy.argtypes = [_P]
-    if path is None:
-        _lib = L
-    return L
 
 
 def default_params(maxeasy: Optional[float] = None, maxrounds: int = 0, sortvars: bool = True,
@@ -427,8 +434,9 @@ class Server:
     by worker threads inside libgbp into batched launches."""
 
     def __init__(self, inst, rootlb, rootub, params: Optional[GbpParams] = None, device: int = 0, workers: int = 2,
-                 max_batch: int = 4096, hbm_cap: int = 0, inst_workers: int = 0):
-        self.L = load_library()
+                 max_batch: int = 4096, hbm_cap: int = 0, inst_workers: int = 0, lib=None):
+        """lib: a library exporting gbp_server_* other than libgbp (declare_server applied), e.g. a test build."""
+        self.L = lib if lib is not None else load_library()
         self.n = inst.n
         self._keep = [np.ascontiguousarray(a) for a in (inst.rowptr.astype(np.int64), inst.colidx.astype(np.int32),
                                                         inst.vals, inst.lhs, inst.rhs, inst.isint.astype(np.int8),

@@ -31,6 +31,9 @@ struct gbp_ctx
    double* dub;
    int bset;
    int sciporder;  /* GBP_FLAG_SCIPORDER: batched nodes through the restatement of SCIP's order */
+   int64_t ninst;  /* gbp_upload_instance_list: the parts' offsets into the block-diagonal problem */
+   int64_t* row_off;
+   int64_t* col_off;
 };
 
 int gbp_version(void) { return 0; }
@@ -73,6 +76,8 @@ static void freeProblem(gbp_ctx* c)
    c->has_global = 0;
    free(c->dlb); free(c->dub);
    c->dlb = NULL; c->dub = NULL; c->bset = 0;
+   free(c->row_off); free(c->col_off);
+   c->row_off = NULL; c->col_off = NULL; c->ninst = 0;
 }
 
 int gbp_destroy(gbp_ctx* ctx)
@@ -443,3 +448,155 @@ int gbp_propagate_nodes(gbp_ctx* ctx, const double* baselb, const double* baseub
    free(tu);
    return rc;
 }
+
+/* the instances as parts of one block-diagonal problem; the checks of the library: row pointers from 0 and not
+ * decreasing, every column index inside its part */
+int gbp_upload_instance_list(gbp_ctx* ctx, int64_t ninst, const int64_t* m_k, const int64_t* n_k,
+   const int64_t* const* rowptr_k, const int32_t* const* colidx_k, const double* const* vals_k,
+   const double* const* lhs_k, const double* const* rhs_k, const int8_t* const* isint_k)
+{
+   int64_t m = 0, n = 0, nnz = 0;
+   int64_t k;
+   int64_t* rowptr;
+   int32_t* colidx;
+   double* vals;
+   double* lhs;
+   double* rhs;
+   int8_t* isint;
+   int rc;
+   if( ctx == NULL || ninst < 1 || m_k == NULL || n_k == NULL || rowptr_k == NULL )
+      return GBP_ERR_INVALID;
+   for( k = 0; k < ninst; ++k )
+   {
+      int64_t i;
+      const int64_t* rp = rowptr_k[k];
+      if( m_k[k] < 0 || n_k[k] < 0 || rp == NULL || rp[0] != 0 )
+         return GBP_ERR_INVALID;
+      for( i = 0; i < m_k[k]; ++i )
+         if( rp[i + 1] < rp[i] )
+            return GBP_ERR_INVALID;
+      for( i = 0; i < rp[m_k[k]]; ++i )
+         if( colidx_k[k][i] < 0 || colidx_k[k][i] >= n_k[k] )
+            return GBP_ERR_INVALID;
+      m += m_k[k];
+      n += n_k[k];
+      nnz += rp[m_k[k]];
+   }
+   rowptr = malloc(sizeof(int64_t) * (size_t)(m + 1));
+   colidx = malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+   vals = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+   lhs = malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+   rhs = malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+   isint = malloc((size_t)(n > 0 ? n : 1));
+   {
+      int64_t r = 0, c = 0, z = 0;
+      rowptr[0] = 0;
+      for( k = 0; k < ninst; ++k )
+      {
+         int64_t i;
+         const int64_t* rp = rowptr_k[k];
+         for( i = 0; i < m_k[k]; ++i )
+         {
+            rowptr[r + i + 1] = z + rp[i + 1];
+            lhs[r + i] = lhs_k[k][i];
+            rhs[r + i] = rhs_k[k][i];
+         }
+         for( i = 0; i < rp[m_k[k]]; ++i )
+         {
+            colidx[z + i] = (int32_t)(colidx_k[k][i] + c);
+            vals[z + i] = vals_k[k][i];
+         }
+         if( n_k[k] > 0 )
+            memcpy(isint + c, isint_k[k], (size_t)n_k[k]);
+         r += m_k[k];
+         c += n_k[k];
+         z += rp[m_k[k]];
+      }
+   }
+   rc = gbp_upload_problem(ctx, m, n, rowptr, colidx, vals, lhs, rhs, isint);
+   free(rowptr); free(colidx); free(vals); free(lhs); free(rhs); free(isint);
+   if( rc != GBP_OK )
+      return rc;
+   ctx->ninst = ninst;
+   ctx->row_off = malloc(sizeof(int64_t) * (size_t)(ninst + 1));
+   ctx->col_off = malloc(sizeof(int64_t) * (size_t)(ninst + 1));
+   ctx->row_off[0] = ctx->col_off[0] = 0;
+   for( k = 0; k < ninst; ++k )
+   {
+      ctx->row_off[k + 1] = ctx->row_off[k] + m_k[k];
+      ctx->col_off[k + 1] = ctx->col_off[k] + n_k[k];
+   }
+   return GBP_OK;
+}
+
+/* every part to its own root fixpoint (the oracle on the part alone), a cutoff flag per part */
+int gbp_propagate_instances(gbp_ctx* ctx, double* lb, double* ub, int8_t* inst_cutoff, gbp_result* res)
+{
+   int64_t k;
+   int32_t ncut = 0;
+   if( ctx == NULL || ctx->ninst < 1 || lb == NULL || ub == NULL )
+      return GBP_ERR_INVALID;
+   if( res != NULL )
+      memset(res, 0, sizeof(*res));
+   for( k = 0; k < ctx->ninst; ++k )
+   {
+      const int64_t r0 = ctx->row_off[k], c0 = ctx->col_off[k];
+      lpo_problem part = ctx->P;
+      lpo_result r;
+      int64_t* rp = malloc(sizeof(int64_t) * (size_t)(ctx->row_off[k + 1] - r0 + 1));
+      int32_t* ci;
+      int64_t i;
+      const int64_t z0 = ctx->rowptr[r0];
+      const int64_t nz = ctx->rowptr[ctx->row_off[k + 1]] - z0;
+      ci = malloc(sizeof(int32_t) * (size_t)(nz > 0 ? nz : 1));
+      for( i = 0; i <= ctx->row_off[k + 1] - r0; ++i )
+         rp[i] = ctx->rowptr[r0 + i] - z0;
+      for( i = 0; i < nz; ++i )
+         ci[i] = (int32_t)(ctx->colidx[z0 + i] - c0);
+      part.m = ctx->row_off[k + 1] - r0;
+      part.n = ctx->col_off[k + 1] - c0;
+      part.rowptr = rp;
+      part.colidx = ci;
+      part.vals = ctx->vals + z0;
+      part.lhs = ctx->lhs + r0;
+      part.rhs = ctx->rhs + r0;
+      part.isint = ctx->isint + c0;
+      part.colptr = NULL;  /* built below: the column view of the part */
+      {
+         int64_t* cp = calloc((size_t)part.n + 1, sizeof(int64_t));
+         int32_t* ri = malloc(sizeof(int32_t) * (size_t)(nz > 0 ? nz : 1));
+         double* cv = malloc(sizeof(double) * (size_t)(nz > 0 ? nz : 1));
+         int64_t* fill = malloc(sizeof(int64_t) * (size_t)(part.n > 0 ? part.n : 1));
+         int64_t p;
+         for( p = 0; p < nz; ++p )
+            cp[ci[p] + 1]++;
+         for( i = 0; i < part.n; ++i )
+            cp[i + 1] += cp[i];
+         for( i = 0; i < part.n; ++i )
+            fill[i] = cp[i];
+         for( i = 0; i < part.m; ++i )
+            for( p = rp[i]; p < rp[i + 1]; ++p )
+            {
+               int64_t q = fill[ci[p]]++;
+               ri[q] = (int32_t)i;
+               cv[q] = part.vals[p];
+            }
+         part.colptr = cp;
+         part.rowidx = ri;
+         part.cvals = cv;
+         memset(&r, 0, sizeof(r));
+         lpo_propagate(&part, &ctx->par, lb + c0, ub + c0, 0, NULL, NULL, NULL, NULL, NULL, &r);
+         free(fill); free(cp); free(ri); free(cv);
+      }
+      free(rp);
+      free(ci);
+      inst_cutoff[k] = (int8_t)(r.cutoff != 0);
+      ncut += inst_cutoff[k];
+      if( res != NULL && r.rounds > res->rounds )
+         res->rounds = r.rounds;
+   }
+   if( res != NULL )
+      res->cutoff = ncut;
+   return GBP_OK;
+}
+
