@@ -1131,6 +1131,79 @@ static int propagateRounds(Seq* q, int32_t* rounds)
    return q->nm > 0 ? 2 : 0;
 }
 
+/* The order in which SCIP created the transformed variables, i.e. their unique index (SCIPvarGetIndex): the host
+ * adds the columns in column order to a problem that keeps its variables grouped by type -- binaries, integers,
+ * continuous -- and makes room for a new variable by moving the first variable of each later group to that group's
+ * end (prob.c probInsertVar); an integral column with bounds in {0,1} is a binary variable; transforming the problem
+ * creates the transformed variables in that array's order (SCIPprobTransform).  pos[j] = column j's rank. */
+static void creationRank(const lpo_problem* P, const double* lb, const double* ub, int32_t* arr, int32_t* pos)
+{
+   int64_t nb = 0, ni = 0, nv = 0, j;
+   for( j = 0; j < P->n; ++j )
+   {
+      int64_t at = nv;
+      int bin = P->isint[j] != 0 && (lb[j] == 0.0 || lb[j] == 1.0) && (ub[j] == 0.0 || ub[j] == 1.0);
+      if( P->isint[j] != 0 )
+      {
+         if( at > nb + ni )
+         {
+            arr[at] = arr[nb + ni];
+            at = nb + ni;
+         }
+         if( bin && at > nb )
+         {
+            arr[at] = arr[nb];
+            at = nb;
+         }
+         if( bin )
+            ++nb;
+         else
+            ++ni;
+      }
+      arr[at] = (int32_t)j;
+      ++nv;
+   }
+   for( j = 0; j < P->n; ++j )
+      pos[arr[j]] = (int32_t)j;
+}
+
+/* Before solving SCIP sorts every row by consdataCompVar (cons_linear.c:3152-3187; consdataSort below
+ * SCIP_STAGE_INITSOLVE, :3355-3360): binaries first, then by type, ties by the variables' unique index -- together
+ * the creation rank.  Rows keep that order until tightenBounds sorts them for propagation (with sortvars). */
+static void indexSortRows(Seq* q, const double* lb, const double* ub)
+{
+   const lpo_problem* P = q->P;
+   int32_t* arr = malloc(sizeof(int32_t) * (size_t)(P->n + 1));
+   int32_t* pos = malloc(sizeof(int32_t) * (size_t)(P->n + 1));
+   int64_t i;
+   if( arr == NULL || pos == NULL )
+   {
+      free(arr);
+      free(pos);
+      return;
+   }
+   creationRank(P, lb, ub, arr, pos);
+   for( i = 0; i < P->m; ++i )
+   {
+      int32_t* a = q->ord + P->rowptr[i];
+      int64_t len = P->rowptr[i + 1] - P->rowptr[i];
+      int64_t k;
+      for( k = 1; k < len; ++k )  /* insertion sort: rows are short and the ranks distinct */
+      {
+         int32_t x = a[k];
+         int64_t t = k;
+         while( t > 0 && pos[P->colidx[a[t - 1]]] > pos[P->colidx[x]] )
+         {
+            a[t] = a[t - 1];
+            --t;
+         }
+         a[t] = x;
+      }
+   }
+   free(arr);
+   free(pos);
+}
+
 static int seqInit(Seq* q, const lpo_problem* P, const lpo_params* par, int root, int track)
 {
    int64_t m = P->m;
@@ -1206,6 +1279,7 @@ int lpo_propagate_seq_states(const lpo_problem* prob, const lpo_params* par, dou
    q.glb = lb;
    q.gub = ub;
    q.res = res;
+   indexSortRows(&q, lb, ub);
    /* every row is marked on activation, in the order the rows were added */
    for( i = 0; i < prob->m; ++i )
       hdlrMark(&q, (int32_t)i, rowSt(&q, (int32_t)i));

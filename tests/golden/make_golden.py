@@ -165,9 +165,9 @@ MIXED = {"mixed_small": (instances.mixed_small, range(5000, 5300)),
 def save_mixed(name):
     """300 small random MIPs of instances.mixed_small (seeds 5000..5299; coefficient magnitudes 1e-5..1e7 in one
     row, infinite bounds, equations) or instances.mixed_huge (seeds 7000..7299; contributions past hugeval too),
-    concatenated with offsets, with SCIP's root (bounds, row orders, deleted rows) for both rules and up to 8 nodes
-    per feasible instance (1..4 fixings, from SCIP's residual-rule root, every node from a newly transformed
-    problem), under tests/golden/fuzz/<name>.npz."""
+    concatenated with offsets, with SCIP's root (bounds, row orders, deleted rows) for both rules, with sortvars on
+    and off (tags res, easy, res_nosort, easy_nosort), and up to 8 nodes per feasible instance (1..4 fixings, from
+    SCIP's residual-rule root, every node from a newly transformed problem), under tests/golden/fuzz/<name>.npz."""
     make, MIXED_SEEDS = MIXED[name]
     insts = [make(np.random.default_rng(np.random.PCG64(s))) for s in MIXED_SEEDS]
     big, row_off, col_off = instances.concat_instances(insts)
@@ -176,14 +176,15 @@ def save_mixed(name):
            "seeds": np.array(list(MIXED_SEEDS), np.int64)}
     K = len(insts)
     nodes = []
+    tags = [(easy, sortvars) for sortvars in (True, False) for easy in (False, True)]
     for k, inst in enumerate(insts):
-        for easy in (False, True):
-            tag = "easy" if easy else "res"
-            rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy)
+        for easy, sortvars in tags:
+            tag = ("easy" if easy else "res") + ("" if sortvars else "_nosort")
+            rcut, rlb, rub, _ = oracle.run_scip(inst, easy=easy, sortvars=sortvars)
             if rcut:
                 order, rowdel = np.arange(inst.nnz, dtype=np.int32), np.zeros(inst.m, bool)
             else:
-                _, _, _, _, order, rowdel = oracle.run_scip(inst, easy=easy, order=True)
+                _, _, _, _, order, rowdel = oracle.run_scip(inst, easy=easy, order=True, sortvars=sortvars)
             out.setdefault(f"{tag}_rootcut", np.zeros(K, np.int8))[k] = rcut
             out.setdefault(f"{tag}_rootlb", np.empty(big.n))[col_off[k]:col_off[k + 1]] = rlb
             out.setdefault(f"{tag}_rootub", np.empty(big.n))[col_off[k]:col_off[k + 1]] = rub
@@ -200,8 +201,9 @@ def save_mixed(name):
                 nb = None
         res = {}
         if nb is not None:
-            for easy in (False, True):
-                _, _, _, res["easy" if easy else "res"] = oracle.run_scip(inst, nb, easy=easy, fresh=True)
+            for easy, sortvars in tags:
+                tag = ("easy" if easy else "res") + ("" if sortvars else "_nosort")
+                _, _, _, res[tag] = oracle.run_scip(inst, nb, easy=easy, fresh=True, sortvars=sortvars)
         nodes.append((nb, res))
     # nodes: node_inst[q] = the instance of node q; node columns and SCIP's changed columns are instance-local
     cnt = [0 if nb is None else nb.nnodes for nb, _ in nodes]
@@ -212,7 +214,7 @@ def save_mixed(name):
     out["node_col"] = np.concatenate([nb.col for nb in parts]).astype(np.int32)
     out["node_lb"] = np.concatenate([nb.lb for nb in parts])
     out["node_ub"] = np.concatenate([nb.ub for nb in parts])
-    for tag in ("res", "easy"):
+    for tag in ("res", "easy", "res_nosort", "easy_nosort"):
         allres = [r for nb, rr in nodes if nb is not None for r in rr[tag]]
         cut, ptr, col, lb, ub = node_arrays(allres)
         out[f"{tag}_ncut"], out[f"{tag}_nptr"], out[f"{tag}_ncol"] = cut, ptr, col

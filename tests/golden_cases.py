@@ -141,7 +141,7 @@ def load_mixed_small():
 
 def load_mixed(name):
     """golden/fuzz/<name>.npz split into its 300 instances: per instance a dict with the instance, its seed,
-    per rule ("res", "easy") SCIP's root (cut, lb, ub, order, rowdel) and its nodes' results (a list of
+    per rule and sortvars setting ("res", "easy", "res_nosort", "easy_nosort") SCIP's root (cut, lb, ub, order, rowdel) and its nodes' results (a list of
     (cutoff, cols, lb, ub) with instance-local columns that differ from that rule's root), and the nodes
     (instance-local NodeBatch, or None)."""
     with np.load(os.path.join(GOLDEN, "fuzz", f"{name}.npz")) as f:
@@ -164,7 +164,7 @@ def load_mixed(name):
             sl = slice(int(ptr[0]), int(ptr[-1]))
             nb = NodeBatch(ptr - ptr[0], z["node_col"][sl], z["node_lb"][sl], z["node_ub"][sl])
         d = {"inst": inst, "seed": int(z["seeds"][k]), "nodes": nb}
-        for tag in ("res", "easy"):
+        for tag in [t for t in ("res", "easy", "res_nosort", "easy_nosort") if f"{t}_rootcut" in z]:
             root = {"cut": bool(z[f"{tag}_rootcut"][k]), "lb": z[f"{tag}_rootlb"][c0:c1],
                     "ub": z[f"{tag}_rootub"][c0:c1], "order": z[f"{tag}_order"][p0:p1],
                     "rowdel": z[f"{tag}_rowdel"][r0:r1].astype(bool)}

@@ -23,7 +23,8 @@ from scip_gb300.instances import Instance, scip_var_index
 
 
 def _par(oracle_mod, tag):
-    return oracle_mod.params(0.0 if tag == "res" else 1e6)
+    """res / easy: the residual rule everywhere or SCIP's default rule choice; _nosort: sortvars off."""
+    return oracle_mod.params(0.0 if tag.startswith("res") else 1e6, sortvars=not tag.endswith("_nosort"))
 
 
 def _full(base_lb, base_ub, cols, lb, ub):
@@ -107,12 +108,17 @@ KNOWN_AFRESH = {("mixed_small", "res"): {(5056, 4)}, ("mixed_small", "easy"): {(
                 ("mixed_huge", "easy"): _HUGE_RES | {(7156, 1), (7156, 2), (7156, 6)}}
 
 
-@pytest.mark.parametrize("tag", ["res", "easy"])
+TAGS = ["res", "easy", "res_nosort", "easy_nosort"]
+
+
+@pytest.mark.parametrize("tag", TAGS)
 @pytest.mark.parametrize("name", ["mixed_small", "mixed_huge"])
 def test_mixed_roots_equal_scip(oracle_mod, name, tag):
     """300 small instances mixing coefficient magnitudes 1e-5..1e7 in one row, infinite bounds and equations
-    (mixed_small), and 300 more with contributions past hugeval (mixed_huge): the restatement's root equals SCIP's
-    bit for bit -- cutoff verdict, every bound, each row's final order and the rows deleted as redundant."""
+    (mixed_small), and 300 more with contributions past hugeval (mixed_huge), both rules, sortvars on and off: the
+    restatement's root equals SCIP's bit for bit -- cutoff verdict, every bound, each row's final order and the rows
+    deleted as redundant.  (With sortvars off the rows keep the order SCIP sorts them into before solving, by
+    variable type and creation: the restatement's first step.)"""
     par = _par(oracle_mod, tag)
     for c in _mixed(name):
         inst, root = c["inst"], c[tag]["root"]
@@ -128,7 +134,7 @@ def test_mixed_roots_equal_scip(oracle_mod, name, tag):
         assert np.array_equal(orc.states_deleted_rows(states), root["rowdel"]), inst.name
 
 
-@pytest.mark.parametrize("tag", ["res", "easy"])
+@pytest.mark.parametrize("tag", TAGS)
 @pytest.mark.parametrize("name", ["mixed_small", "mixed_huge"])
 def test_mixed_nodes_carried_and_afresh(oracle_mod, name, tag):
     par = _par(oracle_mod, tag)
@@ -151,4 +157,4 @@ def test_mixed_nodes_carried_and_afresh(oracle_mod, name, tag):
             if ag.cont_cols_out_of_tol:
                 outside.add((c["seed"], k))
     assert nodes > 1500
-    assert outside == KNOWN_AFRESH[(name, tag)]
+    assert outside == KNOWN_AFRESH[(name, tag.replace("_nosort", ""))]
