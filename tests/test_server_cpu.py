@@ -37,7 +37,10 @@ def lib(tmp_path_factory):
                         "-c", src, "-o", o], check=True, capture_output=True)
         objs.append(o)
     so = str(d / "libgbp_server_host.so")
-    subprocess.run(["g++", "-shared", "-o", so, *objs, "-lpthread"], check=True, capture_output=True)
+    # -Bsymbolic: the library's own stand-ins and test double, even where the process has loaded the CUDA runtime
+    # or libgbp itself
+    subprocess.run(["g++", "-shared", "-Wl,-Bsymbolic", "-o", so, *objs, "-lpthread"], check=True,
+                   capture_output=True)
     L = ctypes.CDLL(so)
     gbp.declare_server(L)
     L.gbp_default_params.argtypes = [ctypes.POINTER(gbp.GbpParams)]
