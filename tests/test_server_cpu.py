@@ -168,3 +168,31 @@ def test_shutdown_with_requests_outstanding(lib, oracle_mod):
     t.start()
     t.join(timeout=120)
     assert not t.is_alive()
+
+
+def test_node_requests_in_scip_order(lib, oracle_mod):
+    """A server created with GBP_FLAG_SCIPORDER answers node requests in SCIP's own order: rows uploaded in the order
+    SCIP sorts them into on the root bounds, every reply equal to the oracle's restatement of that order."""
+    inst, rlb, rub, nodes, _ = _setup(oracle_mod, m=1000, nnodes=60)
+    order = instances.scip_row_order(inst, rlb, rub, instances.scip_var_index(inst.isint, inst.lb, inst.ub))
+    ordered = instances.in_order(inst, order)
+    want = oracle_mod.Oracle(ordered).propagate_nodes(rlb, rub, nodes, oracle_mod.params(0.0), cap=inst.n, seq=True)
+    par = _params(lib)
+    par.flags |= gbp.GBP_FLAG_SCIPORDER
+    srv = gbp.Server(ordered, rlb, rub, params=par, workers=2, max_batch=16, lib=lib)
+    try:
+        tk = []
+        for k in range(nodes.nnodes):
+            sl = slice(nodes.ptr[k], nodes.ptr[k + 1])
+            tk.append(srv.submit(nodes.col[sl], nodes.lb[sl], nodes.ub[sl]))
+        for k, t in enumerate(tk):
+            cut, c, l, u, _, _ = srv.poll(t)
+            assert cut == bool(want["cutoff"][k]), f"node {k}"
+            if cut:
+                continue
+            n = want["n"][k]
+            o = np.argsort(want["col"][k, :n])
+            assert np.array_equal(c, want["col"][k, :n][o]), f"node {k}"
+            assert np.array_equal(l, want["lb"][k, :n][o]) and np.array_equal(u, want["ub"][k, :n][o]), f"node {k}"
+    finally:
+        srv.close()
