@@ -1167,6 +1167,7 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
    double* olb = NULL;
    double* oub = NULL;
    gbp_result res;
+   SCIP_Bool wasranged;
    int nchg;
    int rc;
    int j;
@@ -1188,10 +1189,13 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
       SCIP_CALL( upload(scip, pd) );
       if( pd->failed )
          return SCIP_OKAY;
-      if( pd->nspecialrows > 0 || wantRanged(scip) )
+      /* ranged-row propagation needs no refusal: a probing node keeps every row's rangedrowpropagated mark
+       * (cons_linear.c:17222-17224), and a row propagated at the base after its last change carries it, so SCIP's
+       * own probing of these nodes runs no ranged-row rule either */
+      if( pd->nspecialrows > 0 )
       {
-         SCIPwarningMessage(scip, "propagator <%s>: SCIP's order needs linear rows alone and no ranged-row "
-            "propagation; batched nodes not propagated\n", PROP_NAME);
+         SCIPwarningMessage(scip, "propagator <%s>: SCIP's order needs linear rows alone; batched nodes not "
+            "propagated\n", PROP_NAME);
          return SCIP_OKAY;
       }
       /* the device takes a row's leading binaries under the base (local) bounds; SCIP's are binary in the global
@@ -1253,13 +1257,20 @@ SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* node
       else
          col[k] = j;
    }
-   if( rc == GBP_OK && pd->sciporder && setDeviceParamsWith(scip, pd, GBP_FLAG_SCIPORDER) != SCIP_OKAY )
+   /* the nodes run as SCIP's probing runs them: without the ranged-row rule, since a probing node keeps every
+    * row's rangedrowpropagated mark (cons_linear.c:17222-17224) and a row propagated at the base after its last
+    * change carries it; in SCIP's order or in rounds */
+   wasranged = pd->ranged;
+   pd->ranged = FALSE;
+   if( rc == GBP_OK && (pd->sciporder || wasranged)
+      && setDeviceParamsWith(scip, pd, pd->sciporder ? GBP_FLAG_SCIPORDER : 0) != SCIP_OKAY )
       rc = GBP_ERR_CUDA;
    if( rc == GBP_OK )
       rc = gbp_propagate_nodes(pd->ctx, pd->lb, pd->ub, nnodes, ptr, col, lbs, ubs, ocut, orounds, ooff, on, ocol, olb,
          oub, outcap, &res);
-   /* the propagator's own calls run in rounds */
-   if( pd->sciporder && setDeviceParams(scip, pd) != SCIP_OKAY )
+   /* the propagator's own calls: rounds, and the ranged-row rule where it was on */
+   pd->ranged = wasranged;
+   if( (pd->sciporder || wasranged) && setDeviceParams(scip, pd) != SCIP_OKAY )
       disable(scip, pd, "restoring the device parameters failed", GBP_ERR_INVALID);
    if( rc == GBP_OK || rc == GBP_ERR_LIMIT )
    {

@@ -55,9 +55,12 @@ SCIP_Longint SCIPgetGpulinearRangedReasons(SCIP* scip);
  *  rows again in the order SCIP holds them and uploads them, and each node starts from the local bounds with no row
  *  marked, so that its cutoff verdict and integer bounds are the ones SCIP's own propagation of the node reaches
  *  (continuous bounds within 1e-9 relative or feastol absolute).  That mode needs a matrix of linear rows alone
- *  (no rows of setppc, logicor, knapsack or varbound constraints), ranged-row propagation off, and below the root
- *  no integer variable that is binary in its local domain only (the device takes a row's binaries under the local
- *  bounds, SCIP under the global ones); otherwise *success is FALSE. */
+ *  (no rows of setppc, logicor, knapsack or varbound constraints), and below the root no integer variable that is
+ *  binary in its local domain only (the device takes a row's binaries under the local bounds, SCIP under the global
+ *  ones); otherwise *success is FALSE.
+ *  In both modes the nodes run without the ranged-row rule, as SCIP's probing does: a probing node keeps every
+ *  row's rangedrowpropagated mark, so rows propagated at the base after their last change are not ranged-propagated
+ *  again. */
 SCIP_RETCODE SCIPpropagateGpulinearNodes(SCIP* scip, int nnodes, const int* nodebeg, SCIP_VAR** vars,
    const SCIP_Real* lbs, const SCIP_Real* ubs, int outcap, SCIP_Bool* cutoff, int* outbeg, SCIP_VAR** outvars,
    SCIP_Real* outlbs, SCIP_Real* outubs, SCIP_Bool* success);

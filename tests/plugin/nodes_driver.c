@@ -11,7 +11,9 @@
  * so that every node starts with no row marked, as that mode assumes.
  * With "easy" last, cons_linear and the plugin use SCIP's default rule choice (maxeasyactivitydelta 1e6) instead of
  * the residual rule everywhere (0).
- * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy] */
+ * With "ranged" after that, ranged-row propagation is on (constraints/linear/rangedrowpropagation, without
+ * artificial constraints) for SCIP and the plugin.
+ * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy|res] [ranged] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -24,6 +26,7 @@ static int nwant = 200;
 static int done = 0;
 static int sciporder = 0;
 static int easyrule = 0;
+static int ranged = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -233,6 +236,8 @@ int main(int argc, char** argv)
       sciporder = 1;
    if( argc > 4 && strcmp(argv[4], "easy") == 0 )
       easyrule = 1;
+   if( argc > 5 && strcmp(argv[5], "ranged") == 0 )
+      ranged = 1;
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
@@ -258,7 +263,8 @@ int main(int argc, char** argv)
          SCIPsetIntParam(scip, name, -1);
    }
    SCIPsetIntParam(scip, "presolving/maxrounds", 0);
-   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", FALSE);
+   SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", ranged ? TRUE : FALSE);
+   SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);
    SCIPsetRealParam(scip, "constraints/linear/maxeasyactivitydelta", easyrule ? 1e6 : 0.0);
    /* an infeasible probing node must not tighten the root's bounds for the nodes after it (conflict analysis of

@@ -235,6 +235,31 @@ def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_drive
         line[0] + "\n" + r.stderr[-1500:]
 
 
+@pytest.mark.parametrize("rule", ["res", "easy"])
+@pytest.mark.parametrize("seed", [5, 6, 7, 8])
+def test_batched_plugin_entry_with_ranged_rows(nodes_driver, tmp_path, seed, rule):
+    """Ranged-row propagation on, on rows whose integer part shares a divisor: SCIP's probing keeps every row's
+    rangedrowpropagated mark, so its nodes run no ranged-row rule, and neither does the batched entry.  In SCIP's
+    order the 200 nodes equal SCIP's probing (cutoff verdicts, integer bounds, continuous bounds within tolerance);
+    in rounds the cutoff verdicts do (the rounds reach other fixpoints on at most a few integer bounds)."""
+    from scip_gb300 import instances, mps
+    inst = instances.gcd_rows(np.random.default_rng(seed), 300, 900, equations=True, continuous=False)
+    path = str(tmp_path / f"gcd{seed}.mps")
+    mps.write_mps(inst, path, obj=np.random.default_rng(seed + 100).integers(-5, 6, inst.n))
+    for mode in ("sciporder", "rounds"):
+        r = subprocess.run([nodes_driver, path, "200", mode, rule, "ranged"], capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")][0]
+        f = line.split()
+        got = {f[i]: f[i + 1] for i in range(len(f) - 1) if not f[i].lstrip("-").isdigit()}
+        assert got["success"] == "1" and got["cutoffmismatch"] == "0", line
+        if mode == "sciporder":
+            assert got["intmismatch"] == "0" and got["contmismatch"] == "0", line + "\n" + r.stderr[-1500:]
+        else:
+            assert int(got["intmismatch"]) <= 2, line
+
+
 def test_constraint_with_a_fixed_variable_added_while_solving(tmp_path, oracle_mod):
     """SCIP's own scenario tests/src/cons/linear/fixedvar.c with the propagator in place: after bell5's root a
     variable fixed to 0 and a linear constraint over it and five more variables are added, and the search continues
