@@ -13,7 +13,9 @@
  * the residual rule everywhere (0).
  * With "ranged" after that, ranged-row propagation is on (constraints/linear/rangedrowpropagation, without
  * artificial constraints) for SCIP and the plugin.
- * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy|res] [ranged] */
+ * With a depth last, the check runs at the first search node of that depth instead of the root: the nodes' base
+ * is that node's local bounds, below SCIP's global ones.
+ * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy|res] [ranged|plain] [depth] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -27,6 +29,7 @@ static int done = 0;
 static int sciporder = 0;
 static int easyrule = 0;
 static int ranged = 0;
+static int atdepth = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -60,7 +63,7 @@ static SCIP_DECL_HEUREXEC(heurExecCheck)
    (void)nodeinfeasible;
    (void)heurtiming;
    *result = SCIP_DIDNOTRUN;
-   if( done )
+   if( done || SCIPgetDepth(scip) < atdepth )
       return SCIP_OKAY;
    done = 1;
    SCIP_CALL( SCIPallocBufferArray(scip, &cand, nvars) );
@@ -238,6 +241,8 @@ int main(int argc, char** argv)
       easyrule = 1;
    if( argc > 5 && strcmp(argv[5], "ranged") == 0 )
       ranged = 1;
+   if( argc > 6 )
+      atdepth = atoi(argv[6]);
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
