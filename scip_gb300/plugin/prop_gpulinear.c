@@ -1089,8 +1089,7 @@ SCIP_RETCODE SCIPincludePropGpulinear(SCIP* scip)
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/sciporder",
          "SCIPpropagateGpulinearNodes propagates its nodes in SCIP's own order (one marked row at a time, every "
          "tightening applied at once) instead of rounds, with the rows re-read in the order SCIP holds them; only "
-         "for matrices of linear rows alone and without ranged-row propagation", &pd->sciporder, FALSE, FALSE, NULL,
-         NULL) );
+         "for matrices of linear rows alone", &pd->sciporder, FALSE, FALSE, NULL, NULL) );
    SCIP_CALL( SCIPaddBoolParam(scip, "propagating/" PROP_NAME "/replacespecialised",
          "switch off the propagation of setppc, logicor, knapsack and varbound (constraints/<handler>/propfreq = -1)",
          &pd->replacespecialised, FALSE, FALSE, paramChgdReplacespecialised, NULL) );
