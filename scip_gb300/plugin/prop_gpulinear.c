@@ -269,6 +269,99 @@ static SCIP_RETCODE creationOrder(SCIP* scip, SCIP_CONS** conss, int nc, SCIP_CO
    return SCIP_OKAY;
 }
 
+/** a variable's type as SCIP's row orders see it: implied integers between integers and continuous variables */
+static int typeRank(SCIP_VAR* v)
+{
+   return SCIPvarIsImpliedIntegral(v) ? (int)SCIP_DEPRECATED_VARTYPE_IMPLINT : (int)SCIPvarGetType(v);
+}
+
+/** whether a comes before b in the order SCIP gives a row's variables before solving (consdataCompVar,
+ *  cons_linear.c:3152-3187): binaries first, then by type, ties by the variables' unique index */
+static SCIP_Bool indexBefore(SCIP_VAR* a, SCIP_VAR* b)
+{
+   if( SCIPvarIsBinary(a) != SCIPvarIsBinary(b) )
+      return SCIPvarIsBinary(a);
+   if( !SCIPvarIsBinary(a) && typeRank(a) != typeRank(b) )
+      return typeRank(a) < typeRank(b);
+   return SCIPvarCompare(a, b) < 0;
+}
+
+/** whether (a, va) comes before (b, vb) in the order tightenBounds sorts a row into (consdataCompVarProp,
+ *  cons_linear.c:3191-3254): binaries first by decreasing |coefficient|, then by type, integers by decreasing
+ *  |coefficient| * (global domain width), ties by problem index */
+static SCIP_Bool propBefore(SCIP_VAR* a, SCIP_Real va, SCIP_VAR* b, SCIP_Real vb)
+{
+   SCIP_Real ka;
+   SCIP_Real kb;
+   if( SCIPvarIsBinary(a) != SCIPvarIsBinary(b) )
+      return SCIPvarIsBinary(a);
+   if( SCIPvarIsBinary(a) )
+   {
+      ka = REALABS(va);
+      kb = REALABS(vb);
+   }
+   else
+   {
+      if( typeRank(a) != typeRank(b) )
+         return typeRank(a) < typeRank(b);
+      if( !SCIPvarIsIntegral(a) )
+         return SCIPvarGetProbindex(a) < SCIPvarGetProbindex(b);
+      ka = REALABS(va * (SCIPvarGetUbGlobal(a) - SCIPvarGetLbGlobal(a)));
+      kb = REALABS(vb * (SCIPvarGetUbGlobal(b) - SCIPvarGetLbGlobal(b)));
+   }
+   if( EPSGT(ka, kb, 1e-9) )
+      return TRUE;
+   if( EPSGT(kb, ka, 1e-9) )
+      return FALSE;
+   return SCIPvarGetProbindex(a) < SCIPvarGetProbindex(b);
+}
+
+/** the order SCIP's propagation of a node visits a linear row in.  tightenBounds sorts a row the first time it
+ *  visits it during solving (cons_linear.c:7041-7046); until then SCIP holds it in the order of presolving, by
+ *  index.  A row whose variables are in that index order is therefore sorted here as tightenBounds will sort it;
+ *  a row in any other order has been sorted already and keeps it. */
+static SCIP_RETCODE propagationOrder(SCIP* scip, SCIP_VAR** vars, SCIP_Real* vals, int n)
+{
+   SCIP_VAR** tv;
+   SCIP_Real* tc;
+   int w;
+   int k;
+   for( k = 0; k + 1 < n; ++k )
+      if( indexBefore(vars[k + 1], vars[k]) )
+         return SCIP_OKAY;
+   SCIP_CALL( SCIPallocBufferArray(scip, &tv, MAX(n, 1)) );
+   SCIP_CALL( SCIPallocBufferArray(scip, &tc, MAX(n, 1)) );
+   for( w = 1; w < n; w *= 2 )  /* bottom-up merge sort */
+   {
+      for( k = 0; k < n; k += 2 * w )
+      {
+         int m = MIN(k + w, n);
+         int e = MIN(k + 2 * w, n);
+         int x = k;
+         int y = m;
+         int t = k;
+         while( t < e )
+         {
+            if( y >= e || (x < m && !propBefore(vars[y], vals[y], vars[x], vals[x])) )
+            {
+               tv[t] = vars[x];
+               tc[t++] = vals[x++];
+            }
+            else
+            {
+               tv[t] = vars[y];
+               tc[t++] = vals[y++];
+            }
+         }
+      }
+      memcpy(vars, tv, sizeof(SCIP_VAR*) * (size_t)n);
+      memcpy(vals, tc, sizeof(SCIP_Real) * (size_t)n);
+   }
+   SCIPfreeBufferArray(scip, &tc);
+   SCIPfreeBufferArray(scip, &tv);
+   return SCIP_OKAY;
+}
+
 /** copies the rows of the handlers into CSR form over the active variables (columns = SCIPvarGetProbindex): fixed,
  *  aggregated, multi-aggregated and negated variables are replaced by their active variables
  *  (SCIPgetProbvarLinearSum), constants move into the sides; modifiable constraints are left to their handler */
@@ -283,9 +376,12 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
    SCIP_VAR** bv;
    SCIP_Real* bc;
    int64_t* where;   /* position of a column's entry in the row being built (< the row's start: none) */
+   SCIP_Bool sortvars = TRUE;
    int h;
    int j;
 
+   if( SCIPgetBoolParam(scip, "constraints/linear/sortvars", &sortvars) != SCIP_OKAY )
+      sortvars = TRUE;
    freeMatrix(scip, pd);
    pd->ncols = nvars;
    pd->nconss = countConss(scip, pd);
@@ -376,6 +472,8 @@ static SCIP_RETCODE buildMatrix(SCIP* scip, SCIP_PROPDATA* pd)
             SCIP_CALL( SCIPreallocBufferArray(scip, &bc, bufsize) );
             SCIP_CALL( consRow(scip, h, cons, bv, bc, bufsize, &n, &l, &r) );
          }
+         if( pd->sciporder && h == 0 && sortvars )
+            SCIP_CALL( propagationOrder(scip, bv, bc, n) );
          SCIP_CALL( SCIPgetProbvarLinearSum(scip, bv, bc, &n, bufsize, &constant, &need) );
          if( need > bufsize )
          {

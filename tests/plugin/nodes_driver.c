@@ -15,7 +15,8 @@
  * artificial constraints) for SCIP and the plugin.
  * With a depth last, the check runs at the first search node of that depth instead of the root: the nodes' base
  * is that node's local bounds, below SCIP's global ones.
- * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy|res] [ranged|plain] [depth] */
+ * With "presolve" after the depth, SCIP presolves first (its rows stay linear: every upgrade is off).
+ * Usage: nodes_driver <instance.mps> [nodes] [sciporder|rounds] [easy|res] [ranged|plain] [depth] [presolve] */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -30,6 +31,7 @@ static int sciporder = 0;
 static int easyrule = 0;
 static int ranged = 0;
 static int atdepth = 0;
+static int presolve = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -243,6 +245,8 @@ int main(int argc, char** argv)
       ranged = 1;
    if( argc > 6 )
       atdepth = atoi(argv[6]);
+   if( argc > 7 && strcmp(argv[7], "presolve") == 0 )
+      presolve = 1;
    if( SCIPcreate(&scip) != SCIP_OKAY || SCIPincludeDefaultPlugins(scip) != SCIP_OKAY )
       return 1;
    if( SCIPincludePropGpulinear(scip) != SCIP_OKAY )
@@ -267,7 +271,9 @@ int main(int argc, char** argv)
          && strcmp(name, "propagating/gpulinear/freq") != 0 )
          SCIPsetIntParam(scip, name, -1);
    }
-   SCIPsetIntParam(scip, "presolving/maxrounds", 0);
+   /* with "presolve": SCIP's presolving runs (aggregations, fixings, negated variables in rows), the rows stay
+    * linear (no upgrade) */
+   SCIPsetIntParam(scip, "presolving/maxrounds", presolve ? -1 : 0);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", ranged ? TRUE : FALSE);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);

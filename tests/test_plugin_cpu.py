@@ -238,6 +238,27 @@ def test_batched_plugin_entry_in_scip_order_agrees_with_scip_probing(nodes_drive
 @pytest.mark.parametrize("rule", ["res", "easy"])
 @pytest.mark.parametrize("name", ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03",
                                   "p0548", "rgn"])
+def test_batched_plugin_entry_in_scip_order_after_presolving(nodes_driver, oracle_mod, name, rule):
+    """SCIP presolves first (its rows stay linear).  Presolving leaves rows in index order with their tightening
+    already done, so SCIP's root does not sort them; the first visit in a node does.  The batched entry uploads such
+    rows in the order that visit gives them, and its 200 nodes in SCIP's order equal SCIP's probing."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    r = subprocess.run([nodes_driver, path, "200", "sciporder", rule, "plain", "0", "presolve"], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")][0]
+    f = line.split()
+    got = {f[i]: f[i + 1] for i in range(len(f) - 1) if not f[i].lstrip("-").isdigit()}
+    assert got["success"] == "1", r.stderr[-2000:]
+    assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0" and got["contmismatch"] == "0", \
+        line + "\n" + r.stderr[-1500:]
+
+
+@pytest.mark.parametrize("rule", ["res", "easy"])
+@pytest.mark.parametrize("name", ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03",
+                                  "p0548", "rgn"])
 def test_batched_plugin_entry_below_the_root(nodes_driver, oracle_mod, name, rule):
     """The batched entry at the first search node of depth 3: the nodes' base is that node's local bounds, tighter
     than SCIP's global ones (the binary test reads the global domain).  In SCIP's order the 200 nodes equal SCIP's
