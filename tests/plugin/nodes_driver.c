@@ -11,8 +11,9 @@
  * so that every node starts with no row marked, as that mode assumes.
  * With "easy" last, cons_linear and the plugin use SCIP's default rule choice (maxeasyactivitydelta 1e6) instead of
  * the residual rule everywhere (0).
- * With "ranged" after that, ranged-row propagation is on (constraints/linear/rangedrowpropagation, without
- * artificial constraints) for SCIP and the plugin.
+ * The fifth argument lists options: "ranged" turns ranged-row propagation on (constraints/linear/
+ * rangedrowpropagation, without artificial constraints) for SCIP and the plugin, "nosort" sets
+ * constraints/linear/sortvars to FALSE ("plain": neither).
  * With a depth last, the check runs at the first search node of that depth instead of the root: the nodes' base
  * is that node's local bounds, below SCIP's global ones.
  * With "presolve" after the depth, SCIP presolves first (its rows stay linear: every upgrade is off).
@@ -32,6 +33,7 @@ static int easyrule = 0;
 static int ranged = 0;
 static int atdepth = 0;
 static int presolve = 0;
+static int nosort = 0;
 
 static unsigned long long lcg = 0x2545f4914f6cdd1dull;
 static unsigned long long nextRand(void)
@@ -241,8 +243,10 @@ int main(int argc, char** argv)
       sciporder = 1;
    if( argc > 4 && strcmp(argv[4], "easy") == 0 )
       easyrule = 1;
-   if( argc > 5 && strcmp(argv[5], "ranged") == 0 )
+   if( argc > 5 && strstr(argv[5], "ranged") != NULL )
       ranged = 1;
+   if( argc > 5 && strstr(argv[5], "nosort") != NULL )
+      nosort = 1;
    if( argc > 6 )
       atdepth = atoi(argv[6]);
    if( argc > 7 && strcmp(argv[7], "presolve") == 0 )
@@ -275,6 +279,7 @@ int main(int argc, char** argv)
     * linear (no upgrade) */
    SCIPsetIntParam(scip, "presolving/maxrounds", presolve ? -1 : 0);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowpropagation", ranged ? TRUE : FALSE);
+   SCIPsetBoolParam(scip, "constraints/linear/sortvars", nosort ? FALSE : TRUE);
    SCIPsetBoolParam(scip, "constraints/linear/rangedrowartcons", FALSE);
    SCIPsetIntParam(scip, "lp/solvefreq", -1);
    SCIPsetRealParam(scip, "constraints/linear/maxeasyactivitydelta", easyrule ? 1e6 : 0.0);

@@ -256,6 +256,26 @@ def test_batched_plugin_entry_in_scip_order_after_presolving(nodes_driver, oracl
         line + "\n" + r.stderr[-1500:]
 
 
+@pytest.mark.parametrize("presolve", ["0", "presolve"])
+@pytest.mark.parametrize("name", ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03",
+                                  "p0548", "rgn"])
+def test_batched_plugin_entry_in_scip_order_without_sortvars(nodes_driver, oracle_mod, name, presolve):
+    """constraints/linear/sortvars = FALSE: SCIP visits every row in the order presolving left it, and so does the
+    batched entry; its 200 nodes in SCIP's order equal SCIP's probing, with and without presolving."""
+    path = os.path.join(oracle_mod.REFDIR, "check", "instances", "MIP", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.mps not shipped")
+    r = subprocess.run([nodes_driver, path, "200", "sciporder", "res", "nosort", "0", presolve], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("nodes ")][0]
+    f = line.split()
+    got = {f[i]: f[i + 1] for i in range(len(f) - 1) if not f[i].lstrip("-").isdigit()}
+    assert got["success"] == "1", r.stderr[-2000:]
+    assert got["cutoffmismatch"] == "0" and got["intmismatch"] == "0" and got["contmismatch"] == "0", \
+        line + "\n" + r.stderr[-1500:]
+
+
 @pytest.mark.parametrize("rule", ["res", "easy"])
 @pytest.mark.parametrize("name", ["bell5", "blend2", "dcmulti", "egout", "enigma", "flugpl", "gt2", "lseu", "misc03",
                                   "p0548", "rgn"])
